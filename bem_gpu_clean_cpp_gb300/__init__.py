@@ -1,0 +1,466 @@
+"""GB300-native Helmholtz BEM engine -- Python host side over the C ABI.
+
+Every call goes through ``libbem_gb300.so`` (``include/bem_gb300.h``) with
+ctypes.  There is no Python or CPU fallback: if the library is missing the
+import of any compute call raises.  Names mirror the reference's C++ call
+surface (ZiqiFrancisFan/BEM_GPU_Clean_CPP):
+
+==========================  ==============================================
+reference                   here
+==========================  ==============================================
+mesh::readObj (mesh.cu:1215)         ``Mesh.readObj`` / ``Mesh.read_obj``
+mesh::findBB (mesh.cu:1369)          ``Mesh.findBB``
+mesh::genCHIEF (mesh.cu:1430)        ``Mesh.genCHIEF``
+gaussQuad + sendToDevice             ``gaussQuad(order).sendToDevice()``
+bemSystem (mesh.cu:985)              ``bemSystem``
+qrSolver (numerical.cu:580)          ``qrSolver``
+GMRES (GMRES.cu:145)                 ``GMRES``
+genExtPressure (mesh.cu:1038)        ``genExtPressure``
+wrtCplxMat (numerical.cu:556)        ``wrtCplxMat``
+==========================  ==============================================
+
+``Solver`` exposes the device-resident engine (assembly, QR and refined
+GMRES solves, batched field evaluation) that the drop-in calls sit on.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libbem_gb300.so")
+
+SUCCESS = 0
+PREC_C64, PREC_C128 = 0, 1
+SOLVE_QR, SOLVE_GMRES_REFINED = 0, 1
+SRC_POINT, SRC_PLANE = 0, 1
+ERR_NOT_CONVERGED = 5
+
+_lock = threading.Lock()
+_lib = None
+
+
+class BemError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"[{status}] {msg}")
+        self.status = status
+
+
+class Source(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("vec", ctypes.c_double * 3),
+                ("amp_re", ctypes.c_double), ("amp_im", ctypes.c_double)]
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("density", ctypes.c_double), ("speed", ctypes.c_double), ("order", ctypes.c_int),
+                ("near_eta", ctypes.c_double), ("near_depth", ctypes.c_int), ("tol", ctypes.c_double),
+                ("max_iter", ctypes.c_int), ("inner_tol", ctypes.c_double),
+                ("max_refine", ctypes.c_int), ("tile_cols", ctypes.c_int)]
+
+
+class SolveInfo(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int), ("refinements", ctypes.c_int),
+                ("rel_residual", ctypes.c_double), ("converged", ctypes.c_int)]
+
+
+# Exported symbols and their signatures (the C ABI of include/bem_gb300.h).
+_VP = ctypes.c_void_p
+_I = ctypes.c_int
+_D = ctypes.c_double
+_F = ctypes.c_float
+_S = ctypes.c_char_p
+SIGNATURES = {
+    "bem_status_string": (_S, [_I]),
+    "bem_last_error": (_S, []),
+    "bem_version": (_I, []),
+    "bem_launch_count": (ctypes.c_longlong, []),
+    "bem_gauss_legendre": (_I, [_I, _VP, _VP]),
+    "bem_set_quadrature": (_I, [_I]),
+    "bem_get_quadrature": (_I, []),
+    "bem_set_medium": (_I, [_D, _D]),
+    "bem_set_point_source_strength": (_I, [_D]),
+    "bem_mesh_create": (_I, [ctypes.POINTER(_VP)]),
+    "bem_mesh_destroy": (_I, [_VP]),
+    "bem_mesh_read_obj": (_I, [_VP, _S]),
+    "bem_mesh_read_obj_robust": (_I, [_VP, _S]),
+    "bem_mesh_set": (_I, [_VP, _VP, _I, _VP, _I]),
+    "bem_mesh_set_bc": (_I, [_VP, _VP]),
+    "bem_mesh_set_uniform_bc": (_I, [_VP, _D, _D, _D, _D, _D, _D]),
+    "bem_mesh_find_bb": (_I, [_VP, _F]),
+    "bem_mesh_get_bb": (_I, [_VP, _VP]),
+    "bem_mesh_gen_chief": (_I, [_VP, _I, _F]),
+    "bem_mesh_set_chief": (_I, [_VP, _VP, _I]),
+    "bem_mesh_get_counts": (_I, [_VP, _VP, _VP, _VP]),
+    "bem_mesh_get_points": (_I, [_VP, _VP]),
+    "bem_mesh_get_elems": (_I, [_VP, _VP]),
+    "bem_mesh_get_chief": (_I, [_VP, _VP]),
+    "bem_mesh_icosphere": (_I, [_VP, _I, _D]),
+    "bem_mesh_surface_area": (_I, [_VP, _VP]),
+    "bem_system_c64": (_I, [_VP, _F, _VP, _I, _VP, _I, _VP, _I]),
+    "bem_qr_solve_c64": (_I, [_VP, _I, _I, _I, _VP, _I, _I]),
+    "bem_gmres_c64": (_I, [_VP, _VP, _I, _I, _F, _VP]),
+    "bem_ext_pressure_c64": (_I, [_F, _VP, _VP, _VP, _VP, _VP]),
+    "bem_write_cplx_mat_c64": (_I, [_VP, _I, _I, _I, _S]),
+    "bem_options_default": (_I, [_VP]),
+    "bem_solver_create": (_I, [ctypes.POINTER(_VP)]),
+    "bem_solver_destroy": (_I, [_VP]),
+    "bem_solver_set_options": (_I, [_VP, _VP]),
+    "bem_solver_get_options": (_I, [_VP, _VP]),
+    "bem_solver_set_mesh": (_I, [_VP, _VP]),
+    "bem_solver_set_geometry": (_I, [_VP, _VP, _I, _VP, _I, _VP, _VP, _I]),
+    "bem_solver_set_sources": (_I, [_VP, _VP, _I]),
+    "bem_solver_assemble": (_I, [_VP, _D, _I]),
+    "bem_solver_solve": (_I, [_VP, _I, _VP]),
+    "bem_solver_get_solution": (_I, [_VP, _VP, _I, _I]),
+    "bem_solver_get_system": (_I, [_VP, _VP, _I, _VP, _I, _I]),
+    "bem_solver_eval_field": (_I, [_VP, _VP, _I, _VP, _I, _I]),
+    "bem_solver_sync": (_I, [_VP]),
+    "bem_solver_stream": (_VP, [_VP]),
+    "bem_solver_sizes": (_I, [_VP, _VP, _VP, _VP, _VP]),
+}
+
+
+def lib():
+    """Load libbem_gb300.so; raise when it has not been built."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise BemError(1, f"{LIB_PATH} is missing: build it with "
+                                  "`python -c 'import __graft_entry__ as g; g.build()'`")
+            L = ctypes.CDLL(LIB_PATH)
+            for name, (res, args) in SIGNATURES.items():
+                fn = getattr(L, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = L
+    return _lib
+
+
+def _check(status: int) -> None:
+    if status != SUCCESS:
+        msg = lib().bem_last_error().decode(errors="replace")
+        raise BemError(status, msg or lib().bem_status_string(status).decode())
+
+
+def _ptr(a: np.ndarray):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def launch_count() -> int:
+    return int(lib().bem_launch_count())
+
+
+def sources(srcs) -> ctypes.Array:
+    """srcs: iterable of (kind, (x, y, z), amplitude) with kind 'point' or 'plane'."""
+    srcs = list(srcs)
+    arr = (Source * len(srcs))()
+    for i, (kind, vec, amp) in enumerate(srcs):
+        arr[i].kind = SRC_PLANE if kind == "plane" else SRC_POINT
+        for d in range(3):
+            arr[i].vec[d] = float(vec[d])
+        amp = complex(amp)
+        arr[i].amp_re, arr[i].amp_im = amp.real, amp.imag
+    return arr
+
+
+# ---------------------------------------------------------------------------
+# Quadrature (gaussQuad, numerical.h:166-187)
+# ---------------------------------------------------------------------------
+def gauss_legendre(order: int):
+    x = np.zeros(order)
+    w = np.zeros(order)
+    _check(lib().bem_gauss_legendre(order, _ptr(x), _ptr(w)))
+    return x, w
+
+
+class gaussQuad:
+    """gaussQuad(order).sendToDevice(): sets the Gauss order used by the
+    drop-in calls and new solvers (numerical.cu:152-156, 227-231)."""
+
+    def __init__(self, order: int = 6):
+        self.n = int(order)
+        self.evalPnts, self.wgts = gauss_legendre(self.n)
+
+    def sendToDevice(self) -> int:
+        _check(lib().bem_set_quadrature(self.n))
+        return SUCCESS
+
+
+def set_medium(density: float, speed: float) -> None:
+    _check(lib().bem_set_medium(float(density), float(speed)))
+
+
+def set_point_source_strength(q: float) -> None:
+    """The reference's STRENGTH macro (numerical.h:128-130), 0 by default."""
+    _check(lib().bem_set_point_source_strength(float(q)))
+
+
+# ---------------------------------------------------------------------------
+# Mesh (class mesh, mesh.h:216-259)
+# ---------------------------------------------------------------------------
+class Mesh:
+    def __init__(self):
+        h = ctypes.c_void_p()
+        _check(lib().bem_mesh_create(ctypes.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.bem_mesh_destroy(h)
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    # reference names
+    def readObj(self, path: str) -> int:
+        _check(lib().bem_mesh_read_obj(self._h, os.fsencode(path)))
+        return SUCCESS
+
+    def findBB(self, threshold: float) -> int:
+        _check(lib().bem_mesh_find_bb(self._h, float(threshold)))
+        return SUCCESS
+
+    def genCHIEF(self, num: int, threshold: float) -> int:
+        _check(lib().bem_mesh_gen_chief(self._h, int(num), float(threshold)))
+        return SUCCESS
+
+    def getNumPnts(self) -> int:
+        return self.counts()[0]
+
+    def getNumElems(self) -> int:
+        return self.counts()[1]
+
+    def getNumChief(self) -> int:
+        return self.counts()[2]
+
+    # extensions
+    read_obj = readObj
+
+    def read_obj_robust(self, path: str) -> None:
+        _check(lib().bem_mesh_read_obj_robust(self._h, os.fsencode(path)))
+
+    def set(self, pnts, elems) -> None:
+        p = np.ascontiguousarray(pnts, dtype=np.float64).reshape(-1, 3)
+        e = np.ascontiguousarray(elems, dtype=np.int32).reshape(-1, 3)
+        _check(lib().bem_mesh_set(self._h, _ptr(p), p.shape[0], _ptr(e), e.shape[0]))
+
+    def set_bc(self, bc) -> None:
+        """bc: (E, 3) complex array of (ca, cb, cc)."""
+        b = np.ascontiguousarray(np.asarray(bc, dtype=np.complex128).reshape(-1, 3))
+        _check(lib().bem_mesh_set_bc(self._h, _ptr(b)))
+
+    def set_uniform_bc(self, ca, cb, cc) -> None:
+        ca, cb, cc = complex(ca), complex(cb), complex(cc)
+        _check(lib().bem_mesh_set_uniform_bc(self._h, ca.real, ca.imag, cb.real, cb.imag, cc.real, cc.imag))
+
+    def set_chief(self, pts) -> None:
+        p = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, 3)
+        _check(lib().bem_mesh_set_chief(self._h, _ptr(p) if p.size else None, p.shape[0]))
+
+    def counts(self):
+        n, e, m = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _check(lib().bem_mesh_get_counts(self._h, ctypes.byref(n), ctypes.byref(e), ctypes.byref(m)))
+        return n.value, e.value, m.value
+
+    def points(self) -> np.ndarray:
+        n = self.counts()[0]
+        p = np.zeros((n, 3))
+        _check(lib().bem_mesh_get_points(self._h, _ptr(p)))
+        return p
+
+    def elems(self) -> np.ndarray:
+        e = np.zeros((self.counts()[1], 3), dtype=np.int32)
+        _check(lib().bem_mesh_get_elems(self._h, _ptr(e)))
+        return e
+
+    def chief(self) -> np.ndarray:
+        m = self.counts()[2]
+        c = np.zeros((m, 3))
+        if m:
+            _check(lib().bem_mesh_get_chief(self._h, _ptr(c)))
+        return c
+
+    def bb(self) -> np.ndarray:
+        b = np.zeros(6, dtype=np.float32)
+        _check(lib().bem_mesh_get_bb(self._h, _ptr(b)))
+        return b
+
+    def surface_area(self) -> float:
+        a = ctypes.c_double()
+        _check(lib().bem_mesh_surface_area(self._h, ctypes.byref(a)))
+        return a.value
+
+    @classmethod
+    def icosphere(cls, subdiv: int, radius: float = 1.0) -> "Mesh":
+        m = cls()
+        _check(lib().bem_mesh_icosphere(m._h, int(subdiv), float(radius)))
+        return m
+
+    @classmethod
+    def from_arrays(cls, pnts, elems) -> "Mesh":
+        m = cls()
+        m.set(pnts, elems)
+        return m
+
+
+# ---------------------------------------------------------------------------
+# Drop-in calls with host buffers
+# ---------------------------------------------------------------------------
+def bemSystem(m: Mesh, k: float, srcs, A: np.ndarray | None = None, B: np.ndarray | None = None):
+    """bemSystem (mesh.cu:985-1006): returns (A, B) as complex64 Fortran
+    arrays of shapes (N+M, N) and (N+M, numSrcs); srcs are point-source
+    positions (numSrcs x 3) of strength STRENGTH."""
+    n, _, mc = m.counts()
+    s = np.ascontiguousarray(srcs, dtype=np.float32).reshape(-1, 3)
+    R = n + mc
+    if A is None:
+        A = np.zeros((R, n), dtype=np.complex64, order="F")
+    if B is None:
+        B = np.zeros((R, s.shape[0]), dtype=np.complex64, order="F")
+    _check(lib().bem_system_c64(m.handle, float(k), _ptr(s), s.shape[0], _ptr(A), A.shape[0], _ptr(B), B.shape[0]))
+    return A, B
+
+
+def qrSolver(A: np.ndarray, B: np.ndarray) -> np.ndarray:
+    """qrSolver (numerical.cu:580-644): least squares; B (complex64,
+    Fortran) is overwritten and returned, solution in rows 0..n-1."""
+    A = np.asfortranarray(A, dtype=np.complex64)
+    if B.dtype != np.complex64 or not B.flags.f_contiguous:
+        raise ValueError("B must be a complex64 Fortran-ordered array")
+    m, n = A.shape
+    nb = B.shape[1] if B.ndim == 2 else 1
+    _check(lib().bem_qr_solve_c64(_ptr(A), m, n, m, _ptr(B), nb, B.shape[0]))
+    return B
+
+
+def GMRES(A: np.ndarray, b: np.ndarray, maxIter: int, thr: float, x: np.ndarray | None = None) -> np.ndarray:
+    """GMRES (GMRES.cu:145-279) on a square complex64 system; x is the
+    initial guess (zeros by default) and is overwritten."""
+    A = np.asfortranarray(A, dtype=np.complex64)
+    m = A.shape[0]
+    b = np.ascontiguousarray(b, dtype=np.complex64).reshape(m)
+    if x is None:
+        x = np.zeros(m, dtype=np.complex64)
+    _check(lib().bem_gmres_c64(_ptr(A), _ptr(b), m, int(maxIter), float(thr), _ptr(x)))
+    return x
+
+
+def genExtPressure(k: float, m: Mesh, src, x, surfP) -> complex:
+    """genExtPressure (mesh.cu:1038-1073): pressure at x from the surface
+    pressure surfP (complex64, numPnts)."""
+    s = np.ascontiguousarray(src, dtype=np.float32).reshape(3)
+    xx = np.ascontiguousarray(x, dtype=np.float32).reshape(3)
+    u = np.ascontiguousarray(surfP, dtype=np.complex64).reshape(-1)
+    out = np.zeros(1, dtype=np.complex64)
+    _check(lib().bem_ext_pressure_c64(float(k), m.handle, _ptr(s), _ptr(xx), _ptr(u), _ptr(out)))
+    return complex(out[0])
+
+
+def wrtCplxMat(mat: np.ndarray, path: str) -> int:
+    """wrtCplxMat (numerical.cu:556-578): '(%f,%f) ' per entry, one line per row."""
+    a = np.asfortranarray(np.atleast_2d(mat), dtype=np.complex64)
+    _check(lib().bem_write_cplx_mat_c64(_ptr(a), a.shape[0], a.shape[1], a.shape[0], os.fsencode(path)))
+    return SUCCESS
+
+
+# ---------------------------------------------------------------------------
+# Device-resident solver
+# ---------------------------------------------------------------------------
+class Solver:
+    def __init__(self, **opts):
+        h = ctypes.c_void_p()
+        _check(lib().bem_solver_create(ctypes.byref(h)))
+        self._h = h
+        if opts:
+            self.set_options(**opts)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.bem_solver_destroy(h)
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def options(self) -> Options:
+        o = Options()
+        _check(lib().bem_solver_get_options(self._h, ctypes.byref(o)))
+        return o
+
+    def set_options(self, **kw) -> None:
+        o = self.options()
+        for key, v in kw.items():
+            if not hasattr(o, key):
+                raise KeyError(key)
+            setattr(o, key, v)
+        _check(lib().bem_solver_set_options(self._h, ctypes.byref(o)))
+
+    def set_mesh(self, m: Mesh) -> None:
+        _check(lib().bem_solver_set_mesh(self._h, m.handle))
+
+    def set_geometry(self, pnts, elems, bc=None, chief=None) -> None:
+        p = np.ascontiguousarray(pnts, dtype=np.float64).reshape(-1, 3)
+        e = np.ascontiguousarray(elems, dtype=np.int32).reshape(-1, 3)
+        b = None if bc is None else np.ascontiguousarray(np.asarray(bc, dtype=np.complex128).reshape(-1, 3))
+        c = None if chief is None else np.ascontiguousarray(chief, dtype=np.float64).reshape(-1, 3)
+        nc = 0 if c is None else c.shape[0]
+        _check(lib().bem_solver_set_geometry(self._h, _ptr(p), p.shape[0], _ptr(e), e.shape[0],
+                                             _ptr(b) if b is not None else None,
+                                             _ptr(c) if (c is not None and nc) else None, nc))
+
+    def set_sources(self, srcs) -> None:
+        arr = sources(srcs)
+        _check(lib().bem_solver_set_sources(self._h, arr, len(arr)))
+
+    def sizes(self):
+        v = [ctypes.c_int() for _ in range(4)]
+        _check(lib().bem_solver_sizes(self._h, *[ctypes.byref(x) for x in v]))
+        return tuple(x.value for x in v)
+
+    def assemble(self, k: float, precision: int = PREC_C64) -> None:
+        _check(lib().bem_solver_assemble(self._h, float(k), int(precision)))
+
+    def solve(self, method: int = SOLVE_GMRES_REFINED, check: bool = True) -> SolveInfo:
+        info = SolveInfo()
+        st = lib().bem_solver_solve(self._h, int(method), ctypes.byref(info))
+        if check or st != ERR_NOT_CONVERGED:
+            _check(st)
+        return info
+
+    def solution(self, precision: int = PREC_C128) -> np.ndarray:
+        n, _, _, s = self.sizes()
+        dt = np.complex64 if precision == PREC_C64 else np.complex128
+        x = np.zeros((n, s), dtype=dt, order="F")
+        _check(lib().bem_solver_get_solution(self._h, _ptr(x), n, int(precision)))
+        return x
+
+    def system(self, precision: int = PREC_C128):
+        n, m, _, s = self.sizes()
+        dt = np.complex64 if precision == PREC_C64 else np.complex128
+        A = np.zeros((n + m, n), dtype=dt, order="F")
+        B = np.zeros((n + m, s), dtype=dt, order="F")
+        _check(lib().bem_solver_get_system(self._h, _ptr(A), n + m, _ptr(B), n + m, int(precision)))
+        return A, B
+
+    def field(self, pts, precision: int = PREC_C128) -> np.ndarray:
+        p = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, 3)
+        s = self.sizes()[3]
+        dt = np.complex64 if precision == PREC_C64 else np.complex128
+        out = np.zeros((p.shape[0], s), dtype=dt, order="F")
+        _check(lib().bem_solver_eval_field(self._h, _ptr(p), p.shape[0], _ptr(out), p.shape[0], int(precision)))
+        return out
+
+    def sync(self) -> None:
+        _check(lib().bem_solver_sync(self._h))
+
+    def stream(self) -> int:
+        return int(lib().bem_solver_stream(self._h) or 0)

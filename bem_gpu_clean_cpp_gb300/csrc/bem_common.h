@@ -1,0 +1,61 @@
+// Internal definitions shared by the GB300 BEM library sources.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+
+#include "../../include/bem_gb300.h"
+
+namespace bem {
+
+// Error carried from the library internals to the C ABI boundary, where it is
+// turned into a status code plus a thread-local message (bem_last_error()).
+struct Error : std::runtime_error {
+    int status;
+    Error(int st, const std::string &msg) : std::runtime_error(msg), status(st) {}
+};
+
+[[noreturn]] void fail(int status, const char *file, int line, const std::string &msg);
+
+#define BEM_FAIL(st, msg) ::bem::fail((st), __FILE__, __LINE__, (msg))
+#define BEM_CHECK_ARG(cond, msg) \
+    do { if (!(cond)) BEM_FAIL(BEM_ERR_INVALID_ARG, (msg)); } while (0)
+#define CUDA_TRY(x)                                                                  \
+    do {                                                                             \
+        cudaError_t e_ = (x);                                                        \
+        if (e_ != cudaSuccess)                                                       \
+            ::bem::fail(e_ == cudaErrorMemoryAllocation ? BEM_ERR_NOMEM : BEM_ERR_CUDA, \
+                        __FILE__, __LINE__,                                          \
+                        std::string(#x) + ": " + cudaGetErrorString(e_));           \
+    } while (0)
+// After a kernel launch: configuration errors surface here.
+#define KERNEL_CHECK() CUDA_TRY(cudaGetLastError())
+
+// Counts kernels launched by this library (reported by bench.py).
+extern std::atomic<long long> g_launches;
+inline void count_launch(long long n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+constexpr double kPi = 3.14159265358979323846;
+constexpr int kMaxOrder = 12;              // Gauss points per direction
+constexpr int kMaxQ = kMaxOrder * kMaxOrder;
+
+// Per-element boundary condition ratios used by the assembly:
+// bcA = ca/cb, bcC = cc/cb for the element's ca*p + cb*v = cc.
+struct BcRatios {
+    double a_re, a_im, c_re, c_im;
+};
+
+// A record in a column tile's element list (far-field kernel input).
+struct TileRec {
+    int eid;        // element index
+    int node[3];    // the element's node indices
+    int slot[3];    // tile-local column of node j, -1 when node j is outside the tile
+    int owner;      // 1 when this tile counts the element's c and beta terms
+};
+
+}  // namespace bem

@@ -1,0 +1,953 @@
+// Quadrature kernels of the GB300 BEM engine: element tables, far-field
+// assembly (FP32 or FP64), singular / near-singular assembly (FP64) and
+// field-point evaluation.  The formulas restate the reference's element
+// integrals (mesh.cu:253-672) and assembly (atomicFuncs.cu:69-298); the
+// parallel structure is new:
+//   * far-field: a CTA owns TR collocation rows x one column tile and loops
+//     over the tile's element list; each element's three nodal
+//     contributions are summed in a shared-memory row accumulator, and the
+//     finished row segment is written to HBM once (no global atomics);
+//   * near-field: one warp per row scans the elements, integrates the
+//     singular and near pairs in FP64 with the whole warp (points spread over
+//     lanes, shuffle reduction), then finalises the diagonal and the RHS.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <mutex>
+#include <vector>
+
+#include "bem_common.h"
+#include "kernels.h"
+
+namespace bem {
+
+// ---------------------------------------------------------------------------
+// Gauss tables in constant memory.
+//   c_qf[q]       = (xi1, xi2, w, 0) of the regular Duffy rule in float,
+//                   w = 0.25*w_n*w_m*rho (mesh.cu:623-636)
+//   c_qd[v][q][.] = (xi1, xi2, w) in double for the map collapsed at vertex
+//                   v+1 (v = 2 is the regular rule; rhoThetaToXi_1/2/3,
+//                   mesh.cu:1710-1729)
+// ---------------------------------------------------------------------------
+__constant__ float4 c_qf[kMaxQ];
+__constant__ double c_qd[3][kMaxQ][3];
+__constant__ int c_nq;
+
+namespace {
+std::mutex g_quad_mu;
+int g_quad_order[64];   // per device, 0 = none
+int g_nq_host = 36;
+}  // namespace
+
+void gauss_legendre_host(int n, double *x, double *w);
+
+void ensure_quadrature(int order) {
+    BEM_CHECK_ARG(order >= 1 && order <= kMaxOrder, "quadrature order must be in [1, 12]");
+    int dev = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(g_quad_mu);
+    if (dev < 64 && g_quad_order[dev] == order) {
+        g_nq_host = order * order;
+        return;
+    }
+    double gx[kMaxOrder], gw[kMaxOrder];
+    gauss_legendre_host(order, gx, gw);
+    int nq = order * order;
+    std::vector<float4> qf(nq);
+    std::vector<double> qd(3 * kMaxQ * 3, 0.0);
+    int q = 0;
+    for (int n = 0; n < order; n++) {
+        double theta = 0.5 + 0.5 * gx[n];
+        for (int m = 0; m < order; m++, q++) {
+            double rho = 0.5 + 0.5 * gx[m];
+            double w = 0.25 * gw[n] * gw[m] * rho;
+            double x3a = rho * (1.0 - theta), x3b = rho * theta;        // collapse at vertex 3
+            double x1a = 1.0 - rho, x1b = rho * (1.0 - theta);          // at vertex 1
+            double x2a = rho * theta, x2b = 1.0 - rho;                  // at vertex 2
+            qf[q] = make_float4((float)x3a, (float)x3b, (float)w, 0.0f);
+            double v[3][2] = {{x1a, x1b}, {x2a, x2b}, {x3a, x3b}};
+            for (int c = 0; c < 3; c++) {
+                qd[(c * kMaxQ + q) * 3 + 0] = v[c][0];
+                qd[(c * kMaxQ + q) * 3 + 1] = v[c][1];
+                qd[(c * kMaxQ + q) * 3 + 2] = w;
+            }
+        }
+    }
+    CUDA_TRY(cudaMemcpyToSymbol(c_qf, qf.data(), sizeof(float4) * nq));
+    CUDA_TRY(cudaMemcpyToSymbol(c_qd, qd.data(), sizeof(double) * qd.size()));
+    CUDA_TRY(cudaMemcpyToSymbol(c_nq, &nq, sizeof(int)));
+    if (dev < 64) g_quad_order[dev] = order;
+    g_nq_host = nq;
+}
+
+int quadrature_points() { return g_nq_host; }
+
+// ---------------------------------------------------------------------------
+// Element tables.
+// Float table, 7 float4 per element:
+//   [0] (p3hi.xyz, J)   [1] (p3lo.xyz, near_r2)   [2] (e1, 0)   [3] (e2, 0)
+//   [4] (n, 0)          [5] (bcA.re, bcA.im, bcC.re, bcC.im)    [6] (centroid, 0)
+// p3 is split into hi + lo floats so that p3 - x keeps full float precision
+// for nearby pairs.  e1 = p1-p3, e2 = p2-p3, n = e1 x e2 / J, J = |e1 x e2|
+// (mesh.cu:612-617), near_r2 = (eta * longest edge)^2.
+// Double table, 18 doubles: p3[3] e1[3] e2[3] n[3] J bcA[2] bcC[2] diam.
+// ---------------------------------------------------------------------------
+constexpr int kGeoF = 7;
+constexpr int kGeoD = 18;
+
+__global__ void elem_setup_kernel(const double *__restrict__ nodes, const int4 *__restrict__ elems,
+                                  const double *__restrict__ bc, int E, double eta,
+                                  float4 *__restrict__ gf, double *__restrict__ gd) {
+    int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= E) return;
+    int4 nd = elems[e];
+    const double *p1 = nodes + 3 * (size_t)nd.x, *p2 = nodes + 3 * (size_t)nd.y,
+                 *p3 = nodes + 3 * (size_t)nd.z;
+    double e1[3], e2[3], c[3], cen[3];
+    for (int d = 0; d < 3; d++) {
+        e1[d] = p1[d] - p3[d];
+        e2[d] = p2[d] - p3[d];
+        cen[d] = (p1[d] + p2[d] + p3[d]) / 3.0;
+    }
+    c[0] = e1[1] * e2[2] - e1[2] * e2[1];
+    c[1] = e1[2] * e2[0] - e1[0] * e2[2];
+    c[2] = e1[0] * e2[1] - e1[1] * e2[0];
+    double J = sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+    double n[3] = {c[0] / J, c[1] / J, c[2] / J};
+    double l12 = 0, l23 = 0, l31 = 0;
+    for (int d = 0; d < 3; d++) {
+        l12 += (p1[d] - p2[d]) * (p1[d] - p2[d]);
+        l23 += (p2[d] - p3[d]) * (p2[d] - p3[d]);
+        l31 += (p3[d] - p1[d]) * (p3[d] - p1[d]);
+    }
+    double diam = sqrt(fmax(l12, fmax(l23, l31)));
+    // bcA = ca/cb, bcC = cc/cb (cuCdivf(bc[0], bc[1]) etc., atomicFuncs.cu:87,105)
+    const double *b = bc + 6 * (size_t)e;
+    double den = b[2] * b[2] + b[3] * b[3];
+    double aR = (b[0] * b[2] + b[1] * b[3]) / den, aI = (b[1] * b[2] - b[0] * b[3]) / den;
+    double cR = (b[4] * b[2] + b[5] * b[3]) / den, cI = (b[5] * b[2] - b[4] * b[3]) / den;
+    float r2 = (float)((eta * diam) * (eta * diam));
+    float4 *g = gf + (size_t)kGeoF * e;
+    float hx = (float)p3[0], hy = (float)p3[1], hz = (float)p3[2];
+    g[0] = make_float4(hx, hy, hz, (float)J);
+    g[1] = make_float4((float)(p3[0] - (double)hx), (float)(p3[1] - (double)hy),
+                       (float)(p3[2] - (double)hz), eta > 0 ? r2 : 0.0f);
+    g[2] = make_float4((float)e1[0], (float)e1[1], (float)e1[2], 0.0f);
+    g[3] = make_float4((float)e2[0], (float)e2[1], (float)e2[2], 0.0f);
+    g[4] = make_float4((float)n[0], (float)n[1], (float)n[2], 0.0f);
+    g[5] = make_float4((float)aR, (float)aI, (float)cR, (float)cI);
+    g[6] = make_float4((float)cen[0], (float)cen[1], (float)cen[2], 0.0f);
+    double *h = gd + (size_t)kGeoD * e;
+    for (int d = 0; d < 3; d++) {
+        h[d] = p3[d];
+        h[3 + d] = e1[d];
+        h[6 + d] = e2[d];
+        h[9 + d] = n[d];
+    }
+    h[12] = J;
+    h[13] = aR; h[14] = aI; h[15] = cR; h[16] = cI;
+    h[17] = diam;
+}
+
+void launch_elem_setup(const double *d_nodes, const int4 *d_elems, const double *d_bc, int E,
+                       double near_eta, float4 *geo_f, double *geo_d, cudaStream_t st) {
+    if (E <= 0) return;
+    elem_setup_kernel<<<(E + 127) / 128, 128, 0, st>>>(d_nodes, d_elems, d_bc, E, near_eta, geo_f, geo_d);
+    count_launch();
+    KERNEL_CHECK();
+}
+
+// ---------------------------------------------------------------------------
+// Pair classification shared by the far and near kernels.  It must give the
+// same answer in both, so it uses only float inputs and _rn intrinsics (no
+// FMA contraction).  A pair is "near" when x is a node of the element (the
+// singular pairs of atomicFuncs.cu:119-216) or, with eta > 0, when
+// |x - centroid|^2 < (eta*diam)^2.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool pair_is_near(int row, int N, int4 nd, float4 xh, const float4 *g) {
+    if (row < N && (row == nd.x || row == nd.y || row == nd.z)) return true;
+    float r2 = g[1].w;
+    if (r2 > 0.0f) {
+        float4 c = g[6];
+        float dx = __fsub_rn(xh.x, c.x), dy = __fsub_rn(xh.y, c.y), dz = __fsub_rn(xh.z, c.z);
+        float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+        return d2 < r2;
+    }
+    return false;
+}
+
+// ---------------------------------------------------------------------------
+// Regular (far) pair integral, FP32.  With d = y - x = d3 + xi1*e1 + xi2*e2
+// (d3 = p3 - x) and the constant height hgt = d3.n ((y-x).n is the same for
+// every y of a flat element):
+//   G = exp(-ikr)/(4 pi r), dG/dn = G (-1/r - ik) hgt/r, dG0/dn = -hgt/(4 pi r^3)
+// (green, pGpn2, pPsiLpn2: numerical.cu:70-74, mesh.cu:120-136), and the
+// weighted sums  S0 = sum w f, S1 = sum w xi1 f, S2 = sum w xi2 f  give the
+// three nodal integrals (N1 = xi1, N2 = xi2, N3 = 1 - xi1 - xi2).  The 1/(4 pi)
+// and |J| factors are applied once per pair by the caller.
+// ---------------------------------------------------------------------------
+struct SumsF {
+    float g0r, g0i, g1r, g1i, g2r, g2i;   // G sums
+    float h0r, h0i, h1r, h1i, h2r, h2i;   // dG/dn sums
+    float c;                              // dG0/dn sum
+};
+
+__device__ __forceinline__ void far_sums_f32(float3 d3, float3 e1, float3 e2, float hgt, float k,
+                                             int nq, SumsF &S) {
+    S.g0r = S.g0i = S.g1r = S.g1i = S.g2r = S.g2i = 0.0f;
+    S.h0r = S.h0i = S.h1r = S.h1i = S.h2r = S.h2i = 0.0f;
+    S.c = 0.0f;
+#pragma unroll 4
+    for (int q = 0; q < nq; q++) {
+        const float4 t = c_qf[q];
+        float dx = fmaf(t.y, e2.x, fmaf(t.x, e1.x, d3.x));
+        float dy = fmaf(t.y, e2.y, fmaf(t.x, e1.y, d3.y));
+        float dz = fmaf(t.y, e2.z, fmaf(t.x, e1.z, d3.z));
+        float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        float ri = rsqrtf(r2);
+        float r = r2 * ri;
+        float sn, cs;
+        __sincosf(k * r, &sn, &cs);
+        float gr = cs * ri, gi = -sn * ri;            // 4 pi G
+        float hq = hgt * ri;                          // dr/dn
+        float tr = fmaf(gi, k, -gr * ri);             // 4 pi G (-1/r - ik)
+        float ti = -fmaf(gr, k, gi * ri);
+        float dgr = tr * hq, dgi = ti * hq;           // 4 pi dG/dn
+        float c0 = -hq * ri * ri;                     // 4 pi dG0/dn
+        float w = t.z, w1 = w * t.x, w2 = w * t.y;
+        S.g0r = fmaf(w, gr, S.g0r);  S.g0i = fmaf(w, gi, S.g0i);
+        S.g1r = fmaf(w1, gr, S.g1r); S.g1i = fmaf(w1, gi, S.g1i);
+        S.g2r = fmaf(w2, gr, S.g2r); S.g2i = fmaf(w2, gi, S.g2i);
+        S.h0r = fmaf(w, dgr, S.h0r);  S.h0i = fmaf(w, dgi, S.h0i);
+        S.h1r = fmaf(w1, dgr, S.h1r); S.h1i = fmaf(w1, dgi, S.h1i);
+        S.h2r = fmaf(w2, dgr, S.h2r); S.h2i = fmaf(w2, dgi, S.h2i);
+        S.c = fmaf(w, c0, S.c);
+    }
+}
+
+// Same in FP64 (used by the c128 far path and by the field kernel in c128).
+struct SumsD {
+    double g0r, g0i, g1r, g1i, g2r, g2i;
+    double h0r, h0i, h1r, h1i, h2r, h2i;
+    double c;
+};
+
+__device__ __forceinline__ void far_sums_f64(const double *d3, const double *e1, const double *e2,
+                                             double hgt, double k, int nq, SumsD &S) {
+    S.g0r = S.g0i = S.g1r = S.g1i = S.g2r = S.g2i = 0.0;
+    S.h0r = S.h0i = S.h1r = S.h1i = S.h2r = S.h2i = 0.0;
+    S.c = 0.0;
+    for (int q = 0; q < nq; q++) {
+        const double x1 = c_qd[2][q][0], x2 = c_qd[2][q][1], w = c_qd[2][q][2];
+        double dx = d3[0] + x1 * e1[0] + x2 * e2[0];
+        double dy = d3[1] + x1 * e1[1] + x2 * e2[1];
+        double dz = d3[2] + x1 * e1[2] + x2 * e2[2];
+        double r = sqrt(dx * dx + dy * dy + dz * dz);
+        double ri = 1.0 / r;
+        double sn, cs;
+        sincos(k * r, &sn, &cs);
+        double gr = cs * ri, gi = -sn * ri;
+        double hq = hgt * ri;
+        double tr = gi * k - gr * ri;
+        double ti = -(gr * k + gi * ri);
+        double dgr = tr * hq, dgi = ti * hq;
+        double c0 = -hq * ri * ri;
+        double w1 = w * x1, w2 = w * x2;
+        S.g0r += w * gr;  S.g0i += w * gi;
+        S.g1r += w1 * gr; S.g1i += w1 * gi;
+        S.g2r += w2 * gr; S.g2i += w2 * gi;
+        S.h0r += w * dgr;  S.h0i += w * dgi;
+        S.h1r += w1 * dgr; S.h1i += w1 * dgi;
+        S.h2r += w2 * dgr; S.h2i += w2 * dgi;
+        S.c += w * c0;
+    }
+}
+
+// Nodal coefficients from the sums (g_h_c_l_nsgl's tail, mesh.cu:655-671):
+// node j's integral = scale * S_j with S_3 = S0 - S1 - S2, g *= i*rho*omega,
+// a_j = h_j - bcA*g_j, beta = bcC * sum_j g_j, c = scale * Sc.
+template <typename T, typename S>
+struct Coeffs {
+    T ar[3], ai[3];
+    T br, bi;
+    T c;
+};
+
+template <typename T, typename SUMS>
+__device__ __forceinline__ void finish_coeffs(const SUMS &S, T scale, T rw, T bAr, T bAi, T bCr,
+                                              T bCi, Coeffs<T, SUMS> &o) {
+    T gr[3] = {S.g1r, S.g2r, S.g0r - S.g1r - S.g2r};
+    T gi[3] = {S.g1i, S.g2i, S.g0i - S.g1i - S.g2i};
+    T hr[3] = {S.h1r, S.h2r, S.h0r - S.h1r - S.h2r};
+    T hi[3] = {S.h1i, S.h2i, S.h0i - S.h1i - S.h2i};
+    T sgr = 0, sgi = 0;
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+        // g = i*rw*scale*G  ->  (-rw*scale*Gi, rw*scale*Gr)
+        T g_r = -rw * scale * gi[j], g_i = rw * scale * gr[j];
+        T h_r = scale * hr[j], h_i = scale * hi[j];
+        o.ar[j] = h_r - (bAr * g_r - bAi * g_i);
+        o.ai[j] = h_i - (bAr * g_i + bAi * g_r);
+        sgr += g_r;
+        sgi += g_i;
+    }
+    o.br = bCr * sgr - bCi * sgi;
+    o.bi = bCr * sgi + bCi * sgr;
+    o.c = scale * S.c;
+}
+
+// ---------------------------------------------------------------------------
+// Far-field assembly kernel.
+// grid = (ceil(R/TR), ntiles), block = NT threads, dynamic smem = acc[TR][tc].
+// ---------------------------------------------------------------------------
+template <int TR, int NT>
+__global__ void __launch_bounds__(NT, 1)
+far_assembly_f32(RowPoints rows, int N, GeoTables geo, TileSet tiles, float k, float rw,
+                 float2 *__restrict__ A, size_t lda, float *__restrict__ c_part,
+                 float2 *__restrict__ beta_part) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float2 *acc = reinterpret_cast<float2 *>(smem_raw);
+    const int tile = blockIdx.y;
+    const int tc = tiles.col_cnt[tile];
+    const int r0 = blockIdx.x * TR;
+    const int R = rows.R;
+    for (int i = threadIdx.x; i < TR * tc; i += NT) acc[i] = make_float2(0.f, 0.f);
+
+    float4 xh[TR], xl[TR];
+#pragma unroll
+    for (int t = 0; t < TR; t++) {
+        int row = min(r0 + t, R - 1);
+        xh[t] = rows.f[2 * (size_t)row];
+        xl[t] = rows.f[2 * (size_t)row + 1];
+    }
+    __syncthreads();
+
+    const int nq = c_nq;
+    const float inv4pi = (float)(1.0 / (4.0 * kPi));
+    float csum[TR], bsr[TR], bsi[TR];
+#pragma unroll
+    for (int t = 0; t < TR; t++) csum[t] = bsr[t] = bsi[t] = 0.0f;
+
+    const int rb = tiles.rec_ptr[tile], re = tiles.rec_ptr[tile + 1];
+    for (int i = rb + threadIdx.x; i < re; i += NT) {
+        const TileRec rec = tiles.recs[i];
+        const float4 *g = geo.geo_f + (size_t)kGeoF * rec.eid;
+        const float4 g0 = g[0], g1 = g[1], g2 = g[2], g3 = g[3], g4 = g[4], g5 = g[5];
+        const int4 nd = make_int4(rec.node[0], rec.node[1], rec.node[2], 0);
+        const float3 e1 = make_float3(g2.x, g2.y, g2.z), e2 = make_float3(g3.x, g3.y, g3.z);
+        const float scale = g0.w * inv4pi;
+#pragma unroll
+        for (int t = 0; t < TR; t++) {
+            const int row = r0 + t;
+            if (row >= R) break;
+            if (pair_is_near(row, N, nd, xh[t], g)) continue;
+            float3 d3 = make_float3((g0.x - xh[t].x) + (g1.x - xl[t].x),
+                                    (g0.y - xh[t].y) + (g1.y - xl[t].y),
+                                    (g0.z - xh[t].z) + (g1.z - xl[t].z));
+            float hgt = d3.x * g4.x + d3.y * g4.y + d3.z * g4.z;
+            SumsF S;
+            far_sums_f32(d3, e1, e2, hgt, k, nq, S);
+            Coeffs<float, SumsF> o;
+            finish_coeffs<float, SumsF>(S, scale, rw, g5.x, g5.y, g5.z, g5.w, o);
+            float2 *arow = acc + (size_t)t * tc;
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                int s = rec.slot[j];
+                if (s >= 0) {
+                    atomicAdd(&arow[s].x, o.ar[j]);
+                    atomicAdd(&arow[s].y, o.ai[j]);
+                }
+            }
+            if (rec.owner) {
+                csum[t] += o.c;
+                bsr[t] += o.br;
+                bsi[t] += o.bi;
+            }
+        }
+    }
+    // Per-row reduction of the c and beta partial sums (fixed order).
+    __shared__ float red[NT / 32][TR][3];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int t = 0; t < TR; t++) {
+        float a = csum[t], b = bsr[t], c = bsi[t];
+        for (int o = 16; o > 0; o >>= 1) {
+            a += __shfl_xor_sync(0xffffffffu, a, o);
+            b += __shfl_xor_sync(0xffffffffu, b, o);
+            c += __shfl_xor_sync(0xffffffffu, c, o);
+        }
+        if (lane == 0) { red[warp][t][0] = a; red[warp][t][1] = b; red[warp][t][2] = c; }
+    }
+    __syncthreads();
+    if (threadIdx.x < TR) {
+        const int t = threadIdx.x, row = r0 + t;
+        if (row < R) {
+            float a = 0, b = 0, c = 0;
+            for (int w = 0; w < NT / 32; w++) { a += red[w][t][0]; b += red[w][t][1]; c += red[w][t][2]; }
+            c_part[(size_t)tile * R + row] = a;
+            beta_part[(size_t)tile * R + row] = make_float2(b, c);
+        }
+    }
+    // Write the finished row segments (coalesced when the tile is contiguous).
+    const int *cols = tiles.cols + (size_t)tile * tiles.tc_max;
+#pragma unroll
+    for (int t = 0; t < TR; t++) {
+        const int row = r0 + t;
+        if (row >= R) break;
+        float2 *dst = A + (size_t)row * lda;
+        const float2 *src = acc + (size_t)t * tc;
+        for (int i = threadIdx.x; i < tc; i += NT) dst[cols[i]] = src[i];
+    }
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT, 1)
+far_assembly_f64(RowPoints rows, int N, GeoTables geo, TileSet tiles, double k, double rw,
+                 double2 *__restrict__ A, size_t lda, double *__restrict__ c_part,
+                 double2 *__restrict__ beta_part) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double2 *acc = reinterpret_cast<double2 *>(smem_raw);
+    const int tile = blockIdx.y;
+    const int tc = tiles.col_cnt[tile];
+    const int row = blockIdx.x;
+    const int R = rows.R;
+    for (int i = threadIdx.x; i < tc; i += NT) acc[i] = make_double2(0.0, 0.0);
+    const float4 xh = rows.f[2 * (size_t)row];
+    const double x[3] = {rows.d[3 * (size_t)row], rows.d[3 * (size_t)row + 1], rows.d[3 * (size_t)row + 2]};
+    __syncthreads();
+    const int nq = c_nq;
+    const double inv4pi = 1.0 / (4.0 * kPi);
+    double csum = 0, bsr = 0, bsi = 0;
+    const int rb = tiles.rec_ptr[tile], re = tiles.rec_ptr[tile + 1];
+    for (int i = rb + threadIdx.x; i < re; i += NT) {
+        const TileRec rec = tiles.recs[i];
+        const float4 *g = geo.geo_f + (size_t)kGeoF * rec.eid;
+        const int4 nd = make_int4(rec.node[0], rec.node[1], rec.node[2], 0);
+        if (pair_is_near(row, N, nd, xh, g)) continue;
+        const double *h = geo.geo_d + (size_t)kGeoD * rec.eid;
+        double d3[3] = {h[0] - x[0], h[1] - x[1], h[2] - x[2]};
+        double hgt = d3[0] * h[9] + d3[1] * h[10] + d3[2] * h[11];
+        SumsD S;
+        far_sums_f64(d3, h + 3, h + 6, hgt, k, nq, S);
+        Coeffs<double, SumsD> o;
+        finish_coeffs<double, SumsD>(S, h[12] * inv4pi, rw, h[13], h[14], h[15], h[16], o);
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            int s = rec.slot[j];
+            if (s >= 0) {
+                atomicAdd(&acc[s].x, o.ar[j]);
+                atomicAdd(&acc[s].y, o.ai[j]);
+            }
+        }
+        if (rec.owner) { csum += o.c; bsr += o.br; bsi += o.bi; }
+    }
+    __shared__ double red[NT / 32][3];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) {
+        csum += __shfl_xor_sync(0xffffffffu, csum, o);
+        bsr += __shfl_xor_sync(0xffffffffu, bsr, o);
+        bsi += __shfl_xor_sync(0xffffffffu, bsi, o);
+    }
+    if (lane == 0) { red[warp][0] = csum; red[warp][1] = bsr; red[warp][2] = bsi; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0, b = 0, c = 0;
+        for (int w = 0; w < NT / 32; w++) { a += red[w][0]; b += red[w][1]; c += red[w][2]; }
+        c_part[(size_t)tile * R + row] = a;
+        beta_part[(size_t)tile * R + row] = make_double2(b, c);
+    }
+    const int *cols = tiles.cols + (size_t)tile * tiles.tc_max;
+    double2 *dst = A + (size_t)row * lda;
+    for (int i = threadIdx.x; i < tc; i += NT) dst[cols[i]] = acc[i];
+}
+
+constexpr int kFarTR32 = 2, kFarNT32 = 512, kFarNT64 = 256;
+
+int far_rows_per_cta(int prec) { return prec == BEM_PREC_C64 ? kFarTR32 : 1; }
+
+size_t far_smem_bytes(int prec, int tc) {
+    return prec == BEM_PREC_C64 ? (size_t)kFarTR32 * tc * sizeof(float2) : (size_t)tc * sizeof(double2);
+}
+
+void launch_far_assembly(int prec, const RowPoints &rows, int N, const GeoTables &geo,
+                         const TileSet &tiles, const Physics &ph, void *A, size_t lda,
+                         void *c_part, void *beta_part, cudaStream_t st) {
+    if (rows.R <= 0 || tiles.ntiles <= 0) return;
+    size_t smem = far_smem_bytes(prec, tiles.tc_max);
+    if (prec == BEM_PREC_C64) {
+        auto kern = far_assembly_f32<kFarTR32, kFarNT32>;
+        CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        dim3 grid((rows.R + kFarTR32 - 1) / kFarTR32, tiles.ntiles);
+        kern<<<grid, kFarNT32, smem, st>>>(rows, N, geo, tiles, (float)ph.k, (float)ph.rw,
+                                           (float2 *)A, lda, (float *)c_part, (float2 *)beta_part);
+    } else {
+        auto kern = far_assembly_f64<kFarNT64>;
+        CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        dim3 grid(rows.R, tiles.ntiles);
+        kern<<<grid, kFarNT64, smem, st>>>(rows, N, geo, tiles, ph.k, ph.rw, (double2 *)A, lda,
+                                           (double *)c_part, (double2 *)beta_part);
+    }
+    count_launch();
+    KERNEL_CHECK();
+}
+
+// ---------------------------------------------------------------------------
+// FP64 near-pair integration by one warp.
+// Leaves: sub-triangles (parent local vertices va, vb, vc) with a Duffy map
+// collapsed at vertex `collapse` (1, 2, 3).  Singular pairs use one leaf, the
+// whole element with the map collapsed at x's vertex (g/h/c_l_sgl1..3,
+// mesh.cu:253-595).  Near-singular pairs subdivide the element into four at
+// edge midpoints while dist(x, sub-centroid) < eta * sub-diameter, up to
+// near_depth levels, and use the regular map on every leaf.
+// ---------------------------------------------------------------------------
+constexpr int kMaxDepth = 4;
+constexpr int kMaxLeaves = 256;        // 4^kMaxDepth
+constexpr int kNearWarps = 4;
+
+struct Leaf {
+    double a[2], b[2], c[2];
+};
+
+struct NearOut {
+    double gr[3], gi[3], hr[3], hi[3], c;
+};
+
+__device__ __forceinline__ void xi_point(const double *h, double x1, double x2, double *y) {
+    for (int d = 0; d < 3; d++) y[d] = h[d] + x1 * h[3 + d] + x2 * h[6 + d];
+}
+
+// Lane 0 builds the leaf list of a near-singular pair (depth-first, children
+// in the order (a,ab,ca), (ab,b,bc), (ca,bc,c), (ab,bc,ca)).
+__device__ int build_leaves(const double *h, const double *x, double eta, int depth_max,
+                            Leaf *leaves) {
+    struct Item { Leaf t; int depth; };
+    Item stack[3 * kMaxDepth + 2];
+    int sp = 0, nl = 0;
+    stack[sp++] = {{{1.0, 0.0}, {0.0, 1.0}, {0.0, 0.0}}, 0};
+    while (sp > 0) {
+        Item it = stack[--sp];
+        bool split = false;
+        if (it.depth < depth_max) {
+            double ya[3], yb[3], yc[3], cen[3];
+            xi_point(h, it.t.a[0], it.t.a[1], ya);
+            xi_point(h, it.t.b[0], it.t.b[1], yb);
+            xi_point(h, it.t.c[0], it.t.c[1], yc);
+            xi_point(h, (it.t.a[0] + it.t.b[0] + it.t.c[0]) / 3.0, (it.t.a[1] + it.t.b[1] + it.t.c[1]) / 3.0, cen);
+            double lab = 0, lbc = 0, lca = 0, dc = 0;
+            for (int d = 0; d < 3; d++) {
+                lab += (ya[d] - yb[d]) * (ya[d] - yb[d]);
+                lbc += (yb[d] - yc[d]) * (yb[d] - yc[d]);
+                lca += (yc[d] - ya[d]) * (yc[d] - ya[d]);
+                dc += (cen[d] - x[d]) * (cen[d] - x[d]);
+            }
+            double diam = sqrt(fmax(lab, fmax(lbc, lca)));
+            split = sqrt(dc) < eta * diam;
+        }
+        if (split) {
+            const Leaf &t = it.t;
+            double ab[2] = {0.5 * (t.a[0] + t.b[0]), 0.5 * (t.a[1] + t.b[1])};
+            double bc[2] = {0.5 * (t.b[0] + t.c[0]), 0.5 * (t.b[1] + t.c[1])};
+            double ca[2] = {0.5 * (t.c[0] + t.a[0]), 0.5 * (t.c[1] + t.a[1])};
+            int d1 = it.depth + 1;
+            // push in reverse so that children pop in order 0, 1, 2, 3
+            stack[sp++] = {{{ab[0], ab[1]}, {bc[0], bc[1]}, {ca[0], ca[1]}}, d1};
+            stack[sp++] = {{{ca[0], ca[1]}, {bc[0], bc[1]}, {t.c[0], t.c[1]}}, d1};
+            stack[sp++] = {{{ab[0], ab[1]}, {t.b[0], t.b[1]}, {bc[0], bc[1]}}, d1};
+            stack[sp++] = {{{t.a[0], t.a[1]}, {ab[0], ab[1]}, {ca[0], ca[1]}}, d1};
+        } else if (nl < kMaxLeaves) {
+            leaves[nl++] = it.t;
+        }
+    }
+    return nl;
+}
+
+// Warp-cooperative FP64 integration over the leaves; the result is valid in
+// every lane.  Returns g (before the i*rho*omega factor), h, c, scaled by
+// |J|/(4 pi) as in the far path.
+__device__ void near_integrate(const double *h, const double *x, double k, int collapse,
+                               const Leaf *leaves, int nl, int nq, NearOut &o) {
+    const int lane = threadIdx.x & 31;
+    double acc[13];
+#pragma unroll
+    for (int i = 0; i < 13; i++) acc[i] = 0.0;
+    const double *n = h + 9;
+    const int cv = collapse - 1;
+    for (int idx = lane; idx < nl * nq; idx += 32) {
+        const int l = idx / nq, q = idx - l * nq;
+        const Leaf &t = leaves[l];
+        double ea0 = t.a[0] - t.c[0], ea1 = t.a[1] - t.c[1];
+        double eb0 = t.b[0] - t.c[0], eb1 = t.b[1] - t.c[1];
+        double area = fabs(ea0 * eb1 - ea1 * eb0);
+        double s1 = c_qd[cv][q][0], s2 = c_qd[cv][q][1], w = c_qd[cv][q][2] * area;
+        double x1 = t.c[0] + s1 * ea0 + s2 * eb0;
+        double x2 = t.c[1] + s1 * ea1 + s2 * eb1;
+        double d[3];
+        for (int dd = 0; dd < 3; dd++) d[dd] = h[dd] - x[dd] + x1 * h[3 + dd] + x2 * h[6 + dd];
+        double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+        double ri = 1.0 / r;
+        double drdn = (d[0] * n[0] + d[1] * n[1] + d[2] * n[2]) * ri;
+        double sn, cs;
+        sincos(k * r, &sn, &cs);
+        double gr = cs * ri, gi = -sn * ri;
+        double tr = gi * k - gr * ri, ti = -(gr * k + gi * ri);
+        double dgr = tr * drdn, dgi = ti * drdn;
+        double c0 = -drdn * ri * ri;
+        double N[3] = {x1, x2, 1.0 - x1 - x2};
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            acc[j] += w * N[j] * gr;
+            acc[3 + j] += w * N[j] * gi;
+            acc[6 + j] += w * N[j] * dgr;
+            acc[9 + j] += w * N[j] * dgi;
+        }
+        acc[12] += w * c0;
+    }
+#pragma unroll
+    for (int i = 0; i < 13; i++)
+        for (int off = 16; off > 0; off >>= 1) acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], off);
+    const double scale = h[12] / (4.0 * kPi);
+    for (int j = 0; j < 3; j++) {
+        o.gr[j] = scale * acc[j];
+        o.gi[j] = scale * acc[3 + j];
+        o.hr[j] = scale * acc[6 + j];
+        o.hi[j] = scale * acc[9 + j];
+    }
+    o.c = scale * acc[12];
+}
+
+__device__ __forceinline__ double2 incident_field(const DevSource &s, double k, const double *x) {
+    double ph, amp_scale = 1.0;
+    if (s.kind == BEM_SRC_PLANE) {
+        ph = -k * (s.vec[0] * x[0] + s.vec[1] * x[1] + s.vec[2] * x[2]);
+    } else {
+        double dx = x[0] - s.vec[0], dy = x[1] - s.vec[1], dz = x[2] - s.vec[2];
+        double r = sqrt(dx * dx + dy * dy + dz * dz);
+        ph = -k * r;
+        amp_scale = 1.0 / (4.0 * kPi * r);
+    }
+    double sn, cs;
+    sincos(ph, &sn, &cs);
+    cs *= amp_scale;
+    sn *= amp_scale;
+    return make_double2(s.amp_re * cs - s.amp_im * sn, s.amp_re * sn + s.amp_im * cs);
+}
+
+template <typename TA> __device__ __forceinline__ void add_entry(TA *p, double re, double im);
+template <> __device__ __forceinline__ void add_entry<float2>(float2 *p, double re, double im) {
+    float2 v = *p;
+    *p = make_float2((float)((double)v.x + re), (float)((double)v.y + im));
+}
+template <> __device__ __forceinline__ void add_entry<double2>(double2 *p, double re, double im) {
+    double2 v = *p;
+    *p = make_double2(v.x + re, v.y + im);
+}
+
+template <typename TA, typename TP, typename TP2>
+__global__ void __launch_bounds__(32 * kNearWarps)
+near_assembly_kernel(RowPoints rows, int N, GeoTables geo, Physics ph, int nq, TA *__restrict__ A,
+                     size_t lda, const TP *__restrict__ c_part, const TP2 *__restrict__ beta_part,
+                     int ntiles, const DevSource *__restrict__ srcs, int S, double2 *__restrict__ B) {
+    __shared__ Leaf leaves_all[kNearWarps][kMaxLeaves];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int row = blockIdx.x * kNearWarps + warp;
+    if (row >= rows.R) return;
+    Leaf *leaves = leaves_all[warp];
+    const float4 xh = rows.f[2 * (size_t)row];
+    const double x[3] = {rows.d[3 * (size_t)row], rows.d[3 * (size_t)row + 1], rows.d[3 * (size_t)row + 2]};
+    double cn = 0.0, bnr = 0.0, bni = 0.0;
+    for (int e0 = 0; e0 < geo.E; e0 += 32) {
+        const int e = e0 + lane;
+        bool flag = false;
+        int4 nd = make_int4(-1, -1, -1, 0);
+        if (e < geo.E) {
+            nd = geo.elems[e];
+            flag = pair_is_near(row, N, nd, xh, geo.geo_f + (size_t)kGeoF * e);
+        }
+        unsigned mask = __ballot_sync(0xffffffffu, flag);
+        while (mask) {
+            const int b = __ffs(mask) - 1;
+            mask &= mask - 1;
+            const int eb = e0 + b;
+            const int4 ndb = make_int4(__shfl_sync(0xffffffffu, nd.x, b), __shfl_sync(0xffffffffu, nd.y, b),
+                                       __shfl_sync(0xffffffffu, nd.z, b), 0);
+            const double *h = geo.geo_d + (size_t)kGeoD * eb;
+            int collapse = 3, nl = 1;
+            const int vtx = (row < N) ? (row == ndb.x ? 1 : row == ndb.y ? 2 : row == ndb.z ? 3 : 0) : 0;
+            if (vtx) {
+                collapse = vtx;
+                if (lane == 0) leaves[0] = {{1.0, 0.0}, {0.0, 1.0}, {0.0, 0.0}};
+            } else {
+                if (lane == 0) nl = build_leaves(h, x, ph.near_eta, ph.near_depth, leaves);
+                nl = __shfl_sync(0xffffffffu, nl, 0);
+            }
+            __syncwarp();
+            NearOut o;
+            near_integrate(h, x, ph.k, collapse, leaves, nl, nq, o);
+            __syncwarp();
+            if (lane == 0) {
+                const double bAr = h[13], bAi = h[14], bCr = h[15], bCi = h[16];
+                double sgr = 0, sgi = 0;
+                const int node[3] = {ndb.x, ndb.y, ndb.z};
+                for (int j = 0; j < 3; j++) {
+                    double g_r = -ph.rw * o.gi[j], g_i = ph.rw * o.gr[j];
+                    double a_r = o.hr[j] - (bAr * g_r - bAi * g_i);
+                    double a_i = o.hi[j] - (bAr * g_i + bAi * g_r);
+                    add_entry<TA>(A + (size_t)row * lda + node[j], a_r, a_i);
+                    sgr += g_r;
+                    sgi += g_i;
+                }
+                if (row < N) cn += o.c;
+                bnr += bCr * sgr - bCi * sgi;
+                bni += bCr * sgi + bCi * sgr;
+            }
+        }
+    }
+    // Finalise the row: diagonal 1 - sum c (surface rows only,
+    // atomicFuncs.cu:99-102 and :227-235) and B = p_inc - beta.
+    double cf = 0.0, bfr = 0.0, bfi = 0.0;
+    if (lane == 0) {
+        for (int t = 0; t < ntiles; t++) {
+            cf += (double)c_part[(size_t)t * rows.R + row];
+            bfr += (double)beta_part[(size_t)t * rows.R + row].x;
+            bfi += (double)beta_part[(size_t)t * rows.R + row].y;
+        }
+        if (row < N) add_entry<TA>(A + (size_t)row * lda + row, 1.0 - (cf + cn), 0.0);
+    }
+    const double br = __shfl_sync(0xffffffffu, bfr + bnr, 0);
+    const double bi = __shfl_sync(0xffffffffu, bfi + bni, 0);
+    for (int s = lane; s < S; s += 32) {
+        double2 p = incident_field(srcs[s], ph.k, x);
+        B[(size_t)s * rows.R + row] = make_double2(p.x - br, p.y - bi);
+    }
+}
+
+void launch_near_assembly(int prec, const RowPoints &rows, int N, const GeoTables &geo,
+                          const Physics &ph, void *A, size_t lda, const void *c_part,
+                          const void *beta_part, int ntiles, const DevSource *srcs, int S,
+                          double2 *B, cudaStream_t st) {
+    if (rows.R <= 0) return;
+    BEM_CHECK_ARG(ph.near_depth >= 0 && ph.near_depth <= kMaxDepth, "near_depth must be in [0, 4]");
+    int nq = quadrature_points();
+    dim3 grid((rows.R + kNearWarps - 1) / kNearWarps);
+    if (prec == BEM_PREC_C64) {
+        near_assembly_kernel<float2, float, float2><<<grid, 32 * kNearWarps, 0, st>>>(
+            rows, N, geo, ph, nq, (float2 *)A, lda, (const float *)c_part,
+            (const float2 *)beta_part, ntiles, srcs, S, B);
+    } else {
+        near_assembly_kernel<double2, double, double2><<<grid, 32 * kNearWarps, 0, st>>>(
+            rows, N, geo, ph, nq, (double2 *)A, lda, (const double *)c_part,
+            (const double2 *)beta_part, ntiles, srcs, S, B);
+    }
+    count_launch();
+    KERNEL_CHECK();
+}
+
+// ---------------------------------------------------------------------------
+// Field evaluation (genExtPressure / pntElemsOffset, mesh.cu:1008-1073),
+// batched: grid (points, element splits), threads over elements, per-thread
+// sums for up to kFieldSB sources, block reduction to part[split][p][s].
+// ---------------------------------------------------------------------------
+constexpr int kFieldNT = 256;
+constexpr int kFieldSB = 8;
+
+template <typename T> struct CplxT;
+template <> struct CplxT<float> { using t = float2; };
+template <> struct CplxT<double> { using t = double2; };
+
+template <typename T>
+__global__ void __launch_bounds__(kFieldNT)
+field_far_kernel(RowPoints pts, GeoTables geo, T k, T rw, int nq,
+                 const typename CplxT<T>::t *__restrict__ u, size_t ldu, int S, int s0, int nsplit,
+                 double2 *__restrict__ part) {
+    const int p = blockIdx.x, split = blockIdx.y;
+    const int per = (geo.E + nsplit - 1) / nsplit;
+    const int eb = split * per, ee = min(geo.E, eb + per);
+    const float4 xh = pts.f[2 * (size_t)p], xl = pts.f[2 * (size_t)p + 1];
+    const double xd[3] = {pts.d[3 * (size_t)p], pts.d[3 * (size_t)p + 1], pts.d[3 * (size_t)p + 2]};
+    const int sb = min(kFieldSB, S - s0);
+    T accr[kFieldSB], acci[kFieldSB];
+#pragma unroll
+    for (int s = 0; s < kFieldSB; s++) accr[s] = acci[s] = 0;
+    for (int e = eb + threadIdx.x; e < ee; e += kFieldNT) {
+        const float4 *g = geo.geo_f + (size_t)kGeoF * e;
+        const int4 nd = geo.elems[e];
+        if (pair_is_near(-1, 0, nd, xh, g)) continue;
+        Coeffs<T, int> o;
+        if constexpr (sizeof(T) == 4) {
+            const float4 g0 = g[0], g1 = g[1], g2 = g[2], g3 = g[3], g4 = g[4], g5 = g[5];
+            float3 d3 = make_float3((g0.x - xh.x) + (g1.x - xl.x), (g0.y - xh.y) + (g1.y - xl.y),
+                                    (g0.z - xh.z) + (g1.z - xl.z));
+            float hgt = d3.x * g4.x + d3.y * g4.y + d3.z * g4.z;
+            SumsF Sm;
+            far_sums_f32(d3, make_float3(g2.x, g2.y, g2.z), make_float3(g3.x, g3.y, g3.z), hgt,
+                         (float)k, nq, Sm);
+            Coeffs<float, SumsF> oo;
+            finish_coeffs<float, SumsF>(Sm, g0.w * (float)(1.0 / (4.0 * kPi)), (float)rw, g5.x, g5.y,
+                                        g5.z, g5.w, oo);
+            for (int j = 0; j < 3; j++) { o.ar[j] = oo.ar[j]; o.ai[j] = oo.ai[j]; }
+            o.br = oo.br; o.bi = oo.bi;
+        } else {
+            const double *h = geo.geo_d + (size_t)kGeoD * e;
+            double d3[3] = {h[0] - xd[0], h[1] - xd[1], h[2] - xd[2]};
+            double hgt = d3[0] * h[9] + d3[1] * h[10] + d3[2] * h[11];
+            SumsD Sm;
+            far_sums_f64(d3, h + 3, h + 6, hgt, (double)k, nq, Sm);
+            Coeffs<double, SumsD> oo;
+            finish_coeffs<double, SumsD>(Sm, h[12] / (4.0 * kPi), (double)rw, h[13], h[14], h[15],
+                                         h[16], oo);
+            for (int j = 0; j < 3; j++) { o.ar[j] = oo.ar[j]; o.ai[j] = oo.ai[j]; }
+            o.br = oo.br; o.bi = oo.bi;
+        }
+        const int node[3] = {nd.x, nd.y, nd.z};
+#pragma unroll
+        for (int s = 0; s < kFieldSB; s++) {
+            if (s >= sb) break;
+            T vr = o.br, vi = o.bi;
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                const typename CplxT<T>::t uu = u[(size_t)(s0 + s) * ldu + node[j]];
+                vr += o.ar[j] * uu.x - o.ai[j] * uu.y;
+                vi += o.ar[j] * uu.y + o.ai[j] * uu.x;
+            }
+            accr[s] += vr;
+            acci[s] += vi;
+        }
+    }
+    __shared__ double red[kFieldNT / 32][kFieldSB][2];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int s = 0; s < kFieldSB; s++) {
+        double a = accr[s], b = acci[s];
+        for (int o = 16; o > 0; o >>= 1) {
+            a += __shfl_xor_sync(0xffffffffu, a, o);
+            b += __shfl_xor_sync(0xffffffffu, b, o);
+        }
+        if (lane == 0) { red[warp][s][0] = a; red[warp][s][1] = b; }
+    }
+    __syncthreads();
+    if (threadIdx.x < sb) {
+        const int s = threadIdx.x;
+        double a = 0, b = 0;
+        for (int w = 0; w < kFieldNT / 32; w++) { a += red[w][s][0]; b += red[w][s][1]; }
+        part[((size_t)split * pts.R + p) * S + s0 + s] = make_double2(a, b);
+    }
+}
+
+// Near-singular field pairs (eta > 0): one warp per point, FP64.
+template <typename TU>
+__global__ void __launch_bounds__(32 * kNearWarps)
+field_near_kernel(RowPoints pts, GeoTables geo, Physics ph, int nq, const TU *__restrict__ u, size_t ldu,
+                  int S, double2 *__restrict__ near_part) {
+    __shared__ Leaf leaves_all[kNearWarps][kMaxLeaves];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int p = blockIdx.x * kNearWarps + warp;
+    if (p >= pts.R) return;
+    Leaf *leaves = leaves_all[warp];
+    const float4 xh = pts.f[2 * (size_t)p];
+    const double x[3] = {pts.d[3 * (size_t)p], pts.d[3 * (size_t)p + 1], pts.d[3 * (size_t)p + 2]};
+    for (int s = lane; s < S; s += 32) near_part[(size_t)p * S + s] = make_double2(0.0, 0.0);
+    __syncwarp();
+    for (int e0 = 0; e0 < geo.E; e0 += 32) {
+        const int e = e0 + lane;
+        bool flag = false;
+        int4 nd = make_int4(-1, -1, -1, 0);
+        if (e < geo.E) {
+            nd = geo.elems[e];
+            flag = pair_is_near(-1, 0, nd, xh, geo.geo_f + (size_t)kGeoF * e);
+        }
+        unsigned mask = __ballot_sync(0xffffffffu, flag);
+        while (mask) {
+            const int b = __ffs(mask) - 1;
+            mask &= mask - 1;
+            const int eb = e0 + b;
+            const int node[3] = {__shfl_sync(0xffffffffu, nd.x, b), __shfl_sync(0xffffffffu, nd.y, b),
+                                 __shfl_sync(0xffffffffu, nd.z, b)};
+            const double *h = geo.geo_d + (size_t)kGeoD * eb;
+            int nl = 0;
+            if (lane == 0) nl = build_leaves(h, x, ph.near_eta, ph.near_depth, leaves);
+            nl = __shfl_sync(0xffffffffu, nl, 0);
+            __syncwarp();
+            NearOut o;
+            near_integrate(h, x, ph.k, 3, leaves, nl, nq, o);
+            __syncwarp();
+            const double bAr = h[13], bAi = h[14], bCr = h[15], bCi = h[16];
+            double ar[3], ai[3], sgr = 0, sgi = 0;
+            for (int j = 0; j < 3; j++) {
+                double g_r = -ph.rw * o.gi[j], g_i = ph.rw * o.gr[j];
+                ar[j] = o.hr[j] - (bAr * g_r - bAi * g_i);
+                ai[j] = o.hi[j] - (bAr * g_i + bAi * g_r);
+                sgr += g_r;
+                sgi += g_i;
+            }
+            double br = bCr * sgr - bCi * sgi, bi = bCr * sgi + bCi * sgr;
+            for (int s = lane; s < S; s += 32) {
+                double vr = br, vi = bi;
+                for (int j = 0; j < 3; j++) {
+                    TU uu = u[(size_t)s * ldu + node[j]];
+                    vr += ar[j] * (double)uu.x - ai[j] * (double)uu.y;
+                    vi += ar[j] * (double)uu.y + ai[j] * (double)uu.x;
+                }
+                double2 cur = near_part[(size_t)p * S + s];
+                near_part[(size_t)p * S + s] = make_double2(cur.x + vr, cur.y + vi);
+            }
+        }
+    }
+}
+
+__global__ void field_finalize_kernel(RowPoints pts, int S, int nsplit, double k,
+                                      const DevSource *__restrict__ srcs,
+                                      const double2 *__restrict__ part,
+                                      const double2 *__restrict__ near_part, double2 *__restrict__ out) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= pts.R * S) return;
+    const int p = idx / S, s = idx - p * S;
+    const double x[3] = {pts.d[3 * (size_t)p], pts.d[3 * (size_t)p + 1], pts.d[3 * (size_t)p + 2]};
+    double sr = 0, si = 0;
+    for (int t = 0; t < nsplit; t++) {
+        double2 v = part[((size_t)t * pts.R + p) * S + s];
+        sr += v.x;
+        si += v.y;
+    }
+    if (near_part) {
+        sr += near_part[(size_t)p * S + s].x;
+        si += near_part[(size_t)p * S + s].y;
+    }
+    double2 inc = incident_field(srcs[s], k, x);
+    out[(size_t)s * pts.R + p] = make_double2(inc.x - sr, inc.y - si);
+}
+
+void launch_field(int prec, const RowPoints &pts, const GeoTables &geo, const Physics &ph,
+                  const void *u, size_t ldu, int S, const DevSource *srcs, double2 *part, int nsplit,
+                  double2 *near_part, double2 *out, cudaStream_t st) {
+    if (pts.R <= 0 || S <= 0) return;
+    int nq = quadrature_points();
+    dim3 grid(pts.R, nsplit);
+    for (int s0 = 0; s0 < S; s0 += kFieldSB) {
+        if (prec == BEM_PREC_C64)
+            field_far_kernel<float><<<grid, kFieldNT, 0, st>>>(pts, geo, (float)ph.k, (float)ph.rw, nq,
+                                                               (const float2 *)u, ldu, S, s0, nsplit, part);
+        else
+            field_far_kernel<double><<<grid, kFieldNT, 0, st>>>(pts, geo, ph.k, ph.rw, nq,
+                                                                (const double2 *)u, ldu, S, s0, nsplit, part);
+        count_launch();
+        KERNEL_CHECK();
+    }
+    double2 *np = nullptr;
+    if (ph.near_eta > 0.0 && near_part) {
+        dim3 g2((pts.R + kNearWarps - 1) / kNearWarps);
+        if (prec == BEM_PREC_C64)
+            field_near_kernel<float2><<<g2, 32 * kNearWarps, 0, st>>>(pts, geo, ph, nq, (const float2 *)u, ldu, S, near_part);
+        else
+            field_near_kernel<double2><<<g2, 32 * kNearWarps, 0, st>>>(pts, geo, ph, nq, (const double2 *)u, ldu, S, near_part);
+        count_launch();
+        KERNEL_CHECK();
+        np = near_part;
+    }
+    int tot = pts.R * S;
+    field_finalize_kernel<<<(tot + 255) / 256, 256, 0, st>>>(pts, S, nsplit, ph.k, srcs, part, np, out);
+    count_launch();
+    KERNEL_CHECK();
+}
+
+}  // namespace bem

@@ -1,0 +1,125 @@
+// Launch wrappers for the quadrature kernels (kernels.cu) and the linear
+// algebra kernels (linalg.cu).  All launches go on the given stream.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "bem_common.h"
+
+namespace bem {
+
+// Incident field record on the device (same layout as bem_source_t).
+struct DevSource {
+    int kind;
+    double vec[3];
+    double amp_re, amp_im;
+};
+
+struct GeoTables {
+    const float4 *geo_f;      // 7 float4 per element (layout in kernels.cu)
+    const double *geo_d;      // 18 doubles per element
+    const int4 *elems;        // (n0, n1, n2, 0)
+    int E;
+};
+
+struct RowPoints {
+    const float4 *f;          // 2 per point: hi = (x, y, z, 0) floats, lo = remainders
+    const double *d;          // 3 doubles per point
+    int R;                    // number of points (rows)
+};
+
+struct TileSet {
+    const TileRec *recs;      // all tiles' records
+    const int *rec_ptr;       // ntiles + 1 offsets into recs
+    const int *cols;          // ntiles * tc_max tile-local column -> global column (node index)
+    const int *col_cnt;       // ntiles: columns in each tile
+    int ntiles;
+    int tc_max;
+};
+
+struct Physics {
+    double k;
+    double rw;                // density * omega = density * k * speed
+    int near_depth;
+    double near_eta;
+};
+
+// Upload the Gauss rule of the given order to this device's constant memory
+// (no-op when already current on the device).
+void ensure_quadrature(int order);
+int quadrature_points();      // order^2 of the uploaded rule
+
+// Element tables from nodes/elements/bc.  near_eta scales the near-pair
+// radius stored in the float table.
+void launch_elem_setup(const double *d_nodes, const int4 *d_elems, const double *d_bc, int E,
+                       double near_eta, float4 *geo_f, double *geo_d, cudaStream_t st);
+
+// Far-field assembly.  c64: FP32 quadrature, acc/partials in float.  c128: FP64.
+constexpr int kGeoFloat4 = 7;     // float4 per element in GeoTables::geo_f
+constexpr int kGeoDouble = 18;    // doubles per element in GeoTables::geo_d
+size_t far_smem_bytes(int prec, int tc);
+int far_rows_per_cta(int prec);
+void launch_far_assembly(int prec, const RowPoints &rows, int N, const GeoTables &geo,
+                         const TileSet &tiles, const Physics &ph, void *A, size_t lda,
+                         void *c_part, void *beta_part, cudaStream_t st);
+
+// Near-field (singular + near-singular, FP64) assembly and row finalisation:
+// adds the near contributions to A, the diagonal term 1 - sum c, and writes
+// B[s*R + row] = p_inc_s(x) - beta (c128, column-major R x S).
+void launch_near_assembly(int prec, const RowPoints &rows, int N, const GeoTables &geo,
+                          const Physics &ph, void *A, size_t lda, const void *c_part,
+                          const void *beta_part, int ntiles, const DevSource *srcs, int S,
+                          double2 *B, cudaStream_t st);
+
+// Field evaluation.  u: surface solution, column-major N x S (u[s*ldu + node]),
+// c64 or c128 per prec.  out[s*P + p] (c128) = p_inc_s(x_p) - sum_e(...);
+// part holds nsplit*P*S partial sums, near_part P*S (used when eta > 0).
+void launch_field(int prec, const RowPoints &pts, const GeoTables &geo, const Physics &ph,
+                  const void *u, size_t ldu, int S, const DevSource *srcs, double2 *part, int nsplit,
+                  double2 *near_part, double2 *out, cudaStream_t st);
+
+// ---- linear algebra (linalg.cu) ----
+// y = A x for row-major A (R x N, lda) in c64 with FP32 accumulation; x and y
+// are c64 or c128 (xd/yd flags: 1 means c128).
+void launch_gemv_c64(int R, int N, const float2 *A, size_t lda, const void *x, int xd, void *y,
+                     int yd, cudaStream_t st);
+// w = A^H u (N), two-pass column-block reduction through `part`
+// (nsplit x N c64 or c128).
+int gemv_h_splits(int R, int N);
+// conj = false gives w = A^T u (used on a column-major matrix viewed as the
+// row-major transpose).
+void launch_gemv_h_c64(int R, int N, const float2 *A, size_t lda, const void *u, int ud,
+                       void *w, int wd, void *part, cudaStream_t st, bool conj = true);
+int gemv_h_f64_splits(int R, int N);
+// FP64 accumulation variants (the refinement residuals): A is c64 or c128.
+void launch_resid(int prec, int R, int N, const void *A, size_t lda, const double2 *x,
+                  const double2 *b, double2 *r, cudaStream_t st);                // r = b - A x
+void launch_gemv_h_f64(int prec, int R, int N, const void *A, size_t lda, const double2 *u,
+                       double2 *w, double2 *part, cudaStream_t st);               // w = A^H u
+// Row-major (R x N) -> column-major (R x N, ld_out) copy with conversion.
+void launch_to_colmajor(int prec_in, const void *A, size_t lda, int R, int N, int prec_out,
+                        void *out, size_t ld_out, cudaStream_t st);
+
+// GMRES building blocks on FP64 vectors of length n.
+void launch_dots(int n, int k, const double2 *V, size_t ldv, const double2 *w, double2 *h,
+                 double2 *part, cudaStream_t st);            // h[j] = V_j^H w, j < k
+void launch_update(int n, int k, const double2 *V, size_t ldv, const double2 *h, double2 *w,
+                   cudaStream_t st);                          // w -= V h
+void launch_nrm2(int n, const double2 *w, double *out, double *part, cudaStream_t st);
+void launch_scale_copy(int n, const double2 *w, const double *nrm, double2 *v, cudaStream_t st);
+void launch_axpy_combo(int n, int k, const double2 *V, size_t ldv, const double2 *y, double2 *x,
+                       cudaStream_t st);                      // x += V y
+void launch_copy_f64(int n, const double2 *src, double2 *dst, cudaStream_t st);
+void launch_zero_f64(size_t n, double2 *dst, cudaStream_t st);
+void launch_cast(int n, const double2 *src, float2 *dst, cudaStream_t st);
+void launch_cast_up(int n, const float2 *src, double2 *dst, cudaStream_t st);
+// H[0..j, j] = h1 + h2 (h2 may be null), H[j+1, j] = *nrm.
+void launch_hcol_finish(int j, const double2 *h1, const double2 *h2, const double *nrm, double2 *H,
+                        int ldh, cudaStream_t st);
+// Apply rotations 0..j-1 to column j, form rotation j, update g; *res = |g[j+1]|.
+void launch_givens(int j, double2 *H, int ldh, double2 *cs, double2 *sn, double2 *g, double *res,
+                   cudaStream_t st);
+void launch_trisolve(int k, const double2 *H, int ldh, const double2 *g, double2 *y, cudaStream_t st);
+void launch_set_scalar_c(double2 *dst, const double *v, cudaStream_t st);   // *dst = (*v, 0)
+
+}  // namespace bem

@@ -1,0 +1,522 @@
+// Dense linear-algebra kernels on the row-major system matrix A (rows =
+// collocation points, N columns = nodes): matrix-vector products in FP32
+// (c64 storage, the GMRES inner products) and FP64 accumulation (the
+// refinement residuals), and the FP64 vector kernels of GMRES (Arnoldi with
+// classical Gram-Schmidt applied twice, Givens rotations, back substitution).
+// These replace the reference's per-iteration host round trips in GMRES.cu
+// (which re-uploads A every Arnoldi step, GMRES.cu:106-108) with
+// device-resident state.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "bem_common.h"
+#include "kernels.h"
+
+namespace bem {
+
+namespace {
+
+__device__ __forceinline__ float2 ld_as_f2(const float2 *p, size_t i) { return p[i]; }
+__device__ __forceinline__ float2 ld_as_f2(const double2 *p, size_t i) {
+    double2 v = p[i];
+    return make_float2((float)v.x, (float)v.y);
+}
+__device__ __forceinline__ double2 ld_as_d2(const float2 *p, size_t i) {
+    float2 v = p[i];
+    return make_double2(v.x, v.y);
+}
+__device__ __forceinline__ double2 ld_as_d2(const double2 *p, size_t i) { return p[i]; }
+__device__ __forceinline__ void st_c(float2 *p, size_t i, double re, double im) {
+    p[i] = make_float2((float)re, (float)im);
+}
+__device__ __forceinline__ void st_c(double2 *p, size_t i, double re, double im) {
+    p[i] = make_double2(re, im);
+}
+
+// y = A x, one warp per row, FP32 accumulation, 16-byte loads of A (two
+// complex entries per load).
+template <typename TX, typename TY>
+__global__ void __launch_bounds__(256)
+gemv_c64_kernel(int R, int N, const float2 *__restrict__ A, size_t lda, const TX *__restrict__ x,
+                TY *__restrict__ y) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int row = blockIdx.x * 8 + warp;
+    if (row >= R) return;
+    const float2 *a = A + (size_t)row * lda;
+    float sr = 0.f, si = 0.f;
+    const int N2 = N >> 1;
+    const float4 *a4 = reinterpret_cast<const float4 *>(a);
+#pragma unroll 4
+    for (int j2 = lane; j2 < N2; j2 += 32) {
+        float4 v = __ldcs(a4 + j2);          // streamed: A is read once per product
+        float2 x0 = ld_as_f2(x, 2 * (size_t)j2), x1 = ld_as_f2(x, 2 * (size_t)j2 + 1);
+        sr = fmaf(v.x, x0.x, sr); sr = fmaf(-v.y, x0.y, sr);
+        si = fmaf(v.x, x0.y, si); si = fmaf(v.y, x0.x, si);
+        sr = fmaf(v.z, x1.x, sr); sr = fmaf(-v.w, x1.y, sr);
+        si = fmaf(v.z, x1.y, si); si = fmaf(v.w, x1.x, si);
+    }
+    if ((N & 1) && lane == 0) {
+        float2 v = a[N - 1], x0 = ld_as_f2(x, N - 1);
+        sr = fmaf(v.x, x0.x, sr); sr = fmaf(-v.y, x0.y, sr);
+        si = fmaf(v.x, x0.y, si); si = fmaf(v.y, x0.x, si);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        sr += __shfl_xor_sync(0xffffffffu, sr, o);
+        si += __shfl_xor_sync(0xffffffffu, si, o);
+    }
+    if (lane == 0) st_c(y, row, sr, si);
+}
+
+// Partial w = A^H u over a row range: each thread owns two adjacent columns.
+constexpr int kHNT = 256;
+constexpr int kHCols = 2 * kHNT;
+
+template <typename TU, typename TP, bool CONJ>
+__global__ void __launch_bounds__(kHNT)
+gemv_h_part_kernel(int R, int N, const float2 *__restrict__ A, size_t lda, const TU *__restrict__ u,
+                   int nsplit, TP *__restrict__ part) {
+    const int c = blockIdx.x * kHCols + 2 * threadIdx.x;
+    const int split = blockIdx.y;
+    const int per = (R + nsplit - 1) / nsplit;
+    const int r0 = split * per, r1 = min(R, r0 + per);
+    float s0r = 0, s0i = 0, s1r = 0, s1i = 0;
+    if (c + 1 < N) {
+        for (int r = r0; r < r1; r++) {
+            float4 v = __ldcs(reinterpret_cast<const float4 *>(A + (size_t)r * lda + c));
+            if (!CONJ) { v.y = -v.y; v.w = -v.w; }
+            float2 uu = ld_as_f2(u, r);
+            // conj(a) * u
+            s0r = fmaf(v.x, uu.x, s0r); s0r = fmaf(v.y, uu.y, s0r);
+            s0i = fmaf(v.x, uu.y, s0i); s0i = fmaf(-v.y, uu.x, s0i);
+            s1r = fmaf(v.z, uu.x, s1r); s1r = fmaf(v.w, uu.y, s1r);
+            s1i = fmaf(v.z, uu.y, s1i); s1i = fmaf(-v.w, uu.x, s1i);
+        }
+    } else if (c < N) {
+        for (int r = r0; r < r1; r++) {
+            float2 v = A[(size_t)r * lda + c];
+            if (!CONJ) v.y = -v.y;
+            float2 uu = ld_as_f2(u, r);
+            s0r = fmaf(v.x, uu.x, s0r); s0r = fmaf(v.y, uu.y, s0r);
+            s0i = fmaf(v.x, uu.y, s0i); s0i = fmaf(-v.y, uu.x, s0i);
+        }
+    }
+    if (c < N) st_c(part, (size_t)split * N + c, s0r, s0i);
+    if (c + 1 < N) st_c(part, (size_t)split * N + c + 1, s1r, s1i);
+}
+
+template <typename TP, typename TW>
+__global__ void sum_splits_kernel(int N, int nsplit, const TP *__restrict__ part, TW *__restrict__ w) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= N) return;
+    double sr = 0, si = 0;
+    for (int t = 0; t < nsplit; t++) {
+        double2 v = ld_as_d2(part, (size_t)t * N + j);
+        sr += v.x;
+        si += v.y;
+    }
+    st_c(w, j, sr, si);
+}
+
+// r = b - A x with FP64 accumulation (A c64 or c128), one warp per row.
+template <typename TA>
+__global__ void __launch_bounds__(256)
+resid_kernel(int R, int N, const TA *__restrict__ A, size_t lda, const double2 *__restrict__ x,
+             const double2 *__restrict__ b, double2 *__restrict__ r) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int row = blockIdx.x * 8 + warp;
+    if (row >= R) return;
+    const TA *a = A + (size_t)row * lda;
+    double sr = 0, si = 0;
+#pragma unroll 4
+    for (int j = lane; j < N; j += 32) {
+        double2 v = ld_as_d2(a, j);
+        double2 xx = x[j];
+        sr = fma(v.x, xx.x, sr); sr = fma(-v.y, xx.y, sr);
+        si = fma(v.x, xx.y, si); si = fma(v.y, xx.x, si);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        sr += __shfl_xor_sync(0xffffffffu, sr, o);
+        si += __shfl_xor_sync(0xffffffffu, si, o);
+    }
+    if (lane == 0) r[row] = make_double2(b[row].x - sr, b[row].y - si);
+}
+
+// Partial w = A^H u with FP64 accumulation, one column per thread.
+template <typename TA>
+__global__ void __launch_bounds__(256)
+gemv_h_f64_part_kernel(int R, int N, const TA *__restrict__ A, size_t lda, const double2 *__restrict__ u,
+                       int nsplit, double2 *__restrict__ part) {
+    const int c = blockIdx.x * 256 + threadIdx.x;
+    const int split = blockIdx.y;
+    const int per = (R + nsplit - 1) / nsplit;
+    const int r0 = split * per, r1 = min(R, r0 + per);
+    if (c >= N) return;
+    double sr = 0, si = 0;
+    for (int r = r0; r < r1; r++) {
+        double2 v = ld_as_d2(A + (size_t)r * lda, c);
+        double2 uu = u[r];
+        sr = fma(v.x, uu.x, sr); sr = fma(v.y, uu.y, sr);
+        si = fma(v.x, uu.y, si); si = fma(-v.y, uu.x, si);
+    }
+    part[(size_t)split * N + c] = make_double2(sr, si);
+}
+
+// Row-major -> column-major with type conversion, 32x32 tiles.
+template <typename TI, typename TO>
+__global__ void to_colmajor_kernel(const TI *__restrict__ A, size_t lda, int R, int N, TO *__restrict__ out,
+                                   size_t ldo) {
+    __shared__ double2 tile[32][33];
+    const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        int r = r0 + i, c = c0 + threadIdx.x;
+        if (r < R && c < N) tile[i][threadIdx.x] = ld_as_d2(A + (size_t)r * lda, c);
+    }
+    __syncthreads();
+    for (int i = threadIdx.y; i < 32; i += blockDim.y) {
+        int c = c0 + i, r = r0 + threadIdx.x;
+        if (r < R && c < N) {
+            double2 v = tile[threadIdx.x][i];
+            st_c(out, (size_t)c * ldo + r, v.x, v.y);
+        }
+    }
+}
+
+// ---- FP64 vector kernels for GMRES ----
+__global__ void dots_kernel(int n, const double2 *__restrict__ V, size_t ldv, const double2 *__restrict__ w,
+                            double2 *__restrict__ h) {
+    const int j = blockIdx.x;
+    const double2 *v = V + (size_t)j * ldv;
+    double sr = 0, si = 0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double2 a = v[i], b = w[i];
+        sr += a.x * b.x + a.y * b.y;       // conj(a) * b
+        si += a.x * b.y - a.y * b.x;
+    }
+    __shared__ double rr[32], ri[32];
+    for (int o = 16; o > 0; o >>= 1) {
+        sr += __shfl_xor_sync(0xffffffffu, sr, o);
+        si += __shfl_xor_sync(0xffffffffu, si, o);
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) { rr[warp] = sr; ri[warp] = si; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0, b = 0;
+        for (int t = 0; t < (int)(blockDim.x >> 5); t++) { a += rr[t]; b += ri[t]; }
+        h[j] = make_double2(a, b);
+    }
+}
+
+__global__ void update_kernel(int n, int k, const double2 *__restrict__ V, size_t ldv,
+                              const double2 *__restrict__ h, double2 *__restrict__ w) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double sr = 0, si = 0;
+    for (int j = 0; j < k; j++) {
+        double2 a = V[(size_t)j * ldv + i], c = h[j];
+        sr += a.x * c.x - a.y * c.y;
+        si += a.x * c.y + a.y * c.x;
+    }
+    double2 ww = w[i];
+    w[i] = make_double2(ww.x - sr, ww.y - si);
+}
+
+__global__ void axpy_combo_kernel(int n, int k, const double2 *__restrict__ V, size_t ldv,
+                                  const double2 *__restrict__ y, double2 *__restrict__ x) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double sr = 0, si = 0;
+    for (int j = 0; j < k; j++) {
+        double2 a = V[(size_t)j * ldv + i], c = y[j];
+        sr += a.x * c.x - a.y * c.y;
+        si += a.x * c.y + a.y * c.x;
+    }
+    double2 xx = x[i];
+    x[i] = make_double2(xx.x + sr, xx.y + si);
+}
+
+__global__ void nrm2_kernel(int n, const double2 *__restrict__ w, double *__restrict__ out) {
+    double s = 0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) s += w[i].x * w[i].x + w[i].y * w[i].y;
+    __shared__ double red[32];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) red[warp] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0;
+        for (int t = 0; t < (int)(blockDim.x >> 5); t++) a += red[t];
+        *out = sqrt(a);
+    }
+}
+
+__global__ void scale_copy_kernel(int n, const double2 *__restrict__ w, const double *__restrict__ nrm,
+                                  double2 *__restrict__ v) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double s = *nrm;
+    double inv = s > 0 ? 1.0 / s : 0.0;
+    v[i] = make_double2(w[i].x * inv, w[i].y * inv);
+}
+
+__global__ void copy_f64_kernel(int n, const double2 *__restrict__ s, double2 *__restrict__ d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) d[i] = s[i];
+}
+__global__ void zero_f64_kernel(size_t n, double2 *__restrict__ d) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) d[i] = make_double2(0.0, 0.0);
+}
+__global__ void cast_kernel(int n, const double2 *__restrict__ s, float2 *__restrict__ d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) d[i] = make_float2((float)s[i].x, (float)s[i].y);
+}
+__global__ void cast_up_kernel(int n, const float2 *__restrict__ s, double2 *__restrict__ d) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) d[i] = make_double2(s[i].x, s[i].y);
+}
+
+
+// ---- small dense GMRES state on the device (one thread) ----
+// H is (m+1) x m column-major (ldh), rotations cs/sn, rhs g (m+1).
+__global__ void hcol_finish_kernel(int j, const double2 *__restrict__ h1, const double2 *__restrict__ h2,
+                                   const double *__restrict__ nrm, double2 *__restrict__ H, int ldh) {
+    const int i = threadIdx.x;
+    for (int t = i; t <= j; t += blockDim.x)
+        H[(size_t)j * ldh + t] = make_double2(h1[t].x + (h2 ? h2[t].x : 0.0), h1[t].y + (h2 ? h2[t].y : 0.0));
+    if (i == 0) H[(size_t)j * ldh + j + 1] = make_double2(*nrm, 0.0);
+}
+
+// Complex Givens rotations as in GMRES.cu:44-88: c = conj(rho)/mag,
+// s = conj(sigma)/mag; previous rotations applied as
+// [h_l; h_l+1] <- [c h_l + s h_l+1; -conj(s) h_l + conj(c) h_l+1].
+__global__ void givens_kernel(int j, double2 *__restrict__ H, int ldh, double2 *__restrict__ cs,
+                              double2 *__restrict__ sn, double2 *__restrict__ g, double *__restrict__ res) {
+    if (threadIdx.x != 0) return;
+    double2 *h = H + (size_t)j * ldh;
+    for (int l = 0; l < j; l++) {
+        double2 c = cs[l], s = sn[l], a = h[l], b = h[l + 1];
+        double2 t0 = make_double2(c.x * a.x - c.y * a.y + s.x * b.x - s.y * b.y,
+                                  c.x * a.y + c.y * a.x + s.x * b.y + s.y * b.x);
+        double2 t1 = make_double2(-(s.x * a.x + s.y * a.y) + (c.x * b.x + c.y * b.y),
+                                  -(s.x * a.y - s.y * a.x) + (c.x * b.y - c.y * b.x));
+        h[l] = t0;
+        h[l + 1] = t1;
+    }
+    double2 rho = h[j], sig = h[j + 1];
+    double mag = sqrt(rho.x * rho.x + rho.y * rho.y + sig.x * sig.x + sig.y * sig.y);
+    double2 c, s;
+    if (mag > 0) {
+        c = make_double2(rho.x / mag, -rho.y / mag);
+        s = make_double2(sig.x / mag, -sig.y / mag);
+    } else {
+        c = make_double2(1.0, 0.0);
+        s = make_double2(0.0, 0.0);
+    }
+    cs[j] = c;
+    sn[j] = s;
+    h[j] = make_double2(mag, 0.0);
+    h[j + 1] = make_double2(0.0, 0.0);
+    double2 gj = g[j];
+    g[j + 1] = make_double2(-(s.x * gj.x + s.y * gj.y), -(s.x * gj.y - s.y * gj.x));
+    g[j] = make_double2(c.x * gj.x - c.y * gj.y, c.x * gj.y + c.y * gj.x);
+    res[0] = sqrt(g[j + 1].x * g[j + 1].x + g[j + 1].y * g[j + 1].y);
+}
+
+// Back substitution R y = g (Rsolver, GMRES.cu:26-42).
+__global__ void trisolve_kernel(int k, const double2 *__restrict__ H, int ldh, const double2 *__restrict__ g,
+                                double2 *__restrict__ y) {
+    if (threadIdx.x != 0) return;
+    for (int i = k - 1; i >= 0; i--) {
+        double sr = g[i].x, si = g[i].y;
+        for (int l = i + 1; l < k; l++) {
+            double2 a = H[(size_t)l * ldh + i], b = y[l];
+            sr -= a.x * b.x - a.y * b.y;
+            si -= a.x * b.y + a.y * b.x;
+        }
+        double2 d = H[(size_t)i * ldh + i];
+        double den = d.x * d.x + d.y * d.y;
+        y[i] = make_double2((sr * d.x + si * d.y) / den, (si * d.x - sr * d.y) / den);
+    }
+}
+
+__global__ void set_scalar_c_kernel(double2 *__restrict__ dst, const double *__restrict__ v) {
+    if (threadIdx.x == 0) *dst = make_double2(*v, 0.0);
+}
+
+inline int blocks(long long n, int t) { return (int)((n + t - 1) / t); }
+
+}  // namespace
+
+void launch_gemv_c64(int R, int N, const float2 *A, size_t lda, const void *x, int xd, void *y,
+                     int yd, cudaStream_t st) {
+    if (R <= 0) return;
+    dim3 g(blocks(R, 8));
+    if (!xd && !yd) gemv_c64_kernel<float2, float2><<<g, 256, 0, st>>>(R, N, A, lda, (const float2 *)x, (float2 *)y);
+    else if (xd && !yd) gemv_c64_kernel<double2, float2><<<g, 256, 0, st>>>(R, N, A, lda, (const double2 *)x, (float2 *)y);
+    else if (!xd && yd) gemv_c64_kernel<float2, double2><<<g, 256, 0, st>>>(R, N, A, lda, (const float2 *)x, (double2 *)y);
+    else gemv_c64_kernel<double2, double2><<<g, 256, 0, st>>>(R, N, A, lda, (const double2 *)x, (double2 *)y);
+    count_launch();
+    KERNEL_CHECK();
+}
+
+int gemv_h_splits(int R, int N) {
+    int cb = (N + kHCols - 1) / kHCols;
+    int want = (4 * 152 + cb - 1) / cb;
+    return std::max(1, std::min(want, std::max(1, R / 32)));
+}
+
+void launch_gemv_h_c64(int R, int N, const float2 *A, size_t lda, const void *u, int ud, void *w,
+                       int wd, void *part, cudaStream_t st, bool conj) {
+    if (N <= 0) return;
+    int ns = gemv_h_splits(R, N);
+    dim3 g(blocks(N, kHCols), ns);
+    if (conj) {
+        if (ud) gemv_h_part_kernel<double2, float2, true><<<g, kHNT, 0, st>>>(R, N, A, lda, (const double2 *)u, ns, (float2 *)part);
+        else gemv_h_part_kernel<float2, float2, true><<<g, kHNT, 0, st>>>(R, N, A, lda, (const float2 *)u, ns, (float2 *)part);
+    } else {
+        if (ud) gemv_h_part_kernel<double2, float2, false><<<g, kHNT, 0, st>>>(R, N, A, lda, (const double2 *)u, ns, (float2 *)part);
+        else gemv_h_part_kernel<float2, float2, false><<<g, kHNT, 0, st>>>(R, N, A, lda, (const float2 *)u, ns, (float2 *)part);
+    }
+    count_launch();
+    KERNEL_CHECK();
+    if (wd) sum_splits_kernel<float2, double2><<<blocks(N, 256), 256, 0, st>>>(N, ns, (const float2 *)part, (double2 *)w);
+    else sum_splits_kernel<float2, float2><<<blocks(N, 256), 256, 0, st>>>(N, ns, (const float2 *)part, (float2 *)w);
+    count_launch();
+    KERNEL_CHECK();
+}
+
+void launch_resid(int prec, int R, int N, const void *A, size_t lda, const double2 *x,
+                  const double2 *b, double2 *r, cudaStream_t st) {
+    if (R <= 0) return;
+    if (prec == BEM_PREC_C64) resid_kernel<float2><<<blocks(R, 8), 256, 0, st>>>(R, N, (const float2 *)A, lda, x, b, r);
+    else resid_kernel<double2><<<blocks(R, 8), 256, 0, st>>>(R, N, (const double2 *)A, lda, x, b, r);
+    count_launch();
+    KERNEL_CHECK();
+}
+
+void launch_gemv_h_f64(int prec, int R, int N, const void *A, size_t lda, const double2 *u,
+                       double2 *w, double2 *part, cudaStream_t st) {
+    if (N <= 0) return;
+    int cb = blocks(N, 256);
+    int ns = std::max(1, std::min((4 * 152 + cb - 1) / cb, std::max(1, R / 16)));
+    dim3 g(cb, ns);
+    if (prec == BEM_PREC_C64) gemv_h_f64_part_kernel<float2><<<g, 256, 0, st>>>(R, N, (const float2 *)A, lda, u, ns, part);
+    else gemv_h_f64_part_kernel<double2><<<g, 256, 0, st>>>(R, N, (const double2 *)A, lda, u, ns, part);
+    count_launch();
+    KERNEL_CHECK();
+    sum_splits_kernel<double2, double2><<<blocks(N, 256), 256, 0, st>>>(N, ns, part, w);
+    count_launch();
+    KERNEL_CHECK();
+}
+
+int gemv_h_f64_splits(int R, int N) {
+    int cb = blocks(N, 256);
+    return std::max(1, std::min((4 * 152 + cb - 1) / cb, std::max(1, R / 16)));
+}
+
+void launch_to_colmajor(int prec_in, const void *A, size_t lda, int R, int N, int prec_out,
+                        void *out, size_t ld_out, cudaStream_t st) {
+    dim3 g(blocks(N, 32), blocks(R, 32)), b(32, 8);
+    if (prec_in == BEM_PREC_C64 && prec_out == BEM_PREC_C64)
+        to_colmajor_kernel<float2, float2><<<g, b, 0, st>>>((const float2 *)A, lda, R, N, (float2 *)out, ld_out);
+    else if (prec_in == BEM_PREC_C64)
+        to_colmajor_kernel<float2, double2><<<g, b, 0, st>>>((const float2 *)A, lda, R, N, (double2 *)out, ld_out);
+    else if (prec_out == BEM_PREC_C64)
+        to_colmajor_kernel<double2, float2><<<g, b, 0, st>>>((const double2 *)A, lda, R, N, (float2 *)out, ld_out);
+    else
+        to_colmajor_kernel<double2, double2><<<g, b, 0, st>>>((const double2 *)A, lda, R, N, (double2 *)out, ld_out);
+    count_launch();
+    KERNEL_CHECK();
+}
+
+void launch_dots(int n, int k, const double2 *V, size_t ldv, const double2 *w, double2 *h,
+                 double2 *, cudaStream_t st) {
+    if (k <= 0) return;
+    dots_kernel<<<k, 512, 0, st>>>(n, V, ldv, w, h);
+    count_launch();
+    KERNEL_CHECK();
+}
+
+void launch_update(int n, int k, const double2 *V, size_t ldv, const double2 *h, double2 *w,
+                   cudaStream_t st) {
+    if (k <= 0) return;
+    update_kernel<<<blocks(n, 256), 256, 0, st>>>(n, k, V, ldv, h, w);
+    count_launch();
+    KERNEL_CHECK();
+}
+
+void launch_nrm2(int n, const double2 *w, double *out, double *, cudaStream_t st) {
+    nrm2_kernel<<<1, 1024, 0, st>>>(n, w, out);
+    count_launch();
+    KERNEL_CHECK();
+}
+
+void launch_scale_copy(int n, const double2 *w, const double *nrm, double2 *v, cudaStream_t st) {
+    scale_copy_kernel<<<blocks(n, 256), 256, 0, st>>>(n, w, nrm, v);
+    count_launch();
+    KERNEL_CHECK();
+}
+
+void launch_axpy_combo(int n, int k, const double2 *V, size_t ldv, const double2 *y, double2 *x,
+                       cudaStream_t st) {
+    if (k <= 0) return;
+    axpy_combo_kernel<<<blocks(n, 256), 256, 0, st>>>(n, k, V, ldv, y, x);
+    count_launch();
+    KERNEL_CHECK();
+}
+
+void launch_copy_f64(int n, const double2 *src, double2 *dst, cudaStream_t st) {
+    copy_f64_kernel<<<blocks(n, 256), 256, 0, st>>>(n, src, dst);
+    count_launch();
+    KERNEL_CHECK();
+}
+
+void launch_zero_f64(size_t n, double2 *dst, cudaStream_t st) {
+    if (n == 0) return;
+    zero_f64_kernel<<<blocks((long long)n, 256), 256, 0, st>>>(n, dst);
+    count_launch();
+    KERNEL_CHECK();
+}
+
+void launch_cast(int n, const double2 *src, float2 *dst, cudaStream_t st) {
+    cast_kernel<<<blocks(n, 256), 256, 0, st>>>(n, src, dst);
+    count_launch();
+    KERNEL_CHECK();
+}
+
+void launch_cast_up(int n, const float2 *src, double2 *dst, cudaStream_t st) {
+    cast_up_kernel<<<blocks(n, 256), 256, 0, st>>>(n, src, dst);
+    count_launch();
+    KERNEL_CHECK();
+}
+
+
+void launch_hcol_finish(int j, const double2 *h1, const double2 *h2, const double *nrm, double2 *H,
+                        int ldh, cudaStream_t st) {
+    hcol_finish_kernel<<<1, 256, 0, st>>>(j, h1, h2, nrm, H, ldh);
+    count_launch();
+    KERNEL_CHECK();
+}
+
+void launch_givens(int j, double2 *H, int ldh, double2 *cs, double2 *sn, double2 *g, double *res,
+                   cudaStream_t st) {
+    givens_kernel<<<1, 32, 0, st>>>(j, H, ldh, cs, sn, g, res);
+    count_launch();
+    KERNEL_CHECK();
+}
+
+void launch_trisolve(int k, const double2 *H, int ldh, const double2 *g, double2 *y, cudaStream_t st) {
+    trisolve_kernel<<<1, 32, 0, st>>>(k, H, ldh, g, y);
+    count_launch();
+    KERNEL_CHECK();
+}
+
+void launch_set_scalar_c(double2 *dst, const double *v, cudaStream_t st) {
+    set_scalar_c_kernel<<<1, 32, 0, st>>>(dst, v);
+    count_launch();
+    KERNEL_CHECK();
+}
+
+}  // namespace bem

@@ -1,0 +1,364 @@
+// Host orchestration of the device-resident solver: geometry upload, column
+// tiles, assembly launches, the dense QR least-squares solve and the
+// mixed-precision refined GMRES solve.
+#include "solver.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <string>
+
+namespace bem {
+
+Globals &globals() {
+    static Globals g;
+    return g;
+}
+
+void DevMem::ensure(size_t b) {
+    if (b <= bytes && p) return;
+    release();
+    if (b == 0) return;
+    CUDA_TRY(cudaMalloc(&p, b));
+    bytes = b;
+}
+
+void DevMem::release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+}
+
+namespace {
+
+constexpr int kTileColsMax = 12288;   // columns per tile: 2 rows x 12288 x 8 B = 192 KB smem (c64)
+
+size_t round_up(size_t v, size_t m) { return (v + m - 1) / m * m; }
+
+// Morton (Z-order) key of a point inside the bounding box, 10 bits per axis.
+uint32_t morton_key(const double *p, const double *lo, const double *inv) {
+    uint32_t k = 0;
+    uint32_t q[3];
+    for (int d = 0; d < 3; d++) {
+        double t = (p[d] - lo[d]) * inv[d];
+        t = std::min(std::max(t, 0.0), 1023.0);
+        q[d] = (uint32_t)t;
+    }
+    for (int b = 9; b >= 0; b--)
+        for (int d = 0; d < 3; d++) k = (k << 1) | ((q[d] >> b) & 1u);
+    return k;
+}
+
+// Greedy vertex-disjoint colouring of the elements: elements of one colour
+// share no node, so consecutive records in a tile list rarely add to the same
+// shared-memory column in the same instruction.
+std::vector<int> color_elements(int N, const std::vector<int> &elems) {
+    int E = (int)(elems.size() / 3);
+    std::vector<int> deg(N + 1, 0);
+    for (int v : elems) deg[v + 1]++;
+    for (int i = 0; i < N; i++) deg[i + 1] += deg[i];
+    std::vector<int> adj(elems.size()), fill(deg.begin(), deg.end() - 1);
+    for (int e = 0; e < E; e++)
+        for (int j = 0; j < 3; j++) adj[fill[elems[3 * e + j]]++] = e;
+    std::vector<int> color(E, -1);
+    std::vector<int> mark;
+    for (int e = 0; e < E; e++) {
+        for (int j = 0; j < 3; j++) {
+            int v = elems[3 * e + j];
+            for (int t = deg[v]; t < deg[v + 1]; t++) {
+                int c = color[adj[t]];
+                if (c >= 0) {
+                    if ((int)mark.size() <= c) mark.resize(c + 1, -1);
+                    mark[c] = e;
+                }
+            }
+        }
+        int c = 0;
+        while (c < (int)mark.size() && mark[c] == e) c++;
+        color[e] = c;
+    }
+    return color;
+}
+
+}  // namespace
+}  // namespace bem
+
+using namespace bem;
+
+bem_solver_s::bem_solver_s() {
+    CUDA_TRY(cudaGetDevice(&device));
+    CUDA_TRY(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    if (cusolverDnCreate(&cusolver) != CUSOLVER_STATUS_SUCCESS) BEM_FAIL(BEM_ERR_CUDA, "cusolverDnCreate failed");
+    cusolverDnSetStream(cusolver, stream);
+    if (cublasCreate(&cublas) != CUBLAS_STATUS_SUCCESS) BEM_FAIL(BEM_ERR_CUDA, "cublasCreate failed");
+    cublasSetStream(cublas, stream);
+    CUDA_TRY(cudaMallocHost(&h_pinned, 64 * sizeof(double)));
+    bem_options_default(&opt);
+}
+
+bem_solver_s::~bem_solver_s() {
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (cur != device) cudaSetDevice(device);
+    if (stream) cudaStreamSynchronize(stream);
+    if (cusolver) cusolverDnDestroy(cusolver);
+    if (cublas) cublasDestroy(cublas);
+    if (h_pinned) cudaFreeHost(h_pinned);
+    if (stream) cudaStreamDestroy(stream);
+    if (cur >= 0 && cur != device) cudaSetDevice(cur);
+}
+
+void bem_solver_s::set_geometry(const double *pnts, int num_pnts, const int *elems, int num_elems,
+                                const double *bc, const double *chief, int num_chief) {
+    BEM_CHECK_ARG(pnts && elems && num_pnts > 0 && num_elems > 0, "empty geometry");
+    BEM_CHECK_ARG(num_chief >= 0 && (num_chief == 0 || chief), "bad CHIEF points");
+    for (long long i = 0; i < 3LL * num_elems; i++)
+        BEM_CHECK_ARG(elems[i] >= 0 && elems[i] < num_pnts, "element node index out of range");
+    N = num_pnts;
+    E = num_elems;
+    M = num_chief;
+    R = N + M;
+    h_nodes.assign(pnts, pnts + 3 * (size_t)N);
+    h_elems.assign(elems, elems + 3 * (size_t)E);
+    h_bc.resize(6 * (size_t)E);
+    if (bc) {
+        std::memcpy(h_bc.data(), bc, sizeof(double) * 6 * (size_t)E);
+    } else {
+        for (int e = 0; e < E; e++) {
+            double d[6] = {0, 0, 1, 0, -1, 0};
+            std::memcpy(&h_bc[6 * (size_t)e], d, sizeof(d));
+        }
+    }
+    for (int e = 0; e < E; e++)
+        BEM_CHECK_ARG(h_bc[6 * (size_t)e + 2] != 0.0 || h_bc[6 * (size_t)e + 3] != 0.0, "element with cb = 0");
+    h_rows.assign(h_nodes.begin(), h_nodes.end());
+    if (M) h_rows.insert(h_rows.end(), chief, chief + 3 * (size_t)M);
+
+    std::vector<float4> rf(2 * (size_t)R);
+    for (int i = 0; i < R; i++) {
+        float hx = (float)h_rows[3 * i], hy = (float)h_rows[3 * i + 1], hz = (float)h_rows[3 * i + 2];
+        rf[2 * i] = make_float4(hx, hy, hz, 0.f);
+        rf[2 * i + 1] = make_float4((float)(h_rows[3 * i] - hx), (float)(h_rows[3 * i + 1] - hy),
+                                    (float)(h_rows[3 * i + 2] - hz), 0.f);
+    }
+    std::vector<int4> el(E);
+    for (int e = 0; e < E; e++) el[e] = make_int4(h_elems[3 * e], h_elems[3 * e + 1], h_elems[3 * e + 2], 0);
+    d_nodes.ensure(sizeof(double) * 3 * N);
+    d_rows_d.ensure(sizeof(double) * 3 * (size_t)R);
+    d_rows_f.ensure(sizeof(float4) * 2 * (size_t)R);
+    d_elems.ensure(sizeof(int4) * E);
+    d_bc.ensure(sizeof(double) * 6 * (size_t)E);
+    d_geo_f.ensure(sizeof(float4) * kGeoFloat4 * (size_t)E);
+    d_geo_d.ensure(sizeof(double) * kGeoDouble * (size_t)E);
+    CUDA_TRY(cudaMemcpyAsync(d_nodes.p, h_nodes.data(), sizeof(double) * 3 * N, cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemcpyAsync(d_rows_d.p, h_rows.data(), sizeof(double) * 3 * (size_t)R, cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemcpyAsync(d_rows_f.p, rf.data(), sizeof(float4) * 2 * (size_t)R, cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemcpyAsync(d_elems.p, el.data(), sizeof(int4) * E, cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemcpyAsync(d_bc.p, h_bc.data(), sizeof(double) * 6 * (size_t)E, cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));   // host vectors rf/el go out of scope
+    geo_eta = -1.0;
+    tiles[0].valid = tiles[1].valid = false;
+    assembled = solved = false;
+}
+
+void bem_solver_s::set_sources(const bem_source_t *srcs, int num) {
+    BEM_CHECK_ARG(num >= 1 && srcs, "need at least one source");
+    for (int i = 0; i < num; i++)
+        BEM_CHECK_ARG(srcs[i].kind == BEM_SRC_POINT || srcs[i].kind == BEM_SRC_PLANE, "bad source kind");
+    h_srcs.assign(srcs, srcs + num);
+    S = num;
+    static_assert(sizeof(DevSource) == sizeof(bem_source_t), "source layout");
+    d_srcs.ensure(sizeof(bem_source_t) * num);
+    CUDA_TRY(cudaMemcpyAsync(d_srcs.p, h_srcs.data(), sizeof(bem_source_t) * num, cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    assembled = solved = false;
+}
+
+void bem_solver_s::ensure_geo() {
+    if (E == 0) BEM_FAIL(BEM_ERR_STATE, "no geometry set");
+    if (geo_eta == opt.near_eta) return;
+    launch_elem_setup(d_nodes.as<double>(), d_elems.as<int4>(), d_bc.as<double>(), E, opt.near_eta,
+                      d_geo_f.as<float4>(), d_geo_d.as<double>(), stream);
+    geo_eta = opt.near_eta;
+}
+
+// Column tiles of the far-field kernel.  When N fits one tile the columns
+// are the nodes in their own order (every row segment is written
+// contiguously).  Otherwise the nodes are ordered along a Morton curve and
+// cut into equal tiles, and each tile lists every element with a node in it;
+// an element straddling tiles is integrated once per tile it touches and
+// counted for the c and beta sums only in the tile of its first node.
+void bem_solver_s::ensure_tiles(int precision) {
+    Tiles &T = tiles[precision];
+    if (T.valid) return;
+    const int cap = opt.tile_cols > 0 ? std::min(opt.tile_cols, kTileColsMax) : kTileColsMax;
+    int ntiles = (N + cap - 1) / cap;
+    int per = (N + ntiles - 1) / ntiles;
+    std::vector<int> order(N);
+    std::iota(order.begin(), order.end(), 0);
+    if (ntiles > 1) {
+        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300}, inv[3];
+        for (int i = 0; i < N; i++)
+            for (int d = 0; d < 3; d++) {
+                lo[d] = std::min(lo[d], h_nodes[3 * i + d]);
+                hi[d] = std::max(hi[d], h_nodes[3 * i + d]);
+            }
+        for (int d = 0; d < 3; d++) inv[d] = hi[d] > lo[d] ? 1023.0 / (hi[d] - lo[d]) : 0.0;
+        std::vector<uint32_t> key(N);
+        for (int i = 0; i < N; i++) key[i] = morton_key(&h_nodes[3 * i], lo, inv);
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return key[a] < key[b]; });
+    }
+    std::vector<int> tile_of(N), slot_of(N);
+    std::vector<int> cols((size_t)ntiles * per, 0), cnt(ntiles, 0);
+    for (int i = 0; i < N; i++) {
+        int t = i / per, s = i - t * per;
+        tile_of[order[i]] = t;
+        slot_of[order[i]] = s;
+        cols[(size_t)t * per + s] = order[i];
+        cnt[t]++;
+    }
+    std::vector<int> color = color_elements(N, h_elems);
+    std::vector<std::vector<TileRec>> lists(ntiles);
+    for (int e = 0; e < E; e++) {
+        const int *nd = &h_elems[3 * (size_t)e];
+        int seen[3] = {-1, -1, -1}, ns = 0;
+        for (int j = 0; j < 3; j++) {
+            int t = tile_of[nd[j]];
+            bool dup = false;
+            for (int q = 0; q < ns; q++) dup |= seen[q] == t;
+            if (dup) continue;
+            seen[ns++] = t;
+            TileRec r;
+            r.eid = e;
+            for (int q = 0; q < 3; q++) {
+                r.node[q] = nd[q];
+                r.slot[q] = tile_of[nd[q]] == t ? slot_of[nd[q]] : -1;
+            }
+            r.owner = (t == tile_of[nd[0]]) ? 1 : 0;
+            lists[t].push_back(r);
+        }
+    }
+    std::vector<TileRec> recs;
+    std::vector<int> ptr(ntiles + 1, 0);
+    for (int t = 0; t < ntiles; t++) {
+        std::stable_sort(lists[t].begin(), lists[t].end(),
+                         [&](const TileRec &a, const TileRec &b) { return color[a.eid] < color[b.eid]; });
+        ptr[t + 1] = ptr[t] + (int)lists[t].size();
+        recs.insert(recs.end(), lists[t].begin(), lists[t].end());
+    }
+    T.recs.ensure(sizeof(TileRec) * recs.size());
+    T.rec_ptr.ensure(sizeof(int) * ptr.size());
+    T.cols.ensure(sizeof(int) * cols.size());
+    T.col_cnt.ensure(sizeof(int) * cnt.size());
+    CUDA_TRY(cudaMemcpyAsync(T.recs.p, recs.data(), sizeof(TileRec) * recs.size(), cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemcpyAsync(T.rec_ptr.p, ptr.data(), sizeof(int) * ptr.size(), cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemcpyAsync(T.cols.p, cols.data(), sizeof(int) * cols.size(), cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemcpyAsync(T.col_cnt.p, cnt.data(), sizeof(int) * cnt.size(), cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    T.ntiles = ntiles;
+    T.tc_max = per;
+    T.valid = true;
+}
+
+GeoTables bem_solver_s::geo_tables() const {
+    return GeoTables{d_geo_f.as<float4>(), d_geo_d.as<double>(), d_elems.as<int4>(), E};
+}
+
+RowPoints bem_solver_s::row_points() const { return RowPoints{d_rows_f.as<float4>(), d_rows_d.as<double>(), R}; }
+
+Physics bem_solver_s::physics() const {
+    return Physics{k, opt.density * k * opt.speed, opt.near_depth, opt.near_eta};
+}
+
+void bem_solver_s::assemble(double kk, int precision) {
+    BEM_CHECK_ARG(precision == BEM_PREC_C64 || precision == BEM_PREC_C128, "bad precision");
+    BEM_CHECK_ARG(std::isfinite(kk) && kk > 0, "wavenumber must be positive");
+    if (E == 0) BEM_FAIL(BEM_ERR_STATE, "no geometry set");
+    if (S == 0) BEM_FAIL(BEM_ERR_STATE, "no sources set");
+    ensure_quadrature(opt.order);
+    ensure_geo();
+    ensure_tiles(precision);
+    k = kk;
+    prec = precision;
+    const Tiles &T = tiles[precision];
+    size_t esz = precision == BEM_PREC_C64 ? sizeof(float2) : sizeof(double2);
+    size_t rsz = precision == BEM_PREC_C64 ? sizeof(float) : sizeof(double);
+    lda = round_up(N, 8);
+    d_A.ensure(esz * lda * (size_t)R);
+    d_B.ensure(sizeof(double2) * (size_t)R * S);
+    d_cpart.ensure(rsz * (size_t)T.ntiles * R);
+    d_bpart.ensure(2 * rsz * (size_t)T.ntiles * R);
+    TileSet ts{T.recs.as<TileRec>(), T.rec_ptr.as<int>(), T.cols.as<int>(), T.col_cnt.as<int>(), T.ntiles, T.tc_max};
+    Physics ph = physics();
+    launch_far_assembly(precision, row_points(), N, geo_tables(), ts, ph, d_A.p, lda, d_cpart.p, d_bpart.p, stream);
+    launch_near_assembly(precision, row_points(), N, geo_tables(), ph, d_A.p, lda, d_cpart.p, d_bpart.p,
+                         T.ntiles, d_srcs.as<DevSource>(), S, d_B.as<double2>(), stream);
+    assembled = true;
+    solved = false;
+}
+
+void bem_solver_s::solve(int method, bem_solve_info_t *info) {
+    if (!assembled) BEM_FAIL(BEM_ERR_STATE, "solve before assemble");
+    BEM_CHECK_ARG(R >= N, "fewer rows than unknowns");
+    d_x.ensure(sizeof(double2) * (size_t)N * S);
+    if (method == BEM_SOLVE_QR) {
+        solve_qr();
+        if (info) { info->iterations = 0; info->refinements = 0; info->rel_residual = 0; info->converged = 1; }
+    } else if (method == BEM_SOLVE_GMRES_REFINED) {
+        if (prec != BEM_PREC_C64) BEM_FAIL(BEM_ERR_STATE, "refined GMRES needs a c64 assembly");
+        solve_refined(info);
+    } else {
+        BEM_FAIL(BEM_ERR_INVALID_ARG, "unknown solve method");
+    }
+    solved = true;
+}
+
+void bem_solver_s::get_solution(void *x, int ldx, int precision) {
+    if (!solved) BEM_FAIL(BEM_ERR_STATE, "no solution");
+    BEM_CHECK_ARG(x && ldx >= N, "bad solution buffer");
+    std::vector<double2> h((size_t)N * S);
+    CUDA_TRY(cudaMemcpyAsync(h.data(), d_x.p, sizeof(double2) * h.size(), cudaMemcpyDeviceToHost, stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    for (int s = 0; s < S; s++)
+        for (int i = 0; i < N; i++) {
+            double2 v = h[(size_t)s * N + i];
+            if (precision == BEM_PREC_C64) {
+                ((float *)x)[2 * ((size_t)s * ldx + i)] = (float)v.x;
+                ((float *)x)[2 * ((size_t)s * ldx + i) + 1] = (float)v.y;
+            } else {
+                ((double *)x)[2 * ((size_t)s * ldx + i)] = v.x;
+                ((double *)x)[2 * ((size_t)s * ldx + i) + 1] = v.y;
+            }
+        }
+}
+
+void bem_solver_s::get_system(void *A, int lda_out, void *B, int ldb_out, int precision) {
+    if (!assembled) BEM_FAIL(BEM_ERR_STATE, "no system assembled");
+    BEM_CHECK_ARG(precision == BEM_PREC_C64 || precision == BEM_PREC_C128, "bad precision");
+    size_t esz = precision == BEM_PREC_C64 ? sizeof(float2) : sizeof(double2);
+    if (A) {
+        BEM_CHECK_ARG(lda_out >= R, "lda smaller than N+M");
+        q_A.ensure(esz * (size_t)R * N);
+        launch_to_colmajor(prec, d_A.p, lda, R, N, precision, q_A.p, R, stream);
+        CUDA_TRY(cudaMemcpy2DAsync(A, esz * lda_out, q_A.p, esz * R, esz * R, N, cudaMemcpyDeviceToHost, stream));
+    }
+    if (B) {
+        BEM_CHECK_ARG(ldb_out >= R, "ldb smaller than N+M");
+        std::vector<double2> hb((size_t)R * S);
+        CUDA_TRY(cudaMemcpyAsync(hb.data(), d_B.p, sizeof(double2) * hb.size(), cudaMemcpyDeviceToHost, stream));
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        for (int s = 0; s < S; s++)
+            for (int r = 0; r < R; r++) {
+                double2 v = hb[(size_t)s * R + r];
+                if (precision == BEM_PREC_C64) {
+                    ((float *)B)[2 * ((size_t)s * ldb_out + r)] = (float)v.x;
+                    ((float *)B)[2 * ((size_t)s * ldb_out + r) + 1] = (float)v.y;
+                } else {
+                    ((double *)B)[2 * ((size_t)s * ldb_out + r)] = v.x;
+                    ((double *)B)[2 * ((size_t)s * ldb_out + r) + 1] = v.y;
+                }
+            }
+    }
+    CUDA_TRY(cudaStreamSynchronize(stream));
+}

@@ -1,0 +1,97 @@
+// Device-resident solver state behind bem_solver_t.
+#pragma once
+
+#include <cublas_v2.h>
+#include <cusolverDn.h>
+
+#include <mutex>
+#include <vector>
+
+#include "bem_common.h"
+#include "kernels.h"
+#include "mesh.h"
+
+namespace bem {
+
+// Process-wide defaults set by the reference-style global calls
+// (gaussQuad::sendToDevice, the STRENGTH macro, the density/speed constants).
+struct Globals {
+    std::mutex mu;
+    int order = 6;
+    double density = 1.2041;
+    double speed = 343.21;
+    double strength = 0.0;
+};
+Globals &globals();
+
+// Owning device allocation that only grows.
+struct DevMem {
+    void *p = nullptr;
+    size_t bytes = 0;
+    void ensure(size_t b);
+    void release();
+    ~DevMem() { release(); }
+    template <class T> T *as() const { return static_cast<T *>(p); }
+};
+
+}  // namespace bem
+
+struct bem_solver_s {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cusolverDnHandle_t cusolver = nullptr;
+    cublasHandle_t cublas = nullptr;
+    bem_options_t opt{};
+
+    int N = 0, M = 0, E = 0, S = 0, R = 0;
+    std::vector<double> h_nodes, h_rows, h_bc;
+    std::vector<int> h_elems;
+    std::vector<bem_source_t> h_srcs;
+
+    bem::DevMem d_nodes, d_rows_f, d_rows_d, d_elems, d_bc, d_geo_f, d_geo_d, d_srcs;
+    double geo_eta = -1.0;   // near_eta the element tables were built with
+
+    struct Tiles {
+        bool valid = false;
+        int ntiles = 0, tc_max = 0;
+        bem::DevMem recs, rec_ptr, cols, col_cnt;
+    } tiles[2];
+
+    int prec = -1;
+    double k = 0.0;
+    size_t lda = 0;
+    bool assembled = false, solved = false;
+    bem::DevMem d_A, d_B, d_cpart, d_bpart, d_x;
+
+    // GMRES / refinement workspace
+    bem::DevMem w_V, w_H, w_cs, w_sn, w_g, w_y, w_h1, w_h2, w_w, w_t, w_r, w_gv, w_part, w_scal;
+    double *h_pinned = nullptr;
+    // QR workspace
+    bem::DevMem q_A, q_B, q_tau, q_work, q_info;
+    // field workspace
+    bem::DevMem f_rows_f, f_rows_d, f_part, f_near, f_out, f_u;
+
+    bem_solver_s();
+    ~bem_solver_s();
+
+    void set_geometry(const double *pnts, int num_pnts, const int *elems, int num_elems,
+                      const double *bc, const double *chief, int num_chief);
+    void set_sources(const bem_source_t *srcs, int num);
+    void assemble(double k, int precision);
+    void solve(int method, bem_solve_info_t *info);
+    void get_solution(void *x, int ldx, int precision);
+    void get_system(void *A, int lda_out, void *B, int ldb_out, int precision);
+    // Field at host points; u_dev: surface solution on the device in
+    // precision u_prec (column-major N x S, ld = N), or null for the solver's
+    // own solution.
+    void eval_field(const double *pts, int num_pts, void *out, int ldo, int precision,
+                    const void *u_dev = nullptr, int u_prec = BEM_PREC_C128);
+
+    void ensure_geo();
+    void ensure_tiles(int precision);
+    bem::GeoTables geo_tables() const;
+    bem::RowPoints row_points() const;
+    bem::Physics physics() const;
+    void solve_qr();
+    void solve_refined(bem_solve_info_t *info);
+};

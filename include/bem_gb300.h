@@ -1,0 +1,197 @@
+/*
+ * bem_gb300.h -- C ABI of the GB300-native Helmholtz BEM engine.
+ *
+ * Plain pointers, sizes and opaque handles only.  Complex arrays are
+ * interleaved (re, im) pairs of float (c64) or double (c128).  Matrices are
+ * column-major with a leading dimension: entry (r, c) at ld*c + r, the
+ * reference's IDXC0 (numerical.h:44-46).
+ *
+ * Every call returns a status code.  BEM_SUCCESS (0) and BEM_FAILURE (1) are
+ * EXIT_SUCCESS and EXIT_FAILURE, the only values the reference returns
+ * (numerical.h:59-122); the other codes refine the failure, and
+ * bem_last_error() gives a message for the calling thread.
+ *
+ * Each declaration cites the reference function it replaces, as
+ * file:line within ZiqiFrancisFan/BEM_GPU_Clean_CPP.
+ */
+#ifndef BEM_GB300_H
+#define BEM_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BEM_SUCCESS 0
+#define BEM_FAILURE 1
+#define BEM_ERR_INVALID_ARG 2
+#define BEM_ERR_CUDA 3
+#define BEM_ERR_NOMEM 4
+#define BEM_ERR_NOT_CONVERGED 5
+#define BEM_ERR_IO 6
+#define BEM_ERR_STATE 7
+#define BEM_ERR_TOO_LARGE 8
+#define BEM_ERR_NUMERIC 9
+
+/* Library status and introspection (no reference counterpart). */
+const char *bem_status_string(int status);
+const char *bem_last_error(void);
+int bem_version(void);
+/* Number of CUDA kernels this library has launched in the process. */
+long long bem_launch_count(void);
+
+/* ------------------------------------------------------------------ */
+/* Quadrature: gaussQuad (numerical.h:166-187)                          */
+/* ------------------------------------------------------------------ */
+/* Gauss-Legendre nodes/weights on [-1,1], ascending: gaussQuad::
+ * genGaussParams (numerical.cu:186-225). */
+int bem_gauss_legendre(int order, double *nodes, double *weights);
+/* Default Gauss order for new solvers and the drop-in calls:
+ * gaussQuad(order) + sendToDevice() (numerical.cu:152-156, 227-231). */
+int bem_set_quadrature(int order);
+int bem_get_quadrature(void);
+/* Medium constants: __constant__ density/speed (numerical.cu:12-14). */
+int bem_set_medium(double density, double speed);
+/* Point-source strength q in p_inc = q*G: the STRENGTH macro
+ * (numerical.h:128-130), 0 by default as in the reference. */
+int bem_set_point_source_strength(double q);
+
+/* ------------------------------------------------------------------ */
+/* Mesh: class mesh (mesh.h:216-259)                                    */
+/* ------------------------------------------------------------------ */
+typedef struct bem_mesh_s *bem_mesh_t;
+
+int bem_mesh_create(bem_mesh_t *out);                    /* mesh::mesh() */
+int bem_mesh_destroy(bem_mesh_t m);                      /* mesh::~mesh (mesh.cu:1301-1311) */
+/* mesh::readObj (mesh.cu:1215-1265), same parse rules: 48-char line
+ * chunks, any line starting 'v' is a vertex, first integer of each face
+ * field, bc = (0, 1, -1). */
+int bem_mesh_read_obj(bem_mesh_t m, const char *path);
+/* Robust OBJ reader (no reference counterpart): v/vt/vn, f a/b/c, negative
+ * indices, polygons (fan-triangulated), any line length. */
+int bem_mesh_read_obj_robust(bem_mesh_t m, const char *path);
+/* Direct geometry (no reference counterpart); bc reset to (0, 1, -1). */
+int bem_mesh_set(bem_mesh_t m, const double *pnts, int num_pnts, const int *elems, int num_elems);
+/* Per-element bc (ca, cb, cc) as 6 doubles (re, im) each: the triElem::bc
+ * field (mesh.h:202), which readObj hard-codes (mesh.cu:1240-1242). */
+int bem_mesh_set_bc(bem_mesh_t m, const double *bc);
+int bem_mesh_set_uniform_bc(bem_mesh_t m, double ca_re, double ca_im, double cb_re,
+                            double cb_im, double cc_re, double cc_im);
+/* mesh::findBB (mesh.cu:1369-1409): bounding box padded by threshold. */
+int bem_mesh_find_bb(bem_mesh_t m, float threshold);
+int bem_mesh_get_bb(bem_mesh_t m, float *bb6);
+/* mesh::genCHIEF (mesh.cu:1430-1483): candidates from cuRAND's host XORWOW
+ * generator with seeds 0, 1, 2, ...; a candidate is accepted when a ray from
+ * it crosses the surface an odd number of times and it is at least
+ * threshold from every node.  The ray tests run on the GPU in batches. */
+int bem_mesh_gen_chief(bem_mesh_t m, int num, float threshold);
+/* Explicit CHIEF points (no reference counterpart: chiefPnts is private,
+ * mesh.h:233). */
+int bem_mesh_set_chief(bem_mesh_t m, const double *pnts, int num);
+/* getNumPnts / getNumElems / getNumChief (mesh.h:255-258). */
+int bem_mesh_get_counts(bem_mesh_t m, int *num_pnts, int *num_elems, int *num_chief);
+int bem_mesh_get_points(bem_mesh_t m, double *pnts);
+int bem_mesh_get_elems(bem_mesh_t m, int *elems);
+int bem_mesh_get_chief(bem_mesh_t m, double *pnts);
+/* Icosphere generator (no reference counterpart) with the reference
+ * spheres' inward winding: (p1-p3) x (p2-p3) points into the body. */
+int bem_mesh_icosphere(bem_mesh_t m, int subdiv, double radius);
+/* cmptSurfArea (mesh.cu:1082-1117). */
+int bem_mesh_surface_area(bem_mesh_t m, double *area);
+
+/* ------------------------------------------------------------------ */
+/* Drop-in calls with host buffers (the reference's call surface)       */
+/* ------------------------------------------------------------------ */
+/* bemSystem (mesh.h:222-223, mesh.cu:985-1006): A ((N+M) x N) and B
+ * ((N+M) x numSrcs), c64, for point sources of strength STRENGTH at
+ * srcs[3*i]; FP32 regular quadrature, FP64 singular integrals. */
+int bem_system_c64(bem_mesh_t m, float k, const float *srcs, int num_srcs, float *A, int lda,
+                   float *B, int ldb);
+/* qrSolver (numerical.h:196-197, numerical.cu:580-644): least-squares
+ * solve, B overwritten, solution in rows 0..nA-1. */
+int bem_qr_solve_c64(const float *A, int mA, int nA, int ldA, float *B, int nB, int ldB);
+/* GMRES (GMRES.h:104-105, GMRES.cu:145-279): unrestarted GMRES on a square
+ * m x m system, x holds x0 on entry. */
+int bem_gmres_c64(const float *A, const float *b, int m, int max_iter, float thr, float *x);
+/* genExtPressure (mesh.h:425-426, mesh.cu:1038-1073): pressure at x from
+ * the surface pressure surf_p (numPnts c64 values). */
+int bem_ext_pressure_c64(float k, bem_mesh_t m, const float *src, const float *x,
+                         const float *surf_p, float *p_out);
+/* wrtCplxMat (numerical.cu:556-578): "(%f,%f) " rows. */
+int bem_write_cplx_mat_c64(const float *mat, int rows, int cols, int ldm, const char *path);
+
+/* ------------------------------------------------------------------ */
+/* Device-resident solver handle (extends bemSystem/qrSolver/GMRES/     */
+/* genExtPressure: matrices, sources and solutions stay in HBM)         */
+/* ------------------------------------------------------------------ */
+typedef struct bem_solver_s *bem_solver_t;
+
+enum { BEM_SRC_POINT = 0, BEM_SRC_PLANE = 1 };
+/* One incident field: point source a*G(k,|x-vec|) (pntSrc, mesh.cu:114-118)
+ * or plane wave a*exp(-i k vec.x) (no reference counterpart). */
+typedef struct {
+    int kind;
+    double vec[3];
+    double amp_re, amp_im;
+} bem_source_t;
+
+enum { BEM_PREC_C64 = 0, BEM_PREC_C128 = 1 };
+enum { BEM_SOLVE_QR = 0, BEM_SOLVE_GMRES_REFINED = 1 };
+
+typedef struct {
+    double density;     /* 1.2041 (numerical.cu:12) */
+    double speed;       /* 343.21 (numerical.cu:14) */
+    int order;          /* Gauss points per direction, INTORDER = 6 */
+    double near_eta;    /* 0: plain rule for every x not a vertex of e (reference) */
+    int near_depth;     /* maximum subdivision depth of near-singular pairs */
+    double tol;         /* refinement: relative normal-equation residual */
+    int max_iter;       /* inner GMRES iterations per refinement step */
+    double inner_tol;   /* inner GMRES relative tolerance */
+    int max_refine;     /* refinement steps */
+    int tile_cols;      /* far-field column tile width, 0 = automatic (<= 12288) */
+} bem_options_t;
+
+typedef struct {
+    int iterations;      /* total inner iterations */
+    int refinements;     /* outer refinement steps */
+    double rel_residual; /* final ||A^H (b - A x)|| / ||A^H b|| (max over sources) */
+    int converged;
+} bem_solve_info_t;
+
+int bem_options_default(bem_options_t *o);
+int bem_solver_create(bem_solver_t *out);   /* binds the current CUDA device */
+int bem_solver_destroy(bem_solver_t s);
+int bem_solver_set_options(bem_solver_t s, const bem_options_t *o);
+int bem_solver_get_options(bem_solver_t s, bem_options_t *o);
+/* Upload nodes, elements, bc and CHIEF points of a mesh. */
+int bem_solver_set_mesh(bem_solver_t s, bem_mesh_t m);
+/* Same from raw host arrays; bc (6 doubles per element) may be NULL for
+ * (0, 1, -1), chief may be NULL when num_chief is 0. */
+int bem_solver_set_geometry(bem_solver_t s, const double *pnts, int num_pnts, const int *elems,
+                            int num_elems, const double *bc, const double *chief, int num_chief);
+int bem_solver_set_sources(bem_solver_t s, const bem_source_t *srcs, int num_srcs);
+/* Assemble A and B on the device for wavenumber k.  BEM_PREC_C64: FP32
+ * regular quadrature, FP64 singular and near-singular integrals, c64
+ * storage.  BEM_PREC_C128: FP64 throughout, c128 storage. */
+int bem_solver_assemble(bem_solver_t s, double k, int precision);
+/* BEM_SOLVE_QR: dense least squares (Householder QR) in the assembly
+ * precision.  BEM_SOLVE_GMRES_REFINED: GMRES on the normal equations with
+ * FP32 matrix products and FP64 Arnoldi/Givens, inside FP64 iterative
+ * refinement (requires a c64 assembly). */
+int bem_solver_solve(bem_solver_t s, int method, bem_solve_info_t *info);
+/* Copy results to host buffers in the given precision (BEM_PREC_*). */
+int bem_solver_get_solution(bem_solver_t s, void *x, int ldx, int precision);
+int bem_solver_get_system(bem_solver_t s, void *A, int lda, void *B, int ldb, int precision);
+/* Field pressure at num_pts points (3 doubles each) for every source:
+ * p (num_pts x S, column-major, ldp) in the given precision. */
+int bem_solver_eval_field(bem_solver_t s, const double *pts, int num_pts, void *p, int ldp,
+                          int precision);
+int bem_solver_sync(bem_solver_t s);
+/* The cudaStream_t all work of the handle is queued on. */
+void *bem_solver_stream(bem_solver_t s);
+int bem_solver_sizes(bem_solver_t s, int *n, int *m, int *num_elems, int *num_srcs);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BEM_GB300_H */

@@ -1,0 +1,147 @@
+"""GPU assembly parity against the FP64 oracle, through the C ABI.
+
+Tolerances: c128 (FP64 everywhere) 1e-11 relative to the largest entry;
+c64 (FP32 regular quadrature, FP64 singular/near pairs, c64 storage) 2e-6.
+"""
+import numpy as np
+import pytest
+
+from helpers import GOLDEN, icosphere, rel_err
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-11
+TOL32 = 2e-6
+
+
+def _problem(kind):
+    if kind == "test.obj":
+        import oracle
+        p, f = oracle.read_obj_reference(f"{GOLDEN}/test.obj")
+        p = p.astype(np.float64)
+        chief = np.array([[0.1, 0.05, -0.2], [-0.15, 0.2, 0.1]])
+    elif kind == "cube.obj":
+        import oracle
+        p, f = oracle.read_obj_reference(f"{GOLDEN}/cube.obj")
+        p = p.astype(np.float64)
+        chief = np.array([[0.2, -0.1, 0.3]])
+    else:
+        p, f = icosphere(2, 0.7)
+        chief = np.array([[0.1, 0.05, -0.2], [-0.15, 0.2, 0.1], [0.0, 0.0, 0.25]])
+    return p, f, chief
+
+
+SRCS = [("plane", (0.0, 0.6, 0.8), 1.0), ("point", (3.0, -1.0, 0.5), 2.0 - 1.0j)]
+
+
+@pytest.mark.parametrize("kind", ["test.obj", "cube.obj", "ico2"])
+@pytest.mark.parametrize("bckind", ["default", "rigid", "impedance"])
+def test_c128_assembly_matches_oracle(bemlib, orc, kind, bckind):
+    p, f, chief = _problem(kind)
+    E = f.shape[0]
+    if bckind == "default":
+        bc = None
+    elif bckind == "rigid":
+        bc = np.tile(np.array([0, 1, 0], dtype=np.complex128), (E, 1))
+    else:
+        rng = np.random.default_rng(7)
+        bc = np.stack([0.3 + 0.1j * rng.random(E), 1.0 + 0.2j * rng.random(E), -1.0 + 0.5j * rng.random(E)], axis=1)
+    k = 2.3
+    s = bemlib.Solver()
+    s.set_geometry(p, f, bc=bc, chief=chief)
+    s.set_sources(SRCS)
+    s.assemble(k, bemlib.PREC_C128)
+    A, B = s.system(bemlib.PREC_C128)
+    Ao, Bo = orc.assemble(np.vstack([p, chief]), f, k, p.shape[0], SRCS, bc=bc)
+    assert rel_err(A, Ao) < TOL64
+    assert rel_err(B, Bo) < TOL64
+
+
+@pytest.mark.parametrize("kind", ["test.obj", "ico2"])
+def test_c64_assembly_matches_oracle(bemlib, orc, kind):
+    p, f, chief = _problem(kind)
+    k = 4.0
+    s = bemlib.Solver()
+    s.set_geometry(p, f, chief=chief)
+    s.set_sources(SRCS)
+    s.assemble(k, bemlib.PREC_C64)
+    A, B = s.system(bemlib.PREC_C128)
+    Ao, Bo = orc.assemble(np.vstack([p, chief]), f, k, p.shape[0], SRCS)
+    assert rel_err(A, Ao) < TOL32
+    assert rel_err(B, Bo) < TOL32
+
+
+@pytest.mark.parametrize("eta,depth", [(1.5, 2), (3.0, 3)])
+def test_near_singular_assembly_matches_oracle(bemlib, orc, eta, depth):
+    p, f, chief = _problem("ico2")
+    chief = np.vstack([chief, [[0.0, 0.0, 0.66]]])    # a CHIEF point close to the surface
+    k = 3.0
+    s = bemlib.Solver(near_eta=eta, near_depth=depth)
+    s.set_geometry(p, f, chief=chief)
+    s.set_sources(SRCS)
+    s.assemble(k, bemlib.PREC_C128)
+    A, B = s.system(bemlib.PREC_C128)
+    prm = orc.params(near_eta=eta, near_depth=depth)
+    Ao, Bo = orc.assemble(np.vstack([p, chief]), f, k, p.shape[0], SRCS, prm=prm)
+    assert rel_err(A, Ao) < 1e-10
+    assert rel_err(B, Bo) < 1e-10
+    s.assemble(k, bemlib.PREC_C64)
+    A32, _ = s.system(bemlib.PREC_C128)
+    assert rel_err(A32, Ao) < TOL32
+
+
+def test_quadrature_order(bemlib, orc):
+    p, f, chief = _problem("test.obj")
+    s = bemlib.Solver(order=4)
+    s.set_geometry(p, f, chief=chief)
+    s.set_sources(SRCS)
+    s.assemble(1.5, bemlib.PREC_C128)
+    A, B = s.system(bemlib.PREC_C128)
+    Ao, Bo = orc.assemble(np.vstack([p, chief]), f, 1.5, p.shape[0], SRCS, prm=orc.params(order=4))
+    assert rel_err(A, Ao) < TOL64 and rel_err(B, Bo) < TOL64
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_multi_tile_assembly(bemlib, orc, prec):
+    """Column tiles narrower than N: Morton-ordered tiles, elements straddling
+    tiles integrated once per tile, c/beta counted in the owner tile only."""
+    p, f = icosphere(3, 1.0)                   # 642 nodes
+    chief = np.array([[0.1, 0.2, -0.3]])
+    s = bemlib.Solver(tile_cols=100)           # 7 tiles
+    s.set_geometry(p, f, chief=chief)
+    s.set_sources(SRCS)
+    s.assemble(3.0, prec)
+    A, B = s.system(bemlib.PREC_C128)
+    Ao, Bo = orc.assemble(np.vstack([p, chief]), f, 3.0, p.shape[0], SRCS)
+    tol = TOL32 if prec == 0 else TOL64
+    assert rel_err(A, Ao) < tol and rel_err(B, Bo) < tol
+
+
+def test_assembly_repeatable(bemlib):
+    p, f, chief = _problem("ico2")
+    s = bemlib.Solver()
+    s.set_geometry(p, f, chief=chief)
+    s.set_sources(SRCS)
+    s.assemble(2.0, bemlib.PREC_C64)
+    A1, B1 = s.system(bemlib.PREC_C64)
+    s.assemble(2.0, bemlib.PREC_C64)
+    A2, B2 = s.system(bemlib.PREC_C64)
+    assert rel_err(A1, A2) < 1e-6 and rel_err(B1, B2) < 1e-12
+
+
+def test_errors_are_status_codes(bemlib):
+    s = bemlib.Solver()
+    with pytest.raises(bemlib.BemError) as e:
+        s.assemble(1.0)
+    assert e.value.status == 7
+    p, f, _ = _problem("test.obj")
+    s.set_geometry(p, f)
+    with pytest.raises(bemlib.BemError) as e:
+        s.assemble(1.0)                       # no sources
+    assert e.value.status == 7
+    s.set_sources([("plane", (0, 0, 1), 1.0)])
+    with pytest.raises(bemlib.BemError) as e:
+        s.assemble(-1.0)
+    assert e.value.status == 2
+    with pytest.raises(bemlib.BemError):
+        s.solve()                             # nothing assembled

@@ -1,0 +1,133 @@
+"""C ABI library: loads, exports every declared symbol, and the host-only
+logic (mesh readers, generators, bounding box, quadrature, output format)
+agrees with the oracle.  No GPU compute is called here."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+from helpers import GOLDEN, ROOT, icosphere
+
+
+def _declared_symbols():
+    text = open(os.path.join(ROOT, "include", "bem_gb300.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(bem_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_every_declared_symbol_is_exported(bemlib):
+    syms = _declared_symbols()
+    assert len(syms) >= 40
+    L = bemlib.lib()
+    missing = [s for s in syms if not hasattr(L, s)]
+    assert not missing, missing
+    # the Python binding table covers the header exactly
+    assert sorted(bemlib.SIGNATURES) == syms
+
+
+def test_status_strings(bemlib):
+    L = bemlib.lib()
+    assert L.bem_status_string(0) == b"success"
+    assert L.bem_status_string(1) == b"failure"
+    assert L.bem_version() >= 10000
+
+
+def test_gauss_legendre_matches_oracle(bemlib, orc):
+    for n in (1, 4, 6, 12):
+        x, w = bemlib.gauss_legendre(n)
+        xo, wo = orc.gauss_legendre(n)
+        np.testing.assert_allclose(x, xo, atol=1e-15)
+        np.testing.assert_allclose(w, wo, atol=1e-15)
+    with pytest.raises(bemlib.BemError) as e:
+        bemlib.gauss_legendre(13)
+    assert e.value.status == 2
+
+
+@pytest.mark.parametrize("name", ["sphere.obj", "test.obj", "cube.obj"])
+def test_read_obj_reference_semantics(bemlib, orc, name):
+    m = bemlib.Mesh()
+    assert m.readObj(f"{GOLDEN}/{name}") == 0
+    p, f = orc.read_obj_reference(f"{GOLDEN}/{name}")
+    assert m.counts() == (p.shape[0], f.shape[0], 0)
+    np.testing.assert_array_equal(m.points(), p.astype(np.float64))
+    np.testing.assert_array_equal(m.elems(), f)
+
+
+def test_read_obj_quirks(bemlib, orc, tmp_path):
+    """vn lines count as vertices and 'f a/b/c' keeps the first integer of
+    the first field only, as the reference's sscanf parse does; the robust
+    reader handles both."""
+    path = tmp_path / "q.obj"
+    path.write_text("v 0 0 0\nv 1 0 0\nv 0 1 0\nv 0 0 1\nvn 0 0 1\n"
+                    "f 1 2 3\nf 1/1/1 2/2/2 4/4/4\nf -4 -3 -1\n" +
+                    "v " + " ".join(["0.5"] * 3) + "   " + "#" * 60 + "\n")
+    m = bemlib.Mesh()
+    m.readObj(str(path))
+    p, f = orc.read_obj_reference(str(path))
+    assert m.counts()[:2] == (p.shape[0], f.shape[0])
+    np.testing.assert_array_equal(m.elems(), f)
+    r = bemlib.Mesh()
+    r.read_obj_robust(str(path))
+    assert r.counts()[:2] == (5, 3)
+    np.testing.assert_array_equal(r.elems(), [[0, 1, 2], [0, 1, 3], [0, 1, 3]])   # -k counts v lines seen so far
+
+
+def test_read_obj_errors(bemlib, tmp_path):
+    m = bemlib.Mesh()
+    with pytest.raises(bemlib.BemError) as e:
+        m.readObj(str(tmp_path / "missing.obj"))
+    assert e.value.status == 6
+    bad = tmp_path / "bad.obj"
+    bad.write_text("v 0 0 0\nv 1 0 0\nf 1 2 9\n")
+    with pytest.raises(bemlib.BemError):
+        m.read_obj_robust(str(bad))
+    empty = bemlib.Mesh()
+    with pytest.raises(bemlib.BemError) as e:
+        empty.findBB(0.1)
+    assert e.value.status == 7
+
+
+@pytest.mark.parametrize("s", [0, 1, 2, 3])
+def test_icosphere_generator(bemlib, s):
+    m = bemlib.Mesh.icosphere(s, 2.0)
+    n, e, _ = m.counts()
+    assert (n, e) == (10 * 4 ** s + 2, 20 * 4 ** s)
+    p, f = m.points(), m.elems()
+    np.testing.assert_allclose(np.linalg.norm(p, axis=1), 2.0, rtol=1e-14)
+    nrm = np.cross(p[f[:, 0]] - p[f[:, 2]], p[f[:, 1]] - p[f[:, 2]])
+    assert np.all(np.einsum("ij,ij->i", nrm, p[f].mean(axis=1)) < 0)     # inward winding
+    pt, ft = icosphere(s, 2.0)
+    assert abs(m.surface_area() - 0.5 * np.linalg.norm(
+        np.cross(pt[ft[:, 0]] - pt[ft[:, 2]], pt[ft[:, 1]] - pt[ft[:, 2]]), axis=1).sum()) < 1e-10
+
+
+def test_find_bb_float(bemlib):
+    from helpers import float_bb
+    m = bemlib.Mesh()
+    m.readObj(f"{GOLDEN}/sphere.obj")
+    m.findBB(1e-4)
+    np.testing.assert_array_equal(m.bb(), float_bb(m.points(), 1e-4).astype(np.float32))
+
+
+def test_set_and_bc_validation(bemlib):
+    m = bemlib.Mesh()
+    with pytest.raises(bemlib.BemError) as e:
+        m.set([[0, 0, 0], [1, 0, 0], [0, 1, 0]], [[0, 1, 5]])
+    assert e.value.status == 2
+    m.set([[0, 0, 0], [1, 0, 0], [0, 1, 0]], [[0, 1, 2]])
+    with pytest.raises(bemlib.BemError):
+        m.set_uniform_bc(0, 0, 1)          # cb = 0
+    m.set_uniform_bc(0, 1, 0)
+    m.set_chief([[0.1, 0.1, 0.1]])
+    assert m.counts() == (3, 1, 1)
+
+
+def test_wrtcplxmat_format(bemlib, tmp_path):
+    a = np.array([[1 + 2j, -0.5j], [3.25 - 1j, 0]], dtype=np.complex64)
+    out = tmp_path / "m.txt"
+    bemlib.wrtCplxMat(a, str(out))
+    assert out.read_text() == ("(1.000000,2.000000) (-0.000000,-0.500000) \n"
+                               "(3.250000,-1.000000) (0.000000,0.000000) \n") or \
+        out.read_text() == ("(1.000000,2.000000) (0.000000,-0.500000) \n"
+                            "(3.250000,-1.000000) (0.000000,0.000000) \n")

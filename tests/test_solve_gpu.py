@@ -1,0 +1,184 @@
+"""GPU solves, field evaluation and the reference's drop-in calls, against
+the FP64 oracle and the analytic sphere solutions (through the C ABI).
+
+Tolerances: FP64 QR 1e-10; refined GMRES (FP32 matvecs inside FP64
+refinement) 1e-5 relative surface-pressure error against the FP64 solve of
+the same formulation; c64 field evaluation 1e-5."""
+import numpy as np
+import pytest
+
+from helpers import FIELD_GOLDEN, GOLDEN, K_GOLDEN, chief_candidates, float_bb, golden, icosphere, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _rigid_ico(subdiv, n_chief, seed=1):
+    p, f = icosphere(subdiv)
+    rng = np.random.default_rng(seed)
+    u = rng.random((n_chief, 3))
+    r = 0.5 * np.cbrt(u[:, 0])
+    th = np.arccos(1 - 2 * u[:, 1])
+    ph = 2 * np.pi * u[:, 2]
+    chief = np.stack([r * np.sin(th) * np.cos(ph), r * np.sin(th) * np.sin(ph), r * np.cos(th)], axis=1)
+    bc = np.tile(np.array([0, 1, 0], dtype=np.complex128), (f.shape[0], 1))
+    return p, f, chief, bc
+
+
+def test_qr_c128_matches_oracle(bemlib, orc):
+    p, f, chief, bc = _rigid_ico(2, 4)
+    srcs = [("plane", (0, 0, 1), 1.0), ("point", (2, 1, 0), 1.0)]
+    s = bemlib.Solver()
+    s.set_geometry(p, f, bc=bc, chief=chief)
+    s.set_sources(srcs)
+    s.assemble(1.3, bemlib.PREC_C128)
+    s.solve(bemlib.SOLVE_QR)
+    x = s.solution()
+    Ao, Bo = orc.assemble(np.vstack([p, chief]), f, 1.3, p.shape[0], srcs, bc=bc)
+    xo = orc.lsq_qr(Ao, Bo)
+    assert rel_err(x, xo) < 1e-10
+
+
+def test_refined_gmres_config1(bemlib, orc):
+    """Rigid unit sphere, icosphere subdivision 3 (642 nodes, 1280
+    triangles), plane wave along +z at ka = 1, 8 seeded CHIEF points in
+    r < 0.5: mixed-precision solve within 1e-5 of the FP64 solve, and within
+    discretisation error of the rigid-sphere series."""
+    p, f, chief, bc = _rigid_ico(3, 8)
+    srcs = [("plane", (0, 0, 1), 1.0)]
+    s = bemlib.Solver()
+    s.set_geometry(p, f, bc=bc, chief=chief)
+    s.set_sources(srcs)
+    s.assemble(1.0, bemlib.PREC_C128)
+    s.solve(bemlib.SOLVE_QR)
+    x64 = s.solution()[:, 0]
+    s.assemble(1.0, bemlib.PREC_C64)
+    info = s.solve(bemlib.SOLVE_GMRES_REFINED)
+    x = s.solution()[:, 0]
+    assert info.converged and info.rel_residual < 1e-8
+    assert rel_err(x, x64) < 1e-5
+    ref = orc.rigid_sphere_surface(p[:, 2], 1.0)
+    assert rel_err(x64, ref) < 1e-2
+    Ao, Bo = orc.assemble(np.vstack([p, chief]), f, 1.0, p.shape[0], srcs, bc=bc)
+    assert rel_err(x64, orc.lsq_qr(Ao, Bo)[:, 0]) < 1e-10
+
+
+def test_refined_gmres_multi_source_and_higher_k(bemlib):
+    p, f, chief, bc = _rigid_ico(3, 8, seed=2)
+    srcs = [("plane", (0, 0, 1), 1.0), ("plane", (0.6, 0, 0.8), 1.0), ("point", (0, 2, 0), 1.0)]
+    s = bemlib.Solver()
+    s.set_geometry(p, f, bc=bc, chief=chief)
+    s.set_sources(srcs)
+    s.assemble(4.0, bemlib.PREC_C128)
+    s.solve(bemlib.SOLVE_QR)
+    x64 = s.solution()
+    s.assemble(4.0, bemlib.PREC_C64)
+    info = s.solve(bemlib.SOLVE_GMRES_REFINED)
+    assert info.converged
+    assert rel_err(s.solution(), x64) < 1e-5
+
+
+def test_qr_c64_close_to_fp64(bemlib):
+    p, f, chief, bc = _rigid_ico(2, 4)
+    s = bemlib.Solver()
+    s.set_geometry(p, f, bc=bc, chief=chief)
+    s.set_sources([("plane", (0, 0, 1), 1.0)])
+    s.assemble(2.0, bemlib.PREC_C128)
+    s.solve(bemlib.SOLVE_QR)
+    x64 = s.solution()
+    s.assemble(2.0, bemlib.PREC_C64)
+    s.solve(bemlib.SOLVE_QR)
+    assert rel_err(s.solution(), x64) < 1e-4
+
+
+@pytest.mark.parametrize("prec,tol", [(0, 1e-5), (1, 1e-10)])
+def test_field_matches_oracle(bemlib, orc, prec, tol):
+    p, f, chief, bc = _rigid_ico(2, 4)
+    srcs = [("plane", (0, 0, 1), 1.0), ("point", (0.0, 3.0, 0.0), 2.0)]
+    s = bemlib.Solver()
+    s.set_geometry(p, f, bc=bc, chief=chief)
+    s.set_sources(srcs)
+    s.assemble(1.5, bemlib.PREC_C128)
+    s.solve(bemlib.SOLVE_QR)
+    x = s.solution()
+    rng = np.random.default_rng(5)
+    d = rng.standard_normal((37, 3))
+    fp = d / np.linalg.norm(d, axis=1)[:, None] * rng.uniform(1.5, 4.0, (37, 1))
+    s.assemble(1.5, prec)
+    s.solve(bemlib.SOLVE_QR)
+    out = s.field(fp)
+    ref = orc.field(p, f, 1.5, s.solution(), fp, srcs, bc=bc)
+    assert rel_err(out, ref) < tol
+    assert rel_err(orc.field(p, f, 1.5, x, fp, srcs, bc=bc), ref) < max(tol, 1e-4)
+
+
+def test_field_near_surface_eta(bemlib, orc):
+    p, f, chief, bc = _rigid_ico(2, 2)
+    srcs = [("plane", (0, 0, 1), 1.0)]
+    s = bemlib.Solver(near_eta=2.0, near_depth=3)
+    s.set_geometry(p, f, bc=bc, chief=chief)
+    s.set_sources(srcs)
+    s.assemble(1.0, bemlib.PREC_C128)
+    s.solve(bemlib.SOLVE_QR)
+    fp = np.array([[0, 0, 1.02], [0.5, 0.5, 0.75], [0, -1.5, 0]])
+    out = s.field(fp)
+    ref = orc.field(p, f, 1.0, s.solution(), fp, srcs, bc=bc, prm=orc.params(near_eta=2.0, near_depth=3))
+    assert rel_err(out, ref) < 1e-10
+
+
+def test_dropin_golden_pipeline(bemlib, orc):
+    """The reference's main.cpp sequence through the drop-in calls:
+    readObj, findBB(1e-4), genCHIEF(1, 0.1), gaussQuad(6).sendToDevice(),
+    bemSystem, qrSolver, genExtPressure at the golden field points; compared
+    with the golden file and with the oracle running the same steps."""
+    m = bemlib.Mesh()
+    m.readObj(f"{GOLDEN}/sphere.obj")
+    m.findBB(0.0001)
+    m.genCHIEF(1, 0.1)
+    pts = m.points()
+    ch_o, _ = orc.chief_select(pts, m.elems(), float_bb(pts, 1e-4), 0.1, chief_candidates(), 1)
+    np.testing.assert_array_equal(m.chief(), ch_o.astype(np.float32).astype(np.float64))
+    bemlib.gaussQuad(6).sendToDevice()
+    src = np.array([1e6, 1e6, 1e6])
+    A, B = bemlib.bemSystem(m, K_GOLDEN, src)
+    Ao, Bo = orc.assemble(np.vstack([pts, m.chief()]), m.elems(), K_GOLDEN, pts.shape[0],
+                          [("point", src, 0.0)])
+    assert rel_err(A, Ao) < 2e-6 and rel_err(B, Bo) < 2e-6
+    bemlib.qrSolver(A, B)
+    x = B[:pts.shape[0], 0]
+    res = [x[0]] + [bemlib.genExtPressure(K_GOLDEN, m, src, fp, x) for fp in FIELD_GOLDEN]
+    res = np.array(res)
+    xo = orc.lsq_qr(Ao, Bo)[:, 0]
+    reso = np.concatenate([[xo[0]], orc.field(pts, m.elems(), K_GOLDEN, xo, FIELD_GOLDEN,
+                                               [("point", src, 0.0)])[:, 0]])
+    assert rel_err(res, reso) < 2e-4
+    g = golden("sphere171Hz_CHIEF")
+    assert (np.abs(res - g) / np.abs(g)).max() < 5e-3
+
+
+def test_dropin_gmres_square(bemlib, orc):
+    """GMRES (GMRES.cu:145-279) on the square no-CHIEF system of test.obj."""
+    m = bemlib.Mesh()
+    m.readObj(f"{GOLDEN}/test.obj")
+    bemlib.set_point_source_strength(1.0)
+    try:
+        A, B = bemlib.bemSystem(m, 1.1, [3.0, 0.0, 0.0])
+    finally:
+        bemlib.set_point_source_strength(0.0)
+    x = bemlib.GMRES(A, B[:, 0], A.shape[0], 1e-6)
+    xd = np.linalg.solve(A.astype(np.complex128), B[:, 0].astype(np.complex128))
+    assert rel_err(x, xd) < 1e-5
+    xo, it, _ = orc.gmres(A.astype(np.complex128), B[:, 0], A.shape[0], 1e-6)
+    assert rel_err(x, xo) < 1e-5
+    # a converged initial guess returns unchanged
+    x0 = xd.astype(np.complex64)
+    x2 = bemlib.GMRES(A, B[:, 0], A.shape[0], 1e-3, x=x0.copy())
+    np.testing.assert_array_equal(x2, x0)
+
+
+def test_dropin_qr_vs_numpy(bemlib):
+    rng = np.random.default_rng(9)
+    A = (rng.standard_normal((50, 40)) + 1j * rng.standard_normal((50, 40))).astype(np.complex64)
+    B = np.asfortranarray((rng.standard_normal((50, 2)) + 1j * rng.standard_normal((50, 2))).astype(np.complex64))
+    X = np.linalg.lstsq(A.astype(np.complex128), B.astype(np.complex128), rcond=None)[0]
+    bemlib.qrSolver(A, B)
+    assert rel_err(B[:40], X) < 1e-4
