@@ -77,6 +77,8 @@ SIGNATURES = {
     "bem_last_error": (_S, []),
     "bem_version": (_I, []),
     "bem_launch_count": (ctypes.c_longlong, []),
+    "bem_profile_enable": (_I, [_I]),
+    "bem_profile_report": (_I, [ctypes.c_char_p, _I]),
     "bem_gauss_legendre": (_I, [_I, _VP, _VP]),
     "bem_set_quadrature": (_I, [_I]),
     "bem_get_quadrature": (_I, []),
@@ -152,6 +154,24 @@ def _ptr(a: np.ndarray):
 
 def launch_count() -> int:
     return int(lib().bem_launch_count())
+
+
+def profile_enable(on: bool = True) -> None:
+    """Bracket every library kernel launch with CUDA events (clears old records)."""
+    _check(lib().bem_profile_enable(1 if on else 0))
+
+
+def profile_report() -> dict:
+    """{kernel name: (launches, total_ms)} for the current profiling window."""
+    buf = ctypes.create_string_buffer(1 << 16)
+    n = lib().bem_profile_report(buf, len(buf))
+    if n < 0:
+        _check(-n)
+    out = {}
+    for line in buf.value.decode().splitlines():
+        name, cnt, ms = line.split()
+        out[name] = (int(cnt), float(ms))
+    return out
 
 
 def sources(srcs) -> ctypes.Array:
@@ -436,10 +456,14 @@ class Solver:
             _check(st)
         return info
 
-    def solution(self, precision: int = PREC_C128) -> np.ndarray:
+    def solution(self, precision: int = PREC_C128, out: np.ndarray | None = None) -> np.ndarray:
+        """Surface pressure (N x S, Fortran order); `out` may be a
+        caller-owned (e.g. pinned) array of the right dtype and shape."""
         n, _, _, s = self.sizes()
         dt = np.complex64 if precision == PREC_C64 else np.complex128
-        x = np.zeros((n, s), dtype=dt, order="F")
+        x = np.zeros((n, s), dtype=dt, order="F") if out is None else out
+        if x.dtype != dt or x.shape != (n, s) or not x.flags.f_contiguous:
+            raise ValueError("solution buffer must be an (N, S) Fortran array of the requested precision")
         _check(lib().bem_solver_get_solution(self._h, _ptr(x), n, int(precision)))
         return x
 

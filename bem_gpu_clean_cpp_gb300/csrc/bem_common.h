@@ -40,6 +40,18 @@ struct Error : std::runtime_error {
 extern std::atomic<long long> g_launches;
 inline void count_launch(long long n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
+// Optional kernel timing: while enabled (bem_profile_enable), a ProfScope
+// brackets a launch with CUDA events on its stream; bem_profile_report sums
+// the elapsed times per name.
+extern std::atomic<bool> g_profiling;
+struct ProfScope {
+    ProfScope(const char *name, cudaStream_t st);
+    ~ProfScope();
+    int slot = -1;
+    cudaStream_t stream = nullptr;
+};
+#define BEM_PROF(name, st) ::bem::ProfScope bem_prof_scope_((name), (st))
+
 constexpr double kPi = 3.14159265358979323846;
 constexpr int kMaxOrder = 12;              // Gauss points per direction
 constexpr int kMaxQ = kMaxOrder * kMaxOrder;

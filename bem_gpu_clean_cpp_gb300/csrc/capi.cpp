@@ -21,7 +21,44 @@
 namespace bem {
 
 std::atomic<long long> g_launches{0};
+std::atomic<bool> g_profiling{false};
 thread_local std::string g_last_error;
+
+namespace {
+struct ProfRec {
+    const char *name;
+    cudaEvent_t ev[2];
+};
+std::mutex g_prof_mu;
+std::vector<ProfRec> g_prof;           // records of the current profiling window
+std::vector<cudaEvent_t> g_ev_pool;    // events for reuse
+
+cudaEvent_t pool_event() {
+    if (!g_ev_pool.empty()) {
+        cudaEvent_t e = g_ev_pool.back();
+        g_ev_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+}  // namespace
+
+ProfScope::ProfScope(const char *name, cudaStream_t st) : stream(st) {
+    if (!g_profiling.load(std::memory_order_relaxed)) return;
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    ProfRec r{name, {pool_event(), pool_event()}};
+    cudaEventRecord(r.ev[0], st);
+    slot = (int)g_prof.size();
+    g_prof.push_back(r);
+}
+
+ProfScope::~ProfScope() {
+    if (slot < 0) return;
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    if (slot < (int)g_prof.size()) cudaEventRecord(g_prof[slot].ev[1], stream);
+}
 
 [[noreturn]] void fail(int status, const char *file, int line, const std::string &msg) {
     const char *base = std::strrchr(file, '/');
@@ -235,6 +272,54 @@ const char *bem_status_string(int s) {
 const char *bem_last_error(void) { return g_last_error.c_str(); }
 int bem_version(void) { return 10000; }
 long long bem_launch_count(void) { return g_launches.load(); }
+
+int bem_profile_enable(int on) {
+    BEM_API_BEGIN
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    for (ProfRec &r : g_prof) {
+        cudaEventSynchronize(r.ev[1]);
+        g_ev_pool.push_back(r.ev[0]);
+        g_ev_pool.push_back(r.ev[1]);
+    }
+    g_prof.clear();
+    g_profiling.store(on != 0);
+    BEM_API_END
+}
+
+int bem_profile_report(char *buf, int buflen) {
+    try {
+        std::lock_guard<std::mutex> lk(g_prof_mu);
+        std::vector<std::string> names;
+        std::vector<long long> cnt;
+        std::vector<double> tot;
+        for (ProfRec &r : g_prof) {
+            CUDA_TRY(cudaEventSynchronize(r.ev[1]));
+            float ms = 0.f;
+            CUDA_TRY(cudaEventElapsedTime(&ms, r.ev[0], r.ev[1]));
+            size_t i = 0;
+            while (i < names.size() && names[i] != r.name) i++;
+            if (i == names.size()) {
+                names.push_back(r.name);
+                cnt.push_back(0);
+                tot.push_back(0.0);
+            }
+            cnt[i]++;
+            tot[i] += ms;
+        }
+        std::string out;
+        for (size_t i = 0; i < names.size(); i++)
+            out += names[i] + " " + std::to_string(cnt[i]) + " " + std::to_string(tot[i]) + "\n";
+        if (!buf || buflen <= (int)out.size()) {
+            g_last_error = "report buffer too small";
+            return -BEM_ERR_INVALID_ARG;
+        }
+        std::memcpy(buf, out.c_str(), out.size() + 1);
+        return (int)names.size();
+    } catch (const bem::Error &e) {
+        g_last_error = e.what();
+        return -e.status;
+    }
+}
 
 int bem_gauss_legendre(int order, double *nodes, double *weights) {
     BEM_API_BEGIN

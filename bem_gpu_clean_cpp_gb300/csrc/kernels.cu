@@ -152,6 +152,7 @@ __global__ void elem_setup_kernel(const double *__restrict__ nodes, const int4 *
 
 void launch_elem_setup(const double *d_nodes, const int4 *d_elems, const double *d_bc, int E,
                        double near_eta, float4 *geo_f, double *geo_d, cudaStream_t st) {
+    BEM_PROF("elem_setup", st);
     if (E <= 0) return;
     elem_setup_kernel<<<(E + 127) / 128, 128, 0, st>>>(d_nodes, d_elems, d_bc, E, near_eta, geo_f, geo_d);
     count_launch();
@@ -473,6 +474,7 @@ size_t far_smem_bytes(int prec, int tc) {
 void launch_far_assembly(int prec, const RowPoints &rows, int N, const GeoTables &geo,
                          const TileSet &tiles, const Physics &ph, void *A, size_t lda,
                          void *c_part, void *beta_part, cudaStream_t st) {
+    BEM_PROF((prec == BEM_PREC_C64 ? "far_assembly_f32" : "far_assembly_f64"), st);
     if (rows.R <= 0 || tiles.ntiles <= 0) return;
     size_t smem = far_smem_bytes(prec, tiles.tc_max);
     if (prec == BEM_PREC_C64) {
@@ -726,6 +728,7 @@ void launch_near_assembly(int prec, const RowPoints &rows, int N, const GeoTable
                           const Physics &ph, void *A, size_t lda, const void *c_part,
                           const void *beta_part, int ntiles, const DevSource *srcs, int S,
                           double2 *B, cudaStream_t st) {
+    BEM_PROF("near_assembly_f64", st);
     if (rows.R <= 0) return;
     BEM_CHECK_ARG(ph.near_depth >= 0 && ph.near_depth <= kMaxDepth, "near_depth must be in [0, 4]");
     int nq = quadrature_points();
@@ -920,6 +923,7 @@ __global__ void field_finalize_kernel(RowPoints pts, int S, int nsplit, double k
 void launch_field(int prec, const RowPoints &pts, const GeoTables &geo, const Physics &ph,
                   const void *u, size_t ldu, int S, const DevSource *srcs, double2 *part, int nsplit,
                   double2 *near_part, double2 *out, cudaStream_t st) {
+    BEM_PROF("field_eval", st);
     if (pts.R <= 0 || S <= 0) return;
     int nq = quadrature_points();
     dim3 grid(pts.R, nsplit);

@@ -92,8 +92,10 @@ void launch_gemv_h_c64(int R, int N, const float2 *A, size_t lda, const void *u,
                        void *w, int wd, void *part, cudaStream_t st, bool conj = true);
 int gemv_h_f64_splits(int R, int N);
 // FP64 accumulation variants (the refinement residuals): A is c64 or c128.
+// r = b - A x.  For c64 A the products are exact double-float FP32
+// arithmetic; xsplit is scratch for x's float head and tail (2N c64).
 void launch_resid(int prec, int R, int N, const void *A, size_t lda, const double2 *x,
-                  const double2 *b, double2 *r, cudaStream_t st);                // r = b - A x
+                  const double2 *b, double2 *r, float2 *xsplit, cudaStream_t st);
 void launch_gemv_h_f64(int prec, int R, int N, const void *A, size_t lda, const double2 *u,
                        double2 *w, double2 *part, cudaStream_t st);               // w = A^H u
 // Row-major (R x N) -> column-major (R x N, ld_out) copy with conversion.
@@ -106,7 +108,9 @@ void launch_dots(int n, int k, const double2 *V, size_t ldv, const double2 *w, d
 void launch_update(int n, int k, const double2 *V, size_t ldv, const double2 *h, double2 *w,
                    cudaStream_t st);                          // w -= V h
 void launch_nrm2(int n, const double2 *w, double *out, double *part, cudaStream_t st);
-void launch_scale_copy(int n, const double2 *w, const double *nrm, double2 *v, cudaStream_t st);
+// v = w / *nrm; also writes a c64 copy to vf when vf is not null.
+void launch_scale_copy(int n, const double2 *w, const double *nrm, double2 *v, cudaStream_t st,
+                       float2 *vf = nullptr);
 void launch_axpy_combo(int n, int k, const double2 *V, size_t ldv, const double2 *y, double2 *x,
                        cudaStream_t st);                      // x += V y
 void launch_copy_f64(int n, const double2 *src, double2 *dst, cudaStream_t st);

@@ -34,38 +34,181 @@ __device__ __forceinline__ void st_c(double2 *p, size_t i, double re, double im)
     p[i] = make_double2(re, im);
 }
 
-// y = A x, one warp per row, FP32 accumulation, 16-byte loads of A (two
-// complex entries per load).
+// y = A x with FP32 accumulation.  A warp owns kMvRPW consecutive rows and
+// sweeps the columns two complex entries (16 bytes) at a time, so each x load
+// serves kMvRPW rows of A; A is streamed once (__ldcs).
+constexpr int kMvRPW = 4;
+constexpr int kMvWPC = 4;
+
 template <typename TX, typename TY>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(32 * kMvWPC)
 gemv_c64_kernel(int R, int N, const float2 *__restrict__ A, size_t lda, const TX *__restrict__ x,
                 TY *__restrict__ y) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int row = blockIdx.x * 8 + warp;
-    if (row >= R) return;
-    const float2 *a = A + (size_t)row * lda;
-    float sr = 0.f, si = 0.f;
+    const int row0 = (blockIdx.x * kMvWPC + warp) * kMvRPW;
+    if (row0 >= R) return;
+    const int nr = min(kMvRPW, R - row0);
+    const float4 *a4[kMvRPW];
+    float sr[kMvRPW], si[kMvRPW];
+#pragma unroll
+    for (int r = 0; r < kMvRPW; r++) {
+        a4[r] = reinterpret_cast<const float4 *>(A + (size_t)(row0 + min(r, nr - 1)) * lda);
+        sr[r] = si[r] = 0.f;
+    }
     const int N2 = N >> 1;
-    const float4 *a4 = reinterpret_cast<const float4 *>(a);
-#pragma unroll 4
+#pragma unroll 2
     for (int j2 = lane; j2 < N2; j2 += 32) {
-        float4 v = __ldcs(a4 + j2);          // streamed: A is read once per product
-        float2 x0 = ld_as_f2(x, 2 * (size_t)j2), x1 = ld_as_f2(x, 2 * (size_t)j2 + 1);
-        sr = fmaf(v.x, x0.x, sr); sr = fmaf(-v.y, x0.y, sr);
-        si = fmaf(v.x, x0.y, si); si = fmaf(v.y, x0.x, si);
-        sr = fmaf(v.z, x1.x, sr); sr = fmaf(-v.w, x1.y, sr);
-        si = fmaf(v.z, x1.y, si); si = fmaf(v.w, x1.x, si);
+        const float2 x0 = ld_as_f2(x, 2 * (size_t)j2), x1 = ld_as_f2(x, 2 * (size_t)j2 + 1);
+#pragma unroll
+        for (int r = 0; r < kMvRPW; r++) {
+            const float4 v = __ldcs(a4[r] + j2);
+            sr[r] = fmaf(v.x, x0.x, sr[r]); sr[r] = fmaf(-v.y, x0.y, sr[r]);
+            si[r] = fmaf(v.x, x0.y, si[r]); si[r] = fmaf(v.y, x0.x, si[r]);
+            sr[r] = fmaf(v.z, x1.x, sr[r]); sr[r] = fmaf(-v.w, x1.y, sr[r]);
+            si[r] = fmaf(v.z, x1.y, si[r]); si[r] = fmaf(v.w, x1.x, si[r]);
+        }
     }
     if ((N & 1) && lane == 0) {
-        float2 v = a[N - 1], x0 = ld_as_f2(x, N - 1);
-        sr = fmaf(v.x, x0.x, sr); sr = fmaf(-v.y, x0.y, sr);
-        si = fmaf(v.x, x0.y, si); si = fmaf(v.y, x0.x, si);
+        const float2 x0 = ld_as_f2(x, N - 1);
+#pragma unroll
+        for (int r = 0; r < kMvRPW; r++) {
+            const float2 v = reinterpret_cast<const float2 *>(a4[r])[N - 1];
+            sr[r] = fmaf(v.x, x0.x, sr[r]); sr[r] = fmaf(-v.y, x0.y, sr[r]);
+            si[r] = fmaf(v.x, x0.y, si[r]); si[r] = fmaf(v.y, x0.x, si[r]);
+        }
     }
-    for (int o = 16; o > 0; o >>= 1) {
-        sr += __shfl_xor_sync(0xffffffffu, sr, o);
-        si += __shfl_xor_sync(0xffffffffu, si, o);
+#pragma unroll
+    for (int r = 0; r < kMvRPW; r++) {
+        for (int o = 16; o > 0; o >>= 1) {
+            sr[r] += __shfl_xor_sync(0xffffffffu, sr[r], o);
+            si[r] += __shfl_xor_sync(0xffffffffu, si[r], o);
+        }
+        if (lane == 0 && r < nr) st_c(y, row0 + r, sr[r], si[r]);
     }
-    if (lane == 0) st_c(y, row, sr, si);
+}
+
+// ---- double-float accumulation for the FP64 refinement residuals ----
+// The entries of a c64 matrix are exact floats.  A product a*xh (xh the float
+// head of an FP64 value) is split exactly into p + e by TwoProduct (FMA), p is
+// added to the running head with TwoSum (Knuth), and all the low-order parts
+// go into a float tail; x's own tail xl contributes a*xl to the tail.  The
+// result (head + tail, summed in FP64 at the end) is accurate to ~1e-13
+// relative while the kernel runs on the FP32 pipe, so the FP64-accurate
+// residual costs one HBM pass over A instead of FP64 FMA throughput.  _rn
+// intrinsics keep the compiler from contracting the error-free transforms.
+__device__ __forceinline__ void df_mac(float &hi, float &lo, float a, float xh, float xl) {
+    const float p = __fmul_rn(a, xh);
+    const float e = fmaf(a, xh, -p);
+    const float s = __fadd_rn(hi, p);
+    const float bb = __fsub_rn(s, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+    hi = s;
+    lo = fmaf(a, xl, __fadd_rn(lo, __fadd_rn(err, e)));
+}
+
+// Splits FP64 complex values into float head and tail.
+__global__ void split_f64_kernel(int n, const double2 *__restrict__ x, float2 *__restrict__ xh,
+                                 float2 *__restrict__ xl) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double2 v = x[i];
+    const float hr = (float)v.x, hi = (float)v.y;
+    xh[i] = make_float2(hr, hi);
+    xl[i] = make_float2((float)(v.x - (double)hr), (float)(v.y - (double)hi));
+}
+
+// r = b - A x for c64 A, FP64-accurate (x given as head/tail floats).
+__global__ void __launch_bounds__(32 * kMvWPC)
+resid_df_kernel(int R, int N, const float2 *__restrict__ A, size_t lda, const float2 *__restrict__ xh,
+                const float2 *__restrict__ xl, const double2 *__restrict__ b, double2 *__restrict__ r) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int row0 = (blockIdx.x * kMvWPC + warp) * kMvRPW;
+    if (row0 >= R) return;
+    const int nr = min(kMvRPW, R - row0);
+    const float4 *a4[kMvRPW];
+    float rh[kMvRPW], rl[kMvRPW], ih[kMvRPW], il[kMvRPW];
+#pragma unroll
+    for (int q = 0; q < kMvRPW; q++) {
+        a4[q] = reinterpret_cast<const float4 *>(A + (size_t)(row0 + min(q, nr - 1)) * lda);
+        rh[q] = rl[q] = ih[q] = il[q] = 0.f;
+    }
+    const float4 *xh4 = reinterpret_cast<const float4 *>(xh);
+    const float4 *xl4 = reinterpret_cast<const float4 *>(xl);
+    const int N2 = N >> 1;
+    for (int j2 = lane; j2 < N2; j2 += 32) {
+        const float4 h = xh4[j2], l = xl4[j2];
+#pragma unroll
+        for (int q = 0; q < kMvRPW; q++) {
+            const float4 v = __ldcs(a4[q] + j2);
+            df_mac(rh[q], rl[q], v.x, h.x, l.x);
+            df_mac(rh[q], rl[q], -v.y, h.y, l.y);
+            df_mac(ih[q], il[q], v.x, h.y, l.y);
+            df_mac(ih[q], il[q], v.y, h.x, l.x);
+            df_mac(rh[q], rl[q], v.z, h.z, l.z);
+            df_mac(rh[q], rl[q], -v.w, h.w, l.w);
+            df_mac(ih[q], il[q], v.z, h.w, l.w);
+            df_mac(ih[q], il[q], v.w, h.z, l.z);
+        }
+    }
+    if ((N & 1) && lane == 0) {
+        const float2 h = xh[N - 1], l = xl[N - 1];
+#pragma unroll
+        for (int q = 0; q < kMvRPW; q++) {
+            const float2 v = reinterpret_cast<const float2 *>(a4[q])[N - 1];
+            df_mac(rh[q], rl[q], v.x, h.x, l.x);
+            df_mac(rh[q], rl[q], -v.y, h.y, l.y);
+            df_mac(ih[q], il[q], v.x, h.y, l.y);
+            df_mac(ih[q], il[q], v.y, h.x, l.x);
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < kMvRPW; q++) {
+        double sr = (double)rh[q] + (double)rl[q], si = (double)ih[q] + (double)il[q];
+        for (int o = 16; o > 0; o >>= 1) {
+            sr += __shfl_xor_sync(0xffffffffu, sr, o);
+            si += __shfl_xor_sync(0xffffffffu, si, o);
+        }
+        if (lane == 0 && q < nr) {
+            const double2 bb = b[row0 + q];
+            r[row0 + q] = make_double2(bb.x - sr, bb.y - si);
+        }
+    }
+}
+
+// Partial w = A^H u for c64 A, FP64-accurate; each thread owns two columns.
+__global__ void __launch_bounds__(256)
+gemv_h_df_part_kernel(int R, int N, const float2 *__restrict__ A, size_t lda, const double2 *__restrict__ u,
+                      int nsplit, double2 *__restrict__ part) {
+    const int c = blockIdx.x * 512 + 2 * threadIdx.x;
+    const int split = blockIdx.y;
+    const int per = (R + nsplit - 1) / nsplit;
+    const int r0 = split * per, r1 = min(R, r0 + per);
+    if (c >= N) return;
+    float ah = 0, al = 0, bh = 0, bl = 0, ch = 0, cl = 0, dh = 0, dl = 0;
+    const bool two = (c + 1 < N);
+    for (int r = r0; r < r1; r++) {
+        const double2 uu = u[r];
+        const float uh = (float)uu.x, vh = (float)uu.y;
+        const float ul = (float)(uu.x - (double)uh), vl = (float)(uu.y - (double)vh);
+        float4 v;
+        if (two) {
+            v = __ldcs(reinterpret_cast<const float4 *>(A + (size_t)r * lda + c));
+        } else {
+            const float2 t = A[(size_t)r * lda + c];
+            v = make_float4(t.x, t.y, 0.f, 0.f);
+        }
+        // conj(a) * u = (ar ur + ai ui) + i (ar ui - ai ur)
+        df_mac(ah, al, v.x, uh, ul);
+        df_mac(ah, al, v.y, vh, vl);
+        df_mac(bh, bl, v.x, vh, vl);
+        df_mac(bh, bl, -v.y, uh, ul);
+        df_mac(ch, cl, v.z, uh, ul);
+        df_mac(ch, cl, v.w, vh, vl);
+        df_mac(dh, dl, v.z, vh, vl);
+        df_mac(dh, dl, -v.w, uh, ul);
+    }
+    part[(size_t)split * N + c] = make_double2((double)ah + (double)al, (double)bh + (double)bl);
+    if (two) part[(size_t)split * N + c + 1] = make_double2((double)ch + (double)cl, (double)dh + (double)dl);
 }
 
 // Partial w = A^H u over a row range: each thread owns two adjacent columns.
@@ -252,12 +395,14 @@ __global__ void nrm2_kernel(int n, const double2 *__restrict__ w, double *__rest
 }
 
 __global__ void scale_copy_kernel(int n, const double2 *__restrict__ w, const double *__restrict__ nrm,
-                                  double2 *__restrict__ v) {
+                                  double2 *__restrict__ v, float2 *__restrict__ vf) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double s = *nrm;
     double inv = s > 0 ? 1.0 / s : 0.0;
-    v[i] = make_double2(w[i].x * inv, w[i].y * inv);
+    const double2 o = make_double2(w[i].x * inv, w[i].y * inv);
+    v[i] = o;
+    if (vf) vf[i] = make_float2((float)o.x, (float)o.y);
 }
 
 __global__ void copy_f64_kernel(int n, const double2 *__restrict__ s, double2 *__restrict__ d) {
@@ -351,12 +496,13 @@ inline int blocks(long long n, int t) { return (int)((n + t - 1) / t); }
 
 void launch_gemv_c64(int R, int N, const float2 *A, size_t lda, const void *x, int xd, void *y,
                      int yd, cudaStream_t st) {
+    BEM_PROF("gemv_c64", st);
     if (R <= 0) return;
-    dim3 g(blocks(R, 8));
-    if (!xd && !yd) gemv_c64_kernel<float2, float2><<<g, 256, 0, st>>>(R, N, A, lda, (const float2 *)x, (float2 *)y);
-    else if (xd && !yd) gemv_c64_kernel<double2, float2><<<g, 256, 0, st>>>(R, N, A, lda, (const double2 *)x, (float2 *)y);
-    else if (!xd && yd) gemv_c64_kernel<float2, double2><<<g, 256, 0, st>>>(R, N, A, lda, (const float2 *)x, (double2 *)y);
-    else gemv_c64_kernel<double2, double2><<<g, 256, 0, st>>>(R, N, A, lda, (const double2 *)x, (double2 *)y);
+    dim3 g(blocks(R, kMvRPW * kMvWPC)), b(32 * kMvWPC);
+    if (!xd && !yd) gemv_c64_kernel<float2, float2><<<g, b, 0, st>>>(R, N, A, lda, (const float2 *)x, (float2 *)y);
+    else if (xd && !yd) gemv_c64_kernel<double2, float2><<<g, b, 0, st>>>(R, N, A, lda, (const double2 *)x, (float2 *)y);
+    else if (!xd && yd) gemv_c64_kernel<float2, double2><<<g, b, 0, st>>>(R, N, A, lda, (const float2 *)x, (double2 *)y);
+    else gemv_c64_kernel<double2, double2><<<g, b, 0, st>>>(R, N, A, lda, (const double2 *)x, (double2 *)y);
     count_launch();
     KERNEL_CHECK();
 }
@@ -369,6 +515,7 @@ int gemv_h_splits(int R, int N) {
 
 void launch_gemv_h_c64(int R, int N, const float2 *A, size_t lda, const void *u, int ud, void *w,
                        int wd, void *part, cudaStream_t st, bool conj) {
+    BEM_PROF("gemv_h_c64", st);
     if (N <= 0) return;
     int ns = gemv_h_splits(R, N);
     dim3 g(blocks(N, kHCols), ns);
@@ -388,22 +535,41 @@ void launch_gemv_h_c64(int R, int N, const float2 *A, size_t lda, const void *u,
 }
 
 void launch_resid(int prec, int R, int N, const void *A, size_t lda, const double2 *x,
-                  const double2 *b, double2 *r, cudaStream_t st) {
+                  const double2 *b, double2 *r, float2 *xsplit, cudaStream_t st) {
+    BEM_PROF("resid", st);
     if (R <= 0) return;
-    if (prec == BEM_PREC_C64) resid_kernel<float2><<<blocks(R, 8), 256, 0, st>>>(R, N, (const float2 *)A, lda, x, b, r);
-    else resid_kernel<double2><<<blocks(R, 8), 256, 0, st>>>(R, N, (const double2 *)A, lda, x, b, r);
+    if (prec == BEM_PREC_C64) {
+        split_f64_kernel<<<blocks(N, 256), 256, 0, st>>>(N, x, xsplit, xsplit + N);
+        count_launch();
+        KERNEL_CHECK();
+        resid_df_kernel<<<blocks(R, kMvRPW * kMvWPC), 32 * kMvWPC, 0, st>>>(R, N, (const float2 *)A, lda, xsplit,
+                                                                          xsplit + N, b, r);
+    } else {
+        resid_kernel<double2><<<blocks(R, 8), 256, 0, st>>>(R, N, (const double2 *)A, lda, x, b, r);
+    }
     count_launch();
     KERNEL_CHECK();
 }
 
+namespace {
+int h_f64_splits(int prec, int R, int N) {
+    int cb = prec == BEM_PREC_C64 ? blocks(N, 512) : blocks(N, 256);
+    return std::max(1, std::min((4 * 152 + cb - 1) / cb, std::max(1, R / 16)));
+}
+}  // namespace
+
 void launch_gemv_h_f64(int prec, int R, int N, const void *A, size_t lda, const double2 *u,
                        double2 *w, double2 *part, cudaStream_t st) {
+    BEM_PROF("gemv_h_f64", st);
     if (N <= 0) return;
-    int cb = blocks(N, 256);
-    int ns = std::max(1, std::min((4 * 152 + cb - 1) / cb, std::max(1, R / 16)));
-    dim3 g(cb, ns);
-    if (prec == BEM_PREC_C64) gemv_h_f64_part_kernel<float2><<<g, 256, 0, st>>>(R, N, (const float2 *)A, lda, u, ns, part);
-    else gemv_h_f64_part_kernel<double2><<<g, 256, 0, st>>>(R, N, (const double2 *)A, lda, u, ns, part);
+    const int ns = h_f64_splits(prec, R, N);
+    if (prec == BEM_PREC_C64) {
+        dim3 g(blocks(N, 512), ns);
+        gemv_h_df_part_kernel<<<g, 256, 0, st>>>(R, N, (const float2 *)A, lda, u, ns, part);
+    } else {
+        dim3 g(blocks(N, 256), ns);
+        gemv_h_f64_part_kernel<double2><<<g, 256, 0, st>>>(R, N, (const double2 *)A, lda, u, ns, part);
+    }
     count_launch();
     KERNEL_CHECK();
     sum_splits_kernel<double2, double2><<<blocks(N, 256), 256, 0, st>>>(N, ns, part, w);
@@ -412,12 +578,12 @@ void launch_gemv_h_f64(int prec, int R, int N, const void *A, size_t lda, const 
 }
 
 int gemv_h_f64_splits(int R, int N) {
-    int cb = blocks(N, 256);
-    return std::max(1, std::min((4 * 152 + cb - 1) / cb, std::max(1, R / 16)));
+    return std::max(h_f64_splits(BEM_PREC_C64, R, N), h_f64_splits(BEM_PREC_C128, R, N));
 }
 
 void launch_to_colmajor(int prec_in, const void *A, size_t lda, int R, int N, int prec_out,
                         void *out, size_t ld_out, cudaStream_t st) {
+    BEM_PROF("to_colmajor", st);
     dim3 g(blocks(N, 32), blocks(R, 32)), b(32, 8);
     if (prec_in == BEM_PREC_C64 && prec_out == BEM_PREC_C64)
         to_colmajor_kernel<float2, float2><<<g, b, 0, st>>>((const float2 *)A, lda, R, N, (float2 *)out, ld_out);
@@ -433,6 +599,7 @@ void launch_to_colmajor(int prec_in, const void *A, size_t lda, int R, int N, in
 
 void launch_dots(int n, int k, const double2 *V, size_t ldv, const double2 *w, double2 *h,
                  double2 *, cudaStream_t st) {
+    BEM_PROF("dots", st);
     if (k <= 0) return;
     dots_kernel<<<k, 512, 0, st>>>(n, V, ldv, w, h);
     count_launch();
@@ -441,6 +608,7 @@ void launch_dots(int n, int k, const double2 *V, size_t ldv, const double2 *w, d
 
 void launch_update(int n, int k, const double2 *V, size_t ldv, const double2 *h, double2 *w,
                    cudaStream_t st) {
+    BEM_PROF("update", st);
     if (k <= 0) return;
     update_kernel<<<blocks(n, 256), 256, 0, st>>>(n, k, V, ldv, h, w);
     count_launch();
@@ -448,19 +616,22 @@ void launch_update(int n, int k, const double2 *V, size_t ldv, const double2 *h,
 }
 
 void launch_nrm2(int n, const double2 *w, double *out, double *, cudaStream_t st) {
+    BEM_PROF("nrm2", st);
     nrm2_kernel<<<1, 1024, 0, st>>>(n, w, out);
     count_launch();
     KERNEL_CHECK();
 }
 
-void launch_scale_copy(int n, const double2 *w, const double *nrm, double2 *v, cudaStream_t st) {
-    scale_copy_kernel<<<blocks(n, 256), 256, 0, st>>>(n, w, nrm, v);
+void launch_scale_copy(int n, const double2 *w, const double *nrm, double2 *v, cudaStream_t st, float2 *vf) {
+    BEM_PROF("scale_copy", st);
+    scale_copy_kernel<<<blocks(n, 256), 256, 0, st>>>(n, w, nrm, v, vf);
     count_launch();
     KERNEL_CHECK();
 }
 
 void launch_axpy_combo(int n, int k, const double2 *V, size_t ldv, const double2 *y, double2 *x,
                        cudaStream_t st) {
+    BEM_PROF("axpy_combo", st);
     if (k <= 0) return;
     axpy_combo_kernel<<<blocks(n, 256), 256, 0, st>>>(n, k, V, ldv, y, x);
     count_launch();
@@ -468,12 +639,14 @@ void launch_axpy_combo(int n, int k, const double2 *V, size_t ldv, const double2
 }
 
 void launch_copy_f64(int n, const double2 *src, double2 *dst, cudaStream_t st) {
+    BEM_PROF("copy_f64", st);
     copy_f64_kernel<<<blocks(n, 256), 256, 0, st>>>(n, src, dst);
     count_launch();
     KERNEL_CHECK();
 }
 
 void launch_zero_f64(size_t n, double2 *dst, cudaStream_t st) {
+    BEM_PROF("zero_f64", st);
     if (n == 0) return;
     zero_f64_kernel<<<blocks((long long)n, 256), 256, 0, st>>>(n, dst);
     count_launch();
@@ -481,12 +654,14 @@ void launch_zero_f64(size_t n, double2 *dst, cudaStream_t st) {
 }
 
 void launch_cast(int n, const double2 *src, float2 *dst, cudaStream_t st) {
+    BEM_PROF("cast", st);
     cast_kernel<<<blocks(n, 256), 256, 0, st>>>(n, src, dst);
     count_launch();
     KERNEL_CHECK();
 }
 
 void launch_cast_up(int n, const float2 *src, double2 *dst, cudaStream_t st) {
+    BEM_PROF("cast_up", st);
     cast_up_kernel<<<blocks(n, 256), 256, 0, st>>>(n, src, dst);
     count_launch();
     KERNEL_CHECK();
@@ -495,6 +670,7 @@ void launch_cast_up(int n, const float2 *src, double2 *dst, cudaStream_t st) {
 
 void launch_hcol_finish(int j, const double2 *h1, const double2 *h2, const double *nrm, double2 *H,
                         int ldh, cudaStream_t st) {
+    BEM_PROF("hcol_finish", st);
     hcol_finish_kernel<<<1, 256, 0, st>>>(j, h1, h2, nrm, H, ldh);
     count_launch();
     KERNEL_CHECK();
@@ -502,18 +678,21 @@ void launch_hcol_finish(int j, const double2 *h1, const double2 *h2, const doubl
 
 void launch_givens(int j, double2 *H, int ldh, double2 *cs, double2 *sn, double2 *g, double *res,
                    cudaStream_t st) {
+    BEM_PROF("givens", st);
     givens_kernel<<<1, 32, 0, st>>>(j, H, ldh, cs, sn, g, res);
     count_launch();
     KERNEL_CHECK();
 }
 
 void launch_trisolve(int k, const double2 *H, int ldh, const double2 *g, double2 *y, cudaStream_t st) {
+    BEM_PROF("trisolve", st);
     trisolve_kernel<<<1, 32, 0, st>>>(k, H, ldh, g, y);
     count_launch();
     KERNEL_CHECK();
 }
 
 void launch_set_scalar_c(double2 *dst, const double *v, cudaStream_t st) {
+    BEM_PROF("set_scalar_c", st);
     set_scalar_c_kernel<<<1, 32, 0, st>>>(dst, v);
     count_launch();
     KERNEL_CHECK();

@@ -33,6 +33,7 @@ void cublas_check(cublasStatus_t s, const char *what) {
 
 void bem_solver_s::solve_qr() {
     const int m = R, n = N;
+    BEM_PROF(prec == BEM_PREC_C64 ? "cusolver_qr_c64" : "cusolver_qr_c128", stream);
     if (prec == BEM_PREC_C64) {
         q_A.ensure(sizeof(float2) * (size_t)m * n);
         q_B.ensure(sizeof(float2) * (size_t)m * S);
@@ -106,6 +107,7 @@ void bem_solver_s::solve_refined(bem_solve_info_t *info) {
     w_t.ensure(sizeof(float2) * R);
     w_r.ensure(sizeof(double2) * R);
     w_gv.ensure(sizeof(double2) * n);
+    w_vf.ensure(sizeof(float2) * 2 * (size_t)n);   // c64 copy of v_j, and x head/tail for the residual
     size_t part = std::max(sizeof(float2) * (size_t)gemv_h_splits(R, n), sizeof(double2) * (size_t)gemv_h_f64_splits(R, n));
     w_part.ensure(part * n);
     w_scal.ensure(sizeof(double) * 8);
@@ -130,7 +132,7 @@ void bem_solver_s::solve_refined(bem_solve_info_t *info) {
         bool conv = false;
         int ref = 0;
         for (;; ref++) {
-            launch_resid(prec, R, n, A, lda, x, b, w_r.as<double2>(), stream);
+            launch_resid(prec, R, n, A, lda, x, b, w_r.as<double2>(), w_vf.as<float2>(), stream);
             launch_gemv_h_f64(prec, R, n, A, lda, w_r.as<double2>(), w_gv.as<double2>(), w_part.as<double2>(), stream);
             launch_nrm2(n, w_gv.as<double2>(), scal + 1, nullptr, stream);
             const double gn = read_scalar(1);
@@ -139,13 +141,12 @@ void bem_solver_s::solve_refined(bem_solve_info_t *info) {
             if (rel <= opt.tol) { conv = true; break; }
             if (ref >= opt.max_refine) break;
             // Inner GMRES on A^H A d = g, d accumulated into x.
-            launch_scale_copy(n, w_gv.as<double2>(), scal + 1, V, stream);
+            launch_scale_copy(n, w_gv.as<double2>(), scal + 1, V, stream, w_vf.as<float2>());
             launch_zero_f64(m + 1, w_g.as<double2>(), stream);
             launch_set_scalar_c(w_g.as<double2>(), scal + 1, stream);
             int jdone = 0;
             for (int j = 0; j < m; j++) {
-                double2 *vj = V + (size_t)j * n;
-                launch_gemv_c64(R, n, A, lda, vj, 1, w_t.p, 0, stream);                      // t = A v_j
+                launch_gemv_c64(R, n, A, lda, w_vf.p, 0, w_t.p, 0, stream);                  // t = A v_j (c64 copy)
                 launch_gemv_h_c64(R, n, A, lda, w_t.p, 0, w_w.p, 1, w_part.p, stream);      // w = A^H t
                 launch_dots(n, j + 1, V, n, w_w.as<double2>(), w_h1.as<double2>(), nullptr, stream);
                 launch_update(n, j + 1, V, n, w_h1.as<double2>(), w_w.as<double2>(), stream);
@@ -153,7 +154,7 @@ void bem_solver_s::solve_refined(bem_solve_info_t *info) {
                 launch_update(n, j + 1, V, n, w_h2.as<double2>(), w_w.as<double2>(), stream);
                 launch_nrm2(n, w_w.as<double2>(), scal + 2, nullptr, stream);
                 launch_hcol_finish(j, w_h1.as<double2>(), w_h2.as<double2>(), scal + 2, w_H.as<double2>(), ldh, stream);
-                launch_scale_copy(n, w_w.as<double2>(), scal + 2, V + (size_t)(j + 1) * n, stream);
+                launch_scale_copy(n, w_w.as<double2>(), scal + 2, V + (size_t)(j + 1) * n, stream, w_vf.as<float2>());
                 launch_givens(j, w_H.as<double2>(), ldh, w_cs.as<double2>(), w_sn.as<double2>(),
                               w_g.as<double2>(), scal + 3, stream);
                 jdone = j + 1;

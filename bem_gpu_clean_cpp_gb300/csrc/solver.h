@@ -64,7 +64,7 @@ struct bem_solver_s {
     bem::DevMem d_A, d_B, d_cpart, d_bpart, d_x;
 
     // GMRES / refinement workspace
-    bem::DevMem w_V, w_H, w_cs, w_sn, w_g, w_y, w_h1, w_h2, w_w, w_t, w_r, w_gv, w_part, w_scal;
+    bem::DevMem w_V, w_H, w_cs, w_sn, w_g, w_y, w_h1, w_h2, w_w, w_t, w_r, w_gv, w_vf, w_part, w_scal;
     double *h_pinned = nullptr;
     // QR workspace
     bem::DevMem q_A, q_B, q_tau, q_work, q_info;

@@ -1,0 +1,487 @@
+#!/usr/bin/env python3
+"""BEM solves/s on GB300 -- the headline benchmark.
+
+Workload (the precision configuration): rigid (Neumann, bc = (0, 1, 0)) unit
+sphere as an icosphere at subdivision 5 (10242 nodes, 20480 triangles) at
+ka = 10, a plane wave from a seeded random direction, 32 seeded CHIEF points
+uniform in r < 0.5; system (10274 x 10242) complex.
+
+One step = one complete surface solve through the library:
+  assembly  -- FP32 regular quadrature, FP64 singular and near-singular pairs
+               (eta = 1, depth 2), c64 storage, rewritten every step;
+  solve     -- GMRES on the normal equations with FP32 matrix products and
+               FP64 Arnoldi/Givens, inside FP64 iterative refinement to a
+               relative normal-equation residual of 1e-8.
+
+value: solves/s with inputs resident in HBM.  e2e: the same through the C ABI
+from pinned host buffers (geometry, sources in; surface pressure out).
+The plain FP64 path (FP64 assembly + Householder QR, one solve) is run once
+and the mixed solution's error against it is reported.
+
+--impl reference times the CPU restatement of the path (the FP64 oracle,
+OpenMP on every host core) on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+WORKLOAD = "rigid-sphere icosphere s5 (N=10242, E=20480), ka=10, seeded plane wave, 32 CHIEF"
+METRIC = "BEM solves/s (surface solve, <=1e-5 rel err vs FP64)"
+UNIT = "solves/s"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--subdiv", type=int, default=5)
+    ap.add_argument("--ka", type=float, default=10.0)
+    ap.add_argument("--chief", type=int, default=32)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--eta", type=float, default=1.0)
+    ap.add_argument("--depth", type=int, default=2)
+    ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 reference solve")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--mode", default="bench", choices=["bench", "profile"],
+                    help="profile: one warm-up solve and one more solve, nothing timed (for ncu captures)")
+    return ap.parse_args()
+
+
+def run_profile(args):
+    """Two solves of the workload and nothing else, so that an ncu capture
+    (-k <kernel> -s/-c) sees the kernels of a steady-state solve."""
+    import bem_gpu_clean_cpp_gb300 as bem
+    pts, elems, chief, d, k, bc = workload(args)
+    s = bem.Solver(near_eta=args.eta, near_depth=args.depth, tol=1e-8, inner_tol=1e-4, max_iter=300)
+    s.set_geometry(pts, elems, bc=bc, chief=chief)
+    s.set_sources([("plane", d, 1.0)])
+    for _ in range(2):
+        s.assemble(k, bem.PREC_C64)
+        info = s.solve(bem.SOLVE_GMRES_REFINED)
+    s.sync()
+    print(json.dumps({"mode": "profile", "iterations": info.iterations, "refinements": info.refinements,
+                      "rel_residual": info.rel_residual}))
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# Synthetic inputs (numpy, shared by both arms)
+# ---------------------------------------------------------------------------
+def icosphere(subdiv: int, radius: float = 1.0):
+    """Icosahedron subdivided `subdiv` times, projected to the sphere, faces
+    wound so that (p1-p3) x (p2-p3) points inwards."""
+    t = (1 + 5 ** 0.5) / 2
+    v = [[-1, t, 0], [1, t, 0], [-1, -t, 0], [1, -t, 0], [0, -1, t], [0, 1, t], [0, -1, -t], [0, 1, -t],
+         [t, 0, -1], [t, 0, 1], [-t, 0, -1], [-t, 0, 1]]
+    v = [np.array(p, dtype=np.float64) / np.linalg.norm(p) for p in v]
+    f = [[0, 11, 5], [0, 5, 1], [0, 1, 7], [0, 7, 10], [0, 10, 11], [1, 5, 9], [5, 11, 4], [11, 10, 2],
+         [10, 7, 6], [7, 1, 8], [3, 9, 4], [3, 4, 2], [3, 2, 6], [3, 6, 8], [3, 8, 9], [4, 9, 5], [2, 4, 11],
+         [6, 2, 10], [8, 6, 7], [9, 8, 1]]
+    for _ in range(subdiv):
+        cache = {}
+
+        def mid(a, b):
+            key = (a, b) if a < b else (b, a)
+            if key not in cache:
+                p = v[a] + v[b]
+                v.append(p / np.linalg.norm(p))
+                cache[key] = len(v) - 1
+            return cache[key]
+        nf = []
+        for a, b, c in f:
+            ab, bc, ca = mid(a, b), mid(b, c), mid(c, a)
+            nf += [[a, ab, ca], [b, bc, ab], [c, ca, bc], [ab, bc, ca]]
+        f = nf
+    p = np.array(v) * radius
+    f = np.array(f, dtype=np.int32)
+    n = np.cross(p[f[:, 0]] - p[f[:, 2]], p[f[:, 1]] - p[f[:, 2]])
+    out = np.einsum("ij,ij->i", n, p[f].sum(axis=1)) > 0
+    f[out, 0], f[out, 1] = f[out, 1].copy(), f[out, 0].copy()
+    return p, f
+
+
+def workload(args):
+    rng = np.random.default_rng(args.seed)
+    pts, elems = icosphere(args.subdiv)
+    u = rng.random((args.chief, 3))
+    r = 0.5 * np.cbrt(u[:, 0])
+    th = np.arccos(1 - 2 * u[:, 1])
+    ph = 2 * np.pi * u[:, 2]
+    chief = np.stack([r * np.sin(th) * np.cos(ph), r * np.sin(th) * np.sin(ph), r * np.cos(th)], axis=1)
+    d = rng.standard_normal(3)
+    d /= np.linalg.norm(d)
+    bc = np.tile(np.array([0, 1, 0], dtype=np.complex128), (elems.shape[0], 1))
+    return pts, elems, chief, d, float(args.ka), bc
+
+
+# ---------------------------------------------------------------------------
+# Distributed helpers (replicas: every rank solves its own copy)
+# ---------------------------------------------------------------------------
+def dist_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class Dist:
+    def __init__(self, use_cuda: bool):
+        self.rank, self.world, self.local = dist_info()
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as td
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            td.init_process_group(backend="nccl" if use_cuda else "gloo")
+            self.pg = td
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64, device="cuda" if self.pg.get_backend() == "nccl" else "cpu")
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+# Clock sampling during the timed region
+# ---------------------------------------------------------------------------
+class Clocks:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, power, reasons = [], [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+                power.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[4:8]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "power_w_max": max(power) if power else None, "samples": len(sm), "reasons": sorted(reasons)}
+
+
+# ---------------------------------------------------------------------------
+# CPU restatement timing (the oracle), bounded sample of the same workload
+# ---------------------------------------------------------------------------
+def cpu_sample(pts, elems, chief, d, k, bc, eta, depth, threads, rows=64, n_qr=1024):
+    """FP64 CPU solve time of the full workload, extrapolated from a sample:
+    assembly of `rows` rows (all elements, x (N+M)/rows) plus a Householder QR
+    least-squares solve of an (n_qr+32) x n_qr system (x flop ratio
+    (8mn^2 - 8n^3/3) of the full system)."""
+    import oracle
+    oracle.build()
+    oracle.set_threads(threads)
+    R, N = pts.shape[0] + chief.shape[0], pts.shape[0]
+    allp = np.vstack([pts, chief])
+    prm = oracle.params(near_eta=eta, near_depth=depth)
+    t0 = time.perf_counter()
+    oracle.assemble(allp, elems, k, N, [("plane", d, 1.0)], bc=bc, prm=prm, rows=(0, rows))
+    t_asm = (time.perf_counter() - t0) * R / rows
+    rng = np.random.default_rng(1)
+    m_s = n_qr + 32
+    Aq = rng.standard_normal((m_s, n_qr)) + 1j * rng.standard_normal((m_s, n_qr))
+    Bq = rng.standard_normal((m_s, 1)) + 1j * rng.standard_normal((m_s, 1))
+    t0 = time.perf_counter()
+    oracle.lsq_qr(Aq, Bq)
+    t_qr_s = time.perf_counter() - t0
+    flops = lambda m, n: 8.0 * m * n * n - 8.0 / 3.0 * n ** 3
+    t_qr = t_qr_s * flops(R, N) / flops(m_s, n_qr)
+    total = t_asm + t_qr
+    return {"value": 1.0 / total, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"oracle FP64: assembly of {rows}/{R} rows (x{R / rows:.1f}) + Householder LS-QR "
+                      f"{m_s}x{n_qr} (x{flops(R, N) / flops(m_s, n_qr):.0f} by flop count); "
+                      f"extrapolated solve {total:.1f} s (assembly {t_asm:.1f} s, QR {t_qr:.1f} s)"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return 0
+    pts, elems, chief, d, k, bc = workload(args)
+    threads = os.cpu_count() or 1
+    vals = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_sample(pts, elems, chief, d, k, bc, args.eta, args.depth, threads, rows=16, n_qr=512)
+        if i >= args.warmup:
+            vals.append(r["value"])
+    v = float(np.mean(vals))
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "subdiv": args.subdiv, "ka": args.ka, "chief": args.chief,
+                       "seed": args.seed, "near_eta": args.eta},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": r["sample"].replace("16/", "16 rows of ") + "; per step"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# Our arm
+# ---------------------------------------------------------------------------
+# Algorithmic bytes per launch of the HBM-bound kernels (A is (N+M) x N c64).
+def kernel_bytes(name, R, N):
+    a = 8.0 * R * N
+    return {"gemv_c64": a + 16.0 * N + 8.0 * R,
+            "gemv_h_c64": a + 8.0 * R + 16.0 * N,
+            "resid": a + 16.0 * N + 32.0 * R,
+            "gemv_h_f64": a + 16.0 * R + 16.0 * N}.get(name)
+
+
+def run_ours(args):
+    import torch
+    import bem_gpu_clean_cpp_gb300 as bem
+
+    dist = Dist(use_cuda=True)
+    torch.cuda.set_device(dist.local)
+    bem.lib()
+    pts, elems, chief, d, k, bc = workload(args)
+    N, E, M = pts.shape[0], elems.shape[0], chief.shape[0]
+    R = N + M
+    src = [("plane", d, 1.0)]
+    opts = dict(near_eta=args.eta, near_depth=args.depth, tol=1e-8, inner_tol=1e-4, max_iter=300, max_refine=10)
+
+    s = bem.Solver(**opts)
+    s.set_geometry(pts, elems, bc=bc, chief=chief)
+    s.set_sources(src)
+    stream = torch.cuda.ExternalStream(s.stream())
+    infos = []
+
+    def step():
+        s.assemble(k, bem.PREC_C64)
+        infos.append(s.solve(bem.SOLVE_GMRES_REFINED))
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    s.sync()
+    torch.cuda.synchronize()
+
+    # ---- timed region: inputs resident, K steps ----
+    infos.clear()
+    dev_index = int(os.environ.get("CUDA_VISIBLE_DEVICES", str(dist.local)).split(",")[0]) \
+        if os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0].isdigit() else dist.local
+    clocks = Clocks(dev_index)
+    bem.profile_enable(True)
+    l0 = bem.launch_count()
+    dist.barrier()
+    torch.cuda.synchronize()
+    s.sync()
+    clocks.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for i in range(args.steps):
+        ev[i][0].record(stream)
+        step()
+        ev[i][1].record(stream)
+    s.sync()
+    torch.cuda.synchronize()
+    dist.barrier()
+    clk = clocks.stop()
+    launches = bem.launch_count() - l0
+    prof = bem.profile_report()
+    bem.profile_enable(False)
+    lat = [a.elapsed_time(b) for a, b in ev]
+    total_ms = ev[0][0].elapsed_time(ev[-1][1])
+    total_ms = dist.max(total_ms)
+    value = dist.world * args.steps / (total_ms / 1000.0)
+
+    # ---- e2e: host buffers through the C ABI, pinned memory ----
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    h_pts, h_elems, h_chief, h_bc = pin(pts), pin(elems), pin(chief), pin(bc)
+    h_x = torch.empty((1, N), dtype=torch.complex128).pin_memory().numpy().T
+    s2 = bem.Solver(**opts)
+    # Bytes the library copies host -> device per step: nodes (24N), row
+    # points in double and hi/lo float (24R + 32R), elements (16E), bc (48E),
+    # one column tile's element records (32E) and column map (4N + 12), the
+    # source record (48); device -> host: the surface pressure (16N) plus the
+    # 8-byte residual estimates read by the solver loop.
+    h2d = 24 * N + 56 * R + 64 * E + 32 * E + 4 * N + 12 + 48
+    d2h = h_x.nbytes
+
+    def e2e_step():
+        s2.set_geometry(h_pts, h_elems, bc=h_bc, chief=h_chief)
+        s2.set_sources(src)
+        s2.assemble(k, bem.PREC_C64)
+        s2.solve(bem.SOLVE_GMRES_REFINED)
+        s2.solution(out=h_x)
+
+    for _ in range(max(1, min(2, args.warmup))):
+        e2e_step()
+    dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = dist.max(time.perf_counter() - t0)
+    e2e_value = dist.world * args.steps / e2e_s
+    x_mixed = h_x[:, 0].copy()
+    if infos:
+        d2h += 8 * int(np.mean([i.iterations + 2 * i.refinements + 1 for i in infos]))
+
+    # ---- plain FP64 path once (FP64 assembly + Householder QR) ----
+    fp64 = None
+    if not args.no_fp64:
+        s3 = bem.Solver(**opts)
+        s3.set_geometry(pts, elems, bc=bc, chief=chief)
+        s3.set_sources(src)
+        st3 = torch.cuda.ExternalStream(s3.stream())
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(st3)
+        s3.assemble(k, bem.PREC_C128)
+        s3.solve(bem.SOLVE_QR)
+        b.record(st3)
+        s3.sync()
+        ms64 = a.elapsed_time(b)
+        x64 = s3.solution()[:, 0]
+        err = float(np.abs(x_mixed - x64).max() / np.abs(x64).max())
+        fp64 = {"ms": ms64, "solves_per_s": 1000.0 / ms64, "rel_err_mixed_vs_fp64": err,
+                "speedup_mixed_vs_fp64": (1000.0 / ms64) and value / dist.world / (1000.0 / ms64)}
+        del s3
+
+    # ---- roofline of the dominant kernel ----
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    peak_src = "of measured" if "hbm_gbs" in peaks else "of fallback"
+    per_kernel = {n: {"launches": c, "total_ms": ms, "avg_ms": ms / max(c, 1)} for n, (c, ms) in prof.items()}
+    dom = max(per_kernel, key=lambda n: per_kernel[n]["total_ms"])
+    hbm_kernels = [n for n in per_kernel if kernel_bytes(n, R, N)]
+    hbm_dom = max(hbm_kernels, key=lambda n: per_kernel[n]["total_ms"]) if hbm_kernels else None
+    traffic = None
+    try:
+        tr = json.load(open(os.path.join(ROOT, "profiles", "ncu_traffic.json")))
+        traffic = tr.get(hbm_dom, {}).get("bytes_per_launch")
+    except (OSError, ValueError):
+        pass
+    roofline = None
+    if hbm_dom:
+        bpl = kernel_bytes(hbm_dom, R, N)
+        ach = bpl / (per_kernel[hbm_dom]["avg_ms"] / 1000.0) / 1e9
+        roofline = {"kernel": hbm_dom, "bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
+                    "frac": ach / hbm_peak, "traffic": traffic, "peak_source": peak_src,
+                    "algorithmic_bytes_per_launch": bpl}
+    asm = per_kernel.get("far_assembly_f32")
+    pairs = R * E
+    far_extra = None
+    if asm:
+        # 60 FP32 flops + 3 MUFU per quadrature point (36 points per pair)
+        tflops = 60.0 * 36 * pairs / (asm["avg_ms"] / 1000.0) / 1e12
+        mhz = clk.get("sm_mhz") or 2070.0
+        fp32_peak = 152 * 128 * 2 * mhz * 1e6 / 1e12
+        far_extra = {"kernel": "far_assembly_f32", "bound": "fp32", "achieved": tflops, "unit": "TFLOP/s",
+                     "peak": fp32_peak, "frac": tflops / fp32_peak,
+                     "peak_source": f"nominal 152 SM x 128 FP32 lanes x 2 at the sampled {mhz:.0f} MHz",
+                     "pairs_per_launch": pairs}
+    it = [i.iterations for i in infos]
+    A_bytes = 8.0 * R * N
+    B_bytes = 16.0 * R
+    asm_ms = (per_kernel.get("far_assembly_f32", {"avg_ms": 0})["avg_ms"] +
+              per_kernel.get("near_assembly_f64", {"avg_ms": 0})["avg_ms"])
+
+    cpu = None
+    if dist.rank == 0 and not args.no_cpu:
+        cpu = cpu_sample(pts, elems, chief, d, k, bc, args.eta, args.depth, os.cpu_count() or 1)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c64 (FP32) + f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "subdiv": args.subdiv, "nodes": N, "triangles": E, "chief": M,
+                   "ka": args.ka, "seed": args.seed, "near_eta": args.eta, "near_depth": args.depth,
+                   "refine_tol": 1e-8, "parallelism": f"replicas x{dist.world}",
+                   "l2": "inputs larger than L2: A (%.0f MB c64) is rewritten every step" % (A_bytes / 1e6)},
+        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                       "min": min(lat), "max": max(lat)},
+        "solver": {"inner_iterations_per_solve": float(np.mean(it)) if it else None,
+                   "refinements": max(i.refinements for i in infos) if infos else None,
+                   "rel_residual": max(i.rel_residual for i in infos) if infos else None},
+        "assembly_gbs": (A_bytes + B_bytes) / (asm_ms / 1000.0) / 1e9 if asm_ms else None,
+        "fp64_plain": fp64,
+        "roofline": roofline,
+        "roofline_assembly": far_extra,
+        "kernels": per_kernel,
+        "dominant_kernel": dom,
+        "gpu_launches": launches,
+        "clocks": clk,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "cpu_baseline": cpu,
+    }
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    dist.close()
+    return 0
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    if args.mode == "profile":
+        return run_profile(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

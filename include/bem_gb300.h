@@ -38,6 +38,14 @@ const char *bem_last_error(void);
 int bem_version(void);
 /* Number of CUDA kernels this library has launched in the process. */
 long long bem_launch_count(void);
+/* Kernel timing: while on, every kernel (and cuSOLVER call sequence) the
+ * library launches is bracketed by CUDA events on its stream.  Turning it
+ * on clears the previous records. */
+int bem_profile_enable(int on);
+/* Writes one "name launches total_ms\n" line per kernel name into buf
+ * (after waiting for the recorded events); returns the number of lines or a
+ * negative status. */
+int bem_profile_report(char *buf, int buflen);
 
 /* ------------------------------------------------------------------ */
 /* Quadrature: gaussQuad (numerical.h:166-187)                          */

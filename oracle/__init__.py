@@ -143,7 +143,7 @@ def assemble(pts, elems, k, n_nodes, srcs, bc=None, prm=None, rows=None, want_A=
     """A ((N+M) x N) and B ((N+M) x S) in FP64, column-major complex128 arrays.
 
     pts holds the N nodes followed by the M CHIEF points.  rows=(r0, r1)
-    restricts the work to a row range (the other rows are left zero)."""
+    computes only that row range and returns its (r1-r0) rows."""
     prm = prm or params()
     pts = np.ascontiguousarray(pts, dtype=np.float64)
     elems = np.ascontiguousarray(elems, dtype=np.int32)
@@ -151,18 +151,19 @@ def assemble(pts, elems, k, n_nodes, srcs, bc=None, prm=None, rows=None, want_A=
     N = int(n_nodes)
     M = R - N
     S = len(srcs)
-    A = np.zeros((R, N), dtype=np.complex128, order="F") if want_A else None
-    B = np.zeros((R, max(S, 1)), dtype=np.complex128, order="F")
+    r0, r1 = (0, R) if rows is None else rows
+    nr = r1 - r0
+    A = np.zeros((nr, N), dtype=np.complex128, order="F") if want_A else None
+    B = np.zeros((nr, max(S, 1)), dtype=np.complex128, order="F")
     bcp = None
     if bc is not None:
         bcarr = np.ascontiguousarray(np.asarray(bc, dtype=np.complex128).reshape(-1, 3))
         bcp = bcarr.view(np.float64)
-    r0, r1 = (0, R) if rows is None else rows
     st = lib().orc_assemble(N, M, _dp(pts), elems.shape[0], _ip(elems),
                             _dp(bcp) if bcp is not None else None, float(k), ctypes.byref(prm),
                             S, sources(srcs), _dp(A.reshape(-1, order="F").view(np.float64))
-                            if A is not None else None, R,
-                            _dp(B.reshape(-1, order="F").view(np.float64)), R, int(r0), int(r1))
+                            if A is not None else None, nr,
+                            _dp(B.reshape(-1, order="F").view(np.float64)), nr, int(r0), int(r1))
     if st != 0:
         raise ValueError(f"orc_assemble failed ({st})")
     return A, B

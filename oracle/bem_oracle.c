@@ -319,7 +319,9 @@ static cplx incident(double k, const orc_source *s, const double *x) {
  *     same three updates.
  * bc holds (ca, cb, cc) per element as 6 doubles (re, im); NULL means the
  * readObj default (0, 1, -1) (mesh.cu:1240-1242).
- * Each row is independent; rows are spread over OpenMP threads.
+ * Only rows row_begin..row_end-1 are computed; A and B hold those rows
+ * (local row x - row_begin).  Each row is independent; rows are spread over
+ * OpenMP threads.
  */
 int orc_assemble(int N, int M, const double *pts, int E, const int *elems, const double *bc,
                  double k, const orc_params *prm, int S, const orc_source *src,
@@ -336,7 +338,7 @@ int orc_assemble(int N, int M, const double *pts, int E, const int *elems, const
     for (int x = row_begin; x < row_end; x++) {
         const double *px = pts + 3 * (size_t)x;
         if (A) {
-            for (int j = 0; j < N; j++) A[IDX(x, j, lda)] = (x == j) ? 1.0 : 0.0;
+            for (int j = 0; j < N; j++) A[IDX(x - row_begin, j, lda)] = (x == j) ? 1.0 : 0.0;
         }
         cplx beta = 0.0;
         double csum = 0.0;
@@ -361,16 +363,16 @@ int orc_assemble(int N, int M, const double *pts, int E, const int *elems, const
                 for (int j = 0; j < 3; j++) {
                     cplx gj = g[2 * j] + I * g[2 * j + 1];
                     cplx hj = h[2 * j] + I * h[2 * j + 1];
-                    if (A) A[IDX(x, nd[j], lda)] += hj - bcA * gj;
+                    if (A) A[IDX(x - row_begin, nd[j], lda)] += hj - bcA * gj;
                     gs += gj;
                 }
                 if (x < N) csum += c;
                 beta += bcC * gs;
             }
         }
-        if (A && x < N) A[IDX(x, x, lda)] -= csum;
+        if (A && x < N) A[IDX(x - row_begin, x, lda)] -= csum;
         if (B) {
-            for (int s = 0; s < S; s++) B[IDX(x, s, ldb)] = incident(k, src + s, px) - beta;
+            for (int s = 0; s < S; s++) B[IDX(x - row_begin, s, ldb)] = incident(k, src + s, px) - beta;
         }
     }
     return err;
