@@ -58,7 +58,7 @@ class Options(ctypes.Structure):
     _fields_ = [("density", ctypes.c_double), ("speed", ctypes.c_double), ("order", ctypes.c_int),
                 ("near_eta", ctypes.c_double), ("near_depth", ctypes.c_int), ("tol", ctypes.c_double),
                 ("max_iter", ctypes.c_int), ("inner_tol", ctypes.c_double),
-                ("max_refine", ctypes.c_int), ("tile_cols", ctypes.c_int)]
+                ("max_refine", ctypes.c_int), ("tile_cols", ctypes.c_int), ("far_variant", ctypes.c_int)]
 
 
 class SolveInfo(ctypes.Structure):

@@ -601,6 +601,7 @@ int bem_options_default(bem_options_t *o) {
     o->inner_tol = 1e-4;
     o->max_refine = 10;
     o->tile_cols = 0;
+    o->far_variant = -1;
     apply_global_options(o);
     return BEM_SUCCESS;
 }
@@ -625,6 +626,7 @@ int bem_solver_set_options(bem_solver_t s, const bem_options_t *o) {
     BEM_CHECK_ARG(o->near_eta >= 0 && o->near_depth >= 0 && o->near_depth <= 4, "near_eta >= 0, near_depth in [0, 4]");
     BEM_CHECK_ARG(o->tol > 0 && o->max_iter >= 1 && o->inner_tol > 0 && o->max_refine >= 0, "bad solver tolerances");
     BEM_CHECK_ARG(o->tile_cols >= 0, "tile_cols must be >= 0");
+    BEM_CHECK_ARG(o->far_variant >= -1 && o->far_variant < far_variants(BEM_PREC_C64), "bad far_variant");
     if (o->tile_cols != s->opt.tile_cols) s->tiles[0].valid = s->tiles[1].valid = false;
     s->opt = *o;
     s->assembled = s->solved = false;

@@ -227,6 +227,75 @@ __device__ __forceinline__ void far_sums_f32(float3 d3, float3 e1, float3 e2, fl
     }
 }
 
+// The same sums for the 6 x 6 rule (the reference's INTORDER = 6), arranged
+// for the FP32 issue rate:
+//   * the Duffy points lie on lines of constant theta_n: d = d3 + rho_m v_n
+//     with v_n = e1 + theta_n (e2 - e1), so a point costs 3 FMAs for d;
+//   * along a line, S0 needs sum w_m rho_m f and S1, S2 both need
+//     sum w_m rho_m^2 f (xi1 = rho (1-theta), xi2 = rho theta): two inner sums
+//     per quantity instead of three;
+//   * with E = exp(-ikr) = c - i s:  4 pi G = E/r  and
+//     4 pi dG/dn = -(hgt/r^3) [(c + kr s) + i (kr c - s)],
+//     4 pi dG0/dn = -hgt/r^3, so the height leaves the sums.
+// The Gauss abscissae/weights are the published 6-point values as
+// compile-time constants; the loops unroll completely.
+__device__ __forceinline__ float gl6_x(int i) {
+    return i == 0 ? -0.9324695142031521f : i == 1 ? -0.6612093864662645f : i == 2 ? -0.2386191860831969f
+         : i == 3 ? 0.2386191860831969f : i == 4 ? 0.6612093864662645f : 0.9324695142031521f;
+}
+__device__ __forceinline__ float gl6_w(int i) {
+    return (i == 0 || i == 5) ? 0.1713244923791704f : (i == 1 || i == 4) ? 0.3607615730481386f
+                                                                           : 0.4679139345726910f;
+}
+
+__device__ __forceinline__ void far_sums_f32_o6(float3 d3, float3 e1, float3 e2, float hgt, float k,
+                                                SumsF &S) {
+    S.g0r = S.g0i = S.g1r = S.g1i = S.g2r = S.g2i = 0.0f;
+    S.h0r = S.h0i = S.h1r = S.h1i = S.h2r = S.h2i = 0.0f;
+    S.c = 0.0f;
+    const float3 e21 = make_float3(e2.x - e1.x, e2.y - e1.y, e2.z - e1.z);
+#pragma unroll
+    for (int n = 0; n < 6; n++) {
+        const float th = 0.5f + 0.5f * gl6_x(n);
+        const float vx = fmaf(th, e21.x, e1.x), vy = fmaf(th, e21.y, e1.y), vz = fmaf(th, e21.z, e1.z);
+        float u0gr = 0.f, u1gr = 0.f, u0gs = 0.f, u1gs = 0.f;
+        float u0ha = 0.f, u1ha = 0.f, u0hb = 0.f, u1hb = 0.f, u0c = 0.f;
+#pragma unroll
+        for (int m = 0; m < 6; m++) {
+            const float rho = 0.5f + 0.5f * gl6_x(m);
+            const float wr1 = gl6_w(m) * rho, wr2 = gl6_w(m) * rho * rho;
+            const float dx = fmaf(rho, vx, d3.x), dy = fmaf(rho, vy, d3.y), dz = fmaf(rho, vz, d3.z);
+            const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+            const float ri = rsqrtf(r2);
+            const float kr = k * (r2 * ri);
+            float sn, cs;
+            __sincosf(kr, &sn, &cs);
+            const float A = fmaf(kr, sn, cs);      // c + kr s
+            const float Bv = fmaf(kr, cs, -sn);    // kr c - s
+            const float ri3 = ri * ri * ri;
+            const float gr = cs * ri, gs = sn * ri;
+            const float ha = ri3 * A, hb = ri3 * Bv;
+            u0gr = fmaf(wr1, gr, u0gr); u1gr = fmaf(wr2, gr, u1gr);
+            u0gs = fmaf(wr1, gs, u0gs); u1gs = fmaf(wr2, gs, u1gs);
+            u0ha = fmaf(wr1, ha, u0ha); u1ha = fmaf(wr2, ha, u1ha);
+            u0hb = fmaf(wr1, hb, u0hb); u1hb = fmaf(wr2, hb, u1hb);
+            u0c = fmaf(wr1, ri3, u0c);
+        }
+        const float a = 0.25f * gl6_w(n), b = a * (1.0f - th), c = a * th;
+        S.g0r = fmaf(a, u0gr, S.g0r); S.g1r = fmaf(b, u1gr, S.g1r); S.g2r = fmaf(c, u1gr, S.g2r);
+        S.g0i = fmaf(a, u0gs, S.g0i); S.g1i = fmaf(b, u1gs, S.g1i); S.g2i = fmaf(c, u1gs, S.g2i);
+        S.h0r = fmaf(a, u0ha, S.h0r); S.h1r = fmaf(b, u1ha, S.h1r); S.h2r = fmaf(c, u1ha, S.h2r);
+        S.h0i = fmaf(a, u0hb, S.h0i); S.h1i = fmaf(b, u1hb, S.h1i); S.h2i = fmaf(c, u1hb, S.h2i);
+        S.c = fmaf(a, u0c, S.c);
+    }
+    // signs and the height: G = (gr, -gs); dG/dn = -hgt (ha, hb); dG0/dn = -hgt c
+    const float mh = -hgt;
+    S.g0i = -S.g0i; S.g1i = -S.g1i; S.g2i = -S.g2i;
+    S.h0r *= mh; S.h1r *= mh; S.h2r *= mh;
+    S.h0i *= mh; S.h1i *= mh; S.h2i *= mh;
+    S.c *= mh;
+}
+
 // Same in FP64 (used by the c128 far path and by the field kernel in c128).
 struct SumsD {
     double g0r, g0i, g1r, g1i, g2r, g2i;
@@ -302,97 +371,81 @@ __device__ __forceinline__ void finish_coeffs(const SUMS &S, T scale, T rw, T bA
 // Far-field assembly kernel.
 // grid = (ceil(R/TR), ntiles), block = NT threads, dynamic smem = acc[TR][tc].
 // ---------------------------------------------------------------------------
-template <int TR, int NT>
-__global__ void __launch_bounds__(NT, 1)
+template <int TR, int NT, int MINB, bool O6>
+__global__ void __launch_bounds__(NT, MINB)
 far_assembly_f32(RowPoints rows, int N, GeoTables geo, TileSet tiles, float k, float rw,
                  float2 *__restrict__ A, size_t lda, float *__restrict__ c_part,
                  float2 *__restrict__ beta_part) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2 *acc = reinterpret_cast<float2 *>(smem_raw);
+    __shared__ float red[NT / 32][3];
     const int tile = blockIdx.y;
     const int tc = tiles.col_cnt[tile];
     const int r0 = blockIdx.x * TR;
     const int R = rows.R;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int i = threadIdx.x; i < TR * tc; i += NT) acc[i] = make_float2(0.f, 0.f);
-
-    float4 xh[TR], xl[TR];
-#pragma unroll
-    for (int t = 0; t < TR; t++) {
-        int row = min(r0 + t, R - 1);
-        xh[t] = rows.f[2 * (size_t)row];
-        xl[t] = rows.f[2 * (size_t)row + 1];
-    }
     __syncthreads();
 
     const int nq = c_nq;
     const float inv4pi = (float)(1.0 / (4.0 * kPi));
-    float csum[TR], bsr[TR], bsi[TR];
-#pragma unroll
-    for (int t = 0; t < TR; t++) csum[t] = bsr[t] = bsi[t] = 0.0f;
-
     const int rb = tiles.rec_ptr[tile], re = tiles.rec_ptr[tile + 1];
-    for (int i = rb + threadIdx.x; i < re; i += NT) {
-        const TileRec rec = tiles.recs[i];
-        const float4 *g = geo.geo_f + (size_t)kGeoF * rec.eid;
-        const float4 g0 = g[0], g1 = g[1], g2 = g[2], g3 = g[3], g4 = g[4], g5 = g[5];
-        const int4 nd = make_int4(rec.node[0], rec.node[1], rec.node[2], 0);
-        const float3 e1 = make_float3(g2.x, g2.y, g2.z), e2 = make_float3(g3.x, g3.y, g3.z);
-        const float scale = g0.w * inv4pi;
-#pragma unroll
-        for (int t = 0; t < TR; t++) {
-            const int row = r0 + t;
-            if (row >= R) break;
-            if (pair_is_near(row, N, nd, xh[t], g)) continue;
-            float3 d3 = make_float3((g0.x - xh[t].x) + (g1.x - xl[t].x),
-                                    (g0.y - xh[t].y) + (g1.y - xl[t].y),
-                                    (g0.z - xh[t].z) + (g1.z - xl[t].z));
-            float hgt = d3.x * g4.x + d3.y * g4.y + d3.z * g4.z;
+    // One pass over the tile's element list per row (rows are not
+    // interleaved, which keeps the per-thread state to one pair).
+#pragma unroll 1
+    for (int t = 0; t < TR; t++) {
+        const int row = r0 + t;
+        if (row >= R) break;                              // uniform over the CTA
+        const float4 xh = rows.f[2 * (size_t)row], xl = rows.f[2 * (size_t)row + 1];
+        float csum = 0.f, bsr = 0.f, bsi = 0.f;
+        float2 *arow = acc + (size_t)t * tc;
+        for (int i = rb + threadIdx.x; i < re; i += NT) {
+            const TileRec rec = tiles.recs[i];
+            const float4 *g = geo.geo_f + (size_t)kGeoF * rec.eid;
+            const int4 nd = make_int4(rec.node[0], rec.node[1], rec.node[2], 0);
+            if (pair_is_near(row, N, nd, xh, g)) continue;
+            const float4 g0 = g[0], g1 = g[1], g2 = g[2], g3 = g[3], g4 = g[4], g5 = g[5];
+            const float3 e1 = make_float3(g2.x, g2.y, g2.z), e2 = make_float3(g3.x, g3.y, g3.z);
+            const float3 d3 = make_float3((g0.x - xh.x) + (g1.x - xl.x), (g0.y - xh.y) + (g1.y - xl.y),
+                                          (g0.z - xh.z) + (g1.z - xl.z));
+            const float hgt = d3.x * g4.x + d3.y * g4.y + d3.z * g4.z;
             SumsF S;
-            far_sums_f32(d3, e1, e2, hgt, k, nq, S);
+            if (O6) far_sums_f32_o6(d3, e1, e2, hgt, k, S);
+            else far_sums_f32(d3, e1, e2, hgt, k, nq, S);
             Coeffs<float, SumsF> o;
-            finish_coeffs<float, SumsF>(S, scale, rw, g5.x, g5.y, g5.z, g5.w, o);
-            float2 *arow = acc + (size_t)t * tc;
+            finish_coeffs<float, SumsF>(S, g0.w * inv4pi, rw, g5.x, g5.y, g5.z, g5.w, o);
 #pragma unroll
             for (int j = 0; j < 3; j++) {
-                int s = rec.slot[j];
+                const int s = rec.slot[j];
                 if (s >= 0) {
                     atomicAdd(&arow[s].x, o.ar[j]);
                     atomicAdd(&arow[s].y, o.ai[j]);
                 }
             }
             if (rec.owner) {
-                csum[t] += o.c;
-                bsr[t] += o.br;
-                bsi[t] += o.bi;
+                csum += o.c;
+                bsr += o.br;
+                bsi += o.bi;
             }
         }
-    }
-    // Per-row reduction of the c and beta partial sums (fixed order).
-    __shared__ float red[NT / 32][TR][3];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int t = 0; t < TR; t++) {
-        float a = csum[t], b = bsr[t], c = bsi[t];
-        for (int o = 16; o > 0; o >>= 1) {
-            a += __shfl_xor_sync(0xffffffffu, a, o);
-            b += __shfl_xor_sync(0xffffffffu, b, o);
-            c += __shfl_xor_sync(0xffffffffu, c, o);
+        // Row reduction of the c and beta partial sums (fixed order).
+        for (int off = 16; off > 0; off >>= 1) {
+            csum += __shfl_xor_sync(0xffffffffu, csum, off);
+            bsr += __shfl_xor_sync(0xffffffffu, bsr, off);
+            bsi += __shfl_xor_sync(0xffffffffu, bsi, off);
         }
-        if (lane == 0) { red[warp][t][0] = a; red[warp][t][1] = b; red[warp][t][2] = c; }
-    }
-    __syncthreads();
-    if (threadIdx.x < TR) {
-        const int t = threadIdx.x, row = r0 + t;
-        if (row < R) {
+        if (lane == 0) { red[warp][0] = csum; red[warp][1] = bsr; red[warp][2] = bsi; }
+        __syncthreads();
+        if (threadIdx.x == 0) {
             float a = 0, b = 0, c = 0;
-            for (int w = 0; w < NT / 32; w++) { a += red[w][t][0]; b += red[w][t][1]; c += red[w][t][2]; }
+            for (int w = 0; w < NT / 32; w++) { a += red[w][0]; b += red[w][1]; c += red[w][2]; }
             c_part[(size_t)tile * R + row] = a;
             beta_part[(size_t)tile * R + row] = make_float2(b, c);
         }
+        __syncthreads();
     }
     // Write the finished row segments (coalesced when the tile is contiguous).
     const int *cols = tiles.cols + (size_t)tile * tiles.tc_max;
-#pragma unroll
     for (int t = 0; t < TR; t++) {
         const int row = r0 + t;
         if (row >= R) break;
@@ -463,26 +516,64 @@ far_assembly_f64(RowPoints rows, int N, GeoTables geo, TileSet tiles, double k, 
     for (int i = threadIdx.x; i < tc; i += NT) dst[cols[i]] = acc[i];
 }
 
-constexpr int kFarTR32 = 2, kFarNT32 = 512, kFarNT64 = 256;
+constexpr int kFarNT64 = 256;
 
-int far_rows_per_cta(int prec) { return prec == BEM_PREC_C64 ? kFarTR32 : 1; }
+// Launch shapes of the FP32 far kernel (the autotuner times each once per
+// problem shape and keeps the fastest):
+//   0: 2 rows x 512 threads, 1 CTA/SM     1: 2 rows x 1024 threads, 1 CTA/SM
+//   2: 1 row  x 512 threads, 2 CTAs/SM    3: 4 rows x 1024 threads, 1 CTA/SM
+struct FarShape {
+    int tr, nt;
+};
+constexpr FarShape kFarShapes[] = {{2, 512}, {2, 1024}, {1, 512}, {4, 1024}};
+constexpr int kNumFarShapes = 4;
 
-size_t far_smem_bytes(int prec, int tc) {
-    return prec == BEM_PREC_C64 ? (size_t)kFarTR32 * tc * sizeof(float2) : (size_t)tc * sizeof(double2);
+int far_variants(int prec) { return prec == BEM_PREC_C64 ? kNumFarShapes : 1; }
+
+int far_rows_per_cta(int prec, int variant) {
+    return prec == BEM_PREC_C64 ? kFarShapes[variant].tr : 1;
+}
+
+size_t far_smem_bytes(int prec, int tc, int variant) {
+    return prec == BEM_PREC_C64 ? (size_t)kFarShapes[variant].tr * tc * sizeof(float2)
+                                : (size_t)tc * sizeof(double2);
+}
+
+bool far_variant_fits(int prec, int tc, int variant) {
+    int dev = 0, maxs = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&maxs, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    return far_smem_bytes(prec, tc, variant) + 1024 <= (size_t)maxs;
+}
+
+template <int TR, int NT, int MINB>
+static void launch_far_f32(const RowPoints &rows, int N, const GeoTables &geo, const TileSet &tiles,
+                           const Physics &ph, void *A, size_t lda, void *c_part, void *beta_part,
+                           size_t smem, cudaStream_t st) {
+    const bool o6 = quadrature_points() == 36;
+    auto kern = o6 ? far_assembly_f32<TR, NT, MINB, true> : far_assembly_f32<TR, NT, MINB, false>;
+    CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid((rows.R + TR - 1) / TR, tiles.ntiles);
+    kern<<<grid, NT, smem, st>>>(rows, N, geo, tiles, (float)ph.k, (float)ph.rw, (float2 *)A, lda,
+                                 (float *)c_part, (float2 *)beta_part);
 }
 
 void launch_far_assembly(int prec, const RowPoints &rows, int N, const GeoTables &geo,
                          const TileSet &tiles, const Physics &ph, void *A, size_t lda,
-                         void *c_part, void *beta_part, cudaStream_t st) {
+                         void *c_part, void *beta_part, cudaStream_t st, int variant) {
     BEM_PROF((prec == BEM_PREC_C64 ? "far_assembly_f32" : "far_assembly_f64"), st);
     if (rows.R <= 0 || tiles.ntiles <= 0) return;
-    size_t smem = far_smem_bytes(prec, tiles.tc_max);
+    BEM_CHECK_ARG(variant >= 0 && variant < far_variants(prec), "bad far-kernel variant");
+    if (!far_variant_fits(prec, tiles.tc_max, variant))
+        BEM_FAIL(BEM_ERR_TOO_LARGE, "column tile does not fit in shared memory");
+    const size_t smem = far_smem_bytes(prec, tiles.tc_max, variant);
     if (prec == BEM_PREC_C64) {
-        auto kern = far_assembly_f32<kFarTR32, kFarNT32>;
-        CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        dim3 grid((rows.R + kFarTR32 - 1) / kFarTR32, tiles.ntiles);
-        kern<<<grid, kFarNT32, smem, st>>>(rows, N, geo, tiles, (float)ph.k, (float)ph.rw,
-                                           (float2 *)A, lda, (float *)c_part, (float2 *)beta_part);
+        switch (variant) {
+            case 0: launch_far_f32<2, 512, 1>(rows, N, geo, tiles, ph, A, lda, c_part, beta_part, smem, st); break;
+            case 1: launch_far_f32<2, 1024, 1>(rows, N, geo, tiles, ph, A, lda, c_part, beta_part, smem, st); break;
+            case 2: launch_far_f32<1, 512, 2>(rows, N, geo, tiles, ph, A, lda, c_part, beta_part, smem, st); break;
+            default: launch_far_f32<4, 1024, 1>(rows, N, geo, tiles, ph, A, lda, c_part, beta_part, smem, st); break;
+        }
     } else {
         auto kern = far_assembly_f64<kFarNT64>;
         CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

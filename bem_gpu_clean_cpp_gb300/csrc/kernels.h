@@ -57,11 +57,16 @@ void launch_elem_setup(const double *d_nodes, const int4 *d_elems, const double 
 // Far-field assembly.  c64: FP32 quadrature, acc/partials in float.  c128: FP64.
 constexpr int kGeoFloat4 = 7;     // float4 per element in GeoTables::geo_f
 constexpr int kGeoDouble = 18;    // doubles per element in GeoTables::geo_d
-size_t far_smem_bytes(int prec, int tc);
-int far_rows_per_cta(int prec);
+// `variant` selects a launch shape (rows per CTA, threads, CTAs per SM);
+// far_variants(prec) shapes exist, far_variant_fits says whether the
+// shape's shared-memory row accumulator fits the device for tile width tc.
+int far_variants(int prec);
+int far_rows_per_cta(int prec, int variant);
+size_t far_smem_bytes(int prec, int tc, int variant);
+bool far_variant_fits(int prec, int tc, int variant);
 void launch_far_assembly(int prec, const RowPoints &rows, int N, const GeoTables &geo,
                          const TileSet &tiles, const Physics &ph, void *A, size_t lda,
-                         void *c_part, void *beta_part, cudaStream_t st);
+                         void *c_part, void *beta_part, cudaStream_t st, int variant);
 
 // Near-field (singular + near-singular, FP64) assembly and row finalisation:
 // adds the near contributions to A, the diagonal term 1 - sum c, and writes
@@ -96,8 +101,10 @@ int gemv_h_f64_splits(int R, int N);
 // arithmetic; xsplit is scratch for x's float head and tail (2N c64).
 void launch_resid(int prec, int R, int N, const void *A, size_t lda, const double2 *x,
                   const double2 *b, double2 *r, float2 *xsplit, cudaStream_t st);
+// w = A^H u, FP64-accurate; for c64 A, usplit is scratch for u's float head
+// and tail (2R c64).
 void launch_gemv_h_f64(int prec, int R, int N, const void *A, size_t lda, const double2 *u,
-                       double2 *w, double2 *part, cudaStream_t st);               // w = A^H u
+                       double2 *w, double2 *part, float2 *usplit, cudaStream_t st);
 // Row-major (R x N) -> column-major (R x N, ld_out) copy with conversion.
 void launch_to_colmajor(int prec_in, const void *A, size_t lda, int R, int N, int prec_out,
                         void *out, size_t ld_out, cudaStream_t st);

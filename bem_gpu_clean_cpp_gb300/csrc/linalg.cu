@@ -177,8 +177,8 @@ resid_df_kernel(int R, int N, const float2 *__restrict__ A, size_t lda, const fl
 
 // Partial w = A^H u for c64 A, FP64-accurate; each thread owns two columns.
 __global__ void __launch_bounds__(256)
-gemv_h_df_part_kernel(int R, int N, const float2 *__restrict__ A, size_t lda, const double2 *__restrict__ u,
-                      int nsplit, double2 *__restrict__ part) {
+gemv_h_df_part_kernel(int R, int N, const float2 *__restrict__ A, size_t lda, const float2 *__restrict__ uhd,
+                      const float2 *__restrict__ uld, int nsplit, double2 *__restrict__ part) {
     const int c = blockIdx.x * 512 + 2 * threadIdx.x;
     const int split = blockIdx.y;
     const int per = (R + nsplit - 1) / nsplit;
@@ -187,9 +187,8 @@ gemv_h_df_part_kernel(int R, int N, const float2 *__restrict__ A, size_t lda, co
     float ah = 0, al = 0, bh = 0, bl = 0, ch = 0, cl = 0, dh = 0, dl = 0;
     const bool two = (c + 1 < N);
     for (int r = r0; r < r1; r++) {
-        const double2 uu = u[r];
-        const float uh = (float)uu.x, vh = (float)uu.y;
-        const float ul = (float)(uu.x - (double)uh), vl = (float)(uu.y - (double)vh);
+        const float2 hh = uhd[r], ll = uld[r];
+        const float uh = hh.x, vh = hh.y, ul = ll.x, vl = ll.y;
         float4 v;
         if (two) {
             v = __ldcs(reinterpret_cast<const float4 *>(A + (size_t)r * lda + c));
@@ -559,13 +558,16 @@ int h_f64_splits(int prec, int R, int N) {
 }  // namespace
 
 void launch_gemv_h_f64(int prec, int R, int N, const void *A, size_t lda, const double2 *u,
-                       double2 *w, double2 *part, cudaStream_t st) {
+                       double2 *w, double2 *part, float2 *usplit, cudaStream_t st) {
     BEM_PROF("gemv_h_f64", st);
     if (N <= 0) return;
     const int ns = h_f64_splits(prec, R, N);
     if (prec == BEM_PREC_C64) {
+        split_f64_kernel<<<blocks(R, 256), 256, 0, st>>>(R, u, usplit, usplit + R);
+        count_launch();
+        KERNEL_CHECK();
         dim3 g(blocks(N, 512), ns);
-        gemv_h_df_part_kernel<<<g, 256, 0, st>>>(R, N, (const float2 *)A, lda, u, ns, part);
+        gemv_h_df_part_kernel<<<g, 256, 0, st>>>(R, N, (const float2 *)A, lda, usplit, usplit + R, ns, part);
     } else {
         dim3 g(blocks(N, 256), ns);
         gemv_h_f64_part_kernel<double2><<<g, 256, 0, st>>>(R, N, (const double2 *)A, lda, u, ns, part);

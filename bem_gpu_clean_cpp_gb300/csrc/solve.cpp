@@ -107,7 +107,9 @@ void bem_solver_s::solve_refined(bem_solve_info_t *info) {
     w_t.ensure(sizeof(float2) * R);
     w_r.ensure(sizeof(double2) * R);
     w_gv.ensure(sizeof(double2) * n);
-    w_vf.ensure(sizeof(float2) * 2 * (size_t)n);   // c64 copy of v_j, and x head/tail for the residual
+    // c64 copy of v_j and the float head/tail split of x (residual) or of a
+    // length-R vector (A^H u): 2 max(N, R) c64
+    w_vf.ensure(sizeof(float2) * 2 * (size_t)std::max(n, R));
     size_t part = std::max(sizeof(float2) * (size_t)gemv_h_splits(R, n), sizeof(double2) * (size_t)gemv_h_f64_splits(R, n));
     w_part.ensure(part * n);
     w_scal.ensure(sizeof(double) * 8);
@@ -124,7 +126,7 @@ void bem_solver_s::solve_refined(bem_solve_info_t *info) {
         const double2 *b = d_B.as<double2>() + (size_t)s * R;
         double2 *x = d_x.as<double2>() + (size_t)s * n;
         launch_zero_f64(n, x, stream);
-        launch_gemv_h_f64(prec, R, n, A, lda, b, w_gv.as<double2>(), w_part.as<double2>(), stream);
+        launch_gemv_h_f64(prec, R, n, A, lda, b, w_gv.as<double2>(), w_part.as<double2>(), w_vf.as<float2>(), stream);
         launch_nrm2(n, w_gv.as<double2>(), scal + 0, nullptr, stream);
         const double bn = read_scalar(0);
         if (!(bn > 0.0)) continue;
@@ -133,7 +135,8 @@ void bem_solver_s::solve_refined(bem_solve_info_t *info) {
         int ref = 0;
         for (;; ref++) {
             launch_resid(prec, R, n, A, lda, x, b, w_r.as<double2>(), w_vf.as<float2>(), stream);
-            launch_gemv_h_f64(prec, R, n, A, lda, w_r.as<double2>(), w_gv.as<double2>(), w_part.as<double2>(), stream);
+            launch_gemv_h_f64(prec, R, n, A, lda, w_r.as<double2>(), w_gv.as<double2>(), w_part.as<double2>(),
+                              w_vf.as<float2>(), stream);
             launch_nrm2(n, w_gv.as<double2>(), scal + 1, nullptr, stream);
             const double gn = read_scalar(1);
             rel = gn / bn;

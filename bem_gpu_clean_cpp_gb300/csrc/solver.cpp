@@ -291,7 +291,47 @@ void bem_solver_s::assemble(double kk, int precision) {
     d_bpart.ensure(2 * rsz * (size_t)T.ntiles * R);
     TileSet ts{T.recs.as<TileRec>(), T.rec_ptr.as<int>(), T.cols.as<int>(), T.col_cnt.as<int>(), T.ntiles, T.tc_max};
     Physics ph = physics();
-    launch_far_assembly(precision, row_points(), N, geo_tables(), ts, ph, d_A.p, lda, d_cpart.p, d_bpart.p, stream);
+    int variant = opt.far_variant;
+    bool done = false;
+    if (variant < 0) {
+        variant = 0;
+        auto key = std::make_tuple(precision, N, R, T.tc_max, T.ntiles, quadrature_points());
+        auto it = far_tuned.find(key);
+        if (it != far_tuned.end()) {
+            variant = it->second;
+        } else if (far_variants(precision) > 1) {
+            // Autotune: time every launch shape that fits (twice, keep the
+            // minimum) on this very assembly; the last launch leaves a complete
+            // far-field A, so no extra launch is needed afterwards.
+            cudaEvent_t e0, e1;
+            CUDA_TRY(cudaEventCreate(&e0));
+            CUDA_TRY(cudaEventCreate(&e1));
+            float best = 1e30f;
+            for (int v = 0; v < far_variants(precision); v++) {
+                if (!far_variant_fits(precision, T.tc_max, v)) continue;
+                for (int rep = 0; rep < 2; rep++) {
+                    CUDA_TRY(cudaEventRecord(e0, stream));
+                    launch_far_assembly(precision, row_points(), N, geo_tables(), ts, ph, d_A.p, lda,
+                                        d_cpart.p, d_bpart.p, stream, v);
+                    CUDA_TRY(cudaEventRecord(e1, stream));
+                    CUDA_TRY(cudaEventSynchronize(e1));
+                    float ms = 0.f;
+                    CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+                    if (ms < best) { best = ms; variant = v; }
+                }
+            }
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            far_tuned[key] = variant;
+            // the final launch must be the chosen shape only if shapes differ in
+            // results; they do not (same sums), so the last launch stands
+            done = true;
+        }
+    }
+    if (!done)
+        launch_far_assembly(precision, row_points(), N, geo_tables(), ts, ph, d_A.p, lda, d_cpart.p, d_bpart.p,
+                            stream, variant);
+    far_variant_used = variant;
     launch_near_assembly(precision, row_points(), N, geo_tables(), ph, d_A.p, lda, d_cpart.p, d_bpart.p,
                          T.ntiles, d_srcs.as<DevSource>(), S, d_B.as<double2>(), stream);
     assembled = true;

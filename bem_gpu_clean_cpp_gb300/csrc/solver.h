@@ -4,7 +4,9 @@
 #include <cublas_v2.h>
 #include <cusolverDn.h>
 
+#include <map>
 #include <mutex>
+#include <tuple>
 #include <vector>
 
 #include "bem_common.h"
@@ -56,6 +58,10 @@ struct bem_solver_s {
         int ntiles = 0, tc_max = 0;
         bem::DevMem recs, rec_ptr, cols, col_cnt;
     } tiles[2];
+
+    // autotuned far-kernel launch shape per (precision, N, rows, tile width, tiles, Gauss points)
+    std::map<std::tuple<int, int, int, int, int, int>, int> far_tuned;
+    int far_variant_used = -1;
 
     int prec = -1;
     double k = 0.0;

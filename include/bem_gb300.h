@@ -156,6 +156,7 @@ typedef struct {
     double inner_tol;   /* inner GMRES relative tolerance */
     int max_refine;     /* refinement steps */
     int tile_cols;      /* far-field column tile width, 0 = automatic (<= 12288) */
+    int far_variant;    /* far-field launch shape, -1 = autotuned per problem shape */
 } bem_options_t;
 
 typedef struct {

@@ -90,6 +90,21 @@ def test_near_singular_assembly_matches_oracle(bemlib, orc, eta, depth):
     assert rel_err(A32, Ao) < TOL32
 
 
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
+@pytest.mark.parametrize("order", [6, 5])
+def test_far_kernel_launch_shapes(bemlib, orc, variant, order):
+    """Every far-kernel launch shape (and both the unrolled 6x6 path and the
+    generic Gauss loop) gives the oracle's matrix."""
+    p, f, chief = _problem("ico2")
+    s = bemlib.Solver(far_variant=variant, order=order)
+    s.set_geometry(p, f, chief=chief)
+    s.set_sources(SRCS)
+    s.assemble(5.0, bemlib.PREC_C64)
+    A, B = s.system(bemlib.PREC_C128)
+    Ao, Bo = orc.assemble(np.vstack([p, chief]), f, 5.0, p.shape[0], SRCS, prm=orc.params(order=order))
+    assert rel_err(A, Ao) < TOL32 and rel_err(B, Bo) < TOL32
+
+
 def test_quadrature_order(bemlib, orc):
     p, f, chief = _problem("test.obj")
     s = bemlib.Solver(order=4)
