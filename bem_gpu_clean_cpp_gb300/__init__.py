@@ -104,6 +104,7 @@ SIGNATURES = {
     "bem_system_c64": (_I, [_VP, _F, _VP, _I, _VP, _I, _VP, _I]),
     "bem_qr_solve_c64": (_I, [_VP, _I, _I, _I, _VP, _I, _I]),
     "bem_gmres_c64": (_I, [_VP, _VP, _I, _I, _F, _VP]),
+    "bem_gmres_c64_noalloc": (_I, [_VP, _I, _VP, _I, _I, _F, _VP, _VP, ctypes.POINTER(_I)]),
     "bem_ext_pressure_c64": (_I, [_F, _VP, _VP, _VP, _VP, _VP]),
     "bem_write_cplx_mat_c64": (_I, [_VP, _I, _I, _I, _S]),
     "bem_options_default": (_I, [_VP]),

@@ -120,6 +120,26 @@ int bem_qr_solve_c64(const float *A, int mA, int nA, int ldA, float *B, int nB, 
 /* GMRES (GMRES.h:104-105, GMRES.cu:145-279): unrestarted GMRES on a square
  * m x m system, x holds x0 on entry. */
 int bem_gmres_c64(const float *A, const float *b, int m, int max_iter, float thr, float *x);
+/* GMRES on device buffers that allocates nothing.  No counterpart in the
+ * reference: it is for callers that cannot allocate GPU memory while they
+ * solve (a serving process whose device memory is owned and capped by its
+ * own pool allocator, code that must not add allocations while a CUDA stream
+ * capture of another component is in progress, a real-time loop that cannot
+ * afford cudaMalloc's latency and implicit synchronisation).  Same algorithm
+ * and stopping rule as bem_gmres_c64.  A_dev is m x m column-major c64 with
+ * an even lda >= m and a 16-byte aligned start; b_dev and x_dev hold m c64
+ * values (x_dev: x0 on entry, the solution on return); stream is a
+ * cudaStream_t or NULL; *iters (may be NULL) receives the iteration count.
+ * All scratch lives in one static device array of about 5.4 MiB that every
+ * GPU loading the library keeps until exit, which limits m to
+ * BEM_NOALLOC_MAX_M and min(max_iter, m) to BEM_NOALLOC_MAX_ITER; larger
+ * sizes return BEM_ERR_TOO_LARGE.  The first call on a device looks up the
+ * array's device address (make that first call before any stream capture).
+ * Calls share the array: calls that overlap on the GPU race. */
+#define BEM_NOALLOC_MAX_M 2048
+#define BEM_NOALLOC_MAX_ITER 128
+int bem_gmres_c64_noalloc(const float *A_dev, int lda, const float *b_dev, int m, int max_iter,
+                          float thr, float *x_dev, void *stream, int *iters);
 /* genExtPressure (mesh.h:425-426, mesh.cu:1038-1073): pressure at x from
  * the surface pressure surf_p (numPnts c64 values). */
 int bem_ext_pressure_c64(float k, bem_mesh_t m, const float *src, const float *x,
