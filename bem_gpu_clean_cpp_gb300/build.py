@@ -52,6 +52,8 @@ def _stale() -> bool:
 def build(force: bool = False, jobs: int | None = None) -> str:
     """Compile every source for sm_103a and link libbem_gb300.so (in-tree)."""
     if not force and not _stale():
+        if not os.path.exists(DRIVER):
+            _build_driver()
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     jobs = jobs or min(len(SOURCES), os.cpu_count() or 4)
@@ -66,7 +68,22 @@ def build(force: bool = False, jobs: int | None = None) -> str:
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
     os.replace(tmp, LIB)
+    _build_driver()
     return LIB
+
+
+DRIVER = os.path.join(HERE, "bem_sphere_driver")
+
+
+def _build_driver() -> None:
+    """The C++ program that runs the reference driver's call sequence through
+    include/bem_gb300.hpp (host-only C++, linked to libbem_gb300.so)."""
+    cuda_inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
+    cmd = ["g++", "-std=c++17", "-O2", "-I", cuda_inc, os.path.join(HERE, "cpp", "sphere_driver.cpp"),
+           "-o", DRIVER, "-L", HERE, "-lbem_gb300", "-Wl,-rpath,$ORIGIN"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"driver build failed:\n{res.stdout}\n{res.stderr}")
 
 
 if __name__ == "__main__":

@@ -397,6 +397,36 @@ def run_ours(args):
                 "speedup_mixed_vs_fp64": (1000.0 / ms64) and value / dist.world / (1000.0 / ms64)}
         del s3
 
+    # ---- the reference's own GPU path on this GB300, once ----
+    # (its assembly kernels from the cubin built from its sources, launched as
+    # atomicGenSystem does, and qrSolver's cuSOLVER sequence; FP32, no
+    # near-singular rule)
+    ref_gpu = None
+    if not args.no_fp64 and dist.rank == 0:
+        try:
+            from oracle import ref as refk
+            from oracle import ref_build
+            ref_build.build_if_possible()
+            if refk.available():
+                rows = np.vstack([pts, chief]).astype(np.float32)
+                bc_ref = np.tile(np.array([0, 1, 0], dtype=np.complex128), (E, 1))
+                Ar, Br, ms_asm = refk.assemble(rows, elems, N, k, srcs=[(1e6, 1e6, 1e6)], strength=0.0, bc=bc_ref)
+                ms_asm2 = refk.assemble(rows, elems, N, k, srcs=[(1e6, 1e6, 1e6)], strength=0.0, bc=bc_ref)[2]
+                inc = np.exp(-1j * k * (rows.astype(np.float64) @ d)).astype(np.complex64)   # plane wave RHS
+                xr, ms_qr = refk.qr(Ar, (Br[:, 0] + inc).reshape(-1, 1))
+                err_ref = None
+                if fp64:
+                    err_ref = float(np.abs(xr[:, 0] - x64).max() / np.abs(x64).max())
+                ref_gpu = {"assembly_ms": min(ms_asm, ms_asm2), "qr_ms": ms_qr,
+                           "solve_ms": min(ms_asm, ms_asm2) + ms_qr,
+                           "solves_per_s": 1000.0 / (min(ms_asm, ms_asm2) + ms_qr),
+                           "rel_err_vs_fp64": err_ref,
+                           "note": "reference kernels + cusolver Cgeqrf/Cunmqr/cublasCtrsm, FP32, plain 6x6 "
+                                   "rule for near pairs; timed with its own event spans"}
+                del Ar, Br
+        except Exception as exc:   # reported, not fatal: the reference path is a comparison only
+            ref_gpu = {"unavailable": str(exc)[:200]}
+
     # ---- roofline of the dominant kernel ----
     peaks = {}
     try:
@@ -459,6 +489,7 @@ def run_ours(args):
                    "rel_residual": max(i.rel_residual for i in infos) if infos else None},
         "assembly_gbs": (A_bytes + B_bytes) / (asm_ms / 1000.0) / 1e9 if asm_ms else None,
         "fp64_plain": fp64,
+        "reference_gpu": ref_gpu,
         "roofline": roofline,
         "roofline_assembly": far_extra,
         "kernels": per_kernel,
