@@ -14,13 +14,6 @@
 #ifndef PI
 #define PI 3.1415926535897932
 #endif
-#define HOST_CALL(x)                                              \
-    do {                                                          \
-        if ((x) != EXIT_SUCCESS) {                                \
-            std::printf("Error at %s:%d\n", __FILE__, __LINE__); \
-            return EXIT_FAILURE;                                  \
-        }                                                         \
-    } while (0)
 
 int main(int argc, char **argv) {
     if (argc < 3) {

@@ -37,7 +37,7 @@ __device__ __forceinline__ void st_c(double2 *p, size_t i, double re, double im)
 // y = A x with FP32 accumulation.  A warp owns kMvRPW consecutive rows and
 // sweeps the columns two complex entries (16 bytes) at a time, so each x load
 // serves kMvRPW rows of A; A is streamed once (__ldcs).
-constexpr int kMvRPW = 4;
+constexpr int kMvRPW = 2;
 constexpr int kMvWPC = 4;
 
 template <typename TX, typename TY>
@@ -508,7 +508,7 @@ void launch_gemv_c64(int R, int N, const float2 *A, size_t lda, const void *x, i
 
 int gemv_h_splits(int R, int N) {
     int cb = (N + kHCols - 1) / kHCols;
-    int want = (4 * 152 + cb - 1) / cb;
+    int want = (8 * 152 + cb - 1) / cb;
     return std::max(1, std::min(want, std::max(1, R / 32)));
 }
 
@@ -553,7 +553,7 @@ void launch_resid(int prec, int R, int N, const void *A, size_t lda, const doubl
 namespace {
 int h_f64_splits(int prec, int R, int N) {
     int cb = prec == BEM_PREC_C64 ? blocks(N, 512) : blocks(N, 256);
-    return std::max(1, std::min((4 * 152 + cb - 1) / cb, std::max(1, R / 16)));
+    return std::max(1, std::min((8 * 152 + cb - 1) / cb, std::max(1, R / 16)));
 }
 }  // namespace
 

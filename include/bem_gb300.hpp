@@ -19,6 +19,18 @@
 
 #include "bem_gb300.h"
 
+// The reference's status-check macro (numerical.h:59-64), which its callers use
+// around every call.
+#ifndef HOST_CALL
+#define HOST_CALL(x)                                              \
+    do {                                                          \
+        if ((x) != EXIT_SUCCESS) {                                \
+            std::printf("Error at %s:%d\n", __FILE__, __LINE__); \
+            return EXIT_FAILURE;                                  \
+        }                                                         \
+    } while (0)
+#endif
+
 namespace bem_gb300 {
 
 // Error report in the reference's style ("Error at file:line", numerical.h:59-122)
