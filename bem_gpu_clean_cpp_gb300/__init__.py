@@ -35,7 +35,8 @@ LIB_PATH = os.path.join(_HERE, "libbem_gb300.so")
 
 SUCCESS = 0
 PREC_C64, PREC_C128 = 0, 1
-SOLVE_QR, SOLVE_GMRES_REFINED = 0, 1
+SOLVE_QR, SOLVE_GMRES_REFINED, SOLVE_BLOCK_GMRES = 0, 1, 2
+GEMM_FP32, GEMM_SPLIT_BF16, GEMM_TF32 = 0, 1, 2
 SRC_POINT, SRC_PLANE = 0, 1
 ERR_NOT_CONVERGED = 5
 
@@ -58,7 +59,8 @@ class Options(ctypes.Structure):
     _fields_ = [("density", ctypes.c_double), ("speed", ctypes.c_double), ("order", ctypes.c_int),
                 ("near_eta", ctypes.c_double), ("near_depth", ctypes.c_int), ("tol", ctypes.c_double),
                 ("max_iter", ctypes.c_int), ("inner_tol", ctypes.c_double),
-                ("max_refine", ctypes.c_int), ("tile_cols", ctypes.c_int), ("far_variant", ctypes.c_int)]
+                ("max_refine", ctypes.c_int), ("tile_cols", ctypes.c_int), ("far_variant", ctypes.c_int),
+                ("gemm_mode", ctypes.c_int), ("block_tol", ctypes.c_double)]
 
 
 class SolveInfo(ctypes.Structure):
@@ -101,6 +103,9 @@ SIGNATURES = {
     "bem_mesh_get_chief": (_I, [_VP, _VP]),
     "bem_mesh_icosphere": (_I, [_VP, _I, _D]),
     "bem_mesh_surface_area": (_I, [_VP, _VP]),
+    "bem_mesh_geodesic": (_I, [_VP, _I, _D]),
+    "bem_mesh_perturbed_ellipsoid": (_I, [_VP, _D, _D, _D, _I, _D, ctypes.c_ulonglong]),
+    "bem_fibonacci_sphere": (_I, [_I, _D, _VP]),
     "bem_system_c64": (_I, [_VP, _F, _VP, _I, _VP, _I, _VP, _I]),
     "bem_qr_solve_c64": (_I, [_VP, _I, _I, _I, _VP, _I, _I]),
     "bem_gmres_c64": (_I, [_VP, _VP, _I, _I, _F, _VP]),
@@ -209,6 +214,13 @@ class gaussQuad:
     def sendToDevice(self) -> int:
         _check(lib().bem_set_quadrature(self.n))
         return SUCCESS
+
+
+def fibonacci_sphere(n: int, radius: float = 1.0) -> np.ndarray:
+    """n points of a Fibonacci lattice on a sphere (source sets of the benchmarks)."""
+    out = np.zeros((n, 3))
+    _check(lib().bem_fibonacci_sphere(int(n), float(radius), _ptr(out)))
+    return out
 
 
 def set_medium(density: float, speed: float) -> None:
@@ -323,6 +335,19 @@ class Mesh:
         m = cls()
         _check(lib().bem_mesh_icosphere(m._h, int(subdiv), float(radius)))
         return m
+
+    @classmethod
+    def geodesic(cls, nu: int, radius: float = 1.0) -> "Mesh":
+        m = cls()
+        _check(lib().bem_mesh_geodesic(m._h, int(nu), float(radius)))
+        return m
+
+    def perturbed_ellipsoid(self, a: float, b: float, c: float, lmax: int = 8, amp: float = 0.05,
+                            seed: int = 0) -> "Mesh":
+        """Map this unit-sphere mesh onto a seeded, radially perturbed ellipsoid."""
+        _check(lib().bem_mesh_perturbed_ellipsoid(self._h, float(a), float(b), float(c), int(lmax),
+                                                  float(amp), int(seed)))
+        return self
 
     @classmethod
     def from_arrays(cls, pnts, elems) -> "Mesh":

@@ -12,8 +12,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libbem_gb300.so")
 
-SOURCES = ["kernels.cu", "linalg.cu", "chief.cu", "noalloc.cu", "mesh.cpp", "solver.cpp", "solve.cpp",
-           "capi.cpp"]
+SOURCES = ["kernels.cu", "linalg.cu", "block.cu", "chief.cu", "noalloc.cu", "mesh.cpp", "generators.cpp",
+           "solver.cpp", "solve.cpp", "capi.cpp"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

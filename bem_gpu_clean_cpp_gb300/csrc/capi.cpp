@@ -500,6 +500,27 @@ int bem_mesh_surface_area(bem_mesh_t m, double *area) {
     BEM_API_END
 }
 
+int bem_mesh_geodesic(bem_mesh_t m, int nu, double radius) {
+    BEM_API_BEGIN
+    BEM_CHECK_ARG(m, "null mesh");
+    make_geodesic(*m, nu, radius);
+    BEM_API_END
+}
+
+int bem_mesh_perturbed_ellipsoid(bem_mesh_t m, double a, double b, double c, int lmax, double amp,
+                                 unsigned long long seed) {
+    BEM_API_BEGIN
+    BEM_CHECK_ARG(m, "null mesh");
+    map_perturbed_ellipsoid(*m, a, b, c, lmax, amp, seed);
+    BEM_API_END
+}
+
+int bem_fibonacci_sphere(int n, double radius, double *pts) {
+    BEM_API_BEGIN
+    fibonacci_sphere(n, radius, pts);
+    BEM_API_END
+}
+
 // ---- drop-in calls ----
 static void reference_options(bem_options_t *o) {
     bem_options_default(o);
@@ -602,6 +623,8 @@ int bem_options_default(bem_options_t *o) {
     o->max_refine = 10;
     o->tile_cols = 0;
     o->far_variant = -1;
+    o->gemm_mode = BEM_GEMM_SPLIT_BF16;
+    o->block_tol = 1e-6;
     apply_global_options(o);
     return BEM_SUCCESS;
 }
@@ -627,6 +650,8 @@ int bem_solver_set_options(bem_solver_t s, const bem_options_t *o) {
     BEM_CHECK_ARG(o->tol > 0 && o->max_iter >= 1 && o->inner_tol > 0 && o->max_refine >= 0, "bad solver tolerances");
     BEM_CHECK_ARG(o->tile_cols >= 0, "tile_cols must be >= 0");
     BEM_CHECK_ARG(o->far_variant >= -1 && o->far_variant < far_variants(BEM_PREC_C64), "bad far_variant");
+    BEM_CHECK_ARG(o->gemm_mode >= BEM_GEMM_FP32 && o->gemm_mode <= BEM_GEMM_TF32, "bad gemm_mode");
+    BEM_CHECK_ARG(o->block_tol > 0, "block_tol must be positive");
     if (o->tile_cols != s->opt.tile_cols) s->tiles[0].valid = s->tiles[1].valid = false;
     s->opt = *o;
     s->assembled = s->solved = false;

@@ -26,6 +26,10 @@ namespace bem {
 void read_obj_reference(bem_mesh_s &m, const char *path);
 void read_obj_robust(bem_mesh_s &m, const char *path);
 void make_icosphere(bem_mesh_s &m, int subdiv, double radius);
+void make_geodesic(bem_mesh_s &m, int nu, double radius);
+void map_perturbed_ellipsoid(bem_mesh_s &m, double a, double b, double c, int lmax, double amp,
+                             unsigned long long seed);
+void fibonacci_sphere(int n, double radius, double *out);
 void find_bb(bem_mesh_s &m, float threshold);
 void gen_chief(bem_mesh_s &m, int num, float threshold);
 

@@ -348,6 +348,9 @@ void bem_solver_s::solve(int method, bem_solve_info_t *info) {
     } else if (method == BEM_SOLVE_GMRES_REFINED) {
         if (prec != BEM_PREC_C64) BEM_FAIL(BEM_ERR_STATE, "refined GMRES needs a c64 assembly");
         solve_refined(info);
+    } else if (method == BEM_SOLVE_BLOCK_GMRES) {
+        if (prec != BEM_PREC_C64) BEM_FAIL(BEM_ERR_STATE, "block GMRES needs a c64 assembly");
+        solve_block(info);
     } else {
         BEM_FAIL(BEM_ERR_INVALID_ARG, "unknown solve method");
     }

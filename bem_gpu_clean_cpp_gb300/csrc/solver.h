@@ -100,4 +100,5 @@ struct bem_solver_s {
     bem::Physics physics() const;
     void solve_qr();
     void solve_refined(bem_solve_info_t *info);
+    void solve_block(bem_solve_info_t *info);
 };

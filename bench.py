@@ -57,6 +57,9 @@ def parse_args():
     ap.add_argument("--depth", type=int, default=2)
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 reference solve")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--config", default="precision", choices=["precision", "rhs"],
+                    help="precision: the headline workload (one plane wave); rhs: perturbed ellipsoid, "
+                         "8 kHz, 256 point sources solved together (block GMRES)")
     ap.add_argument("--mode", default="bench", choices=["bench", "profile"],
                     help="profile: one warm-up solve and one more solve, nothing timed (for ncu captures)")
     return ap.parse_args()
@@ -66,13 +69,14 @@ def run_profile(args):
     """Two solves of the workload and nothing else, so that an ncu capture
     (-k <kernel> -s/-c) sees the kernels of a steady-state solve."""
     import bem_gpu_clean_cpp_gb300 as bem
-    pts, elems, chief, d, k, bc = workload(args)
+    pts, elems, chief, srcs, k, bc, _ = select_workload(args)
     s = bem.Solver(near_eta=args.eta, near_depth=args.depth, tol=1e-8, inner_tol=1e-4, max_iter=300)
     s.set_geometry(pts, elems, bc=bc, chief=chief)
-    s.set_sources([("plane", d, 1.0)])
+    s.set_sources(srcs)
+    method = bem.SOLVE_BLOCK_GMRES if args.config == "rhs" else bem.SOLVE_GMRES_REFINED
     for _ in range(2):
         s.assemble(k, bem.PREC_C64)
-        info = s.solve(bem.SOLVE_GMRES_REFINED)
+        info = s.solve(method)
     s.sync()
     print(json.dumps({"mode": "profile", "iterations": info.iterations, "refinements": info.refinements,
                       "rel_residual": info.rel_residual}))
@@ -115,6 +119,27 @@ def icosphere(subdiv: int, radius: float = 1.0):
     return p, f
 
 
+WORKLOAD_RHS = ("perturbed ellipsoid 0.075/0.09/0.11 m (SH l<=8, 5%), geodesic nu=39 (N=15212, E=30420), "
+                "8 kHz, 256 Fibonacci point sources at 1 m, 32 CHIEF, block GMRES")
+
+
+def workload_rhs(args):
+    """The multi-right-hand-side configuration (rigid body)."""
+    import bem_gpu_clean_cpp_gb300 as bem
+    m = bem.Mesh.geodesic(39).perturbed_ellipsoid(0.075, 0.09, 0.11, lmax=8, amp=0.05, seed=args.seed)
+    pts, elems = m.points(), m.elems()
+    rng = np.random.default_rng(args.seed)
+    u = rng.random((args.chief, 3))
+    r = 0.5 * 0.075 * np.cbrt(u[:, 0])
+    th = np.arccos(1 - 2 * u[:, 1])
+    ph = 2 * np.pi * u[:, 2]
+    chief = np.stack([r * np.sin(th) * np.cos(ph), r * np.sin(th) * np.sin(ph), r * np.cos(th)], axis=1)
+    srcs = [("point", s, 1.0) for s in bem.fibonacci_sphere(256, 1.0)]
+    bc = np.tile(np.array([0, 1, 0], dtype=np.complex128), (elems.shape[0], 1))
+    k = 2 * np.pi * 8000.0 / 343.21
+    return pts, elems, chief, srcs, k, bc
+
+
 def workload(args):
     rng = np.random.default_rng(args.seed)
     pts, elems = icosphere(args.subdiv)
@@ -127,6 +152,15 @@ def workload(args):
     d /= np.linalg.norm(d)
     bc = np.tile(np.array([0, 1, 0], dtype=np.complex128), (elems.shape[0], 1))
     return pts, elems, chief, d, float(args.ka), bc
+
+
+def select_workload(args):
+    """(pts, elems, chief, sources, k, bc, workload name) of the chosen config."""
+    if args.config == "rhs":
+        pts, elems, chief, srcs, k, bc = workload_rhs(args)
+        return pts, elems, chief, srcs, k, bc, WORKLOAD_RHS
+    pts, elems, chief, d, k, bc = workload(args)
+    return pts, elems, chief, [("plane", d, 1.0)], k, bc, WORKLOAD
 
 
 # ---------------------------------------------------------------------------
@@ -221,11 +255,12 @@ class Clocks:
 # ---------------------------------------------------------------------------
 # CPU restatement timing (the oracle), bounded sample of the same workload
 # ---------------------------------------------------------------------------
-def cpu_sample(pts, elems, chief, d, k, bc, eta, depth, threads, rows=64, n_qr=1024):
-    """FP64 CPU solve time of the full workload, extrapolated from a sample:
-    assembly of `rows` rows (all elements, x (N+M)/rows) plus a Householder QR
-    least-squares solve of an (n_qr+32) x n_qr system (x flop ratio
-    (8mn^2 - 8n^3/3) of the full system)."""
+def cpu_sample(pts, elems, chief, srcs, k, bc, eta, depth, threads, rows=64, n_qr=1024):
+    """FP64 CPU time of one surface solve, extrapolated from a sample:
+    assembly of `rows` rows (all elements and sources, x (N+M)/rows) plus a
+    Householder QR least-squares solve of an (n_qr+32) x n_qr system (x flop
+    ratio (8mn^2 - 8n^3/3) of the full system), divided by the number of
+    sources that share the factorisation."""
     import oracle
     oracle.build()
     oracle.set_threads(threads)
@@ -233,7 +268,7 @@ def cpu_sample(pts, elems, chief, d, k, bc, eta, depth, threads, rows=64, n_qr=1
     allp = np.vstack([pts, chief])
     prm = oracle.params(near_eta=eta, near_depth=depth)
     t0 = time.perf_counter()
-    oracle.assemble(allp, elems, k, N, [("plane", d, 1.0)], bc=bc, prm=prm, rows=(0, rows))
+    oracle.assemble(allp, elems, k, N, srcs, bc=bc, prm=prm, rows=(0, rows))
     t_asm = (time.perf_counter() - t0) * R / rows
     rng = np.random.default_rng(1)
     m_s = n_qr + 32
@@ -242,32 +277,35 @@ def cpu_sample(pts, elems, chief, d, k, bc, eta, depth, threads, rows=64, n_qr=1
     t0 = time.perf_counter()
     oracle.lsq_qr(Aq, Bq)
     t_qr_s = time.perf_counter() - t0
-    flops = lambda m, n: 8.0 * m * n * n - 8.0 / 3.0 * n ** 3
-    t_qr = t_qr_s * flops(R, N) / flops(m_s, n_qr)
+    S = len(srcs)
+    # factorisation once, then Q^H b and the triangular solve per source
+    flops = lambda m, n, s: 8.0 * m * n * n - 8.0 / 3.0 * n ** 3 + s * (8.0 * m * n)
+    t_qr = t_qr_s * flops(R, N, S) / flops(m_s, n_qr, 1)
     total = t_asm + t_qr
-    return {"value": 1.0 / total, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"oracle FP64: assembly of {rows}/{R} rows (x{R / rows:.1f}) + Householder LS-QR "
-                      f"{m_s}x{n_qr} (x{flops(R, N) / flops(m_s, n_qr):.0f} by flop count); "
-                      f"extrapolated solve {total:.1f} s (assembly {t_asm:.1f} s, QR {t_qr:.1f} s)"}
+    return {"value": S / total, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"oracle FP64: assembly of {rows}/{R} rows with {S} source(s) (x{R / rows:.1f}) + "
+                      f"Householder LS-QR {m_s}x{n_qr} (x{flops(R, N, S) / flops(m_s, n_qr, 1):.0f} by flop "
+                      f"count); extrapolated {total:.1f} s for {S} solve(s) (assembly {t_asm:.1f} s, "
+                      f"QR {t_qr:.1f} s)"}
 
 
 def run_reference(args):
     rank, world, _ = dist_info()
     if rank != 0:
         return 0
-    pts, elems, chief, d, k, bc = workload(args)
+    pts, elems, chief, srcs, k, bc, name = select_workload(args)
     threads = os.cpu_count() or 1
     vals = []
     for i in range(args.warmup + args.steps):
-        r = cpu_sample(pts, elems, chief, d, k, bc, args.eta, args.depth, threads, rows=16, n_qr=512)
+        r = cpu_sample(pts, elems, chief, srcs, k, bc, args.eta, args.depth, threads, rows=16, n_qr=512)
         if i >= args.warmup:
             vals.append(r["value"])
     v = float(np.mean(vals))
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "subdiv": args.subdiv, "ka": args.ka, "chief": args.chief,
-                       "seed": args.seed, "near_eta": args.eta},
+            "config": {"workload": name, "subdiv": args.subdiv, "ka": args.ka, "chief": args.chief,
+                       "sources": len(srcs), "seed": args.seed, "near_eta": args.eta},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": r["sample"].replace("16/", "16 rows of ") + "; per step"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -294,11 +332,19 @@ def run_ours(args):
     dist = Dist(use_cuda=True)
     torch.cuda.set_device(dist.local)
     bem.lib()
-    pts, elems, chief, d, k, bc = workload(args)
+    pts, elems, chief, src, k, bc, name = select_workload(args)
+    if args.config == "rhs":
+        method = bem.SOLVE_BLOCK_GMRES
+        opts = dict(near_eta=args.eta, near_depth=args.depth, tol=1e-8, inner_tol=1e-4, max_iter=100,
+                    max_refine=6, block_tol=1e-6)
+    else:
+        d = src[0][1]
+        method = bem.SOLVE_GMRES_REFINED
+        opts = dict(near_eta=args.eta, near_depth=args.depth, tol=1e-8, inner_tol=1e-4, max_iter=300,
+                    max_refine=10)
     N, E, M = pts.shape[0], elems.shape[0], chief.shape[0]
     R = N + M
-    src = [("plane", d, 1.0)]
-    opts = dict(near_eta=args.eta, near_depth=args.depth, tol=1e-8, inner_tol=1e-4, max_iter=300, max_refine=10)
+    S = len(src)
 
     s = bem.Solver(**opts)
     s.set_geometry(pts, elems, bc=bc, chief=chief)
@@ -308,7 +354,7 @@ def run_ours(args):
 
     def step():
         s.assemble(k, bem.PREC_C64)
-        infos.append(s.solve(bem.SOLVE_GMRES_REFINED))
+        infos.append(s.solve(method))
 
     for _ in range(max(3, args.warmup)):
         step()
@@ -341,26 +387,26 @@ def run_ours(args):
     lat = [a.elapsed_time(b) for a, b in ev]
     total_ms = ev[0][0].elapsed_time(ev[-1][1])
     total_ms = dist.max(total_ms)
-    value = dist.world * args.steps / (total_ms / 1000.0)
+    value = dist.world * args.steps * S / (total_ms / 1000.0)     # one solve per source
 
     # ---- e2e: host buffers through the C ABI, pinned memory ----
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
     h_pts, h_elems, h_chief, h_bc = pin(pts), pin(elems), pin(chief), pin(bc)
-    h_x = torch.empty((1, N), dtype=torch.complex128).pin_memory().numpy().T
+    h_x = torch.empty((S, N), dtype=torch.complex128).pin_memory().numpy().T
     s2 = bem.Solver(**opts)
     # Bytes the library copies host -> device per step: nodes (24N), row
     # points in double and hi/lo float (24R + 32R), elements (16E), bc (48E),
     # one column tile's element records (32E) and column map (4N + 12), the
     # source record (48); device -> host: the surface pressure (16N) plus the
     # 8-byte residual estimates read by the solver loop.
-    h2d = 24 * N + 56 * R + 64 * E + 32 * E + 4 * N + 12 + 48
+    h2d = 24 * N + 56 * R + 64 * E + 32 * E + 4 * N + 12 + 48 * S
     d2h = h_x.nbytes
 
     def e2e_step():
         s2.set_geometry(h_pts, h_elems, bc=h_bc, chief=h_chief)
         s2.set_sources(src)
         s2.assemble(k, bem.PREC_C64)
-        s2.solve(bem.SOLVE_GMRES_REFINED)
+        s2.solve(method)
         s2.solution(out=h_x)
 
     for _ in range(max(1, min(2, args.warmup))):
@@ -372,8 +418,8 @@ def run_ours(args):
         e2e_step()
     torch.cuda.synchronize()
     e2e_s = dist.max(time.perf_counter() - t0)
-    e2e_value = dist.world * args.steps / e2e_s
-    x_mixed = h_x[:, 0].copy()
+    e2e_value = dist.world * args.steps * S / e2e_s
+    x_mixed = h_x.copy()
     if infos:
         d2h += 8 * int(np.mean([i.iterations + 2 * i.refinements + 1 for i in infos]))
 
@@ -391,10 +437,12 @@ def run_ours(args):
         b.record(st3)
         s3.sync()
         ms64 = a.elapsed_time(b)
-        x64 = s3.solution()[:, 0]
-        err = float(np.abs(x_mixed - x64).max() / np.abs(x64).max())
-        fp64 = {"ms": ms64, "solves_per_s": 1000.0 / ms64, "rel_err_mixed_vs_fp64": err,
-                "speedup_mixed_vs_fp64": (1000.0 / ms64) and value / dist.world / (1000.0 / ms64)}
+        x64_all = s3.solution()
+        x64 = x64_all[:, 0]
+        err = max(float(np.abs(x_mixed[:, j] - x64_all[:, j]).max() / np.abs(x64_all[:, j]).max())
+                  for j in range(S))
+        fp64 = {"ms": ms64, "solves_per_s": S * 1000.0 / ms64, "rel_err_mixed_vs_fp64": err,
+                "speedup_mixed_vs_fp64": value / dist.world / (S * 1000.0 / ms64)}
         del s3
 
     # ---- the reference's own GPU path on this GB300, once ----
@@ -402,7 +450,7 @@ def run_ours(args):
     # atomicGenSystem does, and qrSolver's cuSOLVER sequence; FP32, no
     # near-singular rule)
     ref_gpu = None
-    if not args.no_fp64 and dist.rank == 0:
+    if not args.no_fp64 and dist.rank == 0 and args.config == "precision":
         try:
             from oracle import ref as refk
             from oracle import ref_build
@@ -472,14 +520,16 @@ def run_ours(args):
 
     cpu = None
     if dist.rank == 0 and not args.no_cpu:
-        cpu = cpu_sample(pts, elems, chief, d, k, bc, args.eta, args.depth, os.cpu_count() or 1)
+        cpu = cpu_sample(pts, elems, chief, src, k, bc, args.eta, args.depth, os.cpu_count() or 1)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c64 (FP32) + f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "subdiv": args.subdiv, "nodes": N, "triangles": E, "chief": M,
-                   "ka": args.ka, "seed": args.seed, "near_eta": args.eta, "near_depth": args.depth,
+        "config": {"workload": name, "sources": S, "nodes": N, "triangles": E, "chief": M,
+                   **({"subdiv": args.subdiv, "ka": args.ka} if args.config == "precision" else
+                      {"k": k, "solver": "block GMRES, split-BF16 GEMMs, FP64 refinement"}),
+                   "seed": args.seed, "near_eta": args.eta, "near_depth": args.depth,
                    "refine_tol": 1e-8, "parallelism": f"replicas x{dist.world}",
                    "l2": "inputs larger than L2: A (%.0f MB c64) is rewritten every step" % (A_bytes / 1e6)},
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),

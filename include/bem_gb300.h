@@ -105,6 +105,17 @@ int bem_mesh_get_chief(bem_mesh_t m, double *pnts);
 int bem_mesh_icosphere(bem_mesh_t m, int subdiv, double radius);
 /* cmptSurfArea (mesh.cu:1082-1117). */
 int bem_mesh_surface_area(bem_mesh_t m, double *area);
+/* Synthetic geometry for the benchmark configurations (no reference
+ * counterpart).  Class-I geodesic sphere of frequency nu (V = 10 nu^2 + 2,
+ * F = 20 nu^2), inward winding. */
+int bem_mesh_geodesic(bem_mesh_t m, int nu, double radius);
+/* Maps a unit-sphere mesh onto the ellipsoid (a, b, c) radially perturbed by
+ * a seeded real-spherical-harmonic field up to degree lmax whose largest
+ * magnitude over the nodes is amp (relative). */
+int bem_mesh_perturbed_ellipsoid(bem_mesh_t m, double a, double b, double c, int lmax, double amp,
+                                 unsigned long long seed);
+/* n points (3 doubles each) of a Fibonacci lattice on a sphere. */
+int bem_fibonacci_sphere(int n, double radius, double *pts);
 
 /* ------------------------------------------------------------------ */
 /* Drop-in calls with host buffers (the reference's call surface)       */
@@ -163,7 +174,8 @@ typedef struct {
 } bem_source_t;
 
 enum { BEM_PREC_C64 = 0, BEM_PREC_C128 = 1 };
-enum { BEM_SOLVE_QR = 0, BEM_SOLVE_GMRES_REFINED = 1 };
+enum { BEM_SOLVE_QR = 0, BEM_SOLVE_GMRES_REFINED = 1, BEM_SOLVE_BLOCK_GMRES = 2 };
+enum { BEM_GEMM_FP32 = 0, BEM_GEMM_SPLIT_BF16 = 1, BEM_GEMM_TF32 = 2 };
 
 typedef struct {
     double density;     /* 1.2041 (numerical.cu:12) */
@@ -177,6 +189,8 @@ typedef struct {
     int max_refine;     /* refinement steps */
     int tile_cols;      /* far-field column tile width, 0 = automatic (<= 12288) */
     int far_variant;    /* far-field launch shape, -1 = autotuned per problem shape */
+    int gemm_mode;      /* block solve products: BEM_GEMM_SPLIT_BF16 (FP32-accurate on tensor cores), FP32, TF32 */
+    double block_tol;   /* block solve: relative normal-equation residual per right-hand side */
 } bem_options_t;
 
 typedef struct {
@@ -205,7 +219,10 @@ int bem_solver_assemble(bem_solver_t s, double k, int precision);
 /* BEM_SOLVE_QR: dense least squares (Householder QR) in the assembly
  * precision.  BEM_SOLVE_GMRES_REFINED: GMRES on the normal equations with
  * FP32 matrix products and FP64 Arnoldi/Givens, inside FP64 iterative
- * refinement (requires a c64 assembly). */
+ * refinement (requires a c64 assembly).  BEM_SOLVE_BLOCK_GMRES: all sources
+ * together; the normal-operator products for every source are GEMMs on the
+ * tensor cores (gemm_mode), each source keeps an FP64 Krylov space, outer
+ * refinement to block_tol (requires a c64 assembly). */
 int bem_solver_solve(bem_solver_t s, int method, bem_solve_info_t *info);
 /* Copy results to host buffers in the given precision (BEM_PREC_*). */
 int bem_solver_get_solution(bem_solver_t s, void *x, int ldx, int precision);

@@ -131,3 +131,21 @@ def test_wrtcplxmat_format(bemlib, tmp_path):
                                "(3.250000,-1.000000) (0.000000,0.000000) \n") or \
         out.read_text() == ("(1.000000,2.000000) (0.000000,-0.500000) \n"
                             "(3.250000,-1.000000) (0.000000,0.000000) \n")
+
+
+def test_geodesic_and_ellipsoid_generators(bemlib):
+    for nu in (1, 3, 8):
+        m = bemlib.Mesh.geodesic(nu)
+        assert m.counts()[:2] == (10 * nu * nu + 2, 20 * nu * nu)
+    m = bemlib.Mesh.geodesic(12).perturbed_ellipsoid(0.075, 0.09, 0.11, 8, 0.05, 7)
+    p, f = m.points(), m.elems()
+    # radial perturbation at most 5% of the ellipsoid radius in that direction
+    u = p / np.linalg.norm(p, axis=1)[:, None]
+    base = 1.0 / np.sqrt((u[:, 0] / 0.075) ** 2 + (u[:, 1] / 0.09) ** 2 + (u[:, 2] / 0.11) ** 2)
+    ratio = np.linalg.norm(p, axis=1) / base
+    assert abs(np.abs(ratio - 1).max() - 0.05) < 1e-9
+    n = np.cross(p[f[:, 0]] - p[f[:, 2]], p[f[:, 1]] - p[f[:, 2]])
+    assert np.all(np.einsum("ij,ij->i", n, p[f].mean(axis=1)) < 0)
+    pts = bemlib.fibonacci_sphere(256, 1.0)
+    np.testing.assert_allclose(np.linalg.norm(pts, axis=1), 1.0, rtol=1e-14)
+    assert abs(pts[:, 2].mean()) < 1e-12
