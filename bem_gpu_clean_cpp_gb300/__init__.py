@@ -39,6 +39,8 @@ SOLVE_QR, SOLVE_GMRES_REFINED, SOLVE_BLOCK_GMRES = 0, 1, 2
 GEMM_FP32, GEMM_SPLIT_BF16, GEMM_TF32 = 0, 1, 2
 SRC_POINT, SRC_PLANE = 0, 1
 ERR_NOT_CONVERGED = 5
+ERR_TOO_LARGE = 8
+ERR_TIMEOUT = 10
 
 _lock = threading.Lock()
 _lib = None
@@ -66,6 +68,35 @@ class Options(ctypes.Structure):
 class SolveInfo(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int), ("refinements", ctypes.c_int),
                 ("rel_residual", ctypes.c_double), ("converged", ctypes.c_int)]
+
+
+class ServerOptions(ctypes.Structure):
+    _fields_ = [("slots", ctypes.c_int), ("hbm_budget_bytes", ctypes.c_double),
+                ("cache_systems", ctypes.c_int), ("block_min_sources", ctypes.c_int),
+                ("solver", Options)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("pnts", ctypes.c_void_p), ("num_pnts", ctypes.c_int), ("elems", ctypes.c_void_p),
+                ("num_elems", ctypes.c_int), ("bc", ctypes.c_void_p), ("chief", ctypes.c_void_p),
+                ("num_chief", ctypes.c_int), ("k", ctypes.c_double), ("srcs", ctypes.c_void_p),
+                ("num_srcs", ctypes.c_int)]
+
+
+class RequestResult(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("method", ctypes.c_int), ("iterations", ctypes.c_int),
+                ("refinements", ctypes.c_int), ("converged", ctypes.c_int), ("rel_residual", ctypes.c_double),
+                ("queue_ms", ctypes.c_double), ("service_ms", ctypes.c_double), ("latency_ms", ctypes.c_double),
+                ("cache_hit", ctypes.c_int), ("device_bytes", ctypes.c_double), ("num_pnts", ctypes.c_int),
+                ("num_srcs", ctypes.c_int)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_longlong), ("completed", ctypes.c_longlong), ("failed", ctypes.c_longlong),
+                ("solves", ctypes.c_longlong), ("cache_hits", ctypes.c_longlong), ("evictions", ctypes.c_longlong),
+                ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double), ("mean_ms", ctypes.c_double),
+                ("max_ms", ctypes.c_double), ("resident_bytes", ctypes.c_double), ("peak_bytes", ctypes.c_double),
+                ("max_in_flight", ctypes.c_int)]
 
 
 # Exported symbols and their signatures (the C ABI of include/bem_gb300.h).
@@ -128,6 +159,13 @@ SIGNATURES = {
     "bem_solver_sync": (_I, [_VP]),
     "bem_solver_stream": (_VP, [_VP]),
     "bem_solver_sizes": (_I, [_VP, _VP, _VP, _VP, _VP]),
+    "bem_server_options_default": (_I, [_VP]),
+    "bem_server_create": (_I, [_VP, ctypes.POINTER(_VP)]),
+    "bem_server_destroy": (_I, [_VP]),
+    "bem_server_submit": (_I, [_VP, _VP, ctypes.POINTER(ctypes.c_longlong)]),
+    "bem_server_wait": (_I, [_VP, ctypes.c_longlong, _D, _VP, _I, _VP]),
+    "bem_server_stats": (_I, [_VP, _VP]),
+    "bem_server_reset_stats": (_I, [_VP]),
 }
 
 
@@ -514,3 +552,81 @@ class Solver:
 
     def stream(self) -> int:
         return int(lib().bem_solver_stream(self._h) or 0)
+
+
+# ---------------------------------------------------------------------------
+# Request server (continuous batching of independent solves)
+# ---------------------------------------------------------------------------
+class Server:
+    """Concurrent surface solves on one GPU (``bem_server_*``): requests are
+    admitted by device footprint while others run, assembled systems are
+    cached by geometry and wavenumber.  ``slots``, ``hbm_budget_bytes``,
+    ``cache_systems`` and ``block_min_sources`` are server options; any other
+    keyword is a solver option (``Options``)."""
+
+    def __init__(self, **kw):
+        o = ServerOptions()
+        _check(lib().bem_server_options_default(ctypes.byref(o)))
+        for key, v in kw.items():
+            if key in ("slots", "hbm_budget_bytes", "cache_systems", "block_min_sources"):
+                setattr(o, key, v)
+            elif hasattr(o.solver, key):
+                setattr(o.solver, key, v)
+            else:
+                raise KeyError(key)
+        h = ctypes.c_void_p()
+        _check(lib().bem_server_create(ctypes.byref(o), ctypes.byref(h)))
+        self._h = h
+        self._shapes = {}
+
+    def close(self) -> None:
+        h = getattr(self, "_h", None)
+        if h and _lib is not None:
+            _lib.bem_server_destroy(h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def submit(self, pnts, elems, k: float, srcs, bc=None, chief=None) -> int:
+        p = np.ascontiguousarray(pnts, dtype=np.float64).reshape(-1, 3)
+        e = np.ascontiguousarray(elems, dtype=np.int32).reshape(-1, 3)
+        b = None if bc is None else np.ascontiguousarray(np.asarray(bc, dtype=np.complex128).reshape(-1, 3))
+        c = None if chief is None else np.ascontiguousarray(chief, dtype=np.float64).reshape(-1, 3)
+        nc = 0 if c is None else c.shape[0]
+        arr = sources(srcs)
+        r = Request(p.ctypes.data, p.shape[0], e.ctypes.data, e.shape[0],
+                    b.ctypes.data if b is not None else None, c.ctypes.data if nc else None, nc,
+                    float(k), ctypes.cast(arr, ctypes.c_void_p), len(arr))
+        t = ctypes.c_longlong()
+        _check(lib().bem_server_submit(self._h, ctypes.byref(r), ctypes.byref(t)))
+        self._shapes[t.value] = (p.shape[0], len(arr))
+        return t.value
+
+    def wait(self, ticket: int, timeout: float = -1.0, check: bool = True):
+        """(x, result): x is the N x S c128 surface pressure (Fortran order)."""
+        n, s = self._shapes[ticket]
+        x = np.zeros((n, s), dtype=np.complex128, order="F")
+        res = RequestResult()
+        st = lib().bem_server_wait(self._h, int(ticket), float(timeout), _ptr(x), n, ctypes.byref(res))
+        if st == ERR_TIMEOUT:
+            _check(st)
+        self._shapes.pop(ticket, None)
+        if check or st != ERR_NOT_CONVERGED:
+            _check(st)
+        out = {f: getattr(res, f) for f, _ in RequestResult._fields_}
+        return x, out
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        _check(lib().bem_server_stats(self._h, ctypes.byref(st)))
+        return {f: getattr(st, f) for f, _ in ServerStats._fields_}
+
+    def reset_stats(self) -> None:
+        _check(lib().bem_server_reset_stats(self._h))

@@ -13,7 +13,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libbem_gb300.so")
 
 SOURCES = ["kernels.cu", "linalg.cu", "block.cu", "chief.cu", "noalloc.cu", "mesh.cpp", "generators.cpp",
-           "solver.cpp", "solve.cpp", "capi.cpp"]
+           "solver.cpp", "solve.cpp", "server.cpp", "capi.cpp"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -33,6 +33,26 @@ struct Error : std::runtime_error {
                         __FILE__, __LINE__,                                          \
                         std::string(#x) + ": " + cudaGetErrorString(e_));           \
     } while (0)
+// Message of the last failed call on this thread (bem_last_error()).
+extern thread_local std::string g_last_error;
+// Body of an extern "C" entry point: exceptions become status codes.
+#define BEM_API_BEGIN try {
+#define BEM_API_END                                   \
+    return BEM_SUCCESS;                               \
+    }                                                 \
+    catch (const ::bem::Error &e) {                   \
+        ::bem::g_last_error = e.what();               \
+        return e.status;                              \
+    }                                                 \
+    catch (const std::bad_alloc &) {                  \
+        ::bem::g_last_error = "host out of memory";   \
+        return BEM_ERR_NOMEM;                         \
+    }                                                 \
+    catch (const std::exception &e) {                 \
+        ::bem::g_last_error = e.what();               \
+        return BEM_FAILURE;                           \
+    }
+
 // After a kernel launch: configuration errors surface here.
 #define KERNEL_CHECK() CUDA_TRY(cudaGetLastError())
 

@@ -9,10 +9,18 @@
 //   W  = A^H T  : Wt (2N x 2S) = At Tt,  W_j = (Wt[2j,s] + Wt[2j+1,S+s]) + i (Wt[2j,S+s] - Wt[2j+1,s]).
 // The GEMMs run on the tensor cores with FP32-accurate split-BF16 emulation
 // (cuBLAS CUBLAS_COMPUTE_32F_EMULATED_16BFX9) or, by option, plain FP32 or
-// TF32.  Each right-hand side keeps its own Krylov space with FP64 Arnoldi
-// (classical Gram-Schmidt twice), Givens rotations and back substitution;
-// iteration stops per right-hand side at its tolerance.  Outer refinement
-// recomputes R = B - A X and G = A^H R with the same GEMMs.
+// TF32.
+//
+// Precision.  Each right-hand side keeps its own Krylov space.  The inner
+// solve only has to reduce the correction equation's residual by inner_tol,
+// so its basis is stored and orthogonalised in FP32 (classical Gram-Schmidt
+// twice); the Hessenberg matrix, Givens rotations, back substitution and the
+// solution X are FP64.  Accuracy comes from the outer refinement: the
+// residual R = B - A X, where all the cancellation happens, is computed
+// FP64-accurately with double-float arithmetic on the FP32 pipe (16 sources
+// per pass over A); G = A^H R, whose inputs are already small, uses the
+// second GEMM.  On GB300 the FP64 pipe runs at about 1/64 of FP32, so FP64
+// Arnoldi over 256 Krylov spaces would cost more than the GEMMs themselves.
 #include <cublas_v2.h>
 #include <cuda_runtime.h>
 
@@ -21,15 +29,32 @@
 #include <string>
 #include <vector>
 
+#include "dfloat.h"
 #include "solver.h"
 
 namespace bem {
 namespace {
 
-__global__ void build_vt_kernel(int N, int S, const double2 *__restrict__ V, float *__restrict__ Vt) {
+constexpr int kResSB = 16;       // right-hand sides per pass of the residual kernel
+constexpr int kResWarps = 8;     // rows per CTA (one warp per row)
+constexpr int kDotLB = 8;        // basis vectors per CTA of the dot kernel
+
+template <typename T>
+__device__ __forceinline__ double2 ld_c(const T *p, size_t i);
+template <>
+__device__ __forceinline__ double2 ld_c<double2>(const double2 *p, size_t i) { return p[i]; }
+template <>
+__device__ __forceinline__ double2 ld_c<float2>(const float2 *p, size_t i) {
+    const float2 v = p[i];
+    return make_double2(v.x, v.y);
+}
+
+// Vt (2N x 2S) from the N x S complex block V (column-major, ld = N).
+template <typename T>
+__global__ void build_vt_kernel(int N, int S, const T *__restrict__ V, float *__restrict__ Vt) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, s = blockIdx.y;
     if (i >= N) return;
-    const double2 v = V[(size_t)s * N + i];
+    const double2 v = ld_c(V, (size_t)s * N + i);
     const size_t ld = 2 * (size_t)N;
     Vt[(size_t)s * ld + 2 * i] = (float)v.x;
     Vt[(size_t)(S + s) * ld + 2 * i] = (float)v.y;
@@ -37,81 +62,199 @@ __global__ void build_vt_kernel(int N, int S, const double2 *__restrict__ V, flo
     Vt[(size_t)(S + s) * ld + 2 * i + 1] = (float)v.x;
 }
 
-// From Tt = A X (R x 2S, real and imaginary column blocks): the residual
-// r = b - t in FP64 (Rv) and packed as floats into Rt for the next GEMM.  Rt
-// may be Tt itself (each element is read and written by the same thread).
-__global__ void resid_from_t_kernel(int R, int S, const float *Tt, const double2 *__restrict__ B,
-                                    double2 *__restrict__ Rv, float *Rt) {
+// Tt (R x 2S, real and imaginary column blocks) = B.
+__global__ void pack_b_kernel(int R, int S, const double2 *__restrict__ B, float *__restrict__ Tt) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x, s = blockIdx.y;
     if (r >= R) return;
-    const double tr = Tt[(size_t)s * R + r], ti = Tt[(size_t)(S + s) * R + r];
     const double2 b = B[(size_t)s * R + r];
-    const double2 v = make_double2(b.x - tr, b.y - ti);
-    Rv[(size_t)s * R + r] = v;
-    Rt[(size_t)s * R + r] = (float)v.x;
-    Rt[(size_t)(S + s) * R + r] = (float)v.y;
+    Tt[(size_t)s * R + r] = (float)b.x;
+    Tt[(size_t)(S + s) * R + r] = (float)b.y;
 }
 
-__global__ void combine_w_kernel(int N, int S, const float *__restrict__ Wt, double2 *__restrict__ W) {
+// Head/tail float split of X (N x S, ld N) into xh/xl (ld ldx, even).
+__global__ void split_x_kernel(int N, int ldx, const double2 *__restrict__ X, float2 *__restrict__ xh,
+                               float2 *__restrict__ xl) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, s = blockIdx.y;
+    if (i >= N) return;
+    const double2 v = X[(size_t)s * N + i];
+    const float hr = (float)v.x, hi = (float)v.y;
+    xh[(size_t)s * ldx + i] = make_float2(hr, hi);
+    xl[(size_t)s * ldx + i] = make_float2((float)(v.x - (double)hr), (float)(v.y - (double)hi));
+}
+
+// R(:, s) = B(:, s) - A X(:, s) for kResSB consecutive sources, FP64-accurate
+// (double-float on the FP32 pipe), written packed as floats into Tt for the
+// A^H R GEMM.  One warp per row; lanes stride over column pairs (float4 of A).
+// The sources' head/tail blocks (N x kResSB) are shared by the CTA's rows
+// through L1/L2; A is read once per kResSB sources.
+__global__ void __launch_bounds__(32 * kResWarps)
+resid_df_multi_kernel(int R, int N, int S, const float2 *__restrict__ A, size_t lda,
+                      const float2 *__restrict__ xh, const float2 *__restrict__ xl, int ldx,
+                      const double2 *__restrict__ B, float *__restrict__ Tt) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int row = blockIdx.x * kResWarps + warp;
+    const int s0 = blockIdx.y * kResSB;
+    if (row >= R) return;
+    const int ns = min(kResSB, S - s0);
+    float rh[kResSB], rl[kResSB], ih[kResSB], il[kResSB];
+#pragma unroll
+    for (int q = 0; q < kResSB; q++) rh[q] = rl[q] = ih[q] = il[q] = 0.f;
+    const float4 *a4 = reinterpret_cast<const float4 *>(A + (size_t)row * lda);
+    const int N2 = N >> 1;
+    for (int j2 = lane; j2 < N2; j2 += 32) {
+        const float4 v = __ldcs(a4 + j2);
+#pragma unroll
+        for (int q = 0; q < kResSB; q++) {
+            if (q < ns) {
+                const size_t o = (size_t)(s0 + q) * ldx / 2 + j2;
+                const float4 h = reinterpret_cast<const float4 *>(xh)[o];
+                const float4 l = reinterpret_cast<const float4 *>(xl)[o];
+                df_mac(rh[q], rl[q], v.x, h.x, l.x);
+                df_mac(rh[q], rl[q], -v.y, h.y, l.y);
+                df_mac(ih[q], il[q], v.x, h.y, l.y);
+                df_mac(ih[q], il[q], v.y, h.x, l.x);
+                df_mac(rh[q], rl[q], v.z, h.z, l.z);
+                df_mac(rh[q], rl[q], -v.w, h.w, l.w);
+                df_mac(ih[q], il[q], v.z, h.w, l.w);
+                df_mac(ih[q], il[q], v.w, h.z, l.z);
+            }
+        }
+    }
+    if ((N & 1) && lane == 0) {
+        const float2 v = A[(size_t)row * lda + N - 1];
+#pragma unroll
+        for (int q = 0; q < kResSB; q++) {
+            if (q < ns) {
+                const float2 h = xh[(size_t)(s0 + q) * ldx + N - 1], l = xl[(size_t)(s0 + q) * ldx + N - 1];
+                df_mac(rh[q], rl[q], v.x, h.x, l.x);
+                df_mac(rh[q], rl[q], -v.y, h.y, l.y);
+                df_mac(ih[q], il[q], v.x, h.y, l.y);
+                df_mac(ih[q], il[q], v.y, h.x, l.x);
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < kResSB; q++) {
+        double sr = (double)rh[q] + (double)rl[q], si = (double)ih[q] + (double)il[q];
+        for (int o = 16; o > 0; o >>= 1) {
+            sr += __shfl_xor_sync(0xffffffffu, sr, o);
+            si += __shfl_xor_sync(0xffffffffu, si, o);
+        }
+        if (lane == 0 && q < ns) {
+            const int s = s0 + q;
+            const double2 b = B[(size_t)s * R + row];
+            Tt[(size_t)s * R + row] = (float)(b.x - sr);
+            Tt[(size_t)(S + s) * R + row] = (float)(b.y - si);
+        }
+    }
+}
+
+// W (N x S complex, float) from Wt (2N x 2S).
+__global__ void combine_w_kernel(int N, int S, const float *__restrict__ Wt, float2 *__restrict__ W) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x, s = blockIdx.y;
     if (j >= N) return;
     const size_t ld = 2 * (size_t)N;
-    const double a = Wt[(size_t)s * ld + 2 * j], b = Wt[(size_t)(S + s) * ld + 2 * j + 1];
-    const double c = Wt[(size_t)(S + s) * ld + 2 * j], d = Wt[(size_t)s * ld + 2 * j + 1];
-    W[(size_t)s * N + j] = make_double2(a + b, c - d);
+    const float a = Wt[(size_t)s * ld + 2 * j], b = Wt[(size_t)(S + s) * ld + 2 * j + 1];
+    const float c = Wt[(size_t)(S + s) * ld + 2 * j], d = Wt[(size_t)s * ld + 2 * j + 1];
+    W[(size_t)s * N + j] = make_float2(a + b, c - d);
 }
 
-// h[s*ldv + l] = V_l(:,s)^H W(:,s), l < k.  V_l block l: N x S column-major.
-__global__ void bdots_kernel(int N, int S, const double2 *__restrict__ V, const double2 *__restrict__ W,
-                             double2 *__restrict__ h, int ldv) {
-    const int l = blockIdx.x, s = blockIdx.y;
-    const double2 *v = V + ((size_t)l * S + s) * N;
-    const double2 *w = W + (size_t)s * N;
-    double sr = 0, si = 0;
+// h[s*ldv + l] = V_l(:,s)^H W(:,s) for l in [l0, l0 + kDotLB) ∩ [0, nl).
+// Basis block l is N x S, column-major, at V + l*N*S.  Per-thread FP32
+// partial sums (N/256 terms), FP64 across threads.
+__global__ void __launch_bounds__(256)
+bdots_kernel(int N, int S, int nl, const float2 *__restrict__ V, const float2 *__restrict__ W,
+             double2 *__restrict__ h, int ldv) {
+    const int s = blockIdx.x, l0 = blockIdx.y * kDotLB;
+    const int nb = min(kDotLB, nl - l0);
+    const size_t NS = (size_t)N * S;
+    const float2 *w = W + (size_t)s * N;
+    const float2 *v = V + (size_t)l0 * NS + (size_t)s * N;
+    float ar[kDotLB], ai[kDotLB];
+#pragma unroll
+    for (int q = 0; q < kDotLB; q++) ar[q] = ai[q] = 0.f;
     for (int i = threadIdx.x; i < N; i += blockDim.x) {
-        const double2 a = v[i], b = w[i];
-        sr += a.x * b.x + a.y * b.y;
-        si += a.x * b.y - a.y * b.x;
+        const float2 b = w[i];
+#pragma unroll
+        for (int q = 0; q < kDotLB; q++) {
+            if (q < nb) {
+                const float2 a = v[(size_t)q * NS + i];
+                ar[q] = fmaf(a.x, b.x, fmaf(a.y, b.y, ar[q]));
+                ai[q] = fmaf(a.x, b.y, fmaf(-a.y, b.x, ai[q]));
+            }
+        }
     }
-    __shared__ double rr[32], ri[32];
-    for (int o = 16; o > 0; o >>= 1) {
-        sr += __shfl_xor_sync(0xffffffffu, sr, o);
-        si += __shfl_xor_sync(0xffffffffu, si, o);
-    }
+    __shared__ double red[kDotLB][2][8];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (lane == 0) { rr[warp] = sr; ri[warp] = si; }
+#pragma unroll
+    for (int q = 0; q < kDotLB; q++) {
+        double xr = ar[q], xi = ai[q];
+        for (int o = 16; o > 0; o >>= 1) {
+            xr += __shfl_xor_sync(0xffffffffu, xr, o);
+            xi += __shfl_xor_sync(0xffffffffu, xi, o);
+        }
+        if (lane == 0) { red[q][0][warp] = xr; red[q][1][warp] = xi; }
+    }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double a = 0, b = 0;
-        for (int t = 0; t < (int)(blockDim.x >> 5); t++) { a += rr[t]; b += ri[t]; }
-        h[(size_t)s * ldv + l] = make_double2(a, b);
+    if (threadIdx.x < nb) {
+        const int q = threadIdx.x;
+        double xr = 0, xi = 0;
+        for (int t = 0; t < (int)(blockDim.x >> 5); t++) { xr += red[q][0][t]; xi += red[q][1][t]; }
+        h[(size_t)s * ldv + l0 + q] = make_double2(xr, xi);
     }
 }
 
-// W(:,s) -= sum_{l<k} V_l(:,s) h[s][l]   (sign = -1), or X(:,s) += ... (sign = +1)
-__global__ void bcombo_kernel(int N, int S, int k, const int *__restrict__ kk, const double2 *__restrict__ V,
-                              const double2 *__restrict__ h, int ldv, double2 *__restrict__ W, double sign) {
+// W(:,s) -= sum_{l<k} V_l(:,s) h[s][l]   (FP32 basis and W).
+__global__ void __launch_bounds__(256)
+bcombo_kernel(int N, int S, int k, const float2 *__restrict__ V, const double2 *__restrict__ h, int ldv,
+              float2 *__restrict__ W) {
+    __shared__ float2 hs[256];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, s = blockIdx.y;
+    for (int t = threadIdx.x; t < k && t < 256; t += blockDim.x) {
+        const double2 c = h[(size_t)s * ldv + t];
+        hs[t] = make_float2((float)c.x, (float)c.y);
+    }
+    __syncthreads();
+    if (i >= N) return;
+    const size_t NS = (size_t)N * S;
+    float sr = 0, si = 0;
+    for (int l = 0; l < k; l++) {
+        const float2 a = V[(size_t)l * NS + (size_t)s * N + i], c = hs[l];
+        sr = fmaf(a.x, c.x, fmaf(-a.y, c.y, sr));
+        si = fmaf(a.x, c.y, fmaf(a.y, c.x, si));
+    }
+    const float2 w = W[(size_t)s * N + i];
+    W[(size_t)s * N + i] = make_float2(w.x - sr, w.y - si);
+}
+
+// X(:,s) += sum_{l<kk[s]} V_l(:,s) y[s][l]  (FP64 accumulation).
+__global__ void __launch_bounds__(256)
+bupdate_x_kernel(int N, int S, const int *__restrict__ kk, const float2 *__restrict__ V,
+                 const double2 *__restrict__ y, int ldv, double2 *__restrict__ X) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, s = blockIdx.y;
     if (i >= N) return;
-    const int ks = kk ? min(k, kk[s]) : k;
+    const int k = kk[s];
+    const size_t NS = (size_t)N * S;
     double sr = 0, si = 0;
-    for (int l = 0; l < ks; l++) {
-        const double2 a = V[((size_t)l * S + s) * N + i], c = h[(size_t)s * ldv + l];
-        sr += a.x * c.x - a.y * c.y;
-        si += a.x * c.y + a.y * c.x;
+    for (int l = 0; l < k; l++) {
+        const float2 a = V[(size_t)l * NS + (size_t)s * N + i];
+        const double2 c = y[(size_t)s * ldv + l];
+        sr += (double)a.x * c.x - (double)a.y * c.y;
+        si += (double)a.x * c.y + (double)a.y * c.x;
     }
-    const double2 w = W[(size_t)s * N + i];
-    W[(size_t)s * N + i] = make_double2(w.x + sign * sr, w.y + sign * si);
+    const double2 x = X[(size_t)s * N + i];
+    X[(size_t)s * N + i] = make_double2(x.x + sr, x.y + si);
 }
 
-__global__ void bnrm2_kernel(int N, const double2 *__restrict__ W, double *__restrict__ out) {
+__global__ void __launch_bounds__(256) bnrm2_kernel(int N, const float2 *__restrict__ W, double *__restrict__ out) {
     const int s = blockIdx.x;
-    const double2 *w = W + (size_t)s * N;
-    double a = 0;
-    for (int i = threadIdx.x; i < N; i += blockDim.x) a += w[i].x * w[i].x + w[i].y * w[i].y;
-    __shared__ double red[32];
-    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = a;
+    const float2 *w = W + (size_t)s * N;
+    float a = 0.f;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) a = fmaf(w[i].x, w[i].x, fmaf(w[i].y, w[i].y, a));
+    double d = a;
+    __shared__ double red[8];
+    for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = d;
     __syncthreads();
     if (threadIdx.x == 0) {
         double t = 0;
@@ -120,14 +263,14 @@ __global__ void bnrm2_kernel(int N, const double2 *__restrict__ W, double *__res
     }
 }
 
-__global__ void bscale_kernel(int N, const double2 *__restrict__ W, const double *__restrict__ nrm,
-                              double2 *__restrict__ Vn) {
+__global__ void bscale_kernel(int N, const float2 *__restrict__ W, const double *__restrict__ nrm,
+                              float2 *__restrict__ Vn) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, s = blockIdx.y;
     if (i >= N) return;
     const double n = nrm[s];
-    const double inv = n > 0 ? 1.0 / n : 0.0;
-    const double2 w = W[(size_t)s * N + i];
-    Vn[(size_t)s * N + i] = make_double2(w.x * inv, w.y * inv);
+    const float inv = n > 0 ? (float)(1.0 / n) : 0.f;
+    const float2 w = W[(size_t)s * N + i];
+    Vn[(size_t)s * N + i] = make_float2(w.x * inv, w.y * inv);
 }
 
 // Per right-hand side: H_s[:, j] = h1 + h2, H_s[j+1, j] = nrm, then the Givens
@@ -244,8 +387,9 @@ static void normal_gemms(bem_solver_s &sv, const float *Vt, float *Tt, float *Wt
 void bem_solver_s::solve_block(bem_solve_info_t *info) {
     const int n = N, m = std::max(1, std::min(opt.max_iter, 200));
     const int ldv = m + 1;
+    const int ldx = (int)lda;   // even: float4 access to the head/tail split of X
     const size_t NS = (size_t)n * S;
-    w_V.ensure(sizeof(double2) * NS * (m + 1));
+    w_V.ensure(sizeof(float2) * NS * (m + 1));             // FP32 Krylov bases, block l = N x S
     w_H.ensure(sizeof(double2) * (size_t)S * m * (m + 1));
     w_cs.ensure(sizeof(double2) * (size_t)S * m);
     w_sn.ensure(sizeof(double2) * (size_t)S * m);
@@ -253,38 +397,47 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
     w_y.ensure(sizeof(double2) * (size_t)S * ldv);
     w_h1.ensure(sizeof(double2) * (size_t)S * ldv);
     w_h2.ensure(sizeof(double2) * (size_t)S * ldv);
-    w_w.ensure(sizeof(double2) * NS);                    // W and the gradient G
-    w_r.ensure(sizeof(double2) * (size_t)R * S);         // residual R
-    w_gv.ensure(sizeof(double2) * NS);                   // A^H B (norms)
-    w_vf.ensure(sizeof(float) * 4 * NS);                 // Vt (2N x 2S)
-    w_t.ensure(sizeof(float) * 2 * (size_t)R * S);       // Tt (R x 2S)
-    w_part.ensure(sizeof(float) * 4 * NS);               // Wt (2N x 2S)
+    w_w.ensure(sizeof(float2) * NS);                       // W and the gradient G
+    w_gv.ensure(sizeof(float2) * 2 * (size_t)ldx * S);     // head/tail split of X
+    w_vf.ensure(sizeof(float) * 4 * NS);                   // Vt (2N x 2S)
+    w_t.ensure(sizeof(float) * 2 * (size_t)R * S);         // Tt (R x 2S)
+    w_part.ensure(sizeof(float) * 4 * NS);                 // Wt (2N x 2S)
     w_scal.ensure(sizeof(double) * 4 * (size_t)S + sizeof(int) * S);
-    double *nrm_b = w_scal.as<double>(), *nrm_g = nrm_b + S, *nrm_w = nrm_b + 2 * S, *res = nrm_b + 3 * S;
+    double *nrm_b = w_scal.as<double>(), *nrm_g = nrm_b + S, *res = nrm_b + 2 * S, *nrm_w = nrm_b + 3 * S;
     int *kk = reinterpret_cast<int *>(nrm_b + 4 * S);
-    double2 *V = w_V.as<double2>(), *W = w_w.as<double2>(), *X = d_x.as<double2>();
+    float2 *V = w_V.as<float2>(), *W = w_w.as<float2>();
+    double2 *X = d_x.as<double2>();
+    float2 *xh = w_gv.as<float2>(), *xl = xh + (size_t)ldx * S;
     float *Vt = w_vf.as<float>(), *Tt = w_t.as<float>(), *Wt = w_part.as<float>();
+    const float2 *A = d_A.as<float2>();
     std::vector<double> h_bn(S), h_gn(S), h_res(S);
     std::vector<int> h_kk(S);
     auto rd = [&](const double *d, std::vector<double> &h) {
         CUDA_TRY(cudaMemcpyAsync(h.data(), d, sizeof(double) * S, cudaMemcpyDeviceToHost, stream));
         CUDA_TRY(cudaStreamSynchronize(stream));
     };
-    const int nb = (n + 255) / 256, sb = (S + 127) / 128;
-    // ||A^H b_s||: X = 0 so the residual is B
+    const int sb = (S + 127) / 128;
     launch_zero_f64(NS, X, stream);
     int total_it = 0, refs = 0;
     double worst = 0.0;
     bool conv = false;
     for (;; refs++) {
-        // R = B - A X ; G = A^H R
-        build_vt_kernel<<<grid2(n, S), 256, 0, stream>>>(n, S, X, Vt);
-        normal_gemms(*this, Vt, Tt, Wt, S, true, false);
-        resid_from_t_kernel<<<grid2(R, S), 256, 0, stream>>>(R, S, Tt, d_B.as<double2>(), w_r.as<double2>(), Tt);
+        // R = B - A X (FP64-accurate), then G = A^H R
+        if (refs == 0) {
+            pack_b_kernel<<<grid2(R, S), 256, 0, stream>>>(R, S, d_B.as<double2>(), Tt);
+            count_launch();
+        } else {
+            BEM_PROF("resid_df_multi", stream);
+            split_x_kernel<<<grid2(n, S), 256, 0, stream>>>(n, ldx, X, xh, xl);
+            resid_df_multi_kernel<<<dim3((R + kResWarps - 1) / kResWarps, (S + kResSB - 1) / kResSB),
+                                    32 * kResWarps, 0, stream>>>(R, n, S, A, lda, xh, xl, ldx,
+                                                                 d_B.as<double2>(), Tt);
+            count_launch(2);
+        }
         normal_gemms(*this, Vt, Tt, Wt, S, false, true);
         combine_w_kernel<<<grid2(n, S), 256, 0, stream>>>(n, S, Wt, W);
         bnrm2_kernel<<<S, 256, 0, stream>>>(n, W, nrm_g);
-        count_launch(5);
+        count_launch(2);
         KERNEL_CHECK();
         rd(nrm_g, h_gn);
         if (refs == 0) h_bn = h_gn;
@@ -292,28 +445,32 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
         for (int s = 0; s < S; s++) worst = std::max(worst, h_bn[s] > 0 ? h_gn[s] / h_bn[s] : 0.0);
         if (worst <= opt.block_tol) { conv = true; break; }
         if (refs >= opt.max_refine) break;
-        // inner batched GMRES on A^H A D = G, D accumulated into X
+        // inner GMRES on A^H A D = G for every source, D accumulated into X
         bscale_kernel<<<grid2(n, S), 256, 0, stream>>>(n, W, nrm_g, V);
         binit_g_kernel<<<sb, 128, 0, stream>>>(S, m, nrm_g, w_g.as<double2>());
         count_launch(2);
         std::fill(h_kk.begin(), h_kk.end(), 0);
         int j = 0;
         for (; j < m; j++) {
-            double2 *Vj = V + (size_t)j * NS;
-            build_vt_kernel<<<grid2(n, S), 256, 0, stream>>>(n, S, Vj, Vt);
+            const float2 *Vj = V + (size_t)j * NS;
+            build_vt_kernel<float2><<<grid2(n, S), 256, 0, stream>>>(n, S, Vj, Vt);
             count_launch();
             normal_gemms(*this, Vt, Tt, Wt, S, true, true);
-            combine_w_kernel<<<grid2(n, S), 256, 0, stream>>>(n, S, Wt, W);
-            bdots_kernel<<<dim3(j + 1, S), 256, 0, stream>>>(n, S, V, W, w_h1.as<double2>(), ldv);
-            bcombo_kernel<<<grid2(n, S), 256, 0, stream>>>(n, S, j + 1, nullptr, V, w_h1.as<double2>(), ldv, W, -1.0);
-            bdots_kernel<<<dim3(j + 1, S), 256, 0, stream>>>(n, S, V, W, w_h2.as<double2>(), ldv);
-            bcombo_kernel<<<grid2(n, S), 256, 0, stream>>>(n, S, j + 1, nullptr, V, w_h2.as<double2>(), ldv, W, -1.0);
-            bnrm2_kernel<<<S, 256, 0, stream>>>(n, W, nrm_w);
-            bscale_kernel<<<grid2(n, S), 256, 0, stream>>>(n, W, nrm_w, V + (size_t)(j + 1) * NS);
-            bhess_givens_kernel<<<sb, 128, 0, stream>>>(j, S, m, w_h1.as<double2>(), w_h2.as<double2>(), ldv, nrm_w,
-                                                        w_H.as<double2>(), w_cs.as<double2>(), w_sn.as<double2>(),
-                                                        w_g.as<double2>(), res);
-            count_launch(9);
+            const dim3 gd(S, (j + 1 + kDotLB - 1) / kDotLB);
+            {
+                BEM_PROF("block_arnoldi", stream);
+                combine_w_kernel<<<grid2(n, S), 256, 0, stream>>>(n, S, Wt, W);
+                bdots_kernel<<<gd, 256, 0, stream>>>(n, S, j + 1, V, W, w_h1.as<double2>(), ldv);
+                bcombo_kernel<<<grid2(n, S), 256, 0, stream>>>(n, S, j + 1, V, w_h1.as<double2>(), ldv, W);
+                bdots_kernel<<<gd, 256, 0, stream>>>(n, S, j + 1, V, W, w_h2.as<double2>(), ldv);
+                bcombo_kernel<<<grid2(n, S), 256, 0, stream>>>(n, S, j + 1, V, w_h2.as<double2>(), ldv, W);
+                bnrm2_kernel<<<S, 256, 0, stream>>>(n, W, nrm_w);
+                bscale_kernel<<<grid2(n, S), 256, 0, stream>>>(n, W, nrm_w, V + (size_t)(j + 1) * NS);
+                bhess_givens_kernel<<<sb, 128, 0, stream>>>(j, S, m, w_h1.as<double2>(), w_h2.as<double2>(), ldv,
+                                                            nrm_w, w_H.as<double2>(), w_cs.as<double2>(),
+                                                            w_sn.as<double2>(), w_g.as<double2>(), res);
+                count_launch(8);
+            }
             KERNEL_CHECK();
             rd(res, h_res);
             bool all = true;
@@ -328,12 +485,11 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
         total_it += j;
         CUDA_TRY(cudaMemcpyAsync(kk, h_kk.data(), sizeof(int) * S, cudaMemcpyHostToDevice, stream));
         btrisolve_kernel<<<sb, 128, 0, stream>>>(S, m, kk, w_H.as<double2>(), w_g.as<double2>(), w_y.as<double2>(), ldv);
-        bcombo_kernel<<<grid2(n, S), 256, 0, stream>>>(n, S, j, kk, V, w_y.as<double2>(), ldv, X, 1.0);
+        bupdate_x_kernel<<<grid2(n, S), 256, 0, stream>>>(n, S, kk, V, w_y.as<double2>(), ldv, X);
         count_launch(2);
         KERNEL_CHECK();
     }
     CUDA_TRY(cudaStreamSynchronize(stream));
-    (void)nb;
     if (info) {
         info->iterations = total_it;
         info->refinements = refs;

@@ -222,6 +222,17 @@ void qr_solve_c64(const float *A_h, int mA, int nA, int ldA, float *B_h, int nB,
     if (hinfo != 0) BEM_FAIL(BEM_ERR_NUMERIC, "QR reported info = " + std::to_string(hinfo));
 }
 
+void validate_options(const bem_options_t &o) {
+    BEM_CHECK_ARG(o.order >= 1 && o.order <= kMaxOrder, "order must be in [1, 12]");
+    BEM_CHECK_ARG(o.density > 0 && o.speed > 0, "density and speed must be positive");
+    BEM_CHECK_ARG(o.near_eta >= 0 && o.near_depth >= 0 && o.near_depth <= 4, "near_eta >= 0, near_depth in [0, 4]");
+    BEM_CHECK_ARG(o.tol > 0 && o.max_iter >= 1 && o.inner_tol > 0 && o.max_refine >= 0, "bad solver tolerances");
+    BEM_CHECK_ARG(o.tile_cols >= 0, "tile_cols must be >= 0");
+    BEM_CHECK_ARG(o.far_variant >= -1 && o.far_variant < far_variants(BEM_PREC_C64), "bad far_variant");
+    BEM_CHECK_ARG(o.gemm_mode >= BEM_GEMM_FP32 && o.gemm_mode <= BEM_GEMM_TF32, "bad gemm_mode");
+    BEM_CHECK_ARG(o.block_tol > 0, "block_tol must be positive");
+}
+
 void apply_global_options(bem_options_t *o) {
     Globals &g = globals();
     std::lock_guard<std::mutex> lk(g.mu);
@@ -233,23 +244,6 @@ void apply_global_options(bem_options_t *o) {
 }  // namespace bem
 
 using namespace bem;
-
-#define BEM_API_BEGIN try {
-#define BEM_API_END                                   \
-    return BEM_SUCCESS;                               \
-    }                                                 \
-    catch (const bem::Error &e) {                     \
-        g_last_error = e.what();                      \
-        return e.status;                              \
-    }                                                 \
-    catch (const std::bad_alloc &) {                  \
-        g_last_error = "host out of memory";          \
-        return BEM_ERR_NOMEM;                         \
-    }                                                 \
-    catch (const std::exception &e) {                 \
-        g_last_error = e.what();                      \
-        return BEM_FAILURE;                           \
-    }
 
 extern "C" {
 
@@ -265,6 +259,7 @@ const char *bem_status_string(int s) {
         case BEM_ERR_STATE: return "invalid state";
         case BEM_ERR_TOO_LARGE: return "size above the supported maximum";
         case BEM_ERR_NUMERIC: return "numerical failure";
+        case BEM_ERR_TIMEOUT: return "timed out";
         default: return "unknown status";
     }
 }
@@ -644,14 +639,7 @@ int bem_solver_destroy(bem_solver_t s) {
 int bem_solver_set_options(bem_solver_t s, const bem_options_t *o) {
     BEM_API_BEGIN
     BEM_CHECK_ARG(s && o, "null argument");
-    BEM_CHECK_ARG(o->order >= 1 && o->order <= kMaxOrder, "order must be in [1, 12]");
-    BEM_CHECK_ARG(o->density > 0 && o->speed > 0, "density and speed must be positive");
-    BEM_CHECK_ARG(o->near_eta >= 0 && o->near_depth >= 0 && o->near_depth <= 4, "near_eta >= 0, near_depth in [0, 4]");
-    BEM_CHECK_ARG(o->tol > 0 && o->max_iter >= 1 && o->inner_tol > 0 && o->max_refine >= 0, "bad solver tolerances");
-    BEM_CHECK_ARG(o->tile_cols >= 0, "tile_cols must be >= 0");
-    BEM_CHECK_ARG(o->far_variant >= -1 && o->far_variant < far_variants(BEM_PREC_C64), "bad far_variant");
-    BEM_CHECK_ARG(o->gemm_mode >= BEM_GEMM_FP32 && o->gemm_mode <= BEM_GEMM_TF32, "bad gemm_mode");
-    BEM_CHECK_ARG(o->block_tol > 0, "block_tol must be positive");
+    validate_options(*o);
     if (o->tile_cols != s->opt.tile_cols) s->tiles[0].valid = s->tiles[1].valid = false;
     s->opt = *o;
     s->assembled = s->solved = false;

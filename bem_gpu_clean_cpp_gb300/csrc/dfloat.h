@@ -1,0 +1,28 @@
+// Double-float arithmetic on the FP32 pipe (FP64-class accuracy where the
+// FP64 pipe is the bottleneck).
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace bem {
+
+// ---- double-float accumulation for the FP64 refinement residuals ----
+// The entries of a c64 matrix are exact floats.  A product a*xh (xh the float
+// head of an FP64 value) is split exactly into p + e by TwoProduct (FMA), p is
+// added to the running head with TwoSum (Knuth), and all the low-order parts
+// go into a float tail; x's own tail xl contributes a*xl to the tail.  The
+// result (head + tail, summed in FP64 at the end) is accurate to ~1e-13
+// relative while the kernel runs on the FP32 pipe, so the FP64-accurate
+// residual costs one HBM pass over A instead of FP64 FMA throughput.  _rn
+// intrinsics keep the compiler from contracting the error-free transforms.
+__device__ __forceinline__ void df_mac(float &hi, float &lo, float a, float xh, float xl) {
+    const float p = __fmul_rn(a, xh);
+    const float e = fmaf(a, xh, -p);
+    const float s = __fadd_rn(hi, p);
+    const float bb = __fsub_rn(s, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+    hi = s;
+    lo = fmaf(a, xl, __fadd_rn(lo, __fadd_rn(err, e)));
+}
+
+}  // namespace bem

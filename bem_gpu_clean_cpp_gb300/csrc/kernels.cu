@@ -740,7 +740,8 @@ template <typename TA, typename TP, typename TP2>
 __global__ void __launch_bounds__(32 * kNearWarps)
 near_assembly_kernel(RowPoints rows, int N, GeoTables geo, Physics ph, int nq, TA *__restrict__ A,
                      size_t lda, const TP *__restrict__ c_part, const TP2 *__restrict__ beta_part,
-                     int ntiles, const DevSource *__restrict__ srcs, int S, double2 *__restrict__ B) {
+                     int ntiles, const DevSource *__restrict__ srcs, int S, double2 *__restrict__ B,
+                     double2 *__restrict__ beta_out) {
     __shared__ Leaf leaves_all[kNearWarps][kMaxLeaves];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int row = blockIdx.x * kNearWarps + warp;
@@ -809,16 +810,39 @@ near_assembly_kernel(RowPoints rows, int N, GeoTables geo, Physics ph, int nq, T
     }
     const double br = __shfl_sync(0xffffffffu, bfr + bnr, 0);
     const double bi = __shfl_sync(0xffffffffu, bfi + bni, 0);
+    if (beta_out && lane == 0) beta_out[row] = make_double2(br, bi);
     for (int s = lane; s < S; s += 32) {
         double2 p = incident_field(srcs[s], ph.k, x);
         B[(size_t)s * rows.R + row] = make_double2(p.x - br, p.y - bi);
     }
 }
 
+// One thread per (row, source): the same incident field and subtraction as
+// the end of near_assembly_kernel.
+__global__ void rhs_from_beta_kernel(RowPoints rows, double k, const DevSource *__restrict__ srcs, int S,
+                                     const double2 *__restrict__ beta, double2 *__restrict__ B) {
+    const int row = blockIdx.x * blockDim.x + threadIdx.x, s = blockIdx.y;
+    if (row >= rows.R || s >= S) return;
+    const double x[3] = {rows.d[3 * (size_t)row], rows.d[3 * (size_t)row + 1], rows.d[3 * (size_t)row + 2]};
+    const double2 b = beta[row];
+    const double2 p = incident_field(srcs[s], k, x);
+    B[(size_t)s * rows.R + row] = make_double2(p.x - b.x, p.y - b.y);
+}
+
+void launch_rhs_from_beta(const RowPoints &rows, double k, const DevSource *srcs, int S, const double2 *beta,
+                          double2 *B, cudaStream_t st) {
+    BEM_PROF("rhs_from_beta", st);
+    if (rows.R <= 0 || S <= 0) return;
+    BEM_CHECK_ARG(S <= 65535, "too many sources for one launch");
+    rhs_from_beta_kernel<<<dim3((rows.R + 127) / 128, S), 128, 0, st>>>(rows, k, srcs, S, beta, B);
+    count_launch();
+    KERNEL_CHECK();
+}
+
 void launch_near_assembly(int prec, const RowPoints &rows, int N, const GeoTables &geo,
                           const Physics &ph, void *A, size_t lda, const void *c_part,
                           const void *beta_part, int ntiles, const DevSource *srcs, int S,
-                          double2 *B, cudaStream_t st) {
+                          double2 *B, double2 *beta_out, cudaStream_t st) {
     BEM_PROF("near_assembly_f64", st);
     if (rows.R <= 0) return;
     BEM_CHECK_ARG(ph.near_depth >= 0 && ph.near_depth <= kMaxDepth, "near_depth must be in [0, 4]");
@@ -827,11 +851,11 @@ void launch_near_assembly(int prec, const RowPoints &rows, int N, const GeoTable
     if (prec == BEM_PREC_C64) {
         near_assembly_kernel<float2, float, float2><<<grid, 32 * kNearWarps, 0, st>>>(
             rows, N, geo, ph, nq, (float2 *)A, lda, (const float *)c_part,
-            (const float2 *)beta_part, ntiles, srcs, S, B);
+            (const float2 *)beta_part, ntiles, srcs, S, B, beta_out);
     } else {
         near_assembly_kernel<double2, double, double2><<<grid, 32 * kNearWarps, 0, st>>>(
             rows, N, geo, ph, nq, (double2 *)A, lda, (const double *)c_part,
-            (const double2 *)beta_part, ntiles, srcs, S, B);
+            (const double2 *)beta_part, ntiles, srcs, S, B, beta_out);
     }
     count_launch();
     KERNEL_CHECK();

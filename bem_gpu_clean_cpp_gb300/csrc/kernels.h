@@ -70,11 +70,17 @@ void launch_far_assembly(int prec, const RowPoints &rows, int N, const GeoTables
 
 // Near-field (singular + near-singular, FP64) assembly and row finalisation:
 // adds the near contributions to A, the diagonal term 1 - sum c, and writes
-// B[s*R + row] = p_inc_s(x) - beta (c128, column-major R x S).
+// B[s*R + row] = p_inc_s(x) - beta (c128, column-major R x S).  beta, the
+// source-independent row term sum_e (cc/cb) sum_j g_j, is also stored in
+// beta_out[row] when beta_out is not null.
 void launch_near_assembly(int prec, const RowPoints &rows, int N, const GeoTables &geo,
                           const Physics &ph, void *A, size_t lda, const void *c_part,
                           const void *beta_part, int ntiles, const DevSource *srcs, int S,
-                          double2 *B, cudaStream_t st);
+                          double2 *B, double2 *beta_out, cudaStream_t st);
+// B[s*R + row] = p_inc_s(x_row) - beta[row]: the right-hand sides of an
+// assembled system for a new set of sources (no element integrals).
+void launch_rhs_from_beta(const RowPoints &rows, double k, const DevSource *srcs, int S,
+                          const double2 *beta, double2 *B, cudaStream_t st);
 
 // Field evaluation.  u: surface solution, column-major N x S (u[s*ldu + node]),
 // c64 or c128 per prec.  out[s*P + p] (c128) = p_inc_s(x_p) - sum_e(...);

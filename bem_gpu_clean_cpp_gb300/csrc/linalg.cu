@@ -11,6 +11,7 @@
 #include <algorithm>
 
 #include "bem_common.h"
+#include "dfloat.h"
 #include "kernels.h"
 
 namespace bem {
@@ -87,24 +88,7 @@ gemv_c64_kernel(int R, int N, const float2 *__restrict__ A, size_t lda, const TX
     }
 }
 
-// ---- double-float accumulation for the FP64 refinement residuals ----
-// The entries of a c64 matrix are exact floats.  A product a*xh (xh the float
-// head of an FP64 value) is split exactly into p + e by TwoProduct (FMA), p is
-// added to the running head with TwoSum (Knuth), and all the low-order parts
-// go into a float tail; x's own tail xl contributes a*xl to the tail.  The
-// result (head + tail, summed in FP64 at the end) is accurate to ~1e-13
-// relative while the kernel runs on the FP32 pipe, so the FP64-accurate
-// residual costs one HBM pass over A instead of FP64 FMA throughput.  _rn
-// intrinsics keep the compiler from contracting the error-free transforms.
-__device__ __forceinline__ void df_mac(float &hi, float &lo, float a, float xh, float xl) {
-    const float p = __fmul_rn(a, xh);
-    const float e = fmaf(a, xh, -p);
-    const float s = __fadd_rn(hi, p);
-    const float bb = __fsub_rn(s, hi);
-    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
-    hi = s;
-    lo = fmaf(a, xl, __fadd_rn(lo, __fadd_rn(err, e)));
-}
+// df_mac (double-float multiply-accumulate) is in dfloat.h.
 
 // Splits FP64 complex values into float head and tail.
 __global__ void split_f64_kernel(int n, const double2 *__restrict__ x, float2 *__restrict__ xh,

@@ -171,8 +171,14 @@ void bem_solver_s::set_sources(const bem_source_t *srcs, int num) {
     static_assert(sizeof(DevSource) == sizeof(bem_source_t), "source layout");
     d_srcs.ensure(sizeof(bem_source_t) * num);
     CUDA_TRY(cudaMemcpyAsync(d_srcs.p, h_srcs.data(), sizeof(bem_source_t) * num, cudaMemcpyHostToDevice, stream));
+    if (assembled) {
+        // A does not depend on the sources: only B = p_inc - beta is rebuilt.
+        d_B.ensure(sizeof(double2) * (size_t)R * S);
+        launch_rhs_from_beta(row_points(), k, d_srcs.as<DevSource>(), S, d_beta.as<double2>(), d_B.as<double2>(),
+                             stream);
+    }
     CUDA_TRY(cudaStreamSynchronize(stream));
-    assembled = solved = false;
+    solved = false;
 }
 
 void bem_solver_s::ensure_geo() {
@@ -332,8 +338,9 @@ void bem_solver_s::assemble(double kk, int precision) {
         launch_far_assembly(precision, row_points(), N, geo_tables(), ts, ph, d_A.p, lda, d_cpart.p, d_bpart.p,
                             stream, variant);
     far_variant_used = variant;
+    d_beta.ensure(sizeof(double2) * (size_t)R);
     launch_near_assembly(precision, row_points(), N, geo_tables(), ph, d_A.p, lda, d_cpart.p, d_bpart.p,
-                         T.ntiles, d_srcs.as<DevSource>(), S, d_B.as<double2>(), stream);
+                         T.ntiles, d_srcs.as<DevSource>(), S, d_B.as<double2>(), d_beta.as<double2>(), stream);
     assembled = true;
     solved = false;
 }
@@ -404,4 +411,41 @@ void bem_solver_s::get_system(void *A, int lda_out, void *B, int ldb_out, int pr
             }
     }
     CUDA_TRY(cudaStreamSynchronize(stream));
+}
+
+size_t bem_solver_s::device_bytes() const {
+    const DevMem *all[] = {&d_nodes, &d_rows_f, &d_rows_d, &d_elems, &d_bc, &d_geo_f, &d_geo_d, &d_srcs,
+                           &tiles[0].recs, &tiles[0].rec_ptr, &tiles[0].cols, &tiles[0].col_cnt,
+                           &tiles[1].recs, &tiles[1].rec_ptr, &tiles[1].cols, &tiles[1].col_cnt,
+                           &d_A, &d_B, &d_cpart, &d_bpart, &d_x, &d_beta,
+                           &w_V, &w_H, &w_cs, &w_sn, &w_g, &w_y, &w_h1, &w_h2, &w_w, &w_t, &w_r, &w_gv, &w_vf,
+                           &w_part, &w_scal, &q_A, &q_B, &q_tau, &q_work, &q_info,
+                           &f_rows_f, &f_rows_d, &f_part, &f_near, &f_out, &f_u};
+    size_t b = 0;
+    for (const DevMem *d : all) b += d->bytes;
+    return b;
+}
+
+size_t bem_solver_s::estimate_bytes(int N, int E, int M, int S, int method, const bem_options_t &o) {
+    const size_t n = (size_t)N, e = (size_t)E, r = (size_t)N + (size_t)M, s = (size_t)S;
+    const size_t lda = (n + 7) / 8 * 8;
+    const size_t ntiles = N <= kTileColsMax ? 1 : (n + kTileColsMax - 1) / kTileColsMax;
+    size_t b = 0;
+    b += 24 * n + 24 * r + 32 * r + 16 * e + 48 * e;                  // nodes, rows, elements, bc
+    b += sizeof(float4) * kGeoFloat4 * e + sizeof(double) * kGeoDouble * e;
+    b += 3 * e * sizeof(TileRec) + 4 * (ntiles + 1) + 4 * n + 4 * ntiles;   // an element touches <= 3 tiles
+    b += 8 * lda * r + 16 * r * s + 12 * ntiles * r + 16 * n * s + 16 * r + 48 * s;
+    if (method == BEM_SOLVE_BLOCK_GMRES) {
+        const size_t m = (size_t)std::max(1, std::min(o.max_iter, 200));
+        b += 16 * n * s * (m + 1) + 16 * s * m * (m + 1) + 16 * s * (4 * m + 4);
+        b += 16 * n * s * 2 + 16 * r * s + 16 * n * s + 8 * r * s + 16 * n * s + 40 * s;
+    } else if (method == BEM_SOLVE_GMRES_REFINED) {
+        const size_t m = (size_t)std::max(1, o.max_iter);
+        b += 16 * n * (m + 1) + 16 * (m + 1) * m + 16 * 6 * (m + 1);
+        b += 16 * n * 2 + 8 * r + 16 * r + 16 * std::max(n, r);
+        b += 16 * n * (size_t)std::max(gemv_h_splits((int)r, N), gemv_h_f64_splits((int)r, N)) + 64;
+    } else {
+        b += 8 * r * n + 8 * r * s + 64 * n + (64u << 20);               // QR copy, tau, library workspace
+    }
+    return b + b / 16 + (8u << 20);
 }

@@ -25,6 +25,8 @@ struct Globals {
     double strength = 0.0;
 };
 Globals &globals();
+// Throws BEM_ERR_INVALID_ARG for options a solver cannot run with.
+void validate_options(const bem_options_t &o);
 
 // Owning device allocation that only grows.
 struct DevMem {
@@ -67,7 +69,7 @@ struct bem_solver_s {
     double k = 0.0;
     size_t lda = 0;
     bool assembled = false, solved = false;
-    bem::DevMem d_A, d_B, d_cpart, d_bpart, d_x;
+    bem::DevMem d_A, d_B, d_cpart, d_bpart, d_x, d_beta;   // d_beta: source-independent row term (R c128)
 
     // GMRES / refinement workspace
     bem::DevMem w_V, w_H, w_cs, w_sn, w_g, w_y, w_h1, w_h2, w_w, w_t, w_r, w_gv, w_vf, w_part, w_scal;
@@ -92,6 +94,12 @@ struct bem_solver_s {
     // own solution.
     void eval_field(const double *pts, int num_pts, void *out, int ldo, int precision,
                     const void *u_dev = nullptr, int u_prec = BEM_PREC_C128);
+
+    // Device bytes currently held by the handle.
+    size_t device_bytes() const;
+    // Upper estimate of the device bytes an assembly (c64) plus solve with the
+    // given method needs, before any allocation.
+    static size_t estimate_bytes(int N, int E, int M, int S, int method, const bem_options_t &o);
 
     void ensure_geo();
     void ensure_tiles(int precision);

@@ -60,6 +60,8 @@ def parse_args():
     ap.add_argument("--config", default="precision", choices=["precision", "rhs"],
                     help="precision: the headline workload (one plane wave); rhs: perturbed ellipsoid, "
                          "8 kHz, 256 point sources solved together (block GMRES)")
+    ap.add_argument("--gemm", type=int, default=1, choices=[0, 1, 2],
+                    help="rhs config: block-solve GEMM mode (0 FP32, 1 split-BF16 FP32-accurate, 2 TF32)")
     ap.add_argument("--mode", default="bench", choices=["bench", "profile"],
                     help="profile: one warm-up solve and one more solve, nothing timed (for ncu captures)")
     return ap.parse_args()
@@ -336,7 +338,7 @@ def run_ours(args):
     if args.config == "rhs":
         method = bem.SOLVE_BLOCK_GMRES
         opts = dict(near_eta=args.eta, near_depth=args.depth, tol=1e-8, inner_tol=1e-4, max_iter=100,
-                    max_refine=6, block_tol=1e-6)
+                    max_refine=10, block_tol=1e-8, gemm_mode=args.gemm)
     else:
         d = src[0][1]
         method = bem.SOLVE_GMRES_REFINED
@@ -528,7 +530,8 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "c64 (FP32) + f64", "data": "synthetic",
         "config": {"workload": name, "sources": S, "nodes": N, "triangles": E, "chief": M,
                    **({"subdiv": args.subdiv, "ka": args.ka} if args.config == "precision" else
-                      {"k": k, "solver": "block GMRES, split-BF16 GEMMs, FP64 refinement"}),
+                      {"k": k, "solver": "block GMRES: %s GEMMs, FP32 Arnoldi, FP64 Givens, FP64-accurate "
+                                          "refinement residual to 1e-8" % ["FP32", "split-BF16", "TF32"][args.gemm]}),
                    "seed": args.seed, "near_eta": args.eta, "near_depth": args.depth,
                    "refine_tol": 1e-8, "parallelism": f"replicas x{dist.world}",
                    "l2": "inputs larger than L2: A (%.0f MB c64) is rewritten every step" % (A_bytes / 1e6)},

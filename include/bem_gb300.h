@@ -31,6 +31,7 @@ extern "C" {
 #define BEM_ERR_STATE 7
 #define BEM_ERR_TOO_LARGE 8
 #define BEM_ERR_NUMERIC 9
+#define BEM_ERR_TIMEOUT 10
 
 /* Library status and introspection (no reference counterpart). */
 const char *bem_status_string(int status);
@@ -235,6 +236,78 @@ int bem_solver_sync(bem_solver_t s);
 /* The cudaStream_t all work of the handle is queued on. */
 void *bem_solver_stream(bem_solver_t s);
 int bem_solver_sizes(bem_solver_t s, int *n, int *m, int *num_elems, int *num_srcs);
+
+/* ------------------------------------------------------------------ */
+/* Request server (no reference counterpart: the reference solves one   */
+/* problem per process, main.cpp:27-73).  Independent surface solves of  */
+/* different meshes, wavenumbers and source counts run concurrently:    */
+/* each of `slots` workers drives its own solver handle on its own CUDA  */
+/* stream, and a request is admitted as soon as a worker is free and its */
+/* device footprint fits the HBM budget, while other requests are on the */
+/* GPU (continuous batching).  Assembled systems stay resident after     */
+/* their request (LRU, `cache_systems`): a later request with the same   */
+/* geometry, boundary condition, CHIEF points and wavenumber reuses A    */
+/* and rebuilds only B for its sources.                                  */
+/* ------------------------------------------------------------------ */
+typedef struct bem_server_s *bem_server_t;
+
+typedef struct {
+    int slots;                 /* requests in flight at once (worker threads) */
+    double hbm_budget_bytes;   /* admission limit; 0 = 85% of the free device memory at creation */
+    int cache_systems;         /* idle assembled systems kept for reuse */
+    int block_min_sources;     /* BEM_SOLVE_BLOCK_GMRES from this many sources on, else GMRES_REFINED */
+    bem_options_t solver;      /* options of every solve */
+} bem_server_options_t;
+
+/* One request.  All arrays are copied by bem_server_submit.  bc: 6 doubles
+ * per element or NULL for (0, 1, -1); chief: NULL when num_chief is 0. */
+typedef struct {
+    const double *pnts;
+    int num_pnts;
+    const int *elems;
+    int num_elems;
+    const double *bc;
+    const double *chief;
+    int num_chief;
+    double k;
+    const bem_source_t *srcs;
+    int num_srcs;
+} bem_request_t;
+
+typedef struct {
+    int status;                /* BEM_SUCCESS or the status of the failed step */
+    int method;                /* BEM_SOLVE_* used */
+    int iterations, refinements, converged;
+    double rel_residual;
+    double queue_ms;           /* submit -> admitted */
+    double service_ms;         /* admitted -> solution on the host */
+    double latency_ms;         /* submit -> solution on the host */
+    int cache_hit;             /* 1: the assembled system was reused */
+    double device_bytes;       /* footprint the request was admitted with */
+    int num_pnts, num_srcs;    /* shape of the solution (N x S) */
+} bem_request_result_t;
+
+typedef struct {
+    long long submitted, completed, failed, solves, cache_hits, evictions;
+    double p50_ms, p99_ms, mean_ms, max_ms;   /* request latency of completed requests */
+    double resident_bytes, peak_bytes;        /* admitted footprints (in flight + cached) */
+    int max_in_flight;
+} bem_server_stats_t;
+
+int bem_server_options_default(bem_server_options_t *o);
+/* Binds the current CUDA device.  Fails with BEM_ERR_CUDA without one. */
+int bem_server_create(const bem_server_options_t *o, bem_server_t *out);
+/* Finishes every admitted and queued request, then frees all device memory. */
+int bem_server_destroy(bem_server_t s);
+int bem_server_submit(bem_server_t s, const bem_request_t *r, long long *ticket);
+/* Waits up to timeout_s seconds (< 0: no limit) for the request.  On
+ * completion copies the surface pressure (N x S c128, column-major, ldx >= N)
+ * to x when x is not NULL, fills res when not NULL, releases the ticket and
+ * returns the request's status; BEM_ERR_TIMEOUT leaves the ticket valid. */
+int bem_server_wait(bem_server_t s, long long ticket, double timeout_s, void *x, int ldx,
+                    bem_request_result_t *res);
+int bem_server_stats(bem_server_t s, bem_server_stats_t *st);
+int bem_server_reset_stats(bem_server_t s);
 
 #ifdef __cplusplus
 }

@@ -160,3 +160,29 @@ def test_errors_are_status_codes(bemlib):
     assert e.value.status == 2
     with pytest.raises(bemlib.BemError):
         s.solve()                             # nothing assembled
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_new_sources_reuse_assembly(bemlib, prec):
+    """set_sources on an assembled system rebuilds B = p_inc - beta only; it
+    equals a full assembly with those sources, and A is unchanged."""
+    p, e, chief = _problem("ico2")
+    k = 2.0
+    bc = np.tile(np.array([0.3 + 0.1j, 1.0, 0.7 - 0.2j]), (e.shape[0], 1))   # cc != 0: beta matters
+    s1 = [("point", (2.0, 0.5, -1.0), 1.0)]
+    s2 = [("plane", (0.0, 0.6, 0.8), 1.0), ("point", (-1.5, 2.0, 0.3), 0.5 - 0.2j)]
+    a = bemlib.Solver()
+    a.set_geometry(p, e, bc=bc, chief=chief)
+    a.set_sources(s1)
+    a.assemble(k, prec)
+    A1, _ = a.system()
+    a.set_sources(s2)
+    A2, B2 = a.system()
+    b = bemlib.Solver()
+    b.set_geometry(p, e, bc=bc, chief=chief)
+    b.set_sources(s2)
+    b.assemble(k, prec)
+    Ab, Bb = b.system()
+    assert rel_err(B2, Bb) < 1e-14
+    assert np.array_equal(A1, A2)
+    assert rel_err(A2, Ab) < (1e-14 if prec == 1 else 1e-6)

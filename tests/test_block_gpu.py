@@ -29,7 +29,7 @@ def _ellipsoid_problem(bemlib, nu=8, nsrc=16, f_hz=4000.0, seed=3):
 @pytest.mark.parametrize("gemm_mode", [0, 1])
 def test_block_gmres_matches_fp64(bemlib, gemm_mode):
     p, e, chief, srcs, bc, k = _ellipsoid_problem(bemlib)
-    s = bemlib.Solver(gemm_mode=gemm_mode, block_tol=1e-6)
+    s = bemlib.Solver(gemm_mode=gemm_mode, block_tol=1e-8)
     s.set_geometry(p, e, bc=bc, chief=chief)
     s.set_sources(srcs)
     s.assemble(k, bemlib.PREC_C128)
@@ -38,7 +38,7 @@ def test_block_gmres_matches_fp64(bemlib, gemm_mode):
     s.assemble(k, bemlib.PREC_C64)
     info = s.solve(bemlib.SOLVE_BLOCK_GMRES)
     xb = s.solution()
-    assert info.converged and info.rel_residual <= 1e-6
+    assert info.converged and info.rel_residual <= 1e-8
     for j in range(xb.shape[1]):
         assert rel_err(xb[:, j], x64[:, j]) < 1e-5, j
     # same answer as solving the sources one by one with the refined solver

@@ -149,3 +149,32 @@ def test_geodesic_and_ellipsoid_generators(bemlib):
     pts = bemlib.fibonacci_sphere(256, 1.0)
     np.testing.assert_allclose(np.linalg.norm(pts, axis=1), 1.0, rtol=1e-14)
     assert abs(pts[:, 2].mean()) < 1e-12
+
+
+def test_server_host_checks(bemlib):
+    """Server options and argument checks that run before any device work."""
+    import ctypes
+    L = bemlib.lib()
+    o = bemlib.ServerOptions()
+    assert L.bem_server_options_default(ctypes.byref(o)) == 0
+    assert (o.slots, o.cache_systems, o.block_min_sources) == (4, 8, 4)
+    assert o.solver.max_iter == 300 and o.solver.order == 6
+    h = ctypes.c_void_p()
+    bad = bemlib.ServerOptions.from_buffer_copy(o)
+    bad.slots = 0
+    assert L.bem_server_create(ctypes.byref(bad), ctypes.byref(h)) == 2
+    bad = bemlib.ServerOptions.from_buffer_copy(o)
+    bad.solver.near_depth = 9
+    assert L.bem_server_create(ctypes.byref(bad), ctypes.byref(h)) == 2
+    t = ctypes.c_longlong()
+    r = bemlib.Request()
+    assert L.bem_server_submit(None, ctypes.byref(r), ctypes.byref(t)) == 2
+    assert L.bem_server_wait(None, 1, 0.0, None, 0, None) == 2
+    st = L.bem_server_create(ctypes.byref(o), ctypes.byref(h))
+    if st == 0:           # a device is present: the empty server shuts down cleanly
+        s = bemlib.ServerStats()
+        assert L.bem_server_stats(h, ctypes.byref(s)) == 0 and s.submitted == 0
+        assert L.bem_server_submit(h, ctypes.byref(r), ctypes.byref(t)) == 2   # empty geometry
+        assert L.bem_server_destroy(h) == 0
+    else:
+        assert st == 3    # no CUDA device: a status, not a crash
