@@ -121,6 +121,8 @@ SIGNATURES = {
     "bem_mesh_destroy": (_I, [_VP]),
     "bem_mesh_read_obj": (_I, [_VP, _S]),
     "bem_mesh_read_obj_robust": (_I, [_VP, _S]),
+    "bem_mesh_read_ply": (_I, [_VP, _S]),
+    "bem_mesh_orient": (_I, [_VP, _VP, _VP, _VP, _VP, _VP]),
     "bem_mesh_set": (_I, [_VP, _VP, _I, _VP, _I]),
     "bem_mesh_set_bc": (_I, [_VP, _VP]),
     "bem_mesh_set_uniform_bc": (_I, [_VP, _D, _D, _D, _D, _D, _D]),
@@ -316,6 +318,18 @@ class Mesh:
 
     def read_obj_robust(self, path: str) -> None:
         _check(lib().bem_mesh_read_obj_robust(self._h, os.fsencode(path)))
+
+    def read_ply(self, path: str) -> None:
+        _check(lib().bem_mesh_read_ply(self._h, os.fsencode(path)))
+
+    def orient(self) -> dict:
+        """Consistent winding with (p1-p3) x (p2-p3) into the body; returns
+        flipped / components / open_edges / nonmanifold / volume."""
+        v = [ctypes.c_int() for _ in range(4)]
+        vol = ctypes.c_double()
+        _check(lib().bem_mesh_orient(self._h, *[ctypes.byref(x) for x in v], ctypes.byref(vol)))
+        return dict(zip(("flipped", "components", "open_edges", "nonmanifold"), (x.value for x in v)),
+                    volume=vol.value)
 
     def set(self, pnts, elems) -> None:
         p = np.ascontiguousarray(pnts, dtype=np.float64).reshape(-1, 3)

@@ -380,6 +380,27 @@ int bem_mesh_read_obj_robust(bem_mesh_t m, const char *path) {
     BEM_API_END
 }
 
+int bem_mesh_read_ply(bem_mesh_t m, const char *path) {
+    BEM_API_BEGIN
+    BEM_CHECK_ARG(m && path, "null argument");
+    read_ply(*m, path);
+    BEM_API_END
+}
+
+int bem_mesh_orient(bem_mesh_t m, int *flipped, int *components, int *open_edges, int *nonmanifold,
+                    double *volume) {
+    BEM_API_BEGIN
+    BEM_CHECK_ARG(m, "null mesh");
+    m->validate();
+    const MeshOrientReport r = orient_mesh(*m);
+    if (flipped) *flipped = r.flipped;
+    if (components) *components = r.components;
+    if (open_edges) *open_edges = r.open_edges;
+    if (nonmanifold) *nonmanifold = r.nonmanifold;
+    if (volume) *volume = r.volume;
+    BEM_API_END
+}
+
 int bem_mesh_set(bem_mesh_t m, const double *pnts, int num_pnts, const int *elems, int num_elems) {
     BEM_API_BEGIN
     BEM_CHECK_ARG(m && pnts && elems && num_pnts > 0 && num_elems > 0, "bad mesh arrays");

@@ -25,6 +25,13 @@ namespace bem {
 
 void read_obj_reference(bem_mesh_s &m, const char *path);
 void read_obj_robust(bem_mesh_s &m, const char *path);
+void read_ply(bem_mesh_s &m, const char *path);
+
+struct MeshOrientReport {
+    int flipped, components, open_edges, nonmanifold;
+    double volume;   // enclosed volume of the closed components after orientation
+};
+MeshOrientReport orient_mesh(bem_mesh_s &m);
 void make_icosphere(bem_mesh_s &m, int subdiv, double radius);
 void make_geodesic(bem_mesh_s &m, int nu, double radius);
 void map_perturbed_ellipsoid(bem_mesh_s &m, double a, double b, double c, int lmax, double amp,

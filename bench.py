@@ -57,9 +57,13 @@ def parse_args():
     ap.add_argument("--depth", type=int, default=2)
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 reference solve")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
-    ap.add_argument("--config", default="precision", choices=["precision", "rhs"],
+    ap.add_argument("--config", default="precision", choices=["precision", "rhs", "freq", "serve"],
                     help="precision: the headline workload (one plane wave); rhs: perturbed ellipsoid, "
-                         "8 kHz, 256 point sources solved together (block GMRES)")
+                         "8 kHz, 256 point sources solved together (block GMRES); freq: 64 frequencies of "
+                         "uneven mesh size as one batch; serve: Poisson request stream through the server")
+    ap.add_argument("--slots", type=int, default=8, help="freq/serve: requests in flight at once")
+    ap.add_argument("--rate", type=float, default=2.0, help="serve: mean request arrivals per second")
+    ap.add_argument("--requests", type=int, default=40, help="serve: requests in the stream")
     ap.add_argument("--gemm", type=int, default=1, choices=[0, 1, 2],
                     help="rhs config: block-solve GEMM mode (0 FP32, 1 split-BF16 FP32-accurate, 2 TF32)")
     ap.add_argument("--mode", default="bench", choices=["bench", "profile"],
@@ -154,6 +158,69 @@ def workload(args):
     d /= np.linalg.norm(d)
     bc = np.tile(np.array([0, 1, 0], dtype=np.complex128), (elems.shape[0], 1))
     return pts, elems, chief, d, float(args.ka), bc
+
+
+WORKLOAD_FREQ = ("64 log-spaced frequencies 100 Hz-12 kHz, perturbed ellipsoid 0.075/0.09/0.11 m seeded per "
+                 "frequency, icosphere s2-s6 (10 elements per wavelength on the longest edge), 16 point sources, "
+                 "16 CHIEF each; all problems submitted at once to the request server")
+WORKLOAD_SERVE = ("Poisson request stream: ellipsoid semi-axes U[0.05,0.2] m, subdivision U{3..6}, "
+                  "f U[200 Hz, 10 kHz], 1-64 point sources; a quarter of the requests repeat an earlier "
+                  "(mesh, frequency) with new sources")
+
+
+def _max_edge(p, e):
+    return max(float(np.linalg.norm(p[e[:, a]] - p[e[:, b]], axis=1).max()) for a, b in ((0, 1), (1, 2), (2, 0)))
+
+
+def _chief_in(rng, rmax, n):
+    u = rng.random((n, 3))
+    r = rmax * np.cbrt(u[:, 0])
+    th = np.arccos(1 - 2 * u[:, 1])
+    ph = 2 * np.pi * u[:, 2]
+    return np.stack([r * np.sin(th) * np.cos(ph), r * np.sin(th) * np.sin(ph), r * np.cos(th)], axis=1)
+
+
+def freq_problems(args, nfreq=64):
+    """The multi-frequency family: per frequency a seeded perturbed ellipsoid
+    at the coarsest subdivision in 2..6 whose longest edge is <= lambda/10."""
+    import bem_gpu_clean_cpp_gb300 as bem
+    out = []
+    srcs = [("point", s, 1.0) for s in bem.fibonacci_sphere(16, 1.0)]
+    for i, f in enumerate(np.geomspace(100.0, 12000.0, nfreq)):
+        lam = 343.21 / f
+        for sub in range(2, 7):
+            m = bem.Mesh.icosphere(sub).perturbed_ellipsoid(0.075, 0.09, 0.11, lmax=8, amp=0.05, seed=args.seed + i)
+            p, e = m.points(), m.elems()
+            if sub == 6 or _max_edge(p, e) <= lam / 10.0:
+                break
+        rng = np.random.default_rng(1000 + args.seed + i)
+        out.append(dict(pnts=p, elems=e, k=2 * np.pi * f / 343.21, srcs=srcs, chief=_chief_in(rng, 0.0375, 16),
+                        f=float(f), subdiv=sub))
+    return out
+
+
+def serve_requests(args, n=40):
+    """Seeded request stream with arrival times (Poisson, rate args.rate/s)."""
+    import bem_gpu_clean_cpp_gb300 as bem
+    rng = np.random.default_rng(args.seed + 77)
+    t, out, scenes = 0.0, [], []
+    for i in range(n):
+        t += rng.exponential(1.0 / args.rate)
+        S = int(rng.integers(1, 65))
+        rot = np.linalg.qr(rng.standard_normal((3, 3)))[0]
+        srcs = [("point", s, 1.0) for s in bem.fibonacci_sphere(S, 1.0) @ rot.T]
+        if scenes and rng.random() < 0.25:
+            sc = scenes[int(rng.integers(0, len(scenes)))]
+        else:
+            ax = rng.uniform(0.05, 0.2, 3)
+            sub = int(rng.integers(3, 7))
+            m = bem.Mesh.icosphere(sub).perturbed_ellipsoid(*ax, lmax=8, amp=0.05, seed=args.seed + 500 + i)
+            f = rng.uniform(200.0, 10000.0)
+            sc = dict(pnts=m.points(), elems=m.elems(), k=2 * np.pi * f / 343.21,
+                      chief=_chief_in(rng, 0.4 * ax.min(), 16), subdiv=sub, f=float(f))
+            scenes.append(sc)
+        out.append(dict(sc, srcs=srcs, t=t))
+    return out
 
 
 def select_workload(args):
@@ -558,10 +625,152 @@ def run_ours(args):
     return 0
 
 
+# ---------------------------------------------------------------------------
+# Batching over frequencies and serving: both through the request server
+# ---------------------------------------------------------------------------
+def _fp64_solve(bem, p, opts):
+    s = bem.Solver(**opts)
+    s.set_geometry(p["pnts"], p["elems"], chief=p["chief"])
+    s.set_sources(p["srcs"])
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s.assemble(p["k"], bem.PREC_C128)
+    s.solve(bem.SOLVE_QR)
+    x = s.solution()
+    return x, time.perf_counter() - t0
+
+
+def run_server_bench(args):
+    import torch
+    import bem_gpu_clean_cpp_gb300 as bem
+
+    dist = Dist(use_cuda=True)
+    torch.cuda.set_device(dist.local)
+    bem.lib()
+    opts = dict(near_eta=args.eta, near_depth=args.depth, tol=1e-8, inner_tol=1e-4, max_iter=100,
+                max_refine=10, block_tol=1e-8, gemm_mode=args.gemm)
+    if args.config == "freq":
+        probs, name, cache = freq_problems(args), WORKLOAD_FREQ, 0
+    else:
+        probs, name, cache = serve_requests(args, args.requests), WORKLOAD_SERVE, 16
+
+    def one_pass(srv):
+        """All problems (freq: submitted at once; serve: at their arrival
+        times from a feeder thread); returns the results in order."""
+        tickets = [None] * len(probs)
+        t0 = time.perf_counter()
+
+        def feed():
+            for i, p in enumerate(probs):
+                if args.config == "serve":
+                    d = p["t"] - (time.perf_counter() - t0)
+                    if d > 0:
+                        time.sleep(d)
+                tickets[i] = srv.submit(p["pnts"], p["elems"], p["k"], p["srcs"], chief=p["chief"])
+
+        th = threading.Thread(target=feed)
+        th.start()
+        out = []
+        for i in range(len(probs)):
+            while tickets[i] is None:
+                time.sleep(0.0002)
+            out.append(srv.wait(tickets[i]))
+        th.join()
+        return out
+
+    solves = sum(len(p["srcs"]) for p in probs)
+    # warm-up: library, handles and kernels on a separate server
+    with bem.Server(slots=args.slots, cache_systems=0, **opts) as w:
+        small = [p for p in probs if p["pnts"].shape[0] <= 2562][:max(3, args.warmup)]
+        for p in small:
+            w.wait(w.submit(p["pnts"], p["elems"], p["k"], p["srcs"], chief=p["chief"]))
+        if args.config == "freq":
+            for _ in range(max(0, args.warmup - 2)):
+                one_pass(w)
+    torch.cuda.synchronize()
+    dev_index = dist.local
+    clocks = Clocks(dev_index)
+    l0 = bem.launch_count()
+    dist.barrier()
+    clocks.start()
+    elapsed, lat, stats, last = 0.0, [], [], None
+    for _ in range(args.steps):
+        # a fresh server per step: the same conditions (empty cache) every time
+        with bem.Server(slots=args.slots, cache_systems=cache, **opts) as srv:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            last = one_pass(srv)
+            torch.cuda.synchronize()
+            elapsed += time.perf_counter() - t0
+            stats.append(srv.stats())
+            lat += [r["latency_ms"] for _, r in last]
+    clk = clocks.stop()
+    launches = bem.launch_count() - l0
+    elapsed = dist.max(elapsed)
+    value = dist.world * args.steps * solves / elapsed
+
+    # ---- accuracy against the plain FP64 solve, and its one-at-a-time time ----
+    errs, fp64_t = [], {}
+    checked_s5 = 0
+    for i, p in enumerate(probs):
+        n = p["pnts"].shape[0]
+        if n > 10242 or (n == 10242 and checked_s5 >= 1):
+            continue
+        checked_s5 += n == 10242
+        x64, t64 = _fp64_solve(bem, p, opts)
+        x = last[i][0]
+        errs.append(float(max(np.abs(x[:, j] - x64[:, j]).max() / np.abs(x64[:, j]).max()
+                              for j in range(x.shape[1]))))
+        fp64_t.setdefault(n, []).append(t64)
+    per_n = {n: float(np.mean(v)) for n, v in fp64_t.items()}
+    if 10242 in per_n:
+        per_n.setdefault(40962, per_n[10242] * (40962 / 10242) ** 3)   # QR cost ~ N^3
+    est = sum(per_n.get(p["pnts"].shape[0], 0.0) for p in probs)
+    fp64 = {"checked_problems": len(errs), "max_rel_err_vs_fp64": max(errs) if errs else None,
+            "seconds_by_nodes": {str(k): v for k, v in sorted(per_n.items())},
+            "estimated_one_at_a_time_s": est,
+            "solves_per_s": solves / est if est else None,
+            "speedup_vs_fp64_plain": value / (solves / est) if est else None,
+            "note": "plain FP64 = c128 assembly + Householder QR per problem, timed for every problem up to "
+                    "10242 nodes (one at 10242), 40962-node problems extrapolated by N^3 from 10242"}
+    sizes = sorted({p["pnts"].shape[0] for p in probs})
+    h2d = sum(24 * p["pnts"].shape[0] + 12 * p["elems"].shape[0] + 24 * 16 + 48 * len(p["srcs"]) for p in probs)
+    d2h = sum(16 * p["pnts"].shape[0] * len(p["srcs"]) for p in probs)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 * elapsed / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c64 (FP32) + f64", "data": "synthetic",
+        "config": {"workload": name, "problems": len(probs), "solves_per_step": solves, "node_counts": sizes,
+                   "slots": args.slots, "cache_systems": cache, "rate_per_s": args.rate if args.config == "serve"
+                   else None, "parallelism": f"replicas x{dist.world}",
+                   "timing": "wall clock between device synchronisations around each pass (several streams)"},
+        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                       "max": float(max(lat))},
+        "server": stats[-1],
+        "fp64_plain": fp64,
+        "gpu_launches": launches,
+        "clocks": clk,
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "note": "the server path takes host arrays and returns host arrays: value is end to end"},
+        "roofline": None, "cpu_baseline": None,
+    }
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    dist.close()
+    return 0
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
+        if args.config in ("freq", "serve"):
+            print(json.dumps({"impl": "reference", "unavailable": "the reference solves one problem per process; "
+                                                                  "its arm runs the precision and rhs configs"}))
+            return 0
         return run_reference(args)
+    if args.config in ("freq", "serve"):
+        return run_server_bench(args)
     if args.mode == "profile":
         return run_profile(args)
     return run_ours(args)

@@ -78,6 +78,20 @@ int bem_mesh_read_obj(bem_mesh_t m, const char *path);
 /* Robust OBJ reader (no reference counterpart): v/vt/vn, f a/b/c, negative
  * indices, polygons (fan-triangulated), any line length. */
 int bem_mesh_read_obj_robust(bem_mesh_t m, const char *path);
+/* PLY reader (no reference counterpart: the reference ships
+ * Head_20kHz_iso.ply but reads OBJ only): ascii, binary_little_endian and
+ * binary_big_endian; x, y, z of "vertex" (any numeric type), the
+ * vertex_indices list of "face" (polygons fan-triangulated), other elements
+ * and properties skipped; bc = (0, 1, -1). */
+int bem_mesh_read_ply(bem_mesh_t m, const char *path);
+/* Winding check and repair (no reference counterpart; the reference trusts
+ * the file, mesh.cu:1215-1265): makes the winding consistent over each
+ * edge-connected component and turns every closed component so that
+ * (p1-p3) x (p2-p3) points into the body.  Any output pointer may be NULL:
+ * elements flipped, components, edges with one element, edges with more than
+ * two, enclosed volume of the closed components. */
+int bem_mesh_orient(bem_mesh_t m, int *flipped, int *components, int *open_edges, int *nonmanifold,
+                    double *volume);
 /* Direct geometry (no reference counterpart); bc reset to (0, 1, -1). */
 int bem_mesh_set(bem_mesh_t m, const double *pnts, int num_pnts, const int *elems, int num_elems);
 /* Per-element bc (ca, cb, cc) as 6 doubles (re, im) each: the triElem::bc

@@ -178,3 +178,79 @@ def test_server_host_checks(bemlib):
         assert L.bem_server_destroy(h) == 0
     else:
         assert st == 3    # no CUDA device: a status, not a crash
+
+
+def _write_ply(path, p, f, fmt, extra=False):
+    """PLY writer for the tests (numpy): optional extra vertex property and an
+    extra element, to check they are skipped."""
+    import struct
+    nv, nf = p.shape[0], f.shape[0]
+    hdr = ["ply", f"format {fmt} 1.0", "comment test", f"element vertex {nv}", "property double x",
+           "property double y", "property double z"]
+    if extra:
+        hdr.append("property uchar red")
+    hdr += [f"element face {nf}", "property list uchar int vertex_indices"]
+    if extra:
+        hdr += ["element edge 1", "property int vertex1", "property int vertex2"]
+    hdr.append("end_header")
+    with open(path, "wb") as fh:
+        fh.write(("\n".join(hdr) + "\n").encode())
+        if fmt == "ascii":
+            for v in p:
+                fh.write((" ".join(repr(float(c)) for c in v) + (" 7" if extra else "") + "\n").encode())
+            for t in f:
+                fh.write(("3 " + " ".join(str(int(i)) for i in t) + "\n").encode())
+            if extra:
+                fh.write(b"0 1\n")
+        else:
+            e = "<" if fmt == "binary_little_endian" else ">"
+            for v in p:
+                fh.write(struct.pack(e + "ddd", *v) + (struct.pack("B", 7) if extra else b""))
+            for t in f:
+                fh.write(struct.pack(e + "Biii", 3, *[int(i) for i in t]))
+            if extra:
+                fh.write(struct.pack(e + "ii", 0, 1))
+
+
+@pytest.mark.parametrize("fmt", ["ascii", "binary_little_endian", "binary_big_endian"])
+def test_read_ply(bemlib, tmp_path, fmt):
+    p, f = icosphere(2, 0.3)
+    path = str(tmp_path / "m.ply")
+    _write_ply(path, p, f, fmt, extra=True)
+    m = bemlib.Mesh()
+    m.read_ply(path)
+    assert np.array_equal(m.elems(), f)
+    assert np.allclose(m.points(), p, rtol=0, atol=1e-15 if fmt != "ascii" else 1e-15)
+    # a quad face is fan-triangulated
+    with open(tmp_path / "q.ply", "w") as fh:
+        fh.write("ply\nformat ascii 1.0\nelement vertex 4\nproperty float x\nproperty float y\nproperty float z\n"
+                 "element face 1\nproperty list uchar int vertex_indices\nend_header\n"
+                 "0 0 0\n1 0 0\n1 1 0\n0 1 0\n4 0 1 2 3\n")
+    m.read_ply(str(tmp_path / "q.ply"))
+    assert m.elems().tolist() == [[0, 1, 2], [0, 2, 3]]
+    with open(tmp_path / "bad.ply", "w") as fh:
+        fh.write("ply\nformat ascii 1.0\nelement vertex 1\nproperty float x\nproperty float y\nproperty float z\n"
+                 "element face 1\nproperty list uchar int vertex_indices\nend_header\n0 0 0\n3 0 1 2\n")
+    with pytest.raises(bemlib.BemError):
+        m.read_ply(str(tmp_path / "bad.ply"))
+
+
+def test_orient_repairs_winding(bemlib):
+    p, f = icosphere(3, 1.0)
+    rng = np.random.default_rng(0)
+    g = f.copy()
+    flip = rng.random(len(g)) < 0.3
+    g[flip, 0], g[flip, 1] = g[flip, 1].copy(), g[flip, 0].copy()
+    m = bemlib.Mesh.from_arrays(p, g)
+    rep = m.orient()
+    e = m.elems()
+    assert rep["components"] == 1 and rep["open_edges"] == 0 and rep["nonmanifold"] == 0
+    assert rep["flipped"] == int(flip.sum())
+    # same winding as the icosphere (inward normals): every face equals the original up to rotation
+    canon = lambda t: tuple(np.roll(t, -int(np.argmin(t))))
+    assert [canon(t) for t in e] == [canon(t) for t in f]
+    assert abs(rep["volume"] - 4 / 3 * np.pi) < 0.05
+    # a fully outward mesh is turned inward; a second call changes nothing
+    m2 = bemlib.Mesh.from_arrays(p, f[:, [1, 0, 2]])
+    assert m2.orient()["flipped"] == len(f)
+    assert m2.orient()["flipped"] == 0
