@@ -17,7 +17,7 @@
 // twice); the Hessenberg matrix, Givens rotations, back substitution and the
 // solution X are FP64.  Accuracy comes from the outer refinement: the
 // residual R = B - A X, where all the cancellation happens, is computed
-// FP64-accurately with double-float arithmetic on the FP32 pipe (16 sources
+// FP64-accurately with double-float arithmetic on the FP32 pipe (8 sources
 // per pass over A); G = A^H R, whose inputs are already small, uses the
 // second GEMM.  On GB300 the FP64 pipe runs at about 1/64 of FP32, so FP64
 // Arnoldi over 256 Krylov spaces would cost more than the GEMMs themselves.
@@ -35,8 +35,9 @@
 namespace bem {
 namespace {
 
-constexpr int kResSB = 16;       // right-hand sides per pass of the residual kernel
-constexpr int kResWarps = 8;     // rows per CTA (one warp per row)
+constexpr int kResSB = 8;        // right-hand sides per pass of the residual kernel
+constexpr int kResRPW = 2;       // rows per warp of the residual kernel
+constexpr int kResWarps = 8;     // warps per CTA of the residual kernel
 constexpr int kDotLB = 8;        // basis vectors per CTA of the dot kernel
 
 template <typename T>
@@ -49,17 +50,56 @@ __device__ __forceinline__ double2 ld_c<float2>(const float2 *p, size_t i) {
     return make_double2(v.x, v.y);
 }
 
-// Vt (2N x 2S) from the N x S complex block V (column-major, ld = N).
+// TF32 head of a float: round to the nearest value with 10 stored mantissa
+// bits (ties away from zero); v - head(v) is exact in FP32.
+__device__ __forceinline__ float tf32_head(float v) {
+    return __uint_as_float((__float_as_uint(v) + 0x1000u) & 0xFFFFE000u);
+}
+
+// Vt (2N x 2S) from the N x S complex block V (column-major, ld = N); with
+// Vlo, Vt gets the TF32 heads and Vlo the tails.
 template <typename T>
-__global__ void build_vt_kernel(int N, int S, const T *__restrict__ V, float *__restrict__ Vt) {
+__global__ void build_vt_kernel(int N, int S, const T *__restrict__ V, float *__restrict__ Vt,
+                                float *__restrict__ Vlo) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, s = blockIdx.y;
     if (i >= N) return;
     const double2 v = ld_c(V, (size_t)s * N + i);
     const size_t ld = 2 * (size_t)N;
-    Vt[(size_t)s * ld + 2 * i] = (float)v.x;
-    Vt[(size_t)(S + s) * ld + 2 * i] = (float)v.y;
-    Vt[(size_t)s * ld + 2 * i + 1] = -(float)v.y;
-    Vt[(size_t)(S + s) * ld + 2 * i + 1] = (float)v.x;
+    const size_t o[4] = {(size_t)s * ld + 2 * i, (size_t)(S + s) * ld + 2 * i, (size_t)s * ld + 2 * i + 1,
+                         (size_t)(S + s) * ld + 2 * i + 1};
+    const float val[4] = {(float)v.x, (float)v.y, -(float)v.y, (float)v.x};
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        if (Vlo) {
+            const float h = tf32_head(val[q]);
+            Vt[o[q]] = h;
+            Vlo[o[q]] = val[q] - h;
+        } else {
+            Vt[o[q]] = val[q];
+        }
+    }
+}
+
+// In place: x -> TF32 head, lo -> tail (n floats).
+__global__ void split_tf32_kernel(size_t n, float *__restrict__ x, float *__restrict__ lo) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float v = x[i], h = tf32_head(v);
+        x[i] = h;
+        lo[i] = v - h;
+    }
+}
+
+// hi/lo TF32 planes of the interleaved-real view of A (R rows of N2 = 2N
+// floats, row stride ld floats).
+__global__ void split_a_tf32_kernel(int R, int N2, size_t ld, const float *__restrict__ A, float *__restrict__ hi,
+                                    float *__restrict__ lo) {
+    const size_t total = (size_t)R * N2;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+        const size_t i = (t / N2) * ld + t % N2;
+        const float v = A[i], h = tf32_head(v);
+        hi[i] = h;
+        lo[i] = v - h;
+    }
 }
 
 // Tt (R x 2S, real and imaginary column blocks) = B.
@@ -84,67 +124,84 @@ __global__ void split_x_kernel(int N, int ldx, const double2 *__restrict__ X, fl
 
 // R(:, s) = B(:, s) - A X(:, s) for kResSB consecutive sources, FP64-accurate
 // (double-float on the FP32 pipe), written packed as floats into Tt for the
-// A^H R GEMM.  One warp per row; lanes stride over column pairs (float4 of A).
-// The sources' head/tail blocks (N x kResSB) are shared by the CTA's rows
-// through L1/L2; A is read once per kResSB sources.
+// A^H R GEMM.  A warp owns kResRPW rows; lanes stride over column pairs
+// (float4 of A).  Each head/tail load of X serves kResRPW rows, and the
+// sources' blocks (N x kResSB) are shared by the CTA's warps through L1; A is
+// read once per kResSB sources.
 __global__ void __launch_bounds__(32 * kResWarps)
 resid_df_multi_kernel(int R, int N, int S, const float2 *__restrict__ A, size_t lda,
                       const float2 *__restrict__ xh, const float2 *__restrict__ xl, int ldx,
                       const double2 *__restrict__ B, float *__restrict__ Tt) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int row = blockIdx.x * kResWarps + warp;
+    const int row0 = (blockIdx.x * kResWarps + warp) * kResRPW;
     const int s0 = blockIdx.y * kResSB;
-    if (row >= R) return;
-    const int ns = min(kResSB, S - s0);
-    float rh[kResSB], rl[kResSB], ih[kResSB], il[kResSB];
+    if (row0 >= R) return;
+    const int ns = min(kResSB, S - s0), nr = min(kResRPW, R - row0);
+    float rh[kResRPW][kResSB], rl[kResRPW][kResSB], ih[kResRPW][kResSB], il[kResRPW][kResSB];
 #pragma unroll
-    for (int q = 0; q < kResSB; q++) rh[q] = rl[q] = ih[q] = il[q] = 0.f;
-    const float4 *a4 = reinterpret_cast<const float4 *>(A + (size_t)row * lda);
+    for (int p = 0; p < kResRPW; p++)
+#pragma unroll
+        for (int q = 0; q < kResSB; q++) rh[p][q] = rl[p][q] = ih[p][q] = il[p][q] = 0.f;
+    const float4 *a4[kResRPW];
+#pragma unroll
+    for (int p = 0; p < kResRPW; p++)
+        a4[p] = reinterpret_cast<const float4 *>(A + (size_t)(row0 + min(p, nr - 1)) * lda);
+    const float4 *xh4 = reinterpret_cast<const float4 *>(xh), *xl4 = reinterpret_cast<const float4 *>(xl);
     const int N2 = N >> 1;
     for (int j2 = lane; j2 < N2; j2 += 32) {
-        const float4 v = __ldcs(a4 + j2);
+        float4 v[kResRPW];
+#pragma unroll
+        for (int p = 0; p < kResRPW; p++) v[p] = __ldcs(a4[p] + j2);
 #pragma unroll
         for (int q = 0; q < kResSB; q++) {
             if (q < ns) {
-                const size_t o = (size_t)(s0 + q) * ldx / 2 + j2;
-                const float4 h = reinterpret_cast<const float4 *>(xh)[o];
-                const float4 l = reinterpret_cast<const float4 *>(xl)[o];
-                df_mac(rh[q], rl[q], v.x, h.x, l.x);
-                df_mac(rh[q], rl[q], -v.y, h.y, l.y);
-                df_mac(ih[q], il[q], v.x, h.y, l.y);
-                df_mac(ih[q], il[q], v.y, h.x, l.x);
-                df_mac(rh[q], rl[q], v.z, h.z, l.z);
-                df_mac(rh[q], rl[q], -v.w, h.w, l.w);
-                df_mac(ih[q], il[q], v.z, h.w, l.w);
-                df_mac(ih[q], il[q], v.w, h.z, l.z);
+                const size_t o = (size_t)(s0 + q) * (ldx / 2) + j2;
+                const float4 h = xh4[o], l = xl4[o];
+#pragma unroll
+                for (int p = 0; p < kResRPW; p++) {
+                    df_mac(rh[p][q], rl[p][q], v[p].x, h.x, l.x);
+                    df_mac(rh[p][q], rl[p][q], -v[p].y, h.y, l.y);
+                    df_mac(ih[p][q], il[p][q], v[p].x, h.y, l.y);
+                    df_mac(ih[p][q], il[p][q], v[p].y, h.x, l.x);
+                    df_mac(rh[p][q], rl[p][q], v[p].z, h.z, l.z);
+                    df_mac(rh[p][q], rl[p][q], -v[p].w, h.w, l.w);
+                    df_mac(ih[p][q], il[p][q], v[p].z, h.w, l.w);
+                    df_mac(ih[p][q], il[p][q], v[p].w, h.z, l.z);
+                }
             }
         }
     }
     if ((N & 1) && lane == 0) {
-        const float2 v = A[(size_t)row * lda + N - 1];
 #pragma unroll
-        for (int q = 0; q < kResSB; q++) {
-            if (q < ns) {
-                const float2 h = xh[(size_t)(s0 + q) * ldx + N - 1], l = xl[(size_t)(s0 + q) * ldx + N - 1];
-                df_mac(rh[q], rl[q], v.x, h.x, l.x);
-                df_mac(rh[q], rl[q], -v.y, h.y, l.y);
-                df_mac(ih[q], il[q], v.x, h.y, l.y);
-                df_mac(ih[q], il[q], v.y, h.x, l.x);
+        for (int p = 0; p < kResRPW; p++) {
+            const float2 v = reinterpret_cast<const float2 *>(a4[p])[N - 1];
+#pragma unroll
+            for (int q = 0; q < kResSB; q++) {
+                if (q < ns) {
+                    const float2 h = xh[(size_t)(s0 + q) * ldx + N - 1], l = xl[(size_t)(s0 + q) * ldx + N - 1];
+                    df_mac(rh[p][q], rl[p][q], v.x, h.x, l.x);
+                    df_mac(rh[p][q], rl[p][q], -v.y, h.y, l.y);
+                    df_mac(ih[p][q], il[p][q], v.x, h.y, l.y);
+                    df_mac(ih[p][q], il[p][q], v.y, h.x, l.x);
+                }
             }
         }
     }
 #pragma unroll
-    for (int q = 0; q < kResSB; q++) {
-        double sr = (double)rh[q] + (double)rl[q], si = (double)ih[q] + (double)il[q];
-        for (int o = 16; o > 0; o >>= 1) {
-            sr += __shfl_xor_sync(0xffffffffu, sr, o);
-            si += __shfl_xor_sync(0xffffffffu, si, o);
-        }
-        if (lane == 0 && q < ns) {
-            const int s = s0 + q;
-            const double2 b = B[(size_t)s * R + row];
-            Tt[(size_t)s * R + row] = (float)(b.x - sr);
-            Tt[(size_t)(S + s) * R + row] = (float)(b.y - si);
+    for (int p = 0; p < kResRPW; p++) {
+#pragma unroll
+        for (int q = 0; q < kResSB; q++) {
+            double sr = (double)rh[p][q] + (double)rl[p][q], si = (double)ih[p][q] + (double)il[p][q];
+            for (int o = 16; o > 0; o >>= 1) {
+                sr += __shfl_xor_sync(0xffffffffu, sr, o);
+                si += __shfl_xor_sync(0xffffffffu, si, o);
+            }
+            if (lane == 0 && q < ns && p < nr) {
+                const int s = s0 + q, row = row0 + p;
+                const double2 b = B[(size_t)s * R + row];
+                Tt[(size_t)s * R + row] = (float)(b.x - sr);
+                Tt[(size_t)(S + s) * R + row] = (float)(b.y - si);
+            }
         }
     }
 }
@@ -361,26 +418,53 @@ void cublas_ok(cublasStatus_t s, const char *what) {
 }
 }  // namespace
 
-// Tt (R x 2S) = At^T Vt (first) and/or Wt (2N x 2S) = At Tt (second).
-static void normal_gemms(bem_solver_s &sv, const float *Vt, float *Tt, float *Wt, int S, bool first, bool second) {
+// Tt (R x 2S) = At^T Vt (first) and/or Wt (2N x 2S) = At Tt (second).  In
+// TF32x3 mode Vt holds the heads and Vlo the tails of the right-hand block,
+// and Tt is split in place (Tlo) before the second product; each product is
+// head*tail + tail*head + head*head, smallest terms first.
+static void normal_gemms(bem_solver_s &sv, const float *Vt, const float *Vlo, float *Tt, float *Tlo, float *Wt,
+                         int S, bool first, bool second) {
     const float one = 1.f, zero = 0.f;
     const int N = sv.N, R = sv.R;
     const float *At = reinterpret_cast<const float *>(sv.d_A.p);
     const int ldat = (int)(2 * sv.lda);
-    const cublasComputeType_t ct = sv.opt.gemm_mode == 0   ? CUBLAS_COMPUTE_32F
-                                   : sv.opt.gemm_mode == 2 ? CUBLAS_COMPUTE_32F_FAST_TF32
-                                                           : CUBLAS_COMPUTE_32F_EMULATED_16BFX9;
+    const bool x3 = sv.opt.gemm_mode == BEM_GEMM_TF32X3;
+    const cublasComputeType_t ct = sv.opt.gemm_mode == BEM_GEMM_FP32         ? CUBLAS_COMPUTE_32F
+                                   : sv.opt.gemm_mode == BEM_GEMM_SPLIT_BF16 ? CUBLAS_COMPUTE_32F_EMULATED_16BFX9
+                                                                             : CUBLAS_COMPUTE_32F_FAST_TF32;
+    const float *Ahi = x3 ? sv.x_Ahi.as<float>() : At, *Alo = x3 ? sv.x_Alo.as<float>() : nullptr;
+    auto gemm1 = [&](const float *a, const float *b, const float *beta) {
+        cublas_ok(cublasGemmEx(sv.cublas, CUBLAS_OP_T, CUBLAS_OP_N, R, 2 * S, 2 * N, &one, a, CUDA_R_32F, ldat, b,
+                               CUDA_R_32F, 2 * N, beta, Tt, CUDA_R_32F, R, ct, CUBLAS_GEMM_DEFAULT),
+                  "GEMM A V");
+    };
+    auto gemm2 = [&](const float *a, const float *b, const float *beta) {
+        cublas_ok(cublasGemmEx(sv.cublas, CUBLAS_OP_N, CUBLAS_OP_N, 2 * N, 2 * S, R, &one, a, CUDA_R_32F, ldat, b,
+                               CUDA_R_32F, R, beta, Wt, CUDA_R_32F, 2 * N, ct, CUBLAS_GEMM_DEFAULT),
+                  "GEMM A^H T");
+    };
     if (first) {
         BEM_PROF("gemm_AV", sv.stream);
-        cublas_ok(cublasGemmEx(sv.cublas, CUBLAS_OP_T, CUBLAS_OP_N, R, 2 * S, 2 * N, &one, At, CUDA_R_32F, ldat, Vt,
-                               CUDA_R_32F, 2 * N, &zero, Tt, CUDA_R_32F, R, ct, CUBLAS_GEMM_DEFAULT),
-                  "GEMM A V");
+        if (x3) {
+            gemm1(Ahi, Vlo, &zero);
+            gemm1(Alo, Vt, &one);
+            gemm1(Ahi, Vt, &one);
+        } else {
+            gemm1(At, Vt, &zero);
+        }
     }
     if (second) {
         BEM_PROF("gemm_AhT", sv.stream);
-        cublas_ok(cublasGemmEx(sv.cublas, CUBLAS_OP_N, CUBLAS_OP_N, 2 * N, 2 * S, R, &one, At, CUDA_R_32F, ldat, Tt,
-                               CUDA_R_32F, R, &zero, Wt, CUDA_R_32F, 2 * N, ct, CUBLAS_GEMM_DEFAULT),
-                  "GEMM A^H T");
+        if (x3) {
+            const size_t n = 2 * (size_t)R * S;
+            split_tf32_kernel<<<(unsigned)std::min<size_t>((n + 255) / 256, 4096), 256, 0, sv.stream>>>(n, Tt, Tlo);
+            count_launch();
+            gemm2(Ahi, Tlo, &zero);
+            gemm2(Alo, Tt, &one);
+            gemm2(Ahi, Tt, &one);
+        } else {
+            gemm2(At, Tt, &zero);
+        }
     }
 }
 
@@ -410,6 +494,23 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
     float2 *xh = w_gv.as<float2>(), *xl = xh + (size_t)ldx * S;
     float *Vt = w_vf.as<float>(), *Tt = w_t.as<float>(), *Wt = w_part.as<float>();
     const float2 *A = d_A.as<float2>();
+    const bool x3 = opt.gemm_mode == BEM_GEMM_TF32X3;
+    float *Vlo = nullptr, *Tlo = nullptr;
+    if (x3) {
+        x_vlo.ensure(sizeof(float) * 4 * NS);
+        x_tlo.ensure(sizeof(float) * 2 * (size_t)R * S);
+        Vlo = x_vlo.as<float>();
+        Tlo = x_tlo.as<float>();
+        if (!tf32_split_valid) {
+            x_Ahi.ensure(sizeof(float) * 2 * lda * (size_t)R);
+            x_Alo.ensure(sizeof(float) * 2 * lda * (size_t)R);
+            split_a_tf32_kernel<<<152 * 16, 256, 0, stream>>>(R, 2 * n, 2 * lda, reinterpret_cast<const float *>(A),
+                                                              x_Ahi.as<float>(), x_Alo.as<float>());
+            count_launch();
+            KERNEL_CHECK();
+            tf32_split_valid = true;
+        }
+    }
     std::vector<double> h_bn(S), h_gn(S), h_res(S);
     std::vector<int> h_kk(S);
     auto rd = [&](const double *d, std::vector<double> &h) {
@@ -429,12 +530,13 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
         } else {
             BEM_PROF("resid_df_multi", stream);
             split_x_kernel<<<grid2(n, S), 256, 0, stream>>>(n, ldx, X, xh, xl);
-            resid_df_multi_kernel<<<dim3((R + kResWarps - 1) / kResWarps, (S + kResSB - 1) / kResSB),
+            resid_df_multi_kernel<<<dim3((R + kResWarps * kResRPW - 1) / (kResWarps * kResRPW),
+                                         (S + kResSB - 1) / kResSB),
                                     32 * kResWarps, 0, stream>>>(R, n, S, A, lda, xh, xl, ldx,
                                                                  d_B.as<double2>(), Tt);
             count_launch(2);
         }
-        normal_gemms(*this, Vt, Tt, Wt, S, false, true);
+        normal_gemms(*this, Vt, Vlo, Tt, Tlo, Wt, S, false, true);
         combine_w_kernel<<<grid2(n, S), 256, 0, stream>>>(n, S, Wt, W);
         bnrm2_kernel<<<S, 256, 0, stream>>>(n, W, nrm_g);
         count_launch(2);
@@ -453,9 +555,9 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
         int j = 0;
         for (; j < m; j++) {
             const float2 *Vj = V + (size_t)j * NS;
-            build_vt_kernel<float2><<<grid2(n, S), 256, 0, stream>>>(n, S, Vj, Vt);
+            build_vt_kernel<float2><<<grid2(n, S), 256, 0, stream>>>(n, S, Vj, Vt, Vlo);
             count_launch();
-            normal_gemms(*this, Vt, Tt, Wt, S, true, true);
+            normal_gemms(*this, Vt, Vlo, Tt, Tlo, Wt, S, true, true);
             const dim3 gd(S, (j + 1 + kDotLB - 1) / kDotLB);
             {
                 BEM_PROF("block_arnoldi", stream);

@@ -188,6 +188,23 @@ __device__ __forceinline__ bool pair_is_near(int row, int N, int4 nd, float4 xh,
 // three nodal integrals (N1 = xi1, N2 = xi2, N3 = 1 - xi1 - xi2).  The 1/(4 pi)
 // and |J| factors are applied once per pair by the caller.
 // ---------------------------------------------------------------------------
+// sin and cos of a phase x = kr >= 0 for the FP32 quadrature.  The fast
+// __sincosf is documented with a bounded error on [-pi, pi] only, and its
+// error grows with |x| outside (kr reaches ~30 at 8 kHz on a 0.11 m body), so
+// x is first reduced by 2 pi with the two-constant Cody-Waite scheme (Cody & Waite,
+// "Software Manual for the Elementary Functions", 1980) using FMAs:
+// n = rint(x / 2pi), y = (x - n C1) - n C2 with C1 = fl(2 pi), C2 = 2 pi - C1.
+// With the FMA each step rounds once, so y carries an absolute error of a few
+// ulps of y, independent of n.
+__device__ __forceinline__ void sincos_phase(float x, float *sn, float *cs) {
+    constexpr float kInv2Pi = 0.15915493667125702f;
+    constexpr float k2PiHi = 6.2831854820251465f;
+    constexpr float k2PiLo = -1.7484555314695172e-07f;
+    const float n = rintf(x * kInv2Pi);
+    const float y = fmaf(-n, k2PiLo, fmaf(-n, k2PiHi, x));
+    __sincosf(y, sn, cs);
+}
+
 struct SumsF {
     float g0r, g0i, g1r, g1i, g2r, g2i;   // G sums
     float h0r, h0i, h1r, h1i, h2r, h2i;   // dG/dn sums
@@ -209,7 +226,7 @@ __device__ __forceinline__ void far_sums_f32(float3 d3, float3 e1, float3 e2, fl
         float ri = rsqrtf(r2);
         float r = r2 * ri;
         float sn, cs;
-        __sincosf(k * r, &sn, &cs);
+        sincos_phase(k * r, &sn, &cs);
         float gr = cs * ri, gi = -sn * ri;            // 4 pi G
         float hq = hgt * ri;                          // dr/dn
         float tr = fmaf(gi, k, -gr * ri);             // 4 pi G (-1/r - ik)
@@ -269,7 +286,7 @@ __device__ __forceinline__ void far_sums_f32_o6(float3 d3, float3 e1, float3 e2,
             const float ri = rsqrtf(r2);
             const float kr = k * (r2 * ri);
             float sn, cs;
-            __sincosf(kr, &sn, &cs);
+            sincos_phase(kr, &sn, &cs);
             const float A = fmaf(kr, sn, cs);      // c + kr s
             const float Bv = fmaf(kr, cs, -sn);    // kr c - s
             const float ri3 = ri * ri * ri;

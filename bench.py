@@ -64,8 +64,8 @@ def parse_args():
     ap.add_argument("--slots", type=int, default=8, help="freq/serve: requests in flight at once")
     ap.add_argument("--rate", type=float, default=2.0, help="serve: mean request arrivals per second")
     ap.add_argument("--requests", type=int, default=40, help="serve: requests in the stream")
-    ap.add_argument("--gemm", type=int, default=1, choices=[0, 1, 2],
-                    help="rhs config: block-solve GEMM mode (0 FP32, 1 split-BF16 FP32-accurate, 2 TF32)")
+    ap.add_argument("--gemm", type=int, default=1, choices=[0, 1, 2, 3],
+                    help="block-solve GEMM mode (0 FP32, 1 split-BF16 FP32-accurate, 2 TF32, 3 TF32x3)")
     ap.add_argument("--mode", default="bench", choices=["bench", "profile"],
                     help="profile: one warm-up solve and one more solve, nothing timed (for ncu captures)")
     return ap.parse_args()
@@ -598,7 +598,7 @@ def run_ours(args):
         "config": {"workload": name, "sources": S, "nodes": N, "triangles": E, "chief": M,
                    **({"subdiv": args.subdiv, "ka": args.ka} if args.config == "precision" else
                       {"k": k, "solver": "block GMRES: %s GEMMs, FP32 Arnoldi, FP64 Givens, FP64-accurate "
-                                          "refinement residual to 1e-8" % ["FP32", "split-BF16", "TF32"][args.gemm]}),
+                                          "refinement residual to 1e-8" % ["FP32", "split-BF16", "TF32", "TF32x3"][args.gemm]}),
                    "seed": args.seed, "near_eta": args.eta, "near_depth": args.depth,
                    "refine_tol": 1e-8, "parallelism": f"replicas x{dist.world}",
                    "l2": "inputs larger than L2: A (%.0f MB c64) is rewritten every step" % (A_bytes / 1e6)},

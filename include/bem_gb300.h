@@ -190,7 +190,10 @@ typedef struct {
 
 enum { BEM_PREC_C64 = 0, BEM_PREC_C128 = 1 };
 enum { BEM_SOLVE_QR = 0, BEM_SOLVE_GMRES_REFINED = 1, BEM_SOLVE_BLOCK_GMRES = 2 };
-enum { BEM_GEMM_FP32 = 0, BEM_GEMM_SPLIT_BF16 = 1, BEM_GEMM_TF32 = 2 };
+/* Block-solve GEMMs: FP32 (SIMT), FP32-accurate split-BF16 emulation on the
+ * tensor cores (cuBLAS), plain TF32, or TF32x3 (A and the right-hand block
+ * split into TF32 head + tail, three TF32 GEMMs: hh + ht + th). */
+enum { BEM_GEMM_FP32 = 0, BEM_GEMM_SPLIT_BF16 = 1, BEM_GEMM_TF32 = 2, BEM_GEMM_TF32X3 = 3 };
 
 typedef struct {
     double density;     /* 1.2041 (numerical.cu:12) */
@@ -204,7 +207,7 @@ typedef struct {
     int max_refine;     /* refinement steps */
     int tile_cols;      /* far-field column tile width, 0 = automatic (<= 12288) */
     int far_variant;    /* far-field launch shape, -1 = autotuned per problem shape */
-    int gemm_mode;      /* block solve products: BEM_GEMM_SPLIT_BF16 (FP32-accurate on tensor cores), FP32, TF32 */
+    int gemm_mode;      /* block solve products: BEM_GEMM_* */
     double block_tol;   /* block solve: relative normal-equation residual per right-hand side */
 } bem_options_t;
 
