@@ -422,16 +422,16 @@ void cublas_ok(cublasStatus_t s, const char *what) {
 // TF32x3 mode Vt holds the heads and Vlo the tails of the right-hand block,
 // and Tt is split in place (Tlo) before the second product; each product is
 // head*tail + tail*head + head*head, smallest terms first.
-static void normal_gemms(bem_solver_s &sv, const float *Vt, const float *Vlo, float *Tt, float *Tlo, float *Wt,
-                         int S, bool first, bool second) {
+static void normal_gemms(bem_solver_s &sv, int mode, const float *Vt, const float *Vlo, float *Tt, float *Tlo,
+                         float *Wt, int S, bool first, bool second) {
     const float one = 1.f, zero = 0.f;
     const int N = sv.N, R = sv.R;
     const float *At = reinterpret_cast<const float *>(sv.d_A.p);
     const int ldat = (int)(2 * sv.lda);
-    const bool x3 = sv.opt.gemm_mode == BEM_GEMM_TF32X3;
-    const cublasComputeType_t ct = sv.opt.gemm_mode == BEM_GEMM_FP32         ? CUBLAS_COMPUTE_32F
-                                   : sv.opt.gemm_mode == BEM_GEMM_SPLIT_BF16 ? CUBLAS_COMPUTE_32F_EMULATED_16BFX9
-                                                                             : CUBLAS_COMPUTE_32F_FAST_TF32;
+    const bool x3 = mode == BEM_GEMM_TF32X3;
+    const cublasComputeType_t ct = mode == BEM_GEMM_FP32         ? CUBLAS_COMPUTE_32F
+                                   : mode == BEM_GEMM_SPLIT_BF16 ? CUBLAS_COMPUTE_32F_EMULATED_16BFX9
+                                                                 : CUBLAS_COMPUTE_32F_FAST_TF32;
     const float *Ahi = x3 ? sv.x_Ahi.as<float>() : At, *Alo = x3 ? sv.x_Alo.as<float>() : nullptr;
     auto gemm1 = [&](const float *a, const float *b, const float *beta) {
         cublas_ok(cublasGemmEx(sv.cublas, CUBLAS_OP_T, CUBLAS_OP_N, R, 2 * S, 2 * N, &one, a, CUDA_R_32F, ldat, b,
@@ -494,7 +494,8 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
     float2 *xh = w_gv.as<float2>(), *xl = xh + (size_t)ldx * S;
     float *Vt = w_vf.as<float>(), *Tt = w_t.as<float>(), *Wt = w_part.as<float>();
     const float2 *A = d_A.as<float2>();
-    const bool x3 = opt.gemm_mode == BEM_GEMM_TF32X3;
+    const int gmode = block_gemm_mode(opt, S);
+    const bool x3 = gmode == BEM_GEMM_TF32X3;
     float *Vlo = nullptr, *Tlo = nullptr;
     if (x3) {
         x_vlo.ensure(sizeof(float) * 4 * NS);
@@ -536,7 +537,7 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
                                                                  d_B.as<double2>(), Tt);
             count_launch(2);
         }
-        normal_gemms(*this, Vt, Vlo, Tt, Tlo, Wt, S, false, true);
+        normal_gemms(*this, gmode, Vt, Vlo, Tt, Tlo, Wt, S, false, true);
         combine_w_kernel<<<grid2(n, S), 256, 0, stream>>>(n, S, Wt, W);
         bnrm2_kernel<<<S, 256, 0, stream>>>(n, W, nrm_g);
         count_launch(2);
@@ -557,7 +558,7 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
             const float2 *Vj = V + (size_t)j * NS;
             build_vt_kernel<float2><<<grid2(n, S), 256, 0, stream>>>(n, S, Vj, Vt, Vlo);
             count_launch();
-            normal_gemms(*this, Vt, Vlo, Tt, Tlo, Wt, S, true, true);
+            normal_gemms(*this, gmode, Vt, Vlo, Tt, Tlo, Wt, S, true, true);
             const dim3 gd(S, (j + 1 + kDotLB - 1) / kDotLB);
             {
                 BEM_PROF("block_arnoldi", stream);

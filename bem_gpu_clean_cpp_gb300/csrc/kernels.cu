@@ -188,21 +188,30 @@ __device__ __forceinline__ bool pair_is_near(int row, int N, int4 nd, float4 xh,
 // three nodal integrals (N1 = xi1, N2 = xi2, N3 = 1 - xi1 - xi2).  The 1/(4 pi)
 // and |J| factors are applied once per pair by the caller.
 // ---------------------------------------------------------------------------
-// sin and cos of a phase x = kr >= 0 for the FP32 quadrature.  The fast
-// __sincosf is documented with a bounded error on [-pi, pi] only, and its
-// error grows with |x| outside (kr reaches ~30 at 8 kHz on a 0.11 m body), so
-// x is first reduced by 2 pi with the two-constant Cody-Waite scheme (Cody & Waite,
-// "Software Manual for the Elementary Functions", 1980) using FMAs:
-// n = rint(x / 2pi), y = (x - n C1) - n C2 with C1 = fl(2 pi), C2 = 2 pi - C1.
-// With the FMA each step rounds once, so y carries an absolute error of a few
-// ulps of y, independent of n.
-__device__ __forceinline__ void sincos_phase(float x, float *sn, float *cs) {
+// Phase reduction for the FP32 quadrature.  The fast __sincosf is documented
+// with a bounded error on [-pi, pi] only and its error grows with |x| outside
+// (kr reaches ~30 at 8 kHz on a 0.11 m body).  Over one element kr varies by
+// at most k * diam, so one multiple of 2 pi per pair, n = round(k r_c / 2 pi)
+// with r_c the distance to the centroid, brings every point's phase into
+// [-pi - k diam, pi + k diam]:  y = fma(k, r, -n C1) + (-n C2), the
+// two-constant Cody-Waite scheme (Cody & Waite, "Software Manual for the
+// Elementary Functions", 1980) with C1 = 2 pi cut to 16 significant bits (n C1
+// is exact for n < 256) and C2 = fl(2 pi - C1); the FMA rounds k r - n C1 once.
+// Per point this costs one FMA and one add; the per-pair constants are
+// (-n C1, -n C2).
+struct PhaseShift {
+    float c1, c2;
+};
+__device__ __forceinline__ PhaseShift phase_shift(float k, float3 d3, float3 e1, float3 e2) {
     constexpr float kInv2Pi = 0.15915493667125702f;
-    constexpr float k2PiHi = 6.2831854820251465f;
-    constexpr float k2PiLo = -1.7484555314695172e-07f;
-    const float n = rintf(x * kInv2Pi);
-    const float y = fmaf(-n, k2PiLo, fmaf(-n, k2PiHi, x));
-    __sincosf(y, sn, cs);
+    constexpr float kC1 = 6.2830810546875f;
+    constexpr float kC2 = 0.00010425248910905793f;
+    const float cx = d3.x + (e1.x + e2.x) * (1.0f / 3.0f);
+    const float cy = d3.y + (e1.y + e2.y) * (1.0f / 3.0f);
+    const float cz = d3.z + (e1.z + e2.z) * (1.0f / 3.0f);
+    const float rc = sqrtf(fmaf(cz, cz, fmaf(cy, cy, cx * cx)));
+    const float n = fminf(rintf(k * rc * kInv2Pi), 255.0f);
+    return PhaseShift{-n * kC1, -n * kC2};
 }
 
 struct SumsF {
@@ -213,6 +222,7 @@ struct SumsF {
 
 __device__ __forceinline__ void far_sums_f32(float3 d3, float3 e1, float3 e2, float hgt, float k,
                                              int nq, SumsF &S) {
+    const PhaseShift ps = phase_shift(k, d3, e1, e2);
     S.g0r = S.g0i = S.g1r = S.g1i = S.g2r = S.g2i = 0.0f;
     S.h0r = S.h0i = S.h1r = S.h1i = S.h2r = S.h2i = 0.0f;
     S.c = 0.0f;
@@ -226,7 +236,7 @@ __device__ __forceinline__ void far_sums_f32(float3 d3, float3 e1, float3 e2, fl
         float ri = rsqrtf(r2);
         float r = r2 * ri;
         float sn, cs;
-        sincos_phase(k * r, &sn, &cs);
+        __sincosf(fmaf(k, r, ps.c1) + ps.c2, &sn, &cs);
         float gr = cs * ri, gi = -sn * ri;            // 4 pi G
         float hq = hgt * ri;                          // dr/dn
         float tr = fmaf(gi, k, -gr * ri);             // 4 pi G (-1/r - ik)
@@ -267,6 +277,7 @@ __device__ __forceinline__ float gl6_w(int i) {
 
 __device__ __forceinline__ void far_sums_f32_o6(float3 d3, float3 e1, float3 e2, float hgt, float k,
                                                 SumsF &S) {
+    const PhaseShift ps = phase_shift(k, d3, e1, e2);
     S.g0r = S.g0i = S.g1r = S.g1i = S.g2r = S.g2i = 0.0f;
     S.h0r = S.h0i = S.h1r = S.h1i = S.h2r = S.h2i = 0.0f;
     S.c = 0.0f;
@@ -284,9 +295,10 @@ __device__ __forceinline__ void far_sums_f32_o6(float3 d3, float3 e1, float3 e2,
             const float dx = fmaf(rho, vx, d3.x), dy = fmaf(rho, vy, d3.y), dz = fmaf(rho, vz, d3.z);
             const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
             const float ri = rsqrtf(r2);
-            const float kr = k * (r2 * ri);
+            const float r = r2 * ri;
+            const float kr = k * r;
             float sn, cs;
-            sincos_phase(kr, &sn, &cs);
+            __sincosf(fmaf(k, r, ps.c1) + ps.c2, &sn, &cs);
             const float A = fmaf(kr, sn, cs);      // c + kr s
             const float Bv = fmaf(kr, cs, -sn);    // kr c - s
             const float ri3 = ri * ri * ri;
@@ -556,6 +568,24 @@ size_t far_smem_bytes(int prec, int tc, int variant) {
                                 : (size_t)tc * sizeof(double2);
 }
 
+// The dynamic shared-memory limit is an attribute of the kernel function,
+// shared by every thread and stream of the process: it is raised once to the
+// device's opt-in maximum (a launch still gets only the bytes it asks for),
+// never set per launch, so that concurrent solvers cannot lower it under one
+// another's launches.
+template <auto Kern>
+static void allow_max_smem() {
+    static std::once_flag once;   // one per kernel (the kernel is the template argument)
+    static cudaError_t err = cudaSuccess;
+    std::call_once(once, [&] {
+        int dev = 0, maxs = 0;
+        err = cudaGetDevice(&dev);
+        if (err == cudaSuccess) err = cudaDeviceGetAttribute(&maxs, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        if (err == cudaSuccess) err = cudaFuncSetAttribute(Kern, cudaFuncAttributeMaxDynamicSharedMemorySize, maxs);
+    });
+    CUDA_TRY(err);
+}
+
 bool far_variant_fits(int prec, int tc, int variant) {
     int dev = 0, maxs = 0;
     cudaGetDevice(&dev);
@@ -569,7 +599,8 @@ static void launch_far_f32(const RowPoints &rows, int N, const GeoTables &geo, c
                            size_t smem, cudaStream_t st) {
     const bool o6 = quadrature_points() == 36;
     auto kern = o6 ? far_assembly_f32<TR, NT, MINB, true> : far_assembly_f32<TR, NT, MINB, false>;
-    CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (o6) allow_max_smem<far_assembly_f32<TR, NT, MINB, true>>();
+    else allow_max_smem<far_assembly_f32<TR, NT, MINB, false>>();
     dim3 grid((rows.R + TR - 1) / TR, tiles.ntiles);
     kern<<<grid, NT, smem, st>>>(rows, N, geo, tiles, (float)ph.k, (float)ph.rw, (float2 *)A, lda,
                                  (float *)c_part, (float2 *)beta_part);
@@ -593,7 +624,7 @@ void launch_far_assembly(int prec, const RowPoints &rows, int N, const GeoTables
         }
     } else {
         auto kern = far_assembly_f64<kFarNT64>;
-        CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        allow_max_smem<far_assembly_f64<kFarNT64>>();
         dim3 grid(rows.R, tiles.ntiles);
         kern<<<grid, kFarNT64, smem, st>>>(rows, N, geo, tiles, ph.k, ph.rw, (double2 *)A, lda,
                                            (double *)c_part, (double2 *)beta_part);

@@ -113,4 +113,8 @@ struct bem_solver_s {
     void solve_qr();
     void solve_refined(bem_solve_info_t *info);
     void solve_block(bem_solve_info_t *info);
+    // GEMM mode of the block solve for S right-hand sides (resolves AUTO).
+    static int block_gemm_mode(const bem_options_t &o, int S) {
+        return o.gemm_mode >= 0 ? o.gemm_mode : (S >= 48 ? BEM_GEMM_TF32X3 : BEM_GEMM_SPLIT_BF16);
+    }
 };

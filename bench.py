@@ -64,8 +64,10 @@ def parse_args():
     ap.add_argument("--slots", type=int, default=8, help="freq/serve: requests in flight at once")
     ap.add_argument("--rate", type=float, default=2.0, help="serve: mean request arrivals per second")
     ap.add_argument("--requests", type=int, default=40, help="serve: requests in the stream")
-    ap.add_argument("--gemm", type=int, default=1, choices=[0, 1, 2, 3],
-                    help="block-solve GEMM mode (0 FP32, 1 split-BF16 FP32-accurate, 2 TF32, 3 TF32x3)")
+    ap.add_argument("--gemm", type=int, default=-1, choices=[-1, 0, 1, 2, 3],
+                    help="block-solve GEMM mode (-1 auto, 0 FP32, 1 split-BF16 FP32-accurate, 2 TF32, 3 TF32x3)")
+    ap.add_argument("--far-variant", type=int, default=-1,
+                    help="profile mode: fixed far-field launch shape (-1: autotuned)")
     ap.add_argument("--mode", default="bench", choices=["bench", "profile"],
                     help="profile: one warm-up solve and one more solve, nothing timed (for ncu captures)")
     return ap.parse_args()
@@ -76,10 +78,13 @@ def run_profile(args):
     (-k <kernel> -s/-c) sees the kernels of a steady-state solve."""
     import bem_gpu_clean_cpp_gb300 as bem
     pts, elems, chief, srcs, k, bc, _ = select_workload(args)
-    s = bem.Solver(near_eta=args.eta, near_depth=args.depth, tol=1e-8, inner_tol=1e-4, max_iter=300)
+    rhs = args.config == "rhs"
+    s = bem.Solver(near_eta=args.eta, near_depth=args.depth, tol=1e-8, inner_tol=1e-4,
+                   max_iter=100 if rhs else 300, max_refine=10, block_tol=1e-8, gemm_mode=args.gemm,
+                   far_variant=args.far_variant)
     s.set_geometry(pts, elems, bc=bc, chief=chief)
     s.set_sources(srcs)
-    method = bem.SOLVE_BLOCK_GMRES if args.config == "rhs" else bem.SOLVE_GMRES_REFINED
+    method = bem.SOLVE_BLOCK_GMRES if rhs else bem.SOLVE_GMRES_REFINED
     for _ in range(2):
         s.assemble(k, bem.PREC_C64)
         info = s.solve(method)
@@ -598,7 +603,8 @@ def run_ours(args):
         "config": {"workload": name, "sources": S, "nodes": N, "triangles": E, "chief": M,
                    **({"subdiv": args.subdiv, "ka": args.ka} if args.config == "precision" else
                       {"k": k, "solver": "block GMRES: %s GEMMs, FP32 Arnoldi, FP64 Givens, FP64-accurate "
-                                          "refinement residual to 1e-8" % ["FP32", "split-BF16", "TF32", "TF32x3"][args.gemm]}),
+                                          "refinement residual to 1e-8" % {-1: "auto (TF32x3 from 48 sources)", 0: "FP32",
+                                                            1: "split-BF16", 2: "TF32", 3: "TF32x3"}[args.gemm]}),
                    "seed": args.seed, "near_eta": args.eta, "near_depth": args.depth,
                    "refine_tol": 1e-8, "parallelism": f"replicas x{dist.world}",
                    "l2": "inputs larger than L2: A (%.0f MB c64) is rewritten every step" % (A_bytes / 1e6)},
@@ -735,6 +741,18 @@ def run_server_bench(args):
             "note": "plain FP64 = c128 assembly + Householder QR per problem, timed for every problem up to "
                     "10242 nodes (one at 10242), 40962-node problems extrapolated by N^3 from 10242"}
     sizes = sorted({p["pnts"].shape[0] for p in probs})
+    by_sub = {}
+    for p, (_, r) in zip(probs, last):
+        d = by_sub.setdefault(str(p["subdiv"]), {"requests": 0, "nodes": p["pnts"].shape[0], "solves": 0,
+                                                  "service_ms": 0.0, "iterations": 0, "max_latency_ms": 0.0})
+        d["requests"] += 1
+        d["solves"] += len(p["srcs"])
+        d["service_ms"] += r["service_ms"]
+        d["iterations"] += r["iterations"]
+        d["max_latency_ms"] = max(d["max_latency_ms"], r["latency_ms"])
+    for d in by_sub.values():
+        d["mean_service_ms"] = d.pop("service_ms") / d["requests"]
+        d["mean_iterations"] = d.pop("iterations") / d["requests"]
     h2d = sum(24 * p["pnts"].shape[0] + 12 * p["elems"].shape[0] + 24 * 16 + 48 * len(p["srcs"]) for p in probs)
     d2h = sum(16 * p["pnts"].shape[0] * len(p["srcs"]) for p in probs)
     line = {
@@ -748,6 +766,7 @@ def run_server_bench(args):
         "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                        "max": float(max(lat))},
         "server": stats[-1],
+        "per_subdivision": by_sub,
         "fp64_plain": fp64,
         "gpu_launches": launches,
         "clocks": clk,
