@@ -16,11 +16,15 @@
 // so its basis is stored and orthogonalised in FP32 (classical Gram-Schmidt
 // twice); the Hessenberg matrix, Givens rotations, back substitution and the
 // solution X are FP64.  Accuracy comes from the outer refinement: the
-// residual R = B - A X, where all the cancellation happens, is computed
-// FP64-accurately with double-float arithmetic on the FP32 pipe (8 sources
-// per pass over A); G = A^H R, whose inputs are already small, uses the
-// second GEMM.  On GB300 the FP64 pipe runs at about 1/64 of FP32, so FP64
-// Arnoldi over 256 Krylov spaces would cost more than the GEMMs themselves.
+// residual R = B - A X, where all the cancellation happens, is kept in FP64.
+// After the first inner cycle it is computed FP64-accurately from X with
+// double-float arithmetic on the FP32 pipe (8 sources per pass over A); after
+// every later cycle it is updated with that cycle's correction D, R -= A D,
+// by the first GEMM (|A D| has already shrunk by inner_tol, so the GEMM's
+// FP32-level error stays below the FP64 level of R).  G = A^H R, whose input
+// is already small, uses the second GEMM.  On GB300 the FP64 pipe runs at
+// about 1/64 of FP32, so FP64 Arnoldi over 256 Krylov spaces would cost more
+// than the GEMMs themselves.
 #include <cublas_v2.h>
 #include <cuda_runtime.h>
 
@@ -102,13 +106,30 @@ __global__ void split_a_tf32_kernel(int R, int N2, size_t ld, const float *__res
     }
 }
 
-// Tt (R x 2S, real and imaginary column blocks) = B.
-__global__ void pack_b_kernel(int R, int S, const double2 *__restrict__ B, float *__restrict__ Tt) {
+// Rv = B (the residual of X = 0) and its float packing Tt (R x 2S, real and
+// imaginary column blocks).
+__global__ void pack_b_kernel(int R, int S, const double2 *__restrict__ B, double2 *__restrict__ Rv,
+                              float *__restrict__ Tt) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x, s = blockIdx.y;
     if (r >= R) return;
     const double2 b = B[(size_t)s * R + r];
+    Rv[(size_t)s * R + r] = b;
     Tt[(size_t)s * R + r] = (float)b.x;
     Tt[(size_t)(S + s) * R + r] = (float)b.y;
+}
+
+// Residual update Rv -= A D with A D given packed in Tt (from the first
+// GEMM), then Tt = float(Rv) for the A^H R GEMM.  Each thread reads and
+// writes only its own elements of Tt.
+__global__ void resid_update_kernel(int R, int S, double2 *__restrict__ Rv, float *Tt) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x, s = blockIdx.y;
+    if (r >= R) return;
+    const size_t ir = (size_t)s * R + r, ii = (size_t)(S + s) * R + r;
+    const double2 v = Rv[ir];
+    const double2 u = make_double2(v.x - (double)Tt[ir], v.y - (double)Tt[ii]);
+    Rv[ir] = u;
+    Tt[ir] = (float)u.x;
+    Tt[ii] = (float)u.y;
 }
 
 // Head/tail float split of X (N x S, ld N) into xh/xl (ld ldx, even).
@@ -131,7 +152,7 @@ __global__ void split_x_kernel(int N, int ldx, const double2 *__restrict__ X, fl
 __global__ void __launch_bounds__(32 * kResWarps)
 resid_df_multi_kernel(int R, int N, int S, const float2 *__restrict__ A, size_t lda,
                       const float2 *__restrict__ xh, const float2 *__restrict__ xl, int ldx,
-                      const double2 *__restrict__ B, float *__restrict__ Tt) {
+                      const double2 *__restrict__ B, double2 *__restrict__ Rv, float *__restrict__ Tt) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int row0 = (blockIdx.x * kResWarps + warp) * kResRPW;
     const int s0 = blockIdx.y * kResSB;
@@ -199,8 +220,10 @@ resid_df_multi_kernel(int R, int N, int S, const float2 *__restrict__ A, size_t 
             if (lane == 0 && q < ns && p < nr) {
                 const int s = s0 + q, row = row0 + p;
                 const double2 b = B[(size_t)s * R + row];
-                Tt[(size_t)s * R + row] = (float)(b.x - sr);
-                Tt[(size_t)(S + s) * R + row] = (float)(b.y - si);
+                const double2 r = make_double2(b.x - sr, b.y - si);
+                Rv[(size_t)s * R + row] = r;
+                Tt[(size_t)s * R + row] = (float)r.x;
+                Tt[(size_t)(S + s) * R + row] = (float)r.y;
             }
         }
     }
@@ -284,10 +307,10 @@ bcombo_kernel(int N, int S, int k, const float2 *__restrict__ V, const double2 *
     W[(size_t)s * N + i] = make_float2(w.x - sr, w.y - si);
 }
 
-// X(:,s) += sum_{l<kk[s]} V_l(:,s) y[s][l]  (FP64 accumulation).
+// D(:,s) = sum_{l<kk[s]} V_l(:,s) y[s][l] (FP64 accumulation); X += D.
 __global__ void __launch_bounds__(256)
 bupdate_x_kernel(int N, int S, const int *__restrict__ kk, const float2 *__restrict__ V,
-                 const double2 *__restrict__ y, int ldv, double2 *__restrict__ X) {
+                 const double2 *__restrict__ y, int ldv, double2 *__restrict__ X, double2 *__restrict__ D) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, s = blockIdx.y;
     if (i >= N) return;
     const int k = kk[s];
@@ -301,6 +324,7 @@ bupdate_x_kernel(int N, int S, const int *__restrict__ kk, const float2 *__restr
     }
     const double2 x = X[(size_t)s * N + i];
     X[(size_t)s * N + i] = make_double2(x.x + sr, x.y + si);
+    D[(size_t)s * N + i] = make_double2(sr, si);
 }
 
 __global__ void __launch_bounds__(256) bnrm2_kernel(int N, const float2 *__restrict__ W, double *__restrict__ out) {
@@ -483,6 +507,8 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
     w_h2.ensure(sizeof(double2) * (size_t)S * ldv);
     w_w.ensure(sizeof(float2) * NS);                       // W and the gradient G
     w_gv.ensure(sizeof(float2) * 2 * (size_t)ldx * S);     // head/tail split of X
+    w_r.ensure(sizeof(double2) * (size_t)R * S);           // residual R (FP64)
+    w_d.ensure(sizeof(double2) * NS);                      // correction D of the last cycle
     w_vf.ensure(sizeof(float) * 4 * NS);                   // Vt (2N x 2S)
     w_t.ensure(sizeof(float) * 2 * (size_t)R * S);         // Tt (R x 2S)
     w_part.ensure(sizeof(float) * 4 * NS);                 // Wt (2N x 2S)
@@ -490,7 +516,7 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
     double *nrm_b = w_scal.as<double>(), *nrm_g = nrm_b + S, *res = nrm_b + 2 * S, *nrm_w = nrm_b + 3 * S;
     int *kk = reinterpret_cast<int *>(nrm_b + 4 * S);
     float2 *V = w_V.as<float2>(), *W = w_w.as<float2>();
-    double2 *X = d_x.as<double2>();
+    double2 *X = d_x.as<double2>(), *Rv = w_r.as<double2>(), *Dc = w_d.as<double2>();
     float2 *xh = w_gv.as<float2>(), *xl = xh + (size_t)ldx * S;
     float *Vt = w_vf.as<float>(), *Tt = w_t.as<float>(), *Wt = w_part.as<float>();
     const float2 *A = d_A.as<float2>();
@@ -524,18 +550,28 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
     double worst = 0.0;
     bool conv = false;
     for (;; refs++) {
-        // R = B - A X (FP64-accurate), then G = A^H R
+        // The residual R = B - A X, then G = A^H R.  After the first inner
+        // cycle R is formed FP64-accurately (double float) from X; after each
+        // later cycle it is updated, R -= A D, with the correction D of that
+        // cycle: |A D| is already down by inner_tol per cycle, so the GEMM's
+        // FP32-level error in A D stays below the FP64 level of R.
         if (refs == 0) {
-            pack_b_kernel<<<grid2(R, S), 256, 0, stream>>>(R, S, d_B.as<double2>(), Tt);
+            pack_b_kernel<<<grid2(R, S), 256, 0, stream>>>(R, S, d_B.as<double2>(), Rv, Tt);
             count_launch();
-        } else {
+        } else if (refs == 1) {
             BEM_PROF("resid_df_multi", stream);
             split_x_kernel<<<grid2(n, S), 256, 0, stream>>>(n, ldx, X, xh, xl);
             resid_df_multi_kernel<<<dim3((R + kResWarps * kResRPW - 1) / (kResWarps * kResRPW),
                                          (S + kResSB - 1) / kResSB),
                                     32 * kResWarps, 0, stream>>>(R, n, S, A, lda, xh, xl, ldx,
-                                                                 d_B.as<double2>(), Tt);
+                                                                 d_B.as<double2>(), Rv, Tt);
             count_launch(2);
+        } else {
+            build_vt_kernel<double2><<<grid2(n, S), 256, 0, stream>>>(n, S, Dc, Vt, Vlo);
+            count_launch();
+            normal_gemms(*this, gmode, Vt, Vlo, Tt, Tlo, Wt, S, true, false);
+            resid_update_kernel<<<grid2(R, S), 256, 0, stream>>>(R, S, Rv, Tt);
+            count_launch();
         }
         normal_gemms(*this, gmode, Vt, Vlo, Tt, Tlo, Wt, S, false, true);
         combine_w_kernel<<<grid2(n, S), 256, 0, stream>>>(n, S, Wt, W);
@@ -588,7 +624,7 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
         total_it += j;
         CUDA_TRY(cudaMemcpyAsync(kk, h_kk.data(), sizeof(int) * S, cudaMemcpyHostToDevice, stream));
         btrisolve_kernel<<<sb, 128, 0, stream>>>(S, m, kk, w_H.as<double2>(), w_g.as<double2>(), w_y.as<double2>(), ldv);
-        bupdate_x_kernel<<<grid2(n, S), 256, 0, stream>>>(n, S, kk, V, w_y.as<double2>(), ldv, X);
+        bupdate_x_kernel<<<grid2(n, S), 256, 0, stream>>>(n, S, kk, V, w_y.as<double2>(), ldv, X, Dc);
         count_launch(2);
         KERNEL_CHECK();
     }

@@ -570,7 +570,8 @@ size_t far_smem_bytes(int prec, int tc, int variant) {
 
 // The dynamic shared-memory limit is an attribute of the kernel function,
 // shared by every thread and stream of the process: it is raised once to the
-// device's opt-in maximum (a launch still gets only the bytes it asks for),
+// device's opt-in maximum less the kernel's static shared memory (a launch
+// still gets only the bytes it asks for),
 // never set per launch, so that concurrent solvers cannot lower it under one
 // another's launches.
 template <auto Kern>
@@ -581,7 +582,11 @@ static void allow_max_smem() {
         int dev = 0, maxs = 0;
         err = cudaGetDevice(&dev);
         if (err == cudaSuccess) err = cudaDeviceGetAttribute(&maxs, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        if (err == cudaSuccess) err = cudaFuncSetAttribute(Kern, cudaFuncAttributeMaxDynamicSharedMemorySize, maxs);
+        cudaFuncAttributes fa{};
+        if (err == cudaSuccess) err = cudaFuncGetAttributes(&fa, Kern);   // static shared memory counts too
+        if (err == cudaSuccess)
+            err = cudaFuncSetAttribute(Kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       maxs - (int)fa.sharedSizeBytes);
     });
     CUDA_TRY(err);
 }
