@@ -198,7 +198,10 @@ __device__ __forceinline__ bool pair_is_near(int row, int N, int4 nd, float4 xh,
 // Elementary Functions", 1980) with C1 = 2 pi cut to 16 significant bits (n C1
 // is exact for n < 256) and C2 = fl(2 pi - C1); the FMA rounds k r - n C1 once.
 // Per point this costs one FMA and one add; the per-pair constants are
-// (-n C1, -n C2).
+// (-n C1, -n C2).  When an element spans a large phase (k * longest edge above
+// kWrapKh, coarse meshes at high frequency) the point's own multiple of 2 pi
+// is removed as well (WRAP: three more FMA-pipe instructions per point).
+constexpr double kWrapKh = 0.75;
 struct PhaseShift {
     float c1, c2;
 };
@@ -214,12 +217,25 @@ __device__ __forceinline__ PhaseShift phase_shift(float k, float3 d3, float3 e1,
     return PhaseShift{-n * kC1, -n * kC2};
 }
 
+template <bool WRAP>
+__device__ __forceinline__ float phase_arg(float k, float r, const PhaseShift &ps) {
+    float y = fmaf(k, r, ps.c1) + ps.c2;
+    if (WRAP) {
+        constexpr float kInv2Pi = 0.15915493667125702f, kRound = 12582912.0f;
+        constexpr float kC1 = 6.2830810546875f, kC2 = 0.00010425248910905793f;
+        const float n = __fsub_rn(__fmaf_rn(y, kInv2Pi, kRound), kRound);
+        y = __fmaf_rn(-n, kC2, __fmaf_rn(-n, kC1, y));
+    }
+    return y;
+}
+
 struct SumsF {
     float g0r, g0i, g1r, g1i, g2r, g2i;   // G sums
     float h0r, h0i, h1r, h1i, h2r, h2i;   // dG/dn sums
     float c;                              // dG0/dn sum
 };
 
+template <bool WRAP>
 __device__ __forceinline__ void far_sums_f32(float3 d3, float3 e1, float3 e2, float hgt, float k,
                                              int nq, SumsF &S) {
     const PhaseShift ps = phase_shift(k, d3, e1, e2);
@@ -236,7 +252,7 @@ __device__ __forceinline__ void far_sums_f32(float3 d3, float3 e1, float3 e2, fl
         float ri = rsqrtf(r2);
         float r = r2 * ri;
         float sn, cs;
-        __sincosf(fmaf(k, r, ps.c1) + ps.c2, &sn, &cs);
+        __sincosf(phase_arg<WRAP>(k, r, ps), &sn, &cs);
         float gr = cs * ri, gi = -sn * ri;            // 4 pi G
         float hq = hgt * ri;                          // dr/dn
         float tr = fmaf(gi, k, -gr * ri);             // 4 pi G (-1/r - ik)
@@ -275,6 +291,7 @@ __device__ __forceinline__ float gl6_w(int i) {
                                                                            : 0.4679139345726910f;
 }
 
+template <bool WRAP>
 __device__ __forceinline__ void far_sums_f32_o6(float3 d3, float3 e1, float3 e2, float hgt, float k,
                                                 SumsF &S) {
     const PhaseShift ps = phase_shift(k, d3, e1, e2);
@@ -298,7 +315,7 @@ __device__ __forceinline__ void far_sums_f32_o6(float3 d3, float3 e1, float3 e2,
             const float r = r2 * ri;
             const float kr = k * r;
             float sn, cs;
-            __sincosf(fmaf(k, r, ps.c1) + ps.c2, &sn, &cs);
+            __sincosf(phase_arg<WRAP>(k, r, ps), &sn, &cs);
             const float A = fmaf(kr, sn, cs);      // c + kr s
             const float Bv = fmaf(kr, cs, -sn);    // kr c - s
             const float ri3 = ri * ri * ri;
@@ -400,7 +417,7 @@ __device__ __forceinline__ void finish_coeffs(const SUMS &S, T scale, T rw, T bA
 // Far-field assembly kernel.
 // grid = (ceil(R/TR), ntiles), block = NT threads, dynamic smem = acc[TR][tc].
 // ---------------------------------------------------------------------------
-template <int TR, int NT, int MINB, bool O6>
+template <int TR, int NT, int MINB, bool O6, bool WRAP>
 __global__ void __launch_bounds__(NT, MINB)
 far_assembly_f32(RowPoints rows, int N, GeoTables geo, TileSet tiles, float k, float rw,
                  float2 *__restrict__ A, size_t lda, float *__restrict__ c_part,
@@ -439,8 +456,8 @@ far_assembly_f32(RowPoints rows, int N, GeoTables geo, TileSet tiles, float k, f
                                           (g0.z - xh.z) + (g1.z - xl.z));
             const float hgt = d3.x * g4.x + d3.y * g4.y + d3.z * g4.z;
             SumsF S;
-            if (O6) far_sums_f32_o6(d3, e1, e2, hgt, k, S);
-            else far_sums_f32(d3, e1, e2, hgt, k, nq, S);
+            if (O6) far_sums_f32_o6<WRAP>(d3, e1, e2, hgt, k, S);
+            else far_sums_f32<WRAP>(d3, e1, e2, hgt, k, nq, S);
             Coeffs<float, SumsF> o;
             finish_coeffs<float, SumsF>(S, g0.w * inv4pi, rw, g5.x, g5.y, g5.z, g5.w, o);
 #pragma unroll
@@ -603,9 +620,13 @@ static void launch_far_f32(const RowPoints &rows, int N, const GeoTables &geo, c
                            const Physics &ph, void *A, size_t lda, void *c_part, void *beta_part,
                            size_t smem, cudaStream_t st) {
     const bool o6 = quadrature_points() == 36;
-    auto kern = o6 ? far_assembly_f32<TR, NT, MINB, true> : far_assembly_f32<TR, NT, MINB, false>;
-    if (o6) allow_max_smem<far_assembly_f32<TR, NT, MINB, true>>();
-    else allow_max_smem<far_assembly_f32<TR, NT, MINB, false>>();
+    const bool wrap = ph.k * ph.max_edge > kWrapKh;
+    auto kern = o6 ? (wrap ? far_assembly_f32<TR, NT, MINB, true, true> : far_assembly_f32<TR, NT, MINB, true, false>)
+                   : (wrap ? far_assembly_f32<TR, NT, MINB, false, true> : far_assembly_f32<TR, NT, MINB, false, false>);
+    if (o6 && wrap) allow_max_smem<far_assembly_f32<TR, NT, MINB, true, true>>();
+    else if (o6) allow_max_smem<far_assembly_f32<TR, NT, MINB, true, false>>();
+    else if (wrap) allow_max_smem<far_assembly_f32<TR, NT, MINB, false, true>>();
+    else allow_max_smem<far_assembly_f32<TR, NT, MINB, false, false>>();
     dim3 grid((rows.R + TR - 1) / TR, tiles.ntiles);
     kern<<<grid, NT, smem, st>>>(rows, N, geo, tiles, (float)ph.k, (float)ph.rw, (float2 *)A, lda,
                                  (float *)c_part, (float2 *)beta_part);
@@ -794,28 +815,27 @@ __global__ void __launch_bounds__(32 * kNearWarps)
 near_assembly_kernel(RowPoints rows, int N, GeoTables geo, Physics ph, int nq, TA *__restrict__ A,
                      size_t lda, const TP *__restrict__ c_part, const TP2 *__restrict__ beta_part,
                      int ntiles, const DevSource *__restrict__ srcs, int S, double2 *__restrict__ B,
-                     double2 *__restrict__ beta_out) {
+                     double2 *__restrict__ beta_out, const int *__restrict__ near_ptr,
+                     const int *__restrict__ near_ids) {
     __shared__ Leaf leaves_all[kNearWarps][kMaxLeaves];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int row = blockIdx.x * kNearWarps + warp;
     if (row >= rows.R) return;
     Leaf *leaves = leaves_all[warp];
-    const float4 xh = rows.f[2 * (size_t)row];
     const double x[3] = {rows.d[3 * (size_t)row], rows.d[3 * (size_t)row + 1], rows.d[3 * (size_t)row + 2]};
     double cn = 0.0, bnr = 0.0, bni = 0.0;
-    for (int e0 = 0; e0 < geo.E; e0 += 32) {
-        const int e = e0 + lane;
-        bool flag = false;
+    // The row's near elements, in increasing element order (near_list_kernel).
+    const int pe = near_ptr[row + 1];
+    for (int p0 = near_ptr[row]; p0 < pe; p0 += 32) {
+        const int cnt = min(32, pe - p0);
+        int ebl = 0;
         int4 nd = make_int4(-1, -1, -1, 0);
-        if (e < geo.E) {
-            nd = geo.elems[e];
-            flag = pair_is_near(row, N, nd, xh, geo.geo_f + (size_t)kGeoF * e);
+        if (lane < cnt) {
+            ebl = near_ids[p0 + lane];
+            nd = geo.elems[ebl];
         }
-        unsigned mask = __ballot_sync(0xffffffffu, flag);
-        while (mask) {
-            const int b = __ffs(mask) - 1;
-            mask &= mask - 1;
-            const int eb = e0 + b;
+        for (int b = 0; b < cnt; b++) {
+            const int eb = __shfl_sync(0xffffffffu, ebl, b);
             const int4 ndb = make_int4(__shfl_sync(0xffffffffu, nd.x, b), __shfl_sync(0xffffffffu, nd.y, b),
                                        __shfl_sync(0xffffffffu, nd.z, b), 0);
             const double *h = geo.geo_d + (size_t)kGeoD * eb;
@@ -892,10 +912,41 @@ void launch_rhs_from_beta(const RowPoints &rows, double k, const DevSource *srcs
     KERNEL_CHECK();
 }
 
+// Near pairs of every row (the pairs pair_is_near flags, which the far kernel
+// skips): count pass (ids == nullptr: cnt[row]) and fill pass (ids[ptr[row]..]
+// in increasing element order).  One warp per row, ballot over 32 elements.
+__global__ void near_list_kernel(RowPoints rows, int N, GeoTables geo, const int *__restrict__ ptr,
+                                 int *__restrict__ cnt, int *__restrict__ ids) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int row = blockIdx.x * kNearWarps + warp;
+    if (row >= rows.R) return;
+    const float4 xh = rows.f[2 * (size_t)row];
+    int n = 0;
+    for (int e0 = 0; e0 < geo.E; e0 += 32) {
+        const int e = e0 + lane;
+        bool flag = false;
+        if (e < geo.E) flag = pair_is_near(row, N, geo.elems[e], xh, geo.geo_f + (size_t)kGeoF * e);
+        const unsigned mask = __ballot_sync(0xffffffffu, flag);
+        if (ids && flag) ids[ptr[row] + n + __popc(mask & ((1u << lane) - 1u))] = e;
+        n += __popc(mask);
+    }
+    if (!ids && lane == 0) cnt[row] = n;
+}
+
+void launch_near_list(const RowPoints &rows, int N, const GeoTables &geo, const int *d_ptr, int *d_cnt,
+                      int *d_ids, cudaStream_t st) {
+    if (rows.R <= 0) return;
+    const dim3 grid((rows.R + kNearWarps - 1) / kNearWarps);
+    near_list_kernel<<<grid, 32 * kNearWarps, 0, st>>>(rows, N, geo, d_ptr, d_cnt, d_ids);
+    count_launch();
+    KERNEL_CHECK();
+}
+
 void launch_near_assembly(int prec, const RowPoints &rows, int N, const GeoTables &geo,
                           const Physics &ph, void *A, size_t lda, const void *c_part,
                           const void *beta_part, int ntiles, const DevSource *srcs, int S,
-                          double2 *B, double2 *beta_out, cudaStream_t st) {
+                          double2 *B, double2 *beta_out, const int *near_ptr, const int *near_ids,
+                          cudaStream_t st) {
     BEM_PROF("near_assembly_f64", st);
     if (rows.R <= 0) return;
     BEM_CHECK_ARG(ph.near_depth >= 0 && ph.near_depth <= kMaxDepth, "near_depth must be in [0, 4]");
@@ -904,11 +955,11 @@ void launch_near_assembly(int prec, const RowPoints &rows, int N, const GeoTable
     if (prec == BEM_PREC_C64) {
         near_assembly_kernel<float2, float, float2><<<grid, 32 * kNearWarps, 0, st>>>(
             rows, N, geo, ph, nq, (float2 *)A, lda, (const float *)c_part,
-            (const float2 *)beta_part, ntiles, srcs, S, B, beta_out);
+            (const float2 *)beta_part, ntiles, srcs, S, B, beta_out, near_ptr, near_ids);
     } else {
         near_assembly_kernel<double2, double, double2><<<grid, 32 * kNearWarps, 0, st>>>(
             rows, N, geo, ph, nq, (double2 *)A, lda, (const double *)c_part,
-            (const double2 *)beta_part, ntiles, srcs, S, B, beta_out);
+            (const double2 *)beta_part, ntiles, srcs, S, B, beta_out, near_ptr, near_ids);
     }
     count_launch();
     KERNEL_CHECK();
@@ -951,8 +1002,8 @@ field_far_kernel(RowPoints pts, GeoTables geo, T k, T rw, int nq,
                                     (g0.z - xh.z) + (g1.z - xl.z));
             float hgt = d3.x * g4.x + d3.y * g4.y + d3.z * g4.z;
             SumsF Sm;
-            far_sums_f32(d3, make_float3(g2.x, g2.y, g2.z), make_float3(g3.x, g3.y, g3.z), hgt,
-                         (float)k, nq, Sm);
+            far_sums_f32<true>(d3, make_float3(g2.x, g2.y, g2.z), make_float3(g3.x, g3.y, g3.z), hgt,
+                               (float)k, nq, Sm);
             Coeffs<float, SumsF> oo;
             finish_coeffs<float, SumsF>(Sm, g0.w * (float)(1.0 / (4.0 * kPi)), (float)rw, g5.x, g5.y,
                                         g5.z, g5.w, oo);

@@ -42,6 +42,7 @@ struct Physics {
     double rw;                // density * omega = density * k * speed
     int near_depth;
     double near_eta;
+    double max_edge = 0.0;    // longest element edge (selects the per-point phase wrap)
 };
 
 // Upload the Gauss rule of the given order to this device's constant memory
@@ -73,10 +74,19 @@ void launch_far_assembly(int prec, const RowPoints &rows, int N, const GeoTables
 // B[s*R + row] = p_inc_s(x) - beta (c128, column-major R x S).  beta, the
 // source-independent row term sum_e (cc/cb) sum_j g_j, is also stored in
 // beta_out[row] when beta_out is not null.
+// The near elements of each row are listed in CSR form (near_ptr: R + 1
+// offsets, near_ids: element ids in increasing order), built once per
+// geometry and near_eta by launch_near_list.
 void launch_near_assembly(int prec, const RowPoints &rows, int N, const GeoTables &geo,
                           const Physics &ph, void *A, size_t lda, const void *c_part,
                           const void *beta_part, int ntiles, const DevSource *srcs, int S,
-                          double2 *B, double2 *beta_out, cudaStream_t st);
+                          double2 *B, double2 *beta_out, const int *near_ptr, const int *near_ids,
+                          cudaStream_t st);
+// The pairs the far kernel skips (pair_is_near): with d_ids null, d_cnt[row]
+// = number of near elements of the row; else the ids are written at
+// d_ids[d_ptr[row]..].
+void launch_near_list(const RowPoints &rows, int N, const GeoTables &geo, const int *d_ptr, int *d_cnt,
+                      int *d_ids, cudaStream_t st);
 // B[s*R + row] = p_inc_s(x_row) - beta[row]: the right-hand sides of an
 // assembled system for a new set of sources (no element integrals).
 void launch_rhs_from_beta(const RowPoints &rows, double k, const DevSource *srcs, int S,

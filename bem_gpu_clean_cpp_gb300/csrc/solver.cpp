@@ -121,6 +121,14 @@ void bem_solver_s::set_geometry(const double *pnts, int num_pnts, const int *ele
     R = N + M;
     h_nodes.assign(pnts, pnts + 3 * (size_t)N);
     h_elems.assign(elems, elems + 3 * (size_t)E);
+    max_edge = 0.0;
+    for (int e = 0; e < E; e++)
+        for (int a = 0; a < 3; a++) {
+            const double *p = &h_nodes[3 * (size_t)h_elems[3 * e + a]];
+            const double *q = &h_nodes[3 * (size_t)h_elems[3 * e + (a + 1) % 3]];
+            max_edge = std::max(max_edge, std::sqrt((p[0] - q[0]) * (p[0] - q[0]) + (p[1] - q[1]) * (p[1] - q[1]) +
+                                                    (p[2] - q[2]) * (p[2] - q[2])));
+        }
     h_bc.resize(6 * (size_t)E);
     if (bc) {
         std::memcpy(h_bc.data(), bc, sizeof(double) * 6 * (size_t)E);
@@ -187,6 +195,29 @@ void bem_solver_s::ensure_geo() {
     launch_elem_setup(d_nodes.as<double>(), d_elems.as<int4>(), d_bc.as<double>(), E, opt.near_eta,
                       d_geo_f.as<float4>(), d_geo_d.as<double>(), stream);
     geo_eta = opt.near_eta;
+    near_valid = false;
+}
+
+// The near-pair list depends on the geometry and near_eta only, so every
+// assembly of one geometry (any wavenumber, any sources) reuses it.
+void bem_solver_s::ensure_near_list() {
+    ensure_geo();
+    if (near_valid) return;
+    d_near_ptr.ensure(sizeof(int) * ((size_t)R + 1));
+    launch_near_list(row_points(), N, geo_tables(), nullptr, d_near_ptr.as<int>(), nullptr, stream);
+    std::vector<int> cnt(R);
+    CUDA_TRY(cudaMemcpyAsync(cnt.data(), d_near_ptr.p, sizeof(int) * R, cudaMemcpyDeviceToHost, stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    std::vector<int> ptr(R + 1, 0);
+    for (int r = 0; r < R; r++) {
+        if (ptr[r] > 0x7fffffff - cnt[r]) BEM_FAIL(BEM_ERR_TOO_LARGE, "too many near pairs");
+        ptr[r + 1] = ptr[r] + cnt[r];
+    }
+    CUDA_TRY(cudaMemcpyAsync(d_near_ptr.p, ptr.data(), sizeof(int) * (R + 1), cudaMemcpyHostToDevice, stream));
+    d_near_ids.ensure(sizeof(int) * std::max(1, ptr[R]));
+    launch_near_list(row_points(), N, geo_tables(), d_near_ptr.as<int>(), nullptr, d_near_ids.as<int>(), stream);
+    CUDA_TRY(cudaStreamSynchronize(stream));   // ptr (host) must outlive the copy
+    near_valid = true;
 }
 
 // Column tiles of the far-field kernel.  When N fits one tile the columns
@@ -274,7 +305,7 @@ GeoTables bem_solver_s::geo_tables() const {
 RowPoints bem_solver_s::row_points() const { return RowPoints{d_rows_f.as<float4>(), d_rows_d.as<double>(), R}; }
 
 Physics bem_solver_s::physics() const {
-    return Physics{k, opt.density * k * opt.speed, opt.near_depth, opt.near_eta};
+    return Physics{k, opt.density * k * opt.speed, opt.near_depth, opt.near_eta, max_edge};
 }
 
 void bem_solver_s::assemble(double kk, int precision) {
@@ -339,8 +370,10 @@ void bem_solver_s::assemble(double kk, int precision) {
                             stream, variant);
     far_variant_used = variant;
     d_beta.ensure(sizeof(double2) * (size_t)R);
+    ensure_near_list();
     launch_near_assembly(precision, row_points(), N, geo_tables(), ph, d_A.p, lda, d_cpart.p, d_bpart.p,
-                         T.ntiles, d_srcs.as<DevSource>(), S, d_B.as<double2>(), d_beta.as<double2>(), stream);
+                         T.ntiles, d_srcs.as<DevSource>(), S, d_B.as<double2>(), d_beta.as<double2>(),
+                         d_near_ptr.as<int>(), d_near_ids.as<int>(), stream);
     assembled = true;
     solved = false;
     tf32_split_valid = false;
@@ -418,7 +451,7 @@ size_t bem_solver_s::device_bytes() const {
     const DevMem *all[] = {&d_nodes, &d_rows_f, &d_rows_d, &d_elems, &d_bc, &d_geo_f, &d_geo_d, &d_srcs,
                            &tiles[0].recs, &tiles[0].rec_ptr, &tiles[0].cols, &tiles[0].col_cnt,
                            &tiles[1].recs, &tiles[1].rec_ptr, &tiles[1].cols, &tiles[1].col_cnt,
-                           &d_A, &d_B, &d_cpart, &d_bpart, &d_x, &d_beta,
+                           &d_A, &d_B, &d_cpart, &d_bpart, &d_x, &d_beta, &d_near_ptr, &d_near_ids,
                            &w_V, &w_H, &w_cs, &w_sn, &w_g, &w_y, &w_h1, &w_h2, &w_w, &w_t, &w_r, &w_gv, &w_vf,
                            &w_part, &w_scal, &x_Ahi, &x_Alo, &x_vlo, &x_tlo, &w_d, &q_A, &q_B, &q_tau, &q_work, &q_info,
                            &f_rows_f, &f_rows_d, &f_part, &f_near, &f_out, &f_u};
@@ -435,6 +468,7 @@ size_t bem_solver_s::estimate_bytes(int N, int E, int M, int S, int method, cons
     b += 24 * n + 24 * r + 32 * r + 16 * e + 48 * e;                  // nodes, rows, elements, bc
     b += sizeof(float4) * kGeoFloat4 * e + sizeof(double) * kGeoDouble * e;
     b += 3 * e * sizeof(TileRec) + 4 * (ntiles + 1) + 4 * n + 4 * ntiles;   // an element touches <= 3 tiles
+    b += 4 * (r + 1) + 256 * r;                                              // near-pair list (typ. < 64 per row)
     b += 8 * lda * r + 16 * r * s + 12 * ntiles * r + 16 * n * s + 16 * r + 48 * s;
     if (method == BEM_SOLVE_BLOCK_GMRES) {
         const size_t m = (size_t)std::max(1, std::min(o.max_iter, 200));

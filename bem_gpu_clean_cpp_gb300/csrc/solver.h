@@ -54,6 +54,10 @@ struct bem_solver_s {
 
     bem::DevMem d_nodes, d_rows_f, d_rows_d, d_elems, d_bc, d_geo_f, d_geo_d, d_srcs;
     double geo_eta = -1.0;   // near_eta the element tables were built with
+    // near pairs per row (CSR), valid for the current geometry and geo_eta
+    bool near_valid = false;
+    bem::DevMem d_near_ptr, d_near_ids;
+    double max_edge = 0.0;   // longest element edge
 
     struct Tiles {
         bool valid = false;
@@ -106,6 +110,7 @@ struct bem_solver_s {
     static size_t estimate_bytes(int N, int E, int M, int S, int method, const bem_options_t &o);
 
     void ensure_geo();
+    void ensure_near_list();
     void ensure_tiles(int precision);
     bem::GeoTables geo_tables() const;
     bem::RowPoints row_points() const;

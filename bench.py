@@ -717,7 +717,7 @@ def run_server_bench(args):
     value = dist.world * args.steps * solves / elapsed
 
     # ---- accuracy against the plain FP64 solve, and its one-at-a-time time ----
-    errs, fp64_t = [], {}
+    errs, fp64_t, worst_cases = [], {}, []
     checked_s5 = 0
     for i, p in enumerate(probs):
         n = p["pnts"].shape[0]
@@ -728,6 +728,9 @@ def run_server_bench(args):
         x = last[i][0]
         errs.append(float(max(np.abs(x[:, j] - x64[:, j]).max() / np.abs(x64[:, j]).max()
                               for j in range(x.shape[1]))))
+        worst_cases.append({"request": i, "nodes": n, "f_hz": round(p["f"], 1), "sources": len(p["srcs"]),
+                            "k_times_max_edge": round(p["k"] * _max_edge(p["pnts"], p["elems"]), 3),
+                            "rel_err": errs[-1]})
         fp64_t.setdefault(n, []).append(t64)
     per_n = {n: float(np.mean(v)) for n, v in fp64_t.items()}
     if 10242 in per_n:
@@ -738,6 +741,7 @@ def run_server_bench(args):
             "estimated_one_at_a_time_s": est,
             "solves_per_s": solves / est if est else None,
             "speedup_vs_fp64_plain": value / (solves / est) if est else None,
+            "largest_errors": sorted(worst_cases, key=lambda c: -c["rel_err"])[:5],
             "note": "plain FP64 = c128 assembly + Householder QR per problem, timed for every problem up to "
                     "10242 nodes (one at 10242), 40962-node problems extrapolated by N^3 from 10242"}
     sizes = sorted({p["pnts"].shape[0] for p in probs})
