@@ -86,8 +86,9 @@ int quadrature_points() { return g_nq_host; }
 // ---------------------------------------------------------------------------
 // Element tables.
 // Float table, 7 float4 per element:
-//   [0] (p3hi.xyz, J)   [1] (p3lo.xyz, near_r2)   [2] (e1, 0)   [3] (e2, 0)
-//   [4] (n, 0)          [5] (bcA.re, bcA.im, bcC.re, bcC.im)    [6] (centroid, 0)
+//   [0] (p3hi.xyz, J)   [1] (p3lo.xyz, near_r2)   [2] (e1, coff.x)   [3] (e2, coff.y)
+//   [4] (n, coff.z)     [5] (bcA.re, bcA.im, bcC.re, bcC.im)    [6] (centroid, 0)
+//   with coff = centroid - p3 = (e1 + e2) / 3
 // p3 is split into hi + lo floats so that p3 - x keeps full float precision
 // for nearby pairs.  e1 = p1-p3, e2 = p2-p3, n = e1 x e2 / J, J = |e1 x e2|
 // (mesh.cu:612-617), near_r2 = (eta * longest edge)^2.
@@ -133,9 +134,9 @@ __global__ void elem_setup_kernel(const double *__restrict__ nodes, const int4 *
     g[0] = make_float4(hx, hy, hz, (float)J);
     g[1] = make_float4((float)(p3[0] - (double)hx), (float)(p3[1] - (double)hy),
                        (float)(p3[2] - (double)hz), eta > 0 ? r2 : 0.0f);
-    g[2] = make_float4((float)e1[0], (float)e1[1], (float)e1[2], 0.0f);
-    g[3] = make_float4((float)e2[0], (float)e2[1], (float)e2[2], 0.0f);
-    g[4] = make_float4((float)n[0], (float)n[1], (float)n[2], 0.0f);
+    g[2] = make_float4((float)e1[0], (float)e1[1], (float)e1[2], (float)((e1[0] + e2[0]) / 3.0));
+    g[3] = make_float4((float)e2[0], (float)e2[1], (float)e2[2], (float)((e1[1] + e2[1]) / 3.0));
+    g[4] = make_float4((float)n[0], (float)n[1], (float)n[2], (float)((e1[2] + e2[2]) / 3.0));
     g[5] = make_float4((float)aR, (float)aI, (float)cR, (float)cI);
     g[6] = make_float4((float)cen[0], (float)cen[1], (float)cen[2], 0.0f);
     double *h = gd + (size_t)kGeoD * e;
@@ -188,45 +189,100 @@ __device__ __forceinline__ bool pair_is_near(int row, int N, int4 nd, float4 xh,
 // three nodal integrals (N1 = xi1, N2 = xi2, N3 = 1 - xi1 - xi2).  The 1/(4 pi)
 // and |J| factors are applied once per pair by the caller.
 // ---------------------------------------------------------------------------
-// Phase reduction for the FP32 quadrature.  The fast __sincosf is documented
-// with a bounded error on [-pi, pi] only and its error grows with |x| outside
-// (kr reaches ~30 at 8 kHz on a 0.11 m body).  Over one element kr varies by
-// at most k * diam, so one multiple of 2 pi per pair, n = round(k r_c / 2 pi)
-// with r_c the distance to the centroid, brings every point's phase into
-// [-pi - k diam, pi + k diam]:  y = fma(k, r, -n C1) + (-n C2), the
-// two-constant Cody-Waite scheme (Cody & Waite, "Software Manual for the
-// Elementary Functions", 1980) with C1 = 2 pi cut to 16 significant bits (n C1
-// is exact for n < 256) and C2 = fl(2 pi - C1); the FMA rounds k r - n C1 once.
-// Per point this costs one FMA and one add; the per-pair constants are
-// (-n C1, -n C2).  When an element spans a large phase (k * longest edge above
-// kWrapKh, coarse meshes at high frequency) the point's own multiple of 2 pi
-// is removed as well (WRAP: three more FMA-pipe instructions per point).
-constexpr double kWrapKh = 0.75;
-struct PhaseShift {
-    float c1, c2;
+// Phase of the FP32 quadrature.  The fast __sincosf is documented with a
+// bounded error on [-pi, pi] only and its error grows with |x| outside (kr
+// reaches ~30 at 8 kHz on a 0.11 m body).  Three modes, chosen per launch on
+// the host from the problem's size in wavelengths:
+//
+// kPhaseShift: over one element kr varies by at most k * diam, so one multiple
+//   of 2 pi per pair, n = round(k r_c / 2 pi) (r_c = distance to the centroid),
+//   brings every point's phase into [-pi - k diam, pi + k diam]:
+//   y = fma(k, r, -n C1) + (-n C2), the two-constant Cody-Waite scheme (Cody &
+//   Waite, "Software Manual for the Elementary Functions", 1980) with C1 = 2 pi
+//   cut to 16 significant bits (n C1 is exact for n < 256), C2 = fl(2 pi - C1).
+// kPhaseWrap: the same, and the point's own multiple of 2 pi is removed too
+//   (elements spanning a large phase: k * longest edge above kWrapKh).
+// kPhaseAcc: FP32 r carries a relative error of ~1e-7, a phase error of
+//   ~1e-7 kr that dominates when kr is large.  The phase is split as
+//   k r = k r_c + k (r - r_c): k r_c in double float once per pair (centroid
+//   offset from the row point in head/tail floats, k as head/tail), reduced by
+//   2 pi; r - r_c = (r^2 - r_c^2) / (r + r_c) where r^2 - r_c^2 =
+//   (d - d_c).(d + d_c) is a quadratic in the Duffy radius with coefficients
+//   free of cancellation, so the per-point term is accurate to ~1e-7 of
+//   k (r - r_c) <= k * diam.  Then wrapped as in kPhaseWrap.
+constexpr double kWrapKh = 0.75;    // k * longest edge above which the point phase is wrapped
+constexpr double kAccKd = 40.0;     // k * extent above which the phase is split (kPhaseAcc)
+enum { kPhaseShift = 0, kPhaseWrap = 1, kPhaseAcc = 2 };
+
+struct PairPhase {
+    float c1, c2;    // shift modes: -n C1, -n C2
+    float yc, rc;    // kPhaseAcc: k r_c reduced by 2 pi, r_c
+    float c0;        // kPhaseAcc: |d3|^2 - |d_c|^2 = -coff.(2 d3 + coff)
 };
-__device__ __forceinline__ PhaseShift phase_shift(float k, float3 d3, float3 e1, float3 e2) {
-    constexpr float kInv2Pi = 0.15915493667125702f;
-    constexpr float kC1 = 6.2830810546875f;
-    constexpr float kC2 = 0.00010425248910905793f;
-    const float cx = d3.x + (e1.x + e2.x) * (1.0f / 3.0f);
-    const float cy = d3.y + (e1.y + e2.y) * (1.0f / 3.0f);
-    const float cz = d3.z + (e1.z + e2.z) * (1.0f / 3.0f);
+
+constexpr float kInv2PiF = 0.15915493667125702f;
+constexpr float kC1F = 6.2830810546875f;
+constexpr float kC2F = 0.00010425248910905793f;
+
+__device__ __forceinline__ PairPhase pair_phase_shift(float k, float3 d3, float3 coff) {
+    const float cx = d3.x + coff.x, cy = d3.y + coff.y, cz = d3.z + coff.z;
     const float rc = sqrtf(fmaf(cz, cz, fmaf(cy, cy, cx * cx)));
-    const float n = fminf(rintf(k * rc * kInv2Pi), 255.0f);
-    return PhaseShift{-n * kC1, -n * kC2};
+    const float n = fminf(rintf(k * rc * kInv2PiF), 255.0f);
+    PairPhase p;
+    p.c1 = -n * kC1F;
+    p.c2 = -n * kC2F;
+    p.yc = p.rc = p.c0 = 0.f;
+    return p;
 }
 
-template <bool WRAP>
-__device__ __forceinline__ float phase_arg(float k, float r, const PhaseShift &ps) {
-    float y = fmaf(k, r, ps.c1) + ps.c2;
-    if (WRAP) {
-        constexpr float kInv2Pi = 0.15915493667125702f, kRound = 12582912.0f;
-        constexpr float kC1 = 6.2830810546875f, kC2 = 0.00010425248910905793f;
-        const float n = __fsub_rn(__fmaf_rn(y, kInv2Pi, kRound), kRound);
-        y = __fmaf_rn(-n, kC2, __fmaf_rn(-n, kC1, y));
-    }
-    return y;
+// x + y = s + e exactly (Knuth's TwoSum)
+__device__ __forceinline__ float two_sum(float a, float b, float &e) {
+    const float s = __fadd_rn(a, b), bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return s;
+}
+
+// kPhaseAcc per-pair terms: p3 = p3h + p3l and the row point x = xh + xl as
+// head/tail floats, coff = centroid - p3, k = kh + kl.
+__device__ __forceinline__ PairPhase pair_phase_acc(float kh, float kl, float3 p3h, float3 p3l, float4 xh,
+                                                    float4 xl, float3 d3, float3 coff) {
+    float e0, e1, e2;
+    const float hx = two_sum(p3h.x, -xh.x, e0), hy = two_sum(p3h.y, -xh.y, e1), hz = two_sum(p3h.z, -xh.z, e2);
+    const float lx = e0 + (p3l.x - xl.x) + coff.x, ly = e1 + (p3l.y - xl.y) + coff.y,
+                lz = e2 + (p3l.z - xl.z) + coff.z;
+    // r_c^2 = |(hx, hy, hz) + (lx, ly, lz)|^2 in double float
+    const float px = __fmul_rn(hx, hx), py = __fmul_rn(hy, hy), pz = __fmul_rn(hz, hz);
+    const float ex = __fmaf_rn(hx, hx, -px), ey = __fmaf_rn(hy, hy, -py), ez = __fmaf_rn(hz, hz, -pz);
+    float t0, t1;
+    const float s01 = two_sum(px, py, t0);
+    const float shi = two_sum(s01, pz, t1);
+    const float slo = (t0 + t1) + (ex + ey + ez) + 2.0f * (hx * lx + hy * ly + hz * lz);
+    const float r0 = __fsqrt_rn(shi);
+    const float rlo = (__fmaf_rn(-r0, r0, shi) + slo) * (0.5f / r0);
+    // k r_c = (kh + kl)(r0 + rlo), reduced by 2 pi
+    const float ph = __fmul_rn(kh, r0);
+    const float plo = __fmaf_rn(kh, r0, -ph) + kh * rlo + kl * r0;
+    const float n = fminf(rintf(ph * kInv2PiF), 255.0f);
+    PairPhase p;
+    p.c1 = p.c2 = 0.f;
+    p.yc = __fmaf_rn(-n, kC2F, __fmaf_rn(-n, kC1F, ph)) + plo;
+    p.rc = r0;
+    p.c0 = -(coff.x * (2.0f * d3.x + coff.x) + coff.y * (2.0f * d3.y + coff.y) + coff.z * (2.0f * d3.z + coff.z));
+    return p;
+}
+
+__device__ __forceinline__ float wrap_phase(float y) {
+    constexpr float kRound = 12582912.0f;   // 1.5 * 2^23: rounds to an integer (|y| < 2^22)
+    const float n = __fsub_rn(__fmaf_rn(y, kInv2PiF, kRound), kRound);
+    return __fmaf_rn(-n, kC2F, __fmaf_rn(-n, kC1F, y));
+}
+
+// Phase argument of a point at distance r; q = r^2 - r_c^2 (kPhaseAcc only).
+template <int PH>
+__device__ __forceinline__ float phase_arg(float k, float r, float q, const PairPhase &pp) {
+    if (PH == kPhaseAcc) return wrap_phase(fmaf(k, __fdividef(q, r + pp.rc), pp.yc));
+    const float y = fmaf(k, r, pp.c1) + pp.c2;
+    return PH == kPhaseWrap ? wrap_phase(y) : y;
 }
 
 struct SumsF {
@@ -235,10 +291,9 @@ struct SumsF {
     float c;                              // dG0/dn sum
 };
 
-template <bool WRAP>
-__device__ __forceinline__ void far_sums_f32(float3 d3, float3 e1, float3 e2, float hgt, float k,
-                                             int nq, SumsF &S) {
-    const PhaseShift ps = phase_shift(k, d3, e1, e2);
+template <int PH>
+__device__ __forceinline__ void far_sums_f32(float3 d3, float3 e1, float3 e2, float3 coff, float hgt, float k,
+                                             const PairPhase &pp, int nq, SumsF &S) {
     S.g0r = S.g0i = S.g1r = S.g1i = S.g2r = S.g2i = 0.0f;
     S.h0r = S.h0i = S.h1r = S.h1i = S.h2r = S.h2i = 0.0f;
     S.c = 0.0f;
@@ -252,7 +307,15 @@ __device__ __forceinline__ void far_sums_f32(float3 d3, float3 e1, float3 e2, fl
         float ri = rsqrtf(r2);
         float r = r2 * ri;
         float sn, cs;
-        __sincosf(phase_arg<WRAP>(k, r, ps), &sn, &cs);
+        float dq = 0.f;
+        if (PH == kPhaseAcc) {
+            // (d - d_c).(d + d_c) with d - d_c = t.x e1 + t.y e2 - coff
+            const float ux = fmaf(t.y, e2.x, fmaf(t.x, e1.x, -coff.x));
+            const float uy = fmaf(t.y, e2.y, fmaf(t.x, e1.y, -coff.y));
+            const float uz = fmaf(t.y, e2.z, fmaf(t.x, e1.z, -coff.z));
+            dq = fmaf(uz, dz + d3.z + coff.z, fmaf(uy, dy + d3.y + coff.y, ux * (dx + d3.x + coff.x)));
+        }
+        __sincosf(phase_arg<PH>(k, r, dq, pp), &sn, &cs);
         float gr = cs * ri, gi = -sn * ri;            // 4 pi G
         float hq = hgt * ri;                          // dr/dn
         float tr = fmaf(gi, k, -gr * ri);             // 4 pi G (-1/r - ik)
@@ -291,10 +354,9 @@ __device__ __forceinline__ float gl6_w(int i) {
                                                                            : 0.4679139345726910f;
 }
 
-template <bool WRAP>
-__device__ __forceinline__ void far_sums_f32_o6(float3 d3, float3 e1, float3 e2, float hgt, float k,
-                                                SumsF &S) {
-    const PhaseShift ps = phase_shift(k, d3, e1, e2);
+template <int PH>
+__device__ __forceinline__ void far_sums_f32_o6(float3 d3, float3 e1, float3 e2, float3 coff, float hgt, float k,
+                                                const PairPhase &pp, SumsF &S) {
     S.g0r = S.g0i = S.g1r = S.g1i = S.g2r = S.g2i = 0.0f;
     S.h0r = S.h0i = S.h1r = S.h1i = S.h2r = S.h2i = 0.0f;
     S.c = 0.0f;
@@ -303,6 +365,9 @@ __device__ __forceinline__ void far_sums_f32_o6(float3 d3, float3 e1, float3 e2,
     for (int n = 0; n < 6; n++) {
         const float th = 0.5f + 0.5f * gl6_x(n);
         const float vx = fmaf(th, e21.x, e1.x), vy = fmaf(th, e21.y, e1.y), vz = fmaf(th, e21.z, e1.z);
+        // kPhaseAcc: r^2 - r_c^2 = qa rho^2 + qb rho + c0 along the line
+        const float qa = PH == kPhaseAcc ? fmaf(vz, vz, fmaf(vy, vy, vx * vx)) : 0.f;
+        const float qb = PH == kPhaseAcc ? 2.0f * fmaf(vz, d3.z, fmaf(vy, d3.y, vx * d3.x)) : 0.f;
         float u0gr = 0.f, u1gr = 0.f, u0gs = 0.f, u1gs = 0.f;
         float u0ha = 0.f, u1ha = 0.f, u0hb = 0.f, u1hb = 0.f, u0c = 0.f;
 #pragma unroll
@@ -315,7 +380,8 @@ __device__ __forceinline__ void far_sums_f32_o6(float3 d3, float3 e1, float3 e2,
             const float r = r2 * ri;
             const float kr = k * r;
             float sn, cs;
-            __sincosf(phase_arg<WRAP>(k, r, ps), &sn, &cs);
+            const float q = PH == kPhaseAcc ? fmaf(fmaf(qa, rho, qb), rho, pp.c0) : 0.f;
+            __sincosf(phase_arg<PH>(k, r, q, pp), &sn, &cs);
             const float A = fmaf(kr, sn, cs);      // c + kr s
             const float Bv = fmaf(kr, cs, -sn);    // kr c - s
             const float ri3 = ri * ri * ri;
@@ -417,9 +483,9 @@ __device__ __forceinline__ void finish_coeffs(const SUMS &S, T scale, T rw, T bA
 // Far-field assembly kernel.
 // grid = (ceil(R/TR), ntiles), block = NT threads, dynamic smem = acc[TR][tc].
 // ---------------------------------------------------------------------------
-template <int TR, int NT, int MINB, bool O6, bool WRAP>
+template <int TR, int NT, int MINB, bool O6, int PH>
 __global__ void __launch_bounds__(NT, MINB)
-far_assembly_f32(RowPoints rows, int N, GeoTables geo, TileSet tiles, float k, float rw,
+far_assembly_f32(RowPoints rows, int N, GeoTables geo, TileSet tiles, float k, float k_lo, float rw,
                  float2 *__restrict__ A, size_t lda, float *__restrict__ c_part,
                  float2 *__restrict__ beta_part) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -456,8 +522,13 @@ far_assembly_f32(RowPoints rows, int N, GeoTables geo, TileSet tiles, float k, f
                                           (g0.z - xh.z) + (g1.z - xl.z));
             const float hgt = d3.x * g4.x + d3.y * g4.y + d3.z * g4.z;
             SumsF S;
-            if (O6) far_sums_f32_o6<WRAP>(d3, e1, e2, hgt, k, S);
-            else far_sums_f32<WRAP>(d3, e1, e2, hgt, k, nq, S);
+            const float3 coff = make_float3(g2.w, g3.w, g4.w);
+            const PairPhase pp = PH == kPhaseAcc
+                                     ? pair_phase_acc(k, k_lo, make_float3(g0.x, g0.y, g0.z),
+                                                      make_float3(g1.x, g1.y, g1.z), xh, xl, d3, coff)
+                                     : pair_phase_shift(k, d3, coff);
+            if (O6) far_sums_f32_o6<PH>(d3, e1, e2, coff, hgt, k, pp, S);
+            else far_sums_f32<PH>(d3, e1, e2, coff, hgt, k, pp, nq, S);
             Coeffs<float, SumsF> o;
             finish_coeffs<float, SumsF>(S, g0.w * inv4pi, rw, g5.x, g5.y, g5.z, g5.w, o);
 #pragma unroll
@@ -615,20 +686,35 @@ bool far_variant_fits(int prec, int tc, int variant) {
     return far_smem_bytes(prec, tc, variant) + 1024 <= (size_t)maxs;
 }
 
+int far_phase_mode(const Physics &ph) {
+    if (ph.k * ph.extent > kAccKd) return kPhaseAcc;
+    if (ph.k * ph.max_edge > kWrapKh) return kPhaseWrap;
+    return kPhaseShift;
+}
+
 template <int TR, int NT, int MINB>
 static void launch_far_f32(const RowPoints &rows, int N, const GeoTables &geo, const TileSet &tiles,
                            const Physics &ph, void *A, size_t lda, void *c_part, void *beta_part,
                            size_t smem, cudaStream_t st) {
     const bool o6 = quadrature_points() == 36;
-    const bool wrap = ph.k * ph.max_edge > kWrapKh;
-    auto kern = o6 ? (wrap ? far_assembly_f32<TR, NT, MINB, true, true> : far_assembly_f32<TR, NT, MINB, true, false>)
-                   : (wrap ? far_assembly_f32<TR, NT, MINB, false, true> : far_assembly_f32<TR, NT, MINB, false, false>);
-    if (o6 && wrap) allow_max_smem<far_assembly_f32<TR, NT, MINB, true, true>>();
-    else if (o6) allow_max_smem<far_assembly_f32<TR, NT, MINB, true, false>>();
-    else if (wrap) allow_max_smem<far_assembly_f32<TR, NT, MINB, false, true>>();
-    else allow_max_smem<far_assembly_f32<TR, NT, MINB, false, false>>();
+    const int mode = far_phase_mode(ph);
+    decltype(&far_assembly_f32<TR, NT, MINB, true, kPhaseShift>) kern;
+    if (!o6) {   // other Gauss orders: always the accurate phase (not the tuned path)
+        kern = far_assembly_f32<TR, NT, MINB, false, kPhaseAcc>;
+        allow_max_smem<far_assembly_f32<TR, NT, MINB, false, kPhaseAcc>>();
+    } else if (mode == kPhaseAcc) {
+        kern = far_assembly_f32<TR, NT, MINB, true, kPhaseAcc>;
+        allow_max_smem<far_assembly_f32<TR, NT, MINB, true, kPhaseAcc>>();
+    } else if (mode == kPhaseWrap) {
+        kern = far_assembly_f32<TR, NT, MINB, true, kPhaseWrap>;
+        allow_max_smem<far_assembly_f32<TR, NT, MINB, true, kPhaseWrap>>();
+    } else {
+        kern = far_assembly_f32<TR, NT, MINB, true, kPhaseShift>;
+        allow_max_smem<far_assembly_f32<TR, NT, MINB, true, kPhaseShift>>();
+    }
+    const float kh = (float)ph.k, kl = (float)(ph.k - (double)kh);
     dim3 grid((rows.R + TR - 1) / TR, tiles.ntiles);
-    kern<<<grid, NT, smem, st>>>(rows, N, geo, tiles, (float)ph.k, (float)ph.rw, (float2 *)A, lda,
+    kern<<<grid, NT, smem, st>>>(rows, N, geo, tiles, kh, kl, (float)ph.rw, (float2 *)A, lda,
                                  (float *)c_part, (float2 *)beta_part);
 }
 
@@ -1002,8 +1088,10 @@ field_far_kernel(RowPoints pts, GeoTables geo, T k, T rw, int nq,
                                     (g0.z - xh.z) + (g1.z - xl.z));
             float hgt = d3.x * g4.x + d3.y * g4.y + d3.z * g4.z;
             SumsF Sm;
-            far_sums_f32<true>(d3, make_float3(g2.x, g2.y, g2.z), make_float3(g3.x, g3.y, g3.z), hgt,
-                               (float)k, nq, Sm);
+            const float3 coff = make_float3(g2.w, g3.w, g4.w);
+            const PairPhase pp = pair_phase_shift((float)k, d3, coff);
+            far_sums_f32<kPhaseWrap>(d3, make_float3(g2.x, g2.y, g2.z), make_float3(g3.x, g3.y, g3.z), coff, hgt,
+                                     (float)k, pp, nq, Sm);
             Coeffs<float, SumsF> oo;
             finish_coeffs<float, SumsF>(Sm, g0.w * (float)(1.0 / (4.0 * kPi)), (float)rw, g5.x, g5.y,
                                         g5.z, g5.w, oo);

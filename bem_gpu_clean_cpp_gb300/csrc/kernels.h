@@ -42,8 +42,11 @@ struct Physics {
     double rw;                // density * omega = density * k * speed
     int near_depth;
     double near_eta;
-    double max_edge = 0.0;    // longest element edge (selects the per-point phase wrap)
+    double max_edge = 0.0;    // longest element edge } select the phase mode of the
+    double extent = 0.0;      // diagonal of the rows' and nodes' box } FP32 quadrature
 };
+// Phase mode of the FP32 far kernel for this problem (kernels.cu).
+int far_phase_mode(const Physics &ph);
 
 // Upload the Gauss rule of the given order to this device's constant memory
 // (no-op when already current on the device).
@@ -111,6 +114,12 @@ int gemv_h_splits(int R, int N);
 // row-major transpose).
 void launch_gemv_h_c64(int R, int N, const float2 *A, size_t lda, const void *u, int ud,
                        void *w, int wd, void *part, cudaStream_t st, bool conj = true);
+// w = A^H (A v) for c64 A with A read once (cluster kernel); v c64, w c128;
+// part: scratch of normal_op_clusters(N) x N c64.  Returns false (nothing
+// launched) when N is above what one cluster covers (45056).
+int normal_op_clusters(int N);
+bool launch_normal_op(int R, int N, const float2 *A, size_t lda, const float2 *v, double2 *w, float2 *part,
+                      cudaStream_t st);
 int gemv_h_f64_splits(int R, int N);
 // FP64 accumulation variants (the refinement residuals): A is c64 or c128.
 // r = b - A x.  For c64 A the products are exact double-float FP32

@@ -6,9 +6,11 @@
 // These replace the reference's per-iteration host round trips in GMRES.cu
 // (which re-uploads A every Arnoldi step, GMRES.cu:106-108) with
 // device-resident state.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <mutex>
 
 #include "bem_common.h"
 #include "dfloat.h"
@@ -475,6 +477,116 @@ __global__ void set_scalar_c_kernel(double2 *__restrict__ dst, const double *__r
 
 inline int blocks(long long n, int t) { return (int)((n + t - 1) / t); }
 
+
+// ---- fused normal operator w = A^H (A v), A read once from HBM ----
+// A thread-block cluster of C CTAs (C = ceil(N / kNoW)) owns a block of rows;
+// CTA q of the cluster owns columns [q kNoW, (q+1) kNoW) with v and its
+// partial w in shared memory.  For kNoRB rows at a time each thread loads its
+// kNoCPT columns of those rows into registers, forms its part of the row dot
+// products t_r = A_r v, the CTA reduces them, the cluster adds the CTAs' sums
+// through distributed shared memory (one cluster barrier per row group), and
+// the same registers give w += conj(A_r) t_r.  A is read once where A v and
+// A^H t as two kernels read it twice.  The clusters' partial w are summed in
+// FP64 by sum_splits_kernel.
+//
+// Every CTA of a cluster runs the same number of row groups (rows past R are
+// masked, never skipped) and calls the cluster barrier the same number of
+// times, including the final one that keeps each CTA's shared memory alive
+// until its peers have read it.
+constexpr int kNoNT = 512;
+constexpr int kNoCPT = 11;
+constexpr int kNoW = kNoNT * kNoCPT;   // 5632 columns per CTA
+constexpr int kNoRB = 2;               // rows per group
+constexpr int kNoMaxCluster = 8;
+
+__global__ void __launch_bounds__(kNoNT, 2)
+normal_op_kernel(int R, int N, const float2 *__restrict__ A, size_t lda, const float2 *__restrict__ v,
+                 int rows_per_cluster, int ngroups, float2 *__restrict__ wpart) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    const int C = (int)cluster.num_blocks();
+    const int q = (int)cluster.block_rank();
+    const int cl = blockIdx.x / C;
+    extern __shared__ __align__(16) float2 no_smem[];
+    float2 *vs = no_smem, *ws = no_smem + kNoW;
+    __shared__ float red[kNoRB][2][kNoNT / 32];
+    __shared__ float tot[2][kNoRB * 2];      // this CTA's row sums, double-buffered; read by the peers
+    __shared__ float tsum[kNoRB * 2];        // the cluster's row sums t_r
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int c0 = q * kNoW;
+    for (int i = tid; i < kNoW; i += kNoNT) {
+        const int c = c0 + i;
+        vs[i] = c < N ? v[c] : make_float2(0.f, 0.f);
+        ws[i] = make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    const int r_begin = cl * rows_per_cluster;
+    const int r_end = min(R, r_begin + rows_per_cluster);
+    for (int g = 0; g < ngroups; g++) {
+        const int par = g & 1;
+        float2 a[kNoRB][kNoCPT];
+        float pr[kNoRB], pim[kNoRB];
+#pragma unroll
+        for (int rb = 0; rb < kNoRB; rb++) {
+            const int row = r_begin + g * kNoRB + rb;
+            const bool ok = row < r_end;
+            const float2 *arow = A + (size_t)(ok ? row : 0) * lda;
+            pr[rb] = pim[rb] = 0.f;
+#pragma unroll
+            for (int i = 0; i < kNoCPT; i++) {
+                const int c = c0 + tid + i * kNoNT;
+                a[rb][i] = (ok && c < N) ? __ldcs(arow + c) : make_float2(0.f, 0.f);
+            }
+        }
+#pragma unroll
+        for (int rb = 0; rb < kNoRB; rb++) {
+#pragma unroll
+            for (int i = 0; i < kNoCPT; i++) {
+                const float2 x = vs[tid + i * kNoNT], y = a[rb][i];
+                pr[rb] = fmaf(y.x, x.x, fmaf(-y.y, x.y, pr[rb]));
+                pim[rb] = fmaf(y.x, x.y, fmaf(y.y, x.x, pim[rb]));
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                pr[rb] += __shfl_xor_sync(0xffffffffu, pr[rb], o);
+                pim[rb] += __shfl_xor_sync(0xffffffffu, pim[rb], o);
+            }
+            if (lane == 0) {
+                red[rb][0][warp] = pr[rb];
+                red[rb][1][warp] = pim[rb];
+            }
+        }
+        __syncthreads();
+        if (tid < 2 * kNoRB) {
+            float t = 0.f;
+            for (int w = 0; w < kNoNT / 32; w++) t += red[tid >> 1][tid & 1][w];
+            tot[par][tid] = t;
+        }
+        cluster.sync();   // every CTA's row sums of this group are in its tot[par]
+        if (tid < 2 * kNoRB) {
+            float t = 0.f;
+            for (int p = 0; p < C; p++) t += cluster.map_shared_rank(&tot[par][0], p)[tid];
+            tsum[tid] = t;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int rb = 0; rb < kNoRB; rb++) {
+            const float tr = tsum[2 * rb], ti = tsum[2 * rb + 1];
+#pragma unroll
+            for (int i = 0; i < kNoCPT; i++) {
+                const float2 y = a[rb][i];
+                float2 &w = ws[tid + i * kNoNT];
+                w.x = fmaf(y.x, tr, fmaf(y.y, ti, w.x));     // conj(a) t
+                w.y = fmaf(y.x, ti, fmaf(-y.y, tr, w.y));
+            }
+        }
+    }
+    cluster.sync();   // the peers have read tot; shared memory may go
+    for (int i = tid; i < kNoW; i += kNoNT) {
+        const int c = c0 + i;
+        if (c < N) wpart[(size_t)cl * N + c] = ws[i];
+    }
+}
+
 }  // namespace
 
 void launch_gemv_c64(int R, int N, const float2 *A, size_t lda, const void *x, int xd, void *y,
@@ -515,6 +627,66 @@ void launch_gemv_h_c64(int R, int N, const float2 *A, size_t lda, const void *u,
     else sum_splits_kernel<float2, float2><<<blocks(N, 256), 256, 0, st>>>(N, ns, (const float2 *)part, (float2 *)w);
     count_launch();
     KERNEL_CHECK();
+}
+
+int normal_op_clusters(int N) {
+    const int C = (N + kNoW - 1) / kNoW;
+    if (C > kNoMaxCluster) return 0;
+    return (2 * 152) / C;
+}
+
+bool launch_normal_op(int R, int N, const float2 *A, size_t lda, const float2 *v, double2 *w, float2 *part,
+                      cudaStream_t st) {
+    const int C = (N + kNoW - 1) / kNoW;
+    if (N <= 0 || R <= 0 || C > kNoMaxCluster) return false;
+    BEM_PROF("normal_op", st);
+    static std::once_flag once;
+    static cudaError_t attr_err = cudaSuccess;
+    const size_t smem = 2 * (size_t)kNoW * sizeof(float2);
+    std::call_once(once, [&] {
+        attr_err = cudaFuncSetAttribute(normal_op_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    });
+    CUDA_TRY(attr_err);
+    const int ncl = normal_op_clusters(N);
+    {
+        // the cluster shape must be schedulable on this device (else the two-kernel path runs)
+        cudaLaunchConfig_t probe = {};
+        probe.gridDim = dim3((unsigned)(ncl * C));
+        probe.blockDim = dim3(kNoNT);
+        probe.dynamicSmemBytes = smem;
+        cudaLaunchAttribute pa[1];
+        pa[0].id = cudaLaunchAttributeClusterDimension;
+        pa[0].val.clusterDim.x = (unsigned)C;
+        pa[0].val.clusterDim.y = 1;
+        pa[0].val.clusterDim.z = 1;
+        probe.attrs = pa;
+        probe.numAttrs = 1;
+        int active = 0;
+        if (cudaOccupancyMaxActiveClusters(&active, normal_op_kernel, &probe) != cudaSuccess || active < 1) {
+            cudaGetLastError();
+            return false;
+        }
+    }
+    const int rpc = (R + ncl - 1) / ncl;
+    const int ngroups = (rpc + kNoRB - 1) / kNoRB;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(ncl * C));
+    cfg.blockDim = dim3(kNoNT);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)C;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    CUDA_TRY(cudaLaunchKernelEx(&cfg, normal_op_kernel, R, N, A, lda, v, rpc, ngroups, part));
+    count_launch();
+    sum_splits_kernel<float2, double2><<<blocks(N, 256), 256, 0, st>>>(N, ncl, part, w);
+    count_launch();
+    KERNEL_CHECK();
+    return true;
 }
 
 void launch_resid(int prec, int R, int N, const void *A, size_t lda, const double2 *x,

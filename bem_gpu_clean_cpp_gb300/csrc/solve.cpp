@@ -111,6 +111,7 @@ void bem_solver_s::solve_refined(bem_solve_info_t *info) {
     // length-R vector (A^H u): 2 max(N, R) c64
     w_vf.ensure(sizeof(float2) * 2 * (size_t)std::max(n, R));
     size_t part = std::max(sizeof(float2) * (size_t)gemv_h_splits(R, n), sizeof(double2) * (size_t)gemv_h_f64_splits(R, n));
+    part = std::max(part, sizeof(float2) * (size_t)normal_op_clusters(n));
     w_part.ensure(part * n);
     w_scal.ensure(sizeof(double) * 8);
     double2 *V = w_V.as<double2>();
@@ -149,8 +150,12 @@ void bem_solver_s::solve_refined(bem_solve_info_t *info) {
             launch_set_scalar_c(w_g.as<double2>(), scal + 1, stream);
             int jdone = 0;
             for (int j = 0; j < m; j++) {
-                launch_gemv_c64(R, n, A, lda, w_vf.p, 0, w_t.p, 0, stream);                  // t = A v_j (c64 copy)
-                launch_gemv_h_c64(R, n, A, lda, w_t.p, 0, w_w.p, 1, w_part.p, stream);      // w = A^H t
+                // w = A^H A v_j (c64 copy of v_j): one pass over A when a cluster covers N
+                if (!launch_normal_op(R, n, A, lda, w_vf.as<float2>(), w_w.as<double2>(), w_part.as<float2>(),
+                                      stream)) {
+                    launch_gemv_c64(R, n, A, lda, w_vf.p, 0, w_t.p, 0, stream);              // t = A v_j
+                    launch_gemv_h_c64(R, n, A, lda, w_t.p, 0, w_w.p, 1, w_part.p, stream);  // w = A^H t
+                }
                 launch_dots(n, j + 1, V, n, w_w.as<double2>(), w_h1.as<double2>(), nullptr, stream);
                 launch_update(n, j + 1, V, n, w_h1.as<double2>(), w_w.as<double2>(), stream);
                 launch_dots(n, j + 1, V, n, w_w.as<double2>(), w_h2.as<double2>(), nullptr, stream);

@@ -142,6 +142,15 @@ void bem_solver_s::set_geometry(const double *pnts, int num_pnts, const int *ele
         BEM_CHECK_ARG(h_bc[6 * (size_t)e + 2] != 0.0 || h_bc[6 * (size_t)e + 3] != 0.0, "element with cb = 0");
     h_rows.assign(h_nodes.begin(), h_nodes.end());
     if (M) h_rows.insert(h_rows.end(), chief, chief + 3 * (size_t)M);
+    {
+        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+        for (size_t i = 0; i < h_rows.size(); i++) {
+            lo[i % 3] = std::min(lo[i % 3], h_rows[i]);
+            hi[i % 3] = std::max(hi[i % 3], h_rows[i]);
+        }
+        extent = std::sqrt((hi[0] - lo[0]) * (hi[0] - lo[0]) + (hi[1] - lo[1]) * (hi[1] - lo[1]) +
+                           (hi[2] - lo[2]) * (hi[2] - lo[2]));
+    }
 
     std::vector<float4> rf(2 * (size_t)R);
     for (int i = 0; i < R; i++) {
@@ -305,7 +314,7 @@ GeoTables bem_solver_s::geo_tables() const {
 RowPoints bem_solver_s::row_points() const { return RowPoints{d_rows_f.as<float4>(), d_rows_d.as<double>(), R}; }
 
 Physics bem_solver_s::physics() const {
-    return Physics{k, opt.density * k * opt.speed, opt.near_depth, opt.near_eta, max_edge};
+    return Physics{k, opt.density * k * opt.speed, opt.near_depth, opt.near_eta, max_edge, extent};
 }
 
 void bem_solver_s::assemble(double kk, int precision) {

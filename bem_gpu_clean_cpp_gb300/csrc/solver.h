@@ -58,6 +58,7 @@ struct bem_solver_s {
     bool near_valid = false;
     bem::DevMem d_near_ptr, d_near_ids;
     double max_edge = 0.0;   // longest element edge
+    double extent = 0.0;     // diagonal of the box around nodes and CHIEF points
 
     struct Tiles {
         bool valid = false;

@@ -182,3 +182,25 @@ def test_dropin_qr_vs_numpy(bemlib):
     X = np.linalg.lstsq(A.astype(np.complex128), B.astype(np.complex128), rcond=None)[0]
     bemlib.qrSolver(A, B)
     assert rel_err(B[:40], X) < 1e-4
+
+
+@pytest.mark.parametrize("nu", [24, 33])
+def test_refined_solve_cluster_sizes(bemlib, nu):
+    """Refined GMRES on meshes whose node counts need two-CTA clusters in the
+    fused A^H A v kernel (5762 and 10892 nodes), against the FP64 solve."""
+    m = bemlib.Mesh.geodesic(nu).perturbed_ellipsoid(1.0, 0.8, 0.9, lmax=4, amp=0.03, seed=nu)
+    p, e = m.points(), m.elems()
+    rng = np.random.default_rng(nu)
+    chief = rng.uniform(-0.25, 0.25, (8, 3))
+    d = np.array([0.3, -0.5, 0.81])
+    src = [("plane", d / np.linalg.norm(d), 1.0)]
+    s = bemlib.Solver(near_eta=1.0, near_depth=2)
+    s.set_geometry(p, e, bc=np.tile(np.array([0, 1, 0], dtype=np.complex128), (e.shape[0], 1)), chief=chief)
+    s.set_sources(src)
+    s.assemble(5.0, bemlib.PREC_C128)
+    s.solve(bemlib.SOLVE_QR)
+    x64 = s.solution()
+    s.assemble(5.0, bemlib.PREC_C64)
+    info = s.solve(bemlib.SOLVE_GMRES_REFINED)
+    assert info.converged
+    assert rel_err(s.solution(), x64) < 1e-5
