@@ -246,10 +246,12 @@ __device__ __forceinline__ float two_sum(float a, float b, float &e) {
 // head/tail floats, coff = centroid - p3, k = kh + kl.
 __device__ __forceinline__ PairPhase pair_phase_acc(float kh, float kl, float3 p3h, float3 p3l, float4 xh,
                                                     float4 xl, float3 d3, float3 coff) {
-    float e0, e1, e2;
-    const float hx = two_sum(p3h.x, -xh.x, e0), hy = two_sum(p3h.y, -xh.y, e1), hz = two_sum(p3h.z, -xh.z, e2);
-    const float lx = e0 + (p3l.x - xl.x) + coff.x, ly = e1 + (p3l.y - xl.y) + coff.y,
-                lz = e2 + (p3l.z - xl.z) + coff.z;
+    // centroid - x = (p3h - xh) + coff + (p3l - xl): head hx (two rounded sums), tail lx
+    float a0, a1, a2, b0, b1, b2;
+    const float hx = two_sum(two_sum(p3h.x, -xh.x, a0), coff.x, b0);
+    const float hy = two_sum(two_sum(p3h.y, -xh.y, a1), coff.y, b1);
+    const float hz = two_sum(two_sum(p3h.z, -xh.z, a2), coff.z, b2);
+    const float lx = (a0 + b0) + (p3l.x - xl.x), ly = (a1 + b1) + (p3l.y - xl.y), lz = (a2 + b2) + (p3l.z - xl.z);
     // r_c^2 = |(hx, hy, hz) + (lx, ly, lz)|^2 in double float
     const float px = __fmul_rn(hx, hx), py = __fmul_rn(hy, hy), pz = __fmul_rn(hz, hz);
     const float ex = __fmaf_rn(hx, hx, -px), ey = __fmaf_rn(hy, hy, -py), ez = __fmaf_rn(hz, hz, -pz);

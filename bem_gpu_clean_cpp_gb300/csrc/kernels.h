@@ -114,6 +114,15 @@ int gemv_h_splits(int R, int N);
 // row-major transpose).
 void launch_gemv_h_c64(int R, int N, const float2 *A, size_t lda, const void *u, int ud,
                        void *w, int wd, void *part, cudaStream_t st, bool conj = true);
+// One Arnoldi step (CGS2, norm, next basis vector and its c64 copy, the
+// Hessenberg column and its Givens rotation, *res = |g_{j+1}|) in a single
+// cooperative launch; part is scratch of 3 (j+1) x arnoldi_step_blocks()
+// c128.  Returns false (nothing launched) when a cooperative launch is not
+// available, then the caller runs the separate kernels.
+int arnoldi_step_blocks();
+bool launch_arnoldi_step(int n, int j, double2 *V, size_t ldv, double2 *w, float2 *vf, double2 *h1, double2 *h2,
+                         double2 *H, int ldh, double2 *cs, double2 *sn, double2 *g, double *res, double2 *part,
+                         cudaStream_t st);
 // w = A^H (A v) for c64 A with A read once (cluster kernel); v c64, w c128;
 // part: scratch of normal_op_clusters(N) x N c64.  Returns false (nothing
 // launched) when N is above what one cluster covers (45056).

@@ -478,6 +478,156 @@ __global__ void set_scalar_c_kernel(double2 *__restrict__ dst, const double *__r
 inline int blocks(long long n, int t) { return (int)((n + t - 1) / t); }
 
 
+// ---- one Arnoldi step of the refined solver in one cooperative launch ----
+// For basis vectors V_0..V_j (FP64, column stride ldv) and w = A^H A v_j:
+// classical Gram-Schmidt twice (h1 = V^H w, w -= V h1, h2 = V^H w,
+// w -= V h2), |w|, v_{j+1} = w/|w| (and its c64 copy), then the Hessenberg
+// column and its Givens rotation (GMRES.cu:44-88) with the residual estimate
+// |g_{j+1}| in *res.  Each CTA owns a contiguous slice of the n entries; the
+// dot products and the norm are per-CTA partial sums reduced after a grid
+// barrier, in the same order by every CTA.  Every CTA passes the same three
+// grid barriers (no early exit), and the launch is cooperative, so all CTAs
+// are resident.
+constexpr int kArNT = 256;
+constexpr int kArnoldiMaxK = 1024;   // basis vectors per step (shared-memory coefficients)
+
+__global__ void __launch_bounds__(kArNT)
+arnoldi_step_kernel(int n, int j, double2 *__restrict__ V, size_t ldv, double2 *__restrict__ w,
+                    float2 *__restrict__ vf, double2 *__restrict__ h1, double2 *__restrict__ h2,
+                    double2 *__restrict__ H, int ldh, double2 *__restrict__ cs, double2 *__restrict__ sn,
+                    double2 *__restrict__ g, double *__restrict__ res, double2 *__restrict__ part) {
+    namespace cg = cooperative_groups;
+    cg::grid_group grid = cg::this_grid();
+    const int nb = gridDim.x, b = blockIdx.x, tid = threadIdx.x;
+    const int per = (n + nb - 1) / nb;
+    const int i0 = min(n, b * per), i1 = min(n, i0 + per);
+    const int k = j + 1;                              // basis vectors in use
+    __shared__ double sr_[kArNT / 32], si_[kArNT / 32];
+    extern __shared__ double2 hs[];                   // k coefficients
+    // partial dots of this CTA's slice: part[q * nb + b] for q < k
+    auto partial_dots = [&](double2 *out_part) {
+        for (int q = 0; q < k; q++) {
+            const double2 *v = V + (size_t)q * ldv;
+            double a = 0.0, c = 0.0;
+            for (int i = i0 + tid; i < i1; i += kArNT) {
+                const double2 x = v[i], y = w[i];
+                a += x.x * y.x + x.y * y.y;   // conj(v) w
+                c += x.x * y.y - x.y * y.x;
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                a += __shfl_xor_sync(0xffffffffu, a, o);
+                c += __shfl_xor_sync(0xffffffffu, c, o);
+            }
+            if ((tid & 31) == 0) { sr_[tid >> 5] = a; si_[tid >> 5] = c; }
+            __syncthreads();
+            if (tid == 0) {
+                double ta = 0.0, tc = 0.0;
+                for (int t = 0; t < kArNT / 32; t++) { ta += sr_[t]; tc += si_[t]; }
+                out_part[(size_t)q * nb + b] = make_double2(ta, tc);
+            }
+            __syncthreads();
+        }
+    };
+    // h[q] = sum over CTAs (fixed order), into shared memory and, from CTA 0, into hout
+    auto reduce_dots = [&](const double2 *in_part, double2 *hout) {
+        for (int q = tid; q < k; q += kArNT) {
+            double a = 0.0, c = 0.0;
+            for (int t = 0; t < nb; t++) {
+                const double2 p = in_part[(size_t)q * nb + t];
+                a += p.x;
+                c += p.y;
+            }
+            hs[q] = make_double2(a, c);
+            if (b == 0) hout[q] = hs[q];
+        }
+        __syncthreads();
+    };
+    auto subtract = [&]() {
+        for (int i = i0 + tid; i < i1; i += kArNT) {
+            double a = 0.0, c = 0.0;
+            for (int q = 0; q < k; q++) {
+                const double2 x = V[(size_t)q * ldv + i], y = hs[q];
+                a += x.x * y.x - x.y * y.y;
+                c += x.x * y.y + x.y * y.x;
+            }
+            const double2 ww = w[i];
+            w[i] = make_double2(ww.x - a, ww.y - c);
+        }
+        __syncthreads();
+    };
+    double2 *p1 = part, *p2 = part + (size_t)k * nb, *p3 = part + 2 * (size_t)k * nb;
+    partial_dots(p1);
+    grid.sync();
+    reduce_dots(p1, h1);
+    subtract();
+    partial_dots(p2);
+    grid.sync();
+    reduce_dots(p2, h2);
+    subtract();
+    // |w|^2 partials
+    {
+        double a = 0.0;
+        for (int i = i0 + tid; i < i1; i += kArNT) a += w[i].x * w[i].x + w[i].y * w[i].y;
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+        if ((tid & 31) == 0) sr_[tid >> 5] = a;
+        __syncthreads();
+        if (tid == 0) {
+            double t = 0.0;
+            for (int q = 0; q < kArNT / 32; q++) t += sr_[q];
+            p3[b] = make_double2(t, 0.0);
+        }
+    }
+    grid.sync();
+    __shared__ double nrm_s;
+    if (tid == 0) {
+        double t = 0.0;
+        for (int q = 0; q < nb; q++) t += p3[q].x;
+        nrm_s = sqrt(t);
+    }
+    __syncthreads();
+    const double nrm = nrm_s;
+    const double inv = nrm > 0 ? 1.0 / nrm : 0.0;
+    double2 *vn = V + (size_t)k * ldv;
+    for (int i = i0 + tid; i < i1; i += kArNT) {
+        const double2 o = make_double2(w[i].x * inv, w[i].y * inv);
+        vn[i] = o;
+        vf[i] = make_float2((float)o.x, (float)o.y);
+    }
+    if (b == 0 && tid == 0) {
+        // Hessenberg column j = h1 + h2, H[j+1, j] = |w|, then the rotations
+        double2 *h = H + (size_t)j * ldh;
+        for (int t = 0; t <= j; t++) h[t] = make_double2(h1[t].x + h2[t].x, h1[t].y + h2[t].y);
+        h[j + 1] = make_double2(nrm, 0.0);
+        for (int l = 0; l < j; l++) {
+            const double2 c = cs[l], s = sn[l], a = h[l], bb = h[l + 1];
+            const double2 t0 = make_double2(c.x * a.x - c.y * a.y + s.x * bb.x - s.y * bb.y,
+                                            c.x * a.y + c.y * a.x + s.x * bb.y + s.y * bb.x);
+            const double2 t1 = make_double2(-(s.x * a.x + s.y * a.y) + (c.x * bb.x + c.y * bb.y),
+                                            -(s.x * a.y - s.y * a.x) + (c.x * bb.y - c.y * bb.x));
+            h[l] = t0;
+            h[l + 1] = t1;
+        }
+        const double2 rho = h[j], sig = h[j + 1];
+        const double mag = sqrt(rho.x * rho.x + rho.y * rho.y + sig.x * sig.x + sig.y * sig.y);
+        double2 c, s;
+        if (mag > 0) {
+            c = make_double2(rho.x / mag, -rho.y / mag);
+            s = make_double2(sig.x / mag, -sig.y / mag);
+        } else {
+            c = make_double2(1.0, 0.0);
+            s = make_double2(0.0, 0.0);
+        }
+        cs[j] = c;
+        sn[j] = s;
+        h[j] = make_double2(mag, 0.0);
+        h[j + 1] = make_double2(0.0, 0.0);
+        const double2 gj = g[j];
+        g[j + 1] = make_double2(-(s.x * gj.x + s.y * gj.y), -(s.x * gj.y - s.y * gj.x));
+        g[j] = make_double2(c.x * gj.x - c.y * gj.y, c.x * gj.y + c.y * gj.x);
+        res[0] = sqrt(g[j + 1].x * g[j + 1].x + g[j + 1].y * g[j + 1].y);
+    }
+}
+
 // ---- fused normal operator w = A^H (A v), A read once from HBM ----
 // A thread-block cluster of C CTAs (C = ceil(N / kNoW)) owns a block of rows;
 // CTA q of the cluster owns columns [q kNoW, (q+1) kNoW) with v and its
@@ -627,6 +777,43 @@ void launch_gemv_h_c64(int R, int N, const float2 *A, size_t lda, const void *u,
     else sum_splits_kernel<float2, float2><<<blocks(N, 256), 256, 0, st>>>(N, ns, (const float2 *)part, (float2 *)w);
     count_launch();
     KERNEL_CHECK();
+}
+
+int arnoldi_step_blocks() {
+    static int nb = -1;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        int dev = 0, sms = 0, per = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, arnoldi_step_kernel, kArNT,
+                                                          (size_t)kArnoldiMaxK * sizeof(double2)) != cudaSuccess ||
+            per < 1) {
+            cudaGetLastError();
+            nb = 0;
+        } else {
+            nb = sms;   // one CTA per SM: every CTA is resident, as the grid barrier needs
+        }
+    });
+    return nb;
+}
+
+bool launch_arnoldi_step(int n, int j, double2 *V, size_t ldv, double2 *w, float2 *vf, double2 *h1, double2 *h2,
+                         double2 *H, int ldh, double2 *cs, double2 *sn, double2 *g, double *res, double2 *part,
+                         cudaStream_t st) {
+    const int nb = arnoldi_step_blocks();
+    if (nb <= 0 || j + 1 > kArnoldiMaxK || n < 1) return false;
+    BEM_PROF("arnoldi_step", st);
+    const size_t smem = (size_t)(j + 1) * sizeof(double2);
+    void *args[] = {&n, &j, &V, &ldv, &w, &vf, &h1, &h2, &H, &ldh, &cs, &sn, &g, &res, &part};
+    const cudaError_t e = cudaLaunchCooperativeKernel((const void *)arnoldi_step_kernel, dim3(nb), dim3(kArNT),
+                                                      args, smem, st);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    count_launch();
+    return true;
 }
 
 int normal_op_clusters(int N) {

@@ -114,6 +114,7 @@ void bem_solver_s::solve_refined(bem_solve_info_t *info) {
     part = std::max(part, sizeof(float2) * (size_t)normal_op_clusters(n));
     w_part.ensure(part * n);
     w_scal.ensure(sizeof(double) * 8);
+    w_ap.ensure(sizeof(double2) * 3 * (size_t)(m + 1) * std::max(1, arnoldi_step_blocks()));
     double2 *V = w_V.as<double2>();
     double *scal = w_scal.as<double>();
     int total_it = 0, max_ref = 0, all_conv = 1;
@@ -156,15 +157,22 @@ void bem_solver_s::solve_refined(bem_solve_info_t *info) {
                     launch_gemv_c64(R, n, A, lda, w_vf.p, 0, w_t.p, 0, stream);              // t = A v_j
                     launch_gemv_h_c64(R, n, A, lda, w_t.p, 0, w_w.p, 1, w_part.p, stream);  // w = A^H t
                 }
-                launch_dots(n, j + 1, V, n, w_w.as<double2>(), w_h1.as<double2>(), nullptr, stream);
-                launch_update(n, j + 1, V, n, w_h1.as<double2>(), w_w.as<double2>(), stream);
-                launch_dots(n, j + 1, V, n, w_w.as<double2>(), w_h2.as<double2>(), nullptr, stream);
-                launch_update(n, j + 1, V, n, w_h2.as<double2>(), w_w.as<double2>(), stream);
-                launch_nrm2(n, w_w.as<double2>(), scal + 2, nullptr, stream);
-                launch_hcol_finish(j, w_h1.as<double2>(), w_h2.as<double2>(), scal + 2, w_H.as<double2>(), ldh, stream);
-                launch_scale_copy(n, w_w.as<double2>(), scal + 2, V + (size_t)(j + 1) * n, stream, w_vf.as<float2>());
-                launch_givens(j, w_H.as<double2>(), ldh, w_cs.as<double2>(), w_sn.as<double2>(),
-                              w_g.as<double2>(), scal + 3, stream);
+                if (!launch_arnoldi_step(n, j, V, n, w_w.as<double2>(), w_vf.as<float2>(), w_h1.as<double2>(),
+                                         w_h2.as<double2>(), w_H.as<double2>(), ldh, w_cs.as<double2>(),
+                                         w_sn.as<double2>(), w_g.as<double2>(), scal + 3, w_ap.as<double2>(),
+                                         stream)) {
+                    launch_dots(n, j + 1, V, n, w_w.as<double2>(), w_h1.as<double2>(), nullptr, stream);
+                    launch_update(n, j + 1, V, n, w_h1.as<double2>(), w_w.as<double2>(), stream);
+                    launch_dots(n, j + 1, V, n, w_w.as<double2>(), w_h2.as<double2>(), nullptr, stream);
+                    launch_update(n, j + 1, V, n, w_h2.as<double2>(), w_w.as<double2>(), stream);
+                    launch_nrm2(n, w_w.as<double2>(), scal + 2, nullptr, stream);
+                    launch_hcol_finish(j, w_h1.as<double2>(), w_h2.as<double2>(), scal + 2, w_H.as<double2>(), ldh,
+                                       stream);
+                    launch_scale_copy(n, w_w.as<double2>(), scal + 2, V + (size_t)(j + 1) * n, stream,
+                                      w_vf.as<float2>());
+                    launch_givens(j, w_H.as<double2>(), ldh, w_cs.as<double2>(), w_sn.as<double2>(),
+                                  w_g.as<double2>(), scal + 3, stream);
+                }
                 jdone = j + 1;
                 const double res = read_scalar(3);
                 if (!(res / gn > opt.inner_tol)) break;

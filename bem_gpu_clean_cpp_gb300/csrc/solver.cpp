@@ -462,7 +462,7 @@ size_t bem_solver_s::device_bytes() const {
                            &tiles[1].recs, &tiles[1].rec_ptr, &tiles[1].cols, &tiles[1].col_cnt,
                            &d_A, &d_B, &d_cpart, &d_bpart, &d_x, &d_beta, &d_near_ptr, &d_near_ids,
                            &w_V, &w_H, &w_cs, &w_sn, &w_g, &w_y, &w_h1, &w_h2, &w_w, &w_t, &w_r, &w_gv, &w_vf,
-                           &w_part, &w_scal, &x_Ahi, &x_Alo, &x_vlo, &x_tlo, &w_d, &q_A, &q_B, &q_tau, &q_work, &q_info,
+                           &w_part, &w_scal, &x_Ahi, &x_Alo, &x_vlo, &x_tlo, &w_d, &w_ap, &q_A, &q_B, &q_tau, &q_work, &q_info,
                            &f_rows_f, &f_rows_d, &f_part, &f_near, &f_out, &f_u};
     size_t b = 0;
     for (const DevMem *d : all) b += d->bytes;
@@ -489,6 +489,8 @@ size_t bem_solver_s::estimate_bytes(int N, int E, int M, int S, int method, cons
         b += 16 * n * (m + 1) + 16 * (m + 1) * m + 16 * 6 * (m + 1);
         b += 16 * n * 2 + 8 * r + 16 * r + 16 * std::max(n, r);
         b += 16 * n * (size_t)std::max(gemv_h_splits((int)r, N), gemv_h_f64_splits((int)r, N)) + 64;
+        b += 8 * n * (size_t)std::max(0, normal_op_clusters(N) - 2 * gemv_h_splits((int)r, N));
+        b += 48 * (m + 1) * 160;                                                     // Arnoldi step partials
     } else {
         b += 8 * r * n + 8 * r * s + 64 * n + (64u << 20);               // QR copy, tau, library workspace
     }

@@ -81,6 +81,7 @@ struct bem_solver_s {
     // TF32x3 block products: head/tail planes of A (valid for the current
     // assembly) and the tails of the right-hand blocks
     bem::DevMem x_Ahi, x_Alo, x_vlo, x_tlo, w_d;
+    bem::DevMem w_ap;   // partial sums of the cooperative Arnoldi step
     bool tf32_split_valid = false;
     double *h_pinned = nullptr;
     // QR workspace
