@@ -209,9 +209,12 @@ __device__ __forceinline__ bool pair_is_near(int row, int N, int4 nd, float4 xh,
 //   2 pi; r - r_c = (r^2 - r_c^2) / (r + r_c) where r^2 - r_c^2 =
 //   (d - d_c).(d + d_c) is a quadratic in the Duffy radius with coefficients
 //   free of cancellation, so the per-point term is accurate to ~1e-7 of
-//   k (r - r_c) <= k * diam.  Then wrapped as in kPhaseWrap.
+//   k (r - r_c) <= k * diam.  sin and cos then come from sincos_acc instead
+//   of the fast intrinsic.  Used when k * extent > kAccKd or k * longest edge
+//   > kAccKh (coarse meshes at high frequency, whose oscillating sums cancel).
 constexpr double kWrapKh = 0.75;    // k * longest edge above which the point phase is wrapped
-constexpr double kAccKd = 40.0;     // k * extent above which the phase is split (kPhaseAcc)
+constexpr double kAccKd = 40.0;     // k * extent above which kPhaseAcc is used
+constexpr double kAccKh = 1.2;      // k * longest edge above which kPhaseAcc is used
 enum { kPhaseShift = 0, kPhaseWrap = 1, kPhaseAcc = 2 };
 
 struct PairPhase {
@@ -279,12 +282,40 @@ __device__ __forceinline__ float wrap_phase(float y) {
     return __fmaf_rn(-n, kC2F, __fmaf_rn(-n, kC1F, y));
 }
 
-// Phase argument of a point at distance r; q = r^2 - r_c^2 (kPhaseAcc only).
+// sin and cos to ~1e-7 absolute for |y| < 400 (kPhaseAcc): quadrant
+// j = round(2y/pi), z = y - j pi/2 by a two-constant Cody-Waite FMA (P1 = pi/2
+// cut to 16 significant bits, P2 = fl(pi/2 - P1)), then the Taylor series of
+// sin (to z^9) and cos (to z^8) on |z| <= pi/4, whose truncation errors are
+// 2e-9 and 3e-8, and the quadrant's swap and signs.  The fast __sincosf is
+// documented at 2^-21.41 absolute on [-pi, pi]; on coarse meshes at high
+// frequency the quadrature sums cancel and that error shows in the matrix.
+__device__ __forceinline__ void sincos_acc(float y, float *sn, float *cs) {
+    constexpr float k2OverPi = 0.6366197723675814f, kRound = 12582912.0f;
+    constexpr float kP1 = 1.570770263671875f, kP2 = 2.6063122277264483e-05f;
+    const float t = __fmaf_rn(y, k2OverPi, kRound);
+    const float j = __fsub_rn(t, kRound);
+    const unsigned qd = __float_as_uint(t) & 3u;      // j mod 4 (t's last mantissa bits)
+    const float z = __fmaf_rn(-j, kP2, __fmaf_rn(-j, kP1, y));
+    const float z2 = z * z;
+    const float ps = fmaf(z2, fmaf(z2, fmaf(z2, fmaf(z2, 2.7557319223985893e-06f, -1.984126984126984e-04f),
+                                             8.333333333333333e-03f), -0.16666666666666666f), 1.0f) * z;
+    const float pc = fmaf(z2, fmaf(z2, fmaf(z2, fmaf(z2, 2.48015873015873e-05f, -1.388888888888889e-03f),
+                                             4.1666666666666664e-02f), -0.5f), 1.0f);
+    const float s0 = (qd & 1u) ? pc : ps, c0 = (qd & 1u) ? ps : pc;
+    *sn = (qd & 2u) ? -s0 : s0;
+    *cs = ((qd + 1u) & 2u) ? -c0 : c0;
+}
+
+// sin and cos of the phase of a point at distance r; q = r^2 - r_c^2
+// (kPhaseAcc only).
 template <int PH>
-__device__ __forceinline__ float phase_arg(float k, float r, float q, const PairPhase &pp) {
-    if (PH == kPhaseAcc) return wrap_phase(fmaf(k, __fdividef(q, r + pp.rc), pp.yc));
-    const float y = fmaf(k, r, pp.c1) + pp.c2;
-    return PH == kPhaseWrap ? wrap_phase(y) : y;
+__device__ __forceinline__ void phase_sincos(float k, float r, float q, const PairPhase &pp, float *sn, float *cs) {
+    if (PH == kPhaseAcc) {
+        sincos_acc(fmaf(k, __fdividef(q, r + pp.rc), pp.yc), sn, cs);
+    } else {
+        const float y = fmaf(k, r, pp.c1) + pp.c2;
+        __sincosf(PH == kPhaseWrap ? wrap_phase(y) : y, sn, cs);
+    }
 }
 
 struct SumsF {
@@ -317,7 +348,7 @@ __device__ __forceinline__ void far_sums_f32(float3 d3, float3 e1, float3 e2, fl
             const float uz = fmaf(t.y, e2.z, fmaf(t.x, e1.z, -coff.z));
             dq = fmaf(uz, dz + d3.z + coff.z, fmaf(uy, dy + d3.y + coff.y, ux * (dx + d3.x + coff.x)));
         }
-        __sincosf(phase_arg<PH>(k, r, dq, pp), &sn, &cs);
+        phase_sincos<PH>(k, r, dq, pp, &sn, &cs);
         float gr = cs * ri, gi = -sn * ri;            // 4 pi G
         float hq = hgt * ri;                          // dr/dn
         float tr = fmaf(gi, k, -gr * ri);             // 4 pi G (-1/r - ik)
@@ -383,7 +414,7 @@ __device__ __forceinline__ void far_sums_f32_o6(float3 d3, float3 e1, float3 e2,
             const float kr = k * r;
             float sn, cs;
             const float q = PH == kPhaseAcc ? fmaf(fmaf(qa, rho, qb), rho, pp.c0) : 0.f;
-            __sincosf(phase_arg<PH>(k, r, q, pp), &sn, &cs);
+            phase_sincos<PH>(k, r, q, pp, &sn, &cs);
             const float A = fmaf(kr, sn, cs);      // c + kr s
             const float Bv = fmaf(kr, cs, -sn);    // kr c - s
             const float ri3 = ri * ri * ri;
@@ -689,7 +720,7 @@ bool far_variant_fits(int prec, int tc, int variant) {
 }
 
 int far_phase_mode(const Physics &ph) {
-    if (ph.k * ph.extent > kAccKd) return kPhaseAcc;
+    if (ph.k * ph.extent > kAccKd || ph.k * ph.max_edge > kAccKh) return kPhaseAcc;
     if (ph.k * ph.max_edge > kWrapKh) return kPhaseWrap;
     return kPhaseShift;
 }

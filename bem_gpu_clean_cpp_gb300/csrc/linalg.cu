@@ -502,43 +502,63 @@ arnoldi_step_kernel(int n, int j, double2 *__restrict__ V, size_t ldv, double2 *
     const int per = (n + nb - 1) / nb;
     const int i0 = min(n, b * per), i1 = min(n, i0 + per);
     const int k = j + 1;                              // basis vectors in use
-    __shared__ double sr_[kArNT / 32], si_[kArNT / 32];
+    constexpr int kQB = 8;                            // dot products per block reduction
+    __shared__ double sr_[kQB][kArNT / 32], si_[kQB][kArNT / 32];
     extern __shared__ double2 hs[];                   // k coefficients
-    // partial dots of this CTA's slice: part[q * nb + b] for q < k
+    const int lane = tid & 31, warp = tid >> 5;
+    // partial dots of this CTA's slice, kQB basis vectors per pass:
+    // out_part[q * nb + b] for q < k
     auto partial_dots = [&](double2 *out_part) {
-        for (int q = 0; q < k; q++) {
-            const double2 *v = V + (size_t)q * ldv;
-            double a = 0.0, c = 0.0;
+        for (int q0 = 0; q0 < k; q0 += kQB) {
+            double a[kQB], c[kQB];
+#pragma unroll
+            for (int u = 0; u < kQB; u++) a[u] = c[u] = 0.0;
             for (int i = i0 + tid; i < i1; i += kArNT) {
-                const double2 x = v[i], y = w[i];
-                a += x.x * y.x + x.y * y.y;   // conj(v) w
-                c += x.x * y.y - x.y * y.x;
+                const double2 y = w[i];
+#pragma unroll
+                for (int u = 0; u < kQB; u++) {
+                    if (q0 + u < k) {
+                        const double2 x = V[(size_t)(q0 + u) * ldv + i];
+                        a[u] += x.x * y.x + x.y * y.y;   // conj(v) w
+                        c[u] += x.x * y.y - x.y * y.x;
+                    }
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kQB; u++) {
+                for (int o = 16; o > 0; o >>= 1) {
+                    a[u] += __shfl_xor_sync(0xffffffffu, a[u], o);
+                    c[u] += __shfl_xor_sync(0xffffffffu, c[u], o);
+                }
+                if (lane == 0) { sr_[u][warp] = a[u]; si_[u][warp] = c[u]; }
+            }
+            __syncthreads();
+            if (tid < kQB && q0 + tid < k) {
+                double ta = 0.0, tc = 0.0;
+                for (int t = 0; t < kArNT / 32; t++) { ta += sr_[tid][t]; tc += si_[tid][t]; }
+                out_part[(size_t)(q0 + tid) * nb + b] = make_double2(ta, tc);
+            }
+            __syncthreads();
+        }
+    };
+    // h[q] = sum over the CTAs' partials (one warp per q, fixed order), into
+    // shared memory and, from CTA 0, into hout
+    auto reduce_dots = [&](const double2 *in_part, double2 *hout) {
+        for (int q = warp; q < k; q += kArNT / 32) {
+            double a = 0.0, c = 0.0;
+            for (int t = lane; t < nb; t += 32) {
+                const double2 p = in_part[(size_t)q * nb + t];
+                a += p.x;
+                c += p.y;
             }
             for (int o = 16; o > 0; o >>= 1) {
                 a += __shfl_xor_sync(0xffffffffu, a, o);
                 c += __shfl_xor_sync(0xffffffffu, c, o);
             }
-            if ((tid & 31) == 0) { sr_[tid >> 5] = a; si_[tid >> 5] = c; }
-            __syncthreads();
-            if (tid == 0) {
-                double ta = 0.0, tc = 0.0;
-                for (int t = 0; t < kArNT / 32; t++) { ta += sr_[t]; tc += si_[t]; }
-                out_part[(size_t)q * nb + b] = make_double2(ta, tc);
+            if (lane == 0) {
+                hs[q] = make_double2(a, c);
+                if (b == 0) hout[q] = hs[q];
             }
-            __syncthreads();
-        }
-    };
-    // h[q] = sum over CTAs (fixed order), into shared memory and, from CTA 0, into hout
-    auto reduce_dots = [&](const double2 *in_part, double2 *hout) {
-        for (int q = tid; q < k; q += kArNT) {
-            double a = 0.0, c = 0.0;
-            for (int t = 0; t < nb; t++) {
-                const double2 p = in_part[(size_t)q * nb + t];
-                a += p.x;
-                c += p.y;
-            }
-            hs[q] = make_double2(a, c);
-            if (b == 0) hout[q] = hs[q];
         }
         __syncthreads();
     };
@@ -569,20 +589,21 @@ arnoldi_step_kernel(int n, int j, double2 *__restrict__ V, size_t ldv, double2 *
         double a = 0.0;
         for (int i = i0 + tid; i < i1; i += kArNT) a += w[i].x * w[i].x + w[i].y * w[i].y;
         for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-        if ((tid & 31) == 0) sr_[tid >> 5] = a;
+        if (lane == 0) sr_[0][warp] = a;
         __syncthreads();
         if (tid == 0) {
             double t = 0.0;
-            for (int q = 0; q < kArNT / 32; q++) t += sr_[q];
+            for (int q = 0; q < kArNT / 32; q++) t += sr_[0][q];
             p3[b] = make_double2(t, 0.0);
         }
     }
     grid.sync();
     __shared__ double nrm_s;
-    if (tid == 0) {
+    if (warp == 0) {
         double t = 0.0;
-        for (int q = 0; q < nb; q++) t += p3[q].x;
-        nrm_s = sqrt(t);
+        for (int q = lane; q < nb; q += 32) t += p3[q].x;
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (lane == 0) nrm_s = sqrt(t);
     }
     __syncthreads();
     const double nrm = nrm_s;

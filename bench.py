@@ -390,10 +390,12 @@ def run_reference(args):
 # ---------------------------------------------------------------------------
 # Our arm
 # ---------------------------------------------------------------------------
-# Algorithmic bytes per launch of the HBM-bound kernels (A is (N+M) x N c64).
+# Algorithmic bytes per launch of the HBM-bound kernels (A is (N+M) x N c64);
+# normal_op reads A once for w = A^H (A v) (v in, w out).
 def kernel_bytes(name, R, N):
     a = 8.0 * R * N
-    return {"gemv_c64": a + 16.0 * N + 8.0 * R,
+    return {"normal_op": a + 24.0 * N,
+            "gemv_c64": a + 16.0 * N + 8.0 * R,
             "gemv_h_c64": a + 8.0 * R + 16.0 * N,
             "resid": a + 16.0 * N + 32.0 * R,
             "gemv_h_f64": a + 16.0 * R + 16.0 * N}.get(name)

@@ -188,16 +188,18 @@ def test_new_sources_reuse_assembly(bemlib, prec):
     assert rel_err(A2, Ab) < (1e-14 if prec == 1 else 1e-6)
 
 
-@pytest.mark.parametrize("radius,k,mode", [(0.7, 6.0, "wrap"), (1.0, 25.0, "split"), (0.6, 30.0, "split")])
+@pytest.mark.parametrize("radius,k,mode", [(0.7, 4.0, "wrap"), (0.7, 7.0, "split"), (1.0, 25.0, "split"),
+                                           (0.6, 30.0, "split")])
 def test_c64_phase_modes_match_oracle(bemlib, orc, radius, k, mode):
     """The FP32 quadrature's phase modes: per-point wrap (k times the longest
-    edge above 0.75) and the split accurate phase (k times the extent above
-    40), on coarse meshes where kr reaches ~90, against the FP64 oracle."""
+    edge in (0.75, 1.2]) and the split accurate phase with the polynomial
+    sin/cos (k times the extent above 40 or k times the longest edge above
+    1.2), on coarse meshes where kr reaches ~90, against the FP64 oracle."""
     p, f = icosphere(2, radius)
     chief = np.array([[0.1, 0.05, -0.2], [-0.15, 0.2, 0.1]]) * radius
     edge = max(np.linalg.norm(p[f[:, a]] - p[f[:, b]], axis=1).max() for a, b in ((0, 1), (1, 2), (2, 0)))
     extent = np.linalg.norm(np.ptp(np.vstack([p, chief]), axis=0))
-    assert k * edge > 0.75 and ((k * extent > 40) == (mode == "split"))
+    assert k * edge > 0.75 and ((k * extent > 40 or k * edge > 1.2) == (mode == "split"))
     s = bemlib.Solver()
     s.set_geometry(p, f, chief=chief)
     s.set_sources(SRCS)
