@@ -478,6 +478,33 @@ __global__ void set_scalar_c_kernel(double2 *__restrict__ dst, const double *__r
 inline int blocks(long long n, int t) { return (int)((n + t - 1) / t); }
 
 
+// w[c] = sum over ns partial vectors (part[t * N + c], c64) in FP64, for many
+// partials: a CTA covers 32 columns, its 8 warps take every 8th partial with
+// lanes on consecutive columns (coalesced), then the warps' sums are added in
+// a fixed order.
+__global__ void __launch_bounds__(256)
+sum_many_splits_kernel(int N, int ns, const float2 *__restrict__ part, double2 *__restrict__ w) {
+    __shared__ double2 acc[8][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int c = blockIdx.x * 32 + lane;
+    double a = 0.0, b = 0.0;
+    if (c < N) {
+#pragma unroll 4
+        for (int t = warp; t < ns; t += 8) {
+            const float2 v = part[(size_t)t * N + c];
+            a += v.x;
+            b += v.y;
+        }
+    }
+    acc[warp][lane] = make_double2(a, b);
+    __syncthreads();
+    if (warp == 0 && c < N) {
+        double x = 0.0, y = 0.0;
+        for (int q = 0; q < 8; q++) { x += acc[q][lane].x; y += acc[q][lane].y; }
+        w[c] = make_double2(x, y);
+    }
+}
+
 // ---- one Arnoldi step of the refined solver in one cooperative launch ----
 // For basis vectors V_0..V_j (FP64, column stride ldv) and w = A^H A v_j:
 // classical Gram-Schmidt twice (h1 = V^H w, w -= V h1, h2 = V^H w,
@@ -891,7 +918,7 @@ bool launch_normal_op(int R, int N, const float2 *A, size_t lda, const float2 *v
     cfg.numAttrs = 1;
     CUDA_TRY(cudaLaunchKernelEx(&cfg, normal_op_kernel, R, N, A, lda, v, rpc, ngroups, part));
     count_launch();
-    sum_splits_kernel<float2, double2><<<blocks(N, 256), 256, 0, st>>>(N, ncl, part, w);
+    sum_many_splits_kernel<<<blocks(N, 32), 256, 0, st>>>(N, ncl, part, w);
     count_launch();
     KERNEL_CHECK();
     return true;
