@@ -1032,31 +1032,60 @@ void launch_rhs_from_beta(const RowPoints &rows, double k, const DevSource *srcs
 }
 
 // Near pairs of every row (the pairs pair_is_near flags, which the far kernel
-// skips): count pass (ids == nullptr: cnt[row]) and fill pass (ids[ptr[row]..]
-// in increasing element order).  One warp per row, ballot over 32 elements.
-__global__ void near_list_kernel(RowPoints rows, int N, GeoTables geo, const int *__restrict__ ptr,
+// skips).  Candidates come from a uniform grid over the element centroids
+// whose cell edge is at least the largest near radius and the longest element
+// (NearGrid, built on the host): every element that can be near a row point
+// has its centroid in the 27 cells around the point's cell, and pair_is_near
+// decides exactly as in the far kernel.  Count pass (ids == nullptr:
+// cnt[row]) and fill pass (ids[ptr[row]..], cells in fixed order, elements
+// in increasing order within a cell).  One warp per row, ballot over 32
+// candidates.
+__global__ void near_list_kernel(RowPoints rows, int N, GeoTables geo, NearGrid grid, const int *__restrict__ ptr,
                                  int *__restrict__ cnt, int *__restrict__ ids) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int row = blockIdx.x * kNearWarps + warp;
     if (row >= rows.R) return;
     const float4 xh = rows.f[2 * (size_t)row];
+    const double *xd = rows.d + 3 * (size_t)row;
+    int c[3];
+    for (int a = 0; a < 3; a++) {
+        const int v = (int)floor((xd[a] - grid.lo[a]) * grid.inv_cell);
+        c[a] = min(max(v, 0), grid.dim[a] - 1);
+    }
     int n = 0;
-    for (int e0 = 0; e0 < geo.E; e0 += 32) {
-        const int e = e0 + lane;
-        bool flag = false;
-        if (e < geo.E) flag = pair_is_near(row, N, geo.elems[e], xh, geo.geo_f + (size_t)kGeoF * e);
-        const unsigned mask = __ballot_sync(0xffffffffu, flag);
-        if (ids && flag) ids[ptr[row] + n + __popc(mask & ((1u << lane) - 1u))] = e;
-        n += __popc(mask);
+    for (int dz = -1; dz <= 1; dz++) {
+        const int z = c[2] + dz;
+        if (z < 0 || z >= grid.dim[2]) continue;
+        for (int dy = -1; dy <= 1; dy++) {
+            const int y = c[1] + dy;
+            if (y < 0 || y >= grid.dim[1]) continue;
+            for (int dx = -1; dx <= 1; dx++) {
+                const int x = c[0] + dx;
+                if (x < 0 || x >= grid.dim[0]) continue;
+                const size_t cell = ((size_t)z * grid.dim[1] + y) * grid.dim[0] + x;
+                const int cb = grid.cell_start[cell], ce = grid.cell_start[cell + 1];
+                for (int e0 = cb; e0 < ce; e0 += 32) {
+                    bool flag = false;
+                    int e = 0;
+                    if (e0 + lane < ce) {
+                        e = grid.cell_elems[e0 + lane];
+                        flag = pair_is_near(row, N, geo.elems[e], xh, geo.geo_f + (size_t)kGeoF * e);
+                    }
+                    const unsigned mask = __ballot_sync(0xffffffffu, flag);
+                    if (ids && flag) ids[ptr[row] + n + __popc(mask & ((1u << lane) - 1u))] = e;
+                    n += __popc(mask);
+                }
+            }
+        }
     }
     if (!ids && lane == 0) cnt[row] = n;
 }
 
-void launch_near_list(const RowPoints &rows, int N, const GeoTables &geo, const int *d_ptr, int *d_cnt,
-                      int *d_ids, cudaStream_t st) {
+void launch_near_list(const RowPoints &rows, int N, const GeoTables &geo, const NearGrid &grid, const int *d_ptr,
+                      int *d_cnt, int *d_ids, cudaStream_t st) {
     if (rows.R <= 0) return;
-    const dim3 grid((rows.R + kNearWarps - 1) / kNearWarps);
-    near_list_kernel<<<grid, 32 * kNearWarps, 0, st>>>(rows, N, geo, d_ptr, d_cnt, d_ids);
+    const dim3 g((rows.R + kNearWarps - 1) / kNearWarps);
+    near_list_kernel<<<g, 32 * kNearWarps, 0, st>>>(rows, N, geo, grid, d_ptr, d_cnt, d_ids);
     count_launch();
     KERNEL_CHECK();
 }

@@ -85,11 +85,21 @@ void launch_near_assembly(int prec, const RowPoints &rows, int N, const GeoTable
                           const void *beta_part, int ntiles, const DevSource *srcs, int S,
                           double2 *B, double2 *beta_out, const int *near_ptr, const int *near_ids,
                           cudaStream_t st);
+// Uniform grid over element centroids for the near-pair search: cell edge
+// 1/inv_cell, dim[0] x dim[1] x dim[2] cells from corner lo, elements of cell
+// c at cell_elems[cell_start[c] .. cell_start[c+1]).
+struct NearGrid {
+    double lo[3];
+    double inv_cell;
+    int dim[3];
+    const int *cell_start;
+    const int *cell_elems;
+};
 // The pairs the far kernel skips (pair_is_near): with d_ids null, d_cnt[row]
 // = number of near elements of the row; else the ids are written at
 // d_ids[d_ptr[row]..].
-void launch_near_list(const RowPoints &rows, int N, const GeoTables &geo, const int *d_ptr, int *d_cnt,
-                      int *d_ids, cudaStream_t st);
+void launch_near_list(const RowPoints &rows, int N, const GeoTables &geo, const NearGrid &grid, const int *d_ptr,
+                      int *d_cnt, int *d_ids, cudaStream_t st);
 // B[s*R + row] = p_inc_s(x_row) - beta[row]: the right-hand sides of an
 // assembled system for a new set of sources (no element integrals).
 void launch_rhs_from_beta(const RowPoints &rows, double k, const DevSource *srcs, int S,

@@ -212,8 +212,44 @@ void bem_solver_s::ensure_geo() {
 void bem_solver_s::ensure_near_list() {
     ensure_geo();
     if (near_valid) return;
+    // Grid of element centroids: cell edge >= the largest near radius
+    // (near_eta x element diameter) and >= the longest element (vertex pairs),
+    // over the box of all row points and nodes; at most ~4M cells.
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (size_t i = 0; i < h_rows.size(); i++) {
+        lo[i % 3] = std::min(lo[i % 3], h_rows[i]);
+        hi[i % 3] = std::max(hi[i % 3], h_rows[i]);
+    }
+    double cell = std::max(1.0, opt.near_eta) * max_edge * 1.01 + 1e-12;
+    const double span = std::max({hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2], 1e-12});
+    cell = std::max(cell, span / 160.0);
+    int dim[3];
+    for (int a = 0; a < 3; a++) dim[a] = std::max(1, (int)std::floor((hi[a] - lo[a]) / cell) + 1);
+    const size_t ncell = (size_t)dim[0] * dim[1] * dim[2];
+    std::vector<int> cid(E), start(ncell + 1, 0), order(E);
+    for (int e = 0; e < E; e++) {
+        int c[3];
+        for (int a = 0; a < 3; a++) {
+            const double m = (h_nodes[3 * (size_t)h_elems[3 * e] + a] + h_nodes[3 * (size_t)h_elems[3 * e + 1] + a] +
+                              h_nodes[3 * (size_t)h_elems[3 * e + 2] + a]) / 3.0;
+            c[a] = std::min(std::max((int)std::floor((m - lo[a]) / cell), 0), dim[a] - 1);
+        }
+        cid[e] = (int)(((size_t)c[2] * dim[1] + c[1]) * dim[0] + c[0]);
+        start[cid[e] + 1]++;
+    }
+    for (size_t c = 0; c < ncell; c++) start[c + 1] += start[c];
+    {
+        std::vector<int> fill(start.begin(), start.end() - 1);
+        for (int e = 0; e < E; e++) order[fill[cid[e]]++] = e;   // increasing e within a cell
+    }
+    d_grid_start.ensure(sizeof(int) * (ncell + 1));
+    d_grid_elems.ensure(sizeof(int) * std::max(1, E));
+    CUDA_TRY(cudaMemcpyAsync(d_grid_start.p, start.data(), sizeof(int) * (ncell + 1), cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemcpyAsync(d_grid_elems.p, order.data(), sizeof(int) * E, cudaMemcpyHostToDevice, stream));
+    NearGrid grid{{lo[0], lo[1], lo[2]}, 1.0 / cell, {dim[0], dim[1], dim[2]}, d_grid_start.as<int>(),
+                  d_grid_elems.as<int>()};
     d_near_ptr.ensure(sizeof(int) * ((size_t)R + 1));
-    launch_near_list(row_points(), N, geo_tables(), nullptr, d_near_ptr.as<int>(), nullptr, stream);
+    launch_near_list(row_points(), N, geo_tables(), grid, nullptr, d_near_ptr.as<int>(), nullptr, stream);
     std::vector<int> cnt(R);
     CUDA_TRY(cudaMemcpyAsync(cnt.data(), d_near_ptr.p, sizeof(int) * R, cudaMemcpyDeviceToHost, stream));
     CUDA_TRY(cudaStreamSynchronize(stream));
@@ -224,8 +260,9 @@ void bem_solver_s::ensure_near_list() {
     }
     CUDA_TRY(cudaMemcpyAsync(d_near_ptr.p, ptr.data(), sizeof(int) * (R + 1), cudaMemcpyHostToDevice, stream));
     d_near_ids.ensure(sizeof(int) * std::max(1, ptr[R]));
-    launch_near_list(row_points(), N, geo_tables(), d_near_ptr.as<int>(), nullptr, d_near_ids.as<int>(), stream);
-    CUDA_TRY(cudaStreamSynchronize(stream));   // ptr (host) must outlive the copy
+    launch_near_list(row_points(), N, geo_tables(), grid, d_near_ptr.as<int>(), nullptr, d_near_ids.as<int>(),
+                     stream);
+    CUDA_TRY(cudaStreamSynchronize(stream));   // host arrays must outlive the copies
     near_valid = true;
 }
 
@@ -460,7 +497,7 @@ size_t bem_solver_s::device_bytes() const {
     const DevMem *all[] = {&d_nodes, &d_rows_f, &d_rows_d, &d_elems, &d_bc, &d_geo_f, &d_geo_d, &d_srcs,
                            &tiles[0].recs, &tiles[0].rec_ptr, &tiles[0].cols, &tiles[0].col_cnt,
                            &tiles[1].recs, &tiles[1].rec_ptr, &tiles[1].cols, &tiles[1].col_cnt,
-                           &d_A, &d_B, &d_cpart, &d_bpart, &d_x, &d_beta, &d_near_ptr, &d_near_ids,
+                           &d_A, &d_B, &d_cpart, &d_bpart, &d_x, &d_beta, &d_near_ptr, &d_near_ids, &d_grid_start, &d_grid_elems,
                            &w_V, &w_H, &w_cs, &w_sn, &w_g, &w_y, &w_h1, &w_h2, &w_w, &w_t, &w_r, &w_gv, &w_vf,
                            &w_part, &w_scal, &x_Ahi, &x_Alo, &x_vlo, &x_tlo, &w_d, &w_ap, &q_A, &q_B, &q_tau, &q_work, &q_info,
                            &f_rows_f, &f_rows_d, &f_part, &f_near, &f_out, &f_u};
@@ -477,7 +514,7 @@ size_t bem_solver_s::estimate_bytes(int N, int E, int M, int S, int method, cons
     b += 24 * n + 24 * r + 32 * r + 16 * e + 48 * e;                  // nodes, rows, elements, bc
     b += sizeof(float4) * kGeoFloat4 * e + sizeof(double) * kGeoDouble * e;
     b += 3 * e * sizeof(TileRec) + 4 * (ntiles + 1) + 4 * n + 4 * ntiles;   // an element touches <= 3 tiles
-    b += 4 * (r + 1) + 256 * r;                                              // near-pair list (typ. < 64 per row)
+    b += 4 * (r + 1) + 256 * r + 4 * e + (16u << 20);                       // near-pair list and search grid
     b += 8 * lda * r + 16 * r * s + 12 * ntiles * r + 16 * n * s + 16 * r + 48 * s;
     if (method == BEM_SOLVE_BLOCK_GMRES) {
         const size_t m = (size_t)std::max(1, std::min(o.max_iter, 200));

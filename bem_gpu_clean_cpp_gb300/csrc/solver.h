@@ -56,7 +56,7 @@ struct bem_solver_s {
     double geo_eta = -1.0;   // near_eta the element tables were built with
     // near pairs per row (CSR), valid for the current geometry and geo_eta
     bool near_valid = false;
-    bem::DevMem d_near_ptr, d_near_ids;
+    bem::DevMem d_near_ptr, d_near_ids, d_grid_start, d_grid_elems;
     double max_edge = 0.0;   // longest element edge
     double extent = 0.0;     // diagonal of the box around nodes and CHIEF points
 
