@@ -61,6 +61,7 @@ def parse_args():
                     help="precision: the headline workload (one plane wave); rhs: perturbed ellipsoid, "
                          "8 kHz, 256 point sources solved together (block GMRES); freq: 64 frequencies of "
                          "uneven mesh size as one batch; serve: Poisson request stream through the server")
+    ap.add_argument("--sources", type=int, default=256, help="rhs: point sources (the configuration has 256)")
     ap.add_argument("--slots", type=int, default=8, help="freq/serve: requests in flight at once")
     ap.add_argument("--rate", type=float, default=2.0, help="serve: mean request arrivals per second")
     ap.add_argument("--requests", type=int, default=40, help="serve: requests in the stream")
@@ -131,7 +132,7 @@ def icosphere(subdiv: int, radius: float = 1.0):
 
 
 WORKLOAD_RHS = ("perturbed ellipsoid 0.075/0.09/0.11 m (SH l<=8, 5%), geodesic nu=39 (N=15212, E=30420), "
-                "8 kHz, 256 Fibonacci point sources at 1 m, 32 CHIEF, block GMRES")
+                "8 kHz, Fibonacci point sources at 1 m (256), 32 CHIEF, block GMRES")
 
 
 def workload_rhs(args):
@@ -145,7 +146,7 @@ def workload_rhs(args):
     th = np.arccos(1 - 2 * u[:, 1])
     ph = 2 * np.pi * u[:, 2]
     chief = np.stack([r * np.sin(th) * np.cos(ph), r * np.sin(th) * np.sin(ph), r * np.cos(th)], axis=1)
-    srcs = [("point", s, 1.0) for s in bem.fibonacci_sphere(256, 1.0)]
+    srcs = [("point", s, 1.0) for s in bem.fibonacci_sphere(args.sources, 1.0)]
     bc = np.tile(np.array([0, 1, 0], dtype=np.complex128), (elems.shape[0], 1))
     k = 2 * np.pi * 8000.0 / 343.21
     return pts, elems, chief, srcs, k, bc
