@@ -851,6 +851,44 @@ __device__ int build_leaves(const double *h, const double *x, double eta, int de
 // Warp-cooperative FP64 integration over the leaves; the result is valid in
 // every lane.  Returns g (before the i*rho*omega factor), h, c, scaled by
 // |J|/(4 pi) as in the far path.
+// sin and cos in FP64 for the near-field quadrature: quadrant j = round(2y/pi),
+// z = y - j pi/2 by a three-constant Cody-Waite reduction with FMAs (P1 =
+// fl(pi/2), P2 = fl(pi/2 - P1), P3 = fl(pi/2 - P1 - P2)), then the Taylor
+// series of sin to z^17 and cos to z^18 on |z| <= pi/4 (truncation below
+// 1e-18) and the quadrant's swap and signs.  Near pairs have kr of order one,
+// so the reduction is short and exact; this replaces the general-argument
+// library call on the FP64 pipe, which GB300 runs at ~1/64 of FP32.
+__device__ __forceinline__ void sincos_near(double y, double *sn, double *cs) {
+    const double j = rint(y * 0.6366197723675814);
+    double z = fma(-j, 1.5707963267948966, y);
+    z = fma(-j, 6.123233995736766e-17, z);
+    z = fma(-j, -1.4973849048591698e-33, z);
+    const double z2 = z * z;
+    double ps = 2.8114572543455206e-15;
+    ps = fma(ps, z2, -7.647163731819816e-13);
+    ps = fma(ps, z2, 1.6059043836821613e-10);
+    ps = fma(ps, z2, -2.505210838544172e-08);
+    ps = fma(ps, z2, 2.7557319223985893e-06);
+    ps = fma(ps, z2, -0.0001984126984126984);
+    ps = fma(ps, z2, 0.008333333333333333);
+    ps = fma(ps, z2, -0.16666666666666666);
+    ps = fma(ps * z2, z, z);
+    double pc = -1.5619206968586225e-16;
+    pc = fma(pc, z2, 4.779477332387385e-14);
+    pc = fma(pc, z2, -1.1470745597729725e-11);
+    pc = fma(pc, z2, 2.08767569878681e-09);
+    pc = fma(pc, z2, -2.755731922398589e-07);
+    pc = fma(pc, z2, 2.48015873015873e-05);
+    pc = fma(pc, z2, -0.001388888888888889);
+    pc = fma(pc, z2, 0.041666666666666664);
+    pc = fma(pc, z2, -0.5);
+    pc = fma(pc, z2, 1.0);
+    const unsigned q = (unsigned)((long long)j & 3);
+    const double s0 = (q & 1u) ? pc : ps, c0 = (q & 1u) ? ps : pc;
+    *sn = (q & 2u) ? -s0 : s0;
+    *cs = ((q + 1u) & 2u) ? -c0 : c0;
+}
+
 __device__ void near_integrate(const double *h, const double *x, double k, int collapse,
                                const Leaf *leaves, int nl, int nq, NearOut &o) {
     const int lane = threadIdx.x & 31;
@@ -870,11 +908,12 @@ __device__ void near_integrate(const double *h, const double *x, double k, int c
         double x2 = t.c[1] + s1 * ea1 + s2 * eb1;
         double d[3];
         for (int dd = 0; dd < 3; dd++) d[dd] = h[dd] - x[dd] + x1 * h[3 + dd] + x2 * h[6 + dd];
-        double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-        double ri = 1.0 / r;
+        const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        const double ri = rsqrt(r2);
+        const double r = r2 * ri;
         double drdn = (d[0] * n[0] + d[1] * n[1] + d[2] * n[2]) * ri;
         double sn, cs;
-        sincos(k * r, &sn, &cs);
+        sincos_near(k * r, &sn, &cs);
         double gr = cs * ri, gi = -sn * ri;
         double tr = gi * k - gr * ri, ti = -(gr * k + gi * ri);
         double dgr = tr * drdn, dgi = ti * drdn;
