@@ -709,7 +709,6 @@ normal_op_kernel(int R, int N, const float2 *__restrict__ A, size_t lda, const f
     float2 *vs = no_smem, *ws = no_smem + kNoW;
     __shared__ float red[kNoRB][2][kNoNT / 32];
     __shared__ float tot[2][kNoRB * 2];      // this CTA's row sums, double-buffered; read by the peers
-    __shared__ float tsum[kNoRB * 2];        // the cluster's row sums t_r
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int c0 = q * kNoW;
     for (int i = tid; i < kNoW; i += kNoNT) {
@@ -760,15 +759,19 @@ normal_op_kernel(int R, int N, const float2 *__restrict__ A, size_t lda, const f
             tot[par][tid] = t;
         }
         cluster.sync();   // every CTA's row sums of this group are in its tot[par]
-        if (tid < 2 * kNoRB) {
-            float t = 0.f;
-            for (int p = 0; p < C; p++) t += cluster.map_shared_rank(&tot[par][0], p)[tid];
-            tsum[tid] = t;
+        // every thread adds the C CTAs' sums itself (broadcast reads, same
+        // order everywhere): no further barrier before the update
+        float ts[2 * kNoRB];
+#pragma unroll
+        for (int u = 0; u < 2 * kNoRB; u++) ts[u] = 0.f;
+        for (int p = 0; p < C; p++) {
+            const float *peer = cluster.map_shared_rank(&tot[par][0], p);
+#pragma unroll
+            for (int u = 0; u < 2 * kNoRB; u++) ts[u] += peer[u];
         }
-        __syncthreads();
 #pragma unroll
         for (int rb = 0; rb < kNoRB; rb++) {
-            const float tr = tsum[2 * rb], ti = tsum[2 * rb + 1];
+            const float tr = ts[2 * rb], ti = ts[2 * rb + 1];
 #pragma unroll
             for (int i = 0; i < kNoCPT; i++) {
                 const float2 y = a[rb][i];

@@ -90,7 +90,7 @@ def test_near_singular_assembly_matches_oracle(bemlib, orc, eta, depth):
     assert rel_err(A32, Ao) < TOL32
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5])
 @pytest.mark.parametrize("order", [6, 5])
 def test_far_kernel_launch_shapes(bemlib, orc, variant, order):
     """Every far-kernel launch shape (and both the unrolled 6x6 path and the
