@@ -78,6 +78,15 @@ class mesh {
     }
     // extensions (no reference counterpart)
     int readObjRobust(const char *file) { return report(bem_mesh_read_obj_robust(h_, file), "readObjRobust"); }
+    int readPly(const char *file) { return report(bem_mesh_read_ply(h_, file), "readPly"); }
+    // Consistent winding with (p1-p3) x (p2-p3) into the body; returns the
+    // number of flipped elements, or -1 on failure.
+    int orient() {
+        int flipped = 0;
+        return report(bem_mesh_orient(h_, &flipped, nullptr, nullptr, nullptr, nullptr), "orient") == EXIT_SUCCESS
+                   ? flipped
+                   : -1;
+    }
     int setCHIEF(const std::vector<cartCoord> &pts) {
         std::vector<double> c;
         for (const cartCoord &p : pts) c.insert(c.end(), {p.coords[0], p.coords[1], p.coords[2]});
