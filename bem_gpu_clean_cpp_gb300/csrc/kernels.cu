@@ -795,8 +795,10 @@ constexpr int kMaxDepth = 4;
 constexpr int kMaxLeaves = 256;        // 4^kMaxDepth
 constexpr int kNearWarps = 4;
 
+// A leaf triangle in the element's (xi1, xi2) coordinates; its corners are
+// multiples of 2^-depth (depth <= 4), exact in float.
 struct Leaf {
-    double a[2], b[2], c[2];
+    float a[2], b[2], c[2];
 };
 
 struct NearOut {
@@ -807,49 +809,80 @@ __device__ __forceinline__ void xi_point(const double *h, double x1, double x2, 
     for (int d = 0; d < 3; d++) y[d] = h[d] + x1 * h[3 + d] + x2 * h[6 + d];
 }
 
-// Lane 0 builds the leaf list of a near-singular pair (depth-first, children
-// in the order (a,ab,ca), (ab,b,bc), (ca,bc,c), (ab,bc,ca)).
-__device__ int build_leaves(const double *h, const double *x, double eta, int depth_max,
-                            Leaf *leaves) {
-    struct Item { Leaf t; int depth; };
-    Item stack[3 * kMaxDepth + 2];
-    int sp = 0, nl = 0;
-    stack[sp++] = {{{1.0, 0.0}, {0.0, 1.0}, {0.0, 0.0}}, 0};
-    while (sp > 0) {
-        Item it = stack[--sp];
-        bool split = false;
-        if (it.depth < depth_max) {
-            double ya[3], yb[3], yc[3], cen[3];
-            xi_point(h, it.t.a[0], it.t.a[1], ya);
-            xi_point(h, it.t.b[0], it.t.b[1], yb);
-            xi_point(h, it.t.c[0], it.t.c[1], yc);
-            xi_point(h, (it.t.a[0] + it.t.b[0] + it.t.c[0]) / 3.0, (it.t.a[1] + it.t.b[1] + it.t.c[1]) / 3.0, cen);
-            double lab = 0, lbc = 0, lca = 0, dc = 0;
-            for (int d = 0; d < 3; d++) {
-                lab += (ya[d] - yb[d]) * (ya[d] - yb[d]);
-                lbc += (yb[d] - yc[d]) * (yb[d] - yc[d]);
-                lca += (yc[d] - ya[d]) * (yc[d] - ya[d]);
-                dc += (cen[d] - x[d]) * (cen[d] - x[d]);
-            }
-            double diam = sqrt(fmax(lab, fmax(lbc, lca)));
-            split = sqrt(dc) < eta * diam;
-        }
-        if (split) {
-            const Leaf &t = it.t;
-            double ab[2] = {0.5 * (t.a[0] + t.b[0]), 0.5 * (t.a[1] + t.b[1])};
-            double bc[2] = {0.5 * (t.b[0] + t.c[0]), 0.5 * (t.b[1] + t.c[1])};
-            double ca[2] = {0.5 * (t.c[0] + t.a[0]), 0.5 * (t.c[1] + t.a[1])};
-            int d1 = it.depth + 1;
-            // push in reverse so that children pop in order 0, 1, 2, 3
-            stack[sp++] = {{{ab[0], ab[1]}, {bc[0], bc[1]}, {ca[0], ca[1]}}, d1};
-            stack[sp++] = {{{ca[0], ca[1]}, {bc[0], bc[1]}, {t.c[0], t.c[1]}}, d1};
-            stack[sp++] = {{{ab[0], ab[1]}, {t.b[0], t.b[1]}, {bc[0], bc[1]}}, d1};
-            stack[sp++] = {{{t.a[0], t.a[1]}, {ab[0], ab[1]}, {ca[0], ca[1]}}, d1};
-        } else if (nl < kMaxLeaves) {
-            leaves[nl++] = it.t;
-        }
+// Corners of the sub-triangle reached from the element by the child indices
+// in code (two bits per level, level i in bits 2i..2i+1); children of (a, b, c)
+// are (a,ab,ca), (ab,b,bc), (ca,bc,c), (ab,bc,ca).
+__device__ __forceinline__ Leaf leaf_from_code(int code, int depth) {
+    float ax = 1.f, ay = 0.f, bx = 0.f, by = 1.f, cx = 0.f, cy = 0.f;
+    for (int i = 0; i < depth; i++) {
+        const int k = (code >> (2 * i)) & 3;
+        const float abx = 0.5f * (ax + bx), aby = 0.5f * (ay + by);
+        const float bcx = 0.5f * (bx + cx), bcy = 0.5f * (by + cy);
+        const float cax = 0.5f * (cx + ax), cay = 0.5f * (cy + ay);
+        if (k == 0) { bx = abx; by = aby; cx = cax; cy = cay; }
+        else if (k == 1) { ax = abx; ay = aby; cx = bcx; cy = bcy; }
+        else if (k == 2) { ax = cax; ay = cay; bx = bcx; by = bcy; }
+        else { ax = abx; ay = aby; bx = bcx; by = bcy; cx = cax; cy = cay; }
     }
-    return nl;
+    return Leaf{{ax, ay}, {bx, by}, {cx, cy}};
+}
+
+// The leaf list of a near-singular pair, built by the whole warp breadth
+// first: at each level the lanes test the frontier's triangles in parallel
+// (split while |centroid - x| < eta * diameter and depth < depth_max, as the
+// reference-style recursion does), leaves and children are compacted with
+// ballots.  cur/nxt: per-warp scratch of kMaxLeaves codes each.  Returns the
+// number of leaves in every lane.
+__device__ int build_leaves_warp(const double *h, const double *x, double eta, int depth_max, Leaf *leaves,
+                                 int *cur, int *nxt) {
+    const int lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    if (lane == 0) cur[0] = 0;
+    __syncwarp();
+    int ncur = 1, nl = 0;
+    for (int depth = 0; depth <= depth_max && ncur > 0; depth++) {
+        int nnext = 0;
+        for (int base = 0; base < ncur; base += 32) {
+            const int i = base + lane;
+            const bool valid = i < ncur;
+            const int code = valid ? cur[i] : 0;
+            const Leaf t = leaf_from_code(code, depth);
+            bool split = false;
+            if (valid && depth < depth_max) {
+                double ya[3], yb[3], yc[3], cen[3];
+                xi_point(h, t.a[0], t.a[1], ya);
+                xi_point(h, t.b[0], t.b[1], yb);
+                xi_point(h, t.c[0], t.c[1], yc);
+                xi_point(h, ((double)t.a[0] + t.b[0] + t.c[0]) / 3.0, ((double)t.a[1] + t.b[1] + t.c[1]) / 3.0, cen);
+                double lab = 0, lbc = 0, lca = 0, dc = 0;
+                for (int d = 0; d < 3; d++) {
+                    lab += (ya[d] - yb[d]) * (ya[d] - yb[d]);
+                    lbc += (yb[d] - yc[d]) * (yb[d] - yc[d]);
+                    lca += (yc[d] - ya[d]) * (yc[d] - ya[d]);
+                    dc += (cen[d] - x[d]) * (cen[d] - x[d]);
+                }
+                split = sqrt(dc) < eta * sqrt(fmax(lab, fmax(lbc, lca)));
+            }
+            const unsigned mleaf = __ballot_sync(0xffffffffu, valid && !split);
+            const unsigned msplit = __ballot_sync(0xffffffffu, split);
+            if (valid && !split) {
+                const int pos = nl + __popc(mleaf & below);
+                if (pos < kMaxLeaves) leaves[pos] = t;
+            }
+            if (split) {
+                const int pos = nnext + 4 * __popc(msplit & below);
+                for (int c = 0; c < 4; c++) nxt[pos + c] = code | (c << (2 * depth));
+            }
+            nl += __popc(mleaf);
+            nnext += 4 * __popc(msplit);
+        }
+        __syncwarp();
+        int *tmp = cur;
+        cur = nxt;
+        nxt = tmp;
+        ncur = nnext;
+    }
+    return min(nl, kMaxLeaves);
 }
 
 // Warp-cooperative FP64 integration over the leaves; the result is valid in
@@ -904,8 +937,8 @@ __device__ void near_integrate(const double *h, const double *x, double k, int c
     for (int idx = lane; idx < nl * nq; idx += 32) {
         const int l = idx / nq, q = idx - l * nq;
         const Leaf &t = leaves[l];
-        double ea0 = t.a[0] - t.c[0], ea1 = t.a[1] - t.c[1];
-        double eb0 = t.b[0] - t.c[0], eb1 = t.b[1] - t.c[1];
+        double ea0 = (double)t.a[0] - t.c[0], ea1 = (double)t.a[1] - t.c[1];
+        double eb0 = (double)t.b[0] - t.c[0], eb1 = (double)t.b[1] - t.c[1];
         double area = fabs(ea0 * eb1 - ea1 * eb0);
         double s1 = c_qd[cv][q][0], s2 = c_qd[cv][q][1], w = c_qd[cv][q][2] * area;
         double x1 = t.c[0] + s1 * ea0 + s2 * eb0;
@@ -980,6 +1013,7 @@ near_assembly_kernel(RowPoints rows, int N, GeoTables geo, Physics ph, int nq, T
                      double2 *__restrict__ beta_out, const int *__restrict__ near_ptr,
                      const int *__restrict__ near_ids) {
     __shared__ Leaf leaves_all[kNearWarps][kMaxLeaves];
+    __shared__ int codes_all[kNearWarps][2][kMaxLeaves];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int row = blockIdx.x * kNearWarps + warp;
     if (row >= rows.R) return;
@@ -1005,10 +1039,10 @@ near_assembly_kernel(RowPoints rows, int N, GeoTables geo, Physics ph, int nq, T
             const int vtx = (row < N) ? (row == ndb.x ? 1 : row == ndb.y ? 2 : row == ndb.z ? 3 : 0) : 0;
             if (vtx) {
                 collapse = vtx;
-                if (lane == 0) leaves[0] = {{1.0, 0.0}, {0.0, 1.0}, {0.0, 0.0}};
+                if (lane == 0) leaves[0] = {{1.f, 0.f}, {0.f, 1.f}, {0.f, 0.f}};
             } else {
-                if (lane == 0) nl = build_leaves(h, x, ph.near_eta, ph.near_depth, leaves);
-                nl = __shfl_sync(0xffffffffu, nl, 0);
+                nl = build_leaves_warp(h, x, ph.near_eta, ph.near_depth, leaves, codes_all[warp][0],
+                                       codes_all[warp][1]);
             }
             __syncwarp();
             NearOut o;
@@ -1255,6 +1289,7 @@ __global__ void __launch_bounds__(32 * kNearWarps)
 field_near_kernel(RowPoints pts, GeoTables geo, Physics ph, int nq, const TU *__restrict__ u, size_t ldu,
                   int S, double2 *__restrict__ near_part) {
     __shared__ Leaf leaves_all[kNearWarps][kMaxLeaves];
+    __shared__ int codes_all[kNearWarps][2][kMaxLeaves];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int p = blockIdx.x * kNearWarps + warp;
     if (p >= pts.R) return;
@@ -1280,8 +1315,7 @@ field_near_kernel(RowPoints pts, GeoTables geo, Physics ph, int nq, const TU *__
                                  __shfl_sync(0xffffffffu, nd.z, b)};
             const double *h = geo.geo_d + (size_t)kGeoD * eb;
             int nl = 0;
-            if (lane == 0) nl = build_leaves(h, x, ph.near_eta, ph.near_depth, leaves);
-            nl = __shfl_sync(0xffffffffu, nl, 0);
+            nl = build_leaves_warp(h, x, ph.near_eta, ph.near_depth, leaves, codes_all[warp][0], codes_all[warp][1]);
             __syncwarp();
             NearOut o;
             near_integrate(h, x, ph.k, 3, leaves, nl, nq, o);
