@@ -390,8 +390,10 @@ void bem_solver_s::assemble(double kk, int precision) {
             CUDA_TRY(cudaEventCreate(&e0));
             CUDA_TRY(cudaEventCreate(&e1));
             float best = 1e30f;
+            int last = -1;
             for (int v = 0; v < far_variants(precision); v++) {
                 if (!far_variant_fits(precision, T.tc_max, v)) continue;
+                last = v;
                 for (int rep = 0; rep < 2; rep++) {
                     CUDA_TRY(cudaEventRecord(e0, stream));
                     launch_far_assembly(precision, row_points(), N, geo_tables(), ts, ph, d_A.p, lda,
@@ -406,9 +408,10 @@ void bem_solver_s::assemble(double kk, int precision) {
             cudaEventDestroy(e0);
             cudaEventDestroy(e1);
             far_tuned[key] = variant;
-            // the final launch must be the chosen shape only if shapes differ in
-            // results; they do not (same sums), so the last launch stands
-            done = true;
+            // The shapes split the c and beta row sums differently (FP32 order),
+            // so the matrix is left by the chosen shape: every assembly of this
+            // problem shape then gives the same bits.
+            done = last == variant;
         }
     }
     if (!done)
