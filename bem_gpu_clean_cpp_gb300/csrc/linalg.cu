@@ -684,10 +684,8 @@ arnoldi_step_kernel(int n, int j, double2 *__restrict__ V, size_t ldv, double2 *
 // products t_r = A_r v, the CTA reduces them, the cluster adds the CTAs' sums
 // through distributed shared memory (one cluster barrier per row group), and
 // the same registers give w += conj(A_r) t_r.  A is read once where A v and
-// A^H t as two kernels read it twice.  One CTA per SM with two register sets:
-// the next row group's loads are issued before this group's barriers, so HBM
-// stays busy through them.  The clusters' partial w are summed in FP64 by
-// sum_many_splits_kernel.
+// A^H t as two kernels read it twice.  The clusters' partial w are summed in
+// FP64 by sum_splits_kernel.
 //
 // Every CTA of a cluster runs the same number of row groups (rows past R are
 // masked, never skipped) and calls the cluster barrier the same number of
@@ -699,7 +697,7 @@ constexpr int kNoW = kNoNT * kNoCPT;   // 5632 columns per CTA
 constexpr int kNoRB = 2;               // rows per group
 constexpr int kNoMaxCluster = 8;
 
-__global__ void __launch_bounds__(kNoNT, 1)
+__global__ void __launch_bounds__(kNoNT, 2)
 normal_op_kernel(int R, int N, const float2 *__restrict__ A, size_t lda, const float2 *__restrict__ v,
                  int rows_per_cluster, int ngroups, float2 *__restrict__ wpart) {
     namespace cg = cooperative_groups;
@@ -721,26 +719,24 @@ normal_op_kernel(int R, int N, const float2 *__restrict__ A, size_t lda, const f
     __syncthreads();
     const int r_begin = cl * rows_per_cluster;
     const int r_end = min(R, r_begin + rows_per_cluster);
-    // the group's A values into registers (masked past the rows and columns)
-    auto load = [&](int g, float2 (&a)[kNoRB][kNoCPT]) {
+    for (int g = 0; g < ngroups; g++) {
+        const int par = g & 1;
+        float2 a[kNoRB][kNoCPT];
+        float pr[kNoRB], pim[kNoRB];
 #pragma unroll
         for (int rb = 0; rb < kNoRB; rb++) {
             const int row = r_begin + g * kNoRB + rb;
             const bool ok = row < r_end;
             const float2 *arow = A + (size_t)(ok ? row : 0) * lda;
+            pr[rb] = pim[rb] = 0.f;
 #pragma unroll
             for (int i = 0; i < kNoCPT; i++) {
                 const int c = c0 + tid + i * kNoNT;
                 a[rb][i] = (ok && c < N) ? __ldcs(arow + c) : make_float2(0.f, 0.f);
             }
         }
-    };
-    auto process = [&](int g, const float2 (&a)[kNoRB][kNoCPT]) {
-        const int par = g & 1;
-        float pr[kNoRB], pim[kNoRB];
 #pragma unroll
         for (int rb = 0; rb < kNoRB; rb++) {
-            pr[rb] = pim[rb] = 0.f;
 #pragma unroll
             for (int i = 0; i < kNoCPT; i++) {
                 const float2 x = vs[tid + i * kNoNT], y = a[rb][i];
@@ -784,18 +780,6 @@ normal_op_kernel(int R, int N, const float2 *__restrict__ A, size_t lda, const f
                 w.y = fmaf(y.x, ti, fmaf(-y.y, tr, w.y));
             }
         }
-    };
-    // Two register sets: the next group's loads are in flight while this
-    // group waits at its barriers.  ngroups is the same for every CTA, so
-    // every CTA calls the cluster barrier equally often.
-    float2 a0[kNoRB][kNoCPT], a1[kNoRB][kNoCPT];
-    load(0, a0);
-    for (int g = 0; g < ngroups; g += 2) {
-        if (g + 1 < ngroups) load(g + 1, a1);
-        process(g, a0);
-        if (g + 1 >= ngroups) break;
-        if (g + 2 < ngroups) load(g + 2, a0);
-        process(g + 1, a1);
     }
     cluster.sync();   // the peers have read tot; shared memory may go
     for (int i = tid; i < kNoW; i += kNoNT) {
@@ -886,7 +870,7 @@ bool launch_arnoldi_step(int n, int j, double2 *V, size_t ldv, double2 *w, float
 int normal_op_clusters(int N) {
     const int C = (N + kNoW - 1) / kNoW;
     if (C > kNoMaxCluster) return 0;
-    return 152 / C;   // one CTA per SM
+    return (2 * 152) / C;
 }
 
 bool launch_normal_op(int R, int N, const float2 *A, size_t lda, const float2 *v, double2 *w, float2 *part,

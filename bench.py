@@ -62,6 +62,8 @@ def parse_args():
                          "8 kHz, 256 point sources solved together (block GMRES); freq: 64 frequencies of "
                          "uneven mesh size as one batch; serve: Poisson request stream through the server")
     ap.add_argument("--sources", type=int, default=256, help="rhs: point sources (the configuration has 256)")
+    ap.add_argument("--max-iter", type=int, default=100, help="rhs: inner GMRES iterations per refinement cycle")
+    ap.add_argument("--inner-tol", type=float, default=1e-4, help="rhs: inner GMRES relative tolerance")
     ap.add_argument("--slots", type=int, default=8, help="freq/serve: requests in flight at once")
     ap.add_argument("--rate", type=float, default=2.0, help="serve: mean request arrivals per second")
     ap.add_argument("--requests", type=int, default=40, help="serve: requests in the stream")
@@ -412,8 +414,8 @@ def run_ours(args):
     pts, elems, chief, src, k, bc, name = select_workload(args)
     if args.config == "rhs":
         method = bem.SOLVE_BLOCK_GMRES
-        opts = dict(near_eta=args.eta, near_depth=args.depth, tol=1e-8, inner_tol=1e-4, max_iter=100,
-                    max_refine=10, block_tol=1e-8, gemm_mode=args.gemm)
+        opts = dict(near_eta=args.eta, near_depth=args.depth, tol=1e-8, inner_tol=args.inner_tol,
+                    max_iter=args.max_iter, max_refine=10, block_tol=1e-8, gemm_mode=args.gemm)
     else:
         d = src[0][1]
         method = bem.SOLVE_GMRES_REFINED
