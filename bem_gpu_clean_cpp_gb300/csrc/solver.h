@@ -122,6 +122,7 @@ struct bem_solver_s {
     void solve_block(bem_solve_info_t *info);
     // GEMM mode of the block solve for S right-hand sides (resolves AUTO).
     static int block_gemm_mode(const bem_options_t &o, int S) {
-        return o.gemm_mode >= 0 ? o.gemm_mode : (S >= 48 ? BEM_GEMM_TF32X3 : BEM_GEMM_SPLIT_BF16);
+        if (o.gemm_mode >= 0) return o.gemm_mode;
+        return S >= 48 ? BEM_GEMM_TF32X3 : S >= 32 ? BEM_GEMM_SPLIT_BF16 : BEM_GEMM_FP32;
     }
 };

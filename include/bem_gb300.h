@@ -193,8 +193,9 @@ enum { BEM_SOLVE_QR = 0, BEM_SOLVE_GMRES_REFINED = 1, BEM_SOLVE_BLOCK_GMRES = 2 
 /* Block-solve GEMMs: FP32 (SIMT), FP32-accurate split-BF16 emulation on the
  * tensor cores (cuBLAS), plain TF32, or TF32x3 (A and the right-hand block
  * split into TF32 head + tail, three TF32 GEMMs: hh + ht + th).  AUTO takes
- * TF32x3 from 48 right-hand sides on (the products are tensor-bound there)
- * and split-BF16 below (HBM-bound: one pass over A per product). */
+ * TF32x3 from 48 right-hand sides on (the products are tensor-bound there),
+ * split-BF16 from 32, and FP32 below 32, where the tensor kernels' wide tiles
+ * are mostly padding and one SIMT pass over A is as fast. */
 enum { BEM_GEMM_AUTO = -1, BEM_GEMM_FP32 = 0, BEM_GEMM_SPLIT_BF16 = 1, BEM_GEMM_TF32 = 2, BEM_GEMM_TF32X3 = 3 };
 
 typedef struct {
