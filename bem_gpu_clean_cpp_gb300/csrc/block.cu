@@ -9,9 +9,7 @@
 //   W  = A^H T  : Wt (2N x 2S) = At Tt,  W_j = (Wt[2j,s] + Wt[2j+1,S+s]) + i (Wt[2j,S+s] - Wt[2j+1,s]).
 // The GEMMs run on the tensor cores with FP32-accurate split-BF16 emulation
 // (cuBLAS CUBLAS_COMPUTE_32F_EMULATED_16BFX9) or, by option, plain FP32 or
-// TF32.  The TF32x3 mode (head/tail TF32 splits, three TF32 products per real
-// product) uses the 3M form instead: separate real planes of Re A, Im A and
-// Re A + Im A, three real products per complex product rather than four.
+// TF32.
 //
 // Precision.  Each right-hand side keeps its own Krylov space.  The inner
 // solve only has to reduce the correction equation's residual by inner_tol,
@@ -62,17 +60,50 @@ __device__ __forceinline__ float tf32_head(float v) {
     return __uint_as_float((__float_as_uint(v) + 0x1000u) & 0xFFFFE000u);
 }
 
-// Vt (2N x 2S) from the N x S complex block V (column-major, ld = N).
+// Vt (2N x 2S) from the N x S complex block V (column-major, ld = N); with
+// Vlo, Vt gets the TF32 heads and Vlo the tails.
 template <typename T>
-__global__ void build_vt_kernel(int N, int S, const T *__restrict__ V, float *__restrict__ Vt) {
+__global__ void build_vt_kernel(int N, int S, const T *__restrict__ V, float *__restrict__ Vt,
+                                float *__restrict__ Vlo) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, s = blockIdx.y;
     if (i >= N) return;
     const double2 v = ld_c(V, (size_t)s * N + i);
     const size_t ld = 2 * (size_t)N;
-    Vt[(size_t)s * ld + 2 * i] = (float)v.x;
-    Vt[(size_t)(S + s) * ld + 2 * i] = (float)v.y;
-    Vt[(size_t)s * ld + 2 * i + 1] = -(float)v.y;
-    Vt[(size_t)(S + s) * ld + 2 * i + 1] = (float)v.x;
+    const size_t o[4] = {(size_t)s * ld + 2 * i, (size_t)(S + s) * ld + 2 * i, (size_t)s * ld + 2 * i + 1,
+                         (size_t)(S + s) * ld + 2 * i + 1};
+    const float val[4] = {(float)v.x, (float)v.y, -(float)v.y, (float)v.x};
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        if (Vlo) {
+            const float h = tf32_head(val[q]);
+            Vt[o[q]] = h;
+            Vlo[o[q]] = val[q] - h;
+        } else {
+            Vt[o[q]] = val[q];
+        }
+    }
+}
+
+// In place: x -> TF32 head, lo -> tail (n floats).
+__global__ void split_tf32_kernel(size_t n, float *__restrict__ x, float *__restrict__ lo) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float v = x[i], h = tf32_head(v);
+        x[i] = h;
+        lo[i] = v - h;
+    }
+}
+
+// hi/lo TF32 planes of the interleaved-real view of A (R rows of N2 = 2N
+// floats, row stride ld floats).
+__global__ void split_a_tf32_kernel(int R, int N2, size_t ld, const float *__restrict__ A, float *__restrict__ hi,
+                                    float *__restrict__ lo) {
+    const size_t total = (size_t)R * N2;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+        const size_t i = (t / N2) * ld + t % N2;
+        const float v = A[i], h = tf32_head(v);
+        hi[i] = h;
+        lo[i] = v - h;
+    }
 }
 
 // Rv = B (the residual of X = 0) and its float packing Tt (R x 2S, real and
@@ -399,82 +430,6 @@ __global__ void binit_g_kernel(int S, int m, const double *__restrict__ nrm, dou
 
 inline dim3 grid2(int n, int S) { return dim3((n + 255) / 256, S); }
 
-// ---- 3M products (TF32x3 mode) ----
-// A = Ar + i Ai, with As = Ar + Ai:  T = A V is  P1 = Ar Vr, P2 = Ai Vi,
-// P3 = As (Vr + Vi),  Tr = P1 - P2, Ti = P3 - P1 - P2;  W = A^H T is
-// Q1 = Ar^T Tr, Q2 = Ai^T Ti, Q3 = As^T (Tr - Ti),  Wr = Q1 + Q2,
-// Wi = Q1 - Q2 - Q3.  Three real products per complex product instead of
-// the four of the interleaved-real form.  Every real operand is kept as a
-// TF32 head and tail plane.
-
-// A planes, each R x N real (row-major, ld = lda): [r_hi, r_lo, i_hi, i_lo, s_hi, s_lo]
-__global__ void split_a3_kernel(int R, int N, size_t lda, const float2 *__restrict__ A, float *__restrict__ P) {
-    const size_t plane = (size_t)R * lda, total = (size_t)R * N;
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
-        const size_t i = (t / N) * lda + t % N;
-        const float2 a = A[i];
-        const float v[3] = {a.x, a.y, a.x + a.y};
-#pragma unroll
-        for (int q = 0; q < 3; q++) {
-            const float h = tf32_head(v[q]);
-            P[(2 * q) * plane + i] = h;
-            P[(2 * q + 1) * plane + i] = v[q] - h;
-        }
-    }
-}
-
-// Planes of a complex block X (n x S, column-major, ld n): [r, i, s] heads and
-// tails, each n x S (ld n), s = r + i (sub: s = r - i).
-template <typename T>
-__global__ void split_b3_kernel(int n, int S, const T *__restrict__ X, bool sub, float *__restrict__ P) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x, s = blockIdx.y;
-    if (i >= n) return;
-    const size_t plane = (size_t)n * S, o = (size_t)s * n + i;
-    const double2 x = ld_c(X, o);
-    const float r = (float)x.x, im = (float)x.y;
-    const float v[3] = {r, im, sub ? r - im : r + im};
-#pragma unroll
-    for (int q = 0; q < 3; q++) {
-        const float h = tf32_head(v[q]);
-        P[(2 * q) * plane + o] = h;
-        P[(2 * q + 1) * plane + o] = v[q] - h;
-    }
-}
-
-// The same for T given as Tt (R x 2S, real block then imaginary block).
-__global__ void split_t3_kernel(int R, int S, const float *__restrict__ Tt, float *__restrict__ P) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x, s = blockIdx.y;
-    if (r >= R) return;
-    const size_t plane = (size_t)R * S, o = (size_t)s * R + r;
-    const float tr = Tt[o], ti = Tt[(size_t)(S + s) * R + r];
-    const float v[3] = {tr, ti, tr - ti};
-#pragma unroll
-    for (int q = 0; q < 3; q++) {
-        const float h = tf32_head(v[q]);
-        P[(2 * q) * plane + o] = h;
-        P[(2 * q + 1) * plane + o] = v[q] - h;
-    }
-}
-
-// Tt real block = P1 - P2 (P1 in place), imaginary block = P3 - P1 - P2 (P3 in place).
-__global__ void combine_t3_kernel(int R, int S, float *Tt, const float *__restrict__ P2) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x, s = blockIdx.y;
-    if (r >= R) return;
-    const size_t o = (size_t)s * R + r, oi = (size_t)(S + s) * R + r;
-    const float p1 = Tt[o], p2 = P2[o], p3 = Tt[oi];
-    Tt[o] = p1 - p2;
-    Tt[oi] = p3 - p1 - p2;
-}
-
-// W (n x S complex) from Q1, Q2, Q3 (n x S each, ld n, consecutive).
-__global__ void combine_w3_kernel(int n, int S, const float *__restrict__ Q, float2 *__restrict__ W) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x, s = blockIdx.y;
-    if (j >= n) return;
-    const size_t plane = (size_t)n * S, o = (size_t)s * n + j;
-    const float q1 = Q[o], q2 = Q[plane + o], q3 = Q[2 * plane + o];
-    W[o] = make_float2(q1 + q2, q1 - q2 - q3);
-}
-
 }  // namespace
 }  // namespace bem
 
@@ -487,81 +442,54 @@ void cublas_ok(cublasStatus_t s, const char *what) {
 }
 }  // namespace
 
-// Tt (R x 2S) = At^T Vt (first) and/or Wt (2N x 2S) = At Tt (second) on the
-// interleaved-real view of A (modes FP32, split-BF16 and TF32; TF32x3 runs as
-// 3M products, apply_a_3m / apply_ah_3m).
-static void normal_gemms(bem_solver_s &sv, int mode, const float *Vt, float *Tt, float *Wt, int S, bool first,
-                         bool second) {
+// Tt (R x 2S) = At^T Vt (first) and/or Wt (2N x 2S) = At Tt (second).  In
+// TF32x3 mode Vt holds the heads and Vlo the tails of the right-hand block,
+// and Tt is split in place (Tlo) before the second product; each product is
+// head*tail + tail*head + head*head, smallest terms first.
+static void normal_gemms(bem_solver_s &sv, int mode, const float *Vt, const float *Vlo, float *Tt, float *Tlo,
+                         float *Wt, int S, bool first, bool second) {
     const float one = 1.f, zero = 0.f;
     const int N = sv.N, R = sv.R;
     const float *At = reinterpret_cast<const float *>(sv.d_A.p);
     const int ldat = (int)(2 * sv.lda);
+    const bool x3 = mode == BEM_GEMM_TF32X3;
     const cublasComputeType_t ct = mode == BEM_GEMM_FP32         ? CUBLAS_COMPUTE_32F
                                    : mode == BEM_GEMM_SPLIT_BF16 ? CUBLAS_COMPUTE_32F_EMULATED_16BFX9
                                                                  : CUBLAS_COMPUTE_32F_FAST_TF32;
+    const float *Ahi = x3 ? sv.x_Ahi.as<float>() : At, *Alo = x3 ? sv.x_Alo.as<float>() : nullptr;
+    auto gemm1 = [&](const float *a, const float *b, const float *beta) {
+        cublas_ok(cublasGemmEx(sv.cublas, CUBLAS_OP_T, CUBLAS_OP_N, R, 2 * S, 2 * N, &one, a, CUDA_R_32F, ldat, b,
+                               CUDA_R_32F, 2 * N, beta, Tt, CUDA_R_32F, R, ct, CUBLAS_GEMM_DEFAULT),
+                  "GEMM A V");
+    };
+    auto gemm2 = [&](const float *a, const float *b, const float *beta) {
+        cublas_ok(cublasGemmEx(sv.cublas, CUBLAS_OP_N, CUBLAS_OP_N, 2 * N, 2 * S, R, &one, a, CUDA_R_32F, ldat, b,
+                               CUDA_R_32F, R, beta, Wt, CUDA_R_32F, 2 * N, ct, CUBLAS_GEMM_DEFAULT),
+                  "GEMM A^H T");
+    };
     if (first) {
         BEM_PROF("gemm_AV", sv.stream);
-        cublas_ok(cublasGemmEx(sv.cublas, CUBLAS_OP_T, CUBLAS_OP_N, R, 2 * S, 2 * N, &one, At, CUDA_R_32F, ldat, Vt,
-                               CUDA_R_32F, 2 * N, &zero, Tt, CUDA_R_32F, R, ct, CUBLAS_GEMM_DEFAULT),
-                  "GEMM A V");
+        if (x3) {
+            gemm1(Ahi, Vlo, &zero);
+            gemm1(Alo, Vt, &one);
+            gemm1(Ahi, Vt, &one);
+        } else {
+            gemm1(At, Vt, &zero);
+        }
     }
     if (second) {
         BEM_PROF("gemm_AhT", sv.stream);
-        cublas_ok(cublasGemmEx(sv.cublas, CUBLAS_OP_N, CUBLAS_OP_N, 2 * N, 2 * S, R, &one, At, CUDA_R_32F, ldat, Tt,
-                               CUDA_R_32F, R, &zero, Wt, CUDA_R_32F, 2 * N, ct, CUBLAS_GEMM_DEFAULT),
-                  "GEMM A^H T");
+        if (x3) {
+            const size_t n = 2 * (size_t)R * S;
+            split_tf32_kernel<<<(unsigned)std::min<size_t>((n + 255) / 256, 4096), 256, 0, sv.stream>>>(n, Tt, Tlo);
+            count_launch();
+            gemm2(Ahi, Tlo, &zero);
+            gemm2(Alo, Tt, &one);
+            gemm2(Ahi, Tt, &one);
+        } else {
+            gemm2(At, Tt, &zero);
+        }
     }
-}
-
-// C (m x n, ldc) = op(A) B with A and B given as TF32 head/tail planes:
-// head*tail + tail*head + head*head, smallest terms first.
-static void tf32x3_gemm(bem_solver_s &sv, cublasOperation_t opA, int m, int n, int k, const float *Ahi,
-                        const float *Alo, int lda, const float *Bhi, const float *Blo, int ldb, float *C, int ldc) {
-    const float one = 1.f, zero = 0.f;
-    auto g = [&](const float *a, const float *b, const float *beta) {
-        cublas_ok(cublasGemmEx(sv.cublas, opA, CUBLAS_OP_N, m, n, k, &one, a, CUDA_R_32F, lda, b, CUDA_R_32F, ldb,
-                               beta, C, CUDA_R_32F, ldc, CUBLAS_COMPUTE_32F_FAST_TF32, CUBLAS_GEMM_DEFAULT),
-                  "GEMM (3M, TF32x3)");
-    };
-    g(Ahi, Blo, &zero);
-    g(Alo, Bhi, &one);
-    g(Ahi, Bhi, &one);
-}
-
-// Tt (R x 2S) = A X for the complex block X (n x S) by the 3M products.
-// Ap: the six A planes (R x lda each); Bp: scratch for six n x S planes;
-// P2: scratch R x S.
-template <typename T>
-static void apply_a_3m(bem_solver_s &sv, const T *X, const float *Ap, float *Bp, float *Tt, float *P2) {
-    const int N = sv.N, R = sv.R, S = sv.S;
-    const int lda = (int)sv.lda;
-    const size_t ap = (size_t)R * sv.lda, bp = (size_t)N * S;
-    BEM_PROF("gemm_AV", sv.stream);
-    split_b3_kernel<T><<<grid2(N, S), 256, 0, sv.stream>>>(N, S, X, false, Bp);
-    count_launch();
-    tf32x3_gemm(sv, CUBLAS_OP_T, R, S, N, Ap, Ap + ap, lda, Bp, Bp + bp, N, Tt, R);                    // Ar Vr
-    tf32x3_gemm(sv, CUBLAS_OP_T, R, S, N, Ap + 2 * ap, Ap + 3 * ap, lda, Bp + 2 * bp, Bp + 3 * bp, N, P2, R);
-    tf32x3_gemm(sv, CUBLAS_OP_T, R, S, N, Ap + 4 * ap, Ap + 5 * ap, lda, Bp + 4 * bp, Bp + 5 * bp, N,
-                Tt + (size_t)S * R, R);                                                            // As Vs
-    combine_t3_kernel<<<grid2(R, S), 256, 0, sv.stream>>>(R, S, Tt, P2);
-    count_launch();
-}
-
-// W (n x S complex) = A^H T for T given as Tt, by the 3M products.  Bp:
-// scratch for six R x S planes; Q: scratch 3 n x S.
-static void apply_ah_3m(bem_solver_s &sv, const float *Tt, const float *Ap, float *Bp, float *Q, float2 *W) {
-    const int N = sv.N, R = sv.R, S = sv.S;
-    const int lda = (int)sv.lda;
-    const size_t ap = (size_t)R * sv.lda, bp = (size_t)R * S, qp = (size_t)N * S;
-    BEM_PROF("gemm_AhT", sv.stream);
-    split_t3_kernel<<<grid2(R, S), 256, 0, sv.stream>>>(R, S, Tt, Bp);
-    count_launch();
-    tf32x3_gemm(sv, CUBLAS_OP_N, N, S, R, Ap, Ap + ap, lda, Bp, Bp + bp, R, Q, N);                     // Ar^T Tr
-    tf32x3_gemm(sv, CUBLAS_OP_N, N, S, R, Ap + 2 * ap, Ap + 3 * ap, lda, Bp + 2 * bp, Bp + 3 * bp, R, Q + qp, N);
-    tf32x3_gemm(sv, CUBLAS_OP_N, N, S, R, Ap + 4 * ap, Ap + 5 * ap, lda, Bp + 4 * bp, Bp + 5 * bp, R,
-                Q + 2 * qp, N);                                                                    // As^T Td
-    combine_w3_kernel<<<grid2(N, S), 256, 0, sv.stream>>>(N, S, Q, W);
-    count_launch();
 }
 
 void bem_solver_s::solve_block(bem_solve_info_t *info) {
@@ -594,51 +522,22 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
     const float2 *A = d_A.as<float2>();
     const int gmode = block_gemm_mode(opt, S);
     const bool x3 = gmode == BEM_GEMM_TF32X3;
-    // TF32x3 runs as 3M products on real planes: A's six planes (built once
-    // per assembly), six planes of the right-hand block, R x S scratch
-    float *A3 = nullptr, *B3 = nullptr, *P2 = nullptr;
+    float *Vlo = nullptr, *Tlo = nullptr;
     if (x3) {
-        x_vlo.ensure(sizeof(float) * 6 * (size_t)std::max(n, R) * S);
-        x_tlo.ensure(sizeof(float) * (size_t)R * S);
-        B3 = x_vlo.as<float>();
-        P2 = x_tlo.as<float>();
+        x_vlo.ensure(sizeof(float) * 4 * NS);
+        x_tlo.ensure(sizeof(float) * 2 * (size_t)R * S);
+        Vlo = x_vlo.as<float>();
+        Tlo = x_tlo.as<float>();
         if (!tf32_split_valid) {
-            x_Ahi.ensure(sizeof(float) * 6 * lda * (size_t)R);
-            split_a3_kernel<<<152 * 16, 256, 0, stream>>>(R, n, lda, A, x_Ahi.as<float>());
+            x_Ahi.ensure(sizeof(float) * 2 * lda * (size_t)R);
+            x_Alo.ensure(sizeof(float) * 2 * lda * (size_t)R);
+            split_a_tf32_kernel<<<152 * 16, 256, 0, stream>>>(R, 2 * n, 2 * lda, reinterpret_cast<const float *>(A),
+                                                              x_Ahi.as<float>(), x_Alo.as<float>());
             count_launch();
             KERNEL_CHECK();
             tf32_split_valid = true;
         }
-        A3 = x_Ahi.as<float>();
     }
-    // T = A X into Tt, and W = A^H T from Tt, for the mode in use
-    auto apply_a_d = [&](const double2 *X) {
-        if (x3) {
-            apply_a_3m<double2>(*this, X, A3, B3, Tt, P2);
-        } else {
-            build_vt_kernel<double2><<<grid2(n, S), 256, 0, stream>>>(n, S, X, Vt);
-            count_launch();
-            normal_gemms(*this, gmode, Vt, Tt, Wt, S, true, false);
-        }
-    };
-    auto apply_a_f = [&](const float2 *X) {
-        if (x3) {
-            apply_a_3m<float2>(*this, X, A3, B3, Tt, P2);
-        } else {
-            build_vt_kernel<float2><<<grid2(n, S), 256, 0, stream>>>(n, S, X, Vt);
-            count_launch();
-            normal_gemms(*this, gmode, Vt, Tt, Wt, S, true, false);
-        }
-    };
-    auto apply_ah = [&]() {
-        if (x3) {
-            apply_ah_3m(*this, Tt, A3, B3, Wt, W);
-        } else {
-            normal_gemms(*this, gmode, Vt, Tt, Wt, S, false, true);
-            combine_w_kernel<<<grid2(n, S), 256, 0, stream>>>(n, S, Wt, W);
-            count_launch();
-        }
-    };
     std::vector<double> h_bn(S), h_gn(S), h_res(S);
     std::vector<int> h_kk(S);
     auto rd = [&](const double *d, std::vector<double> &h) {
@@ -668,13 +567,16 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
                                                                  d_B.as<double2>(), Rv, Tt);
             count_launch(2);
         } else {
-            apply_a_d(Dc);
+            build_vt_kernel<double2><<<grid2(n, S), 256, 0, stream>>>(n, S, Dc, Vt, Vlo);
+            count_launch();
+            normal_gemms(*this, gmode, Vt, Vlo, Tt, Tlo, Wt, S, true, false);
             resid_update_kernel<<<grid2(R, S), 256, 0, stream>>>(R, S, Rv, Tt);
             count_launch();
         }
-        apply_ah();
+        normal_gemms(*this, gmode, Vt, Vlo, Tt, Tlo, Wt, S, false, true);
+        combine_w_kernel<<<grid2(n, S), 256, 0, stream>>>(n, S, Wt, W);
         bnrm2_kernel<<<S, 256, 0, stream>>>(n, W, nrm_g);
-        count_launch();
+        count_launch(2);
         KERNEL_CHECK();
         rd(nrm_g, h_gn);
         if (refs == 0) h_bn = h_gn;
@@ -690,11 +592,13 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
         int j = 0;
         for (; j < m; j++) {
             const float2 *Vj = V + (size_t)j * NS;
-            apply_a_f(Vj);
-            apply_ah();
+            build_vt_kernel<float2><<<grid2(n, S), 256, 0, stream>>>(n, S, Vj, Vt, Vlo);
+            count_launch();
+            normal_gemms(*this, gmode, Vt, Vlo, Tt, Tlo, Wt, S, true, true);
             const dim3 gd(S, (j + 1 + kDotLB - 1) / kDotLB);
             {
                 BEM_PROF("block_arnoldi", stream);
+                combine_w_kernel<<<grid2(n, S), 256, 0, stream>>>(n, S, Wt, W);
                 bdots_kernel<<<gd, 256, 0, stream>>>(n, S, j + 1, V, W, w_h1.as<double2>(), ldv);
                 bcombo_kernel<<<grid2(n, S), 256, 0, stream>>>(n, S, j + 1, V, w_h1.as<double2>(), ldv, W);
                 bdots_kernel<<<gd, 256, 0, stream>>>(n, S, j + 1, V, W, w_h2.as<double2>(), ldv);
@@ -704,7 +608,7 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
                 bhess_givens_kernel<<<sb, 128, 0, stream>>>(j, S, m, w_h1.as<double2>(), w_h2.as<double2>(), ldv,
                                                             nrm_w, w_H.as<double2>(), w_cs.as<double2>(),
                                                             w_sn.as<double2>(), w_g.as<double2>(), res);
-                count_launch(7);
+                count_launch(8);
             }
             KERNEL_CHECK();
             rd(res, h_res);

@@ -502,7 +502,7 @@ size_t bem_solver_s::device_bytes() const {
                            &tiles[1].recs, &tiles[1].rec_ptr, &tiles[1].cols, &tiles[1].col_cnt,
                            &d_A, &d_B, &d_cpart, &d_bpart, &d_x, &d_beta, &d_near_ptr, &d_near_ids, &d_grid_start, &d_grid_elems,
                            &w_V, &w_H, &w_cs, &w_sn, &w_g, &w_y, &w_h1, &w_h2, &w_w, &w_t, &w_r, &w_gv, &w_vf,
-                           &w_part, &w_scal, &x_Ahi, &x_vlo, &x_tlo, &w_d, &w_ap, &q_A, &q_B, &q_tau, &q_work, &q_info,
+                           &w_part, &w_scal, &x_Ahi, &x_Alo, &x_vlo, &x_tlo, &w_d, &w_ap, &q_A, &q_B, &q_tau, &q_work, &q_info,
                            &f_rows_f, &f_rows_d, &f_part, &f_near, &f_out, &f_u};
     size_t b = 0;
     for (const DevMem *d : all) b += d->bytes;
@@ -523,7 +523,7 @@ size_t bem_solver_s::estimate_bytes(int N, int E, int M, int S, int method, cons
         const size_t m = (size_t)std::max(1, std::min(o.max_iter, 200));
         b += 16 * n * s * (m + 1) + 16 * s * m * (m + 1) + 16 * s * (4 * m + 4);
         b += 16 * n * s * 2 + 16 * r * s + 16 * n * s + 8 * r * s + 16 * n * s + 40 * s + 16 * n * s;
-        if (block_gemm_mode(o, S) == BEM_GEMM_TF32X3) b += 24 * lda * r + 24 * std::max(n, r) * s + 4 * r * s;
+        if (block_gemm_mode(o, S) == BEM_GEMM_TF32X3) b += 16 * lda * r + 16 * n * s + 8 * r * s;
     } else if (method == BEM_SOLVE_GMRES_REFINED) {
         const size_t m = (size_t)std::max(1, o.max_iter);
         b += 16 * n * (m + 1) + 16 * (m + 1) * m + 16 * 6 * (m + 1);

@@ -78,10 +78,9 @@ struct bem_solver_s {
 
     // GMRES / refinement workspace
     bem::DevMem w_V, w_H, w_cs, w_sn, w_g, w_y, w_h1, w_h2, w_w, w_t, w_r, w_gv, w_vf, w_part, w_scal;
-    // TF32x3 block products (3M): six TF32 head/tail planes of A (real,
-    // imaginary, sum; valid for the current assembly), the six planes of the
-    // right-hand block and the second partial product
-    bem::DevMem x_Ahi, x_vlo, x_tlo, w_d;
+    // TF32x3 block products: head/tail planes of A (valid for the current
+    // assembly) and the tails of the right-hand blocks
+    bem::DevMem x_Ahi, x_Alo, x_vlo, x_tlo, w_d;
     bem::DevMem w_ap;   // partial sums of the cooperative Arnoldi step
     bool tf32_split_valid = false;
     double *h_pinned = nullptr;
