@@ -9,7 +9,9 @@
 //   W  = A^H T  : Wt (2N x 2S) = At Tt,  W_j = (Wt[2j,s] + Wt[2j+1,S+s]) + i (Wt[2j,S+s] - Wt[2j+1,s]).
 // The GEMMs run on the tensor cores with FP32-accurate split-BF16 emulation
 // (cuBLAS CUBLAS_COMPUTE_32F_EMULATED_16BFX9) or, by option, plain FP32 or
-// TF32.
+// TF32.  The TF32x3 products run either on that interleaved form or, by
+// option, in the 3M form: separate real planes of Re A, Im A and Re A + Im A,
+// three real products per complex product instead of four.
 //
 // Precision.  Each right-hand side keeps its own Krylov space.  The inner
 // solve only has to reduce the correction equation's residual by inner_tol,
@@ -430,6 +432,90 @@ __global__ void binit_g_kernel(int S, int m, const double *__restrict__ nrm, dou
 
 inline dim3 grid2(int n, int S) { return dim3((n + 255) / 256, S); }
 
+// ---- 3M form of the TF32x3 products (BEM_GEMM_TF32X3_3M) ----
+// A = Ar + i Ai, As = Ar + Ai.  T = A V:  P1 = Ar Vr, P2 = Ai Vi,
+// P3 = As (Vr + Vi);  Tr = P1 - P2, Ti = P3 - P1 - P2.  W = A^H T:
+// Q1 = Ar^T Tr, Q2 = Ai^T Ti, Q3 = As^T (Tr - Ti);  Wr = Q1 + Q2,
+// Wi = Q1 - Q2 - Q3.  Every real operand is kept as TF32 head and tail
+// planes; a real product is two GEMMs, head(A) [head(B) | tail(B)] (one pass
+// over the head plane of A for both terms) and tail(A) head(B), whose output
+// lands on the second block.
+
+// A's planes, each R x N real (row-major, ld = lda): [r_hi, r_lo, i_hi, i_lo, s_hi, s_lo]
+__global__ void split_a3_kernel(int R, int N, size_t lda, const float2 *__restrict__ A, float *__restrict__ P) {
+    const size_t plane = (size_t)R * lda, total = (size_t)R * N;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+        const size_t i = (t / N) * lda + t % N;
+        const float2 a = A[i];
+        const float v[3] = {a.x, a.y, a.x + a.y};
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+            const float h = tf32_head(v[q]);
+            P[(2 * q) * plane + i] = h;
+            P[(2 * q + 1) * plane + i] = v[q] - h;
+        }
+    }
+}
+
+// Planes of a complex block (n x S): for q = r, i, s the head then the tail
+// (each n x S, ld n), so [head | tail] of q is one n x 2S matrix (plane =
+// 2 n S floats apart).  The complex
+// value is X[s n + i] (ld_c) or, from the packed float form Tt (n x 2S: real
+// block, imaginary block), (Tt[s n + i], Tt[(S + s) n + i]).  s = r + i, or
+// r - i with sub.
+__device__ __forceinline__ void put_planes3(float *__restrict__ P, size_t plane, size_t o, float r, float im,
+                                           bool sub) {
+    const float v[3] = {r, im, sub ? r - im : r + im};
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+        const float h = tf32_head(v[q]);
+        P[(size_t)q * plane + o] = h;
+        P[(size_t)q * plane + plane / 2 + o] = v[q] - h;
+    }
+}
+
+template <typename T>
+__global__ void split_x3_kernel(int n, int S, const T *__restrict__ X, float *__restrict__ P) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, s = blockIdx.y;
+    if (i >= n) return;
+    const size_t o = (size_t)s * n + i;
+    const double2 x = ld_c(X, o);
+    put_planes3(P, 2 * (size_t)n * S, o, (float)x.x, (float)x.y, false);
+}
+
+__global__ void split_t3_kernel(int n, int S, const float *__restrict__ Tt, float *__restrict__ P) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, s = blockIdx.y;
+    if (i >= n) return;
+    const size_t o = (size_t)s * n + i;
+    put_planes3(P, 2 * (size_t)n * S, o, Tt[o], Tt[(size_t)(S + s) * n + i], true);
+}
+
+// C holds the three real products, product q as m x 2S (ld m) at C + 2 q m S,
+// its value the sum of the two blocks.
+__device__ __forceinline__ float prod3(const float *__restrict__ C, size_t mS, int q, size_t o) {
+    const float *c = C + 2 * (size_t)q * mS;
+    return c[o] + c[mS + o];
+}
+
+// Tt (R x 2S) = (P1 - P2 | P3 - P1 - P2).
+__global__ void combine_t3_kernel(int R, int S, const float *__restrict__ C, float *__restrict__ Tt) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x, s = blockIdx.y;
+    if (r >= R) return;
+    const size_t o = (size_t)s * R + r, mS = (size_t)R * S;
+    const float p1 = prod3(C, mS, 0, o), p2 = prod3(C, mS, 1, o), p3 = prod3(C, mS, 2, o);
+    Tt[o] = p1 - p2;
+    Tt[mS + o] = p3 - p1 - p2;
+}
+
+// W (n x S complex) = (Q1 + Q2, Q1 - Q2 - Q3).
+__global__ void combine_w3_kernel(int n, int S, const float *__restrict__ C, float2 *__restrict__ W) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x, s = blockIdx.y;
+    if (j >= n) return;
+    const size_t o = (size_t)s * n + j, mS = (size_t)n * S;
+    const float q1 = prod3(C, mS, 0, o), q2 = prod3(C, mS, 1, o), q3 = prod3(C, mS, 2, o);
+    W[o] = make_float2(q1 + q2, q1 - q2 - q3);
+}
+
 }  // namespace
 }  // namespace bem
 
@@ -492,6 +578,50 @@ static void normal_gemms(bem_solver_s &sv, int mode, const float *Vt, const floa
     }
 }
 
+// C (m x 2S, ld m) for one real product of the 3M form: [Ahi Bhi | Ahi Blo +
+// Alo Bhi], op(A) m x k from the planes Ahi, Alo (ld lda), B = [Bhi | Blo]
+// (k x 2S, ld k).
+static void tf32x3_real(bem_solver_s &sv, cublasOperation_t opA, int m, int k, const float *Ahi, const float *Alo,
+                        const float *B, float *C) {
+    const float one = 1.f, zero = 0.f;
+    const int S = sv.S, lda = (int)sv.lda;
+    cublas_ok(cublasGemmEx(sv.cublas, opA, CUBLAS_OP_N, m, 2 * S, k, &one, Ahi, CUDA_R_32F, lda, B, CUDA_R_32F, k,
+                           &zero, C, CUDA_R_32F, m, CUBLAS_COMPUTE_32F_FAST_TF32, CUBLAS_GEMM_DEFAULT),
+              "GEMM (3M, head)");
+    cublas_ok(cublasGemmEx(sv.cublas, opA, CUBLAS_OP_N, m, S, k, &one, Alo, CUDA_R_32F, lda, B, CUDA_R_32F, k, &one,
+                           C + (size_t)m * S, CUDA_R_32F, m, CUBLAS_COMPUTE_32F_FAST_TF32, CUBLAS_GEMM_DEFAULT),
+              "GEMM (3M, tail)");
+}
+
+// Tt (R x 2S) = A X for the complex block X (N x S) in the 3M form.  Ap: A's
+// six planes; Bp: scratch for six N x S planes; C: scratch 6 R x S.
+template <typename T>
+static void apply_a_3m(bem_solver_s &sv, const T *X, const float *Ap, float *Bp, float *C, float *Tt) {
+    const int N = sv.N, R = sv.R, S = sv.S;
+    const size_t ap = (size_t)R * sv.lda, bp = 2 * (size_t)N * S, cp = 2 * (size_t)R * S;
+    BEM_PROF("gemm_AV", sv.stream);
+    split_x3_kernel<T><<<grid2(N, S), 256, 0, sv.stream>>>(N, S, X, Bp);
+    count_launch();
+    for (int q = 0; q < 3; q++)
+        tf32x3_real(sv, CUBLAS_OP_T, R, N, Ap + 2 * q * ap, Ap + (2 * q + 1) * ap, Bp + q * bp, C + q * cp);
+    combine_t3_kernel<<<grid2(R, S), 256, 0, sv.stream>>>(R, S, C, Tt);
+    count_launch();
+}
+
+// W (N x S complex) = A^H T for T given as Tt (R x 2S), in the 3M form.  Bp:
+// scratch for six R x S planes; C: scratch 6 N x S.
+static void apply_ah_3m(bem_solver_s &sv, const float *Tt, const float *Ap, float *Bp, float *C, float2 *W) {
+    const int N = sv.N, R = sv.R, S = sv.S;
+    const size_t ap = (size_t)R * sv.lda, bp = 2 * (size_t)R * S, cp = 2 * (size_t)N * S;
+    BEM_PROF("gemm_AhT", sv.stream);
+    split_t3_kernel<<<grid2(R, S), 256, 0, sv.stream>>>(R, S, Tt, Bp);
+    count_launch();
+    for (int q = 0; q < 3; q++)
+        tf32x3_real(sv, CUBLAS_OP_N, N, R, Ap + 2 * q * ap, Ap + (2 * q + 1) * ap, Bp + q * bp, C + q * cp);
+    combine_w3_kernel<<<grid2(N, S), 256, 0, sv.stream>>>(N, S, C, W);
+    count_launch();
+}
+
 void bem_solver_s::solve_block(bem_solve_info_t *info) {
     const int n = N, m = std::max(1, std::min(opt.max_iter, 200));
     const int ldv = m + 1;
@@ -521,23 +651,67 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
     float *Vt = w_vf.as<float>(), *Tt = w_t.as<float>(), *Wt = w_part.as<float>();
     const float2 *A = d_A.as<float2>();
     const int gmode = block_gemm_mode(opt, S);
-    const bool x3 = gmode == BEM_GEMM_TF32X3;
-    float *Vlo = nullptr, *Tlo = nullptr;
+    const bool x3 = gmode == BEM_GEMM_TF32X3, x3m = gmode == BEM_GEMM_TF32X3_3M;
+    float *Vlo = nullptr, *Tlo = nullptr, *A3 = nullptr, *B3 = nullptr, *C3 = nullptr;
     if (x3) {
         x_vlo.ensure(sizeof(float) * 4 * NS);
         x_tlo.ensure(sizeof(float) * 2 * (size_t)R * S);
         Vlo = x_vlo.as<float>();
         Tlo = x_tlo.as<float>();
-        if (!tf32_split_valid) {
+        if (tf32_split_mode != gmode) {
             x_Ahi.ensure(sizeof(float) * 2 * lda * (size_t)R);
             x_Alo.ensure(sizeof(float) * 2 * lda * (size_t)R);
             split_a_tf32_kernel<<<152 * 16, 256, 0, stream>>>(R, 2 * n, 2 * lda, reinterpret_cast<const float *>(A),
                                                               x_Ahi.as<float>(), x_Alo.as<float>());
             count_launch();
             KERNEL_CHECK();
-            tf32_split_valid = true;
+            tf32_split_mode = gmode;
         }
+    } else if (x3m) {
+        // A's six planes (built once per assembly), six planes of the
+        // right-hand block, the three products (two blocks each)
+        x_vlo.ensure(sizeof(float) * 6 * (size_t)std::max(n, R) * S);
+        x_tlo.ensure(sizeof(float) * 6 * (size_t)std::max(n, R) * S);
+        B3 = x_vlo.as<float>();
+        C3 = x_tlo.as<float>();
+        if (tf32_split_mode != gmode) {
+            x_Ahi.ensure(sizeof(float) * 6 * lda * (size_t)R);
+            split_a3_kernel<<<152 * 16, 256, 0, stream>>>(R, n, lda, A, x_Ahi.as<float>());
+            count_launch();
+            KERNEL_CHECK();
+            tf32_split_mode = gmode;
+        }
+        A3 = x_Ahi.as<float>();
     }
+    // T = A X into Tt (X: the FP64 correction or an FP32 basis block), and
+    // W = A^H T from Tt, in the mode's form
+    auto apply_a_d = [&](const double2 *Xs) {
+        if (x3m) {
+            apply_a_3m<double2>(*this, Xs, A3, B3, C3, Tt);
+            return;
+        }
+        build_vt_kernel<double2><<<grid2(n, S), 256, 0, stream>>>(n, S, Xs, Vt, Vlo);
+        count_launch();
+        normal_gemms(*this, gmode, Vt, Vlo, Tt, Tlo, Wt, S, true, false);
+    };
+    auto apply_a_f = [&](const float2 *Xs) {
+        if (x3m) {
+            apply_a_3m<float2>(*this, Xs, A3, B3, C3, Tt);
+            return;
+        }
+        build_vt_kernel<float2><<<grid2(n, S), 256, 0, stream>>>(n, S, Xs, Vt, Vlo);
+        count_launch();
+        normal_gemms(*this, gmode, Vt, Vlo, Tt, Tlo, Wt, S, true, false);
+    };
+    auto apply_ah = [&]() {
+        if (x3m) {
+            apply_ah_3m(*this, Tt, A3, B3, C3, W);
+            return;
+        }
+        normal_gemms(*this, gmode, Vt, Vlo, Tt, Tlo, Wt, S, false, true);
+        combine_w_kernel<<<grid2(n, S), 256, 0, stream>>>(n, S, Wt, W);
+        count_launch();
+    };
     std::vector<double> h_bn(S), h_gn(S), h_res(S);
     std::vector<int> h_kk(S);
     auto rd = [&](const double *d, std::vector<double> &h) {
@@ -567,16 +741,13 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
                                                                  d_B.as<double2>(), Rv, Tt);
             count_launch(2);
         } else {
-            build_vt_kernel<double2><<<grid2(n, S), 256, 0, stream>>>(n, S, Dc, Vt, Vlo);
-            count_launch();
-            normal_gemms(*this, gmode, Vt, Vlo, Tt, Tlo, Wt, S, true, false);
+            apply_a_d(Dc);
             resid_update_kernel<<<grid2(R, S), 256, 0, stream>>>(R, S, Rv, Tt);
             count_launch();
         }
-        normal_gemms(*this, gmode, Vt, Vlo, Tt, Tlo, Wt, S, false, true);
-        combine_w_kernel<<<grid2(n, S), 256, 0, stream>>>(n, S, Wt, W);
+        apply_ah();
         bnrm2_kernel<<<S, 256, 0, stream>>>(n, W, nrm_g);
-        count_launch(2);
+        count_launch();
         KERNEL_CHECK();
         rd(nrm_g, h_gn);
         if (refs == 0) h_bn = h_gn;
@@ -592,13 +763,11 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
         int j = 0;
         for (; j < m; j++) {
             const float2 *Vj = V + (size_t)j * NS;
-            build_vt_kernel<float2><<<grid2(n, S), 256, 0, stream>>>(n, S, Vj, Vt, Vlo);
-            count_launch();
-            normal_gemms(*this, gmode, Vt, Vlo, Tt, Tlo, Wt, S, true, true);
+            apply_a_f(Vj);
+            apply_ah();
             const dim3 gd(S, (j + 1 + kDotLB - 1) / kDotLB);
             {
                 BEM_PROF("block_arnoldi", stream);
-                combine_w_kernel<<<grid2(n, S), 256, 0, stream>>>(n, S, Wt, W);
                 bdots_kernel<<<gd, 256, 0, stream>>>(n, S, j + 1, V, W, w_h1.as<double2>(), ldv);
                 bcombo_kernel<<<grid2(n, S), 256, 0, stream>>>(n, S, j + 1, V, w_h1.as<double2>(), ldv, W);
                 bdots_kernel<<<gd, 256, 0, stream>>>(n, S, j + 1, V, W, w_h2.as<double2>(), ldv);
@@ -608,7 +777,7 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
                 bhess_givens_kernel<<<sb, 128, 0, stream>>>(j, S, m, w_h1.as<double2>(), w_h2.as<double2>(), ldv,
                                                             nrm_w, w_H.as<double2>(), w_cs.as<double2>(),
                                                             w_sn.as<double2>(), w_g.as<double2>(), res);
-                count_launch(8);
+                count_launch(7);
             }
             KERNEL_CHECK();
             rd(res, h_res);

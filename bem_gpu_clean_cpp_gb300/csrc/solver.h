@@ -78,11 +78,12 @@ struct bem_solver_s {
 
     // GMRES / refinement workspace
     bem::DevMem w_V, w_H, w_cs, w_sn, w_g, w_y, w_h1, w_h2, w_w, w_t, w_r, w_gv, w_vf, w_part, w_scal;
-    // TF32x3 block products: head/tail planes of A (valid for the current
-    // assembly) and the tails of the right-hand blocks
+    // TF32x3 block products: head/tail planes of A (interleaved form: x_Ahi
+    // and x_Alo; 3M form: six planes in x_Ahi) and scratch for the right-hand
+    // blocks and products
     bem::DevMem x_Ahi, x_Alo, x_vlo, x_tlo, w_d;
     bem::DevMem w_ap;   // partial sums of the cooperative Arnoldi step
-    bool tf32_split_valid = false;
+    int tf32_split_mode = -1;   // BEM_GEMM_* the planes of A were built for (this assembly), -1 none
     double *h_pinned = nullptr;
     // QR workspace
     bem::DevMem q_A, q_B, q_tau, q_work, q_info;
@@ -123,6 +124,6 @@ struct bem_solver_s {
     // GEMM mode of the block solve for S right-hand sides (resolves AUTO).
     static int block_gemm_mode(const bem_options_t &o, int S) {
         if (o.gemm_mode >= 0) return o.gemm_mode;
-        return S >= 48 ? BEM_GEMM_TF32X3 : S >= 32 ? BEM_GEMM_SPLIT_BF16 : BEM_GEMM_FP32;
+        return S >= 128 ? BEM_GEMM_TF32X3_3M : S >= 48 ? BEM_GEMM_TF32X3 : S >= 32 ? BEM_GEMM_SPLIT_BF16 : BEM_GEMM_FP32;
     }
 };
