@@ -133,12 +133,16 @@ int arnoldi_step_blocks();
 bool launch_arnoldi_step(int n, int j, double2 *V, size_t ldv, double2 *w, float2 *vf, double2 *h1, double2 *h2,
                          double2 *H, int ldh, double2 *cs, double2 *sn, double2 *g, double *res, double2 *part,
                          cudaStream_t st);
-// w = A^H (A v) for c64 A with A read once (cluster kernel); v c64, w c128;
-// part: scratch of normal_op_clusters(N) x N c64.  Returns false (nothing
-// launched) when N is above what one cluster covers (45056).
+// w = A^H (A v) for c64 A with A read once (cluster kernel, A streamed by
+// TMA bulk copies); v c64, w c128; part: scratch of normal_op_clusters(N) x N
+// c64.  Returns false (nothing launched) when N is above what one cluster
+// covers (45056).
 int normal_op_clusters(int N);
 bool launch_normal_op(int R, int N, const float2 *A, size_t lda, const float2 *v, double2 *w, float2 *part,
                       cudaStream_t st);
+// True (and the flag cleared) when a normal-operator launch on the current
+// device gave up waiting for one of its copies; synchronises the stream.
+bool normal_op_timed_out(cudaStream_t st);
 int gemv_h_f64_splits(int R, int N);
 // FP64 accumulation variants (the refinement residuals): A is c64 or c128.
 // r = b - A x.  For c64 A the products are exact double-float FP32

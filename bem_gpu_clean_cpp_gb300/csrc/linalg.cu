@@ -10,11 +10,15 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdint>
+#include <cstdlib>
 #include <mutex>
+#include <string>
 
 #include "bem_common.h"
 #include "dfloat.h"
 #include "kernels.h"
+#include "tma.h"
 
 namespace bem {
 
@@ -788,6 +792,158 @@ normal_op_kernel(int R, int N, const float2 *__restrict__ A, size_t lda, const f
     }
 }
 
+// The same product with A streamed through shared memory by bulk
+// asynchronous copies (TMA).  One CTA per SM; CTA q of a cluster owns columns
+// [q kNtW, (q+1) kNtW) with v and its partial w in registers (kNtCPT columns
+// per thread).  Thread 0 keeps kNtNS stages of kNtRPS row segments in flight:
+// stage g % kNtNS is refilled with group g + kNtNS as soon as every thread has
+// copied group g into registers (the CTA barrier of the row reduction), so
+// HBM streams on through the cluster barrier that the row sums need, where
+// the register-loading kernel above issues no loads.
+//
+// A row segment starts at A + row lda + q kNtW: 16-byte aligned because lda
+// is even (the launcher checks) and kNtW is even; its length is rounded up to
+// an even element count, which stays inside the row's lda padding.  Padding
+// and columns past N are masked (never multiplied), so the padding's contents
+// do not matter.  Every wait is bounded; on a timeout the CTA records it in
+// g_normal_op_timeout, issues no further copies, keeps the same barrier
+// sequence as its peers, and drains its copies in flight (bounded again)
+// before exiting.
+constexpr int kNtNT = 512;
+constexpr int kNtCPT = 11;
+constexpr int kNtW = kNtNT * kNtCPT;   // 5632 columns per CTA (= kNoW)
+constexpr int kNtRPS = 2;              // rows per stage (one row group)
+constexpr int kNtNS = 2;               // stages
+constexpr size_t kNtSmem = (size_t)kNtNS * kNtRPS * kNtW * sizeof(float2);   // 180224 B
+constexpr long long kNtWaitCycles = 2000000000LL;                          // ~1 s at 2 GHz
+
+__device__ int g_normal_op_timeout = 0;
+
+__global__ void __launch_bounds__(kNtNT, 1)
+normal_op_tma_kernel(int R, int N, const float2 *__restrict__ A, size_t lda, const float2 *__restrict__ v,
+                     int rows_per_cluster, int ngroups, float2 *__restrict__ wpart) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    const int C = (int)cluster.num_blocks();
+    const int q = (int)cluster.block_rank();
+    const int cl = blockIdx.x / C;
+    extern __shared__ __align__(128) float2 nt_stage[];   // [kNtNS][kNtRPS][kNtW]
+    __shared__ __align__(8) uint64_t full[kNtNS];
+    __shared__ float red[kNtRPS][2][kNtNT / 32];
+    __shared__ float tot[2][kNtRPS * 2];
+    __shared__ int abort_flag;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int c0 = q * kNtW;
+    const int cnt = min(kNtW, N - c0);
+    const uint32_t seg_bytes = (uint32_t)(((cnt + 1) & ~1) * sizeof(float2));
+    const int r_begin = cl * rows_per_cluster;
+    const int r_end = min(R, r_begin + rows_per_cluster);
+    auto group_rows = [&](int g) { return max(0, min(kNtRPS, r_end - (r_begin + g * kNtRPS))); };
+    int last_issued = -1;       // thread 0: the last group whose copies were issued
+    auto issue = [&](int g) {   // thread 0 only
+        const int nr = group_rows(g);
+        if (nr == 0) return;
+        const int s = g % kNtNS;
+        last_issued = g;
+        mbar_arrive_expect_tx(&full[s], nr * seg_bytes);
+        for (int rb = 0; rb < nr; rb++) {
+            const int row = r_begin + g * kNtRPS + rb;
+            bulk_copy_g2s(nt_stage + ((size_t)s * kNtRPS + rb) * kNtW, A + (size_t)row * lda + c0, seg_bytes,
+                          &full[s]);
+        }
+    };
+    if (tid == 0) {
+        for (int s = 0; s < kNtNS; s++) mbar_init(&full[s], 1);
+        abort_flag = 0;
+        mbar_fence_init();
+    }
+    __syncthreads();
+    if (tid == 0)
+        for (int g = 0; g < min(kNtNS, ngroups); g++) issue(g);
+    float2 vr[kNtCPT], wr[kNtCPT];
+#pragma unroll
+    for (int i = 0; i < kNtCPT; i++) {
+        const int c = c0 + tid + i * kNtNT;
+        vr[i] = c < N ? v[c] : make_float2(0.f, 0.f);
+        wr[i] = make_float2(0.f, 0.f);
+    }
+    for (int g = 0; g < ngroups; g++) {
+        const int par = g & 1, s = g % kNtNS;
+        const int nr = group_rows(g);
+        if (nr > 0 && !*(volatile int *)&abort_flag) {
+            if (!mbar_wait_bounded(&full[s], (uint32_t)((g / kNtNS) & 1), kNtWaitCycles, &abort_flag)) {
+                abort_flag = 1;
+                atomicExch(&g_normal_op_timeout, 1);
+            }
+        }
+        const float2 *stg = nt_stage + (size_t)s * kNtRPS * kNtW;
+        float2 a[kNtRPS][kNtCPT];
+        float pr[kNtRPS], pim[kNtRPS];
+#pragma unroll
+        for (int rb = 0; rb < kNtRPS; rb++) {
+            pr[rb] = pim[rb] = 0.f;
+#pragma unroll
+            for (int i = 0; i < kNtCPT; i++) {
+                const int col = tid + i * kNtNT;
+                a[rb][i] = (rb < nr && c0 + col < N) ? stg[rb * kNtW + col] : make_float2(0.f, 0.f);
+                const float2 x = vr[i], y = a[rb][i];
+                pr[rb] = fmaf(y.x, x.x, fmaf(-y.y, x.y, pr[rb]));
+                pim[rb] = fmaf(y.x, x.y, fmaf(y.y, x.x, pim[rb]));
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                pr[rb] += __shfl_xor_sync(0xffffffffu, pr[rb], o);
+                pim[rb] += __shfl_xor_sync(0xffffffffu, pim[rb], o);
+            }
+            if (lane == 0) {
+                red[rb][0][warp] = pr[rb];
+                red[rb][1][warp] = pim[rb];
+            }
+        }
+        __syncthreads();   // stage s is in every thread's registers
+        if (tid == 0 && g + kNtNS < ngroups && !abort_flag) {   // after a timeout nothing new is issued
+            fence_proxy_async_smem();
+            issue(g + kNtNS);
+        }
+        if (tid < 2 * kNtRPS) {
+            float t = 0.f;
+            for (int w = 0; w < kNtNT / 32; w++) t += red[tid >> 1][tid & 1][w];
+            tot[par][tid] = t;
+        }
+        cluster.sync();   // every CTA's row sums of this group are in its tot[par]
+        float ts[2 * kNtRPS];
+#pragma unroll
+        for (int u = 0; u < 2 * kNtRPS; u++) ts[u] = 0.f;
+        for (int p = 0; p < C; p++) {
+            const float *peer = cluster.map_shared_rank(&tot[par][0], p);
+#pragma unroll
+            for (int u = 0; u < 2 * kNtRPS; u++) ts[u] += peer[u];
+        }
+#pragma unroll
+        for (int rb = 0; rb < kNtRPS; rb++) {
+            const float tr = ts[2 * rb], ti = ts[2 * rb + 1];
+#pragma unroll
+            for (int i = 0; i < kNtCPT; i++) {
+                const float2 y = a[rb][i];
+                wr[i].x = fmaf(y.x, tr, fmaf(y.y, ti, wr[i].x));     // conj(a) t
+                wr[i].y = fmaf(y.x, ti, fmaf(-y.y, tr, wr[i].y));
+            }
+        }
+    }
+    if (tid == 0 && abort_flag) {
+        // drain: the last copy issued into each stage (earlier phases of a
+        // stage were awaited before it was refilled), bounded
+        int zero = 0;
+        for (int g = max(0, last_issued - kNtNS + 1); g <= last_issued; g++)
+            mbar_wait_bounded(&full[g % kNtNS], (uint32_t)((g / kNtNS) & 1), kNtWaitCycles, &zero);
+    }
+    cluster.sync();   // the peers have read tot; shared memory may go
+#pragma unroll
+    for (int i = 0; i < kNtCPT; i++) {
+        const int c = c0 + tid + i * kNtNT;
+        if (c < N) wpart[(size_t)cl * N + c] = wr[i];
+    }
+}
+
 }  // namespace
 
 void launch_gemv_c64(int R, int N, const float2 *A, size_t lda, const void *x, int xd, void *y,
@@ -868,9 +1024,54 @@ bool launch_arnoldi_step(int n, int j, double2 *V, size_t ldv, double2 *w, float
 }
 
 int normal_op_clusters(int N) {
-    const int C = (N + kNoW - 1) / kNoW;
+    const int C = (N + kNoW - 1) / kNoW;   // kNoW == kNtW: both kernels split columns alike
     if (C > kNoMaxCluster) return 0;
-    return (2 * 152) / C;
+    return (2 * 152) / C;                  // the register kernel's count; the TMA kernel uses at most half
+}
+
+namespace {
+// Clusters of C CTAs of the kernel that fit on the device at once (0: none).
+int clusters_resident(const void *kern, int C, int nt, size_t smem, int want) {
+    cudaLaunchConfig_t probe = {};
+    probe.gridDim = dim3((unsigned)(want * C));
+    probe.blockDim = dim3(nt);
+    probe.dynamicSmemBytes = smem;
+    cudaLaunchAttribute pa[1];
+    pa[0].id = cudaLaunchAttributeClusterDimension;
+    pa[0].val.clusterDim.x = (unsigned)C;
+    pa[0].val.clusterDim.y = 1;
+    pa[0].val.clusterDim.z = 1;
+    probe.attrs = pa;
+    probe.numAttrs = 1;
+    int active = 0;
+    if (cudaOccupancyMaxActiveClusters(&active, kern, &probe) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return active;
+}
+
+// Which normal-operator kernel runs: the TMA-streamed one unless the
+// environment variable BEM_NORMAL_OP_KERNEL is "regs".
+bool normal_op_use_tma() {
+    static const bool tma = [] {
+        const char *e = std::getenv("BEM_NORMAL_OP_KERNEL");
+        return !(e && std::string(e) == "regs");
+    }();
+    return tma;
+}
+}  // namespace
+
+bool normal_op_timed_out(cudaStream_t st) {
+    int h = 0;
+    static const int zero = 0;
+    CUDA_TRY(cudaMemcpyFromSymbolAsync(&h, g_normal_op_timeout, sizeof(int), 0, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    if (h) {
+        CUDA_TRY(cudaMemcpyToSymbolAsync(g_normal_op_timeout, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaStreamSynchronize(st));
+    }
+    return h != 0;
 }
 
 bool launch_normal_op(int R, int N, const float2 *A, size_t lda, const float2 *v, double2 *w, float2 *part,
@@ -880,37 +1081,28 @@ bool launch_normal_op(int R, int N, const float2 *A, size_t lda, const float2 *v
     BEM_PROF("normal_op", st);
     static std::once_flag once;
     static cudaError_t attr_err = cudaSuccess;
-    const size_t smem = 2 * (size_t)kNoW * sizeof(float2);
+    const size_t smem_regs = 2 * (size_t)kNoW * sizeof(float2);
     std::call_once(once, [&] {
-        attr_err = cudaFuncSetAttribute(normal_op_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr_err = cudaFuncSetAttribute(normal_op_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem_regs);
+        if (attr_err == cudaSuccess)
+            attr_err = cudaFuncSetAttribute(normal_op_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)kNtSmem);
     });
     CUDA_TRY(attr_err);
-    const int ncl = normal_op_clusters(N);
-    {
-        // the cluster shape must be schedulable on this device (else the two-kernel path runs)
-        cudaLaunchConfig_t probe = {};
-        probe.gridDim = dim3((unsigned)(ncl * C));
-        probe.blockDim = dim3(kNoNT);
-        probe.dynamicSmemBytes = smem;
-        cudaLaunchAttribute pa[1];
-        pa[0].id = cudaLaunchAttributeClusterDimension;
-        pa[0].val.clusterDim.x = (unsigned)C;
-        pa[0].val.clusterDim.y = 1;
-        pa[0].val.clusterDim.z = 1;
-        probe.attrs = pa;
-        probe.numAttrs = 1;
-        int active = 0;
-        if (cudaOccupancyMaxActiveClusters(&active, normal_op_kernel, &probe) != cudaSuccess || active < 1) {
-            cudaGetLastError();
-            return false;
-        }
-    }
+    // bulk copies need 16-byte aligned row segments: A 16-byte aligned, lda even
+    const bool tma = normal_op_use_tma() && lda % 2 == 0 && reinterpret_cast<uintptr_t>(A) % 16 == 0;
+    // the cluster shape must be schedulable on this device (else the two-kernel path runs)
+    int ncl = normal_op_clusters(N);
+    if (tma) ncl = std::min(152 / C, clusters_resident((const void *)normal_op_tma_kernel, C, kNtNT, kNtSmem, 152 / C));
+    else if (clusters_resident((const void *)normal_op_kernel, C, kNoNT, smem_regs, ncl) < 1) ncl = 0;
+    if (ncl < 1) return false;
     const int rpc = (R + ncl - 1) / ncl;
-    const int ngroups = (rpc + kNoRB - 1) / kNoRB;
+    const int ngroups = tma ? (rpc + kNtRPS - 1) / kNtRPS : (rpc + kNoRB - 1) / kNoRB;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)(ncl * C));
-    cfg.blockDim = dim3(kNoNT);
-    cfg.dynamicSmemBytes = smem;
+    cfg.blockDim = dim3(tma ? kNtNT : kNoNT);
+    cfg.dynamicSmemBytes = tma ? kNtSmem : smem_regs;
     cfg.stream = st;
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeClusterDimension;
@@ -919,7 +1111,8 @@ bool launch_normal_op(int R, int N, const float2 *A, size_t lda, const float2 *v
     at[0].val.clusterDim.z = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    CUDA_TRY(cudaLaunchKernelEx(&cfg, normal_op_kernel, R, N, A, lda, v, rpc, ngroups, part));
+    if (tma) CUDA_TRY(cudaLaunchKernelEx(&cfg, normal_op_tma_kernel, R, N, A, lda, v, rpc, ngroups, part));
+    else CUDA_TRY(cudaLaunchKernelEx(&cfg, normal_op_kernel, R, N, A, lda, v, rpc, ngroups, part));
     count_launch();
     sum_many_splits_kernel<<<blocks(N, 32), 256, 0, st>>>(N, ncl, part, w);
     count_launch();

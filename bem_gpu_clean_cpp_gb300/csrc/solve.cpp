@@ -186,6 +186,8 @@ void bem_solver_s::solve_refined(bem_solve_info_t *info) {
         all_conv &= conv ? 1 : 0;
     }
     CUDA_TRY(cudaStreamSynchronize(stream));
+    if (normal_op_timed_out(stream))
+        BEM_FAIL(BEM_ERR_TIMEOUT, "normal operator: a bulk copy of A did not complete in time");
     if (info) {
         info->iterations = total_it;
         info->refinements = max_ref;
