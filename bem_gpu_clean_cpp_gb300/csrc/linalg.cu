@@ -793,33 +793,36 @@ normal_op_kernel(int R, int N, const float2 *__restrict__ A, size_t lda, const f
 }
 
 // The same product with A streamed through shared memory by bulk
-// asynchronous copies (TMA).  One CTA per SM; CTA q of a cluster owns columns
-// [q kNtW, (q+1) kNtW) with v and its partial w in registers (kNtCPT columns
-// per thread).  Thread 0 keeps kNtNS stages of kNtRPS row segments in flight:
-// stage g % kNtNS is refilled with group g + kNtNS as soon as every thread has
-// copied group g into registers (the CTA barrier of the row reduction), so
-// HBM streams on through the cluster barrier that the row sums need, where
-// the register-loading kernel above issues no loads.
+// asynchronous copies (TMA).  CTA q of a cluster owns columns
+// [q W, (q+1) W), W = NT kNtCPT, with v and its partial w in registers
+// (kNtCPT columns per thread).  Thread 0 keeps kNtNS stages of kNtRPS row
+// segments in flight: stage g % kNtNS is refilled with group g + kNtNS once
+// every thread has copied group g into registers (the CTA barrier of the row
+// reduction; the refill is issued after the cluster barrier that follows),
+// so HBM streams on through the barriers the row sums need, where the
+// register-loading kernel above issues no loads.  The CTA barrier orders the
+// threads' shared-memory reads before the refill (no proxy fence is needed
+// for a write-after-read).  NT = 512: one CTA per SM; NT = 256: two.
 //
-// A row segment starts at A + row lda + q kNtW: 16-byte aligned because lda
-// is even (the launcher checks) and kNtW is even; its length is rounded up to
-// an even element count, which stays inside the row's lda padding.  Padding
-// and columns past N are masked (never multiplied), so the padding's contents
-// do not matter.  Every wait is bounded; on a timeout the CTA records it in
+// A row segment starts at A + row lda + q W: 16-byte aligned because lda is
+// even (the launcher checks) and W is even; its length is rounded up to an
+// even element count, which stays inside the row's lda padding.  Padding and
+// columns past N are masked (never multiplied), so the padding's contents do
+// not matter.  Every wait is bounded; on a timeout the CTA records it in
 // g_normal_op_timeout, issues no further copies, keeps the same barrier
 // sequence as its peers, and drains its copies in flight (bounded again)
 // before exiting.
-constexpr int kNtNT = 512;
 constexpr int kNtCPT = 11;
-constexpr int kNtW = kNtNT * kNtCPT;   // 5632 columns per CTA (= kNoW)
 constexpr int kNtRPS = 2;              // rows per stage (one row group)
 constexpr int kNtNS = 2;               // stages
-constexpr size_t kNtSmem = (size_t)kNtNS * kNtRPS * kNtW * sizeof(float2);   // 180224 B
+template <int NT>
+constexpr size_t nt_smem() { return (size_t)kNtNS * kNtRPS * NT * kNtCPT * sizeof(float2); }
 constexpr long long kNtWaitCycles = 2000000000LL;                          // ~1 s at 2 GHz
 
 __device__ int g_normal_op_timeout = 0;
 
-__global__ void __launch_bounds__(kNtNT, 1)
+template <int NT>
+__global__ void __launch_bounds__(NT, 512 / NT)
 normal_op_tma_kernel(int R, int N, const float2 *__restrict__ A, size_t lda, const float2 *__restrict__ v,
                      int rows_per_cluster, int ngroups, float2 *__restrict__ wpart) {
     namespace cg = cooperative_groups;
@@ -827,6 +830,7 @@ normal_op_tma_kernel(int R, int N, const float2 *__restrict__ A, size_t lda, con
     const int C = (int)cluster.num_blocks();
     const int q = (int)cluster.block_rank();
     const int cl = blockIdx.x / C;
+    constexpr int kNtNT = NT, kNtW = NT * kNtCPT;
     extern __shared__ __align__(128) float2 nt_stage[];   // [kNtNS][kNtRPS][kNtW]
     __shared__ __align__(8) uint64_t full[kNtNS];
     __shared__ float red[kNtRPS][2][kNtNT / 32];
@@ -900,16 +904,13 @@ normal_op_tma_kernel(int R, int N, const float2 *__restrict__ A, size_t lda, con
             }
         }
         __syncthreads();   // stage s is in every thread's registers
-        if (tid == 0 && g + kNtNS < ngroups && !abort_flag) {   // after a timeout nothing new is issued
-            fence_proxy_async_smem();
-            issue(g + kNtNS);
-        }
         if (tid < 2 * kNtRPS) {
             float t = 0.f;
             for (int w = 0; w < kNtNT / 32; w++) t += red[tid >> 1][tid & 1][w];
             tot[par][tid] = t;
         }
         cluster.sync();   // every CTA's row sums of this group are in its tot[par]
+        if (tid == 0 && g + kNtNS < ngroups && !abort_flag) issue(g + kNtNS);   // none after a timeout
         float ts[2 * kNtRPS];
 #pragma unroll
         for (int u = 0; u < 2 * kNtRPS; u++) ts[u] = 0.f;
@@ -1026,7 +1027,7 @@ bool launch_arnoldi_step(int n, int j, double2 *V, size_t ldv, double2 *w, float
 int normal_op_clusters(int N) {
     const int C = (N + kNoW - 1) / kNoW;   // kNoW == kNtW: both kernels split columns alike
     if (C > kNoMaxCluster) return 0;
-    return (2 * 152) / C;                  // the register kernel's count; the TMA kernel uses at most half
+    return (2 * 152) / C;                  // the most clusters any variant launches
 }
 
 namespace {
@@ -1051,14 +1052,17 @@ int clusters_resident(const void *kern, int C, int nt, size_t smem, int want) {
     return active;
 }
 
-// Which normal-operator kernel runs: the TMA-streamed one unless the
-// environment variable BEM_NORMAL_OP_KERNEL is "regs".
-bool normal_op_use_tma() {
-    static const bool tma = [] {
+// Which normal-operator kernel runs (environment variable
+// BEM_NORMAL_OP_KERNEL): 0 = "regs" (A loaded into registers), 512 = "tma"
+// (TMA-streamed, 512 threads, one CTA per SM; the default), 256 = "tma256"
+// (256 threads, two CTAs per SM).
+int normal_op_variant() {
+    static const int var = [] {
         const char *e = std::getenv("BEM_NORMAL_OP_KERNEL");
-        return !(e && std::string(e) == "regs");
+        const std::string v = e ? e : "";
+        return v == "regs" ? 0 : v == "tma256" ? 256 : 512;
     }();
-    return tma;
+    return var;
 }
 }  // namespace
 
@@ -1076,8 +1080,7 @@ bool normal_op_timed_out(cudaStream_t st) {
 
 bool launch_normal_op(int R, int N, const float2 *A, size_t lda, const float2 *v, double2 *w, float2 *part,
                       cudaStream_t st) {
-    const int C = (N + kNoW - 1) / kNoW;
-    if (N <= 0 || R <= 0 || C > kNoMaxCluster) return false;
+    if (N <= 0 || R <= 0 || (N + kNoW - 1) / kNoW > kNoMaxCluster) return false;
     BEM_PROF("normal_op", st);
     static std::once_flag once;
     static cudaError_t attr_err = cudaSuccess;
@@ -1086,23 +1089,33 @@ bool launch_normal_op(int R, int N, const float2 *A, size_t lda, const float2 *v
         attr_err = cudaFuncSetAttribute(normal_op_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)smem_regs);
         if (attr_err == cudaSuccess)
-            attr_err = cudaFuncSetAttribute(normal_op_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)kNtSmem);
+            attr_err = cudaFuncSetAttribute(normal_op_tma_kernel<512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)nt_smem<512>());
+        if (attr_err == cudaSuccess)
+            attr_err = cudaFuncSetAttribute(normal_op_tma_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)nt_smem<256>());
     });
     CUDA_TRY(attr_err);
     // bulk copies need 16-byte aligned row segments: A 16-byte aligned, lda even
-    const bool tma = normal_op_use_tma() && lda % 2 == 0 && reinterpret_cast<uintptr_t>(A) % 16 == 0;
+    int nt = (lda % 2 == 0 && reinterpret_cast<uintptr_t>(A) % 16 == 0) ? normal_op_variant() : 0;
+    int C = (N + kNoW - 1) / kNoW;
+    if (nt == 256 && (N + 256 * kNtCPT - 1) / (256 * kNtCPT) > kNoMaxCluster) nt = 512;
+    if (nt == 256) C = (N + 256 * kNtCPT - 1) / (256 * kNtCPT);
+    const void *kern = nt == 512   ? (const void *)normal_op_tma_kernel<512>
+                       : nt == 256 ? (const void *)normal_op_tma_kernel<256>
+                                   : (const void *)normal_op_kernel;
+    const size_t smem = nt == 512 ? nt_smem<512>() : nt == 256 ? nt_smem<256>() : smem_regs;
+    const int bt = nt ? nt : kNoNT;
     // the cluster shape must be schedulable on this device (else the two-kernel path runs)
-    int ncl = normal_op_clusters(N);
-    if (tma) ncl = std::min(152 / C, clusters_resident((const void *)normal_op_tma_kernel, C, kNtNT, kNtSmem, 152 / C));
-    else if (clusters_resident((const void *)normal_op_kernel, C, kNoNT, smem_regs, ncl) < 1) ncl = 0;
+    const int want = nt == 512 ? 152 / C : 304 / C;
+    const int ncl = std::min(want, clusters_resident(kern, C, bt, smem, want));
     if (ncl < 1) return false;
     const int rpc = (R + ncl - 1) / ncl;
-    const int ngroups = tma ? (rpc + kNtRPS - 1) / kNtRPS : (rpc + kNoRB - 1) / kNoRB;
+    const int ngroups = nt ? (rpc + kNtRPS - 1) / kNtRPS : (rpc + kNoRB - 1) / kNoRB;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)(ncl * C));
-    cfg.blockDim = dim3(tma ? kNtNT : kNoNT);
-    cfg.dynamicSmemBytes = tma ? kNtSmem : smem_regs;
+    cfg.blockDim = dim3(bt);
+    cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
     cudaLaunchAttribute at[1];
     at[0].id = cudaLaunchAttributeClusterDimension;
@@ -1111,7 +1124,8 @@ bool launch_normal_op(int R, int N, const float2 *A, size_t lda, const float2 *v
     at[0].val.clusterDim.z = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    if (tma) CUDA_TRY(cudaLaunchKernelEx(&cfg, normal_op_tma_kernel, R, N, A, lda, v, rpc, ngroups, part));
+    if (nt == 512) CUDA_TRY(cudaLaunchKernelEx(&cfg, normal_op_tma_kernel<512>, R, N, A, lda, v, rpc, ngroups, part));
+    else if (nt == 256) CUDA_TRY(cudaLaunchKernelEx(&cfg, normal_op_tma_kernel<256>, R, N, A, lda, v, rpc, ngroups, part));
     else CUDA_TRY(cudaLaunchKernelEx(&cfg, normal_op_kernel, R, N, A, lda, v, rpc, ngroups, part));
     count_launch();
     sum_many_splits_kernel<<<blocks(N, 32), 256, 0, st>>>(N, ncl, part, w);
