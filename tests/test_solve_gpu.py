@@ -204,3 +204,43 @@ def test_refined_solve_cluster_sizes(bemlib, nu):
     info = s.solve(bemlib.SOLVE_GMRES_REFINED)
     assert info.converged
     assert rel_err(s.solution(), x64) < 1e-5
+
+
+_VARIANT_SCRIPT = r"""
+import sys
+import numpy as np
+sys.path.insert(0, sys.argv[1])
+import bem_gpu_clean_cpp_gb300 as bem
+m = bem.Mesh.geodesic(33).perturbed_ellipsoid(1.0, 0.8, 0.9, lmax=4, amp=0.03, seed=33)
+p, e = m.points(), m.elems()
+chief = np.random.default_rng(33).uniform(-0.25, 0.25, (8, 3))
+d = np.array([0.3, -0.5, 0.81])
+s = bem.Solver(near_eta=1.0, near_depth=2)
+s.set_geometry(p, e, bc=np.tile(np.array([0, 1, 0], dtype=np.complex128), (e.shape[0], 1)), chief=chief)
+s.set_sources([("plane", d / np.linalg.norm(d), 1.0)])
+s.assemble(5.0, bem.PREC_C128)
+s.solve(bem.SOLVE_QR)
+x64 = s.solution()
+s.assemble(5.0, bem.PREC_C64)
+info = s.solve(bem.SOLVE_GMRES_REFINED)
+err = np.linalg.norm(s.solution() - x64) / np.linalg.norm(x64)
+print("RESULT", int(info.converged), err)
+"""
+
+
+@pytest.mark.parametrize("variant", ["regs", "tma256"])
+def test_normal_op_variants(bemlib, variant):
+    """The other two normal-operator kernels, chosen per process by
+    BEM_NORMAL_OP_KERNEL (register-loading, and the 256-thread TMA kernel
+    with two CTAs per SM and four-CTA clusters at 10892 nodes), give a
+    refined solve within 1e-5 of the FP64 solve, like the default one."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, BEM_NORMAL_OP_KERNEL=variant)
+    out = subprocess.run([sys.executable, "-c", _VARIANT_SCRIPT, root], env=env, capture_output=True, text=True,
+                         timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = [ln for ln in out.stdout.splitlines() if ln.startswith("RESULT")][-1].split()
+    assert line[1] == "1" and float(line[2]) < 1e-5, line
