@@ -189,8 +189,9 @@ __device__ __forceinline__ bool pair_is_near(int row, int N, int4 nd, float4 xh,
 // three nodal integrals (N1 = xi1, N2 = xi2, N3 = 1 - xi1 - xi2).  The 1/(4 pi)
 // and |J| factors are applied once per pair by the caller.
 // ---------------------------------------------------------------------------
-// Phase of the FP32 quadrature.  The fast __sincosf is documented with a
-// bounded error on [-pi, pi] only and its error grows with |x| outside (kr
+// Phase of the FP32 quadrature.  The hardware sin/cos approximation
+// (sin.approx, as in __sincosf) is documented with a bounded error on
+// [-pi, pi] only and its error grows with |x| outside (kr
 // reaches ~30 at 8 kHz on a 0.11 m body).  Three modes, chosen per launch on
 // the host from the problem's size in wavelengths:
 //
@@ -306,6 +307,20 @@ __device__ __forceinline__ void sincos_acc(float y, float *sn, float *cs) {
     *cs = ((qd + 1u) & 2u) ? -c0 : c0;
 }
 
+// The hardware approximations (PTX rsqrt/sin/cos.approx) with subnormal
+// inputs and results flushed to zero.  The quadrature's r^2 and phases are
+// far from the subnormal range, so the flush changes nothing there; it drops
+// the subnormal handling that the default (non-flushing) forms carry.
+__device__ __forceinline__ float rsqrt_ftz(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ void sincos_ftz(float x, float *sn, float *cs) {
+    asm("sin.approx.ftz.f32 %0, %1;" : "=f"(*sn) : "f"(x));
+    asm("cos.approx.ftz.f32 %0, %1;" : "=f"(*cs) : "f"(x));
+}
+
 // sin and cos of the phase of a point at distance r; q = r^2 - r_c^2
 // (kPhaseAcc only).
 template <int PH>
@@ -314,7 +329,7 @@ __device__ __forceinline__ void phase_sincos(float k, float r, float q, const Pa
         sincos_acc(fmaf(k, __fdividef(q, r + pp.rc), pp.yc), sn, cs);
     } else {
         const float y = fmaf(k, r, pp.c1) + pp.c2;
-        __sincosf(PH == kPhaseWrap ? wrap_phase(y) : y, sn, cs);
+        sincos_ftz(PH == kPhaseWrap ? wrap_phase(y) : y, sn, cs);
     }
 }
 
@@ -337,7 +352,7 @@ __device__ __forceinline__ void far_sums_f32(float3 d3, float3 e1, float3 e2, fl
         float dy = fmaf(t.y, e2.y, fmaf(t.x, e1.y, d3.y));
         float dz = fmaf(t.y, e2.z, fmaf(t.x, e1.z, d3.z));
         float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-        float ri = rsqrtf(r2);
+        float ri = rsqrt_ftz(r2);
         float r = r2 * ri;
         float sn, cs;
         float dq = 0.f;
@@ -409,7 +424,7 @@ __device__ __forceinline__ void far_sums_f32_o6(float3 d3, float3 e1, float3 e2,
             const float wr1 = gl6_w(m) * rho, wr2 = gl6_w(m) * rho * rho;
             const float dx = fmaf(rho, vx, d3.x), dy = fmaf(rho, vy, d3.y), dz = fmaf(rho, vz, d3.z);
             const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-            const float ri = rsqrtf(r2);
+            const float ri = rsqrt_ftz(r2);
             const float r = r2 * ri;
             const float kr = k * r;
             float sn, cs;
