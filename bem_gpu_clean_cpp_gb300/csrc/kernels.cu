@@ -384,7 +384,8 @@ __device__ __forceinline__ void far_sums_f32(float3 d3, float3 e1, float3 e2, fl
 // The same sums for the 6 x 6 rule (the reference's INTORDER = 6), arranged
 // for the FP32 issue rate:
 //   * the Duffy points lie on lines of constant theta_n: d = d3 + rho_m v_n
-//     with v_n = e1 + theta_n (e2 - e1), so a point costs 3 FMAs for d;
+//     with v_n = e1 + theta_n (e2 - e1), so r^2 is a quadratic in rho_m
+//     with per-line coefficients: 2 FMAs per point;
 //   * along a line, S0 needs sum w_m rho_m f and S1, S2 both need
 //     sum w_m rho_m^2 f (xi1 = rho (1-theta), xi2 = rho theta): two inner sums
 //     per quantity instead of three;
@@ -409,32 +410,34 @@ __device__ __forceinline__ void far_sums_f32_o6(float3 d3, float3 e1, float3 e2,
     S.h0r = S.h0i = S.h1r = S.h1i = S.h2r = S.h2i = 0.0f;
     S.c = 0.0f;
     const float3 e21 = make_float3(e2.x - e1.x, e2.y - e1.y, e2.z - e1.z);
+    const float dd = fmaf(d3.z, d3.z, fmaf(d3.y, d3.y, d3.x * d3.x));   // |d3|^2
 #pragma unroll
     for (int n = 0; n < 6; n++) {
         const float th = 0.5f + 0.5f * gl6_x(n);
         const float vx = fmaf(th, e21.x, e1.x), vy = fmaf(th, e21.y, e1.y), vz = fmaf(th, e21.z, e1.z);
-        // kPhaseAcc: r^2 - r_c^2 = qa rho^2 + qb rho + c0 along the line
-        const float qa = PH == kPhaseAcc ? fmaf(vz, vz, fmaf(vy, vy, vx * vx)) : 0.f;
-        const float qb = PH == kPhaseAcc ? 2.0f * fmaf(vz, d3.z, fmaf(vy, d3.y, vx * d3.x)) : 0.f;
+        // along the line r^2 = qa rho^2 + qb rho + |d3|^2 (and, kPhaseAcc,
+        // r^2 - r_c^2 = qa rho^2 + qb rho + c0).  The terms are within a few
+        // ulps of r^2 for a far pair (|d3| and rho |v| are bounded by r plus
+        // the element's size), as accurate as summing the squared components.
+        const float qa = fmaf(vz, vz, fmaf(vy, vy, vx * vx));
+        const float qb = 2.0f * fmaf(vz, d3.z, fmaf(vy, d3.y, vx * d3.x));
         float u0gr = 0.f, u1gr = 0.f, u0gs = 0.f, u1gs = 0.f;
         float u0ha = 0.f, u1ha = 0.f, u0hb = 0.f, u1hb = 0.f, u0c = 0.f;
 #pragma unroll
         for (int m = 0; m < 6; m++) {
             const float rho = 0.5f + 0.5f * gl6_x(m);
             const float wr1 = gl6_w(m) * rho, wr2 = gl6_w(m) * rho * rho;
-            const float dx = fmaf(rho, vx, d3.x), dy = fmaf(rho, vy, d3.y), dz = fmaf(rho, vz, d3.z);
-            const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+            const float r2 = fmaf(qa, rho * rho, fmaf(qb, rho, dd));
             const float ri = rsqrt_ftz(r2);
             const float r = r2 * ri;
-            const float kr = k * r;
             float sn, cs;
             const float q = PH == kPhaseAcc ? fmaf(fmaf(qa, rho, qb), rho, pp.c0) : 0.f;
             phase_sincos<PH>(k, r, q, pp, &sn, &cs);
-            const float A = fmaf(kr, sn, cs);      // c + kr s
-            const float Bv = fmaf(kr, cs, -sn);    // kr c - s
-            const float ri3 = ri * ri * ri;
+            // (c + kr s)/r^3 = (gr + k s)/r^2 and (kr c - s)/r^3 = (k c - gs)/r^2
+            const float ri2 = ri * ri;
             const float gr = cs * ri, gs = sn * ri;
-            const float ha = ri3 * A, hb = ri3 * Bv;
+            const float ha = ri2 * fmaf(k, sn, gr), hb = ri2 * fmaf(k, cs, -gs);
+            const float ri3 = ri2 * ri;
             u0gr = fmaf(wr1, gr, u0gr); u1gr = fmaf(wr2, gr, u1gr);
             u0gs = fmaf(wr1, gs, u0gs); u1gs = fmaf(wr2, gs, u1gs);
             u0ha = fmaf(wr1, ha, u0ha); u1ha = fmaf(wr2, ha, u1ha);
