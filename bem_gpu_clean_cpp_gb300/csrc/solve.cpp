@@ -136,11 +136,17 @@ void bem_solver_s::solve_refined(bem_solve_info_t *info) {
         bool conv = false;
         int ref = 0;
         for (;; ref++) {
-            launch_resid(prec, R, n, A, lda, x, b, w_r.as<double2>(), w_vf.as<float2>(), stream);
-            launch_gemv_h_f64(prec, R, n, A, lda, w_r.as<double2>(), w_gv.as<double2>(), w_part.as<double2>(),
-                              w_vf.as<float2>(), stream);
-            launch_nrm2(n, w_gv.as<double2>(), scal + 1, nullptr, stream);
-            const double gn = read_scalar(1);
+            // With x = 0 (the first step) r = b and g = A^H b, already in w_gv.
+            double gn = bn;
+            if (ref > 0) {
+                launch_resid(prec, R, n, A, lda, x, b, w_r.as<double2>(), w_vf.as<float2>(), stream);
+                launch_gemv_h_f64(prec, R, n, A, lda, w_r.as<double2>(), w_gv.as<double2>(),
+                                  w_part.as<double2>(), w_vf.as<float2>(), stream);
+                launch_nrm2(n, w_gv.as<double2>(), scal + 1, nullptr, stream);
+                gn = read_scalar(1);
+            } else {
+                CUDA_TRY(cudaMemcpyAsync(scal + 1, scal + 0, sizeof(double), cudaMemcpyDeviceToDevice, stream));
+            }
             rel = gn / bn;
             if (!std::isfinite(rel)) BEM_FAIL(BEM_ERR_NUMERIC, "refinement residual is not finite");
             if (rel <= opt.tol) { conv = true; break; }
