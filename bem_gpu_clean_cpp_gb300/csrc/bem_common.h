@@ -71,6 +71,15 @@ struct ProfScope {
     cudaStream_t stream = nullptr;
 };
 #define BEM_PROF(name, st) ::bem::ProfScope bem_prof_scope_((name), (st))
+// Host-side counterpart: wall time of a host code section (table builds,
+// host-device round trips), reported as "host:<name>" while profiling.
+struct HostProfScope {
+    explicit HostProfScope(const char *name);
+    ~HostProfScope();
+    const char *name = nullptr;
+    long long t0_ns = 0;
+};
+#define BEM_HOST_PROF(name) ::bem::HostProfScope bem_host_prof_scope_(name)
 
 constexpr double kPi = 3.14159265358979323846;
 constexpr int kMaxOrder = 12;              // Gauss points per direction

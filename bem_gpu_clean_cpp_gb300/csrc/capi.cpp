@@ -5,6 +5,7 @@
 #include <cusolverDn.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -31,6 +32,12 @@ struct ProfRec {
 };
 std::mutex g_prof_mu;
 std::vector<ProfRec> g_prof;           // records of the current profiling window
+std::vector<std::pair<const char *, double>> g_host_prof;   // host sections: name, ms
+long long now_ns() {
+    return std::chrono::duration_cast<std::chrono::nanoseconds>(
+               std::chrono::steady_clock::now().time_since_epoch())
+        .count();
+}
 std::vector<cudaEvent_t> g_ev_pool;    // events for reuse
 
 cudaEvent_t pool_event() {
@@ -58,6 +65,19 @@ ProfScope::~ProfScope() {
     if (slot < 0) return;
     std::lock_guard<std::mutex> lk(g_prof_mu);
     if (slot < (int)g_prof.size()) cudaEventRecord(g_prof[slot].ev[1], stream);
+}
+
+HostProfScope::HostProfScope(const char *n) {
+    if (!g_profiling.load(std::memory_order_relaxed)) return;
+    name = n;
+    t0_ns = now_ns();
+}
+
+HostProfScope::~HostProfScope() {
+    if (!name) return;
+    const double ms = 1e-6 * (double)(now_ns() - t0_ns);
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    g_host_prof.emplace_back(name, ms);
 }
 
 [[noreturn]] void fail(int status, const char *file, int line, const std::string &msg) {
@@ -277,6 +297,7 @@ int bem_profile_enable(int on) {
         g_ev_pool.push_back(r.ev[1]);
     }
     g_prof.clear();
+    g_host_prof.clear();
     g_profiling.store(on != 0);
     BEM_API_END
 }
@@ -300,6 +321,18 @@ int bem_profile_report(char *buf, int buflen) {
             }
             cnt[i]++;
             tot[i] += ms;
+        }
+        for (const auto &h : g_host_prof) {
+            const std::string nm = std::string("host:") + h.first;
+            size_t i = 0;
+            while (i < names.size() && names[i] != nm) i++;
+            if (i == names.size()) {
+                names.push_back(nm);
+                cnt.push_back(0);
+                tot.push_back(0.0);
+            }
+            cnt[i]++;
+            tot[i] += h.second;
         }
         std::string out;
         for (size_t i = 0; i < names.size(); i++)

@@ -92,6 +92,7 @@ void bem_solver_s::solve_qr() {
 }
 
 void bem_solver_s::solve_refined(bem_solve_info_t *info) {
+    BEM_HOST_PROF("solve_refined");
     const int n = N, m = std::max(1, opt.max_iter);
     const int ldh = m + 1;
     const float2 *A = d_A.as<float2>();

@@ -54,28 +54,31 @@ uint32_t morton_key(const double *p, const double *lo, const double *inv) {
 // share no node, so consecutive records in a tile list rarely add to the same
 // shared-memory column in the same instruction.
 std::vector<int> color_elements(int N, const std::vector<int> &elems) {
-    int E = (int)(elems.size() / 3);
-    std::vector<int> deg(N + 1, 0);
-    for (int v : elems) deg[v + 1]++;
-    for (int i = 0; i < N; i++) deg[i + 1] += deg[i];
-    std::vector<int> adj(elems.size()), fill(deg.begin(), deg.end() - 1);
-    for (int e = 0; e < E; e++)
-        for (int j = 0; j < 3; j++) adj[fill[elems[3 * e + j]]++] = e;
-    std::vector<int> color(E, -1);
-    std::vector<int> mark;
+    const int E = (int)(elems.size() / 3);
+    // node -> the colours used by elements already coloured at that node, as
+    // a bit set (64 colours; an element whose neighbours use all 64 takes
+    // the first free colour above, found by a scan)
+    std::vector<uint64_t> used(N, 0);
+    std::vector<int> color(E);
+    std::vector<std::vector<int>> high;   // colours >= 64 per node, rarely used
     for (int e = 0; e < E; e++) {
-        for (int j = 0; j < 3; j++) {
-            int v = elems[3 * e + j];
-            for (int t = deg[v]; t < deg[v + 1]; t++) {
-                int c = color[adj[t]];
-                if (c >= 0) {
-                    if ((int)mark.size() <= c) mark.resize(c + 1, -1);
-                    mark[c] = e;
-                }
+        const int *nd = &elems[3 * (size_t)e];
+        const uint64_t m = used[nd[0]] | used[nd[1]] | used[nd[2]];
+        int c;
+        if (~m) {
+            c = __builtin_ctzll(~m);
+            for (int j = 0; j < 3; j++) used[nd[j]] |= 1ull << c;
+        } else {
+            if (high.empty()) high.resize(N);
+            c = 64;
+            for (bool clash = true; clash; ) {
+                clash = false;
+                for (int j = 0; j < 3 && !clash; j++)
+                    clash = std::find(high[nd[j]].begin(), high[nd[j]].end(), c) != high[nd[j]].end();
+                if (clash) c++;
             }
+            for (int j = 0; j < 3; j++) high[nd[j]].push_back(c);
         }
-        int c = 0;
-        while (c < (int)mark.size() && mark[c] == e) c++;
         color[e] = c;
     }
     return color;
@@ -111,6 +114,7 @@ bem_solver_s::~bem_solver_s() {
 
 void bem_solver_s::set_geometry(const double *pnts, int num_pnts, const int *elems, int num_elems,
                                 const double *bc, const double *chief, int num_chief) {
+    BEM_HOST_PROF("set_geometry");
     BEM_CHECK_ARG(pnts && elems && num_pnts > 0 && num_elems > 0, "empty geometry");
     BEM_CHECK_ARG(num_chief >= 0 && (num_chief == 0 || chief), "bad CHIEF points");
     for (long long i = 0; i < 3LL * num_elems; i++)
@@ -212,6 +216,7 @@ void bem_solver_s::ensure_geo() {
 void bem_solver_s::ensure_near_list() {
     ensure_geo();
     if (near_valid) return;
+    BEM_HOST_PROF("near_list");
     // Grid of element centroids: cell edge >= the largest near radius
     // (near_eta x element diameter) and >= the longest element (vertex pairs),
     // over the box of all row points and nodes; at most ~4M cells.
@@ -275,6 +280,7 @@ void bem_solver_s::ensure_near_list() {
 void bem_solver_s::ensure_tiles(int precision) {
     Tiles &T = tiles[precision];
     if (T.valid) return;
+    BEM_HOST_PROF("tiles");
     const int cap = opt.tile_cols > 0 ? std::min(opt.tile_cols, kTileColsMax) : kTileColsMax;
     int ntiles = (N + cap - 1) / cap;
     int per = (N + ntiles - 1) / ntiles;
@@ -301,8 +307,13 @@ void bem_solver_s::ensure_tiles(int precision) {
         cols[(size_t)t * per + s] = order[i];
         cnt[t]++;
     }
-    std::vector<int> color = color_elements(N, h_elems);
+    std::vector<int> color;
+    {
+        BEM_HOST_PROF("color_elements");
+        color = color_elements(N, h_elems);
+    }
     std::vector<std::vector<TileRec>> lists(ntiles);
+    if (ntiles == 1) lists[0].reserve(E);
     for (int e = 0; e < E; e++) {
         const int *nd = &h_elems[3 * (size_t)e];
         int seen[3] = {-1, -1, -1}, ns = 0;
@@ -324,11 +335,17 @@ void bem_solver_s::ensure_tiles(int precision) {
     }
     std::vector<TileRec> recs;
     std::vector<int> ptr(ntiles + 1, 0);
+    int ncolor = 0;
+    for (int c : color) ncolor = std::max(ncolor, c + 1);
+    std::vector<int> cstart(ncolor + 1);
     for (int t = 0; t < ntiles; t++) {
-        std::stable_sort(lists[t].begin(), lists[t].end(),
-                         [&](const TileRec &a, const TileRec &b) { return color[a.eid] < color[b.eid]; });
+        // stable counting sort of the tile's records by element colour
+        std::fill(cstart.begin(), cstart.end(), 0);
+        for (const TileRec &r : lists[t]) cstart[color[r.eid] + 1]++;
+        for (int c = 0; c < ncolor; c++) cstart[c + 1] += cstart[c];
         ptr[t + 1] = ptr[t] + (int)lists[t].size();
-        recs.insert(recs.end(), lists[t].begin(), lists[t].end());
+        recs.resize(ptr[t + 1]);
+        for (const TileRec &r : lists[t]) recs[ptr[t] + cstart[color[r.eid]]++] = r;
     }
     T.recs.ensure(sizeof(TileRec) * recs.size());
     T.rec_ptr.ensure(sizeof(int) * ptr.size());
@@ -355,6 +372,7 @@ Physics bem_solver_s::physics() const {
 }
 
 void bem_solver_s::assemble(double kk, int precision) {
+    BEM_HOST_PROF("assemble");
     BEM_CHECK_ARG(precision == BEM_PREC_C64 || precision == BEM_PREC_C128, "bad precision");
     BEM_CHECK_ARG(std::isfinite(kk) && kk > 0, "wavenumber must be positive");
     if (E == 0) BEM_FAIL(BEM_ERR_STATE, "no geometry set");
