@@ -108,6 +108,7 @@ bem_solver_s::~bem_solver_s() {
     if (cusolver) cusolverDnDestroy(cusolver);
     if (cublas) cublasDestroy(cublas);
     if (h_pinned) cudaFreeHost(h_pinned);
+    if (h_stage) cudaFreeHost(h_stage);
     if (stream) cudaStreamDestroy(stream);
     if (cur >= 0 && cur != device) cudaSetDevice(cur);
 }
@@ -156,14 +157,26 @@ void bem_solver_s::set_geometry(const double *pnts, int num_pnts, const int *ele
                            (hi[2] - lo[2]) * (hi[2] - lo[2]));
     }
 
-    std::vector<float4> rf(2 * (size_t)R);
+    // The float head/tail rows and the int4 element table are built in a
+    // pinned staging buffer; nodes, CHIEF points and BCs go up straight from
+    // the caller's arrays (no host copy; a pinned caller buffer is a direct
+    // DMA).  The caller's arrays are only read until this call returns.
+    const size_t rf_bytes = sizeof(float4) * 2 * (size_t)R, el_bytes = sizeof(int4) * (size_t)E;
+    if (h_stage_bytes < rf_bytes + el_bytes) {
+        if (h_stage) CUDA_TRY(cudaFreeHost(h_stage));
+        h_stage = nullptr;
+        h_stage_bytes = 0;
+        CUDA_TRY(cudaMallocHost(&h_stage, rf_bytes + el_bytes));
+        h_stage_bytes = rf_bytes + el_bytes;
+    }
+    float4 *rf = static_cast<float4 *>(h_stage);
+    int4 *el = reinterpret_cast<int4 *>(static_cast<unsigned char *>(h_stage) + rf_bytes);
     for (int i = 0; i < R; i++) {
         float hx = (float)h_rows[3 * i], hy = (float)h_rows[3 * i + 1], hz = (float)h_rows[3 * i + 2];
         rf[2 * i] = make_float4(hx, hy, hz, 0.f);
         rf[2 * i + 1] = make_float4((float)(h_rows[3 * i] - hx), (float)(h_rows[3 * i + 1] - hy),
                                     (float)(h_rows[3 * i + 2] - hz), 0.f);
     }
-    std::vector<int4> el(E);
     for (int e = 0; e < E; e++) el[e] = make_int4(h_elems[3 * e], h_elems[3 * e + 1], h_elems[3 * e + 2], 0);
     d_nodes.ensure(sizeof(double) * 3 * N);
     d_rows_d.ensure(sizeof(double) * 3 * (size_t)R);
@@ -172,12 +185,16 @@ void bem_solver_s::set_geometry(const double *pnts, int num_pnts, const int *ele
     d_bc.ensure(sizeof(double) * 6 * (size_t)E);
     d_geo_f.ensure(sizeof(float4) * kGeoFloat4 * (size_t)E);
     d_geo_d.ensure(sizeof(double) * kGeoDouble * (size_t)E);
-    CUDA_TRY(cudaMemcpyAsync(d_nodes.p, h_nodes.data(), sizeof(double) * 3 * N, cudaMemcpyHostToDevice, stream));
-    CUDA_TRY(cudaMemcpyAsync(d_rows_d.p, h_rows.data(), sizeof(double) * 3 * (size_t)R, cudaMemcpyHostToDevice, stream));
-    CUDA_TRY(cudaMemcpyAsync(d_rows_f.p, rf.data(), sizeof(float4) * 2 * (size_t)R, cudaMemcpyHostToDevice, stream));
-    CUDA_TRY(cudaMemcpyAsync(d_elems.p, el.data(), sizeof(int4) * E, cudaMemcpyHostToDevice, stream));
-    CUDA_TRY(cudaMemcpyAsync(d_bc.p, h_bc.data(), sizeof(double) * 6 * (size_t)E, cudaMemcpyHostToDevice, stream));
-    CUDA_TRY(cudaStreamSynchronize(stream));   // host vectors rf/el go out of scope
+    CUDA_TRY(cudaMemcpyAsync(d_nodes.p, pnts, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemcpyAsync(d_rows_d.p, pnts, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, stream));
+    if (M)
+        CUDA_TRY(cudaMemcpyAsync(d_rows_d.as<double>() + 3 * (size_t)N, chief, sizeof(double) * 3 * (size_t)M,
+                                 cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemcpyAsync(d_rows_f.p, rf, rf_bytes, cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemcpyAsync(d_elems.p, el, el_bytes, cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemcpyAsync(d_bc.p, bc ? bc : h_bc.data(), sizeof(double) * 6 * (size_t)E, cudaMemcpyHostToDevice,
+                             stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));   // the caller's arrays and the staging buffer are free again
     geo_eta = -1.0;
     tiles[0].valid = tiles[1].valid = false;
     assembled = solved = false;

@@ -85,6 +85,8 @@ struct bem_solver_s {
     bem::DevMem w_ap;   // partial sums of the cooperative Arnoldi step
     int tf32_split_mode = -1;   // BEM_GEMM_* the planes of A were built for (this assembly), -1 none
     double *h_pinned = nullptr;
+    void *h_stage = nullptr;     // pinned staging for geometry uploads
+    size_t h_stage_bytes = 0;
     // QR workspace
     bem::DevMem q_A, q_B, q_tau, q_work, q_info;
     // field workspace
