@@ -156,9 +156,11 @@ void bem_solver_s::solve_refined(bem_solve_info_t *info) {
             launch_scale_copy(n, w_gv.as<double2>(), scal + 1, V, stream, w_vf.as<float2>());
             launch_zero_f64(m + 1, w_g.as<double2>(), stream);
             launch_set_scalar_c(w_g.as<double2>(), scal + 1, stream);
-            int jdone = 0;
-            for (int j = 0; j < m; j++) {
-                // w = A^H A v_j (c64 copy of v_j): one pass over A when a cluster covers N
+            // One GMRES step: w = A^H A v_j (c64 copy of v_j; one pass over A
+            // when a cluster covers N), the Arnoldi step and Givens rotation,
+            // then the residual estimate to h_pinned[4 + (j & 1)], signalled by
+            // ev_res[j & 1].
+            auto launch_step = [&](int j) {
                 if (!launch_normal_op(R, n, A, lda, w_vf.as<float2>(), w_w.as<double2>(), w_part.as<float2>(),
                                       stream)) {
                     launch_gemv_c64(R, n, A, lda, w_vf.p, 0, w_t.p, 0, stream);              // t = A v_j
@@ -180,9 +182,29 @@ void bem_solver_s::solve_refined(bem_solve_info_t *info) {
                     launch_givens(j, w_H.as<double2>(), ldh, w_cs.as<double2>(), w_sn.as<double2>(),
                                   w_g.as<double2>(), scal + 3, stream);
                 }
+                CUDA_TRY(cudaMemcpyAsync(h_pinned + 4 + (j & 1), scal + 3, sizeof(double), cudaMemcpyDeviceToHost,
+                                         stream));
+                CUDA_TRY(cudaEventRecord(ev_res[j & 1], stream));
+            };
+            // While the previous estimate is well above the tolerance, step
+            // j + 1 is launched before step j's estimate is read, so the host
+            // round trip overlaps the GPU.  Should step j be the last after
+            // all, step j + 1 has only written basis vector j + 2, Hessenberg
+            // column j + 1, rotation j + 1 and g[j + 1], g[j + 2], none of
+            // which the solution over the first j + 1 columns reads.
+            constexpr double kSpeculate = 20.0;
+            int jdone = 0;
+            double prev = 1.0;   // estimate / |g| of the previous step (1 before the first)
+            launch_step(0);
+            for (int j = 0; j < m; j++) {
+                const bool ahead = j + 1 < m && prev > kSpeculate * opt.inner_tol;
+                if (ahead) launch_step(j + 1);
+                CUDA_TRY(cudaEventSynchronize(ev_res[j & 1]));
+                const double res = h_pinned[4 + (j & 1)];
                 jdone = j + 1;
-                const double res = read_scalar(3);
                 if (!(res / gn > opt.inner_tol)) break;
+                prev = res / gn;
+                if (!ahead && j + 1 < m) launch_step(j + 1);
             }
             launch_trisolve(jdone, w_H.as<double2>(), ldh, w_g.as<double2>(), w_y.as<double2>(), stream);
             launch_axpy_combo(n, jdone, V, n, w_y.as<double2>(), x, stream);

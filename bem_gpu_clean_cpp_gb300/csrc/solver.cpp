@@ -97,6 +97,7 @@ bem_solver_s::bem_solver_s() {
     if (cublasCreate(&cublas) != CUBLAS_STATUS_SUCCESS) BEM_FAIL(BEM_ERR_CUDA, "cublasCreate failed");
     cublasSetStream(cublas, stream);
     CUDA_TRY(cudaMallocHost(&h_pinned, 64 * sizeof(double)));
+    for (auto &e : ev_res) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     bem_options_default(&opt);
 }
 
@@ -108,6 +109,8 @@ bem_solver_s::~bem_solver_s() {
     if (cusolver) cusolverDnDestroy(cusolver);
     if (cublas) cublasDestroy(cublas);
     if (h_pinned) cudaFreeHost(h_pinned);
+    for (auto &e : ev_res)
+        if (e) cudaEventDestroy(e);
     if (h_stage) cudaFreeHost(h_stage);
     if (stream) cudaStreamDestroy(stream);
     if (cur >= 0 && cur != device) cudaSetDevice(cur);

@@ -85,6 +85,7 @@ struct bem_solver_s {
     bem::DevMem w_ap;   // partial sums of the cooperative Arnoldi step
     int tf32_split_mode = -1;   // BEM_GEMM_* the planes of A were built for (this assembly), -1 none
     double *h_pinned = nullptr;
+    cudaEvent_t ev_res[2] = {nullptr, nullptr};   // refined GMRES: residual estimate of step j in h_pinned[4 + (j & 1)]
     void *h_stage = nullptr;     // pinned staging for geometry uploads
     size_t h_stage_bytes = 0;
     // QR workspace
