@@ -815,8 +815,13 @@ constexpr int kNearWarps = 4;
 
 // A leaf triangle in the element's (xi1, xi2) coordinates; its corners are
 // multiples of 2^-depth (depth <= 4), exact in float.
+// A leaf triangle in the element's reference coordinates (corners a, b, c;
+// dyadic fractions from midpoint subdivision, exact in float).
+// near_integrate turns a and b into the edges a - c, b - c in place and
+// fills area = |det(a - c, b - c)|, all exact in float.
 struct Leaf {
     float a[2], b[2], c[2];
+    float area;
 };
 
 struct NearOut {
@@ -908,36 +913,34 @@ __device__ int build_leaves_warp(const double *h, const double *x, double eta, i
 // |J|/(4 pi) as in the far path.
 // sin and cos in FP64 for the near-field quadrature: quadrant j = round(2y/pi),
 // z = y - j pi/2 by a three-constant Cody-Waite reduction with FMAs (P1 =
-// fl(pi/2), P2 = fl(pi/2 - P1), P3 = fl(pi/2 - P1 - P2)), then the Taylor
-// series of sin to z^17 and cos to z^18 on |z| <= pi/4 (truncation below
-// 1e-18) and the quadrant's swap and signs.  Near pairs have kr of order one,
-// so the reduction is short and exact; this replaces the general-argument
-// library call on the FP64 pipe, which GB300 runs at ~1/64 of FP32.
+// fl(pi/2), P2 = fl(pi/2 - P1), P3 = fl(pi/2 - P1 - P2)), then on |z| <= pi/4,
+// with u = z^2,  sin z = z + z^3 P(u)  and  cos z = 1 - u/2 + u^2 Q(u)  with
+// P, Q of degree 5: Chebyshev interpolants of the exact functions on
+// [0, (pi/4)^2], coefficients from sincos_fit.py beside this package (max
+// error 7e-17 for sin, 1.2e-16 for cos, evaluated in double), and the
+// quadrant's swap and signs.  Near pairs have kr of order one, so the
+// reduction is short and exact; this replaces the general-argument library
+// call on the FP64 pipe, which GB300 runs at ~1/64 of FP32.
 __device__ __forceinline__ void sincos_near(double y, double *sn, double *cs) {
     const double j = rint(y * 0.6366197723675814);
     double z = fma(-j, 1.5707963267948966, y);
     z = fma(-j, 6.123233995736766e-17, z);
     z = fma(-j, -1.4973849048591698e-33, z);
-    const double z2 = z * z;
-    double ps = 2.8114572543455206e-15;
-    ps = fma(ps, z2, -7.647163731819816e-13);
-    ps = fma(ps, z2, 1.6059043836821613e-10);
-    ps = fma(ps, z2, -2.505210838544172e-08);
-    ps = fma(ps, z2, 2.7557319223985893e-06);
-    ps = fma(ps, z2, -0.0001984126984126984);
-    ps = fma(ps, z2, 0.008333333333333333);
-    ps = fma(ps, z2, -0.16666666666666666);
-    ps = fma(ps * z2, z, z);
-    double pc = -1.5619206968586225e-16;
-    pc = fma(pc, z2, 4.779477332387385e-14);
-    pc = fma(pc, z2, -1.1470745597729725e-11);
-    pc = fma(pc, z2, 2.08767569878681e-09);
-    pc = fma(pc, z2, -2.755731922398589e-07);
-    pc = fma(pc, z2, 2.48015873015873e-05);
-    pc = fma(pc, z2, -0.001388888888888889);
-    pc = fma(pc, z2, 0.041666666666666664);
-    pc = fma(pc, z2, -0.5);
-    pc = fma(pc, z2, 1.0);
+    const double u = z * z;
+    double ps = 1.5918129294866608e-10;
+    ps = fma(ps, u, -2.5051131845003624e-08);
+    ps = fma(ps, u, 2.755731610255244e-06);
+    ps = fma(ps, u, -0.00019841269836758574);
+    ps = fma(ps, u, 0.008333333333330948);
+    ps = fma(ps, u, -0.16666666666666666);
+    ps = fma(ps * u, z, z);
+    double pc = -1.1382632425521717e-11;
+    pc = fma(pc, u, 2.08761462684032e-09);
+    pc = fma(pc, u, -2.7557317271729793e-07);
+    pc = fma(pc, u, 2.480158729876569e-05);
+    pc = fma(pc, u, -0.0013888888888887398);
+    pc = fma(pc, u, 0.041666666666666664);
+    pc = fma(pc, u * u, fma(-0.5, u, 1.0));
     const unsigned q = (unsigned)((long long)j & 3);
     const double s0 = (q & 1u) ? pc : ps, c0 = (q & 1u) ? ps : pc;
     *sn = (q & 2u) ? -s0 : s0;
@@ -952,17 +955,29 @@ __device__ void near_integrate(const double *h, const double *x, double k, int c
     for (int i = 0; i < 13; i++) acc[i] = 0.0;
     const double *n = h + 9;
     const int cv = collapse - 1;
+    // per leaf once: edges and area (exact in float; the leaves are rebuilt
+    // for every pair, so they are changed in place)
+    for (int l = lane; l < nl; l += 32) {
+        Leaf &t = const_cast<Leaf &>(leaves[l]);
+        const float ea0 = t.a[0] - t.c[0], ea1 = t.a[1] - t.c[1];
+        const float eb0 = t.b[0] - t.c[0], eb1 = t.b[1] - t.c[1];
+        t.a[0] = ea0;
+        t.a[1] = ea1;
+        t.b[0] = eb0;
+        t.b[1] = eb1;
+        t.area = fabsf(ea0 * eb1 - ea1 * eb0);
+    }
+    __syncwarp();
+    const double d3[3] = {h[0] - x[0], h[1] - x[1], h[2] - x[2]};
     for (int idx = lane; idx < nl * nq; idx += 32) {
         const int l = idx / nq, q = idx - l * nq;
         const Leaf &t = leaves[l];
-        double ea0 = (double)t.a[0] - t.c[0], ea1 = (double)t.a[1] - t.c[1];
-        double eb0 = (double)t.b[0] - t.c[0], eb1 = (double)t.b[1] - t.c[1];
-        double area = fabs(ea0 * eb1 - ea1 * eb0);
-        double s1 = c_qd[cv][q][0], s2 = c_qd[cv][q][1], w = c_qd[cv][q][2] * area;
+        const double ea0 = t.a[0], ea1 = t.a[1], eb0 = t.b[0], eb1 = t.b[1];
+        double s1 = c_qd[cv][q][0], s2 = c_qd[cv][q][1], w = c_qd[cv][q][2] * (double)t.area;
         double x1 = t.c[0] + s1 * ea0 + s2 * eb0;
         double x2 = t.c[1] + s1 * ea1 + s2 * eb1;
         double d[3];
-        for (int dd = 0; dd < 3; dd++) d[dd] = h[dd] - x[dd] + x1 * h[3 + dd] + x2 * h[6 + dd];
+        for (int dd = 0; dd < 3; dd++) d[dd] = d3[dd] + x1 * h[3 + dd] + x2 * h[6 + dd];
         const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
         const double ri = rsqrt(r2);
         const double r = r2 * ri;
