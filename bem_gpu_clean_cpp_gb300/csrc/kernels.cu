@@ -969,6 +969,11 @@ __device__ void near_integrate(const double *h, const double *x, double k, int c
     }
     __syncwarp();
     const double d3[3] = {h[0] - x[0], h[1] - x[1], h[2] - x[2]};
+    // dr/dn = (d . n)/r with d . n = d3 . n for every point of the flat
+    // element (its edges are orthogonal to n): the height leaves the sums,
+    //   4 pi dG/dn = -hgt (gr + k s + i (k c - gs)) / r^2,  4 pi dG0/dn = -hgt / r^3
+    // (gr = c/r, gs = s/r), as in the far-field sums.
+    const double hgt = d3[0] * n[0] + d3[1] * n[1] + d3[2] * n[2];
     for (int idx = lane; idx < nl * nq; idx += 32) {
         const int l = idx / nq, q = idx - l * nq;
         const Leaf &t = leaves[l];
@@ -981,26 +986,30 @@ __device__ void near_integrate(const double *h, const double *x, double k, int c
         const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
         const double ri = rsqrt(r2);
         const double r = r2 * ri;
-        double drdn = (d[0] * n[0] + d[1] * n[1] + d[2] * n[2]) * ri;
         double sn, cs;
         sincos_near(k * r, &sn, &cs);
-        double gr = cs * ri, gi = -sn * ri;
-        double tr = gi * k - gr * ri, ti = -(gr * k + gi * ri);
-        double dgr = tr * drdn, dgi = ti * drdn;
-        double c0 = -drdn * ri * ri;
-        double N[3] = {x1, x2, 1.0 - x1 - x2};
+        const double ri2 = ri * ri;
+        const double gr = cs * ri, gs = sn * ri;
+        const double ha = ri2 * fma(k, sn, gr), hb = ri2 * fma(k, cs, -gs);
+        const double ri3 = ri2 * ri;
+        const double wn[3] = {w * x1, w * x2, w * (1.0 - x1 - x2)};
 #pragma unroll
         for (int j = 0; j < 3; j++) {
-            acc[j] += w * N[j] * gr;
-            acc[3 + j] += w * N[j] * gi;
-            acc[6 + j] += w * N[j] * dgr;
-            acc[9 + j] += w * N[j] * dgi;
+            acc[j] += wn[j] * gr;
+            acc[3 + j] += wn[j] * gs;
+            acc[6 + j] += wn[j] * ha;
+            acc[9 + j] += wn[j] * hb;
         }
-        acc[12] += w * c0;
+        acc[12] += w * ri3;
     }
 #pragma unroll
     for (int i = 0; i < 13; i++)
         for (int off = 16; off > 0; off >>= 1) acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], off);
+    // signs and the height: G = (gr, -gs), dG/dn = -hgt (ha, hb), dG0/dn = -hgt ri3
+#pragma unroll
+    for (int j = 0; j < 3; j++) acc[3 + j] = -acc[3 + j];
+#pragma unroll
+    for (int i = 6; i < 13; i++) acc[i] *= -hgt;
     const double scale = h[12] / (4.0 * kPi);
     for (int j = 0; j < 3; j++) {
         o.gr[j] = scale * acc[j];
