@@ -84,6 +84,12 @@ std::vector<int> color_elements(int N, const std::vector<int> &elems) {
     return color;
 }
 
+// Far-kernel launch shapes chosen by the autotuner, per device and problem
+// shape (precision, N, R, tile width, tiles, Gauss points), for the process.
+using FarTuneKey = std::tuple<int, int, int, int, int, int, int>;
+std::mutex g_far_tune_mu;
+std::map<FarTuneKey, int> g_far_tuned;
+
 }  // namespace
 }  // namespace bem
 
@@ -416,23 +422,31 @@ void bem_solver_s::assemble(double kk, int precision) {
     bool done = false;
     if (variant < 0) {
         variant = 0;
-        auto key = std::make_tuple(precision, N, R, T.tc_max, T.ntiles, quadrature_points());
-        auto it = far_tuned.find(key);
-        if (it != far_tuned.end()) {
-            variant = it->second;
+        const FarTuneKey key{device, precision, N, R, T.tc_max, T.ntiles, quadrature_points()};
+        int cached = -1;
+        {
+            std::lock_guard<std::mutex> lk(g_far_tune_mu);
+            auto it = g_far_tuned.find(key);
+            if (it != g_far_tuned.end()) cached = it->second;
+        }
+        if (cached >= 0) {
+            variant = cached;
         } else if (far_variants(precision) > 1) {
             // Autotune: time every launch shape that fits (twice, keep the
-            // minimum) on this very assembly; the last launch leaves a complete
-            // far-field A, so no extra launch is needed afterwards.
+            // minimum; once when a launch takes over 20 ms) on this very
+            // assembly; the last launch leaves a complete far-field A, so no
+            // extra launch is needed afterwards when it is the chosen shape.
+            // The result is shared by every solver of the process on this
+            // device (the request server's slots tune a problem shape once).
             cudaEvent_t e0, e1;
             CUDA_TRY(cudaEventCreate(&e0));
             CUDA_TRY(cudaEventCreate(&e1));
             float best = 1e30f;
-            int last = -1;
+            int last = -1, reps = 2;
             for (int v = 0; v < far_variants(precision); v++) {
                 if (!far_variant_fits(precision, T.tc_max, v)) continue;
                 last = v;
-                for (int rep = 0; rep < 2; rep++) {
+                for (int rep = 0; rep < reps; rep++) {
                     CUDA_TRY(cudaEventRecord(e0, stream));
                     launch_far_assembly(precision, row_points(), N, geo_tables(), ts, ph, d_A.p, lda,
                                         d_cpart.p, d_bpart.p, stream, v);
@@ -441,11 +455,16 @@ void bem_solver_s::assemble(double kk, int precision) {
                     float ms = 0.f;
                     CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
                     if (ms < best) { best = ms; variant = v; }
+                    if (ms > 20.f) reps = 1;
                 }
             }
             cudaEventDestroy(e0);
             cudaEventDestroy(e1);
-            far_tuned[key] = variant;
+            {
+                std::lock_guard<std::mutex> lk(g_far_tune_mu);
+                g_far_tuned.emplace(key, variant);   // a concurrent tuner's entry stays if it came first
+                variant = g_far_tuned[key];
+            }
             // The shapes split the c and beta row sums differently (FP32 order),
             // so the matrix is left by the chosen shape: every assembly of this
             // problem shape then gives the same bits.

@@ -66,8 +66,6 @@ struct bem_solver_s {
         bem::DevMem recs, rec_ptr, cols, col_cnt;
     } tiles[2];
 
-    // autotuned far-kernel launch shape per (precision, N, rows, tile width, tiles, Gauss points)
-    std::map<std::tuple<int, int, int, int, int, int>, int> far_tuned;
     int far_variant_used = -1;
 
     int prec = -1;
