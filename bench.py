@@ -62,7 +62,8 @@ def parse_args():
                          "8 kHz, 256 point sources solved together (block GMRES); freq: 64 frequencies of "
                          "uneven mesh size as one batch; serve: Poisson request stream through the server")
     ap.add_argument("--sources", type=int, default=256, help="rhs: point sources (the configuration has 256)")
-    ap.add_argument("--max-iter", type=int, default=100, help="rhs: inner GMRES iterations per refinement cycle")
+    ap.add_argument("--max-iter", type=int, default=100,
+                    help="rhs/freq/serve: block GMRES iterations per refinement cycle")
     ap.add_argument("--inner-tol", type=float, default=1e-4, help="rhs: inner GMRES relative tolerance")
     ap.add_argument("--slots", type=int, default=8, help="freq/serve: requests in flight at once")
     ap.add_argument("--rate", type=float, default=2.0, help="serve: mean request arrivals per second")
@@ -661,7 +662,7 @@ def run_server_bench(args):
     dist = Dist(use_cuda=True)
     torch.cuda.set_device(dist.local)
     bem.lib()
-    opts = dict(near_eta=args.eta, near_depth=args.depth, tol=1e-8, inner_tol=1e-4, max_iter=100,
+    opts = dict(near_eta=args.eta, near_depth=args.depth, tol=1e-8, inner_tol=1e-4, max_iter=args.max_iter,
                 max_refine=10, block_tol=1e-8, gemm_mode=args.gemm)
     if args.config == "freq":
         probs, name, cache = freq_problems(args), WORKLOAD_FREQ, 0
