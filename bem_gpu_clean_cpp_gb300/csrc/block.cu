@@ -23,8 +23,9 @@
 // double-float arithmetic on the FP32 pipe (8 sources per pass over A); after
 // every later cycle it is updated with that cycle's correction D, R -= A D,
 // by the first GEMM (|A D| has already shrunk by inner_tol, so the GEMM's
-// FP32-level error stays below the FP64 level of R).  G = A^H R, whose input
-// is already small, uses the second GEMM.  On GB300 the FP64 pipe runs at
+// FP32-level error stays below the FP64 level of R).  G = A^H R cancels
+// strongly (R, the least-squares residual, does not vanish), so it runs
+// FP32-accurate (split-BF16 or FP32) in every mode.  On GB300 the FP64 pipe runs at
 // about 1/64 of FP32, so FP64 Arnoldi over 256 Krylov spaces would cost more
 // than the GEMMs themselves.
 #include <cublas_v2.h>
@@ -83,15 +84,6 @@ __global__ void build_vt_kernel(int N, int S, const T *__restrict__ V, float *__
         } else {
             Vt[o[q]] = val[q];
         }
-    }
-}
-
-// In place: x -> TF32 head, lo -> tail (n floats).
-__global__ void split_tf32_kernel(size_t n, float *__restrict__ x, float *__restrict__ lo) {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        const float v = x[i], h = tf32_head(v);
-        x[i] = h;
-        lo[i] = v - h;
     }
 }
 
@@ -231,14 +223,38 @@ resid_df_multi_kernel(int R, int N, int S, const float2 *__restrict__ A, size_t 
     }
 }
 
-// W (N x S complex, float) from Wt (2N x 2S).
-__global__ void combine_w_kernel(int N, int S, const float *__restrict__ Wt, float2 *__restrict__ W) {
+// W (N x S complex, float) from Wt (2N x 2S), or from Wt + Wb (TF32x3: the
+// head product and the two tail products, each 2N x 2S).
+__global__ void combine_w_kernel(int N, int S, const float *__restrict__ Wt, const float *__restrict__ Wb,
+                                 float2 *__restrict__ W) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x, s = blockIdx.y;
     if (j >= N) return;
     const size_t ld = 2 * (size_t)N;
-    const float a = Wt[(size_t)s * ld + 2 * j], b = Wt[(size_t)(S + s) * ld + 2 * j + 1];
-    const float c = Wt[(size_t)(S + s) * ld + 2 * j], d = Wt[(size_t)s * ld + 2 * j + 1];
+    const size_t oa = (size_t)s * ld + 2 * j, ob = (size_t)(S + s) * ld + 2 * j + 1;
+    const size_t oc = (size_t)(S + s) * ld + 2 * j, od = (size_t)s * ld + 2 * j + 1;
+    float a = Wt[oa], b = Wt[ob], c = Wt[oc], d = Wt[od];
+    if (Wb) {
+        a += Wb[oa];
+        b += Wb[ob];
+        c += Wb[oc];
+        d += Wb[od];
+    }
     W[(size_t)s * N + j] = make_float2(a + b, c - d);
+}
+
+// out[i] = pair[i] + pair[n + i] (the two halves of a TF32x3 product pair).
+__global__ void add_halves_kernel(size_t n, const float *__restrict__ pair, float *__restrict__ out) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = pair[i] + pair[n + i];
+}
+
+// pair = [head(x) | tail(x)] (TF32 head, exact tail), n floats each.
+__global__ void split_pair_kernel(size_t n, const float *__restrict__ x, float *__restrict__ pair) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float v = x[i], h = tf32_head(v);
+        pair[i] = h;
+        pair[n + i] = v - h;
+    }
 }
 
 // h[s*ldv + l] = V_l(:,s)^H W(:,s) for l in [l0, l0 + kDotLB) ∩ [0, nl).
@@ -529,9 +545,11 @@ void cublas_ok(cublasStatus_t s, const char *what) {
 }  // namespace
 
 // Tt (R x 2S) = At^T Vt (first) and/or Wt (2N x 2S) = At Tt (second).  In
-// TF32x3 mode Vt holds the heads and Vlo the tails of the right-hand block,
-// and Tt is split in place (Tlo) before the second product; each product is
-// head*tail + tail*head + head*head, smallest terms first.
+// TF32x3 mode Vt holds the heads and Vlo = Vt + 4NS the tails of the
+// right-hand block, Tlo is scratch for the product pair (R x 4S), Wt holds
+// the pair [Wa | Wb] (2N x 4S) that combine_w adds; each product is
+// head(A) [head(B) | tail(B)] (one pass over the head plane of A for two of
+// the three terms) plus tail(A) head(B) onto the second half.
 static void normal_gemms(bem_solver_s &sv, int mode, const float *Vt, const float *Vlo, float *Tt, float *Tlo,
                          float *Wt, int S, bool first, bool second) {
     const float one = 1.f, zero = 0.f;
@@ -553,12 +571,27 @@ static void normal_gemms(bem_solver_s &sv, int mode, const float *Vt, const floa
                                CUDA_R_32F, R, beta, Wt, CUDA_R_32F, 2 * N, ct, CUBLAS_GEMM_DEFAULT),
                   "GEMM A^H T");
     };
+    // C = [Ahi B | Ahi Blo + Alo B] for B = [B | Blo] (k x 4S, ld ldb; each
+    // half k x 2S): one pass over the head plane for both terms, then the
+    // tail plane's product added onto the second half
+    auto gemm_pair = [&](cublasOperation_t op, int m, int k, const float *Ahi, const float *Alo, int lda_,
+                         const float *B, int ldb, float *C, int ldc) {
+        cublas_ok(cublasGemmEx(sv.cublas, op, CUBLAS_OP_N, m, 4 * S, k, &one, Ahi, CUDA_R_32F, lda_, B, CUDA_R_32F,
+                               ldb, &zero, C, CUDA_R_32F, ldc, ct, CUBLAS_GEMM_DEFAULT),
+                  "GEMM (TF32x3, head)");
+        cublas_ok(cublasGemmEx(sv.cublas, op, CUBLAS_OP_N, m, 2 * S, k, &one, Alo, CUDA_R_32F, lda_, B, CUDA_R_32F,
+                               ldb, &one, C + (size_t)ldc * 2 * S, CUDA_R_32F, ldc, ct, CUBLAS_GEMM_DEFAULT),
+                  "GEMM (TF32x3, tail)");
+    };
     if (first) {
         BEM_PROF("gemm_AV", sv.stream);
         if (x3) {
-            gemm1(Ahi, Vlo, &zero);
-            gemm1(Alo, Vt, &one);
-            gemm1(Ahi, Vt, &one);
+            // Vlo = Vt + 4NS (the block [Vt | Vlo] is 2N x 4S), Tlo = the pair
+            // [Ta | Tb] (R x 4S): Ta = Ahi Vt, Tb = Ahi Vlo + Alo Vt, Tt = Ta + Tb
+            gemm_pair(CUBLAS_OP_T, R, 2 * N, Ahi, Alo, ldat, Vt, 2 * N, Tlo, R);
+            add_halves_kernel<<<(unsigned)std::min<size_t>((2 * (size_t)R * S + 255) / 256, 4096), 256, 0,
+                                sv.stream>>>(2 * (size_t)R * S, Tlo, Tt);
+            count_launch();
         } else {
             gemm1(At, Vt, &zero);
         }
@@ -566,12 +599,12 @@ static void normal_gemms(bem_solver_s &sv, int mode, const float *Vt, const floa
     if (second) {
         BEM_PROF("gemm_AhT", sv.stream);
         if (x3) {
+            // Tlo = [head(Tt) | tail(Tt)] (R x 4S); Wt = [Wa | Wb] (2N x 4S):
+            // Wa = Ahi head, Wb = Ahi tail + Alo head (combine_w adds them)
             const size_t n = 2 * (size_t)R * S;
-            split_tf32_kernel<<<(unsigned)std::min<size_t>((n + 255) / 256, 4096), 256, 0, sv.stream>>>(n, Tt, Tlo);
+            split_pair_kernel<<<(unsigned)std::min<size_t>((n + 255) / 256, 4096), 256, 0, sv.stream>>>(n, Tt, Tlo);
             count_launch();
-            gemm2(Ahi, Tlo, &zero);
-            gemm2(Alo, Tt, &one);
-            gemm2(Ahi, Tt, &one);
+            gemm_pair(CUBLAS_OP_N, 2 * N, R, Ahi, Alo, ldat, Tlo, R, Wt, 2 * N);
         } else {
             gemm2(At, Tt, &zero);
         }
@@ -650,14 +683,19 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
     float2 *xh = w_gv.as<float2>(), *xl = xh + (size_t)ldx * S;
     float *Vt = w_vf.as<float>(), *Tt = w_t.as<float>(), *Wt = w_part.as<float>();
     const float2 *A = d_A.as<float2>();
-    const int gmode = block_gemm_mode(opt, S);
+    const int gmode = block_gemm_mode(opt, S, R, n);
     const bool x3 = gmode == BEM_GEMM_TF32X3, x3m = gmode == BEM_GEMM_TF32X3_3M;
     float *Vlo = nullptr, *Tlo = nullptr, *A3 = nullptr, *B3 = nullptr, *C3 = nullptr;
     if (x3) {
-        x_vlo.ensure(sizeof(float) * 4 * NS);
-        x_tlo.ensure(sizeof(float) * 2 * (size_t)R * S);
-        Vlo = x_vlo.as<float>();
+        // [Vt | Vlo] (2N x 4S), the product pair [Ta | Tb] or [head | tail]
+        // of Tt (R x 4S), and [Wa | Wb] (2N x 4S)
+        x_vlo.ensure(sizeof(float) * 8 * NS);
+        x_tlo.ensure(sizeof(float) * 4 * (size_t)R * S);
+        w_part.ensure(sizeof(float) * 8 * NS);
+        Vt = x_vlo.as<float>();
+        Vlo = Vt + 4 * NS;
         Tlo = x_tlo.as<float>();
+        Wt = w_part.as<float>();
         if (tf32_split_mode != gmode) {
             x_Ahi.ensure(sizeof(float) * 2 * lda * (size_t)R);
             x_Alo.ensure(sizeof(float) * 2 * lda * (size_t)R);
@@ -685,14 +723,13 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
     }
     // T = A X into Tt (X: the FP64 correction or an FP32 basis block), and
     // W = A^H T from Tt, in the mode's form
+    // R -= A D once per refinement cycle (D: the cycle's FP64 correction):
+    // FP32-accurate like the gradient, whatever the inner products use
     auto apply_a_d = [&](const double2 *Xs) {
-        if (x3m) {
-            apply_a_3m<double2>(*this, Xs, A3, B3, C3, Tt);
-            return;
-        }
-        build_vt_kernel<double2><<<grid2(n, S), 256, 0, stream>>>(n, S, Xs, Vt, Vlo);
+        const int gm = gmode == BEM_GEMM_FP32 ? BEM_GEMM_FP32 : BEM_GEMM_SPLIT_BF16;
+        build_vt_kernel<double2><<<grid2(n, S), 256, 0, stream>>>(n, S, Xs, Vt, nullptr);
         count_launch();
-        normal_gemms(*this, gmode, Vt, Vlo, Tt, Tlo, Wt, S, true, false);
+        normal_gemms(*this, gm, Vt, nullptr, Tt, nullptr, Wt, S, true, false);
     };
     auto apply_a_f = [&](const float2 *Xs) {
         if (x3m) {
@@ -709,7 +746,18 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
             return;
         }
         normal_gemms(*this, gmode, Vt, Vlo, Tt, Tlo, Wt, S, false, true);
-        combine_w_kernel<<<grid2(n, S), 256, 0, stream>>>(n, S, Wt, W);
+        combine_w_kernel<<<grid2(n, S), 256, 0, stream>>>(n, S, Wt, x3 ? Wt + 4 * NS : nullptr, W);
+        count_launch();
+    };
+    // G = A^H R once per refinement cycle.  R is the least-squares residual,
+    // which the CHIEF rows keep from vanishing, so the product cancels
+    // strongly and its rounding bounds what the refinement can reach: it runs
+    // FP32-accurate (split-BF16 emulation, or plain FP32 in FP32 mode) whatever
+    // the inner products use.
+    auto apply_ah_grad = [&]() {
+        const int gm = gmode == BEM_GEMM_FP32 ? BEM_GEMM_FP32 : BEM_GEMM_SPLIT_BF16;
+        normal_gemms(*this, gm, Vt, nullptr, Tt, nullptr, Wt, S, false, true);
+        combine_w_kernel<<<grid2(n, S), 256, 0, stream>>>(n, S, Wt, nullptr, W);
         count_launch();
     };
     std::vector<double> h_bn(S), h_gn(S), h_res(S);
@@ -745,7 +793,7 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
             resid_update_kernel<<<grid2(R, S), 256, 0, stream>>>(R, S, Rv, Tt);
             count_launch();
         }
-        apply_ah();
+        apply_ah_grad();
         bnrm2_kernel<<<S, 256, 0, stream>>>(n, W, nrm_g);
         count_launch();
         KERNEL_CHECK();

@@ -610,7 +610,7 @@ def run_ours(args):
         "config": {"workload": name, "sources": S, "nodes": N, "triangles": E, "chief": M,
                    **({"subdiv": args.subdiv, "ka": args.ka} if args.config == "precision" else
                       {"k": k, "solver": "block GMRES: %s GEMMs, FP32 Arnoldi, FP64 Givens, FP64-accurate "
-                                          "refinement residual to 1e-8" % {-1: "auto (TF32x3 from 48 sources)", 0: "FP32",
+                                          "refinement residual to 1e-8" % {-1: "auto (A <= 4 GB: TF32x3 3M from 128 sources, TF32x3 from 4)", 0: "FP32",
                                                             1: "split-BF16", 2: "TF32", 3: "TF32x3",
                                                             4: "TF32x3 3M"}[args.gemm]}),
                    "seed": args.seed, "near_eta": args.eta, "near_depth": args.depth,

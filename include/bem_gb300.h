@@ -190,18 +190,21 @@ typedef struct {
 
 enum { BEM_PREC_C64 = 0, BEM_PREC_C128 = 1 };
 enum { BEM_SOLVE_QR = 0, BEM_SOLVE_GMRES_REFINED = 1, BEM_SOLVE_BLOCK_GMRES = 2 };
-/* Block-solve GEMMs: FP32 (SIMT), FP32-accurate split-BF16 emulation on the
- * tensor cores (cuBLAS), plain TF32, or TF32x3 (A and the right-hand block
- * split into TF32 head + tail, three TF32 GEMMs: hh + ht + th) on the
- * interleaved-real form of the complex product (four real products), or
- * TF32x3 in the 3M form (separate planes of Re A, Im A, Re A + Im A: three
- * real products per complex product, a quarter fewer flops; each product is
- * head(A) [head(B) | tail(B)] plus tail(A) head(B), so A's bytes read per
- * complex product equal the interleaved form's).  AUTO takes the 3M form from
- * 128 right-hand sides on (measured faster at 256), TF32x3 from 48 (the
- * products are tensor-bound there), split-BF16 from 32, and FP32 below 32,
- * where the tensor kernels' wide tiles are mostly padding and one SIMT pass
- * over A is as fast. */
+/* Block-solve GEMMs (the products inside the inner GMRES): FP32 (SIMT),
+ * FP32-accurate split-BF16 emulation on the tensor cores (cuBLAS), plain
+ * TF32, TF32x3 on the interleaved-real form of the complex product (A and the
+ * right-hand block split into TF32 head + tail; each product is
+ * head(A) [head(B) | tail(B)] plus tail(A) head(B): two passes over A's
+ * planes), or TF32x3 in the 3M form (separate planes of Re A, Im A,
+ * Re A + Im A: three real products per complex product, a quarter fewer
+ * flops, the same passes).  The once-per-cycle refinement products (the
+ * residual update R -= A D and the gradient A^H R) run FP32-accurate
+ * (split-BF16, or FP32 in FP32 mode) in every mode.  AUTO, while the c64
+ * matrix is at most 4 GB: the 3M form from 128 right-hand sides on,
+ * interleaved TF32x3 from 4 (measured faster than split-BF16 and FP32 at 8,
+ * 16 and 64), FP32 below 4 (bandwidth-bound: one pass over A beats two over
+ * the planes).  Above 4 GB the planes' memory would cost concurrent requests
+ * more than the products gain: split-BF16 from 32, FP32 below. */
 enum { BEM_GEMM_AUTO = -1, BEM_GEMM_FP32 = 0, BEM_GEMM_SPLIT_BF16 = 1, BEM_GEMM_TF32 = 2, BEM_GEMM_TF32X3 = 3,
        BEM_GEMM_TF32X3_3M = 4 };
 

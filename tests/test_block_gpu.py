@@ -26,7 +26,7 @@ def _ellipsoid_problem(bemlib, nu=8, nsrc=16, f_hz=4000.0, seed=3):
     return p, e, chief, srcs, bc, k
 
 
-@pytest.mark.parametrize("gemm_mode", [0, 1, 3, 4])
+@pytest.mark.parametrize("gemm_mode", [-1, 0, 1, 3, 4])
 def test_block_gmres_matches_fp64(bemlib, gemm_mode):
     p, e, chief, srcs, bc, k = _ellipsoid_problem(bemlib)
     s = bemlib.Solver(gemm_mode=gemm_mode, block_tol=1e-8)
