@@ -396,7 +396,8 @@ def run_reference(args):
 # Our arm
 # ---------------------------------------------------------------------------
 # Algorithmic bytes per launch of the HBM-bound kernels (A is (N+M) x N c64);
-# normal_op reads A once for w = A^H (A v) (v in, w out).
+# normal_op reads A once for w = A^H (A v) (v in, w out; its FP64 sum of the
+# clusters' partial w is a separate kernel, timed as normal_op_sum).
 def kernel_bytes(name, R, N):
     a = 8.0 * R * N
     return {"normal_op": a + 24.0 * N,
