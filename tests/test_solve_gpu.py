@@ -38,7 +38,7 @@ def test_qr_c128_matches_oracle(bemlib, orc):
     assert rel_err(x, xo) < 1e-10
 
 
-def test_refined_gmres_config1(bemlib, orc):
+def test_refined_gmres_icosphere_s3_ka1(bemlib, orc):
     """Rigid unit sphere, icosphere subdivision 3 (642 nodes, 1280
     triangles), plane wave along +z at ka = 1, 8 seeded CHIEF points in
     r < 0.5: mixed-precision solve within 1e-5 of the FP64 solve, and within
