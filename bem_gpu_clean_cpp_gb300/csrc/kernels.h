@@ -146,7 +146,8 @@ bool normal_op_timed_out(cudaStream_t st);
 int gemv_h_f64_splits(int R, int N);
 // FP64 accumulation variants (the refinement residuals): A is c64 or c128.
 // r = b - A x.  For c64 A the products are exact double-float FP32
-// arithmetic; xsplit is scratch for x's float head and tail (2N c64).
+// arithmetic; xsplit is scratch for x's float head and tail (2N + 1 c64:
+// the tail starts at N rounded up to even).
 void launch_resid(int prec, int R, int N, const void *A, size_t lda, const double2 *x,
                   const double2 *b, double2 *r, float2 *xsplit, cudaStream_t st);
 // w = A^H u, FP64-accurate; for c64 A, usplit is scratch for u's float head

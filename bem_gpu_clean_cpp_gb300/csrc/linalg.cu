@@ -1148,11 +1148,14 @@ void launch_resid(int prec, int R, int N, const void *A, size_t lda, const doubl
     BEM_PROF("resid", st);
     if (R <= 0) return;
     if (prec == BEM_PREC_C64) {
-        split_f64_kernel<<<blocks(N, 256), 256, 0, st>>>(N, x, xsplit, xsplit + N);
+        // resid_df_kernel reads the head and the tail of x as float4 (two
+        // entries): the tail starts at an even offset, 16-byte aligned for odd N too
+        float2 *xtail = xsplit + ((N + 1) & ~1);
+        split_f64_kernel<<<blocks(N, 256), 256, 0, st>>>(N, x, xsplit, xtail);
         count_launch();
         KERNEL_CHECK();
         resid_df_kernel<<<blocks(R, kMvRPW * kMvWPC), 32 * kMvWPC, 0, st>>>(R, N, (const float2 *)A, lda, xsplit,
-                                                                          xsplit + N, b, r);
+                                                                          xtail, b, r);
     } else {
         resid_kernel<double2><<<blocks(R, 8), 256, 0, st>>>(R, N, (const double2 *)A, lda, x, b, r);
     }

@@ -108,9 +108,9 @@ void bem_solver_s::solve_refined(bem_solve_info_t *info) {
     w_t.ensure(sizeof(float2) * R);
     w_r.ensure(sizeof(double2) * R);
     w_gv.ensure(sizeof(double2) * n);
-    // c64 copy of v_j and the float head/tail split of x (residual) or of a
-    // length-R vector (A^H u): 2 max(N, R) c64
-    w_vf.ensure(sizeof(float2) * 2 * (size_t)std::max(n, R));
+    // c64 copy of v_j and the float head/tail split of x (residual; the tail
+    // at an even offset) or of a length-R vector (A^H u): 2 max(N, R) + 2 c64
+    w_vf.ensure(sizeof(float2) * (2 * (size_t)std::max(n, R) + 2));
     size_t part = std::max(sizeof(float2) * (size_t)gemv_h_splits(R, n), sizeof(double2) * (size_t)gemv_h_f64_splits(R, n));
     part = std::max(part, sizeof(float2) * (size_t)normal_op_clusters(n));
     w_part.ensure(part * n);

@@ -244,3 +244,50 @@ def test_normal_op_variants(bemlib, variant):
     assert out.returncode == 0, out.stderr[-2000:]
     line = [ln for ln in out.stdout.splitlines() if ln.startswith("RESULT")][-1].split()
     assert line[1] == "1" and float(line[2]) < 1e-5, line
+
+
+def _uv_sphere(n_lat, n_lon, radius=1.0):
+    """Closed latitude-longitude sphere: two poles and n_lat rings of n_lon
+    nodes (2 + n_lat n_lon nodes, odd when n_lat and n_lon are odd)."""
+    pts = [[0.0, 0.0, radius]]
+    for i in range(1, n_lat + 1):
+        th = np.pi * i / (n_lat + 1)
+        for j in range(n_lon):
+            ph = 2 * np.pi * j / n_lon
+            pts.append([radius * np.sin(th) * np.cos(ph), radius * np.sin(th) * np.sin(ph), radius * np.cos(th)])
+    pts.append([0.0, 0.0, -radius])
+    south = len(pts) - 1
+    ring = lambda i, j: 1 + (i - 1) * n_lon + (j % n_lon)
+    tri = []
+    for j in range(n_lon):
+        tri.append([0, ring(1, j), ring(1, j + 1)])
+        tri.append([south, ring(n_lat, j + 1), ring(n_lat, j)])
+    for i in range(1, n_lat):
+        for j in range(n_lon):
+            a, b, c, d = ring(i, j), ring(i, j + 1), ring(i + 1, j), ring(i + 1, j + 1)
+            tri += [[a, c, b], [b, c, d]]
+    return np.array(pts), np.array(tri, dtype=np.int32)
+
+
+def test_refined_solve_odd_node_count(bemlib):
+    """7577 nodes (odd): the fused normal operator's second column segment
+    has an odd length (1945 columns), so its bulk copy is rounded up into the
+    row padding, which must stay masked.  Refined GMRES against the FP64 QR
+    solve."""
+    p, e = _uv_sphere(75, 101)
+    assert p.shape[0] == 7577
+    m = bemlib.Mesh.from_arrays(p, e)
+    m.orient()
+    p, e = m.points(), m.elems()
+    rng = np.random.default_rng(7577)
+    chief = rng.uniform(-0.3, 0.3, (8, 3))
+    s = bemlib.Solver(near_eta=1.0, near_depth=2)
+    s.set_geometry(p, e, bc=np.tile(np.array([0, 1, 0], dtype=np.complex128), (e.shape[0], 1)), chief=chief)
+    s.set_sources([("plane", np.array([0.0, 0.6, 0.8]), 1.0)])
+    s.assemble(4.0, bemlib.PREC_C128)
+    s.solve(bemlib.SOLVE_QR)
+    x64 = s.solution()
+    s.assemble(4.0, bemlib.PREC_C64)
+    info = s.solve(bemlib.SOLVE_GMRES_REFINED)
+    assert info.converged
+    assert rel_err(s.solution(), x64) < 1e-5
