@@ -78,3 +78,26 @@ def rel_err(a, b):
     a = np.asarray(a)
     b = np.asarray(b)
     return float(np.abs(a - b).max() / np.abs(b).max())
+
+
+def uv_sphere(n_lat, n_lon, radius=1.0):
+    """Closed latitude-longitude sphere: two poles and n_lat rings of n_lon
+    nodes (2 + n_lat n_lon nodes, odd when n_lat and n_lon are odd)."""
+    pts = [[0.0, 0.0, radius]]
+    for i in range(1, n_lat + 1):
+        th = np.pi * i / (n_lat + 1)
+        for j in range(n_lon):
+            ph = 2 * np.pi * j / n_lon
+            pts.append([radius * np.sin(th) * np.cos(ph), radius * np.sin(th) * np.sin(ph), radius * np.cos(th)])
+    pts.append([0.0, 0.0, -radius])
+    south = len(pts) - 1
+    ring = lambda i, j: 1 + (i - 1) * n_lon + (j % n_lon)
+    tri = []
+    for j in range(n_lon):
+        tri.append([0, ring(1, j), ring(1, j + 1)])
+        tri.append([south, ring(n_lat, j + 1), ring(n_lat, j)])
+    for i in range(1, n_lat):
+        for j in range(n_lon):
+            a, b, c, d = ring(i, j), ring(i, j + 1), ring(i + 1, j), ring(i + 1, j + 1)
+            tri += [[a, c, b], [b, c, d]]
+    return np.array(pts), np.array(tri, dtype=np.int32)

@@ -5,7 +5,7 @@ against the FP64 solve of the same system (1e-5 relative)."""
 import numpy as np
 import pytest
 
-from helpers import rel_err
+from helpers import rel_err, uv_sphere
 
 pytestmark = pytest.mark.gpu
 
@@ -60,3 +60,30 @@ def test_block_gmres_tf32_mode_runs(bemlib):
     info = s.solve(bemlib.SOLVE_BLOCK_GMRES, check=False)
     assert rel_err(s.solution(), x64) < 1e-2
     assert info.rel_residual < 1e-2
+
+
+@pytest.mark.parametrize("gemm_mode", [-1, 4])
+def test_block_gmres_odd_node_count(bemlib, gemm_mode):
+    """3005 nodes (odd: the interleaved and 3M TF32x3 planes and right-hand
+    blocks have odd leading dimensions), 5 point sources; AUTO takes the
+    interleaved TF32x3 products here.  Against the FP64 solve."""
+    p, e = uv_sphere(39, 77)
+    assert p.shape[0] % 2 == 1
+    m = bemlib.Mesh.from_arrays(p, e)
+    m.orient()
+    p, e = m.points(), m.elems()
+    chief = np.random.default_rng(39).uniform(-0.3, 0.3, (6, 3))
+    srcs = [("point", s, 1.0) for s in bemlib.fibonacci_sphere(5, 3.0)]
+    s = bemlib.Solver(gemm_mode=gemm_mode, block_tol=1e-8)
+    s.set_geometry(p, e, bc=np.tile(np.array([0, 1, 0], dtype=np.complex128), (e.shape[0], 1)), chief=chief)
+    s.set_sources(srcs)
+    s.assemble(6.0, bemlib.PREC_C128)
+    s.solve(bemlib.SOLVE_QR)
+    x64 = s.solution()
+    s.assemble(6.0, bemlib.PREC_C64)
+    info = s.solve(bemlib.SOLVE_BLOCK_GMRES)
+    assert info.converged
+    xb = s.solution()
+    for j in range(xb.shape[1]):
+        assert rel_err(xb[:, j], x64[:, j]) < 1e-5, j
+

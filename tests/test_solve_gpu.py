@@ -7,7 +7,7 @@ the same formulation; c64 field evaluation 1e-5."""
 import numpy as np
 import pytest
 
-from helpers import FIELD_GOLDEN, GOLDEN, K_GOLDEN, chief_candidates, float_bb, golden, icosphere, rel_err
+from helpers import FIELD_GOLDEN, GOLDEN, K_GOLDEN, chief_candidates, float_bb, golden, icosphere, rel_err, uv_sphere
 
 pytestmark = pytest.mark.gpu
 
@@ -246,35 +246,12 @@ def test_normal_op_variants(bemlib, variant):
     assert line[1] == "1" and float(line[2]) < 1e-5, line
 
 
-def _uv_sphere(n_lat, n_lon, radius=1.0):
-    """Closed latitude-longitude sphere: two poles and n_lat rings of n_lon
-    nodes (2 + n_lat n_lon nodes, odd when n_lat and n_lon are odd)."""
-    pts = [[0.0, 0.0, radius]]
-    for i in range(1, n_lat + 1):
-        th = np.pi * i / (n_lat + 1)
-        for j in range(n_lon):
-            ph = 2 * np.pi * j / n_lon
-            pts.append([radius * np.sin(th) * np.cos(ph), radius * np.sin(th) * np.sin(ph), radius * np.cos(th)])
-    pts.append([0.0, 0.0, -radius])
-    south = len(pts) - 1
-    ring = lambda i, j: 1 + (i - 1) * n_lon + (j % n_lon)
-    tri = []
-    for j in range(n_lon):
-        tri.append([0, ring(1, j), ring(1, j + 1)])
-        tri.append([south, ring(n_lat, j + 1), ring(n_lat, j)])
-    for i in range(1, n_lat):
-        for j in range(n_lon):
-            a, b, c, d = ring(i, j), ring(i, j + 1), ring(i + 1, j), ring(i + 1, j + 1)
-            tri += [[a, c, b], [b, c, d]]
-    return np.array(pts), np.array(tri, dtype=np.int32)
-
-
 def test_refined_solve_odd_node_count(bemlib):
     """7577 nodes (odd): the fused normal operator's second column segment
     has an odd length (1945 columns), so its bulk copy is rounded up into the
     row padding, which must stay masked.  Refined GMRES against the FP64 QR
     solve."""
-    p, e = _uv_sphere(75, 101)
+    p, e = uv_sphere(75, 101)
     assert p.shape[0] == 7577
     m = bemlib.Mesh.from_arrays(p, e)
     m.orient()
