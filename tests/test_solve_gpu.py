@@ -184,10 +184,11 @@ def test_dropin_qr_vs_numpy(bemlib):
     assert rel_err(B[:40], X) < 1e-4
 
 
-@pytest.mark.parametrize("nu", [24, 33])
+@pytest.mark.parametrize("nu", [24, 33, 36])
 def test_refined_solve_cluster_sizes(bemlib, nu):
-    """Refined GMRES on meshes whose node counts need two-CTA clusters in the
-    fused A^H A v kernel (5762 and 10892 nodes), against the FP64 solve."""
+    """Refined GMRES on meshes whose node counts need two- and three-CTA
+    clusters in the fused A^H A v kernel (5762, 10892 and 12962 nodes),
+    against the FP64 solve."""
     m = bemlib.Mesh.geodesic(nu).perturbed_ellipsoid(1.0, 0.8, 0.9, lmax=4, amp=0.03, seed=nu)
     p, e = m.points(), m.elems()
     rng = np.random.default_rng(nu)
