@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdint>
 #include <cstdlib>
 #include <mutex>
@@ -825,7 +826,7 @@ __device__ int g_normal_op_timeout = 0;
 template <int NT>
 __global__ void __launch_bounds__(NT, 512 / NT)
 normal_op_tma_kernel(int R, int N, const float2 *__restrict__ A, size_t lda, const float2 *__restrict__ v,
-                     int rows_per_cluster, int ngroups, float2 *__restrict__ wpart) {
+                     int rows_per_cluster, int ngroups, float2 *__restrict__ wpart, uint32_t extra_tx) {
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
     const int C = (int)cluster.num_blocks();
@@ -850,7 +851,9 @@ normal_op_tma_kernel(int R, int N, const float2 *__restrict__ A, size_t lda, con
         if (nr == 0) return;
         const int s = g % kNtNS;
         last_issued = g;
-        mbar_arrive_expect_tx(&full[s], nr * seg_bytes);
+        // extra_tx > 0 (a test of the timeout path only) announces bytes no copy
+        // delivers: every copy completes, the phase never does, the waits run out
+        mbar_arrive_expect_tx(&full[s], nr * seg_bytes + extra_tx);
         for (int rb = 0; rb < nr; rb++) {
             const int row = r_begin + g * kNtRPS + rb;
             bulk_copy_g2s(nt_stage + ((size_t)s * kNtRPS + rb) * kNtW, A + (size_t)row * lda + c0, seg_bytes,
@@ -1067,6 +1070,23 @@ int normal_op_variant() {
 }
 }  // namespace
 
+namespace {
+// Test of the bounded waits: with BEM_TEST_NORMAL_OP_STALL=1 in the
+// environment, the first TMA normal-operator launch of the process announces
+// 16 bytes more per stage than its copies deliver, so its waits time out (about
+// a second each), it records the timeout and finishes on stale data; the solve
+// then reports BEM_ERR_TIMEOUT.  Off unless the variable is set.
+uint32_t normal_op_stall_bytes() {
+    static const bool armed = [] {
+        const char *e = std::getenv("BEM_TEST_NORMAL_OP_STALL");
+        return e && std::string(e) == "1";
+    }();
+    static std::atomic<bool> used{false};
+    if (!armed || used.exchange(true)) return 0;
+    return 16;
+}
+}  // namespace
+
 bool normal_op_timed_out(cudaStream_t st) {
     int h = 0;
     static const int zero = 0;
@@ -1126,10 +1146,11 @@ bool launch_normal_op(int R, int N, const float2 *A, size_t lda, const float2 *v
     cfg.numAttrs = 1;
     {
         BEM_PROF("normal_op", st);   // the pass over A alone
+        const uint32_t stall = nt ? normal_op_stall_bytes() : 0u;
         if (nt == 512)
-            CUDA_TRY(cudaLaunchKernelEx(&cfg, normal_op_tma_kernel<512>, R, N, A, lda, v, rpc, ngroups, part));
+            CUDA_TRY(cudaLaunchKernelEx(&cfg, normal_op_tma_kernel<512>, R, N, A, lda, v, rpc, ngroups, part, stall));
         else if (nt == 256)
-            CUDA_TRY(cudaLaunchKernelEx(&cfg, normal_op_tma_kernel<256>, R, N, A, lda, v, rpc, ngroups, part));
+            CUDA_TRY(cudaLaunchKernelEx(&cfg, normal_op_tma_kernel<256>, R, N, A, lda, v, rpc, ngroups, part, stall));
         else
             CUDA_TRY(cudaLaunchKernelEx(&cfg, normal_op_kernel, R, N, A, lda, v, rpc, ngroups, part));
         count_launch();

@@ -269,3 +269,50 @@ def test_refined_solve_odd_node_count(bemlib):
     info = s.solve(bemlib.SOLVE_GMRES_REFINED)
     assert info.converged
     assert rel_err(s.solution(), x64) < 1e-5
+
+
+_STALL_SCRIPT = r"""
+import sys
+import numpy as np
+sys.path.insert(0, sys.argv[1])
+import bem_gpu_clean_cpp_gb300 as bem
+p, e = bem.Mesh.icosphere(3, 1.0).points(), bem.Mesh.icosphere(3, 1.0).elems()
+bc = np.tile(np.array([0, 1, 0], dtype=np.complex128), (e.shape[0], 1))
+chief = np.random.default_rng(3).uniform(-0.3, 0.3, (8, 3))
+s = bem.Solver(near_eta=1.0, near_depth=2)
+s.set_geometry(p, e, bc=bc, chief=chief)
+s.set_sources([("plane", np.array([0.0, 0.0, 1.0]), 1.0)])
+s.assemble(1.0, bem.PREC_C128)
+s.solve(bem.SOLVE_QR)
+x64 = s.solution()
+s.assemble(1.0, bem.PREC_C64)
+status = 0
+try:
+    s.solve(bem.SOLVE_GMRES_REFINED)
+except bem.BemError as err:
+    status = err.status
+info = s.solve(bem.SOLVE_GMRES_REFINED)
+err2 = np.linalg.norm(s.solution() - x64) / np.linalg.norm(x64)
+print("RESULT", status, int(info.converged), err2)
+"""
+
+
+def test_normal_op_wait_timeout_reported(bemlib):
+    """The TMA normal operator's waits are bounded.  With
+    BEM_TEST_NORMAL_OP_STALL=1 the first launch of the process announces 16
+    bytes per stage that no copy delivers: every copy completes, no barrier
+    phase does, the waits run out after about a second (no fault, no hang),
+    and the refined solve reports BEM_ERR_TIMEOUT.  The next solve in the same
+    process converges to the FP64 answer: the device stays usable and the
+    flag is cleared."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, BEM_TEST_NORMAL_OP_STALL="1")
+    out = subprocess.run([sys.executable, "-c", _STALL_SCRIPT, root], env=env, capture_output=True, text=True,
+                         timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = [ln for ln in out.stdout.splitlines() if ln.startswith("RESULT")][-1].split()
+    assert int(line[1]) == bemlib.ERR_TIMEOUT, line
+    assert line[2] == "1" and float(line[3]) < 1e-5, line
