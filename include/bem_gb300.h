@@ -252,8 +252,9 @@ int bem_solver_assemble(bem_solver_t s, double k, int precision);
  * FP32 matrix products and FP64 Arnoldi/Givens, inside FP64 iterative
  * refinement (requires a c64 assembly).  BEM_SOLVE_BLOCK_GMRES: all sources
  * together; the normal-operator products for every source are GEMMs on the
- * tensor cores (gemm_mode), each source keeps an FP64 Krylov space, outer
- * refinement to block_tol (requires a c64 assembly). */
+ * tensor cores (gemm_mode), each source keeps its own FP32 Krylov space
+ * with FP64 Hessenberg/Givens, outer refinement to block_tol (requires a c64
+ * assembly). */
 int bem_solver_solve(bem_solver_t s, int method, bem_solve_info_t *info);
 /* Copy results to host buffers in the given precision (BEM_PREC_*). */
 int bem_solver_get_solution(bem_solver_t s, void *x, int ldx, int precision);
