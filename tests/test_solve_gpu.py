@@ -316,3 +316,28 @@ def test_normal_op_wait_timeout_reported(bemlib):
     line = [ln for ln in out.stdout.splitlines() if ln.startswith("RESULT")][-1].split()
     assert int(line[1]) == bemlib.ERR_TIMEOUT, line
     assert line[2] == "1" and float(line[3]) < 1e-5, line
+
+
+@pytest.mark.parametrize("mesh", ["geodesic50", "icosphere6"])
+def test_normal_op_large_clusters(bemlib, mesh):
+    """The fused normal operator with five- and eight-CTA clusters (25002 and
+    40962 nodes, where an FP64 QR reference would take minutes): the refined
+    GMRES solution (normal-operator products) agrees with the block GMRES
+    solution of the same c64 system for one source (cuBLAS products, no
+    normal operator) to 1e-6."""
+    if mesh == "geodesic50":
+        m = bemlib.Mesh.geodesic(50).perturbed_ellipsoid(1.0, 0.85, 0.9, lmax=4, amp=0.03, seed=50)
+    else:
+        m = bemlib.Mesh.icosphere(6, 1.0)
+    p, e = m.points(), m.elems()
+    chief = np.random.default_rng(6).uniform(-0.3, 0.3, (8, 3))
+    s = bemlib.Solver(near_eta=1.0, near_depth=2, block_tol=1e-8)
+    s.set_geometry(p, e, bc=np.tile(np.array([0, 1, 0], dtype=np.complex128), (e.shape[0], 1)), chief=chief)
+    s.set_sources([("plane", np.array([0.36, 0.48, 0.8]), 1.0)])
+    s.assemble(3.0, bemlib.PREC_C64)
+    info = s.solve(bemlib.SOLVE_GMRES_REFINED)
+    assert info.converged
+    xr = s.solution()
+    info = s.solve(bemlib.SOLVE_BLOCK_GMRES)
+    assert info.converged
+    assert rel_err(xr, s.solution()) < 1e-6
