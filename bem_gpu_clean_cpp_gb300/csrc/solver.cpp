@@ -4,6 +4,7 @@
 #include "solver.h"
 
 #include <algorithm>
+#include <future>
 #include <cmath>
 #include <cstring>
 #include <numeric>
@@ -125,6 +126,7 @@ bem_solver_s::~bem_solver_s() {
 void bem_solver_s::set_geometry(const double *pnts, int num_pnts, const int *elems, int num_elems,
                                 const double *bc, const double *chief, int num_chief) {
     BEM_HOST_PROF("set_geometry");
+    if (tile_future.valid()) tile_future.wait();   // it reads h_nodes and h_elems
     BEM_CHECK_ARG(pnts && elems && num_pnts > 0 && num_elems > 0, "empty geometry");
     BEM_CHECK_ARG(num_chief >= 0 && (num_chief == 0 || chief), "bad CHIEF points");
     for (long long i = 0; i < 3LL * num_elems; i++)
@@ -135,6 +137,16 @@ void bem_solver_s::set_geometry(const double *pnts, int num_pnts, const int *ele
     R = N + M;
     h_nodes.assign(pnts, pnts + 3 * (size_t)N);
     h_elems.assign(elems, elems + 3 * (size_t)E);
+    // The column-tile tables (host work of ~0.4 ms at 20480 elements) are
+    // built on another host thread while this call and the assembly's first
+    // steps go on; ensure_tiles takes them.
+    host_tiles = HostTiles{};
+    {
+        const int cap = opt.tile_cols > 0 ? std::min(opt.tile_cols, kTileColsMax) : kTileColsMax;
+        tile_future = std::async(std::launch::async, [this, cap] {
+            return build_host_tiles(N, E, h_nodes, h_elems, cap);
+        });
+    }
     max_edge = 0.0;
     for (int e = 0; e < E; e++)
         for (int a = 0; a < 3; a++) {
@@ -303,11 +315,10 @@ void bem_solver_s::ensure_near_list() {
 // cut into equal tiles, and each tile lists every element with a node in it;
 // an element straddling tiles is integrated once per tile it touches and
 // counted for the c and beta sums only in the tile of its first node.
-void bem_solver_s::ensure_tiles(int precision) {
-    Tiles &T = tiles[precision];
-    if (T.valid) return;
-    BEM_HOST_PROF("tiles");
-    const int cap = opt.tile_cols > 0 ? std::min(opt.tile_cols, kTileColsMax) : kTileColsMax;
+bem::HostTiles bem::build_host_tiles(int N, int E, const std::vector<double> &h_nodes,
+                                     const std::vector<int> &h_elems, int cap) {
+    HostTiles out;
+    out.cap = cap;
     int ntiles = (N + cap - 1) / cap;
     int per = (N + ntiles - 1) / ntiles;
     std::vector<int> order(N);
@@ -325,7 +336,9 @@ void bem_solver_s::ensure_tiles(int precision) {
         std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return key[a] < key[b]; });
     }
     std::vector<int> tile_of(N), slot_of(N);
-    std::vector<int> cols((size_t)ntiles * per, 0), cnt(ntiles, 0);
+    std::vector<int> &cols = out.cols, &cnt = out.cnt;
+    cols.assign((size_t)ntiles * per, 0);
+    cnt.assign(ntiles, 0);
     for (int i = 0; i < N; i++) {
         int t = i / per, s = i - t * per;
         tile_of[order[i]] = t;
@@ -333,11 +346,7 @@ void bem_solver_s::ensure_tiles(int precision) {
         cols[(size_t)t * per + s] = order[i];
         cnt[t]++;
     }
-    std::vector<int> color;
-    {
-        BEM_HOST_PROF("color_elements");
-        color = color_elements(N, h_elems);
-    }
+    const std::vector<int> color = color_elements(N, h_elems);
     std::vector<std::vector<TileRec>> lists(ntiles);
     if (ntiles == 1) lists[0].reserve(E);
     for (int e = 0; e < E; e++) {
@@ -359,8 +368,9 @@ void bem_solver_s::ensure_tiles(int precision) {
             lists[t].push_back(r);
         }
     }
-    std::vector<TileRec> recs;
-    std::vector<int> ptr(ntiles + 1, 0);
+    std::vector<TileRec> &recs = out.recs;
+    std::vector<int> &ptr = out.ptr;
+    ptr.assign(ntiles + 1, 0);
     int ncolor = 0;
     for (int c : color) ncolor = std::max(ncolor, c + 1);
     std::vector<int> cstart(ncolor + 1);
@@ -373,6 +383,31 @@ void bem_solver_s::ensure_tiles(int precision) {
         recs.resize(ptr[t + 1]);
         for (const TileRec &r : lists[t]) recs[ptr[t] + cstart[color[r.eid]]++] = r;
     }
+    out.ntiles = ntiles;
+    out.per = per;
+    return out;
+}
+
+void bem_solver_s::ensure_tiles(int precision) {
+    Tiles &T = tiles[precision];
+    if (T.valid) return;
+    BEM_HOST_PROF("tiles");
+    const int cap = opt.tile_cols > 0 ? std::min(opt.tile_cols, kTileColsMax) : kTileColsMax;
+    // the host tables, built beside set_geometry when the column cap matches
+    HostTiles ht;
+    bool have = false;
+    if (tile_future.valid()) {
+        ht = tile_future.get();
+        have = ht.cap == cap;
+    } else if (host_tiles.cap == cap && !host_tiles.ptr.empty()) {
+        ht = host_tiles;
+        have = true;
+    }
+    if (!have) ht = build_host_tiles(N, E, h_nodes, h_elems, cap);
+    host_tiles = ht;
+    const std::vector<TileRec> &recs = ht.recs;
+    const std::vector<int> &ptr = ht.ptr, &cols = ht.cols, &cnt = ht.cnt;
+    const int ntiles = ht.ntiles, per = ht.per;
     T.recs.ensure(sizeof(TileRec) * recs.size());
     T.rec_ptr.ensure(sizeof(int) * ptr.size());
     T.cols.ensure(sizeof(int) * cols.size());

@@ -4,6 +4,7 @@
 #include <cublas_v2.h>
 #include <cusolverDn.h>
 
+#include <future>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -37,6 +38,17 @@ struct DevMem {
     ~DevMem() { release(); }
     template <class T> T *as() const { return static_cast<T *>(p); }
 };
+
+// Host side of the far kernel's column tiles: per tile its element records
+// (ordered by element colour), the tile-local column map and counts; cap =
+// the column cap they were built for.
+struct HostTiles {
+    int cap = -1, ntiles = 0, per = 0;
+    std::vector<TileRec> recs;
+    std::vector<int> ptr, cols, cnt;
+};
+HostTiles build_host_tiles(int N, int E, const std::vector<double> &h_nodes, const std::vector<int> &h_elems,
+                           int cap);
 
 }  // namespace bem
 
@@ -90,6 +102,12 @@ struct bem_solver_s {
     bem::DevMem q_A, q_B, q_tau, q_work, q_info;
     // field workspace
     bem::DevMem f_rows_f, f_rows_d, f_part, f_near, f_out, f_u;
+
+    // column-tile host tables: being built beside set_geometry (tile_future),
+    // or the last ones built; declared after h_nodes/h_elems, so the future
+    // (whose destructor waits for its task) goes first
+    bem::HostTiles host_tiles;
+    std::future<bem::HostTiles> tile_future;
 
     bem_solver_s();
     ~bem_solver_s();
