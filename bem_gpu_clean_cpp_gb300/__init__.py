@@ -36,7 +36,7 @@ LIB_PATH = os.path.join(_HERE, "libbem_gb300.so")
 SUCCESS = 0
 PREC_C64, PREC_C128 = 0, 1
 SOLVE_QR, SOLVE_GMRES_REFINED, SOLVE_BLOCK_GMRES = 0, 1, 2
-GEMM_AUTO, GEMM_FP32, GEMM_SPLIT_BF16, GEMM_TF32, GEMM_TF32X3, GEMM_TF32X3_3M = -1, 0, 1, 2, 3, 4
+GEMM_AUTO, GEMM_FP32, GEMM_SPLIT_BF16, GEMM_TF32, GEMM_TF32X3, GEMM_TF32X3_3M, GEMM_SIMT = -1, 0, 1, 2, 3, 4, 5
 SRC_POINT, SRC_PLANE = 0, 1
 ERR_NOT_CONVERGED = 5
 ERR_TOO_LARGE = 8

@@ -684,7 +684,13 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
     float *Vt = w_vf.as<float>(), *Tt = w_t.as<float>(), *Wt = w_part.as<float>();
     const float2 *A = d_A.as<float2>();
     const int gmode = block_gemm_mode(opt, S, R, n);
-    const bool x3 = gmode == BEM_GEMM_TF32X3, x3m = gmode == BEM_GEMM_TF32X3_3M;
+    const bool x3 = gmode == BEM_GEMM_TF32X3, x3m = gmode == BEM_GEMM_TF32X3_3M, simt = gmode == BEM_GEMM_SIMT;
+    float *simt_part = nullptr;
+    if (simt) {
+        // packed operands and partial sums of the split products
+        x_tlo.ensure(sizeof(float) * block_simt_scratch_floats(R, n, S));
+        simt_part = x_tlo.as<float>();
+    }
     float *Vlo = nullptr, *Tlo = nullptr, *A3 = nullptr, *B3 = nullptr, *C3 = nullptr;
     if (x3) {
         // [Vt | Vlo] (2N x 4S), the product pair [Ta | Tb] or [head | tail]
@@ -726,12 +732,22 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
     // R -= A D once per refinement cycle (D: the cycle's FP64 correction):
     // FP32-accurate like the gradient, whatever the inner products use
     auto apply_a_d = [&](const double2 *Xs) {
+        if (simt) {
+            BEM_PROF("gemm_AV", stream);
+            launch_block_av_c128(A, lda, R, n, S, Xs, Tt, simt_part, stream);
+            return;
+        }
         const int gm = gmode == BEM_GEMM_FP32 ? BEM_GEMM_FP32 : BEM_GEMM_SPLIT_BF16;
         build_vt_kernel<double2><<<grid2(n, S), 256, 0, stream>>>(n, S, Xs, Vt, nullptr);
         count_launch();
         normal_gemms(*this, gm, Vt, nullptr, Tt, nullptr, Wt, S, true, false);
     };
     auto apply_a_f = [&](const float2 *Xs) {
+        if (simt) {
+            BEM_PROF("gemm_AV", stream);
+            launch_block_av(A, lda, R, n, S, Xs, Tt, simt_part, stream);
+            return;
+        }
         if (x3m) {
             apply_a_3m<float2>(*this, Xs, A3, B3, C3, Tt);
             return;
@@ -741,6 +757,11 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
         normal_gemms(*this, gmode, Vt, Vlo, Tt, Tlo, Wt, S, true, false);
     };
     auto apply_ah = [&]() {
+        if (simt) {
+            BEM_PROF("gemm_AhT", stream);
+            launch_block_aht(A, lda, R, n, S, Tt, W, simt_part, stream);
+            return;
+        }
         if (x3m) {
             apply_ah_3m(*this, Tt, A3, B3, C3, W);
             return;
@@ -755,6 +776,11 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
     // FP32-accurate (split-BF16 emulation, or plain FP32 in FP32 mode) whatever
     // the inner products use.
     auto apply_ah_grad = [&]() {
+        if (simt) {
+            BEM_PROF("gemm_AhT", stream);
+            launch_block_aht(A, lda, R, n, S, Tt, W, simt_part, stream);
+            return;
+        }
         const int gm = gmode == BEM_GEMM_FP32 ? BEM_GEMM_FP32 : BEM_GEMM_SPLIT_BF16;
         normal_gemms(*this, gm, Vt, nullptr, Tt, nullptr, Wt, S, false, true);
         combine_w_kernel<<<grid2(n, S), 256, 0, stream>>>(n, S, Wt, nullptr, W);

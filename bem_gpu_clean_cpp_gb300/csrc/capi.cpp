@@ -249,7 +249,7 @@ void validate_options(const bem_options_t &o) {
     BEM_CHECK_ARG(o.tol > 0 && o.max_iter >= 1 && o.inner_tol > 0 && o.max_refine >= 0, "bad solver tolerances");
     BEM_CHECK_ARG(o.tile_cols >= 0, "tile_cols must be >= 0");
     BEM_CHECK_ARG(o.far_variant >= -1 && o.far_variant < far_variants(BEM_PREC_C64), "bad far_variant");
-    BEM_CHECK_ARG(o.gemm_mode >= BEM_GEMM_AUTO && o.gemm_mode <= BEM_GEMM_TF32X3_3M, "bad gemm_mode");
+    BEM_CHECK_ARG(o.gemm_mode >= BEM_GEMM_AUTO && o.gemm_mode <= BEM_GEMM_SIMT, "bad gemm_mode");
     BEM_CHECK_ARG(o.block_tol > 0, "block_tol must be positive");
 }
 

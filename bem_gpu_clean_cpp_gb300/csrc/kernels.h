@@ -144,6 +144,19 @@ bool launch_normal_op(int R, int N, const float2 *A, size_t lda, const float2 *v
 // device gave up waiting for one of its copies; synchronises the stream.
 bool normal_op_timed_out(cudaStream_t st);
 int gemv_h_f64_splits(int R, int N);
+// Block products in FP32 on the CUDA cores (block_simt.cu), one pass over A
+// per product for up to 32 sources: T = A X with X N x S column-major (c64,
+// or c128 rounded to c64) and T planar (R x 2S floats: Re in columns 0..S-1,
+// Im in S..2S-1); W = A^H T with W N x S column-major c64.  A row-major
+// R x N c64, lda a multiple of 8.  scratch: block_simt_scratch_floats(R, N, S)
+// floats (the packed operand and the split products' partial sums).
+size_t block_simt_scratch_floats(int R, int N, int S);
+void launch_block_av(const float2 *A, size_t lda, int R, int N, int S, const float2 *X, float *T, float *scratch,
+                     cudaStream_t st);
+void launch_block_av_c128(const float2 *A, size_t lda, int R, int N, int S, const double2 *X, float *T,
+                          float *scratch, cudaStream_t st);
+void launch_block_aht(const float2 *A, size_t lda, int R, int N, int S, const float *T, float2 *W, float *scratch,
+                      cudaStream_t st);
 // FP64 accumulation variants (the refinement residuals): A is c64 or c128.
 // r = b - A x.  For c64 A the products are exact double-float FP32
 // arithmetic; xsplit is scratch for x's float head and tail (2N + 1 c64:

@@ -618,6 +618,7 @@ size_t bem_solver_s::estimate_bytes(int N, int E, int M, int S, int method, cons
         const int gm = block_gemm_mode(o, S, (int)r, N);
         if (gm == BEM_GEMM_TF32X3) b += 16 * lda * r + 48 * n * s + 16 * r * s;
         if (gm == BEM_GEMM_TF32X3_3M) b += 24 * lda * r + 48 * std::max(n, r) * s;
+        if (gm == BEM_GEMM_SIMT) b += 4 * block_simt_scratch_floats((int)r, N, S);
     } else if (method == BEM_SOLVE_GMRES_REFINED) {
         const size_t m = (size_t)std::max(1, o.max_iter);
         b += 16 * n * (m + 1) + 16 * (m + 1) * m + 16 * 6 * (m + 1);

@@ -199,14 +199,18 @@ enum { BEM_SOLVE_QR = 0, BEM_SOLVE_GMRES_REFINED = 1, BEM_SOLVE_BLOCK_GMRES = 2 
  * Re A + Im A: three real products per complex product, a quarter fewer
  * flops, the same passes).  The once-per-cycle refinement products (the
  * residual update R -= A D and the gradient A^H R) run FP32-accurate
- * (split-BF16, or FP32 in FP32 mode) in every mode.  AUTO, while the c64
- * matrix is at most 4 GB: the 3M form from 128 right-hand sides on,
- * interleaved TF32x3 from 4 (measured faster than split-BF16 and FP32 at 8,
- * 16 and 64), FP32 below 4 (bandwidth-bound: one pass over A beats two over
- * the planes).  Above 4 GB the planes' memory would cost concurrent requests
- * more than the products gain: split-BF16 from 32, FP32 below. */
+ * (split-BF16, or FP32 in FP32 mode) in every mode.
+ * BEM_GEMM_SIMT: FP32 products on the CUDA cores by this library's own
+ * streaming kernels (one pass over A per product for up to 32 right-hand
+ * sides, more in further passes; no extra copies of A; the refinement
+ * products FP32 as well).
+ * AUTO: SIMT up to 8 right-hand sides, and up to 32 while the c64 matrix is
+ * at most 4 GB; above that, while the matrix is at most 4 GB, the 3M form
+ * from 128 right-hand sides on and interleaved TF32x3 below; above 4 GB the
+ * planes' memory would cost concurrent requests more than the products gain:
+ * split-BF16 from 32, FP32 below. */
 enum { BEM_GEMM_AUTO = -1, BEM_GEMM_FP32 = 0, BEM_GEMM_SPLIT_BF16 = 1, BEM_GEMM_TF32 = 2, BEM_GEMM_TF32X3 = 3,
-       BEM_GEMM_TF32X3_3M = 4 };
+       BEM_GEMM_TF32X3_3M = 4, BEM_GEMM_SIMT = 5 };
 
 typedef struct {
     double density;     /* 1.2041 (numerical.cu:12) */
