@@ -33,7 +33,10 @@
 
 #include <algorithm>
 #include <cmath>
+#include <map>
+#include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "dfloat.h"
@@ -533,6 +536,23 @@ __global__ void combine_w3_kernel(int n, int S, const float *__restrict__ C, flo
 }
 
 }  // namespace
+
+namespace {
+std::mutex g_block_mode_mu;
+std::map<std::tuple<int, int, int, int>, int> g_block_mode;   // (device, R, N, S) -> BEM_GEMM_*
+}  // namespace
+
+int block_mode_cached(int device, int R, int N, int S) {
+    std::lock_guard<std::mutex> lk(g_block_mode_mu);
+    const auto it = g_block_mode.find(std::make_tuple(device, R, N, S));
+    return it == g_block_mode.end() ? -1 : it->second;
+}
+
+void block_mode_store(int device, int R, int N, int S, int mode) {
+    std::lock_guard<std::mutex> lk(g_block_mode_mu);
+    g_block_mode[std::make_tuple(device, R, N, S)] = mode;
+}
+
 }  // namespace bem
 
 using namespace bem;
@@ -683,50 +703,63 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
     float2 *xh = w_gv.as<float2>(), *xl = xh + (size_t)ldx * S;
     float *Vt = w_vf.as<float>(), *Tt = w_t.as<float>(), *Wt = w_part.as<float>();
     const float2 *A = d_A.as<float2>();
-    const int gmode = block_gemm_mode(opt, S, R, n);
-    const bool x3 = gmode == BEM_GEMM_TF32X3, x3m = gmode == BEM_GEMM_TF32X3_3M, simt = gmode == BEM_GEMM_SIMT;
-    float *simt_part = nullptr;
-    if (simt) {
-        // packed operands and partial sums of the split products
-        x_tlo.ensure(sizeof(float) * block_simt_scratch_floats(R, n, S));
-        simt_part = x_tlo.as<float>();
-    }
-    float *Vlo = nullptr, *Tlo = nullptr, *A3 = nullptr, *B3 = nullptr, *C3 = nullptr;
-    if (x3) {
-        // [Vt | Vlo] (2N x 4S), the product pair [Ta | Tb] or [head | tail]
-        // of Tt (R x 4S), and [Wa | Wb] (2N x 4S)
-        x_vlo.ensure(sizeof(float) * 8 * NS);
-        x_tlo.ensure(sizeof(float) * 4 * (size_t)R * S);
-        w_part.ensure(sizeof(float) * 8 * NS);
-        Vt = x_vlo.as<float>();
-        Vlo = Vt + 4 * NS;
-        Tlo = x_tlo.as<float>();
+    // Product mode and its buffers; setup() may run more than once while the
+    // candidates of AUTO are timed (block_gemm_candidates).
+    int gmode = -1;
+    bool x3 = false, x3m = false, simt = false;
+    float *Vlo = nullptr, *Tlo = nullptr, *A3 = nullptr, *B3 = nullptr, *C3 = nullptr, *simt_part = nullptr;
+    auto setup = [&](int mode) {
+        gmode = mode;
+        x3 = mode == BEM_GEMM_TF32X3;
+        x3m = mode == BEM_GEMM_TF32X3_3M;
+        simt = mode == BEM_GEMM_SIMT;
+        Vt = w_vf.as<float>();
         Wt = w_part.as<float>();
-        if (tf32_split_mode != gmode) {
-            x_Ahi.ensure(sizeof(float) * 2 * lda * (size_t)R);
-            x_Alo.ensure(sizeof(float) * 2 * lda * (size_t)R);
-            split_a_tf32_kernel<<<152 * 16, 256, 0, stream>>>(R, 2 * n, 2 * lda, reinterpret_cast<const float *>(A),
-                                                              x_Ahi.as<float>(), x_Alo.as<float>());
-            count_launch();
-            KERNEL_CHECK();
-            tf32_split_mode = gmode;
+        Vlo = Tlo = A3 = B3 = C3 = simt_part = nullptr;
+        if (simt) {
+            // packed operands and partial sums of the split products
+            x_tlo.ensure(sizeof(float) * block_simt_scratch_floats(R, n, S));
+            simt_part = x_tlo.as<float>();
+        } else if (x3) {
+            // [Vt | Vlo] (2N x 4S), the product pair [Ta | Tb] or [head | tail]
+            // of Tt (R x 4S), and [Wa | Wb] (2N x 4S)
+            x_vlo.ensure(sizeof(float) * 8 * NS);
+            x_tlo.ensure(sizeof(float) * 4 * (size_t)R * S);
+            w_part.ensure(sizeof(float) * 8 * NS);
+            Vt = x_vlo.as<float>();
+            Vlo = Vt + 4 * NS;
+            Tlo = x_tlo.as<float>();
+            Wt = w_part.as<float>();
+            if (tf32_split_mode != mode) {
+                x_Ahi.ensure(sizeof(float) * 2 * lda * (size_t)R);
+                x_Alo.ensure(sizeof(float) * 2 * lda * (size_t)R);
+                split_a_tf32_kernel<<<152 * 16, 256, 0, stream>>>(R, 2 * n, 2 * lda,
+                                                                  reinterpret_cast<const float *>(A),
+                                                                  x_Ahi.as<float>(), x_Alo.as<float>());
+                count_launch();
+                KERNEL_CHECK();
+                tf32_split_mode = mode;
+            }
+        } else if (x3m) {
+            // A's six planes (built once per assembly), six planes of the
+            // right-hand block, the three products (two blocks each)
+            x_vlo.ensure(sizeof(float) * 6 * (size_t)std::max(n, R) * S);
+            x_tlo.ensure(sizeof(float) * 6 * (size_t)std::max(n, R) * S);
+            B3 = x_vlo.as<float>();
+            C3 = x_tlo.as<float>();
+            if (tf32_split_mode != mode) {
+                x_Ahi.ensure(sizeof(float) * 6 * lda * (size_t)R);
+                split_a3_kernel<<<152 * 16, 256, 0, stream>>>(R, n, lda, A, x_Ahi.as<float>());
+                count_launch();
+                KERNEL_CHECK();
+                tf32_split_mode = mode;
+            }
+            A3 = x_Ahi.as<float>();
         }
-    } else if (x3m) {
-        // A's six planes (built once per assembly), six planes of the
-        // right-hand block, the three products (two blocks each)
-        x_vlo.ensure(sizeof(float) * 6 * (size_t)std::max(n, R) * S);
-        x_tlo.ensure(sizeof(float) * 6 * (size_t)std::max(n, R) * S);
-        B3 = x_vlo.as<float>();
-        C3 = x_tlo.as<float>();
-        if (tf32_split_mode != gmode) {
-            x_Ahi.ensure(sizeof(float) * 6 * lda * (size_t)R);
-            split_a3_kernel<<<152 * 16, 256, 0, stream>>>(R, n, lda, A, x_Ahi.as<float>());
-            count_launch();
-            KERNEL_CHECK();
-            tf32_split_mode = gmode;
-        }
-        A3 = x_Ahi.as<float>();
-    }
+    };
+    const std::vector<int> cands = block_gemm_candidates(opt, S, R, n);
+    const int tuned = cands.size() > 1 ? bem::block_mode_cached(device, R, n, S) : cands[0];
+    setup(tuned >= 0 ? tuned : cands[0]);
     // T = A X into Tt (X: the FP64 correction or an FP32 basis block), and
     // W = A^H T from Tt, in the mode's form
     // R -= A D once per refinement cycle (D: the cycle's FP64 correction):
@@ -833,6 +866,44 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
         bscale_kernel<<<grid2(n, S), 256, 0, stream>>>(n, W, nrm_g, V);
         binit_g_kernel<<<sb, 128, 0, stream>>>(S, m, nrm_g, w_g.as<double2>());
         count_launch(2);
+        if (refs == 0 && tuned < 0) {
+            // First solve of this shape with several AUTO candidates: time one
+            // product pair A^H (A V) per candidate on the first basis block
+            // (after one untimed pair) and keep the fastest for the shape.
+            // W and Tt are free here; the products' results are discarded.
+            cudaEvent_t e0, e1;
+            CUDA_TRY(cudaEventCreate(&e0));
+            CUDA_TRY(cudaEventCreate(&e1));
+            int best = cands[0];
+            float best_ms = 0.f;
+            for (const int c : cands) {
+                setup(c);
+                apply_a_f(V);
+                apply_ah();
+                CUDA_TRY(cudaEventRecord(e0, stream));
+                for (int rep = 0; rep < 2; rep++) {
+                    apply_a_f(V);
+                    apply_ah();
+                }
+                CUDA_TRY(cudaEventRecord(e1, stream));
+                CUDA_TRY(cudaEventSynchronize(e1));
+                float ms = 0.f;
+                CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+                if (c == cands[0] || ms < best_ms) {
+                    best_ms = ms;
+                    best = c;
+                }
+            }
+            CUDA_TRY(cudaEventDestroy(e0));
+            CUDA_TRY(cudaEventDestroy(e1));
+            bem::block_mode_store(device, R, n, S, best);
+            if (best != BEM_GEMM_TF32X3 && best != BEM_GEMM_TF32X3_3M) {
+                x_Ahi.release();   // planes built only for the timing
+                x_Alo.release();
+                tf32_split_mode = -1;
+            }
+            setup(best);
+        }
         std::fill(h_kk.begin(), h_kk.end(), 0);
         int j = 0;
         for (; j < m; j++) {

@@ -615,10 +615,13 @@ size_t bem_solver_s::estimate_bytes(int N, int E, int M, int S, int method, cons
         const size_t m = (size_t)std::max(1, std::min(o.max_iter, 200));
         b += 16 * n * s * (m + 1) + 16 * s * m * (m + 1) + 16 * s * (4 * m + 4);
         b += 16 * n * s * 2 + 16 * r * s + 16 * n * s + 8 * r * s + 16 * n * s + 40 * s + 16 * n * s;
-        const int gm = block_gemm_mode(o, S, (int)r, N);
-        if (gm == BEM_GEMM_TF32X3) b += 16 * lda * r + 48 * n * s + 16 * r * s;
-        if (gm == BEM_GEMM_TF32X3_3M) b += 24 * lda * r + 48 * std::max(n, r) * s;
-        if (gm == BEM_GEMM_SIMT) b += 4 * block_simt_scratch_floats((int)r, N, S);
+        size_t extra = 0;   // the largest of the candidate modes' buffers
+        for (const int gm : block_gemm_candidates(o, S, (int)r, N)) {
+            if (gm == BEM_GEMM_TF32X3) extra = std::max(extra, 16 * lda * r + 48 * n * s + 16 * r * s);
+            if (gm == BEM_GEMM_TF32X3_3M) extra = std::max(extra, 24 * lda * r + 48 * std::max(n, r) * s);
+            if (gm == BEM_GEMM_SIMT) extra = std::max(extra, 4 * block_simt_scratch_floats((int)r, N, S));
+        }
+        b += extra;
     } else if (method == BEM_SOLVE_GMRES_REFINED) {
         const size_t m = (size_t)std::max(1, o.max_iter);
         b += 16 * n * (m + 1) + 16 * (m + 1) * m + 16 * 6 * (m + 1);

@@ -49,6 +49,10 @@ struct HostTiles {
 };
 HostTiles build_host_tiles(int N, int E, const std::vector<double> &h_nodes, const std::vector<int> &h_elems,
                            int cap);
+// Block-solve GEMM mode chosen by timing for (device, R, N, S), shared by
+// every handle of the process: -1 while none is stored.
+int block_mode_cached(int device, int R, int N, int S);
+void block_mode_store(int device, int R, int N, int S, int mode);
 
 }  // namespace bem
 
@@ -140,26 +144,35 @@ struct bem_solver_s {
     void solve_qr();
     void solve_refined(bem_solve_info_t *info);
     void solve_block(bem_solve_info_t *info);
-    // GEMM mode of the block solve for S right-hand sides and an R x N system
-    // (resolves AUTO).  Up to 8 sources (32 while A is at most 4 GB) the
-    // streaming CUDA-core kernels (one pass over A per product) beat the
-    // library GEMMs, whose skinny-shape kernels run far below the bandwidth
-    // bound (per A V + A^H T pair: 40962 nodes, 4 / 8 / 16 sources 4.2 / 6.3 /
-    // 9.9 ms against cuBLAS SGEMM 10.2 / 10.3 / 10.5 ms; 10242 nodes, 16
-    // sources 0.72 ms against 1.0 SGEMM and 1.39 TF32x3).  At 16 sources on
-    // 40962 nodes the margin alone is 6%, and seven such solves running
-    // side by side in the request server finished later with these kernels
-    // (one 172 KB CTA per SM) than with SGEMM, so there SGEMM stays.  The TF32x3 modes
-    // keep head/tail planes of A (2x or 3x the c64 matrix), so they are taken
-    // only while A is at most 4 GB: for larger systems the planes' memory
-    // costs the request server more concurrency than the faster products gain
-    // (64 frequencies up to 40962 nodes: 17.9 against 33.0 solves/s).
-    static int block_gemm_mode(const bem_options_t &o, int S, int R, int N) {
-        if (o.gemm_mode >= 0) return o.gemm_mode;
+    // GEMM modes of the block solve worth running for S right-hand sides and
+    // an R x N system: the fixed mode, or AUTO's candidates; with two, the
+    // first solve of each shape times both and the process keeps the faster
+    // (block_mode_cached / block_mode_store).  Measured per A V + A^H T pair:
+    // * up to 8 sources the streaming CUDA-core kernels (one pass over A per
+    //   product) beat the library GEMMs, whose skinny-shape kernels run far
+    //   below the bandwidth bound (40962 nodes, 4 / 8 sources: 4.2 / 6.3 ms
+    //   against cuBLAS SGEMM 10.2 / 10.3 ms; 15212 nodes, 8 sources: 0.88 ms
+    //   against 1.19 TF32x3 and 1.82 SGEMM);
+    // * from 9 to 32 sources, while A is at most 4 GB, the order of the
+    //   CUDA-core kernels and TF32x3 depends on the shape (16 sources: 10242
+    //   nodes 0.70 against 1.30 ms, 15212 nodes 1.41 against 1.18 ms): both
+    //   are candidates;
+    // * the TF32x3 modes keep head/tail planes of A (2x or 3x the c64
+    //   matrix), so they are taken only while A is at most 4 GB: for larger
+    //   systems the planes' memory costs the request server more concurrency
+    //   than the faster products gain (64 frequencies up to 40962 nodes: 17.9
+    //   against 33.0 solves/s).  There SGEMM (split-BF16 emulation from 32
+    //   sources) stays from 9 sources on: at 16 sources on 40962 nodes the
+    //   CUDA-core kernels are 6% faster alone, but seven such solves side by
+    //   side in the request server finished later with them (one 172 KB CTA
+    //   per SM) than with SGEMM.
+    static std::vector<int> block_gemm_candidates(const bem_options_t &o, int S, int R, int N) {
+        if (o.gemm_mode >= 0) return {o.gemm_mode};
         const bool planes = 8.0 * R * N <= 4e9;
-        if (S <= 8 || (S <= 32 && planes)) return BEM_GEMM_SIMT;
-        if (S >= 128) return planes ? BEM_GEMM_TF32X3_3M : BEM_GEMM_SPLIT_BF16;
-        if (planes) return BEM_GEMM_TF32X3;
-        return S >= 32 ? BEM_GEMM_SPLIT_BF16 : BEM_GEMM_FP32;
+        if (S <= 8) return {BEM_GEMM_SIMT};
+        if (!planes) return {S >= 32 ? BEM_GEMM_SPLIT_BF16 : BEM_GEMM_FP32};
+        if (S >= 128) return {BEM_GEMM_TF32X3_3M};
+        if (S <= 32) return {BEM_GEMM_SIMT, BEM_GEMM_TF32X3};
+        return {BEM_GEMM_TF32X3};
     }
 };

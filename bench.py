@@ -68,9 +68,9 @@ def parse_args():
     ap.add_argument("--slots", type=int, default=8, help="freq/serve: requests in flight at once")
     ap.add_argument("--rate", type=float, default=2.0, help="serve: mean request arrivals per second")
     ap.add_argument("--requests", type=int, default=40, help="serve: requests in the stream")
-    ap.add_argument("--gemm", type=int, default=-1, choices=[-1, 0, 1, 2, 3, 4],
+    ap.add_argument("--gemm", type=int, default=-1, choices=[-1, 0, 1, 2, 3, 4, 5],
                     help="block-solve GEMM mode (-1 auto, 0 FP32, 1 split-BF16 FP32-accurate, 2 TF32, 3 TF32x3, "
-                         "4 TF32x3 in the 3M form)")
+                         "4 TF32x3 in the 3M form, 5 FP32 streaming kernels on the CUDA cores)")
     ap.add_argument("--far-variant", type=int, default=-1,
                     help="profile mode: fixed far-field launch shape (-1: autotuned)")
     ap.add_argument("--mode", default="bench", choices=["bench", "profile"],
@@ -611,9 +611,11 @@ def run_ours(args):
         "config": {"workload": name, "sources": S, "nodes": N, "triangles": E, "chief": M,
                    **({"subdiv": args.subdiv, "ka": args.ka} if args.config == "precision" else
                       {"k": k, "solver": "block GMRES: %s GEMMs, FP32 Arnoldi, FP64 Givens, FP64-accurate "
-                                          "refinement residual to 1e-8" % {-1: "auto (A <= 4 GB: TF32x3 3M from 128 sources, TF32x3 from 4)", 0: "FP32",
+                                          "refinement residual to 1e-8" % {-1: "auto (CUDA-core streaming up to 8 sources; A <= 4 GB: "
+                                                                "timed choice of CUDA-core streaming or TF32x3 at 9-32, "
+                                                                "TF32x3 to 127, TF32x3 3M from 128)", 0: "FP32",
                                                             1: "split-BF16", 2: "TF32", 3: "TF32x3",
-                                                            4: "TF32x3 3M"}[args.gemm]}),
+                                                            4: "TF32x3 3M", 5: "CUDA-core streaming FP32"}[args.gemm]}),
                    "seed": args.seed, "near_eta": args.eta, "near_depth": args.depth,
                    "refine_tol": 1e-8, "parallelism": f"replicas x{dist.world}",
                    "l2": "inputs larger than L2: A (%.0f MB c64) is rewritten every step" % (A_bytes / 1e6)},

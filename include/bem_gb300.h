@@ -204,11 +204,12 @@ enum { BEM_SOLVE_QR = 0, BEM_SOLVE_GMRES_REFINED = 1, BEM_SOLVE_BLOCK_GMRES = 2 
  * streaming kernels (one pass over A per product for up to 32 right-hand
  * sides, more in further passes; no extra copies of A; the refinement
  * products FP32 as well).
- * AUTO: SIMT up to 8 right-hand sides, and up to 32 while the c64 matrix is
- * at most 4 GB; above that, while the matrix is at most 4 GB, the 3M form
- * from 128 right-hand sides on and interleaved TF32x3 below; above 4 GB the
- * planes' memory would cost concurrent requests more than the products gain:
- * split-BF16 from 32, FP32 below. */
+ * AUTO: SIMT up to 8 right-hand sides.  While the c64 matrix is at most
+ * 4 GB: from 9 to 32 the faster of SIMT and interleaved TF32x3 for the shape
+ * (timed on the first solve of each shape, kept for the process), TF32x3 up
+ * to 127, the 3M form from 128.  Above 4 GB the planes' memory would cost
+ * concurrent requests more than the products gain: split-BF16 from 32, FP32
+ * from 9 to 31. */
 enum { BEM_GEMM_AUTO = -1, BEM_GEMM_FP32 = 0, BEM_GEMM_SPLIT_BF16 = 1, BEM_GEMM_TF32 = 2, BEM_GEMM_TF32X3 = 3,
        BEM_GEMM_TF32X3_3M = 4, BEM_GEMM_SIMT = 5 };
 
