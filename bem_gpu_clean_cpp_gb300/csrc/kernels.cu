@@ -459,6 +459,115 @@ __device__ __forceinline__ void far_sums_f32_o6(float3 d3, float3 e1, float3 e2,
     S.c *= mh;
 }
 
+// Two-lane FP32 arithmetic: a 64-bit register pair holds two floats and one
+// f32x2 instruction does both lanes' operations, each lane rounded exactly
+// like the scalar instruction (fma.rn / mul.rn / add.rn).
+__device__ __forceinline__ uint64_t f2(float lo, float hi) {
+    uint64_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void f2_split(uint64_t v, float &lo, float &hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ float f2_sum(uint64_t v) {
+    float lo, hi;
+    f2_split(v, lo, hi);
+    return lo + hi;
+}
+__device__ __forceinline__ uint64_t fma2(uint64_t a, uint64_t b, uint64_t c) {
+    uint64_t d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ uint64_t mul2(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ uint64_t add2(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+
+// far_sums_f32_o6 for the shift and wrap phase modes with the two lanes of
+// f32x2 arithmetic carrying two Duffy points of a line (points 2p and
+// 2p + 1): the same operations per point, half the instructions for all but
+// rsqrt, sin and cos.  The per-point partial sums of a line add the even and
+// the odd points separately and then the two; the dG/dn imaginary sums
+// collect -hb (fma(-k, c, gs) = -fma(k, c, -gs) exactly) and take the sign
+// with the height at the end.
+template <int PH>
+__device__ __forceinline__ void far_sums_f32_o6x2(float3 d3, float3 e1, float3 e2, float hgt, float k,
+                                                  const PairPhase &pp, SumsF &S) {
+    static_assert(PH != kPhaseAcc, "the accurate phase mode has its own per-point arithmetic");
+    S.g0r = S.g0i = S.g1r = S.g1i = S.g2r = S.g2i = 0.0f;
+    S.h0r = S.h0i = S.h1r = S.h1i = S.h2r = S.h2i = 0.0f;
+    S.c = 0.0f;
+    const float3 e21 = make_float3(e2.x - e1.x, e2.y - e1.y, e2.z - e1.z);
+    const float dd = fmaf(d3.z, d3.z, fmaf(d3.y, d3.y, d3.x * d3.x));
+    const uint64_t dd2 = f2(dd, dd), k2 = f2(k, k), nk2 = f2(-k, -k);
+    const uint64_t c1 = f2(pp.c1, pp.c1), c2 = f2(pp.c2, pp.c2);
+#pragma unroll
+    for (int n = 0; n < 6; n++) {
+        const float th = 0.5f + 0.5f * gl6_x(n);
+        const float vx = fmaf(th, e21.x, e1.x), vy = fmaf(th, e21.y, e1.y), vz = fmaf(th, e21.z, e1.z);
+        const float qa = fmaf(vz, vz, fmaf(vy, vy, vx * vx));
+        const float qb = 2.0f * fmaf(vz, d3.z, fmaf(vy, d3.y, vx * d3.x));
+        const uint64_t qa2 = f2(qa, qa), qb2 = f2(qb, qb);
+        uint64_t u0gr = 0, u1gr = 0, u0gs = 0, u1gs = 0, u0ha = 0, u1ha = 0, u0hb = 0, u1hb = 0, u0c = 0;
+#pragma unroll
+        for (int p = 0; p < 3; p++) {
+            const float rho0 = 0.5f + 0.5f * gl6_x(2 * p), rho1 = 0.5f + 0.5f * gl6_x(2 * p + 1);
+            const uint64_t rho = f2(rho0, rho1);
+            const uint64_t wr1 = f2(gl6_w(2 * p) * rho0, gl6_w(2 * p + 1) * rho1);
+            const uint64_t wr2 = f2(gl6_w(2 * p) * rho0 * rho0, gl6_w(2 * p + 1) * rho1 * rho1);
+            const uint64_t r2 = fma2(fma2(qa2, rho, qb2), rho, dd2);   // (qa rho + qb) rho + |d3|^2
+            float ra, rb;
+            f2_split(r2, ra, rb);
+            const uint64_t ri = f2(rsqrt_ftz(ra), rsqrt_ftz(rb));
+            const uint64_t r = mul2(r2, ri);
+            uint64_t y = add2(fma2(k2, r, c1), c2);
+            if (PH == kPhaseWrap) {
+                // wrap_phase on both lanes
+                const uint64_t kr = f2(12582912.0f, 12582912.0f);
+                const uint64_t nn = add2(fma2(y, f2(kInv2PiF, kInv2PiF), kr), f2(-12582912.0f, -12582912.0f));
+                y = fma2(nn, f2(-kC2F, -kC2F), fma2(nn, f2(-kC1F, -kC1F), y));
+            }
+            float ya, yb, sa, ca, sb, cb;
+            f2_split(y, ya, yb);
+            sincos_ftz(ya, &sa, &ca);
+            sincos_ftz(yb, &sb, &cb);
+            const uint64_t sn = f2(sa, sb), cs = f2(ca, cb);
+            const uint64_t ri2 = mul2(ri, ri);
+            const uint64_t gr = mul2(cs, ri), gs = mul2(sn, ri);
+            const uint64_t ha = mul2(ri2, fma2(k2, sn, gr));
+            const uint64_t hbn = mul2(ri2, fma2(nk2, cs, gs));
+            const uint64_t ri3 = mul2(ri2, ri);
+            u0gr = fma2(wr1, gr, u0gr); u1gr = fma2(wr2, gr, u1gr);
+            u0gs = fma2(wr1, gs, u0gs); u1gs = fma2(wr2, gs, u1gs);
+            u0ha = fma2(wr1, ha, u0ha); u1ha = fma2(wr2, ha, u1ha);
+            u0hb = fma2(wr1, hbn, u0hb); u1hb = fma2(wr2, hbn, u1hb);
+            u0c = fma2(wr1, ri3, u0c);
+        }
+        const float a = 0.25f * gl6_w(n), b = a * (1.0f - th), c = a * th;
+        const float v0gr = f2_sum(u0gr), v1gr = f2_sum(u1gr), v0gs = f2_sum(u0gs), v1gs = f2_sum(u1gs);
+        const float v0ha = f2_sum(u0ha), v1ha = f2_sum(u1ha), v0hb = f2_sum(u0hb), v1hb = f2_sum(u1hb);
+        S.g0r = fmaf(a, v0gr, S.g0r); S.g1r = fmaf(b, v1gr, S.g1r); S.g2r = fmaf(c, v1gr, S.g2r);
+        S.g0i = fmaf(a, v0gs, S.g0i); S.g1i = fmaf(b, v1gs, S.g1i); S.g2i = fmaf(c, v1gs, S.g2i);
+        S.h0r = fmaf(a, v0ha, S.h0r); S.h1r = fmaf(b, v1ha, S.h1r); S.h2r = fmaf(c, v1ha, S.h2r);
+        S.h0i = fmaf(a, v0hb, S.h0i); S.h1i = fmaf(b, v1hb, S.h1i); S.h2i = fmaf(c, v1hb, S.h2i);
+        S.c = fmaf(a, f2_sum(u0c), S.c);
+    }
+    // G = (gr, -gs); dG/dn = -hgt (ha, hb) = (-hgt ha, hgt (-hb)); dG0/dn = -hgt c
+    const float mh = -hgt;
+    S.g0i = -S.g0i; S.g1i = -S.g1i; S.g2i = -S.g2i;
+    S.h0r *= mh; S.h1r *= mh; S.h2r *= mh;
+    S.h0i *= hgt; S.h1i *= hgt; S.h2i *= hgt;
+    S.c *= mh;
+}
+
 // Same in FP64 (used by the c128 far path and by the field kernel in c128).
 struct SumsD {
     double g0r, g0i, g1r, g1i, g2r, g2i;
@@ -578,7 +687,8 @@ far_assembly_f32(RowPoints rows, int N, GeoTables geo, TileSet tiles, float k, f
                                      ? pair_phase_acc(k, k_lo, make_float3(g0.x, g0.y, g0.z),
                                                       make_float3(g1.x, g1.y, g1.z), xh, xl, d3, coff)
                                      : pair_phase_shift(k, d3, coff);
-            if (O6) far_sums_f32_o6<PH>(d3, e1, e2, coff, hgt, k, pp, S);
+            if constexpr (O6 && PH != kPhaseAcc) far_sums_f32_o6x2<PH>(d3, e1, e2, hgt, k, pp, S);
+            else if (O6) far_sums_f32_o6<PH>(d3, e1, e2, coff, hgt, k, pp, S);
             else far_sums_f32<PH>(d3, e1, e2, coff, hgt, k, pp, nq, S);
             Coeffs<float, SumsF> o;
             finish_coeffs<float, SumsF>(S, g0.w * inv4pi, rw, g5.x, g5.y, g5.z, g5.w, o);
