@@ -505,16 +505,23 @@ __device__ __forceinline__ void far_sums_f32_o6x2(float3 d3, float3 e1, float3 e
     S.g0r = S.g0i = S.g1r = S.g1i = S.g2r = S.g2i = 0.0f;
     S.h0r = S.h0i = S.h1r = S.h1i = S.h2r = S.h2i = 0.0f;
     S.c = 0.0f;
+    // Along line n, v = e1 + th e21: qa = |v|^2 and qb = 2 v.d3 from five dot
+    // products per pair (v blends two edges from one vertex, th in (0, 1): no
+    // cancellation in the expansion).
     const float3 e21 = make_float3(e2.x - e1.x, e2.y - e1.y, e2.z - e1.z);
+    const float a0 = fmaf(e1.z, e1.z, fmaf(e1.y, e1.y, e1.x * e1.x));
+    const float a1 = 2.0f * fmaf(e1.z, e21.z, fmaf(e1.y, e21.y, e1.x * e21.x));
+    const float a2 = fmaf(e21.z, e21.z, fmaf(e21.y, e21.y, e21.x * e21.x));
+    const float b0 = 2.0f * fmaf(e1.z, d3.z, fmaf(e1.y, d3.y, e1.x * d3.x));
+    const float b1 = 2.0f * fmaf(e21.z, d3.z, fmaf(e21.y, d3.y, e21.x * d3.x));
     const float dd = fmaf(d3.z, d3.z, fmaf(d3.y, d3.y, d3.x * d3.x));
     const uint64_t dd2 = f2(dd, dd), k2 = f2(k, k), nk2 = f2(-k, -k);
     const uint64_t c1 = f2(pp.c1, pp.c1), c2 = f2(pp.c2, pp.c2);
 #pragma unroll
     for (int n = 0; n < 6; n++) {
         const float th = 0.5f + 0.5f * gl6_x(n);
-        const float vx = fmaf(th, e21.x, e1.x), vy = fmaf(th, e21.y, e1.y), vz = fmaf(th, e21.z, e1.z);
-        const float qa = fmaf(vz, vz, fmaf(vy, vy, vx * vx));
-        const float qb = 2.0f * fmaf(vz, d3.z, fmaf(vy, d3.y, vx * d3.x));
+        const float qa = fmaf(th * th, a2, fmaf(th, a1, a0));
+        const float qb = fmaf(th, b1, b0);
         const uint64_t qa2 = f2(qa, qa), qb2 = f2(qb, qb);
         uint64_t u0gr = 0, u1gr = 0, u0gs = 0, u1gs = 0, u0ha = 0, u1ha = 0, u0hb = 0, u1hb = 0, u0c = 0;
 #pragma unroll
