@@ -409,18 +409,25 @@ __device__ __forceinline__ void far_sums_f32_o6(float3 d3, float3 e1, float3 e2,
     S.g0r = S.g0i = S.g1r = S.g1i = S.g2r = S.g2i = 0.0f;
     S.h0r = S.h0i = S.h1r = S.h1i = S.h2r = S.h2i = 0.0f;
     S.c = 0.0f;
+    // Along line n, v = e1 + th e21: qa = |v|^2 and qb = 2 v.d3 from five dot
+    // products per pair (v blends two edges from one vertex, th in (0, 1): no
+    // cancellation in the expansion).
     const float3 e21 = make_float3(e2.x - e1.x, e2.y - e1.y, e2.z - e1.z);
+    const float a0 = fmaf(e1.z, e1.z, fmaf(e1.y, e1.y, e1.x * e1.x));
+    const float a1 = 2.0f * fmaf(e1.z, e21.z, fmaf(e1.y, e21.y, e1.x * e21.x));
+    const float a2 = fmaf(e21.z, e21.z, fmaf(e21.y, e21.y, e21.x * e21.x));
+    const float b0 = 2.0f * fmaf(e1.z, d3.z, fmaf(e1.y, d3.y, e1.x * d3.x));
+    const float b1 = 2.0f * fmaf(e21.z, d3.z, fmaf(e21.y, d3.y, e21.x * d3.x));
     const float dd = fmaf(d3.z, d3.z, fmaf(d3.y, d3.y, d3.x * d3.x));   // |d3|^2
 #pragma unroll
     for (int n = 0; n < 6; n++) {
         const float th = 0.5f + 0.5f * gl6_x(n);
-        const float vx = fmaf(th, e21.x, e1.x), vy = fmaf(th, e21.y, e1.y), vz = fmaf(th, e21.z, e1.z);
         // along the line r^2 = qa rho^2 + qb rho + |d3|^2 (and, kPhaseAcc,
         // r^2 - r_c^2 = qa rho^2 + qb rho + c0).  The terms are within a few
         // ulps of r^2 for a far pair (|d3| and rho |v| are bounded by r plus
         // the element's size), as accurate as summing the squared components.
-        const float qa = fmaf(vz, vz, fmaf(vy, vy, vx * vx));
-        const float qb = 2.0f * fmaf(vz, d3.z, fmaf(vy, d3.y, vx * d3.x));
+        const float qa = fmaf(th * th, a2, fmaf(th, a1, a0));
+        const float qb = fmaf(th, b1, b0);
         float u0gr = 0.f, u1gr = 0.f, u0gs = 0.f, u1gs = 0.f;
         float u0ha = 0.f, u1ha = 0.f, u0hb = 0.f, u1hb = 0.f, u0c = 0.f;
 #pragma unroll
