@@ -254,3 +254,22 @@ def test_orient_repairs_winding(bemlib):
     m2 = bemlib.Mesh.from_arrays(p, f[:, [1, 0, 2]])
     assert m2.orient()["flipped"] == len(f)
     assert m2.orient()["flipped"] == 0
+
+
+def test_python_constants_match_the_header(bemlib):
+    """Every enum of bem_gb300.h that the Python binding mirrors (precisions,
+    solve methods, block-solve GEMM modes, source kinds) has the header's
+    value."""
+    text = open(os.path.join(ROOT, "include", "bem_gb300.h")).read()
+    enums = {}
+    for body in re.findall(r"enum\s*\{([^}]*)\}", text):
+        for name, val in re.findall(r"(BEM_[A-Z0-9_]+)\s*=\s*(-?\d+)", body):
+            enums[name] = int(val)
+    checked = 0
+    for name, val in enums.items():
+        py = name[len("BEM_"):]
+        if hasattr(bemlib, py):
+            assert getattr(bemlib, py) == val, name
+            checked += 1
+    assert enums["BEM_GEMM_SIMT"] == 5 and bemlib.GEMM_SIMT == 5
+    assert checked >= 12
