@@ -707,7 +707,7 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
     // candidates of AUTO are timed (block_gemm_candidates).
     int gmode = -1;
     bool x3 = false, x3m = false, simt = false;
-    float *Vlo = nullptr, *Tlo = nullptr, *A3 = nullptr, *B3 = nullptr, *C3 = nullptr, *simt_part = nullptr;
+    float *Vlo = nullptr, *Tlo = nullptr, *A3 = nullptr, *B3 = nullptr, *C3 = nullptr, *simt_scratch = nullptr;
     auto setup = [&](int mode) {
         gmode = mode;
         x3 = mode == BEM_GEMM_TF32X3;
@@ -715,11 +715,11 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
         simt = mode == BEM_GEMM_SIMT;
         Vt = w_vf.as<float>();
         Wt = w_part.as<float>();
-        Vlo = Tlo = A3 = B3 = C3 = simt_part = nullptr;
+        Vlo = Tlo = A3 = B3 = C3 = simt_scratch = nullptr;
         if (simt) {
             // packed operands and partial sums of the split products
             x_tlo.ensure(sizeof(float) * block_simt_scratch_floats(R, n, S));
-            simt_part = x_tlo.as<float>();
+            simt_scratch = x_tlo.as<float>();
         } else if (x3) {
             // [Vt | Vlo] (2N x 4S), the product pair [Ta | Tb] or [head | tail]
             // of Tt (R x 4S), and [Wa | Wb] (2N x 4S)
@@ -767,7 +767,7 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
     auto apply_a_d = [&](const double2 *Xs) {
         if (simt) {
             BEM_PROF("gemm_AV", stream);
-            launch_block_av_c128(A, lda, R, n, S, Xs, Tt, simt_part, stream);
+            launch_block_av_c128(A, lda, R, n, S, Xs, Tt, simt_scratch, stream);
             return;
         }
         const int gm = gmode == BEM_GEMM_FP32 ? BEM_GEMM_FP32 : BEM_GEMM_SPLIT_BF16;
@@ -778,7 +778,7 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
     auto apply_a_f = [&](const float2 *Xs) {
         if (simt) {
             BEM_PROF("gemm_AV", stream);
-            launch_block_av(A, lda, R, n, S, Xs, Tt, simt_part, stream);
+            launch_block_av(A, lda, R, n, S, Xs, Tt, simt_scratch, stream);
             return;
         }
         if (x3m) {
@@ -792,7 +792,7 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
     auto apply_ah = [&]() {
         if (simt) {
             BEM_PROF("gemm_AhT", stream);
-            launch_block_aht(A, lda, R, n, S, Tt, W, simt_part, stream);
+            launch_block_aht(A, lda, R, n, S, Tt, W, simt_scratch, stream);
             return;
         }
         if (x3m) {
@@ -811,7 +811,7 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
     auto apply_ah_grad = [&]() {
         if (simt) {
             BEM_PROF("gemm_AhT", stream);
-            launch_block_aht(A, lda, R, n, S, Tt, W, simt_part, stream);
+            launch_block_aht(A, lda, R, n, S, Tt, W, simt_scratch, stream);
             return;
         }
         const int gm = gmode == BEM_GEMM_FP32 ? BEM_GEMM_FP32 : BEM_GEMM_SPLIT_BF16;

@@ -94,7 +94,8 @@ struct bem_solver_s {
     bem::DevMem w_V, w_H, w_cs, w_sn, w_g, w_y, w_h1, w_h2, w_w, w_t, w_r, w_gv, w_vf, w_part, w_scal;
     // TF32x3 block products: head/tail planes of A (interleaved form: x_Ahi
     // and x_Alo; 3M form: six planes in x_Ahi) and scratch for the right-hand
-    // blocks and products
+    // blocks and products (x_vlo, x_tlo; in the CUDA-core mode x_tlo holds the
+    // packed operand and the split products' partial sums)
     bem::DevMem x_Ahi, x_Alo, x_vlo, x_tlo, w_d;
     bem::DevMem w_ap;   // partial sums of the cooperative Arnoldi step
     int tf32_split_mode = -1;   // BEM_GEMM_* the planes of A were built for (this assembly), -1 none
