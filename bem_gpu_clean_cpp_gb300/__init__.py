@@ -35,8 +35,8 @@ LIB_PATH = os.path.join(_HERE, "libbem_gb300.so")
 
 SUCCESS = 0
 PREC_C64, PREC_C128 = 0, 1
-SOLVE_QR, SOLVE_GMRES_REFINED, SOLVE_BLOCK_GMRES = 0, 1, 2
-GEMM_AUTO, GEMM_FP32, GEMM_SPLIT_BF16, GEMM_TF32, GEMM_TF32X3, GEMM_TF32X3_3M, GEMM_SIMT = -1, 0, 1, 2, 3, 4, 5
+SOLVE_QR, SOLVE_GMRES_REFINED, SOLVE_BLOCK_GMRES, SOLVE_QR_TC = 0, 1, 2, 3
+GEMM_AUTO, GEMM_FP32, GEMM_SPLIT_BF16, GEMM_TF32, GEMM_TF32X3, GEMM_TF32X3_3M, GEMM_SIMT, GEMM_TC = -1, 0, 1, 2, 3, 4, 5, 6
 SRC_POINT, SRC_PLANE = 0, 1
 ERR_NOT_CONVERGED = 5
 ERR_TOO_LARGE = 8
@@ -143,6 +143,7 @@ SIGNATURES = {
     "bem_qr_solve_c64": (_I, [_VP, _I, _I, _I, _VP, _I, _I]),
     "bem_gmres_c64": (_I, [_VP, _VP, _I, _I, _F, _VP]),
     "bem_gmres_c64_noalloc": (_I, [_VP, _I, _VP, _I, _I, _F, _VP, _VP, ctypes.POINTER(_I)]),
+    "bem_tc_gemm_f32": (_I, [_I, _I, _I, _I, _VP, _I, _VP, _I, _VP, _I, _I]),
     "bem_ext_pressure_c64": (_I, [_F, _VP, _VP, _VP, _VP, _VP]),
     "bem_write_cplx_mat_c64": (_I, [_VP, _I, _I, _I, _S]),
     "bem_options_default": (_I, [_VP]),
@@ -161,6 +162,7 @@ SIGNATURES = {
     "bem_solver_sync": (_I, [_VP]),
     "bem_solver_stream": (_VP, [_VP]),
     "bem_solver_sizes": (_I, [_VP, _VP, _VP, _VP, _VP]),
+    "bem_solver_block_gemm_mode": (_I, [_VP, ctypes.POINTER(_I)]),
     "bem_server_options_default": (_I, [_VP]),
     "bem_server_create": (_I, [_VP, ctypes.POINTER(_VP)]),
     "bem_server_destroy": (_I, [_VP]),
@@ -450,6 +452,25 @@ def GMRES(A: np.ndarray, b: np.ndarray, maxIter: int, thr: float, x: np.ndarray 
     return x
 
 
+def tc_gemm(A: np.ndarray, B: np.ndarray, trans: bool = False, parts: int = 2) -> np.ndarray:
+    """C = op(A) B on the tcgen05 tensor cores (bem_tc_gemm_f32): A float32
+    (op(A) = A, or A^T when trans), B float32 (k x n); fp16 split products,
+    parts = 2 (TF32x3-level accuracy) or 3 (FP32-level)."""
+    A = np.asarray(A, dtype=np.float32)
+    rows, cols = A.shape
+    lda = (cols + 3) // 4 * 4
+    Ap = np.zeros((rows, lda), dtype=np.float32)
+    Ap[:, :cols] = A
+    m, k = (cols, rows) if trans else (rows, cols)
+    Bf = np.asfortranarray(B, dtype=np.float32)
+    if Bf.shape[0] != k:
+        raise ValueError("tc_gemm: inner dimensions differ")
+    n = Bf.shape[1]
+    C = np.zeros((m, n), dtype=np.float32, order="F")
+    _check(lib().bem_tc_gemm_f32(1 if trans else 0, m, k, n, _ptr(Ap), lda, _ptr(Bf), k, _ptr(C), m, int(parts)))
+    return C
+
+
 def genExtPressure(k: float, m: Mesh, src, x, surfP) -> complex:
     """genExtPressure (mesh.cu:1038-1073): pressure at x from the surface
     pressure surfP (complex64, numPnts)."""
@@ -523,6 +544,12 @@ class Solver:
         v = [ctypes.c_int() for _ in range(4)]
         _check(lib().bem_solver_sizes(self._h, *[ctypes.byref(x) for x in v]))
         return tuple(x.value for x in v)
+
+    def block_gemm_mode(self) -> int:
+        """GEMM_* mode of the last block solve's products (AUTO's choice)."""
+        v = ctypes.c_int()
+        _check(lib().bem_solver_block_gemm_mode(self._h, ctypes.byref(v)))
+        return v.value
 
     def assemble(self, k: float, precision: int = PREC_C64) -> None:
         _check(lib().bem_solver_assemble(self._h, float(k), int(precision)))

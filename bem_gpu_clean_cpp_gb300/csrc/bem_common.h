@@ -81,6 +81,9 @@ struct HostProfScope {
 };
 #define BEM_HOST_PROF(name) ::bem::HostProfScope bem_host_prof_scope_(name)
 
+// Streaming multiprocessors of the current device (queried once per device).
+int device_sm_count();
+
 constexpr double kPi = 3.14159265358979323846;
 constexpr int kMaxOrder = 12;              // Gauss points per direction
 constexpr int kMaxQ = kMaxOrder * kMaxOrder;

@@ -41,6 +41,7 @@
 
 #include "dfloat.h"
 #include "solver.h"
+#include "tc_gemm.h"
 
 namespace bem {
 namespace {
@@ -706,13 +707,18 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
     // Product mode and its buffers; setup() may run more than once while the
     // candidates of AUTO are timed (block_gemm_candidates).
     int gmode = -1;
-    bool x3 = false, x3m = false, simt = false;
+    bool x3 = false, x3m = false, simt = false, tc = false;
+    d_status.ensure(4 * sizeof(int));
+    int *tc_status = d_status.as<int>() + 1;
+    CUDA_TRY(cudaMemsetAsync(tc_status, 0, sizeof(int), stream));
+    const float *Af = reinterpret_cast<const float *>(A);
     float *Vlo = nullptr, *Tlo = nullptr, *A3 = nullptr, *B3 = nullptr, *C3 = nullptr, *simt_scratch = nullptr;
     auto setup = [&](int mode) {
         gmode = mode;
         x3 = mode == BEM_GEMM_TF32X3;
         x3m = mode == BEM_GEMM_TF32X3_3M;
         simt = mode == BEM_GEMM_SIMT;
+        tc = mode == BEM_GEMM_TC;
         Vt = w_vf.as<float>();
         Wt = w_part.as<float>();
         Vlo = Tlo = A3 = B3 = C3 = simt_scratch = nullptr;
@@ -720,6 +726,19 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
             // packed operands and partial sums of the split products
             x_tlo.ensure(sizeof(float) * block_simt_scratch_floats(R, n, S));
             simt_scratch = x_tlo.as<float>();
+        } else if (tc) {
+            // the packed right-hand operand (up to three fp16 parts of the
+            // larger of V's and T's interleaved blocks), split-K partial sums,
+            // A's power-of-two scale (once per assembly)
+            x_vlo.ensure(tc_operand_bytes(std::max(2 * n, R), 2 * S, 3));
+            const size_t pf = std::max({tc_gemm_part_floats(R, 2 * n, 2 * S, 2), tc_gemm_part_floats(R, 2 * n, 2 * S, 3),
+                                        tc_gemm_part_floats(2 * n, R, 2 * S, 2), tc_gemm_part_floats(2 * n, R, 2 * S, 3)});
+            if (pf) x_tlo.ensure(sizeof(float) * pf);
+            if (!tc_scale_valid) {
+                tc_scale.ensure(4 * sizeof(float));
+                tc_a_scale(Af, 2 * lda, R, 2 * n, tc_scale.as<float>(), stream);
+                tc_scale_valid = true;
+            }
         } else if (x3) {
             // [Vt | Vlo] (2N x 4S), the product pair [Ta | Tb] or [head | tail]
             // of Tt (R x 4S), and [Wa | Wb] (2N x 4S)
@@ -733,7 +752,7 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
             if (tf32_split_mode != mode) {
                 x_Ahi.ensure(sizeof(float) * 2 * lda * (size_t)R);
                 x_Alo.ensure(sizeof(float) * 2 * lda * (size_t)R);
-                split_a_tf32_kernel<<<152 * 16, 256, 0, stream>>>(R, 2 * n, 2 * lda,
+                split_a_tf32_kernel<<<device_sm_count() * 16, 256, 0, stream>>>(R, 2 * n, 2 * lda,
                                                                   reinterpret_cast<const float *>(A),
                                                                   x_Ahi.as<float>(), x_Alo.as<float>());
                 count_launch();
@@ -749,7 +768,7 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
             C3 = x_tlo.as<float>();
             if (tf32_split_mode != mode) {
                 x_Ahi.ensure(sizeof(float) * 6 * lda * (size_t)R);
-                split_a3_kernel<<<152 * 16, 256, 0, stream>>>(R, n, lda, A, x_Ahi.as<float>());
+                split_a3_kernel<<<device_sm_count() * 16, 256, 0, stream>>>(R, n, lda, A, x_Ahi.as<float>());
                 count_launch();
                 KERNEL_CHECK();
                 tf32_split_mode = mode;
@@ -764,7 +783,30 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
     // W = A^H T from Tt, in the mode's form
     // R -= A D once per refinement cycle (D: the cycle's FP64 correction):
     // FP32-accurate like the gradient, whatever the inner products use
+    // Tensor-core products: Tt = A X (X: N x S complex, packed as the
+    // interleaved real block), and W = A^H T from Tt; parts = 2 for the
+    // inner products, 3 (FP32-accurate) for the once-per-cycle ones.
+    auto tc_av = [&](const void *Xs, bool f64, int parts) {
+        BEM_PROF("gemm_AV", stream);
+        TcOperand op = tc_operand_view(x_vlo.p, 2 * n, 2 * S, parts);
+        if (f64) tc_pack_cplx_f64(static_cast<const double2 *>(Xs), n, S, op, stream);
+        else tc_pack_cplx_f32(static_cast<const float2 *>(Xs), n, S, op, stream);
+        tc_gemm(Af, 2 * lda, false, R, 2 * n, tc_scale.as<float>(), op, Tt, R, x_tlo.as<float>(), tc_status, stream);
+    };
+    auto tc_aht = [&](int parts) {
+        BEM_PROF("gemm_AhT", stream);
+        TcOperand op = tc_operand_view(x_vlo.p, R, 2 * S, parts);
+        tc_pack_real(Tt, R, op, stream);
+        tc_gemm(Af, 2 * lda, true, 2 * n, R, tc_scale.as<float>(), op, Wt, 2 * n, x_tlo.as<float>(), tc_status,
+                stream);
+        combine_w_kernel<<<grid2(n, S), 256, 0, stream>>>(n, S, Wt, nullptr, W);
+        count_launch();
+    };
     auto apply_a_d = [&](const double2 *Xs) {
+        if (tc) {
+            tc_av(Xs, true, 3);
+            return;
+        }
         if (simt) {
             BEM_PROF("gemm_AV", stream);
             launch_block_av_c128(A, lda, R, n, S, Xs, Tt, simt_scratch, stream);
@@ -776,6 +818,10 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
         normal_gemms(*this, gm, Vt, nullptr, Tt, nullptr, Wt, S, true, false);
     };
     auto apply_a_f = [&](const float2 *Xs) {
+        if (tc) {
+            tc_av(Xs, false, 2);
+            return;
+        }
         if (simt) {
             BEM_PROF("gemm_AV", stream);
             launch_block_av(A, lda, R, n, S, Xs, Tt, simt_scratch, stream);
@@ -790,6 +836,10 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
         normal_gemms(*this, gmode, Vt, Vlo, Tt, Tlo, Wt, S, true, false);
     };
     auto apply_ah = [&]() {
+        if (tc) {
+            tc_aht(2);
+            return;
+        }
         if (simt) {
             BEM_PROF("gemm_AhT", stream);
             launch_block_aht(A, lda, R, n, S, Tt, W, simt_scratch, stream);
@@ -809,6 +859,10 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
     // FP32-accurate (split-BF16 emulation, or plain FP32 in FP32 mode) whatever
     // the inner products use.
     auto apply_ah_grad = [&]() {
+        if (tc) {
+            tc_aht(3);
+            return;
+        }
         if (simt) {
             BEM_PROF("gemm_AhT", stream);
             launch_block_aht(A, lda, R, n, S, Tt, W, simt_scratch, stream);
@@ -943,6 +997,10 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
         KERNEL_CHECK();
     }
     CUDA_TRY(cudaStreamSynchronize(stream));
+    last_block_gemm_mode = gmode;
+    int h_status = 0;
+    CUDA_TRY(cudaMemcpy(&h_status, tc_status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h_status) BEM_FAIL(BEM_ERR_TIMEOUT, "block solve: a bounded wait of the tensor-core GEMM timed out");
     if (info) {
         info->iterations = total_it;
         info->refinements = refs;

@@ -371,16 +371,7 @@ __global__ void sum_parts_kernel(size_t n, const float *__restrict__ part, size_
     }
 }
 
-int num_sms() {
-    static const int n = [] {
-        int dev = 0, v = 0;
-        if (cudaGetDevice(&dev) != cudaSuccess ||
-            cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-            return 152;
-        return v > 0 ? v : 152;
-    }();
-    return n;
-}
+int num_sms() { return device_sm_count(); }
 
 // Splits of the reduction dimension (nred chunks) for `units` CTAs per split:
 // the count (<= kMaxSplits, >= 4 chunks per split) whose waves of one CTA per

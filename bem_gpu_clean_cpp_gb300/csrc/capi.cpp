@@ -25,6 +25,22 @@ std::atomic<long long> g_launches{0};
 std::atomic<bool> g_profiling{false};
 thread_local std::string g_last_error;
 
+int device_sm_count() {
+    constexpr int kMaxDev = 64;
+    static std::atomic<int> cache[kMaxDev];
+    int dev = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    if (dev >= 0 && dev < kMaxDev) {
+        const int c = cache[dev].load(std::memory_order_relaxed);
+        if (c > 0) return c;
+    }
+    int v = 0;
+    CUDA_TRY(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev));
+    if (v < 1) BEM_FAIL(BEM_ERR_CUDA, "device reports no multiprocessors");
+    if (dev >= 0 && dev < kMaxDev) cache[dev].store(v, std::memory_order_relaxed);
+    return v;
+}
+
 namespace {
 struct ProfRec {
     const char *name;
@@ -249,7 +265,7 @@ void validate_options(const bem_options_t &o) {
     BEM_CHECK_ARG(o.tol > 0 && o.max_iter >= 1 && o.inner_tol > 0 && o.max_refine >= 0, "bad solver tolerances");
     BEM_CHECK_ARG(o.tile_cols >= 0, "tile_cols must be >= 0");
     BEM_CHECK_ARG(o.far_variant >= -1 && o.far_variant < far_variants(BEM_PREC_C64), "bad far_variant");
-    BEM_CHECK_ARG(o.gemm_mode >= BEM_GEMM_AUTO && o.gemm_mode <= BEM_GEMM_SIMT, "bad gemm_mode");
+    BEM_CHECK_ARG(o.gemm_mode >= BEM_GEMM_AUTO && o.gemm_mode <= BEM_GEMM_TC, "bad gemm_mode");
     BEM_CHECK_ARG(o.block_tol > 0, "block_tol must be positive");
 }
 
@@ -788,6 +804,13 @@ int bem_solver_sizes(bem_solver_t s, int *n, int *m, int *num_elems, int *num_sr
     if (m) *m = s->M;
     if (num_elems) *num_elems = s->E;
     if (num_srcs) *num_srcs = s->S;
+    BEM_API_END
+}
+
+int bem_solver_block_gemm_mode(bem_solver_t s, int *mode) {
+    BEM_API_BEGIN
+    BEM_CHECK_ARG(s && mode, "null argument");
+    *mode = s->last_block_gemm_mode;
     BEM_API_END
 }
 

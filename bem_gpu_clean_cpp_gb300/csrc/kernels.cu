@@ -19,6 +19,7 @@
 
 #include "bem_common.h"
 #include "kernels.h"
+#include "tma.h"
 
 namespace bem {
 
@@ -410,8 +411,12 @@ __device__ __forceinline__ void far_sums_f32_o6(float3 d3, float3 e1, float3 e2,
     S.h0r = S.h0i = S.h1r = S.h1i = S.h2r = S.h2i = 0.0f;
     S.c = 0.0f;
     // Along line n, v = e1 + th e21: qa = |v|^2 and qb = 2 v.d3 from five dot
-    // products per pair (v blends two edges from one vertex, th in (0, 1): no
-    // cancellation in the expansion).
+    // products per pair, qa = a0 + th a1 + th^2 a2.  The expansion cancels
+    // where |v| is well below |e1| (an obtuse angle at the shared vertex, e1.e21
+    // < 0): qa then carries about (|e1| / h)^2 ulps of |v|^2, h the element's
+    // height over that vertex's opposite edge; for far pairs r^2 = qa rho^2 +
+    // qb rho + |d3|^2 is dominated by |d3|^2 and the effect on r is below
+    // FP32 rounding unless the element is a sliver.
     const float3 e21 = make_float3(e2.x - e1.x, e2.y - e1.y, e2.z - e1.z);
     const float a0 = fmaf(e1.z, e1.z, fmaf(e1.y, e1.y, e1.x * e1.x));
     const float a1 = 2.0f * fmaf(e1.z, e21.z, fmaf(e1.y, e21.y, e1.x * e21.x));
@@ -513,8 +518,12 @@ __device__ __forceinline__ void far_sums_f32_o6x2(float3 d3, float3 e1, float3 e
     S.h0r = S.h0i = S.h1r = S.h1i = S.h2r = S.h2i = 0.0f;
     S.c = 0.0f;
     // Along line n, v = e1 + th e21: qa = |v|^2 and qb = 2 v.d3 from five dot
-    // products per pair (v blends two edges from one vertex, th in (0, 1): no
-    // cancellation in the expansion).
+    // products per pair, qa = a0 + th a1 + th^2 a2.  The expansion cancels
+    // where |v| is well below |e1| (an obtuse angle at the shared vertex, e1.e21
+    // < 0): qa then carries about (|e1| / h)^2 ulps of |v|^2, h the element's
+    // height over that vertex's opposite edge; for far pairs r^2 = qa rho^2 +
+    // qb rho + |d3|^2 is dominated by |d3|^2 and the effect on r is below
+    // FP32 rounding unless the element is a sliver.
     const float3 e21 = make_float3(e2.x - e1.x, e2.y - e1.y, e2.z - e1.z);
     const float a0 = fmaf(e1.z, e1.z, fmaf(e1.y, e1.y, e1.x * e1.x));
     const float a1 = 2.0f * fmaf(e1.z, e21.z, fmaf(e1.y, e21.y, e1.x * e21.x));
@@ -665,27 +674,53 @@ far_assembly_f32(RowPoints rows, int N, GeoTables geo, TileSet tiles, float k, f
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2 *acc = reinterpret_cast<float2 *>(smem_raw);
     __shared__ float red[NT / 32][3];
+    __shared__ __align__(8) uint64_t batch_done;   // phase i completes when every thread added batch i
+    __shared__ int wait_abort;
     const int tile = blockIdx.y;
     const int tc = tiles.col_cnt[tile];
     const int r0 = blockIdx.x * TR;
     const int R = rows.R;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+        mbar_init(&batch_done, NT);
+        wait_abort = 0;
+    }
     for (int i = threadIdx.x; i < TR * tc; i += NT) acc[i] = make_float2(0.f, 0.f);
     __syncthreads();
 
     const int nq = c_nq;
     const float inv4pi = (float)(1.0 / (4.0 * kPi));
-    const int rb = tiles.rec_ptr[tile], re = tiles.rec_ptr[tile + 1];
-    // One pass over the tile's element list per row (rows are not
-    // interleaved, which keeps the per-thread state to one pair).
+    const int b0 = tiles.tile_batch[tile], b1 = tiles.tile_batch[tile + 1];
+    const int nr = min(TR, R - r0);                       // rows of this CTA
+    // Records come in node-disjoint batches.  Per batch the CTA's threads
+    // share the (row, record) items of all its rows (item w: row w / bs,
+    // record w % bs) and add into the rows' shared-memory accumulators with
+    // plain adds (no two items of a batch and row meet on a column).  A
+    // split-phase barrier orders the batches: a thread integrates its item of
+    // batch i first, then waits (on the mbarrier batch_done) until every
+    // thread has added batch i - 1, adds, and arrives; so every column of a
+    // row receives its terms in batch order while the wait overlaps the
+    // integration.  The c and beta sums are per thread and row.
+    float csum[TR], bsr[TR], bsi[TR];
+#pragma unroll
+    for (int t = 0; t < TR; t++) csum[t] = bsr[t] = bsi[t] = 0.f;
+    auto wait_batch = [&](int i) {   // batch i (counted from the tile's first) added by every thread
+        if (!mbar_wait_bounded(&batch_done, (uint32_t)(i & 1), kFarWaitCycles, &wait_abort)) {
+            wait_abort = 1;
+            atomicExch(tiles.status, 1);
+        }
+    };
 #pragma unroll 1
-    for (int t = 0; t < TR; t++) {
-        const int row = r0 + t;
-        if (row >= R) break;                              // uniform over the CTA
-        const float4 xh = rows.f[2 * (size_t)row], xl = rows.f[2 * (size_t)row + 1];
-        float csum = 0.f, bsr = 0.f, bsi = 0.f;
-        float2 *arow = acc + (size_t)t * tc;
-        for (int i = rb + threadIdx.x; i < re; i += NT) {
+    for (int b = b0; b < b1; b++) {
+        const int rb = tiles.batch_ptr[b], bs = tiles.batch_ptr[b + 1] - rb;
+        const int items = nr * bs;
+        bool waited = b == b0;
+        for (int w = threadIdx.x; w < items; w += NT) {
+            const int t = w / bs;
+            const int i = rb + (w - t * bs);
+            const int row = r0 + t;
+            const float4 xh = rows.f[2 * (size_t)row], xl = rows.f[2 * (size_t)row + 1];
+            float2 *arow = acc + (size_t)t * tc;
             const TileRec rec = tiles.recs[i];
             const float4 *g = geo.geo_f + (size_t)kGeoF * rec.eid;
             const int4 nd = make_int4(rec.node[0], rec.node[1], rec.node[2], 0);
@@ -706,33 +741,49 @@ far_assembly_f32(RowPoints rows, int N, GeoTables geo, TileSet tiles, float k, f
             else far_sums_f32<PH>(d3, e1, e2, coff, hgt, k, pp, nq, S);
             Coeffs<float, SumsF> o;
             finish_coeffs<float, SumsF>(S, g0.w * inv4pi, rw, g5.x, g5.y, g5.z, g5.w, o);
+            if (!waited) {
+                wait_batch(b - b0 - 1);
+                waited = true;
+            }
 #pragma unroll
             for (int j = 0; j < 3; j++) {
                 const int s = rec.slot[j];
                 if (s >= 0) {
-                    atomicAdd(&arow[s].x, o.ar[j]);
-                    atomicAdd(&arow[s].y, o.ai[j]);
+                    arow[s].x += o.ar[j];
+                    arow[s].y += o.ai[j];
                 }
             }
             if (rec.owner) {
-                csum += o.c;
-                bsr += o.br;
-                bsi += o.bi;
+#pragma unroll
+                for (int u = 0; u < TR; u++)
+                    if (u == t) {
+                        csum[u] += o.c;
+                        bsr[u] += o.br;
+                        bsi[u] += o.bi;
+                    }
             }
         }
-        // Row reduction of the c and beta partial sums (fixed order).
+        if (!waited) wait_batch(b - b0 - 1);   // arrivals for batch i only after batch i - 1 completed
+        mbar_arrive(&batch_done);
+    }
+    __syncthreads();   // every thread's adds of the last batch are done
+    // Row reductions of the c and beta partial sums (fixed order).
+#pragma unroll
+    for (int t = 0; t < TR; t++) {
+        if (t >= nr) break;                               // uniform over the CTA
+        float cs = csum[t], br = bsr[t], bi = bsi[t];
         for (int off = 16; off > 0; off >>= 1) {
-            csum += __shfl_xor_sync(0xffffffffu, csum, off);
-            bsr += __shfl_xor_sync(0xffffffffu, bsr, off);
-            bsi += __shfl_xor_sync(0xffffffffu, bsi, off);
+            cs += __shfl_xor_sync(0xffffffffu, cs, off);
+            br += __shfl_xor_sync(0xffffffffu, br, off);
+            bi += __shfl_xor_sync(0xffffffffu, bi, off);
         }
-        if (lane == 0) { red[warp][0] = csum; red[warp][1] = bsr; red[warp][2] = bsi; }
+        if (lane == 0) { red[warp][0] = cs; red[warp][1] = br; red[warp][2] = bi; }
         __syncthreads();
         if (threadIdx.x == 0) {
             float a = 0, b = 0, c = 0;
             for (int w = 0; w < NT / 32; w++) { a += red[w][0]; b += red[w][1]; c += red[w][2]; }
-            c_part[(size_t)tile * R + row] = a;
-            beta_part[(size_t)tile * R + row] = make_float2(b, c);
+            c_part[(size_t)tile * R + r0 + t] = a;
+            beta_part[(size_t)tile * R + r0 + t] = make_float2(b, c);
         }
         __syncthreads();
     }
@@ -765,7 +816,9 @@ far_assembly_f64(RowPoints rows, int N, GeoTables geo, TileSet tiles, double k, 
     const int nq = c_nq;
     const double inv4pi = 1.0 / (4.0 * kPi);
     double csum = 0, bsr = 0, bsi = 0;
-    const int rb = tiles.rec_ptr[tile], re = tiles.rec_ptr[tile + 1];
+    const int b0 = tiles.tile_batch[tile], b1 = tiles.tile_batch[tile + 1];
+    for (int b = b0; b < b1; b++) {
+    const int rb = tiles.batch_ptr[b], re = tiles.batch_ptr[b + 1];
     for (int i = rb + threadIdx.x; i < re; i += NT) {
         const TileRec rec = tiles.recs[i];
         const float4 *g = geo.geo_f + (size_t)kGeoF * rec.eid;
@@ -782,11 +835,13 @@ far_assembly_f64(RowPoints rows, int N, GeoTables geo, TileSet tiles, double k, 
         for (int j = 0; j < 3; j++) {
             int s = rec.slot[j];
             if (s >= 0) {
-                atomicAdd(&acc[s].x, o.ar[j]);
-                atomicAdd(&acc[s].y, o.ai[j]);
+                acc[s].x += o.ar[j];
+                acc[s].y += o.ai[j];
             }
         }
         if (rec.owner) { csum += o.c; bsr += o.br; bsi += o.bi; }
+    }
+    __syncthreads();
     }
     __shared__ double red[NT / 32][3];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1040,8 +1095,11 @@ __device__ int build_leaves_warp(const double *h, const double *x, double eta, i
 // fl(pi/2), P2 = fl(pi/2 - P1), P3 = fl(pi/2 - P1 - P2)), then on |z| <= pi/4,
 // with u = z^2,  sin z = z + z^3 P(u)  and  cos z = 1 - u/2 + u^2 Q(u)  with
 // P, Q of degree 5: Chebyshev interpolants of the exact functions on
-// [0, (pi/4)^2], coefficients from sincos_fit.py beside this package (max
-// error 7e-17 for sin, 1.2e-16 for cos, evaluated in double), and the
+// [0, (pi/4)^2] (P(u) = (sin sqrt(u) - sqrt(u)) / u^1.5, Q(u) = (cos sqrt(u)
+// - 1 + u/2) / u^2), interpolated at the 6 Chebyshev nodes of that interval
+// in 60-digit arithmetic, converted to monomial coefficients and rounded to
+// double (maximum error of the double-evaluated Horner schemes on a dense
+// grid: 7e-17 for sin, 1.2e-16 for cos), and the
 // quadrant's swap and signs.  Near pairs have kr of order one, so the
 // reduction is short and exact; this replaces the general-argument library
 // call on the FP64 pipe, which GB300 runs at ~1/64 of FP32.

@@ -28,9 +28,21 @@ struct RowPoints {
     int R;                    // number of points (rows)
 };
 
+// A tile's records come in batches of at most kFarBatch records whose nodes
+// inside the tile are all distinct (no two records of a batch add to the
+// same column), so the far kernels add each batch's contributions without
+// atomics and, with a CTA barrier between batches, in batch order: every
+// column of A receives its far-field terms in one fixed order, whatever the
+// launch shape (bitwise repeatable assembly).
+constexpr int kFarBatch = 1024;
+constexpr long long kFarWaitCycles = 2000000000LL;   // bound of the far kernel's batch waits (~1 s)
+
 struct TileSet {
     const TileRec *recs;      // all tiles' records
     const int *rec_ptr;       // ntiles + 1 offsets into recs
+    const int *batch_ptr;     // batch boundaries (offsets into recs), all tiles' batches in order
+    const int *tile_batch;    // ntiles + 1: the batches of tile t are tile_batch[t] .. tile_batch[t+1]-1
+    int *status;              // the solver's status word: set when a bounded wait of the far kernel timed out
     const int *cols;          // ntiles * tc_max tile-local column -> global column (node index)
     const int *col_cnt;       // ntiles: columns in each tile
     int ntiles;
@@ -138,11 +150,13 @@ bool launch_arnoldi_step(int n, int j, double2 *V, size_t ldv, double2 *w, float
 // c64.  Returns false (nothing launched) when N is above what one cluster
 // covers (45056).
 int normal_op_clusters(int N);
+// status: the calling solver's status word (device int), set to 1 when a
+// bounded wait of the kernel times out.
 bool launch_normal_op(int R, int N, const float2 *A, size_t lda, const float2 *v, double2 *w, float2 *part,
-                      cudaStream_t st);
-// True (and the flag cleared) when a normal-operator launch on the current
-// device gave up waiting for one of its copies; synchronises the stream.
-bool normal_op_timed_out(cudaStream_t st);
+                      int *status, cudaStream_t st);
+// True (and the word cleared) when a normal-operator launch gave up waiting
+// for one of its copies and recorded it in *status; synchronises the stream.
+bool normal_op_timed_out(int *status, cudaStream_t st);
 int gemv_h_f64_splits(int R, int N);
 // Block products in FP32 on the CUDA cores (block_simt.cu), one pass over A
 // per product for up to 32 sources: T = A X with X N x S column-major (c64,

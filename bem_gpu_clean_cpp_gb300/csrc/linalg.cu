@@ -811,7 +811,8 @@ normal_op_kernel(int R, int N, const float2 *__restrict__ A, size_t lda, const f
 // even element count, which stays inside the row's lda padding.  Padding and
 // columns past N are masked (never multiplied), so the padding's contents do
 // not matter.  Every wait is bounded; on a timeout the CTA records it in
-// g_normal_op_timeout, issues no further copies, keeps the same barrier
+// *timeout_flag (a status word of the calling solver, so concurrent solves
+// see only their own), issues no further copies, keeps the same barrier
 // sequence as its peers, and drains its copies in flight (bounded again)
 // before exiting.
 constexpr int kNtCPT = 11;
@@ -821,12 +822,11 @@ template <int NT>
 constexpr size_t nt_smem() { return (size_t)kNtNS * kNtRPS * NT * kNtCPT * sizeof(float2); }
 constexpr long long kNtWaitCycles = 2000000000LL;                          // ~1 s at 2 GHz
 
-__device__ int g_normal_op_timeout = 0;
-
 template <int NT>
 __global__ void __launch_bounds__(NT, 512 / NT)
 normal_op_tma_kernel(int R, int N, const float2 *__restrict__ A, size_t lda, const float2 *__restrict__ v,
-                     int rows_per_cluster, int ngroups, float2 *__restrict__ wpart, uint32_t extra_tx) {
+                     int rows_per_cluster, int ngroups, float2 *__restrict__ wpart, uint32_t extra_tx,
+                     int *timeout_flag) {
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
     const int C = (int)cluster.num_blocks();
@@ -881,7 +881,7 @@ normal_op_tma_kernel(int R, int N, const float2 *__restrict__ A, size_t lda, con
         if (nr > 0 && !*(volatile int *)&abort_flag) {
             if (!mbar_wait_bounded(&full[s], (uint32_t)((g / kNtNS) & 1), kNtWaitCycles, &abort_flag)) {
                 abort_flag = 1;
-                atomicExch(&g_normal_op_timeout, 1);
+                atomicExch(timeout_flag, 1);
             }
         }
         const float2 *stg = nt_stage + (size_t)s * kNtRPS * kNtW;
@@ -966,7 +966,8 @@ void launch_gemv_c64(int R, int N, const float2 *A, size_t lda, const void *x, i
 
 int gemv_h_splits(int R, int N) {
     int cb = (N + kHCols - 1) / kHCols;
-    int want = (8 * 152 + cb - 1) / cb;
+    const int sms = device_sm_count();
+    int want = (8 * sms + cb - 1) / cb;
     return std::max(1, std::min(want, std::max(1, R / 32)));
 }
 
@@ -1031,7 +1032,7 @@ bool launch_arnoldi_step(int n, int j, double2 *V, size_t ldv, double2 *w, float
 int normal_op_clusters(int N) {
     const int C = (N + kNoW - 1) / kNoW;   // kNoW == kNtW: both kernels split columns alike
     if (C > kNoMaxCluster) return 0;
-    return (2 * 152) / C;                  // the most clusters any variant launches
+    return (2 * device_sm_count()) / C;    // the most clusters any variant launches
 }
 
 namespace {
@@ -1087,20 +1088,19 @@ uint32_t normal_op_stall_bytes() {
 }
 }  // namespace
 
-bool normal_op_timed_out(cudaStream_t st) {
+bool normal_op_timed_out(int *status, cudaStream_t st) {
     int h = 0;
-    static const int zero = 0;
-    CUDA_TRY(cudaMemcpyFromSymbolAsync(&h, g_normal_op_timeout, sizeof(int), 0, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpyAsync(&h, status, sizeof(int), cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
     if (h) {
-        CUDA_TRY(cudaMemcpyToSymbolAsync(g_normal_op_timeout, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, st));
+        CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), st));
         CUDA_TRY(cudaStreamSynchronize(st));
     }
     return h != 0;
 }
 
 bool launch_normal_op(int R, int N, const float2 *A, size_t lda, const float2 *v, double2 *w, float2 *part,
-                      cudaStream_t st) {
+                      int *status, cudaStream_t st) {
     if (N <= 0 || R <= 0 || (N + kNoW - 1) / kNoW > kNoMaxCluster) return false;
     static std::once_flag once;
     static cudaError_t attr_err = cudaSuccess;
@@ -1127,7 +1127,8 @@ bool launch_normal_op(int R, int N, const float2 *A, size_t lda, const float2 *v
     const size_t smem = nt == 512 ? nt_smem<512>() : nt == 256 ? nt_smem<256>() : smem_regs;
     const int bt = nt ? nt : kNoNT;
     // the cluster shape must be schedulable on this device (else the two-kernel path runs)
-    const int want = nt == 512 ? 152 / C : 304 / C;
+    const int sms = device_sm_count();
+    const int want = nt == 512 ? sms / C : 2 * sms / C;
     const int ncl = std::min(want, clusters_resident(kern, C, bt, smem, want));
     if (ncl < 1) return false;
     const int rpc = (R + ncl - 1) / ncl;
@@ -1148,9 +1149,11 @@ bool launch_normal_op(int R, int N, const float2 *A, size_t lda, const float2 *v
         BEM_PROF("normal_op", st);   // the pass over A alone
         const uint32_t stall = nt ? normal_op_stall_bytes() : 0u;
         if (nt == 512)
-            CUDA_TRY(cudaLaunchKernelEx(&cfg, normal_op_tma_kernel<512>, R, N, A, lda, v, rpc, ngroups, part, stall));
+            CUDA_TRY(cudaLaunchKernelEx(&cfg, normal_op_tma_kernel<512>, R, N, A, lda, v, rpc, ngroups, part, stall,
+                                        status));
         else if (nt == 256)
-            CUDA_TRY(cudaLaunchKernelEx(&cfg, normal_op_tma_kernel<256>, R, N, A, lda, v, rpc, ngroups, part, stall));
+            CUDA_TRY(cudaLaunchKernelEx(&cfg, normal_op_tma_kernel<256>, R, N, A, lda, v, rpc, ngroups, part, stall,
+                                        status));
         else
             CUDA_TRY(cudaLaunchKernelEx(&cfg, normal_op_kernel, R, N, A, lda, v, rpc, ngroups, part));
         count_launch();
@@ -1187,7 +1190,7 @@ void launch_resid(int prec, int R, int N, const void *A, size_t lda, const doubl
 namespace {
 int h_f64_splits(int prec, int R, int N) {
     int cb = prec == BEM_PREC_C64 ? blocks(N, 512) : blocks(N, 256);
-    return std::max(1, std::min((8 * 152 + cb - 1) / cb, std::max(1, R / 16)));
+    return std::max(1, std::min((8 * device_sm_count() + cb - 1) / cb, std::max(1, R / 16)));
 }
 }  // namespace
 

@@ -16,6 +16,7 @@
 // It calls no cudaMalloc, cudaFree, cudaMallocHost or allocating library
 // routine, and creates no handles: kernels go on the caller's stream, and the
 // per-iteration residual estimate is copied into a local host variable.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -53,21 +54,47 @@ constexpr size_t kBytes =
 __device__ __align__(256) unsigned char g_noalloc_scratch[kBytes];
 
 std::mutex g_setup_mu;
-void *g_scratch_addr[64];   // device address of g_noalloc_scratch per device
+struct ScratchAddr {
+    CUcontext ctx;   // the context the address was looked up in
+    void *addr;      // device address of g_noalloc_scratch there
+};
+ScratchAddr g_scratch_addr[64];
 
-// Once per device, with that device current: the array's device address.  In
-// host code g_noalloc_scratch names a host-side shadow, not device memory.
+// The calling thread's current CUDA context (driver entry point through the
+// runtime, no link against the driver library).
+CUcontext current_context() {
+    using Fn = CUresult (*)(CUcontext *);
+    static Fn fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        return cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) ==
+                           cudaSuccess &&
+                       q == cudaDriverEntryPointSuccess
+                   ? reinterpret_cast<Fn>(p)
+                   : nullptr;
+    }();
+    CUcontext c = nullptr;
+    if (!fn || fn(&c) != CUDA_SUCCESS) BEM_FAIL(BEM_ERR_CUDA, "cuCtxGetCurrent is not available");
+    return c;
+}
+
+// Once per device and context, with that device current: the array's device
+// address (looked up again when the device's primary context was re-created,
+// e.g. after cudaDeviceReset, where the module may load at another address).
+// In host code g_noalloc_scratch names a host-side shadow, not device memory.
 unsigned char *scratch_for_current_device() {
     int dev = 0;
     CUDA_TRY(cudaGetDevice(&dev));
     if (dev < 0 || dev >= 64) BEM_FAIL(BEM_ERR_CUDA, "device index out of range");
+    CUcontext ctx = current_context();   // null until the runtime made one current on this thread
     std::lock_guard<std::mutex> lk(g_setup_mu);
-    if (!g_scratch_addr[dev]) {
+    if (!g_scratch_addr[dev].addr || !ctx || g_scratch_addr[dev].ctx != ctx) {
         void *p = nullptr;
-        CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-        g_scratch_addr[dev] = p;
+        CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));   // makes the device's context current
+        ctx = current_context();
+        g_scratch_addr[dev] = {ctx, p};
     }
-    return static_cast<unsigned char *>(g_scratch_addr[dev]);
+    return static_cast<unsigned char *>(g_scratch_addr[dev].addr);
 }
 
 struct Carver {

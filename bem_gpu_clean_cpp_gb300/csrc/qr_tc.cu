@@ -1,0 +1,897 @@
+// Least squares by blocked Householder QR with the trailing updates on the
+// tcgen05 tensor cores (BEM_SOLVE_QR_TC).  Replaces the blocked WY Householder
+// QR of the reference (QR_thin / lsqSolver, numerical.cu:246-554, whose
+// trailing updates are Cgemm calls, :375-396) and its cuSOLVER qrSolver
+// sequence (numerical.cu:580-644) for the device-resident solver.
+//
+// Method (m x n complex A, m >= n, S right-hand sides B).
+// * A and B are copied (c64, column-major, leading dimension ldq) into one
+//   workspace [A | B]: B rides along as extra trailing columns, so Q^H B is
+//   formed by the same updates and Q is never formed.
+// * Panels of kQrNB = 128 columns.  A panel is factored by one thread-block
+//   cluster (up to 16 CTAs, qr_panel_kernel): the CTAs split the panel's rows
+//   and keep a leaf of W = 16 columns in shared memory; per column the
+//   Householder vector (LAPACK's zlarfg convention: beta real, H = I - tau v
+//   v^H, v_1 = 1) needs two cluster-wide sums exchanged through distributed
+//   shared memory (the norm, then v^H times the leaf's other columns).  A
+//   finished leaf is applied to the panel's remaining columns as a block
+//   reflector (I - V T V^H)^H in the same kernel.
+// * The trailing matrix C (the columns right of the panel, B included) is
+//   updated as C -= V T^H (V^H C) with two tensor-core GEMMs (tc_gemm, fp16
+//   split products, TF32x3-level accuracy) on the interleaved-real form of
+//   the complex products, T from V^H V (a third, small GEMM) and the taus.
+// * X = R^{-1} (Q^H B)[0:n] by blocked back substitution.
+// * Refinement to the FP64 least-squares solution (semi-normal equations,
+//   corrected): r = b - A x and g = A^H r with FP64-accurate products (c128
+//   A, or c64 A with double-float sums), R^H R dx = g by two triangular
+//   solves with the FP32 factor, x += dx, until ||g|| <= tol ||A^H b||.  It
+//   converges by a factor of about kappa(A)^2 x 6e-8 per step.
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "bem_common.h"
+#include "kernels.h"
+#include "solver.h"
+#include "tc_gemm.h"
+#include "tc_split.cuh"
+
+namespace bem {
+namespace {
+
+namespace cg = cooperative_groups;
+
+constexpr int kQrNT = 512;      // threads per CTA of the panel kernel
+constexpr int kQrNB = 128;      // panel width (the trailing updates' K)
+constexpr int kQrW = 16;        // leaf width held in shared memory
+constexpr int kQrCL = 16;       // CTAs per cluster (non-portable size)
+constexpr int kQrTB = 64;       // block of the triangular solves
+// Refinement target: relative normal-equation residual ||A^H (b - A x)|| /
+// ||A^H b|| (stagnation at the precision of the FP64-accurate products ends
+// it earlier).
+constexpr double kQrRefineTol = 1e-14;
+constexpr double kQrStagnationOk = 1e-11;
+static_assert(kQrW == 16, "the panel kernel pairs lanes c and c + 16 of a warp on one leaf column");
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// conj(a) b
+__device__ __forceinline__ float2 cjmul(float2 a, float2 b) {
+    return make_float2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ double2 zmul(double2 a, double2 b) {
+    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 zjmul(double2 a, double2 b) {
+    return make_double2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
+}
+
+// Shared-memory layout of the panel kernel (float2 units): the leaf L[W][lds]
+// (column-major, lds = 1 mod 16: the W columns of one row fall in distinct
+// banks), then the reduction slots.
+struct PanelLayout {
+    int lds;
+    size_t leaf, ssq, dot, gram, wpart, gsum, tmat, ysum, scratch, bcast, taus, total;
+    __host__ __device__ PanelLayout(int rb) {
+        lds = ((rb + 15) / 16) * 16 + 1;
+        size_t o = 0;
+        leaf = o;    o += (size_t)kQrW * lds;
+        ssq = o;     o += 2 * 2;                         // [parity][ssq, alpha]
+        dot = o;     o += 2 * kQrW;                      // [parity][column]
+        gram = o;    o += kQrW * kQrW;                   // this CTA's V^H V
+        wpart = o;   o += (size_t)kQrW * kQrNB;          // this CTA's V^H P (leaf x rest of the panel)
+        gsum = o;    o += kQrW * kQrW;
+        tmat = o;    o += kQrW * kQrW;
+        ysum = o;    o += (size_t)kQrW * kQrNB;
+        scratch = o; o += (kQrNT / 32) * kQrW;
+        bcast = o;   o += 4;
+        taus = o;    o += kQrW;                          // this leaf's taus (every CTA forms them)
+        total = o;
+    }
+};
+
+// v_k at local row i of this CTA: 0 above the pivot row g_k, 1 on it, the
+// stored vector below.
+__device__ __forceinline__ float2 vval(const float2 *L, int lds, int k, int grow, int gk, int i) {
+    if (grow < gk) return make_float2(0.f, 0.f);
+    if (grow == gk) return make_float2(1.f, 0.f);
+    return L[(size_t)k * lds + i];
+}
+
+// Factors the panel Q[j0:m, j0:j0+pc] in place (Householder vectors below the
+// diagonal, R on and above it); tau_out[0..pc) receives the taus.  One
+// cluster of gridDim.x CTAs; CTA q owns the rows j0 + q rb .. + rb - 1.
+__global__ void __launch_bounds__(kQrNT, 1)
+qr_panel_kernel(float2 *__restrict__ Q, size_t ldq, int m, int j0, int pc, int rb, float2 *__restrict__ tau_out) {
+    cg::cluster_group cluster = cg::this_cluster();
+    const int CL = (int)cluster.num_blocks();
+    const int q = (int)cluster.block_rank();
+    extern __shared__ __align__(16) float2 ps[];
+    const PanelLayout lay(rb);
+    const int lds = lay.lds;
+    float2 *L = ps + lay.leaf;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int r0 = j0 + q * rb;
+    const int nrows = max(0, min(rb, m - r0));
+    float2 *scratch = ps + lay.scratch, *bcast = ps + lay.bcast;
+    auto peer = [&](size_t off, int p) -> const float2 * {
+        return cluster.map_shared_rank(ps + off, p);
+    };
+
+    for (int l0 = 0; l0 < pc; l0 += kQrW) {
+        const int lw = min(kQrW, pc - l0);
+        // load the leaf (this CTA's rows)
+        for (int c = 0; c < lw; c++)
+            for (int i = tid; i < nrows; i += kQrNT)
+                L[(size_t)c * lds + i] = Q[(size_t)(j0 + l0 + c) * ldq + r0 + i];
+        __syncthreads();
+        for (int jj = 0; jj < lw; jj++) {
+            const int par = jj & 1;
+            const int g = j0 + l0 + jj;   // pivot row
+            // (1) partial |x|^2 below the pivot, and the pivot value
+            float ssq = 0.f;
+            for (int i = tid; i < nrows; i += kQrNT)
+                if (r0 + i > g) {
+                    const float2 x = L[(size_t)jj * lds + i];
+                    ssq = fmaf(x.x, x.x, fmaf(x.y, x.y, ssq));
+                }
+            for (int o = 16; o > 0; o >>= 1) ssq += __shfl_xor_sync(0xffffffffu, ssq, o);
+            if (lane == 0) scratch[warp].x = ssq;
+            __syncthreads();
+            if (tid == 0) {
+                float t = 0.f;
+                for (int w = 0; w < kQrNT / 32; w++) t += scratch[w].x;
+                ps[lay.ssq + 2 * par] = make_float2(t, 0.f);
+                ps[lay.ssq + 2 * par + 1] = (g >= r0 && g < r0 + nrows) ? L[(size_t)jj * lds + (g - r0)]
+                                                                          : make_float2(0.f, 0.f);
+            }
+            cluster.sync();
+            // (2) every CTA forms the reflector from the cluster sums
+            if (warp == 0) {
+                float t = 0.f;
+                float2 a = make_float2(0.f, 0.f);
+                if (lane < CL) {
+                    const float2 *pp = peer(lay.ssq + 2 * par, lane);
+                    t = pp[0].x;
+                    a = pp[1];
+                }
+                for (int o = 16; o > 0; o >>= 1) {
+                    t += __shfl_xor_sync(0xffffffffu, t, o);
+                    a.x += __shfl_xor_sync(0xffffffffu, a.x, o);
+                    a.y += __shfl_xor_sync(0xffffffffu, a.y, o);
+                }
+                if (lane == 0) {
+                    float2 tau, scal;
+                    float beta;
+                    if (t == 0.f && a.y == 0.f) {
+                        tau = make_float2(0.f, 0.f);
+                        scal = make_float2(0.f, 0.f);
+                        beta = a.x;
+                    } else {
+                        beta = -copysignf(sqrtf(a.x * a.x + a.y * a.y + t), a.x);
+                        tau = make_float2((beta - a.x) / beta, -a.y / beta);
+                        const float2 d = make_float2(a.x - beta, a.y);      // scal = 1 / (alpha - beta)
+                        const float dd = d.x * d.x + d.y * d.y;
+                        scal = make_float2(d.x / dd, -d.y / dd);
+                    }
+                    bcast[0] = tau;
+                    bcast[1] = scal;
+                    bcast[2] = make_float2(beta, 0.f);
+                    ps[lay.taus + jj] = tau;
+                    if (q == 0) tau_out[l0 + jj] = tau;
+                }
+            }
+            __syncthreads();
+            const float2 tau = bcast[0], scal = bcast[1];
+            const float beta = bcast[2].x;
+            for (int i = tid; i < nrows; i += kQrNT) {
+                const int grow = r0 + i;
+                if (grow > g) L[(size_t)jj * lds + i] = cmul(L[(size_t)jj * lds + i], scal);
+                else if (grow == g) L[(size_t)jj * lds + i] = make_float2(beta, 0.f);
+            }
+            __syncthreads();
+            // (3) partial w_c = v^H x_c for the leaf's later columns
+            const int c = tid % kQrW, il = tid / kQrW;
+            constexpr int NIL = kQrNT / kQrW;
+            float2 acc = make_float2(0.f, 0.f);
+            if (c > jj && c < lw) {
+                for (int i = il; i < nrows; i += NIL) {
+                    const int grow = r0 + i;
+                    if (grow >= g) {
+                        const float2 u = cjmul(vval(L, lds, jj, grow, g, i), L[(size_t)c * lds + i]);
+                        acc.x += u.x;
+                        acc.y += u.y;
+                    }
+                }
+            }
+            // lanes c and c + 16 share a column
+            acc.x += __shfl_xor_sync(0xffffffffu, acc.x, 16);
+            acc.y += __shfl_xor_sync(0xffffffffu, acc.y, 16);
+            if (lane < kQrW) scratch[warp * kQrW + lane] = acc;
+            __syncthreads();
+            if (tid < kQrW) {
+                float2 t = make_float2(0.f, 0.f);
+                for (int w = 0; w < kQrNT / 32; w++) {
+                    t.x += scratch[w * kQrW + tid].x;
+                    t.y += scratch[w * kQrW + tid].y;
+                }
+                ps[lay.dot + par * kQrW + tid] = t;
+            }
+            cluster.sync();
+            // (4) y_c = conj(tau) w_c; x_c -= v y_c
+            if (warp == 0 && lane < kQrW) {
+                float2 t = make_float2(0.f, 0.f);
+                if (lane > jj && lane < lw)
+                    for (int p = 0; p < CL; p++) {
+                        const float2 u = peer(lay.dot + par * kQrW, p)[lane];
+                        t.x += u.x;
+                        t.y += u.y;
+                    }
+                scratch[lane] = cjmul(tau, t);
+            }
+            __syncthreads();
+            if (c > jj && c < lw) {
+                const float2 y = scratch[c];
+                for (int i = il; i < nrows; i += NIL) {
+                    const int grow = r0 + i;
+                    if (grow >= g) {
+                        const float2 v = vval(L, lds, jj, grow, g, i);
+                        float2 &x = L[(size_t)c * lds + i];
+                        const float2 vy = cmul(v, y);
+                        x.x -= vy.x;
+                        x.y -= vy.y;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        // the factored leaf back to Q
+        for (int c = 0; c < lw; c++)
+            for (int i = tid; i < nrows; i += kQrNT)
+                Q[(size_t)(j0 + l0 + c) * ldq + r0 + i] = L[(size_t)c * lds + i];
+        const int c1 = l0 + lw, nrest = pc - c1;
+        if (nrest <= 0) continue;
+        // ---- the leaf's block reflector applied to the panel's later columns:
+        // P -= V T^H (V^H P), P = Q[j0:m, j0+c1 : j0+pc] ----
+        // (a) this CTA's V^H V (lw x lw) and V^H P (lw x nrest)
+        for (int pr = tid; pr < lw * lw; pr += kQrNT) {
+            const int a = pr / lw, b = pr % lw;
+            const int ga = j0 + l0 + a, gb = j0 + l0 + b;
+            float2 t = make_float2(0.f, 0.f);
+            for (int i = 0; i < nrows; i++) {
+                const int grow = r0 + i;
+                const float2 va = vval(L, lds, a, grow, ga, i), vb = vval(L, lds, b, grow, gb, i);
+                const float2 u = cjmul(va, vb);
+                t.x += u.x;
+                t.y += u.y;
+            }
+            ps[lay.gram + a * kQrW + b] = t;
+        }
+        for (int cc = warp; cc < nrest; cc += kQrNT / 32) {
+            const float2 *pcol = Q + (size_t)(j0 + c1 + cc) * ldq + r0;
+            float2 acc[kQrW];
+#pragma unroll
+            for (int k = 0; k < kQrW; k++) acc[k] = make_float2(0.f, 0.f);
+            for (int i = lane; i < nrows; i += 32) {
+                const float2 x = pcol[i];
+                const int grow = r0 + i;
+#pragma unroll
+                for (int k = 0; k < kQrW; k++)
+                    if (k < lw) {
+                        const float2 u = cjmul(vval(L, lds, k, grow, j0 + l0 + k, i), x);
+                        acc[k].x += u.x;
+                        acc[k].y += u.y;
+                    }
+            }
+#pragma unroll
+            for (int k = 0; k < kQrW; k++)
+                for (int o = 16; o > 0; o >>= 1) {
+                    acc[k].x += __shfl_xor_sync(0xffffffffu, acc[k].x, o);
+                    acc[k].y += __shfl_xor_sync(0xffffffffu, acc[k].y, o);
+                }
+            if (lane == 0)
+#pragma unroll
+                for (int k = 0; k < kQrW; k++)
+                    if (k < lw) ps[lay.wpart + (size_t)k * kQrNB + cc] = acc[k];
+        }
+        cluster.sync();
+        // (b) the cluster sums
+        for (int e = tid; e < lw * lw; e += kQrNT) {
+            const int a = e / lw, b = e % lw;
+            float2 t = make_float2(0.f, 0.f);
+            for (int p = 0; p < CL; p++) {
+                const float2 u = peer(lay.gram, p)[a * kQrW + b];
+                t.x += u.x;
+                t.y += u.y;
+            }
+            ps[lay.gsum + a * kQrW + b] = t;
+        }
+        for (int e = tid; e < lw * nrest; e += kQrNT) {
+            const int k = e / nrest, cc = e % nrest;
+            float2 t = make_float2(0.f, 0.f);
+            for (int p = 0; p < CL; p++) {
+                const float2 u = peer(lay.wpart, p)[(size_t)k * kQrNB + cc];
+                t.x += u.x;
+                t.y += u.y;
+            }
+            ps[lay.ysum + (size_t)k * kQrNB + cc] = t;   // W = V^H P for now
+        }
+        __syncthreads();
+        // (c) T (upper triangular, lw x lw): T_kk = tau_k, T[0:k, k] = -tau_k T[0:k, 0:k] G[0:k, k]
+        float2 *T = ps + lay.tmat;
+        if (warp == 0) {
+            for (int k = 0; k < lw; k++) {
+                const float2 tk = ps[lay.taus + k];
+                float2 t = make_float2(0.f, 0.f);
+                if (lane < k) {
+                    for (int l = lane; l < k; l++) {
+                        const float2 u = cmul(T[lane * kQrW + l], ps[lay.gsum + l * kQrW + k]);
+                        t.x += u.x;
+                        t.y += u.y;
+                    }
+                }
+                __syncwarp();
+                if (lane < k) T[lane * kQrW + k] = cmul(make_float2(-tk.x, -tk.y), t);
+                if (lane == k) T[k * kQrW + k] = tk;
+                if (lane > k && lane < kQrW) T[lane * kQrW + k] = make_float2(0.f, 0.f);
+                __syncwarp();
+            }
+        }
+        __syncthreads();
+        // (d) Y = T^H W (in place, column by column: each column's lw values
+        // are read before any is written)
+        for (int cc = tid; cc < nrest; cc += kQrNT) {
+            float2 w[kQrW];
+#pragma unroll
+            for (int k = 0; k < kQrW; k++) w[k] = k < lw ? ps[lay.ysum + (size_t)k * kQrNB + cc] : make_float2(0.f, 0.f);
+#pragma unroll
+            for (int k = 0; k < kQrW; k++) {
+                if (k >= lw) break;
+                float2 y = make_float2(0.f, 0.f);
+                for (int l = 0; l <= k; l++) {
+                    const float2 u = cjmul(T[l * kQrW + k], w[l]);
+                    y.x += u.x;
+                    y.y += u.y;
+                }
+                ps[lay.ysum + (size_t)k * kQrNB + cc] = y;
+            }
+        }
+        __syncthreads();
+        // (e) P -= V Y (this CTA's rows)
+        for (int cc = warp; cc < nrest; cc += kQrNT / 32) {
+            float2 *pcol = Q + (size_t)(j0 + c1 + cc) * ldq + r0;
+            for (int i = lane; i < nrows; i += 32) {
+                const int grow = r0 + i;
+                float2 x = pcol[i];
+                for (int k = 0; k < lw; k++) {
+                    const float2 u = cmul(vval(L, lds, k, grow, j0 + l0 + k, i), ps[lay.ysum + (size_t)k * kQrNB + cc]);
+                    x.x -= u.x;
+                    x.y -= u.y;
+                }
+                pcol[i] = x;
+            }
+        }
+        __syncthreads();
+    }
+    cluster.sync();   // peers' shared memory is read until here
+}
+
+
+// Q[r + c ldq] = A[r lda + c] (row-major c64 or c128 system) for c < n, and
+// Q[r + (n + j) ldq] = B[r + j R] (c128, column-major): 32 x 32 tiles
+// through shared memory (coalesced on both sides).  grid (ceil(n/32),
+// ceil(R/32)) for A; B by a separate plain kernel.
+template <typename T>
+__global__ void qr_copy_a_kernel(int R, int n, const T *__restrict__ A, size_t lda, float2 *__restrict__ Q,
+                                 size_t ldq) {
+    __shared__ float2 tile[32][33];
+    const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 32 x 8 threads
+    for (int k = ty; k < 32; k += 8) {
+        const int r = r0 + k, c = c0 + tx;
+        if (r < R && c < n) {
+            const T v = A[(size_t)r * lda + c];
+            tile[k][tx] = make_float2((float)v.x, (float)v.y);
+        }
+    }
+    __syncthreads();
+    for (int k = ty; k < 32; k += 8) {
+        const int c = c0 + k, r = r0 + tx;
+        if (r < R && c < n) Q[(size_t)c * ldq + r] = tile[tx][k];
+    }
+}
+
+__global__ void qr_copy_b_kernel(int R, int S, const double2 *__restrict__ B, float2 *__restrict__ Qb, size_t ldq) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (r < R) {
+        const double2 v = B[(size_t)j * R + r];
+        Qb[(size_t)j * ldq + r] = make_float2((float)v.x, (float)v.y);
+    }
+}
+
+// Largest column 2-norm of Q's ncols columns (m rows) into out (as the bits of
+// a non-negative float); one CTA per column.
+__global__ void qr_colnorm_kernel(int m, const float2 *__restrict__ Q, size_t ldq, unsigned *__restrict__ out) {
+    __shared__ float red[32];
+    const float2 *q = Q + (size_t)blockIdx.x * ldq;
+    float s = 0.f;
+    for (int r = threadIdx.x; r < m; r += blockDim.x) s = fmaf(q[r].x, q[r].x, fmaf(q[r].y, q[r].y, s));
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float t = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w];
+        atomicMax(out, __float_as_uint(sqrtf(t)));
+    }
+}
+
+// Scale pairs (scale, 1 / scale) of the GEMMs' left operands: sc[0..1] for the
+// trailing matrix, from the largest column norm (orthogonal updates keep
+// column norms, so it bounds every entry through the factorisation; 2% slack
+// for rounding), sc[2..3] for V (|entries| <= 1: the unit diagonal, and
+// |v_i| = |x_i| / |alpha - beta| <= 1 below it).
+__global__ void qr_scales_kernel(float *sc) {
+    const float bound = __uint_as_float(*reinterpret_cast<const unsigned *>(sc + 4)) * 1.02f;
+    const float s = pow2_scale(bound);
+    sc[0] = s;
+    sc[1] = 1.f / s;
+    sc[2] = 16384.f;
+    sc[3] = 1.f / 16384.f;
+}
+
+// Vf (mr x pc, column-major, ldv): the panel's Householder vectors with the
+// unit diagonal and zeros above it.
+__global__ void qr_vfull_kernel(int mr, int pc, const float2 *__restrict__ P, size_t ldq, float2 *__restrict__ Vf,
+                                size_t ldv) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y;
+    if (i >= mr) return;
+    float2 v = make_float2(0.f, 0.f);
+    if (i == k) v = make_float2(1.f, 0.f);
+    else if (i > k) v = P[(size_t)k * ldq + i];
+    Vf[(size_t)k * ldv + i] = v;
+}
+
+// Vrr (2 mr x ldk floats, row-major): row 2i = (Re v_ik, -Im v_ik)_k, row 2i+1
+// = (Im v_ik, Re v_ik)_k, so that Vrr times the block with rows 2k, 2k+1 =
+// (Re w_k, Im w_k) gives (Re, Im) of V w in rows 2i, 2i+1.
+__global__ void qr_vrr_kernel(int mr, int pc, const float2 *__restrict__ Vf, size_t ldv, float *__restrict__ Vrr,
+                              int ldk) {
+    const int i = blockIdx.x, k = threadIdx.x;
+    if (k >= pc) return;
+    const float2 v = Vf[(size_t)k * ldv + i];
+    float *r0 = Vrr + (size_t)(2 * i) * ldk, *r1 = r0 + ldk;
+    r0[2 * k] = v.x;
+    r0[2 * k + 1] = -v.y;
+    r1[2 * k] = v.y;
+    r1[2 * k + 1] = v.x;
+}
+
+// T (pc x pc, row-major, ld kQrNB, upper triangular) of the panel's block
+// reflector H_1 ... H_pc = I - V T V^H (forward, column by column: T_kk =
+// tau_k, T[0:k, k] = -tau_k T[0:k, 0:k] G[0:k, k]) from the Gram matrix
+// G = V^H V (Greal: pc x 2pc column-major, [Re G | Im G]); one CTA, thread =
+// row of T; FP64 sums, T kept in FP32 (in global memory: the CTA's own
+// writes, ordered by its barriers).
+__global__ void qr_larft_kernel(int pc, const float *__restrict__ Greal, const float2 *__restrict__ tau,
+                                float2 *T) {
+    const int r = threadIdx.x;
+    for (int k = 0; k < pc; k++) {
+        const float2 tk = tau[k];
+        double2 t = make_double2(0.0, 0.0);
+        if (r < k) {
+            for (int l = r; l < k; l++) {
+                const double2 g = make_double2(Greal[(size_t)k * pc + l], Greal[(size_t)(pc + k) * pc + l]);
+                const float2 trl = T[(size_t)r * kQrNB + l];
+                const double2 u = zmul(make_double2(trl.x, trl.y), g);
+                t.x += u.x;
+                t.y += u.y;
+            }
+        }
+        __syncthreads();
+        if (r < k) {
+            const double2 v = zmul(make_double2(-tk.x, -tk.y), t);
+            T[(size_t)r * kQrNB + k] = make_float2((float)v.x, (float)v.y);
+        }
+        if (r == k) T[(size_t)k * kQrNB + k] = tk;
+        if (r > k && r < pc) T[(size_t)r * kQrNB + k] = make_float2(0.f, 0.f);
+        __syncthreads();
+    }
+}
+
+// The right-hand operand of the rank-pc update: for trailing column c, W'[:, c]
+// = T^H W[:, c] with W = V^H C = Z^H (Z = C^H V: Zreal nct x 2pc column-major,
+// [Re Z | Im Z]), i.e. W'[k, c] = conj(sum_{l <= k} T[l, k] Z[c, l]), packed
+// as rows 2k, 2k+1 = (Re, Im) of column c, scaled per column.  kQrTwCols
+// columns per CTA, thread = k.
+constexpr int kQrTwCols = 16;
+template <int P>
+__global__ void qr_pack_tw_kernel(int nct, int pc, const float *__restrict__ Zreal, const float2 *__restrict__ T,
+                                  int Kp, int ncols_pad, __half *__restrict__ planes, float *__restrict__ col_inv) {
+    __shared__ float2 z[kQrNB];
+    __shared__ float red[32];
+    const int k = threadIdx.x;
+    const size_t ps = (size_t)ncols_pad * Kp;
+    for (int cc = 0; cc < kQrTwCols; cc++) {
+        const int c = blockIdx.x * kQrTwCols + cc;
+        if (c >= nct) break;   // uniform over the CTA
+        if (k < pc) z[k] = make_float2(Zreal[(size_t)k * nct + c], Zreal[(size_t)(pc + k) * nct + c]);
+        __syncthreads();
+        float2 y = make_float2(0.f, 0.f);
+        if (k < pc)
+            for (int l = 0; l <= k; l++) {
+                const float2 u = cmul(T[(size_t)l * kQrNB + k], z[l]);
+                y.x += u.x;
+                y.y += u.y;
+            }
+        y.y = -y.y;   // the conjugate
+        const float sc = pow2_scale(block_max(fmaxf(fabsf(y.x), fabsf(y.y)), red));
+        if (k == 0) col_inv[c] = 1.f / sc;
+        if (k < pc) put_parts<P>(planes, ps, (size_t)c * Kp + 2 * k, y.x * sc, y.y * sc);
+        else if (2 * k < Kp) put_parts<P>(planes, ps, (size_t)c * Kp + 2 * k, 0.f, 0.f);
+        __syncthreads();
+    }
+}
+
+// ---- triangular solves with the FP32 factor R (upper triangle of Q[0:n,
+// 0:n]) in FP64 arithmetic, blocks of kQrTB rows ----
+
+// Back substitution on the diagonal block [b0, b1): X[b0:b1, s] from
+// Y[b0:b1, s] (in place).  One CTA (kQrTB threads) per right-hand side.
+__global__ void qr_trsv_back_diag_kernel(int b0, int b1, const float2 *__restrict__ Q, size_t ldq, double2 *X,
+                                         size_t ldx) {
+    __shared__ double2 xk;
+    double2 *x = X + (size_t)blockIdx.x * ldx;
+    const int i = b0 + threadIdx.x;
+    double2 y = i < b1 ? x[i] : make_double2(0.0, 0.0);
+    for (int k = b1 - 1; k >= b0; k--) {
+        if (i == k) {
+            const float2 rk = Q[(size_t)k * ldq + k];
+            const double d = (double)rk.x * rk.x + (double)rk.y * rk.y;
+            y = make_double2((y.x * rk.x + y.y * rk.y) / d, (y.y * rk.x - y.x * rk.y) / d);   // y / r_kk
+            xk = y;
+        }
+        __syncthreads();
+        if (i < k) {
+            const float2 r = Q[(size_t)k * ldq + i];
+            const double2 u = zmul(make_double2(r.x, r.y), xk);
+            y.x -= u.x;
+            y.y -= u.y;
+        }
+        __syncthreads();
+    }
+    if (i < b1) x[i] = y;
+}
+
+// Y[0:b0, s] -= R[0:b0, b0:b1] X[b0:b1, s]; grid (ceil(b0/256), S).
+__global__ void qr_trsv_back_update_kernel(int b0, int b1, const float2 *__restrict__ Q, size_t ldq, double2 *X,
+                                           size_t ldx) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double2 *x = X + (size_t)blockIdx.y * ldx;
+    if (i >= b0) return;
+    double2 y = x[i];
+    for (int k = b0; k < b1; k++) {
+        const float2 r = Q[(size_t)k * ldq + i];
+        const double2 u = zmul(make_double2(r.x, r.y), x[k]);
+        y.x -= u.x;
+        y.y -= u.y;
+    }
+    x[i] = y;
+}
+
+// Forward substitution with R^H on the diagonal block [b0, b1) (in place).
+__global__ void qr_trsv_fwd_diag_kernel(int b0, int b1, const float2 *__restrict__ Q, size_t ldq, double2 *X,
+                                        size_t ldx) {
+    __shared__ double2 xk;
+    double2 *x = X + (size_t)blockIdx.x * ldx;
+    const int i = b0 + threadIdx.x;
+    double2 y = i < b1 ? x[i] : make_double2(0.0, 0.0);
+    for (int k = b0; k < b1; k++) {
+        if (i == k) {
+            const float2 rk = Q[(size_t)k * ldq + k];                  // conj(r_kk) divides
+            const double d = (double)rk.x * rk.x + (double)rk.y * rk.y;
+            y = make_double2((y.x * rk.x - y.y * rk.y) / d, (y.y * rk.x + y.x * rk.y) / d);
+            xk = y;
+        }
+        __syncthreads();
+        if (i > k && i < b1) {
+            const float2 r = Q[(size_t)i * ldq + k];                   // (R^H)_{ik} = conj(R_ki)
+            const double2 u = zjmul(make_double2(r.x, r.y), xk);
+            y.x -= u.x;
+            y.y -= u.y;
+        }
+        __syncthreads();
+    }
+    if (i < b1) x[i] = y;
+}
+
+// Y[b1:n, s] -= (R[b0:b1, b1:n])^H X[b0:b1, s]: one warp per row i, lanes over
+// the block's k (R's column i is contiguous in k).
+__global__ void qr_trsv_fwd_update_kernel(int b0, int b1, int n, const float2 *__restrict__ Q, size_t ldq,
+                                          double2 *X, size_t ldx) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    const int i = b1 + warp;
+    double2 *x = X + (size_t)blockIdx.y * ldx;
+    if (i >= n) return;
+    double2 acc = make_double2(0.0, 0.0);
+    for (int k = b0 + lane; k < b1; k += 32) {
+        const float2 r = Q[(size_t)i * ldq + k];
+        const double2 u = zjmul(make_double2(r.x, r.y), x[k]);
+        acc.x += u.x;
+        acc.y += u.y;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+        acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+    }
+    if (lane == 0) {
+        x[i].x -= acc.x;
+        x[i].y -= acc.y;
+    }
+}
+
+__global__ void qr_take_rhs_kernel(int n, int S, const float2 *__restrict__ Qb, size_t ldq, double2 *__restrict__ X) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (i < n) {
+        const float2 v = Qb[(size_t)j * ldq + i];
+        X[(size_t)j * n + i] = make_double2(v.x, v.y);
+    }
+}
+
+__global__ void qr_axpy_kernel(int n, const double2 *__restrict__ d, double2 *__restrict__ x) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        x[i].x += d[i].x;
+        x[i].y += d[i].y;
+    }
+}
+
+// R X = Y (back) or R^H X = Y (forward) for the S columns of X (ld ldx).
+void qr_trsv(bool forward, int n, int S, const float2 *Q, size_t ldq, double2 *X, size_t ldx, cudaStream_t st) {
+    const int nb = (n + kQrTB - 1) / kQrTB;
+    if (!forward) {
+        for (int b = nb - 1; b >= 0; b--) {
+            const int b0 = b * kQrTB, b1 = std::min(n, b0 + kQrTB);
+            qr_trsv_back_diag_kernel<<<S, kQrTB, 0, st>>>(b0, b1, Q, ldq, X, ldx);
+            if (b0 > 0)
+                qr_trsv_back_update_kernel<<<dim3((b0 + 255) / 256, S), 256, 0, st>>>(b0, b1, Q, ldq, X, ldx);
+            count_launch(b0 > 0 ? 2 : 1);
+        }
+    } else {
+        for (int b = 0; b < nb; b++) {
+            const int b0 = b * kQrTB, b1 = std::min(n, b0 + kQrTB);
+            qr_trsv_fwd_diag_kernel<<<S, kQrTB, 0, st>>>(b0, b1, Q, ldq, X, ldx);
+            if (b1 < n)
+                qr_trsv_fwd_update_kernel<<<dim3((n - b1 + 7) / 8, S), 256, 0, st>>>(b0, b1, n, Q, ldq, X, ldx);
+            count_launch(b1 < n ? 2 : 1);
+        }
+    }
+    KERNEL_CHECK();
+}
+
+// Cluster size of the panel kernel for `smem16` bytes of shared memory per
+// CTA at 16 CTAs: 16 when the device schedules that non-portable size, else
+// 8.  The kernel's attributes (shared-memory limit raised to the device's
+// opt-in maximum, non-portable cluster sizes allowed) are set once.
+int qr_cluster_size(size_t smem16) {
+    static std::once_flag once;
+    static bool nonportable = false;
+    static cudaError_t err = cudaSuccess;
+    std::call_once(once, [&] {
+        int maxs = 0, dev = 0;
+        err = cudaGetDevice(&dev);
+        if (err == cudaSuccess) err = cudaDeviceGetAttribute(&maxs, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        if (err == cudaSuccess)
+            err = cudaFuncSetAttribute(qr_panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, maxs);
+        nonportable = cudaFuncSetAttribute(qr_panel_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+                      cudaSuccess;
+        cudaGetLastError();
+    });
+    CUDA_TRY(err);
+    if (!nonportable) return 8;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(16);
+    cfg.blockDim = dim3(kQrNT);
+    cfg.dynamicSmemBytes = smem16;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = 16;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    const bool ok = cudaOccupancyMaxActiveClusters(&nclusters, qr_panel_kernel, &cfg) == cudaSuccess && nclusters >= 1;
+    cudaGetLastError();
+    return ok ? 16 : 8;
+}
+
+}  // namespace
+}  // namespace bem
+
+using namespace bem;
+
+void bem_solver_s::solve_qr_tc(bem_solve_info_t *info) {
+    const int m = R, n = N;
+    BEM_CHECK_ARG(m >= n && n >= 1, "QR: fewer rows than unknowns");
+    const size_t ldq = (size_t)((m + 1) & ~1);   // even: every column start is 16-byte aligned
+    const size_t ncq = (size_t)n + S;
+    // workspace: [A | B] (c64) with slack for the GEMM converter's last
+    // 16-byte read past the final column, taus, V, its interleaved form, T,
+    // G, Z, the packed operands, split-K partial sums, scales, status
+    const size_t ldv = (size_t)((m + 1) & ~1);
+    const int ldk = ((2 * kQrNB + 3) / 4) * 4;
+    q_A.ensure(sizeof(float2) * (ldq * ncq + 8));
+    q_tau.ensure(sizeof(float2) * (size_t)n);
+    qt_v.ensure(sizeof(float2) * ldv * kQrNB);
+    qt_vrr.ensure(sizeof(float) * 2 * (size_t)m * ldk);
+    qt_t.ensure(sizeof(float2) * kQrNB * kQrNB + sizeof(float) * 2 * kQrNB * kQrNB);
+    qt_z.ensure(sizeof(float) * 2 * kQrNB * ncq);
+    qt_opv.ensure(tc_operand_bytes(2 * m, 2 * kQrNB, 2));
+    qt_opw.ensure(tc_operand_bytes(2 * kQrNB, (int)ncq, 2));
+    const size_t pf = std::max({tc_gemm_part_floats(kQrNB, 2 * m, 2 * kQrNB, 2),
+                                tc_gemm_part_floats((int)ncq, 2 * m, 2 * kQrNB, 2),
+                                tc_gemm_part_floats(2 * m, 2 * kQrNB, (int)ncq, 2)});
+    if (pf) qt_part.ensure(sizeof(float) * pf);
+    qt_scal.ensure(sizeof(float) * 8);
+    d_status.ensure(4 * sizeof(int));
+    int *status = d_status.as<int>() + 1;
+    CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), stream));
+    float2 *Q = q_A.as<float2>();
+    float *sc = qt_scal.as<float>();
+    float2 *T = qt_t.as<float2>();
+    float *G = reinterpret_cast<float *>(T + kQrNB * kQrNB);
+    {
+        BEM_PROF("qr_copy", stream);
+        const dim3 g((n + 31) / 32, (m + 31) / 32);
+        if (prec == BEM_PREC_C64)
+            qr_copy_a_kernel<float2><<<g, 256, 0, stream>>>(m, n, d_A.as<float2>(), lda, Q, ldq);
+        else
+            qr_copy_a_kernel<double2><<<g, 256, 0, stream>>>(m, n, d_A.as<double2>(), lda, Q, ldq);
+        qr_copy_b_kernel<<<dim3((m + 255) / 256, S), 256, 0, stream>>>(m, S, d_B.as<double2>(), Q + (size_t)n * ldq,
+                                                                      ldq);
+        CUDA_TRY(cudaMemsetAsync(sc + 4, 0, sizeof(float), stream));
+        qr_colnorm_kernel<<<(unsigned)ncq, 256, 0, stream>>>(m, Q, ldq, reinterpret_cast<unsigned *>(sc + 4));
+        qr_scales_kernel<<<1, 1, 0, stream>>>(sc);
+        count_launch(4);
+        KERNEL_CHECK();
+    }
+    // panel cluster: 16 CTAs when schedulable and the rows fit
+    const size_t smax = [] {
+        int dev = 0, v = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        return (size_t)v;
+    }();
+    auto smem_for = [](int rows, int cl) { return sizeof(float2) * PanelLayout((rows + cl - 1) / cl).total; };
+    const int CL = smem_for(m, 16) <= smax ? qr_cluster_size(smem_for(m, 16)) : 8;
+    if (smem_for(m, CL) > smax)
+        BEM_FAIL(BEM_ERR_TOO_LARGE, "QR_TC: " + std::to_string(m) + " rows do not fit the panel cluster's shared memory");
+    for (int j0 = 0; j0 < n; j0 += kQrNB) {
+        const int pc = std::min(kQrNB, n - j0), mr = m - j0;
+        const int nct = (int)ncq - j0 - pc;
+        {
+            BEM_PROF("qr_panel", stream);
+            const int rb = (mr + CL - 1) / CL;
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(CL);
+            cfg.blockDim = dim3(kQrNT);
+            cfg.dynamicSmemBytes = smem_for(mr, CL);
+            cfg.stream = stream;
+            cudaLaunchAttribute at[1];
+            at[0].id = cudaLaunchAttributeClusterDimension;
+            at[0].val.clusterDim.x = CL;
+            at[0].val.clusterDim.y = 1;
+            at[0].val.clusterDim.z = 1;
+            cfg.attrs = at;
+            cfg.numAttrs = 1;
+            CUDA_TRY(cudaLaunchKernelEx(&cfg, qr_panel_kernel, Q, ldq, m, j0, pc, rb, q_tau.as<float2>() + j0));
+            count_launch();
+        }
+        if (nct <= 0) continue;
+        float2 *P = Q + (size_t)j0 * ldq + j0;             // the panel
+        float *C = reinterpret_cast<float *>(P + (size_t)pc * ldq);   // the trailing columns (interleaved real)
+        {
+            BEM_PROF("qr_t", stream);
+            qr_vfull_kernel<<<dim3((mr + 255) / 256, pc), 256, 0, stream>>>(mr, pc, P, ldq, qt_v.as<float2>(), ldv);
+            TcOperand opv = tc_operand_view(qt_opv.p, 2 * mr, 2 * pc, 2);
+            tc_pack_cplx_f32(qt_v.as<float2>(), mr, pc, opv, stream, ldv, true);
+            // G = V^H V (pc x pc): conj(V^T) V with V^T's rows the columns of Vf
+            tc_gemm(reinterpret_cast<const float *>(qt_v.p), 2 * ldv, false, pc, 2 * mr, sc + 2, opv, G, pc,
+                    qt_part.as<float>(), status, stream);
+            qr_larft_kernel<<<1, kQrNB, 0, stream>>>(pc, G, q_tau.as<float2>() + j0, T);
+            count_launch(2);
+        }
+        {
+            BEM_PROF("qr_update", stream);
+            // Z = C^H V (nct x pc), W' = T^H Z^H packed, C -= V W'
+            TcOperand opv = tc_operand_view(qt_opv.p, 2 * mr, 2 * pc, 2);
+            tc_gemm(C, 2 * ldq, false, nct, 2 * mr, sc, opv, qt_z.as<float>(), nct, qt_part.as<float>(), status,
+                    stream);
+            TcOperand opw = tc_operand_view(qt_opw.p, 2 * pc, nct, 2);
+            qr_pack_tw_kernel<2><<<(nct + kQrTwCols - 1) / kQrTwCols, kQrNB, 0, stream>>>(
+                nct, pc, qt_z.as<float>(), T, opw.Kp, opw.ncols_pad, opw.planes, opw.col_inv);
+            qr_vrr_kernel<<<mr, kQrNB, 0, stream>>>(mr, pc, qt_v.as<float2>(), ldv, qt_vrr.as<float>(), ldk);
+            count_launch(2);
+            tc_gemm(qt_vrr.as<float>(), ldk, false, 2 * mr, 2 * pc, sc + 2, opw, C, 2 * ldq, qt_part.as<float>(),
+                    status, stream, true);
+        }
+        KERNEL_CHECK();
+    }
+    // X = R^{-1} (Q^H B)[0:n]
+    double2 *X = d_x.as<double2>();
+    {
+        BEM_PROF("qr_trsv", stream);
+        qr_take_rhs_kernel<<<dim3((n + 255) / 256, S), 256, 0, stream>>>(n, S, Q + (size_t)n * ldq, ldq, X);
+        count_launch();
+        qr_trsv(false, n, S, Q, ldq, X, n, stream);
+    }
+    // FP64 refinement through the semi-normal equations with the FP32 factor
+    w_r.ensure(sizeof(double2) * (size_t)m);
+    w_gv.ensure(sizeof(double2) * (size_t)n);
+    w_vf.ensure(sizeof(float2) * (2 * (size_t)std::max(n, m) + 2));
+    w_part.ensure(std::max(sizeof(float2) * (size_t)gemv_h_splits(m, n), sizeof(double2) * (size_t)gemv_h_f64_splits(m, n)) *
+                  (size_t)n);
+    w_scal.ensure(sizeof(double) * 8);
+    double *scal = w_scal.as<double>();
+    auto read_scalar = [&](int i) {
+        CUDA_TRY(cudaMemcpyAsync(h_pinned + i, scal + i, sizeof(double), cudaMemcpyDeviceToHost, stream));
+        CUDA_TRY(cudaStreamSynchronize(stream));
+        return h_pinned[i];
+    };
+    int steps_max = 0;
+    double worst = 0.0;
+    bool all_conv = true;
+    const double tol = kQrRefineTol;
+    for (int s = 0; s < S; s++) {
+        const double2 *b = d_B.as<double2>() + (size_t)s * m;
+        double2 *x = X + (size_t)s * n;
+        launch_gemv_h_f64(prec, m, n, d_A.p, lda, b, w_gv.as<double2>(), w_part.as<double2>(), w_vf.as<float2>(),
+                          stream);
+        launch_nrm2(n, w_gv.as<double2>(), scal + 0, nullptr, stream);
+        const double bn = read_scalar(0);
+        double rel = 0.0, prev = 1e300;
+        int it = 0;
+        bool conv = !(bn > 0.0);
+        for (; !conv && it <= opt.max_refine; it++) {
+            BEM_PROF("qr_refine", stream);
+            launch_resid(prec, m, n, d_A.p, lda, x, b, w_r.as<double2>(), w_vf.as<float2>(), stream);
+            launch_gemv_h_f64(prec, m, n, d_A.p, lda, w_r.as<double2>(), w_gv.as<double2>(), w_part.as<double2>(),
+                              w_vf.as<float2>(), stream);
+            launch_nrm2(n, w_gv.as<double2>(), scal + 1, nullptr, stream);
+            rel = read_scalar(1) / bn;
+            if (!std::isfinite(rel)) BEM_FAIL(BEM_ERR_NUMERIC, "QR refinement residual is not finite");
+            if (rel <= tol) { conv = true; break; }
+            if (rel > 0.5 * prev || it == opt.max_refine) {
+                // stagnated at the precision of the FP64-accurate products:
+                // converged when that level is FP64's
+                conv = rel <= kQrStagnationOk;
+                break;
+            }
+            prev = rel;
+            qr_trsv(true, n, 1, Q, ldq, w_gv.as<double2>(), n, stream);    // R^H y = g
+            qr_trsv(false, n, 1, Q, ldq, w_gv.as<double2>(), n, stream);   // R d = y
+            qr_axpy_kernel<<<(n + 255) / 256, 256, 0, stream>>>(n, w_gv.as<double2>(), x);
+            count_launch();
+        }
+        steps_max = std::max(steps_max, it);
+        worst = std::max(worst, rel);
+        all_conv &= conv;
+    }
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    int h_status = 0;
+    CUDA_TRY(cudaMemcpy(&h_status, status, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h_status) BEM_FAIL(BEM_ERR_TIMEOUT, "QR_TC: a bounded wait of the tensor-core GEMM timed out");
+    if (info) {
+        info->iterations = 0;
+        info->refinements = steps_max;
+        info->rel_residual = worst;
+        info->converged = all_conv ? 1 : 0;
+    }
+}

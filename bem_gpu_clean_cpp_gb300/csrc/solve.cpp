@@ -115,6 +115,9 @@ void bem_solver_s::solve_refined(bem_solve_info_t *info) {
     part = std::max(part, sizeof(float2) * (size_t)normal_op_clusters(n));
     w_part.ensure(part * n);
     w_scal.ensure(sizeof(double) * 8);
+    d_status.ensure(4 * sizeof(int));
+    int *op_status = d_status.as<int>();
+    CUDA_TRY(cudaMemsetAsync(op_status, 0, sizeof(int), stream));
     w_ap.ensure(sizeof(double2) * 3 * (size_t)(m + 1) * std::max(1, arnoldi_step_blocks()));
     double2 *V = w_V.as<double2>();
     double *scal = w_scal.as<double>();
@@ -162,7 +165,7 @@ void bem_solver_s::solve_refined(bem_solve_info_t *info) {
             // ev_res[j & 1].
             auto launch_step = [&](int j) {
                 if (!launch_normal_op(R, n, A, lda, w_vf.as<float2>(), w_w.as<double2>(), w_part.as<float2>(),
-                                      stream)) {
+                                      op_status, stream)) {
                     launch_gemv_c64(R, n, A, lda, w_vf.p, 0, w_t.p, 0, stream);              // t = A v_j
                     launch_gemv_h_c64(R, n, A, lda, w_t.p, 0, w_w.p, 1, w_part.p, stream);  // w = A^H t
                 }
@@ -215,7 +218,7 @@ void bem_solver_s::solve_refined(bem_solve_info_t *info) {
         all_conv &= conv ? 1 : 0;
     }
     CUDA_TRY(cudaStreamSynchronize(stream));
-    if (normal_op_timed_out(stream))
+    if (normal_op_timed_out(op_status, stream))
         BEM_FAIL(BEM_ERR_TIMEOUT, "normal operator: a bulk copy of A did not complete in time");
     if (info) {
         info->iterations = total_it;
@@ -253,7 +256,7 @@ void bem_solver_s::eval_field(const double *pts, int P, void *out, int ldo, int 
         else launch_cast_up(N * S, (const float2 *)u, f_u.as<double2>(), stream);
         u = f_u.p;
     }
-    int nsplit = std::max(1, std::min(64, (4 * 152 + P - 1) / P));
+    int nsplit = std::max(1, std::min(64, (4 * device_sm_count() + P - 1) / P));
     nsplit = std::min(nsplit, std::max(1, E / 256));
     f_part.ensure(sizeof(double2) * (size_t)nsplit * P * S);
     f_near.ensure(sizeof(double2) * (size_t)P * S);

@@ -2,6 +2,7 @@
 // tiles, assembly launches, the dense QR least-squares solve and the
 // mixed-precision refined GMRES solve.
 #include "solver.h"
+#include "tc_gemm.h"
 
 #include <algorithm>
 #include <future>
@@ -51,38 +52,48 @@ uint32_t morton_key(const double *p, const double *lo, const double *inv) {
     return k;
 }
 
-// Greedy vertex-disjoint colouring of the elements: elements of one colour
-// share no node, so consecutive records in a tile list rarely add to the same
-// shared-memory column in the same instruction.
-std::vector<int> color_elements(int N, const std::vector<int> &elems) {
-    const int E = (int)(elems.size() / 3);
-    // node -> the colours used by elements already coloured at that node, as
-    // a bit set (64 colours; an element whose neighbours use all 64 takes
-    // the first free colour above, found by a scan)
-    std::vector<uint64_t> used(N, 0);
-    std::vector<int> color(E);
-    std::vector<std::vector<int>> high;   // colours >= 64 per node, rarely used
-    for (int e = 0; e < E; e++) {
-        const int *nd = &elems[3 * (size_t)e];
-        const uint64_t m = used[nd[0]] | used[nd[1]] | used[nd[2]];
-        int c;
-        if (~m) {
-            c = __builtin_ctzll(~m);
-            for (int j = 0; j < 3; j++) used[nd[j]] |= 1ull << c;
-        } else {
-            if (high.empty()) high.resize(N);
-            c = 64;
-            for (bool clash = true; clash; ) {
-                clash = false;
-                for (int j = 0; j < 3 && !clash; j++)
-                    clash = std::find(high[nd[j]].begin(), high[nd[j]].end(), c) != high[nd[j]].end();
-                if (clash) c++;
+// Balanced packing of one tile's records (in element order) into batches of
+// at most kFarBatch records whose in-tile columns are all distinct: a record
+// goes to the least-filled batch that has room and none of its columns (a new
+// batch when none qualifies), starting from ceil(records / kFarBatch)
+// batches.  An element shares a node with about a dozen others, so the
+// batches come out equal (icosphere subdivision 5: 20 batches of 1024; small
+// meshes: at least 13).  Appends the records batch by batch to `out` and the
+// batch boundaries (offsets into `out`) to `bptr`.
+void pack_batches(const std::vector<TileRec> &list, int tile_cols, std::vector<TileRec> &out,
+                  std::vector<int> &bptr) {
+    std::vector<int> size((list.size() + kFarBatch - 1) / kFarBatch, 0), batch_of(list.size());
+    std::vector<std::vector<int>> slot_batches(tile_cols);   // batches already holding a record on the slot
+    for (size_t r = 0; r < list.size(); r++) {
+        const TileRec &rec = list[r];
+        auto clash = [&](int b) {
+            for (int j = 0; j < 3; j++) {
+                const int s = rec.slot[j];
+                if (s < 0) continue;
+                for (const int u : slot_batches[s])
+                    if (u == b) return true;
             }
-            for (int j = 0; j < 3; j++) high[nd[j]].push_back(c);
+            return false;
+        };
+        int best = -1;
+        for (int b = 0; b < (int)size.size(); b++)
+            if (size[b] < kFarBatch && (best < 0 || size[b] < size[best]) && !clash(b)) best = b;
+        if (best < 0) {
+            best = (int)size.size();
+            size.push_back(0);
         }
-        color[e] = c;
+        size[best]++;
+        batch_of[r] = best;
+        for (int j = 0; j < 3; j++)
+            if (rec.slot[j] >= 0) slot_batches[rec.slot[j]].push_back(best);
     }
-    return color;
+    // stable counting sort of the records by batch
+    std::vector<int> start(size.size() + 1, 0);
+    for (size_t b = 0; b < size.size(); b++) start[b + 1] = start[b] + size[b];
+    const size_t base = out.size();
+    out.resize(base + list.size());
+    for (size_t b = 0; b < size.size(); b++) bptr.push_back((int)(base + start[b + 1]));
+    for (size_t r = 0; r < list.size(); r++) out[base + start[batch_of[r]]++] = list[r];
 }
 
 // Far-kernel launch shapes chosen by the autotuner, per device and problem
@@ -346,7 +357,6 @@ bem::HostTiles bem::build_host_tiles(int N, int E, const std::vector<double> &h_
         cols[(size_t)t * per + s] = order[i];
         cnt[t]++;
     }
-    const std::vector<int> color = color_elements(N, h_elems);
     std::vector<std::vector<TileRec>> lists(ntiles);
     if (ntiles == 1) lists[0].reserve(E);
     for (int e = 0; e < E; e++) {
@@ -371,17 +381,13 @@ bem::HostTiles bem::build_host_tiles(int N, int E, const std::vector<double> &h_
     std::vector<TileRec> &recs = out.recs;
     std::vector<int> &ptr = out.ptr;
     ptr.assign(ntiles + 1, 0);
-    int ncolor = 0;
-    for (int c : color) ncolor = std::max(ncolor, c + 1);
-    std::vector<int> cstart(ncolor + 1);
+    out.bptr.assign(1, 0);
+    out.tbatch.assign(ntiles + 1, 0);
+    recs.reserve(lists[0].size() * ntiles);
     for (int t = 0; t < ntiles; t++) {
-        // stable counting sort of the tile's records by element colour
-        std::fill(cstart.begin(), cstart.end(), 0);
-        for (const TileRec &r : lists[t]) cstart[color[r.eid] + 1]++;
-        for (int c = 0; c < ncolor; c++) cstart[c + 1] += cstart[c];
-        ptr[t + 1] = ptr[t] + (int)lists[t].size();
-        recs.resize(ptr[t + 1]);
-        for (const TileRec &r : lists[t]) recs[ptr[t] + cstart[color[r.eid]]++] = r;
+        pack_batches(lists[t], per, recs, out.bptr);
+        ptr[t + 1] = (int)recs.size();
+        out.tbatch[t + 1] = (int)out.bptr.size() - 1;
     }
     out.ntiles = ntiles;
     out.per = per;
@@ -412,6 +418,12 @@ void bem_solver_s::ensure_tiles(int precision) {
     T.rec_ptr.ensure(sizeof(int) * ptr.size());
     T.cols.ensure(sizeof(int) * cols.size());
     T.col_cnt.ensure(sizeof(int) * cnt.size());
+    T.batch_ptr.ensure(sizeof(int) * ht.bptr.size());
+    T.tile_batch.ensure(sizeof(int) * ht.tbatch.size());
+    CUDA_TRY(cudaMemcpyAsync(T.batch_ptr.p, ht.bptr.data(), sizeof(int) * ht.bptr.size(), cudaMemcpyHostToDevice,
+                             stream));
+    CUDA_TRY(cudaMemcpyAsync(T.tile_batch.p, ht.tbatch.data(), sizeof(int) * ht.tbatch.size(),
+                             cudaMemcpyHostToDevice, stream));
     CUDA_TRY(cudaMemcpyAsync(T.recs.p, recs.data(), sizeof(TileRec) * recs.size(), cudaMemcpyHostToDevice, stream));
     CUDA_TRY(cudaMemcpyAsync(T.rec_ptr.p, ptr.data(), sizeof(int) * ptr.size(), cudaMemcpyHostToDevice, stream));
     CUDA_TRY(cudaMemcpyAsync(T.cols.p, cols.data(), sizeof(int) * cols.size(), cudaMemcpyHostToDevice, stream));
@@ -451,7 +463,10 @@ void bem_solver_s::assemble(double kk, int precision) {
     d_B.ensure(sizeof(double2) * (size_t)R * S);
     d_cpart.ensure(rsz * (size_t)T.ntiles * R);
     d_bpart.ensure(2 * rsz * (size_t)T.ntiles * R);
-    TileSet ts{T.recs.as<TileRec>(), T.rec_ptr.as<int>(), T.cols.as<int>(), T.col_cnt.as<int>(), T.ntiles, T.tc_max};
+    d_status.ensure(4 * sizeof(int));
+    CUDA_TRY(cudaMemsetAsync(d_status.as<int>() + 2, 0, sizeof(int), stream));
+    TileSet ts{T.recs.as<TileRec>(), T.rec_ptr.as<int>(), T.batch_ptr.as<int>(), T.tile_batch.as<int>(),
+               d_status.as<int>() + 2, T.cols.as<int>(), T.col_cnt.as<int>(), T.ntiles, T.tc_max};
     Physics ph = physics();
     int variant = opt.far_variant;
     bool done = false;
@@ -518,6 +533,7 @@ void bem_solver_s::assemble(double kk, int precision) {
     assembled = true;
     solved = false;
     tf32_split_mode = -1;
+    tc_scale_valid = false;
 }
 
 void bem_solver_s::solve(int method, bem_solve_info_t *info) {
@@ -533,9 +549,16 @@ void bem_solver_s::solve(int method, bem_solve_info_t *info) {
     } else if (method == BEM_SOLVE_BLOCK_GMRES) {
         if (prec != BEM_PREC_C64) BEM_FAIL(BEM_ERR_STATE, "block GMRES needs a c64 assembly");
         solve_block(info);
+    } else if (method == BEM_SOLVE_QR_TC) {
+        solve_qr_tc(info);
     } else {
         BEM_FAIL(BEM_ERR_INVALID_ARG, "unknown solve method");
     }
+    // a bounded wait of the assembly's far kernel that timed out (status word 2)
+    int far_status = 0;
+    CUDA_TRY(cudaMemcpyAsync(&far_status, d_status.as<int>() + 2, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    CUDA_TRY(cudaStreamSynchronize(stream));
+    if (far_status) BEM_FAIL(BEM_ERR_TIMEOUT, "assembly: a bounded wait of the far-field kernel timed out");
     solved = true;
 }
 
@@ -591,10 +614,13 @@ void bem_solver_s::get_system(void *A, int lda_out, void *B, int ldb_out, int pr
 size_t bem_solver_s::device_bytes() const {
     const DevMem *all[] = {&d_nodes, &d_rows_f, &d_rows_d, &d_elems, &d_bc, &d_geo_f, &d_geo_d, &d_srcs,
                            &tiles[0].recs, &tiles[0].rec_ptr, &tiles[0].cols, &tiles[0].col_cnt,
+                           &tiles[0].batch_ptr, &tiles[0].tile_batch,
                            &tiles[1].recs, &tiles[1].rec_ptr, &tiles[1].cols, &tiles[1].col_cnt,
+                           &tiles[1].batch_ptr, &tiles[1].tile_batch,
                            &d_A, &d_B, &d_cpart, &d_bpart, &d_x, &d_beta, &d_near_ptr, &d_near_ids, &d_grid_start, &d_grid_elems,
                            &w_V, &w_H, &w_cs, &w_sn, &w_g, &w_y, &w_h1, &w_h2, &w_w, &w_t, &w_r, &w_gv, &w_vf,
-                           &w_part, &w_scal, &x_Ahi, &x_Alo, &x_vlo, &x_tlo, &w_d, &w_ap, &q_A, &q_B, &q_tau, &q_work, &q_info,
+                           &w_part, &w_scal, &x_Ahi, &x_Alo, &x_vlo, &x_tlo, &w_d, &w_ap, &tc_scale, &d_status, &q_A, &q_B, &q_tau, &q_work, &q_info,
+                           &qt_v, &qt_vrr, &qt_t, &qt_z, &qt_opv, &qt_opw, &qt_part, &qt_scal,
                            &f_rows_f, &f_rows_d, &f_part, &f_near, &f_out, &f_u};
     size_t b = 0;
     for (const DevMem *d : all) b += d->bytes;
@@ -609,6 +635,7 @@ size_t bem_solver_s::estimate_bytes(int N, int E, int M, int S, int method, cons
     b += 24 * n + 24 * r + 32 * r + 16 * e + 48 * e;                  // nodes, rows, elements, bc
     b += sizeof(float4) * kGeoFloat4 * e + sizeof(double) * kGeoDouble * e;
     b += 3 * e * sizeof(TileRec) + 4 * (ntiles + 1) + 4 * n + 4 * ntiles;   // an element touches <= 3 tiles
+    b += 4 * (3 * e + 2 * ntiles + 2);                                     // record batches (>= 1 record each)
     b += 4 * (r + 1) + 256 * r + 4 * e + (16u << 20);                       // near-pair list and search grid
     b += 8 * lda * r + 16 * r * s + 12 * ntiles * r + 16 * n * s + 16 * r + 48 * s;
     if (method == BEM_SOLVE_BLOCK_GMRES) {
@@ -620,6 +647,9 @@ size_t bem_solver_s::estimate_bytes(int N, int E, int M, int S, int method, cons
             if (gm == BEM_GEMM_TF32X3) extra = std::max(extra, 16 * lda * r + 48 * n * s + 16 * r * s);
             if (gm == BEM_GEMM_TF32X3_3M) extra = std::max(extra, 24 * lda * r + 48 * std::max(n, r) * s);
             if (gm == BEM_GEMM_SIMT) extra = std::max(extra, 4 * block_simt_scratch_floats((int)r, N, S));
+            if (gm == BEM_GEMM_TC)
+                extra = std::max(extra, tc_operand_bytes((int)std::max(2 * n, r), 2 * S, 3) +
+                                            4 * tc_gemm_part_floats_bound((int)std::max(2 * n, r), 2 * S) + 64);
         }
         b += extra;
     } else if (method == BEM_SOLVE_GMRES_REFINED) {
@@ -629,6 +659,14 @@ size_t bem_solver_s::estimate_bytes(int N, int E, int M, int S, int method, cons
         b += 16 * n * (size_t)std::max(gemv_h_splits((int)r, N), gemv_h_f64_splits((int)r, N)) + 64;
         b += 8 * n * (size_t)std::max(0, normal_op_clusters(N) - 2 * gemv_h_splits((int)r, N));
         b += 48 * (m + 1) * 160;                                                     // Arnoldi step partials
+    } else if (method == BEM_SOLVE_QR_TC) {
+        const size_t nb = 128, rp = r + 1;
+        b += 8 * (rp * (n + s) + 8) + 8 * n;                               // [A | B] c64, taus
+        b += 8 * rp * nb + 4 * 2 * r * 256 + 8 * nb * nb + 8 * nb * nb;  // V, Vrr, T, G
+        b += 4 * 2 * nb * (n + s) + tc_operand_bytes((int)(2 * r), (int)(2 * nb), 2) +
+             tc_operand_bytes((int)(2 * nb), (int)(n + s), 2) + 4 * tc_gemm_part_floats_bound((int)(2 * r), (int)(n + s));
+        b += 16 * r + 16 * n + 8 * (2 * std::max(n, r) + 2) +
+             16 * n * (size_t)std::max(gemv_h_splits((int)r, N), gemv_h_f64_splits((int)r, N));
     } else {
         b += 8 * r * n + 8 * r * s + 64 * n + (64u << 20);               // QR copy, tau, library workspace
     }

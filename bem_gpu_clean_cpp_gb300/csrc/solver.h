@@ -46,6 +46,7 @@ struct HostTiles {
     int cap = -1, ntiles = 0, per = 0;
     std::vector<TileRec> recs;
     std::vector<int> ptr, cols, cnt;
+    std::vector<int> bptr, tbatch;   // node-disjoint batches of records (TileSet::batch_ptr, tile_batch)
 };
 HostTiles build_host_tiles(int N, int E, const std::vector<double> &h_nodes, const std::vector<int> &h_elems,
                            int cap);
@@ -79,7 +80,7 @@ struct bem_solver_s {
     struct Tiles {
         bool valid = false;
         int ntiles = 0, tc_max = 0;
-        bem::DevMem recs, rec_ptr, cols, col_cnt;
+        bem::DevMem recs, rec_ptr, cols, col_cnt, batch_ptr, tile_batch;
     } tiles[2];
 
     int far_variant_used = -1;
@@ -99,12 +100,26 @@ struct bem_solver_s {
     bem::DevMem x_Ahi, x_Alo, x_vlo, x_tlo, w_d;
     bem::DevMem w_ap;   // partial sums of the cooperative Arnoldi step
     int tf32_split_mode = -1;   // BEM_GEMM_* the planes of A were built for (this assembly), -1 none
+    // tensor-core products (BEM_GEMM_TC): the power-of-two scale of A ([0]
+    // scale, [1] inverse, [2] scratch), valid for this assembly
+    bem::DevMem tc_scale;
+    bool tc_scale_valid = false;
+    int last_block_gemm_mode = -1;   // BEM_GEMM_* the last block solve ran its products in
+    // device status words of this handle's kernels (each zeroed by its user
+    // before its kernels run): [0] a bounded wait of the normal operator timed
+    // out, [1] one of the tensor-core GEMM's did, [2] one of the far-field
+    // assembly kernel's did
+    bem::DevMem d_status;
     double *h_pinned = nullptr;
     cudaEvent_t ev_res[2] = {nullptr, nullptr};   // refined GMRES: residual estimate of step j in h_pinned[4 + (j & 1)]
     void *h_stage = nullptr;     // pinned staging for geometry uploads
     size_t h_stage_bytes = 0;
     // QR workspace
     bem::DevMem q_A, q_B, q_tau, q_work, q_info;
+    // tensor-core QR (solve_qr_tc): the panel's V and its interleaved form, T
+    // and V^H V, Z = C^H V, the packed right-hand operands, split-K partial
+    // sums, scales
+    bem::DevMem qt_v, qt_vrr, qt_t, qt_z, qt_opv, qt_opw, qt_part, qt_scal;
     // field workspace
     bem::DevMem f_rows_f, f_rows_d, f_part, f_near, f_out, f_u;
 
@@ -143,6 +158,7 @@ struct bem_solver_s {
     bem::RowPoints row_points() const;
     bem::Physics physics() const;
     void solve_qr();
+    void solve_qr_tc(bem_solve_info_t *info);
     void solve_refined(bem_solve_info_t *info);
     void solve_block(bem_solve_info_t *info);
     // GEMM modes of the block solve worth running for S right-hand sides and
@@ -169,11 +185,7 @@ struct bem_solver_s {
     //   per SM) than with SGEMM.
     static std::vector<int> block_gemm_candidates(const bem_options_t &o, int S, int R, int N) {
         if (o.gemm_mode >= 0) return {o.gemm_mode};
-        const bool planes = 8.0 * R * N <= 4e9;
-        if (S <= 8) return {BEM_GEMM_SIMT};
-        if (!planes) return {S >= 32 ? BEM_GEMM_SPLIT_BF16 : BEM_GEMM_FP32};
-        if (S >= 128) return {BEM_GEMM_TF32X3_3M};
-        if (S <= 32) return {BEM_GEMM_SIMT, BEM_GEMM_TF32X3};
-        return {BEM_GEMM_TF32X3};
+        if (S <= 8) return {BEM_GEMM_SIMT, BEM_GEMM_TC};
+        return {BEM_GEMM_TC};
     }
 };

@@ -57,6 +57,8 @@ def parse_args():
     ap.add_argument("--depth", type=int, default=2)
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 reference solve")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="precision: skip the rhs (256 sources) and serve (request stream) objects of the line")
     ap.add_argument("--config", default="precision", choices=["precision", "rhs", "freq", "serve"],
                     help="precision: the headline workload (one plane wave); rhs: perturbed ellipsoid, "
                          "8 kHz, 256 point sources solved together (block GMRES); freq: 64 frequencies of "
@@ -68,13 +70,15 @@ def parse_args():
     ap.add_argument("--slots", type=int, default=8, help="freq/serve: requests in flight at once")
     ap.add_argument("--rate", type=float, default=2.0, help="serve: mean request arrivals per second")
     ap.add_argument("--requests", type=int, default=40, help="serve: requests in the stream")
-    ap.add_argument("--gemm", type=int, default=-1, choices=[-1, 0, 1, 2, 3, 4, 5],
+    ap.add_argument("--gemm", type=int, default=-1, choices=[-1, 0, 1, 2, 3, 4, 5, 6],
                     help="block-solve GEMM mode (-1 auto, 0 FP32, 1 split-BF16 FP32-accurate, 2 TF32, 3 TF32x3, "
                          "4 TF32x3 in the 3M form, 5 FP32 streaming kernels on the CUDA cores)")
     ap.add_argument("--far-variant", type=int, default=-1,
                     help="profile mode: fixed far-field launch shape (-1: autotuned)")
-    ap.add_argument("--mode", default="bench", choices=["bench", "profile"],
-                    help="profile: one warm-up solve and one more solve, nothing timed (for ncu captures)")
+    ap.add_argument("--mode", default="bench", choices=["bench", "profile", "cpu-validate"],
+                    help="profile: one warm-up solve and one more solve, nothing timed (for ncu captures); "
+                         "cpu-validate: the CPU legs' sample extrapolation against full FP64 CPU solves of "
+                         "the workload at icosphere subdivisions 3 and 4")
     return ap.parse_args()
 
 
@@ -334,7 +338,14 @@ class Clocks:
 # ---------------------------------------------------------------------------
 # CPU restatement timing (the oracle), bounded sample of the same workload
 # ---------------------------------------------------------------------------
-def cpu_sample(pts, elems, chief, srcs, k, bc, eta, depth, threads, rows=64, n_qr=1024):
+# Sample of the CPU legs (the cpu_baseline of our arm and the --impl
+# reference arm use the same): assembly of CPU_ROWS rows, Householder QR of a
+# (CPU_QR + 32) x CPU_QR system (out of cache, like the full one).
+CPU_ROWS = 256
+CPU_QR = 2048
+
+
+def cpu_sample(pts, elems, chief, srcs, k, bc, eta, depth, threads, rows=CPU_ROWS, n_qr=CPU_QR):
     """FP64 CPU time of one surface solve, extrapolated from a sample:
     assembly of `rows` rows (all elements and sources, x (N+M)/rows) plus a
     Householder QR least-squares solve of an (n_qr+32) x n_qr system (x flop
@@ -368,6 +379,40 @@ def cpu_sample(pts, elems, chief, srcs, k, bc, eta, depth, threads, rows=64, n_q
                       f"QR {t_qr:.1f} s)"}
 
 
+def run_cpu_validate(args):
+    """The extrapolation behind cpu_baseline and the reference arm, checked
+    against full FP64 CPU solves (every row assembled, the full least-squares
+    QR) of the headline workload at subdivisions 3 and 4 (642 and 2562
+    nodes), with the sample the CPU legs take at subdivision 5 (256 rows, a
+    QR of 2048 columns), capped at the problem's size: at subdivision 4 the
+    rows are extrapolated x10 and the QR x1.9 by flop count."""
+    import oracle
+    threads = os.cpu_count() or 1
+    out = []
+    for sub in (3, 4):
+        a = argparse.Namespace(**vars(args))
+        a.subdiv = sub
+        pts, elems, chief, d, k, bc = workload(a)
+        srcs = [("plane", d, 1.0)]
+        R, N = pts.shape[0] + chief.shape[0], pts.shape[0]
+        rows, n_qr = min(CPU_ROWS, R), min(CPU_QR, N)
+        est = cpu_sample(pts, elems, chief, srcs, k, bc, args.eta, args.depth, threads, rows=rows, n_qr=n_qr)
+        prm = oracle.params(near_eta=args.eta, near_depth=args.depth)
+        t0 = time.perf_counter()
+        Ao, Bo = oracle.assemble(np.vstack([pts, chief]), elems, k, N, srcs, bc=bc, prm=prm)
+        t_asm = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        oracle.lsq_qr(Ao, Bo)
+        t_qr = time.perf_counter() - t0
+        full = t_asm + t_qr
+        extrap = 1.0 / est["value"]
+        out.append({"subdiv": sub, "nodes": N, "rows": R, "sample_rows": rows, "sample_qr_columns": n_qr,
+                    "extrapolated_s": extrap, "full_s": full, "full_assembly_s": t_asm, "full_qr_s": t_qr,
+                    "extrapolated_over_full": extrap / full, "sample": est["sample"], "cores": threads})
+    print(json.dumps({"mode": "cpu-validate", "results": out}), flush=True)
+    return 0
+
+
 def run_reference(args):
     rank, world, _ = dist_info()
     if rank != 0:
@@ -375,9 +420,11 @@ def run_reference(args):
     pts, elems, chief, srcs, k, bc, name = select_workload(args)
     threads = os.cpu_count() or 1
     vals = []
-    for i in range(args.warmup + args.steps):
-        r = cpu_sample(pts, elems, chief, srcs, k, bc, args.eta, args.depth, threads, rows=16, n_qr=512)
-        if i >= args.warmup:
+    # the same sample as our arm's cpu_baseline; a step is one sample (a few
+    # seconds), warm-up steps capped at one so the run stays within minutes
+    for i in range(min(args.warmup, 1) + args.steps):
+        r = cpu_sample(pts, elems, chief, srcs, k, bc, args.eta, args.depth, threads)
+        if i >= min(args.warmup, 1):
             vals.append(r["value"])
     v = float(np.mean(vals))
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
@@ -386,7 +433,7 @@ def run_reference(args):
             "config": {"workload": name, "subdiv": args.subdiv, "ka": args.ka, "chief": args.chief,
                        "sources": len(srcs), "seed": args.seed, "near_eta": args.eta},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": r["sample"].replace("16/", "16 rows of ") + "; per step"},
+                             "sample": r["sample"] + "; one sample per step"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -505,26 +552,33 @@ def run_ours(args):
     if infos:
         d2h += 8 * int(np.mean([i.iterations + 2 * i.refinements + 1 for i in infos]))
 
-    # ---- plain FP64 path once (FP64 assembly + Householder QR) ----
+    # ---- plain FP64 path (FP64 assembly + Householder QR): one warm-up solve
+    # (handles, library workspace, kernel loading), then the median of 3 ----
     fp64 = None
     if not args.no_fp64:
         s3 = bem.Solver(**opts)
         s3.set_geometry(pts, elems, bc=bc, chief=chief)
         s3.set_sources(src)
         st3 = torch.cuda.ExternalStream(s3.stream())
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(st3)
-        s3.assemble(k, bem.PREC_C128)
-        s3.solve(bem.SOLVE_QR)
-        b.record(st3)
-        s3.sync()
-        ms64 = a.elapsed_time(b)
+        runs = []
+        for rep in range(4):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(st3)
+            s3.assemble(k, bem.PREC_C128)
+            s3.solve(bem.SOLVE_QR)
+            b.record(st3)
+            s3.sync()
+            if rep > 0:
+                runs.append(a.elapsed_time(b))
+        ms64 = statistics.median(runs)
         x64_all = s3.solution()
         x64 = x64_all[:, 0]
         err = max(float(np.abs(x_mixed[:, j] - x64_all[:, j]).max() / np.abs(x64_all[:, j]).max())
                   for j in range(S))
-        fp64 = {"ms": ms64, "solves_per_s": S * 1000.0 / ms64, "rel_err_mixed_vs_fp64": err,
-                "speedup_mixed_vs_fp64": value / dist.world / (S * 1000.0 / ms64)}
+        fp64 = {"ms": ms64, "ms_runs": runs, "spread": (max(runs) - min(runs)) / ms64,
+                "solves_per_s": S * 1000.0 / ms64, "rel_err_mixed_vs_fp64": err,
+                "speedup_mixed_vs_fp64": value / dist.world / (S * 1000.0 / ms64),
+                "timing": "median of 3 after one warm-up solve"}
         del s3
 
     # ---- the reference's own GPU path on this GB300, once ----
@@ -540,19 +594,25 @@ def run_ours(args):
             if refk.available():
                 rows = np.vstack([pts, chief]).astype(np.float32)
                 bc_ref = np.tile(np.array([0, 1, 0], dtype=np.complex128), (E, 1))
-                Ar, Br, ms_asm = refk.assemble(rows, elems, N, k, srcs=[(1e6, 1e6, 1e6)], strength=0.0, bc=bc_ref)
-                ms_asm2 = refk.assemble(rows, elems, N, k, srcs=[(1e6, 1e6, 1e6)], strength=0.0, bc=bc_ref)[2]
-                inc = np.exp(-1j * k * (rows.astype(np.float64) @ d)).astype(np.complex64)   # plane wave RHS
-                xr, ms_qr = refk.qr(Ar, (Br[:, 0] + inc).reshape(-1, 1))
+                asm_runs, qr_runs = [], []
+                for rep in range(4):   # one warm-up, then 3 timed
+                    Ar, Br, ms_asm = refk.assemble(rows, elems, N, k, srcs=[(1e6, 1e6, 1e6)], strength=0.0,
+                                                   bc=bc_ref)
+                    inc = np.exp(-1j * k * (rows.astype(np.float64) @ d)).astype(np.complex64)   # plane wave RHS
+                    xr, ms_qr = refk.qr(Ar, (Br[:, 0] + inc).reshape(-1, 1))
+                    if rep > 0:
+                        asm_runs.append(ms_asm)
+                        qr_runs.append(ms_qr)
                 err_ref = None
                 if fp64:
                     err_ref = float(np.abs(xr[:, 0] - x64).max() / np.abs(x64).max())
-                ref_gpu = {"assembly_ms": min(ms_asm, ms_asm2), "qr_ms": ms_qr,
-                           "solve_ms": min(ms_asm, ms_asm2) + ms_qr,
-                           "solves_per_s": 1000.0 / (min(ms_asm, ms_asm2) + ms_qr),
+                ma, mq = statistics.median(asm_runs), statistics.median(qr_runs)
+                ref_gpu = {"assembly_ms": ma, "qr_ms": mq, "solve_ms": ma + mq, "solves_per_s": 1000.0 / (ma + mq),
+                           "assembly_ms_runs": asm_runs, "qr_ms_runs": qr_runs,
                            "rel_err_vs_fp64": err_ref,
                            "note": "reference kernels + cusolver Cgeqrf/Cunmqr/cublasCtrsm, FP32, plain 6x6 "
-                                   "rule for near pairs; timed with its own event spans"}
+                                   "rule for near pairs; timed with its own event spans; median of 3 after "
+                                   "one warm-up"}
                 del Ar, Br
         except Exception as exc:   # reported, not fatal: the reference path is a comparison only
             ref_gpu = {"unavailable": str(exc)[:200]}
@@ -566,34 +626,42 @@ def run_ours(args):
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     peak_src = "of measured" if "hbm_gbs" in peaks else "of fallback"
     per_kernel = {n: {"launches": c, "total_ms": ms, "avg_ms": ms / max(c, 1)} for n, (c, ms) in prof.items()}
-    dom = max(per_kernel, key=lambda n: per_kernel[n]["total_ms"])
+    dev_kernels = [n for n in per_kernel if not n.startswith("host:")]
+    dom = max(dev_kernels, key=lambda n: per_kernel[n]["total_ms"]) if dev_kernels else None
     hbm_kernels = [n for n in per_kernel if kernel_bytes(n, R, N)]
     hbm_dom = max(hbm_kernels, key=lambda n: per_kernel[n]["total_ms"]) if hbm_kernels else None
-    traffic = None
+    traffic_tab = {}
     try:
-        tr = json.load(open(os.path.join(ROOT, "profiles", "ncu_traffic.json")))
-        traffic = tr.get(hbm_dom, {}).get("bytes_per_launch")
+        traffic_tab = json.load(open(os.path.join(ROOT, "profiles", "ncu_traffic.json")))
     except (OSError, ValueError):
         pass
-    roofline = None
+    roofline_hbm = None
     if hbm_dom:
         bpl = kernel_bytes(hbm_dom, R, N)
         ach = bpl / (per_kernel[hbm_dom]["avg_ms"] / 1000.0) / 1e9
-        roofline = {"kernel": hbm_dom, "bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
-                    "frac": ach / hbm_peak, "traffic": traffic, "peak_source": peak_src,
-                    "algorithmic_bytes_per_launch": bpl}
+        roofline_hbm = {"kernel": hbm_dom, "bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
+                        "frac": ach / hbm_peak, "traffic": traffic_tab.get(hbm_dom, {}).get("bytes_per_launch"),
+                        "peak_source": peak_src, "algorithmic_bytes_per_launch": bpl}
     asm = per_kernel.get("far_assembly_f32")
     pairs = R * E
-    far_extra = None
+    roofline = None
     if asm:
-        # 60 FP32 flops + 3 MUFU per quadrature point (36 points per pair)
+        # The dominant kernel: 60 FP32 flops (+ 3 MUFU) per quadrature point,
+        # 36 points per (row, element) pair, counted once whatever the
+        # implementation; bounded by the FP32 pipe.  MEASURED_PEAKS.json holds
+        # no FP32 figure: the peak is the nominal rate of this device's SMs
+        # (queried) at the SM clock sampled during the timed region.
         tflops = 60.0 * 36 * pairs / (asm["avg_ms"] / 1000.0) / 1e12
-        mhz = clk.get("sm_mhz") or 2070.0
-        fp32_peak = 152 * 128 * 2 * mhz * 1e6 / 1e12
-        far_extra = {"kernel": "far_assembly_f32", "bound": "fp32", "achieved": tflops, "unit": "TFLOP/s",
-                     "peak": fp32_peak, "frac": tflops / fp32_peak,
-                     "peak_source": f"nominal 152 SM x 128 FP32 lanes x 2 at the sampled {mhz:.0f} MHz",
-                     "pairs_per_launch": pairs}
+        mhz = clk.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
+        sms = torch.cuda.get_device_properties(dist.local).multi_processor_count
+        fp32_peak = sms * 128 * 2 * mhz * 1e6 / 1e12
+        roofline = {"kernel": "far_assembly_f32", "bound": "fp32", "achieved": tflops, "unit": "TFLOP/s",
+                    "peak": fp32_peak, "frac": tflops / fp32_peak,
+                    "traffic": traffic_tab.get("far_assembly_f32", {}).get("bytes_per_launch"),
+                    "peak_source": f"nominal: {sms} SMs x 128 FP32 lanes x 2 flops at the sampled {mhz:.0f} MHz "
+                                   "(no FP32 figure in MEASURED_PEAKS.json)",
+                    "pairs_per_launch": pairs, "flops_per_pair": 2160,
+                    "algorithmic_bytes_per_launch": 8.0 * R * N}
     it = [i.iterations for i in infos]
     A_bytes = 8.0 * R * N
     B_bytes = 16.0 * R
@@ -611,11 +679,8 @@ def run_ours(args):
         "config": {"workload": name, "sources": S, "nodes": N, "triangles": E, "chief": M,
                    **({"subdiv": args.subdiv, "ka": args.ka} if args.config == "precision" else
                       {"k": k, "solver": "block GMRES: %s GEMMs, FP32 Arnoldi, FP64 Givens, FP64-accurate "
-                                          "refinement residual to 1e-8" % {-1: "auto (CUDA-core streaming up to 8 sources; A <= 4 GB: "
-                                                                "timed choice of CUDA-core streaming or TF32x3 at 9-32, "
-                                                                "TF32x3 to 127, TF32x3 3M from 128)", 0: "FP32",
-                                                            1: "split-BF16", 2: "TF32", 3: "TF32x3",
-                                                            4: "TF32x3 3M", 5: "CUDA-core streaming FP32"}[args.gemm]}),
+                                          "refinement residual to 1e-8" % GEMM_NAMES[args.gemm],
+                       "gemm_used": GEMM_NAMES.get(s.block_gemm_mode(), None)}),
                    "seed": args.seed, "near_eta": args.eta, "near_depth": args.depth,
                    "refine_tol": 1e-8, "parallelism": f"replicas x{dist.world}",
                    "l2": "inputs larger than L2: A (%.0f MB c64) is rewritten every step" % (A_bytes / 1e6)},
@@ -628,7 +693,7 @@ def run_ours(args):
         "fp64_plain": fp64,
         "reference_gpu": ref_gpu,
         "roofline": roofline,
-        "roofline_assembly": far_extra,
+        "roofline_hbm": roofline_hbm,
         "kernels": per_kernel,
         "dominant_kernel": dom,
         "gpu_launches": launches,
@@ -636,8 +701,13 @@ def run_ours(args):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "cpu_baseline": cpu,
     }
+    if dist.rank == 0 and args.config == "precision" and not args.no_extras:
+        del s, s2
+        line["rhs"] = rhs_extra(args)
+        line["serve"] = serve_extra(args)
     if dist.rank == 0:
         print(json.dumps(line), flush=True)
+    dist.barrier()
     dist.close()
     return 0
 
@@ -658,32 +728,25 @@ def _fp64_solve(bem, p, opts):
     return x, time.perf_counter() - t0
 
 
-def run_server_bench(args):
+def server_passes(bem, args, probs, opts, cache, steps, saturated=False, slots=None):
+    """Timed passes of the request server over `probs` (a fresh server per
+    pass: empty cache every time).  Poisson arrivals at each problem's time
+    "t", or all submitted at once when saturated (capacity).  Returns the
+    solves/s, wall time, per-request latencies, the servers' statistics and
+    the last pass's results."""
     import torch
-    import bem_gpu_clean_cpp_gb300 as bem
-
-    dist = Dist(use_cuda=True)
-    torch.cuda.set_device(dist.local)
-    bem.lib()
-    opts = dict(near_eta=args.eta, near_depth=args.depth, tol=1e-8, inner_tol=1e-4, max_iter=args.max_iter,
-                max_refine=10, block_tol=1e-8, gemm_mode=args.gemm)
-    if args.config == "freq":
-        probs, name, cache = freq_problems(args), WORKLOAD_FREQ, 0
-    else:
-        probs, name, cache = serve_requests(args, args.requests), WORKLOAD_SERVE, 16
+    slots = slots or args.slots
 
     def one_pass(srv):
-        """All problems (freq: submitted at once; serve: at their arrival
-        times from a feeder thread); returns the results in order."""
         tickets = [None] * len(probs)
         t0 = time.perf_counter()
 
         def feed():
             for i, p in enumerate(probs):
-                if args.config == "serve":
-                    d = p["t"] - (time.perf_counter() - t0)
-                    if d > 0:
-                        time.sleep(d)
+                if not saturated and "t" in p:
+                    dt = p["t"] - (time.perf_counter() - t0)
+                    if dt > 0:
+                        time.sleep(dt)
                 tickets[i] = srv.submit(p["pnts"], p["elems"], p["k"], p["srcs"], chief=p["chief"])
 
         th = threading.Thread(target=feed)
@@ -697,24 +760,9 @@ def run_server_bench(args):
         return out
 
     solves = sum(len(p["srcs"]) for p in probs)
-    # warm-up: library, handles and kernels on a separate server
-    with bem.Server(slots=args.slots, cache_systems=0, **opts) as w:
-        small = [p for p in probs if p["pnts"].shape[0] <= 2562][:max(3, args.warmup)]
-        for p in small:
-            w.wait(w.submit(p["pnts"], p["elems"], p["k"], p["srcs"], chief=p["chief"]))
-        if args.config == "freq":
-            for _ in range(max(0, args.warmup - 2)):
-                one_pass(w)
-    torch.cuda.synchronize()
-    dev_index = dist.local
-    clocks = Clocks(dev_index)
-    l0 = bem.launch_count()
-    dist.barrier()
-    clocks.start()
     elapsed, lat, stats, last = 0.0, [], [], None
-    for _ in range(args.steps):
-        # a fresh server per step: the same conditions (empty cache) every time
-        with bem.Server(slots=args.slots, cache_systems=cache, **opts) as srv:
+    for _ in range(steps):
+        with bem.Server(slots=slots, cache_systems=cache, **opts) as srv:
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             last = one_pass(srv)
@@ -722,12 +770,25 @@ def run_server_bench(args):
             elapsed += time.perf_counter() - t0
             stats.append(srv.stats())
             lat += [r["latency_ms"] for _, r in last]
-    clk = clocks.stop()
-    launches = bem.launch_count() - l0
-    elapsed = dist.max(elapsed)
-    value = dist.world * args.steps * solves / elapsed
+    return {"solves": solves, "elapsed": elapsed, "value": steps * solves / elapsed, "lat": lat, "stats": stats,
+            "last": last, "one_pass": one_pass}
 
-    # ---- accuracy against the plain FP64 solve, and its one-at-a-time time ----
+
+def server_warmup(bem, args, probs, opts, passes=0):
+    """Library, handles and kernels warmed on a separate server."""
+    import torch
+    with bem.Server(slots=args.slots, cache_systems=0, **opts) as w:
+        small = [p for p in probs if p["pnts"].shape[0] <= 2562][:max(3, args.warmup)]
+        for p in small:
+            w.wait(w.submit(p["pnts"], p["elems"], p["k"], p["srcs"], chief=p["chief"]))
+    if passes:
+        server_passes(bem, args, probs, opts, 0, passes, saturated=True)
+    torch.cuda.synchronize()
+
+
+def server_fp64_check(bem, probs, last, opts):
+    """Every problem up to 10242 nodes (one at 10242) against its plain FP64
+    solve (c128 assembly + Householder QR), and the one-at-a-time FP64 time."""
     errs, fp64_t, worst_cases = [], {}, []
     checked_s5 = 0
     for i, p in enumerate(probs):
@@ -747,14 +808,45 @@ def run_server_bench(args):
     if 10242 in per_n:
         per_n.setdefault(40962, per_n[10242] * (40962 / 10242) ** 3)   # QR cost ~ N^3
     est = sum(per_n.get(p["pnts"].shape[0], 0.0) for p in probs)
-    fp64 = {"checked_problems": len(errs), "max_rel_err_vs_fp64": max(errs) if errs else None,
+    return {"checked_problems": len(errs), "max_rel_err_vs_fp64": max(errs) if errs else None,
             "seconds_by_nodes": {str(k): v for k, v in sorted(per_n.items())},
             "estimated_one_at_a_time_s": est,
-            "solves_per_s": solves / est if est else None,
-            "speedup_vs_fp64_plain": value / (solves / est) if est else None,
             "largest_errors": sorted(worst_cases, key=lambda c: -c["rel_err"])[:5],
             "note": "plain FP64 = c128 assembly + Householder QR per problem, timed for every problem up to "
                     "10242 nodes (one at 10242), 40962-node problems extrapolated by N^3 from 10242"}
+
+
+def run_server_bench(args):
+    import torch
+    import bem_gpu_clean_cpp_gb300 as bem
+
+    dist = Dist(use_cuda=True)
+    torch.cuda.set_device(dist.local)
+    bem.lib()
+    opts = dict(near_eta=args.eta, near_depth=args.depth, tol=1e-8, inner_tol=1e-4, max_iter=args.max_iter,
+                max_refine=10, block_tol=1e-8, gemm_mode=args.gemm)
+    if args.config == "freq":
+        probs, name, cache = freq_problems(args), WORKLOAD_FREQ, 0
+    else:
+        probs, name, cache = serve_requests(args, args.requests), WORKLOAD_SERVE, 16
+    server_warmup(bem, args, probs, opts, passes=max(0, args.warmup - 2) if args.config == "freq" else 0)
+    dev_index = dist.local
+    clocks = Clocks(dev_index)
+    l0 = bem.launch_count()
+    dist.barrier()
+    clocks.start()
+    res = server_passes(bem, args, probs, opts, cache, args.steps, saturated=args.config == "freq")
+    clk = clocks.stop()
+    launches = bem.launch_count() - l0
+    elapsed = dist.max(res["elapsed"])
+    solves, lat, stats, last = res["solves"], res["lat"], res["stats"], res["last"]
+    value = dist.world * args.steps * solves / elapsed
+
+    # ---- accuracy against the plain FP64 solve, and its one-at-a-time time ----
+    fp64 = server_fp64_check(bem, probs, last, opts)
+    est = fp64["estimated_one_at_a_time_s"]
+    fp64["solves_per_s"] = solves / est if est else None
+    fp64["speedup_vs_fp64_plain"] = value / (solves / est) if est else None
     sizes = sorted({p["pnts"].shape[0] for p in probs})
     by_sub = {}
     for p, (_, r) in zip(probs, last):
@@ -795,6 +887,118 @@ def run_server_bench(args):
     return 0
 
 
+# ---------------------------------------------------------------------------
+# The batching configurations inside the default line (secondary objects)
+# ---------------------------------------------------------------------------
+GEMM_NAMES = {-1: "auto", 0: "FP32 (cuBLAS)", 1: "split-BF16 (cuBLAS)", 2: "TF32 (cuBLAS)", 3: "TF32x3 (cuBLAS)",
+              4: "TF32x3 3M (cuBLAS)", 5: "CUDA-core streaming FP32", 6: "tcgen05 fp16 split (this library)"}
+
+
+def rhs_extra(args):
+    """Config 3 at full size: 256 point sources on the perturbed ellipsoid
+    (15212 nodes), all solved together by block GMRES with the default (AUTO)
+    products.  One warm-up step, then 3 timed steps (assembly + block solve,
+    CUDA events on the solver's stream, median); per-source max error against
+    the plain FP64 solve (c128 assembly + Householder QR) of the same system."""
+    import torch
+    import bem_gpu_clean_cpp_gb300 as bem
+    a = argparse.Namespace(**vars(args))
+    a.config, a.sources = "rhs", 256
+    pts, elems, chief, srcs, k, bc = workload_rhs(a)
+    N, E, M, S = pts.shape[0], elems.shape[0], chief.shape[0], len(srcs)
+    R = N + M
+    s = bem.Solver(near_eta=args.eta, near_depth=args.depth, tol=1e-8, inner_tol=1e-4, max_iter=100,
+                   max_refine=10, block_tol=1e-8, gemm_mode=-1)
+    s.set_geometry(pts, elems, bc=bc, chief=chief)
+    s.set_sources(srcs)
+    st = torch.cuda.ExternalStream(s.stream())
+    s.assemble(k, bem.PREC_C64)
+    s.solve(bem.SOLVE_BLOCK_GMRES)
+    s.sync()
+    bem.profile_enable(True)
+    runs, infos = [], []
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        s.assemble(k, bem.PREC_C64)
+        infos.append(s.solve(bem.SOLVE_BLOCK_GMRES))
+        e1.record(st)
+        s.sync()
+        runs.append(e0.elapsed_time(e1))
+    prof = bem.profile_report()
+    bem.profile_enable(False)
+    mode = s.block_gemm_mode()
+    x = s.solution()
+    s.assemble(k, bem.PREC_C128)
+    s.solve(bem.SOLVE_QR)
+    x64 = s.solution()
+    err = max(float(np.abs(x[:, j] - x64[:, j]).max() / np.abs(x64[:, j]).max()) for j in range(S))
+    del s
+    ms = statistics.median(runs)
+    prods = {}
+    for name in ("gemm_AV", "gemm_AhT"):
+        if name in prof:
+            c, t = prof[name]
+            prods[name] = {"launches": c, "avg_ms": t / max(c, 1)}
+    tensor = None
+    if mode == 6 and "gemm_AV" in prods and "gemm_AhT" in prods:
+        # complex product counted as 8 R N S flops (whatever the method); the
+        # fp16 split runs 3 tensor products per real product of the
+        # interleaved form (24 R N S fp16 flops on the tensor pipe)
+        peaks = {}
+        try:
+            peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        except (OSError, ValueError):
+            pass
+        pk = peaks.get("bf16_tflops", 1900.0)
+        avg = 0.5 * (prods["gemm_AV"]["avg_ms"] + prods["gemm_AhT"]["avg_ms"])
+        alg = 8.0 * R * N * S / (avg / 1000.0) / 1e12
+        tensor = {"kernel": "tc_gemm_kernel", "bound": "tensor", "unit": "TFLOP/s",
+                  "achieved_algorithmic": alg, "achieved_tensor_pipe": 3 * alg, "peak": pk,
+                  "frac": 3 * alg / pk,
+                  "peak_source": ("of measured" if "bf16_tflops" in peaks else "of fallback") +
+                                 " dense bf16 (fp16 runs at the same rate)",
+                  "note": "per product including its operand packing; 8 R N S algorithmic flops, 3x that on the "
+                          "tensor pipe (hh + hl + lh fp16 products)"}
+    return {"workload": WORKLOAD_RHS, "nodes": N, "triangles": E, "chief": M, "sources": S, "k": k,
+            "gemm_mode": GEMM_NAMES.get(mode, mode), "ms_per_step": ms, "ms_runs": runs,
+            "solves_per_s": S * 1000.0 / ms,
+            "iterations": [i.iterations for i in infos], "refinements": [i.refinements for i in infos],
+            "max_rel_err_vs_fp64": err, "products": prods, "roofline_products": tensor,
+            "timing": "assembly + block solve per step, median of 3 after one warm-up step"}
+
+
+def serve_extra(args):
+    """Config 5 inside the default line: the seeded stream of 40 requests
+    (1-64 sources, subdivision 3-6) through the request server with 8 slots,
+    once at the Poisson arrival rate (2/s) and once saturated (all submitted
+    at t = 0: the server's capacity), then every request up to 10242 nodes
+    (one at 10242) checked against its plain FP64 solve."""
+    import bem_gpu_clean_cpp_gb300 as bem
+    a = argparse.Namespace(**vars(args))
+    a.config, a.requests, a.rate, a.slots, a.max_iter, a.gemm = "serve", 40, 2.0, 8, 100, -1
+    probs = serve_requests(a, a.requests)
+    opts = dict(near_eta=args.eta, near_depth=args.depth, tol=1e-8, inner_tol=1e-4, max_iter=a.max_iter,
+                max_refine=10, block_tol=1e-8, gemm_mode=-1)
+    server_warmup(bem, a, probs, opts)
+    out = {"workload": WORKLOAD_SERVE, "requests": len(probs), "slots": a.slots,
+           "solves": sum(len(p["srcs"]) for p in probs)}
+    last = None
+    for key, sat in (("poisson", False), ("saturated", True)):
+        r = server_passes(bem, a, probs, opts, 16, 1, saturated=sat)
+        out[key] = {"solves_per_s": r["value"], "wall_s": r["elapsed"],
+                    "p50_ms": float(np.percentile(r["lat"], 50)), "p99_ms": float(np.percentile(r["lat"], 99)),
+                    "max_in_flight": r["stats"][-1].get("max_in_flight")}
+        if not sat:
+            out[key]["rate_per_s"] = a.rate
+            last = r["last"]
+    chk = server_fp64_check(bem, probs, last, opts)
+    out["max_rel_err_vs_fp64"] = chk["max_rel_err_vs_fp64"]
+    out["checked_problems"] = chk["checked_problems"]
+    out["largest_errors"] = chk["largest_errors"][:3]
+    return out
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
@@ -807,6 +1011,8 @@ def main():
         return run_server_bench(args)
     if args.mode == "profile":
         return run_profile(args)
+    if args.mode == "cpu-validate":
+        return run_cpu_validate(args)
     return run_ours(args)
 
 

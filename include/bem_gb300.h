@@ -159,13 +159,31 @@ int bem_gmres_c64(const float *A, const float *b, int m, int max_iter, float thr
  * All scratch lives in one static device array of about 5.4 MiB that every
  * GPU loading the library keeps until exit, which limits m to
  * BEM_NOALLOC_MAX_M and min(max_iter, m) to BEM_NOALLOC_MAX_ITER; larger
- * sizes return BEM_ERR_TOO_LARGE.  The first call on a device looks up the
- * array's device address (make that first call before any stream capture).
- * Calls share the array: calls that overlap on the GPU race. */
+ * sizes return BEM_ERR_TOO_LARGE.  The first call on a device, and the first
+ * after the device's context was re-created (cudaDeviceReset), looks up the
+ * array's device address: make that call before any stream capture.  Each
+ * iteration reads an 8-byte residual estimate and synchronises `stream`: a
+ * caller that solves while another component's stream capture runs passes a
+ * stream created with cudaStreamNonBlocking, not NULL (work on the legacy
+ * NULL stream synchronises with blocking streams, which would break that
+ * capture).  Calls share the array: calls that overlap on the GPU race. */
 #define BEM_NOALLOC_MAX_M 2048
 #define BEM_NOALLOC_MAX_ITER 128
 int bem_gmres_c64_noalloc(const float *A_dev, int lda, const float *b_dev, int m, int max_iter,
                           float thr, float *x_dev, void *stream, int *iters);
+/* Dense real product C = op(A) B on the tcgen05 tensor cores: the kernel
+ * the block solve's multi-right-hand-side products (which replace the
+ * Cgemm/Cgemv products of numerical.cu:375-396 and GMRES.cu:90-143) and the
+ * QR trailing updates run on.  A is row-major with row stride lda (a
+ * multiple of 4): trans = 0: op(A) = A (m x k); trans = 1: op(A) = A^T with A
+ * stored k x m.  B is k x n and C m x n, column-major (ldb, ldc).  parts = 2:
+ * fp16 head + tail split products, about 2^-22 relative to sum |a||b| (the
+ * accuracy of TF32x3); parts = 3: head + middle + tail, only the tensor
+ * core's FP32 accumulation left (errors of order sqrt(k) 2^-24 relative to
+ * sum |a||b|).  Host buffers; device memory is allocated and freed inside
+ * the call. */
+int bem_tc_gemm_f32(int trans, int m, int k, int n, const float *A, int lda, const float *B, int ldb, float *C,
+                    int ldc, int parts);
 /* genExtPressure (mesh.h:425-426, mesh.cu:1038-1073): pressure at x from
  * the surface pressure surf_p (numPnts c64 values). */
 int bem_ext_pressure_c64(float k, bem_mesh_t m, const float *src, const float *x,
@@ -189,29 +207,29 @@ typedef struct {
 } bem_source_t;
 
 enum { BEM_PREC_C64 = 0, BEM_PREC_C128 = 1 };
-enum { BEM_SOLVE_QR = 0, BEM_SOLVE_GMRES_REFINED = 1, BEM_SOLVE_BLOCK_GMRES = 2 };
-/* Block-solve GEMMs (the products inside the inner GMRES): FP32 (SIMT),
- * FP32-accurate split-BF16 emulation on the tensor cores (cuBLAS), plain
- * TF32, TF32x3 on the interleaved-real form of the complex product (A and the
- * right-hand block split into TF32 head + tail; each product is
- * head(A) [head(B) | tail(B)] plus tail(A) head(B): two passes over A's
- * planes), or TF32x3 in the 3M form (separate planes of Re A, Im A,
- * Re A + Im A: three real products per complex product, a quarter fewer
- * flops, the same passes).  The once-per-cycle refinement products (the
- * residual update R -= A D and the gradient A^H R) run FP32-accurate
- * (split-BF16, or FP32 in FP32 mode) in every mode.
+enum { BEM_SOLVE_QR = 0, BEM_SOLVE_GMRES_REFINED = 1, BEM_SOLVE_BLOCK_GMRES = 2, BEM_SOLVE_QR_TC = 3 };
+/* Block-solve GEMMs (the products inside the inner GMRES).
+ * BEM_GEMM_TC (the default's choice from 9 sources on): this library's own
+ * tcgen05 tensor-core kernel (bem_tc_gemm_f32) on the interleaved-real form
+ * of the complex products, reading the c64 matrix directly (no split copies
+ * of A): fp16 head + tail split products (TF32x3-level accuracy) inside the
+ * inner GMRES, head + middle + tail (FP32-accurate) for the once-per-cycle
+ * refinement products (the residual update R -= A D and the gradient
+ * A^H R).
  * BEM_GEMM_SIMT: FP32 products on the CUDA cores by this library's own
  * streaming kernels (one pass over A per product for up to 32 right-hand
  * sides, more in further passes; no extra copies of A; the refinement
  * products FP32 as well).
- * AUTO: SIMT up to 8 right-hand sides.  While the c64 matrix is at most
- * 4 GB: from 9 to 32 the faster of SIMT and interleaved TF32x3 for the shape
- * (timed on the first solve of each shape, kept for the process), TF32x3 up
- * to 127, the 3M form from 128.  Above 4 GB the planes' memory would cost
- * concurrent requests more than the products gain: split-BF16 from 32, FP32
- * from 9 to 31. */
+ * Library (cuBLAS) modes, kept for comparison: FP32, FP32-accurate
+ * split-BF16 emulation, plain TF32, TF32x3 on the interleaved-real form (A
+ * and the right-hand block split into TF32 head + tail planes), or TF32x3 in
+ * the 3M form (planes of Re A, Im A, Re A + Im A); their refinement products
+ * run split-BF16 (FP32 in FP32 mode).
+ * AUTO: up to 8 right-hand sides the faster of SIMT and TC for the shape
+ * (timed on the first solve of each shape, kept for the process), TC from
+ * 9 on. */
 enum { BEM_GEMM_AUTO = -1, BEM_GEMM_FP32 = 0, BEM_GEMM_SPLIT_BF16 = 1, BEM_GEMM_TF32 = 2, BEM_GEMM_TF32X3 = 3,
-       BEM_GEMM_TF32X3_3M = 4, BEM_GEMM_SIMT = 5 };
+       BEM_GEMM_TF32X3_3M = 4, BEM_GEMM_SIMT = 5, BEM_GEMM_TC = 6 };
 
 typedef struct {
     double density;     /* 1.2041 (numerical.cu:12) */
@@ -259,7 +277,17 @@ int bem_solver_assemble(bem_solver_t s, double k, int precision);
  * together; the normal-operator products for every source are GEMMs on the
  * tensor cores (gemm_mode), each source keeps its own FP32 Krylov space
  * with FP64 Hessenberg/Givens, outer refinement to block_tol (requires a c64
- * assembly). */
+ * assembly).
+ * BEM_SOLVE_QR_TC (either assembly precision): least squares by this
+ * library's blocked Householder QR (the WY blocked QR_thin / lsqSolver of
+ * numerical.cu:246-554 and the qrSolver sequence of numerical.cu:580-644):
+ * panels of 128 columns factored in FP32 by one thread-block cluster each,
+ * trailing updates (I - V T V^H)^H C as tensor-core GEMMs (the kernel of
+ * bem_tc_gemm_f32), Q applied to B on the way and never formed, then FP64
+ * refinement through the semi-normal equations with the FP32 factor (FP64-
+ * accurate residuals of the assembled matrix) to a relative normal-equation
+ * residual of 1e-14 or until it stagnates; info->refinements = refinement
+ * steps, info->rel_residual = the residual reached. */
 int bem_solver_solve(bem_solver_t s, int method, bem_solve_info_t *info);
 /* Copy results to host buffers in the given precision (BEM_PREC_*). */
 int bem_solver_get_solution(bem_solver_t s, void *x, int ldx, int precision);
@@ -272,6 +300,10 @@ int bem_solver_sync(bem_solver_t s);
 /* The cudaStream_t all work of the handle is queued on. */
 void *bem_solver_stream(bem_solver_t s);
 int bem_solver_sizes(bem_solver_t s, int *n, int *m, int *num_elems, int *num_srcs);
+/* The BEM_GEMM_* mode the handle's last BEM_SOLVE_BLOCK_GMRES ran its
+ * products in (AUTO's choice), or BEM_GEMM_AUTO before any block solve (no
+ * reference counterpart). */
+int bem_solver_block_gemm_mode(bem_solver_t s, int *mode);
 
 /* ------------------------------------------------------------------ */
 /* Request server (no reference counterpart: the reference solves one   */

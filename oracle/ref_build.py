@@ -10,6 +10,14 @@ infrastructure).
   holds declarations only, and no host code of the reference is compiled.
 * libref_harness.so -- oracle/ref_harness.cpp (the launcher), built wherever
   the CUDA toolkit is.
+* meshes/ -- the reference's own head and torso meshes (Head_20kHz_iso.obj,
+  Head_20kHz_iso.ply, KEMARTORSO_12000Hz.obj), staged beside the cubin so
+  that the GPU tests of realistic workloads can read them where the reference
+  checkout is absent.  They are the reference's data: never committed.
+
+The reference checkout is named by the environment variable BEM_REFERENCE_DIR;
+without it nothing is taken from the reference and what oracle/_ref already
+holds is used.
 """
 from __future__ import annotations
 
@@ -21,7 +29,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
 CUBIN = os.path.join(OUT, "ref_kernels.cubin")
 HARNESS = os.path.join(OUT, "libref_harness.so")
-REF_DIR = os.environ.get("BEM_REFERENCE_DIR", "/root/reference")
+REF_DIR = os.environ.get("BEM_REFERENCE_DIR", "")
+MESH_DIR = os.path.join(OUT, "meshes")
+MESHES = ("Head_20kHz_iso.obj", "Head_20kHz_iso.ply", "KEMARTORSO_12000Hz.obj")
 
 
 def _cuda() -> str:
@@ -31,7 +41,7 @@ def _cuda() -> str:
 def build_cubin(force: bool = False) -> bool:
     """Compile the reference kernels when the reference sources are present."""
     srcs = [os.path.join(REF_DIR, f) for f in ("numerical.cu", "mesh.cu", "atomicFuncs.cu")]
-    if not all(os.path.exists(s) for s in srcs):
+    if not REF_DIR or not all(os.path.exists(s) for s in srcs):
         return os.path.exists(CUBIN)
     if not force and os.path.exists(CUBIN) and all(os.path.getmtime(CUBIN) > os.path.getmtime(s) for s in srcs):
         return True
@@ -63,10 +73,23 @@ def build_harness(force: bool = False) -> str:
     return HARNESS
 
 
+def stage_meshes() -> list:
+    """Copies the reference's head and torso meshes into oracle/_ref/meshes
+    when the checkout is named; returns the staged paths that exist."""
+    if REF_DIR:
+        os.makedirs(MESH_DIR, exist_ok=True)
+        for f in MESHES:
+            src, dst = os.path.join(REF_DIR, f), os.path.join(MESH_DIR, f)
+            if os.path.exists(src) and not (os.path.exists(dst) and os.path.getmtime(dst) >= os.path.getmtime(src)):
+                shutil.copyfile(src, dst)
+    return [os.path.join(MESH_DIR, f) for f in MESHES if os.path.exists(os.path.join(MESH_DIR, f))]
+
+
 def build_if_possible() -> bool:
-    """Harness always; cubin when the reference sources are here.  True when
-    both exist afterwards."""
+    """Harness always; cubin and staged meshes when the reference checkout is
+    named.  True when cubin and harness exist afterwards."""
     have_cubin = build_cubin()
+    stage_meshes()
     build_harness()
     return have_cubin and os.path.exists(HARNESS)
 

@@ -20,7 +20,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("BEM_REFERENCE_DIR", "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("BEM_REFERENCE_DIR", "")
+    if not ref:
+        sys.exit("name the reference checkout: make_golden.py <dir> or BEM_REFERENCE_DIR=<dir>")
     for f in ["sphere.obj", "test.obj", "cube.obj", "sphere171Hz_CHIEF", "sphere171Hz_NoCHIEF"]:
         shutil.copyfile(os.path.join(ref, f), os.path.join(HERE, f))
     cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")

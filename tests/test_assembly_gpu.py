@@ -132,16 +132,41 @@ def test_multi_tile_assembly(bemlib, orc, prec):
     assert rel_err(A, Ao) < tol and rel_err(B, Bo) < tol
 
 
-def test_assembly_repeatable(bemlib):
+@pytest.mark.parametrize("tile_cols", [0, 100])
+def test_assembly_bitwise_repeatable(bemlib, tile_cols):
+    """The far kernels add each column's terms in one fixed order (records in
+    node-disjoint batches, plain shared-memory adds, a CTA barrier between
+    batches; no atomics), so repeated assemblies give the same bits: c64 with
+    every launch shape of the far kernel, and c128, with one column tile and
+    with several (tile_cols = 100 on 162 nodes).  The off-diagonal entries
+    are also bitwise the same across launch shapes; only the diagonal's c sum
+    and B's beta sum follow the shape's reduction tree."""
     p, f, chief = _problem("ico2")
-    s = bemlib.Solver()
+    n = p.shape[0]
+    ref_off = None
+    for v in range(6):
+        s = bemlib.Solver(far_variant=v, tile_cols=tile_cols)
+        s.set_geometry(p, f, chief=chief)
+        s.set_sources(SRCS)
+        s.assemble(2.0, bemlib.PREC_C64)
+        A1, B1 = s.system(bemlib.PREC_C64)
+        s.assemble(2.0, bemlib.PREC_C64)
+        A2, B2 = s.system(bemlib.PREC_C64)
+        assert np.array_equal(A1, A2) and np.array_equal(B1, B2), v
+        off = A1.copy()
+        off[np.arange(n), np.arange(n)] = 0
+        if ref_off is None:
+            ref_off = off
+        else:
+            assert np.array_equal(off, ref_off), v
+    s = bemlib.Solver(tile_cols=tile_cols)
     s.set_geometry(p, f, chief=chief)
     s.set_sources(SRCS)
-    s.assemble(2.0, bemlib.PREC_C64)
-    A1, B1 = s.system(bemlib.PREC_C64)
-    s.assemble(2.0, bemlib.PREC_C64)
-    A2, B2 = s.system(bemlib.PREC_C64)
-    assert rel_err(A1, A2) < 1e-6 and rel_err(B1, B2) < 1e-12
+    s.assemble(2.0, bemlib.PREC_C128)
+    A1, B1 = s.system(bemlib.PREC_C128)
+    s.assemble(2.0, bemlib.PREC_C128)
+    A2, B2 = s.system(bemlib.PREC_C128)
+    assert np.array_equal(A1, A2) and np.array_equal(B1, B2)
 
 
 def test_errors_are_status_codes(bemlib):
@@ -200,6 +225,27 @@ def test_c64_phase_modes_match_oracle(bemlib, orc, radius, k, mode):
     edge = max(np.linalg.norm(p[f[:, a]] - p[f[:, b]], axis=1).max() for a, b in ((0, 1), (1, 2), (2, 0)))
     extent = np.linalg.norm(np.ptp(np.vstack([p, chief]), axis=0))
     assert k * edge > 0.75 and ((k * extent > 40 or k * edge > 1.2) == (mode == "split"))
+    s = bemlib.Solver()
+    s.set_geometry(p, f, chief=chief)
+    s.set_sources(SRCS)
+    s.assemble(k, bemlib.PREC_C64)
+    A, B = s.system(bemlib.PREC_C128)
+    Ao, Bo = orc.assemble(np.vstack([p, chief]), f, k, p.shape[0], SRCS)
+    assert rel_err(A, Ao) < TOL32
+    assert rel_err(B, Bo) < TOL32
+
+
+def test_c64_assembly_high_aspect_elements(bemlib, orc):
+    """Obtuse, high-aspect-ratio elements (an icosphere stretched 8:1, aspect
+    ratios up to about 10): the far kernel's line coefficients of r^2 lose
+    precision there (a cancellation of about (|e1| / h)^2 ulps in |v|^2), yet
+    the c64 matrix stays within the c64 tolerance of the FP64 oracle."""
+    p, f = icosphere(2, 1.0)
+    p = p * np.array([0.25, 0.25, 2.0])
+    chief = np.array([[0.05, 0.0, 0.9], [-0.05, 0.02, -1.1]])
+    e = np.stack([np.linalg.norm(p[f[:, a]] - p[f[:, b]], axis=1) for a, b in ((0, 1), (1, 2), (2, 0))], axis=1)
+    assert (e.max(axis=1) / e.min(axis=1)).max() > 6.0
+    k = 2.0
     s = bemlib.Solver()
     s.set_geometry(p, f, chief=chief)
     s.set_sources(SRCS)

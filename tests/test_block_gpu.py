@@ -26,7 +26,7 @@ def _ellipsoid_problem(bemlib, nu=8, nsrc=16, f_hz=4000.0, seed=3):
     return p, e, chief, srcs, bc, k
 
 
-@pytest.mark.parametrize("gemm_mode", [-1, 0, 1, 3, 4, 5])
+@pytest.mark.parametrize("gemm_mode", [-1, 0, 1, 3, 4, 5, 6])
 def test_block_gmres_matches_fp64(bemlib, gemm_mode):
     p, e, chief, srcs, bc, k = _ellipsoid_problem(bemlib)
     s = bemlib.Solver(gemm_mode=gemm_mode, block_tol=1e-8)
@@ -62,7 +62,7 @@ def test_block_gmres_tf32_mode_runs(bemlib):
     assert info.rel_residual < 1e-2
 
 
-@pytest.mark.parametrize("gemm_mode", [-1, 4, 5])
+@pytest.mark.parametrize("gemm_mode", [-1, 4, 5, 6])
 def test_block_gmres_odd_node_count(bemlib, gemm_mode):
     """3005 nodes (odd: the interleaved and 3M TF32x3 planes and right-hand
     blocks have odd leading dimensions), 5 point sources; AUTO takes the

@@ -63,3 +63,64 @@ def test_head_like_pipeline(bemlib, tmp_path):
     bemlib.wrtCplxMat(fld.astype(np.complex64), out)
     back = read_cplx_file(out).reshape(fld.shape)                      # one line per row
     assert np.abs(back - fld).max() < 1e-6 + 1e-6 * np.abs(fld).max()
+
+
+def _staged_mesh(name):
+    import os
+    path = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle", "_ref", "meshes",
+                        name)
+    if not os.path.exists(path):
+        pytest.skip("the reference's meshes are staged under oracle/_ref/meshes by oracle/ref_build.py "
+                    "(BEM_REFERENCE_DIR names the reference checkout)")
+    return path
+
+
+@pytest.mark.parametrize("name,f_hz,fp64", [("KEMARTORSO_12000Hz.obj", 12000.0, True),
+                                            ("Head_20kHz_iso.obj", 20000.0, False),
+                                            ("Head_20kHz_iso.ply", 20000.0, False)])
+def test_reference_head_and_torso_meshes(bemlib, name, f_hz, fp64):
+    """The reference's own realistic meshes at their design frequencies: the
+    KEMAR torso (14286 nodes, 28518 triangles) at 12 kHz and the isotropic
+    head (24302 nodes, 48600 triangles) at 20 kHz, read by the reference's
+    OBJ rules (and the head from its binary PLY, whose outward winding is
+    repaired), 8 CHIEF points from genCHIEF, 16 point sources on a 1 m sphere
+    solved together by block GMRES to a normal-equation residual of 1e-10.
+    Every source solved alone by the refined single-right-hand-side solver
+    (same residual) agrees with the block solution to 1e-5;
+    for the torso both are also checked against the plain FP64 solve (c128
+    assembly + Householder QR)."""
+    path = _staged_mesh(name)
+    m = bemlib.Mesh()
+    if name.endswith(".ply"):
+        m.read_ply(path)
+    else:
+        m.readObj(path)
+    rep = m.orient()
+    assert rep["components"] == 1 and rep["open_edges"] == 0 and rep["nonmanifold"] == 0
+    assert rep["flipped"] == (m.elems().shape[0] if name.endswith(".ply") else 0)
+    m.findBB(0.0001)
+    m.genCHIEF(8, 0.01)
+    assert m.chief().shape[0] == 8
+    m.set_uniform_bc(0, 1, 0)
+    k = 2 * np.pi * f_hz / 343.21
+    srcs = [("point", s, 1.0) for s in bemlib.fibonacci_sphere(16, 1.0)]
+    # normal-equation residuals of 1e-10: at these frequencies the systems'
+    # conditioning turns a 1e-8 residual into solution differences above 1e-5
+    s = bemlib.Solver(near_eta=1.0, near_depth=2, max_iter=300, tol=1e-10, block_tol=1e-10)
+    s.set_mesh(m)
+    s.set_sources(srcs)
+    s.assemble(k, bemlib.PREC_C64)
+    info = s.solve(bemlib.SOLVE_BLOCK_GMRES)
+    assert info.converged and info.rel_residual <= 1e-10
+    xb = s.solution()
+    info = s.solve(bemlib.SOLVE_GMRES_REFINED)
+    assert info.converged
+    xr = s.solution()
+    for j in range(xb.shape[1]):
+        assert rel_err(xb[:, j], xr[:, j]) < 1e-5, j
+    if fp64:
+        s.assemble(k, bemlib.PREC_C128)
+        s.solve(bemlib.SOLVE_QR)
+        x64 = s.solution()
+        for j in range(xb.shape[1]):
+            assert rel_err(xb[:, j], x64[:, j]) < 1e-5, j

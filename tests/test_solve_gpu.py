@@ -318,6 +318,70 @@ def test_normal_op_wait_timeout_reported(bemlib):
     assert line[2] == "1" and float(line[3]) < 1e-5, line
 
 
+_STALL_CONCURRENT_SCRIPT = r"""
+import sys, threading, time
+import numpy as np
+sys.path.insert(0, sys.argv[1])
+import bem_gpu_clean_cpp_gb300 as bem
+def problem(seed, subdiv):
+    m = bem.Mesh.icosphere(subdiv, 1.0)
+    p, e = m.points(), m.elems()
+    bc = np.tile(np.array([0, 1, 0], dtype=np.complex128), (e.shape[0], 1))
+    chief = np.random.default_rng(seed).uniform(-0.3, 0.3, (8, 3))
+    s = bem.Solver(near_eta=1.0, near_depth=2)
+    s.set_geometry(p, e, bc=bc, chief=chief)
+    s.set_sources([("plane", np.array([0.0, 0.6, 0.8]), 1.0)])
+    s.assemble(1.5, bem.PREC_C128)
+    s.solve(bem.SOLVE_QR)
+    x64 = s.solution()
+    s.assemble(1.5, bem.PREC_C64)
+    s.sync()
+    return s, x64
+a, xa = problem(3, 3)
+b, xb = problem(4, 4)
+res = {}
+def run_a():
+    try:
+        a.solve(bem.SOLVE_GMRES_REFINED)
+        res["a"] = 0
+    except bem.BemError as err:
+        res["a"] = err.status
+t = threading.Thread(target=run_a)
+t.start()                # a's first normal-operator launch is the stalled one
+time.sleep(0.3)
+status_b = 0
+try:
+    info_b = b.solve(bem.SOLVE_GMRES_REFINED)   # runs while a's launch waits out
+except bem.BemError as err:
+    status_b = err.status
+t.join()
+err_b = np.linalg.norm(b.solution() - xb) / np.linalg.norm(xb) if status_b == 0 else 1.0
+info_a = a.solve(bem.SOLVE_GMRES_REFINED)
+err_a = np.linalg.norm(a.solution() - xa) / np.linalg.norm(xa)
+print("RESULT", res["a"], status_b, err_b, int(info_a.converged), err_a)
+"""
+
+
+def test_normal_op_timeout_reported_to_its_own_solver(bemlib):
+    """The timeout status is per solver: while one solver's stalled launch
+    waits out (BEM_TEST_NORMAL_OP_STALL=1, as above), a second solver in
+    another thread solves its own system.  Only the stalled solver reports
+    BEM_ERR_TIMEOUT; the other converges to its FP64 answer, and the stalled
+    one converges on its next solve."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, BEM_TEST_NORMAL_OP_STALL="1")
+    out = subprocess.run([sys.executable, "-c", _STALL_CONCURRENT_SCRIPT, root], env=env, capture_output=True,
+                         text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = [ln for ln in out.stdout.splitlines() if ln.startswith("RESULT")][-1].split()
+    assert int(line[1]) == bemlib.ERR_TIMEOUT, line
+    assert int(line[2]) == 0 and float(line[3]) < 1e-5, line
+    assert line[4] == "1" and float(line[5]) < 1e-5, line
+
+
 @pytest.mark.parametrize("mesh", ["geodesic50", "icosphere6"])
 def test_normal_op_large_clusters(bemlib, mesh):
     """The fused normal operator with five- and eight-CTA clusters (25002 and
