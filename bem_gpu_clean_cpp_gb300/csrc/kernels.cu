@@ -870,12 +870,14 @@ constexpr int kFarNT64 = 256;
 //   0: 2 rows x 512 threads, 1 CTA/SM     1: 2 rows x 1024 threads, 1 CTA/SM
 //   2: 1 row  x 512 threads, 2 CTAs/SM    3: 4 rows x 1024 threads, 1 CTA/SM
 //   4: 1 row  x 384 threads, 2 CTAs/SM    5: 1 row  x 256 threads, 3 CTAs/SM
-// (4 and 5 trade occupancy for up to 80 registers per thread, no spills).
+//   6: 1 row  x 256 threads, 2 CTAs/SM
+// (4 and 5 trade occupancy for up to 80 registers per thread, 6 for up to 128:
+// no spills).
 struct FarShape {
     int tr, nt;
 };
-constexpr FarShape kFarShapes[] = {{2, 512}, {2, 1024}, {1, 512}, {4, 1024}, {1, 384}, {1, 256}};
-constexpr int kNumFarShapes = 6;
+constexpr FarShape kFarShapes[] = {{2, 512}, {2, 1024}, {1, 512}, {4, 1024}, {1, 384}, {1, 256}, {1, 256}};
+constexpr int kNumFarShapes = 7;
 
 int far_variants(int prec) { return prec == BEM_PREC_C64 ? kNumFarShapes : 1; }
 
@@ -966,7 +968,8 @@ void launch_far_assembly(int prec, const RowPoints &rows, int N, const GeoTables
             case 2: launch_far_f32<1, 512, 2>(rows, N, geo, tiles, ph, A, lda, c_part, beta_part, smem, st); break;
             case 3: launch_far_f32<4, 1024, 1>(rows, N, geo, tiles, ph, A, lda, c_part, beta_part, smem, st); break;
             case 4: launch_far_f32<1, 384, 2>(rows, N, geo, tiles, ph, A, lda, c_part, beta_part, smem, st); break;
-            default: launch_far_f32<1, 256, 3>(rows, N, geo, tiles, ph, A, lda, c_part, beta_part, smem, st); break;
+            case 5: launch_far_f32<1, 256, 3>(rows, N, geo, tiles, ph, A, lda, c_part, beta_part, smem, st); break;
+            default: launch_far_f32<1, 256, 2>(rows, N, geo, tiles, ph, A, lda, c_part, beta_part, smem, st); break;
         }
     } else {
         auto kern = far_assembly_f64<kFarNT64>;

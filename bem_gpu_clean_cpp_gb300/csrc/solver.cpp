@@ -647,9 +647,15 @@ size_t bem_solver_s::estimate_bytes(int N, int E, int M, int S, int method, cons
             if (gm == BEM_GEMM_TF32X3) extra = std::max(extra, 16 * lda * r + 48 * n * s + 16 * r * s);
             if (gm == BEM_GEMM_TF32X3_3M) extra = std::max(extra, 24 * lda * r + 48 * std::max(n, r) * s);
             if (gm == BEM_GEMM_SIMT) extra = std::max(extra, 4 * block_simt_scratch_floats((int)r, N, S));
-            if (gm == BEM_GEMM_TC)
-                extra = std::max(extra, tc_operand_bytes((int)std::max(2 * n, r), 2 * S, 3) +
-                                            4 * tc_gemm_part_floats_bound((int)std::max(2 * n, r), 2 * S) + 64);
+            if (gm == BEM_GEMM_TC) {
+                // the packed right-hand operand and the split-K partial sums of
+                // the four products as the launch plans them on this device
+                size_t pf = 0;
+                for (const int P : {2, 3})
+                    pf = std::max({pf, tc_gemm_part_floats((int)r, 2 * N, 2 * S, P),
+                                   tc_gemm_part_floats(2 * N, (int)r, 2 * S, P)});
+                extra = std::max(extra, tc_operand_bytes((int)std::max(2 * n, r), 2 * S, 3) + 4 * pf + 64);
+            }
         }
         b += extra;
     } else if (method == BEM_SOLVE_GMRES_REFINED) {

@@ -275,9 +275,32 @@ tc_gemm_kernel(const float *__restrict__ A, size_t lda, int M, int K, const floa
                 }
             }
         };
+        // L2 prefetch of a K block's lines (distance 3), register loads two
+        // K blocks ahead (a ring of three), so that about 64 KB of A per SM
+        // is in flight while the tensor cores work
+        auto prefetch = [&](int kb) {
+            const int k0 = kb * kTcKB;
+            if (!TA) {
+                const int kq = k0 + 4 * (ct & 15);
+                if ((ct & 7) == 0 && kq < K)
+#pragma unroll
+                    for (int e = 0; e < 8; e++) {
+                        const int row = m0 + (ct >> 4) + 16 * e;
+                        if (row < M) asm volatile("prefetch.global.L2 [%0];" ::"l"(A + (size_t)row * lda + kq));
+                    }
+            } else {
+                const int k = k0 + (ct >> 5) * 8 + (lane >> 2);
+                const int m = m0 + 32 * (lane & 3);
+                if (k < K && m < M) asm volatile("prefetch.global.L2 [%0];" ::"l"(A + (size_t)k * lda + m));
+            }
+        };
+        float nx2[32];
         if (nkb > 0) load(kb0, cur);
+        if (nkb > 1) load(kb0 + 1, nxt);
+        if (nkb > 2) prefetch(kb0 + 2);
         for (int i = 0; i < nkb; i++) {
-            if (i + 1 < nkb) load(kb0 + i + 1, nxt);
+            if (i + 2 < nkb) load(kb0 + i + 2, nx2);
+            if (i + 3 < nkb) prefetch(kb0 + i + 3);
             const int s = i % STAGES;
             if (i >= STAGES && !tc_wait(&empty[s], (uint32_t)((i / STAGES - 1) & 1), abort_v)) {
                 fail();
@@ -288,7 +311,10 @@ tc_gemm_kernel(const float *__restrict__ A, size_t lda, int M, int K, const floa
             fence_proxy_async_smem();   // generic-proxy writes -> visible to the tensor core
             mbar_arrive(&full_a[s]);
 #pragma unroll
-            for (int q = 0; q < 32; q++) cur[q] = nxt[q];
+            for (int q = 0; q < 32; q++) {
+                cur[q] = nxt[q];
+                nxt[q] = nx2[q];
+            }
         }
         // epilogue
         const int quad = warp & 3, half = (warp - 2) >> 2;
@@ -445,10 +471,10 @@ int tc_nt(int ncols, int P) {
 }
 
 // Splits of the K blocks: fill whole waves of one CTA per SM, at least 8 K
-// blocks per split, at most 4 CTAs per SM in all (bounds the partial sums),
+// blocks per split, at most 8 CTAs per SM in all (bounds the partial sums),
 // fewer splits on near ties.
 int tc_splits(long long tiles, int nkb, int sms) {
-    const int kmax = std::max(1, std::min({kTcMaxSplits, nkb / 8, (int)std::max(1LL, 4LL * sms / tiles)}));
+    const int kmax = std::max(1, std::min({kTcMaxSplits, nkb / 8, (int)std::max(1LL, 8LL * sms / tiles)}));
     int best = 1;
     double best_score = -1.0;
     for (int k = 1; k <= kmax; k++) {
@@ -573,9 +599,9 @@ size_t tc_gemm_part_floats(int M, int K, int ncols, int P) {
 }
 
 size_t tc_gemm_part_floats_bound(int M, int ncols) {
-    // splits <= 16, and splits x tiles <= 4 CTAs per SM with tiles of at
+    // splits <= 16, and splits x tiles <= 8 CTAs per SM with tiles of at
     // most 128 x 256 outputs (SM count <= 256)
-    return std::min((size_t)kTcMaxSplits * M * ncols, (size_t)4 * 256 * kTcM * 256);
+    return std::min((size_t)kTcMaxSplits * M * ncols, (size_t)8 * 256 * kTcM * 256);
 }
 
 void tc_gemm(const float *A, size_t lda, bool trans, int M, int K, const float *a_scale, const TcOperand &B, float *C,

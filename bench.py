@@ -75,10 +75,11 @@ def parse_args():
                          "4 TF32x3 in the 3M form, 5 FP32 streaming kernels on the CUDA cores)")
     ap.add_argument("--far-variant", type=int, default=-1,
                     help="profile mode: fixed far-field launch shape (-1: autotuned)")
-    ap.add_argument("--mode", default="bench", choices=["bench", "profile", "cpu-validate"],
+    ap.add_argument("--mode", default="bench", choices=["bench", "profile", "cpu-validate", "products"],
                     help="profile: one warm-up solve and one more solve, nothing timed (for ncu captures); "
                          "cpu-validate: the CPU legs' sample extrapolation against full FP64 CPU solves of "
-                         "the workload at icosphere subdivisions 3 and 4")
+                         "the workload at icosphere subdivisions 3 and 4; products: the block solve's product "
+                         "pair per GEMM mode at 16, 64 and 256 sources on the rhs configuration's matrix")
     return ap.parse_args()
 
 
@@ -379,6 +380,45 @@ def cpu_sample(pts, elems, chief, srcs, k, bc, eta, depth, threads, rows=CPU_ROW
                       f"QR {t_qr:.1f} s)"}
 
 
+def run_products(args):
+    """The block solve's product pair (T = A V, W = A^H T) per GEMM mode on the
+    rhs configuration's matrix (15244 x 15212 c64) for the first 16, 64 and
+    256 of its sources: a short block solve (20 inner iterations, one cycle)
+    per case under the library's kernel timer; per-product averages."""
+    import bem_gpu_clean_cpp_gb300 as bem
+    bem.lib()
+    a = argparse.Namespace(**vars(args))
+    a.config, a.sources = "rhs", 256
+    pts, elems, chief, srcs, k, bc = workload_rhs(a)
+    out = []
+    for S in (16, 64, 256):
+        for mode in (6, 4, 3, 1, 5):
+            if mode == 5 and S > 32:
+                continue
+            s = bem.Solver(near_eta=args.eta, near_depth=args.depth, max_iter=20, max_refine=1, block_tol=1e-8,
+                           gemm_mode=mode)
+            s.set_geometry(pts, elems, bc=bc, chief=chief)
+            s.set_sources(srcs[:S])
+            s.assemble(k, bem.PREC_C64)
+            s.solve(bem.SOLVE_BLOCK_GMRES, check=False)   # warm-up (planes, tuning, kernels)
+            s.sync()
+            bem.profile_enable(True)
+            s.solve(bem.SOLVE_BLOCK_GMRES, check=False)
+            s.sync()
+            prof = bem.profile_report()
+            bem.profile_enable(False)
+            row = {"sources": S, "mode": GEMM_NAMES[mode]}
+            for name in ("gemm_AV", "gemm_AhT"):
+                c, t = prof.get(name, (0, 0.0))
+                row[name + "_ms"] = t / max(c, 1)
+            row["pair_ms"] = row["gemm_AV_ms"] + row["gemm_AhT_ms"]
+            out.append(row)
+            del s
+    print(json.dumps({"mode": "products", "nodes": pts.shape[0], "rows": pts.shape[0] + chief.shape[0],
+                      "results": out}), flush=True)
+    return 0
+
+
 def run_cpu_validate(args):
     """The extrapolation behind cpu_baseline and the reference arm, checked
     against full FP64 CPU solves (every row assembled, the full least-squares
@@ -575,6 +615,33 @@ def run_ours(args):
         x64 = x64_all[:, 0]
         err = max(float(np.abs(x_mixed[:, j] - x64_all[:, j]).max() / np.abs(x64_all[:, j]).max())
                   for j in range(S))
+        # this library's own least-squares QR (tensor-core trailing updates,
+        # FP64 refinement) on the c64 assembly: one warm-up, median of 3
+        qr_runs, qinfo = [], None
+        for rep in range(4):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s3.assemble(k, bem.PREC_C64)
+            s3.sync()
+            if rep == 3:
+                bem.profile_enable(True)
+            a.record(st3)
+            qinfo = s3.solve(bem.SOLVE_QR_TC)
+            b.record(st3)
+            s3.sync()
+            if rep == 3:
+                qprof = bem.profile_report()
+                bem.profile_enable(False)
+            if rep > 0:
+                qr_runs.append(a.elapsed_time(b))
+        xq = s3.solution()
+        qr_tc = {"solve_ms": statistics.median(qr_runs), "ms_runs": qr_runs,
+                 "refinements": qinfo.refinements, "rel_residual": qinfo.rel_residual,
+                 "rel_err_vs_fp64": max(float(np.abs(xq[:, j] - x64_all[:, j]).max() / np.abs(x64_all[:, j]).max())
+                                        for j in range(S)),
+                 "kernels_ms": {n: round(t, 3) for n, (c, t) in qprof.items() if n.startswith("qr_") or
+                                n in ("resid", "gemv_h_f64")},
+                 "note": "BEM_SOLVE_QR_TC on the c64 assembly (solve only, assembly excluded): cluster "
+                         "panels, tcgen05 trailing updates, FP64 semi-normal-equation refinement"}
         fp64 = {"ms": ms64, "ms_runs": runs, "spread": (max(runs) - min(runs)) / ms64,
                 "solves_per_s": S * 1000.0 / ms64, "rel_err_mixed_vs_fp64": err,
                 "speedup_mixed_vs_fp64": value / dist.world / (S * 1000.0 / ms64),
@@ -691,6 +758,7 @@ def run_ours(args):
                    "rel_residual": max(i.rel_residual for i in infos) if infos else None},
         "assembly_gbs": (A_bytes + B_bytes) / (asm_ms / 1000.0) / 1e9 if asm_ms else None,
         "fp64_plain": fp64,
+        "qr_tc": qr_tc if fp64 else None,
         "reference_gpu": ref_gpu,
         "roofline": roofline,
         "roofline_hbm": roofline_hbm,
@@ -1013,6 +1081,8 @@ def main():
         return run_profile(args)
     if args.mode == "cpu-validate":
         return run_cpu_validate(args)
+    if args.mode == "products":
+        return run_products(args)
     return run_ours(args)
 
 

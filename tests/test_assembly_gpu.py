@@ -90,7 +90,7 @@ def test_near_singular_assembly_matches_oracle(bemlib, orc, eta, depth):
     assert rel_err(A32, Ao) < TOL32
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6])
 @pytest.mark.parametrize("order", [6, 5])
 def test_far_kernel_launch_shapes(bemlib, orc, variant, order):
     """Every far-kernel launch shape (and both the unrolled 6x6 path and the
@@ -144,7 +144,7 @@ def test_assembly_bitwise_repeatable(bemlib, tile_cols):
     p, f, chief = _problem("ico2")
     n = p.shape[0]
     ref_off = None
-    for v in range(6):
+    for v in range(7):
         s = bemlib.Solver(far_variant=v, tile_cols=tile_cols)
         s.set_geometry(p, f, chief=chief)
         s.set_sources(SRCS)
