@@ -913,8 +913,11 @@ normal_op_tma_kernel(int R, int N, const float2 *__restrict__ A, size_t lda, con
             for (int w = 0; w < kNtNT / 32; w++) t += red[tid >> 1][tid & 1][w];
             tot[par][tid] = t;
         }
-        cluster.sync();   // every CTA's row sums of this group are in its tot[par]
+        // the stage is free once every thread of this CTA has copied it (the CTA
+        // barrier above): refill it before the cluster barrier, so the copy runs
+        // while the cluster exchanges its row sums
         if (tid == 0 && g + kNtNS < ngroups && !abort_flag) issue(g + kNtNS);   // none after a timeout
+        cluster.sync();   // every CTA's row sums of this group are in its tot[par]
         float ts[2 * kNtRPS];
 #pragma unroll
         for (int u = 0; u < 2 * kNtRPS; u++) ts[u] = 0.f;

@@ -477,32 +477,36 @@ __global__ void qr_vrr_kernel(int mr, int pc, const float2 *__restrict__ Vf, siz
 // reflector H_1 ... H_pc = I - V T V^H (forward, column by column: T_kk =
 // tau_k, T[0:k, k] = -tau_k T[0:k, 0:k] G[0:k, k]) from the Gram matrix
 // G = V^H V (Greal: pc x 2pc column-major, [Re G | Im G]); one CTA, thread =
-// row of T; FP64 sums, T kept in FP32 (in global memory: the CTA's own
-// writes, ordered by its barriers).
-__global__ void qr_larft_kernel(int pc, const float *__restrict__ Greal, const float2 *__restrict__ tau,
-                                float2 *T) {
+// row of T.  T is built in shared memory (FP32, column-major: the threads'
+// reads of one column are consecutive) with FP64 sums, then written out.
+__global__ void __launch_bounds__(kQrNB)
+qr_larft_kernel(int pc, const float *__restrict__ Greal, const float2 *__restrict__ tau, float2 *__restrict__ T) {
+    extern __shared__ float2 Ts[];     // [k][r]: column k, row r (kQrNB x kQrNB)
+    __shared__ float2 gk[kQrNB];
     const int r = threadIdx.x;
     for (int k = 0; k < pc; k++) {
-        const float2 tk = tau[k];
-        double2 t = make_double2(0.0, 0.0);
-        if (r < k) {
-            for (int l = r; l < k; l++) {
-                const double2 g = make_double2(Greal[(size_t)k * pc + l], Greal[(size_t)(pc + k) * pc + l]);
-                const float2 trl = T[(size_t)r * kQrNB + l];
-                const double2 u = zmul(make_double2(trl.x, trl.y), g);
-                t.x += u.x;
-                t.y += u.y;
-            }
-        }
+        if (r < k) gk[r] = make_float2(Greal[(size_t)k * pc + r], Greal[(size_t)(pc + k) * pc + r]);
         __syncthreads();
+        double2 t = make_double2(0.0, 0.0);
+        for (int l = r; l < k; l++) {
+            const float2 trl = Ts[(size_t)l * kQrNB + r], g = gk[l];
+            const double2 u = zmul(make_double2(trl.x, trl.y), make_double2(g.x, g.y));
+            t.x += u.x;
+            t.y += u.y;
+        }
+        const float2 tk = tau[k];
         if (r < k) {
             const double2 v = zmul(make_double2(-tk.x, -tk.y), t);
-            T[(size_t)r * kQrNB + k] = make_float2((float)v.x, (float)v.y);
+            Ts[(size_t)k * kQrNB + r] = make_float2((float)v.x, (float)v.y);
+        } else if (r == k) {
+            Ts[(size_t)k * kQrNB + k] = tk;
+        } else if (r < pc) {
+            Ts[(size_t)k * kQrNB + r] = make_float2(0.f, 0.f);
         }
-        if (r == k) T[(size_t)k * kQrNB + k] = tk;
-        if (r > k && r < pc) T[(size_t)r * kQrNB + k] = make_float2(0.f, 0.f);
         __syncthreads();
     }
+    for (int k = 0; k < pc; k++)
+        if (r < pc) T[(size_t)r * kQrNB + k] = Ts[(size_t)k * kQrNB + r];
 }
 
 // The right-hand operand of the rank-pc update: for trailing column c, W'[:, c]
@@ -547,19 +551,24 @@ __global__ void qr_pack_tw_kernel(int nct, int pc, const float *__restrict__ Zre
 __global__ void qr_trsv_back_diag_kernel(int b0, int b1, const float2 *__restrict__ Q, size_t ldq, double2 *X,
                                          size_t ldx) {
     __shared__ double2 xk;
+    __shared__ float2 Rb[kQrTB][kQrTB + 1];   // R[b0 + row][b0 + col] as [col][row]
     double2 *x = X + (size_t)blockIdx.x * ldx;
+    const int nbk = b1 - b0;
+    for (int c = 0; c < nbk; c++)
+        if ((int)threadIdx.x < nbk) Rb[c][threadIdx.x] = Q[(size_t)(b0 + c) * ldq + b0 + threadIdx.x];
+    __syncthreads();
     const int i = b0 + threadIdx.x;
     double2 y = i < b1 ? x[i] : make_double2(0.0, 0.0);
     for (int k = b1 - 1; k >= b0; k--) {
         if (i == k) {
-            const float2 rk = Q[(size_t)k * ldq + k];
+            const float2 rk = Rb[k - b0][k - b0];
             const double d = (double)rk.x * rk.x + (double)rk.y * rk.y;
             y = make_double2((y.x * rk.x + y.y * rk.y) / d, (y.y * rk.x - y.x * rk.y) / d);   // y / r_kk
             xk = y;
         }
         __syncthreads();
         if (i < k) {
-            const float2 r = Q[(size_t)k * ldq + i];
+            const float2 r = Rb[k - b0][i - b0];
             const double2 u = zmul(make_double2(r.x, r.y), xk);
             y.x -= u.x;
             y.y -= u.y;
@@ -589,19 +598,24 @@ __global__ void qr_trsv_back_update_kernel(int b0, int b1, const float2 *__restr
 __global__ void qr_trsv_fwd_diag_kernel(int b0, int b1, const float2 *__restrict__ Q, size_t ldq, double2 *X,
                                         size_t ldx) {
     __shared__ double2 xk;
+    __shared__ float2 Rb[kQrTB][kQrTB + 1];   // R[b0 + row][b0 + col] as [col][row]
     double2 *x = X + (size_t)blockIdx.x * ldx;
+    const int nbk = b1 - b0;
+    for (int c = 0; c < nbk; c++)
+        if ((int)threadIdx.x < nbk) Rb[c][threadIdx.x] = Q[(size_t)(b0 + c) * ldq + b0 + threadIdx.x];
+    __syncthreads();
     const int i = b0 + threadIdx.x;
     double2 y = i < b1 ? x[i] : make_double2(0.0, 0.0);
     for (int k = b0; k < b1; k++) {
         if (i == k) {
-            const float2 rk = Q[(size_t)k * ldq + k];                  // conj(r_kk) divides
+            const float2 rk = Rb[k - b0][k - b0];                      // conj(r_kk) divides
             const double d = (double)rk.x * rk.x + (double)rk.y * rk.y;
             y = make_double2((y.x * rk.x - y.y * rk.y) / d, (y.y * rk.x + y.x * rk.y) / d);
             xk = y;
         }
         __syncthreads();
         if (i > k && i < b1) {
-            const float2 r = Q[(size_t)i * ldq + k];                   // (R^H)_{ik} = conj(R_ki)
+            const float2 r = Rb[i - b0][k - b0];                       // (R^H)_{ik} = conj(R_ki)
             const double2 u = zjmul(make_double2(r.x, r.y), xk);
             y.x -= u.x;
             y.y -= u.y;
@@ -689,6 +703,9 @@ int qr_cluster_size(size_t smem16) {
         if (err == cudaSuccess) err = cudaDeviceGetAttribute(&maxs, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
         if (err == cudaSuccess)
             err = cudaFuncSetAttribute(qr_panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, maxs);
+        if (err == cudaSuccess)
+            err = cudaFuncSetAttribute(qr_larft_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)(sizeof(float2) * kQrNB * kQrNB));
         nonportable = cudaFuncSetAttribute(qr_panel_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
                       cudaSuccess;
         cudaGetLastError();
@@ -805,7 +822,7 @@ void bem_solver_s::solve_qr_tc(bem_solve_info_t *info) {
             // G = V^H V (pc x pc): conj(V^T) V with V^T's rows the columns of Vf
             tc_gemm(reinterpret_cast<const float *>(qt_v.p), 2 * ldv, false, pc, 2 * mr, sc + 2, opv, G, pc,
                     qt_part.as<float>(), status, stream);
-            qr_larft_kernel<<<1, kQrNB, 0, stream>>>(pc, G, q_tau.as<float2>() + j0, T);
+            qr_larft_kernel<<<1, kQrNB, sizeof(float2) * kQrNB * kQrNB, stream>>>(pc, G, q_tau.as<float2>() + j0, T);
             count_launch(2);
         }
         {

@@ -62,30 +62,44 @@ uint32_t morton_key(const double *p, const double *lo, const double *inv) {
 // batch boundaries (offsets into `out`) to `bptr`.
 void pack_batches(const std::vector<TileRec> &list, int tile_cols, std::vector<TileRec> &out,
                   std::vector<int> &bptr) {
-    std::vector<int> size((list.size() + kFarBatch - 1) / kFarBatch, 0), batch_of(list.size());
-    std::vector<std::vector<int>> slot_batches(tile_cols);   // batches already holding a record on the slot
+    // per slot, a bit set of the batches already holding a record on it (64
+    // batches per word); per record the allowed batches are the complement of
+    // its slots' union, and the least-filled of those with room is taken
+    const int nb0 = (int)((list.size() + kFarBatch - 1) / kFarBatch);
+    int words = std::max(1, (nb0 + 8 + 63) / 64);
+    std::vector<uint64_t> used((size_t)tile_cols * words, 0);
+    std::vector<int> size(nb0, 0), batch_of(list.size());
     for (size_t r = 0; r < list.size(); r++) {
         const TileRec &rec = list[r];
-        auto clash = [&](int b) {
-            for (int j = 0; j < 3; j++) {
-                const int s = rec.slot[j];
-                if (s < 0) continue;
-                for (const int u : slot_batches[s])
-                    if (u == b) return true;
-            }
-            return false;
-        };
         int best = -1;
-        for (int b = 0; b < (int)size.size(); b++)
-            if (size[b] < kFarBatch && (best < 0 || size[b] < size[best]) && !clash(b)) best = b;
+        for (int w = 0; w < words && w * 64 < (int)size.size(); w++) {
+            uint64_t busy = 0;
+            for (int j = 0; j < 3; j++)
+                if (rec.slot[j] >= 0) busy |= used[(size_t)rec.slot[j] * words + w];
+            uint64_t cand = ~busy;
+            while (cand) {
+                const int b = w * 64 + __builtin_ctzll(cand);
+                cand &= cand - 1;
+                if (b >= (int)size.size()) break;
+                if (size[b] < kFarBatch && (best < 0 || size[b] < size[best])) best = b;
+            }
+        }
         if (best < 0) {
             best = (int)size.size();
             size.push_back(0);
+            if ((best + 64) / 64 > words) {   // widen the bit sets
+                const int nw = words * 2;
+                std::vector<uint64_t> u2((size_t)tile_cols * nw, 0);
+                for (size_t c = 0; c < (size_t)tile_cols; c++)
+                    for (int w = 0; w < words; w++) u2[c * nw + w] = used[c * words + w];
+                used.swap(u2);
+                words = nw;
+            }
         }
         size[best]++;
         batch_of[r] = best;
         for (int j = 0; j < 3; j++)
-            if (rec.slot[j] >= 0) slot_batches[rec.slot[j]].push_back(best);
+            if (rec.slot[j] >= 0) used[(size_t)rec.slot[j] * words + best / 64] |= 1ull << (best % 64);
     }
     // stable counting sort of the records by batch
     std::vector<int> start(size.size() + 1, 0);

@@ -81,10 +81,6 @@ __device__ __forceinline__ bool tc_wait(uint64_t *bar, uint32_t parity, volatile
 }
 
 
-__device__ __forceinline__ uint32_t pack_h2(__half a, __half b) {
-    return (uint32_t)__half_as_ushort(a) | ((uint32_t)__half_as_ushort(b) << 16);
-}
-
 // Byte offset of the 16-byte chunk c (K values 8c..8c+7) of row r in a
 // K-major 128-byte-swizzled tile.
 __device__ __forceinline__ uint32_t sw128_chunk(int r, int c) {
@@ -247,31 +243,26 @@ tc_gemm_kernel(const float *__restrict__ A, size_t lda, int M, int K, const floa
 #pragma unroll
                 for (int e = 0; e < 8; e++) {
                     const int row = (ct >> 4) + 16 * e;
-                    __half h[4][3];
-#pragma unroll
-                    for (int q = 0; q < 4; q++) split_parts<P>(r[4 * e + q] * sa, h[q]);
+                    uint32_t h01[3], h23[3];
+                    split_pair<P>(r[4 * e] * sa, r[4 * e + 1] * sa, h01);
+                    split_pair<P>(r[4 * e + 2] * sa, r[4 * e + 3] * sa, h23);
                     const uint32_t off = sw128_chunk(row, c4 >> 1) + ((c4 & 1) << 3);
 #pragma unroll
-                    for (int p = 0; p < P; p++) {
-                        const uint2 w = make_uint2(pack_h2(h[0][p], h[1][p]), pack_h2(h[2][p], h[3][p]));
-                        *reinterpret_cast<uint2 *>(pl[p] + off) = w;
-                    }
+                    for (int p = 0; p < P; p++)
+                        *reinterpret_cast<uint2 *>(pl[p] + off) = make_uint2(h01[p], h23[p]);
                 }
             } else {
                 const int wc = ct >> 5;
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
                     const int row = lane + 32 * j;
-                    __half h[8][3];
+                    uint32_t h[4][3];
 #pragma unroll
-                    for (int e = 0; e < 8; e++) split_parts<P>(r[8 * j + e] * sa, h[e]);
+                    for (int e = 0; e < 4; e++) split_pair<P>(r[8 * j + 2 * e] * sa, r[8 * j + 2 * e + 1] * sa, h[e]);
                     const uint32_t off = sw128_chunk(row, wc);
 #pragma unroll
-                    for (int p = 0; p < P; p++) {
-                        const uint4 w = make_uint4(pack_h2(h[0][p], h[1][p]), pack_h2(h[2][p], h[3][p]),
-                                                   pack_h2(h[4][p], h[5][p]), pack_h2(h[6][p], h[7][p]));
-                        *reinterpret_cast<uint4 *>(pl[p] + off) = w;
-                    }
+                    for (int p = 0; p < P; p++)
+                        *reinterpret_cast<uint4 *>(pl[p] + off) = make_uint4(h[0][p], h[1][p], h[2][p], h[3][p]);
                 }
             }
         };

@@ -19,6 +19,37 @@ __device__ __forceinline__ void split_parts(float v, __half (&h)[3]) {
     }
 }
 
+// v rounded to 11 significant bits (fp16's precision) by Dekker's splitting
+// (c = (2^13 + 1) v, hi = c - (c - v)): three FP32 operations, exactly
+// representable in fp16 for |hi| >= 2^-14; v - hi is exact.
+__device__ __forceinline__ float dekker_hi11(float v) {
+    const float c = __fmul_rn(v, 8193.0f);
+    return __fsub_rn(c, __fsub_rn(c, v));
+}
+
+__device__ __forceinline__ uint32_t half2_bits(__half2 h) {
+    return *reinterpret_cast<const uint32_t *>(&h);
+}
+
+// The P fp16 parts of the pair (a, b) (already scaled), each part packed as
+// a half2: the same parts as split_parts in fp16's normal range, with one
+// packed conversion per part instead of three scalar conversions per value
+// (below 2^-14 the head is rounded once more into fp16's subnormals, an
+// absolute error of at most 2^-25).
+template <int P>
+__device__ __forceinline__ void split_pair(float a, float b, uint32_t (&out)[3]) {
+    const float ha = dekker_hi11(a), hb = dekker_hi11(b);
+    out[0] = half2_bits(__floats2half2_rn(ha, hb));
+    const float ra = __fsub_rn(a, ha), rb = __fsub_rn(b, hb);
+    if (P == 2) {
+        out[1] = half2_bits(__floats2half2_rn(ra, rb));
+    } else {
+        const float ma = dekker_hi11(ra), mb = dekker_hi11(rb);
+        out[1] = half2_bits(__floats2half2_rn(ma, mb));
+        out[2] = half2_bits(__floats2half2_rn(__fsub_rn(ra, ma), __fsub_rn(rb, mb)));
+    }
+}
+
 // Power-of-two scale of a column from its largest magnitude.
 __device__ __forceinline__ float pow2_scale(float amax) {
     if (!(amax > 0.f) || !isfinite(amax)) return 1.f;
