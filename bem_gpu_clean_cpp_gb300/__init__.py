@@ -163,6 +163,7 @@ SIGNATURES = {
     "bem_solver_stream": (_VP, [_VP]),
     "bem_solver_sizes": (_I, [_VP, _VP, _VP, _VP, _VP]),
     "bem_solver_block_gemm_mode": (_I, [_VP, ctypes.POINTER(_I)]),
+    "bem_solver_far_variant": (_I, [_VP, ctypes.POINTER(_I)]),
     "bem_server_options_default": (_I, [_VP]),
     "bem_server_create": (_I, [_VP, ctypes.POINTER(_VP)]),
     "bem_server_destroy": (_I, [_VP]),
@@ -549,6 +550,12 @@ class Solver:
         """GEMM_* mode of the last block solve's products (AUTO's choice)."""
         v = ctypes.c_int()
         _check(lib().bem_solver_block_gemm_mode(self._h, ctypes.byref(v)))
+        return v.value
+
+    def far_variant(self) -> int:
+        """Launch shape of the far kernel in the last c64 assembly (-1: none)."""
+        v = ctypes.c_int()
+        _check(lib().bem_solver_far_variant(self._h, ctypes.byref(v)))
         return v.value
 
     def assemble(self, k: float, precision: int = PREC_C64) -> None:

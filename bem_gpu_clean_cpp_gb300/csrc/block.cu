@@ -791,13 +791,15 @@ void bem_solver_s::solve_block(bem_solve_info_t *info) {
         TcOperand op = tc_operand_view(x_vlo.p, 2 * n, 2 * S, parts);
         if (f64) tc_pack_cplx_f64(static_cast<const double2 *>(Xs), n, S, op, stream);
         else tc_pack_cplx_f32(static_cast<const float2 *>(Xs), n, S, op, stream);
-        tc_gemm(Af, 2 * lda, false, R, 2 * n, tc_scale.as<float>(), op, Tt, R, x_tlo.as<float>(), tc_status, stream);
+        tc_gemm(Af, 2 * lda, false, R, 2 * n, tc_scale.as<float>(), op, Tt, R, x_tlo.as<float>(),
+                x_tlo.bytes / sizeof(float), tc_status, stream);
     };
     auto tc_aht = [&](int parts) {
         BEM_PROF("gemm_AhT", stream);
         TcOperand op = tc_operand_view(x_vlo.p, R, 2 * S, parts);
         tc_pack_real(Tt, R, op, stream);
-        tc_gemm(Af, 2 * lda, true, 2 * n, R, tc_scale.as<float>(), op, Wt, 2 * n, x_tlo.as<float>(), tc_status,
+        tc_gemm(Af, 2 * lda, true, 2 * n, R, tc_scale.as<float>(), op, Wt, 2 * n, x_tlo.as<float>(),
+                x_tlo.bytes / sizeof(float), tc_status,
                 stream);
         combine_w_kernel<<<grid2(n, S), 256, 0, stream>>>(n, S, Wt, nullptr, W);
         count_launch();

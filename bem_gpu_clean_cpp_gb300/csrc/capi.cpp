@@ -814,4 +814,11 @@ int bem_solver_block_gemm_mode(bem_solver_t s, int *mode) {
     BEM_API_END
 }
 
+int bem_solver_far_variant(bem_solver_t s, int *variant) {
+    BEM_API_BEGIN
+    BEM_CHECK_ARG(s && variant, "null argument");
+    *variant = s->far_variant_used;
+    BEM_API_END
+}
+
 }  // extern "C"

@@ -96,6 +96,23 @@ struct PanelLayout {
     }
 };
 
+// Sum over the cluster's CTAs of the float2 at shared offset `off` + idx:
+// the loads of all peers are issued before any is added (kQrCL independent
+// remote loads in flight instead of one latency per peer).
+template <class Peer>
+__device__ __forceinline__ float2 cluster_sum(const Peer &peer, size_t off, size_t idx, int CL) {
+    float2 u[kQrCL];
+#pragma unroll
+    for (int p = 0; p < kQrCL; p++) u[p] = p < CL ? peer(off, p)[idx] : make_float2(0.f, 0.f);
+    float2 t = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int p = 0; p < kQrCL; p++) {
+        t.x += u[p].x;
+        t.y += u[p].y;
+    }
+    return t;
+}
+
 // v_k at local row i of this CTA: 0 above the pivot row g_k, 1 on it, the
 // stored vector below.
 __device__ __forceinline__ float2 vval(const float2 *L, int lds, int k, int grow, int gk, int i) {
@@ -228,11 +245,7 @@ qr_panel_kernel(float2 *__restrict__ Q, size_t ldq, int m, int j0, int pc, int r
             if (warp == 0 && lane < kQrW) {
                 float2 t = make_float2(0.f, 0.f);
                 if (lane > jj && lane < lw)
-                    for (int p = 0; p < CL; p++) {
-                        const float2 u = peer(lay.dot + par * kQrW, p)[lane];
-                        t.x += u.x;
-                        t.y += u.y;
-                    }
+                    t = cluster_sum(peer, lay.dot + par * kQrW, lane, CL);
                 scratch[lane] = cjmul(tau, t);
             }
             __syncthreads();
@@ -305,21 +318,13 @@ qr_panel_kernel(float2 *__restrict__ Q, size_t ldq, int m, int j0, int pc, int r
         for (int e = tid; e < lw * lw; e += kQrNT) {
             const int a = e / lw, b = e % lw;
             float2 t = make_float2(0.f, 0.f);
-            for (int p = 0; p < CL; p++) {
-                const float2 u = peer(lay.gram, p)[a * kQrW + b];
-                t.x += u.x;
-                t.y += u.y;
-            }
+            t = cluster_sum(peer, lay.gram, a * kQrW + b, CL);
             ps[lay.gsum + a * kQrW + b] = t;
         }
         for (int e = tid; e < lw * nrest; e += kQrNT) {
             const int k = e / nrest, cc = e % nrest;
             float2 t = make_float2(0.f, 0.f);
-            for (int p = 0; p < CL; p++) {
-                const float2 u = peer(lay.wpart, p)[(size_t)k * kQrNB + cc];
-                t.x += u.x;
-                t.y += u.y;
-            }
+            t = cluster_sum(peer, lay.wpart, (size_t)k * kQrNB + cc, CL);
             ps[lay.ysum + (size_t)k * kQrNB + cc] = t;   // W = V^H P for now
         }
         __syncthreads();
@@ -752,10 +757,17 @@ void bem_solver_s::solve_qr_tc(bem_solve_info_t *info) {
     qt_z.ensure(sizeof(float) * 2 * kQrNB * ncq);
     qt_opv.ensure(tc_operand_bytes(2 * m, 2 * kQrNB, 2));
     qt_opw.ensure(tc_operand_bytes(2 * kQrNB, (int)ncq, 2));
-    const size_t pf = std::max({tc_gemm_part_floats(kQrNB, 2 * m, 2 * kQrNB, 2),
-                                tc_gemm_part_floats((int)ncq, 2 * m, 2 * kQrNB, 2),
-                                tc_gemm_part_floats(2 * m, 2 * kQrNB, (int)ncq, 2)});
+    // split-K partial sums: the largest any panel's three products plan (a
+    // later panel with fewer tiles may split more than the first)
+    size_t pf = 0;
+    for (int j0 = 0; j0 < n; j0 += kQrNB) {
+        const int pc = std::min(kQrNB, n - j0), mr = m - j0, nct = (int)ncq - j0 - pc;
+        pf = std::max(pf, tc_gemm_part_floats(pc, 2 * mr, 2 * pc, 2));
+        if (nct > 0)
+            pf = std::max({pf, tc_gemm_part_floats(nct, 2 * mr, 2 * pc, 2), tc_gemm_part_floats(2 * mr, 2 * pc, nct, 2)});
+    }
     if (pf) qt_part.ensure(sizeof(float) * pf);
+    const size_t part_floats = qt_part.bytes / sizeof(float);
     qt_scal.ensure(sizeof(float) * 8);
     d_status.ensure(4 * sizeof(int));
     int *status = d_status.as<int>() + 1;
@@ -821,7 +833,7 @@ void bem_solver_s::solve_qr_tc(bem_solve_info_t *info) {
             tc_pack_cplx_f32(qt_v.as<float2>(), mr, pc, opv, stream, ldv, true);
             // G = V^H V (pc x pc): conj(V^T) V with V^T's rows the columns of Vf
             tc_gemm(reinterpret_cast<const float *>(qt_v.p), 2 * ldv, false, pc, 2 * mr, sc + 2, opv, G, pc,
-                    qt_part.as<float>(), status, stream);
+                    qt_part.as<float>(), part_floats, status, stream);
             qr_larft_kernel<<<1, kQrNB, sizeof(float2) * kQrNB * kQrNB, stream>>>(pc, G, q_tau.as<float2>() + j0, T);
             count_launch(2);
         }
@@ -829,15 +841,15 @@ void bem_solver_s::solve_qr_tc(bem_solve_info_t *info) {
             BEM_PROF("qr_update", stream);
             // Z = C^H V (nct x pc), W' = T^H Z^H packed, C -= V W'
             TcOperand opv = tc_operand_view(qt_opv.p, 2 * mr, 2 * pc, 2);
-            tc_gemm(C, 2 * ldq, false, nct, 2 * mr, sc, opv, qt_z.as<float>(), nct, qt_part.as<float>(), status,
-                    stream);
+            tc_gemm(C, 2 * ldq, false, nct, 2 * mr, sc, opv, qt_z.as<float>(), nct, qt_part.as<float>(), part_floats,
+                    status, stream);
             TcOperand opw = tc_operand_view(qt_opw.p, 2 * pc, nct, 2);
             qr_pack_tw_kernel<2><<<(nct + kQrTwCols - 1) / kQrTwCols, kQrNB, 0, stream>>>(
                 nct, pc, qt_z.as<float>(), T, opw.Kp, opw.ncols_pad, opw.planes, opw.col_inv);
             qr_vrr_kernel<<<mr, kQrNB, 0, stream>>>(mr, pc, qt_v.as<float2>(), ldv, qt_vrr.as<float>(), ldk);
             count_launch(2);
             tc_gemm(qt_vrr.as<float>(), ldk, false, 2 * mr, 2 * pc, sc + 2, opw, C, 2 * ldq, qt_part.as<float>(),
-                    status, stream, true);
+                    part_floats, status, stream, true);
         }
         KERNEL_CHECK();
     }

@@ -62,44 +62,71 @@ uint32_t morton_key(const double *p, const double *lo, const double *inv) {
 // batch boundaries (offsets into `out`) to `bptr`.
 void pack_batches(const std::vector<TileRec> &list, int tile_cols, std::vector<TileRec> &out,
                   std::vector<int> &bptr) {
-    // per slot, a bit set of the batches already holding a record on it (64
-    // batches per word); per record the allowed batches are the complement of
-    // its slots' union, and the least-filled of those with room is taken
+    // Bit sets, 64 batches per word: per slot, the batches already holding a
+    // record on it (`used`); per fill level s, the batches holding s records
+    // (`level`).  A record's allowed batches are the complement of its slots'
+    // union; the occupied levels are scanned upward from the lowest, so
+    // the first allowed batch found is the least-filled (lowest index among
+    // equals) with room, and the fills stay within a few levels of each
+    // other: a handful of word operations per record.
     const int nb0 = (int)((list.size() + kFarBatch - 1) / kFarBatch);
     int words = std::max(1, (nb0 + 8 + 63) / 64);
     std::vector<uint64_t> used((size_t)tile_cols * words, 0);
+    std::vector<uint64_t> level((size_t)(kFarBatch + 1) * words, 0);
     std::vector<int> size(nb0, 0), batch_of(list.size());
+    for (int b = 0; b < nb0; b++) level[b / 64] |= 1ull << (b % 64);
+    int low = 0, high = 0;   // lowest and highest fill levels holding a batch
+    std::vector<uint64_t> busy(words);
     for (size_t r = 0; r < list.size(); r++) {
         const TileRec &rec = list[r];
-        int best = -1;
-        for (int w = 0; w < words && w * 64 < (int)size.size(); w++) {
-            uint64_t busy = 0;
+        for (int w = 0; w < words; w++) {
+            uint64_t u = 0;
             for (int j = 0; j < 3; j++)
-                if (rec.slot[j] >= 0) busy |= used[(size_t)rec.slot[j] * words + w];
-            uint64_t cand = ~busy;
-            while (cand) {
-                const int b = w * 64 + __builtin_ctzll(cand);
-                cand &= cand - 1;
-                if (b >= (int)size.size()) break;
-                if (size[b] < kFarBatch && (best < 0 || size[b] < size[best])) best = b;
-            }
+                if (rec.slot[j] >= 0) u |= used[(size_t)rec.slot[j] * words + w];
+            busy[w] = u;
         }
+        int best = -1;
+        for (int s = low; s <= std::min(high, kFarBatch - 1) && best < 0; s++)
+            for (int w = 0; w < words; w++) {
+                const uint64_t m = level[(size_t)s * words + w] & ~busy[w];
+                if (m) {
+                    best = w * 64 + __builtin_ctzll(m);
+                    break;
+                }
+            }
         if (best < 0) {
             best = (int)size.size();
             size.push_back(0);
             if ((best + 64) / 64 > words) {   // widen the bit sets
                 const int nw = words * 2;
-                std::vector<uint64_t> u2((size_t)tile_cols * nw, 0);
-                for (size_t c = 0; c < (size_t)tile_cols; c++)
-                    for (int w = 0; w < words; w++) u2[c * nw + w] = used[c * words + w];
-                used.swap(u2);
+                auto widen = [](std::vector<uint64_t> &v, size_t rows, int w0, int w1) {
+                    std::vector<uint64_t> v2(rows * w1, 0);
+                    for (size_t c = 0; c < rows; c++)
+                        for (int w = 0; w < w0; w++) v2[c * w1 + w] = v[c * w0 + w];
+                    v.swap(v2);
+                };
+                widen(used, (size_t)tile_cols, words, nw);
+                widen(level, (size_t)kFarBatch + 1, words, nw);
+                busy.resize(nw, 0);
                 words = nw;
             }
+            level[best / 64] |= 1ull << (best % 64);
+            low = 0;
         }
-        size[best]++;
+        const int s = size[best]++;
+        high = std::max(high, s + 1);
+        const uint64_t bit = 1ull << (best % 64);
+        level[(size_t)s * words + best / 64] &= ~bit;
+        level[(size_t)(s + 1) * words + best / 64] |= bit;
+        while (low < kFarBatch) {   // advance past emptied levels
+            bool any = false;
+            for (int w = 0; w < words && !any; w++) any = level[(size_t)low * words + w] != 0;
+            if (any) break;
+            low++;
+        }
         batch_of[r] = best;
         for (int j = 0; j < 3; j++)
-            if (rec.slot[j] >= 0) used[(size_t)rec.slot[j] * words + best / 64] |= 1ull << (best % 64);
+            if (rec.slot[j] >= 0) used[(size_t)rec.slot[j] * words + best / 64] |= bit;
     }
     // stable counting sort of the records by batch
     std::vector<int> start(size.size() + 1, 0);
@@ -162,7 +189,7 @@ void bem_solver_s::set_geometry(const double *pnts, int num_pnts, const int *ele
     R = N + M;
     h_nodes.assign(pnts, pnts + 3 * (size_t)N);
     h_elems.assign(elems, elems + 3 * (size_t)E);
-    // The column-tile tables (host work of ~0.4 ms at 20480 elements) are
+    // The column-tile tables (host work of ~1 ms at 20480 elements) are
     // built on another host thread while this call and the assembly's first
     // steps go on; ensure_tiles takes them.
     host_tiles = HostTiles{};
@@ -466,6 +493,11 @@ void bem_solver_s::assemble(double kk, int precision) {
     if (S == 0) BEM_FAIL(BEM_ERR_STATE, "no sources set");
     ensure_quadrature(opt.order);
     ensure_geo();
+    // The near-pair list (host grid, two small kernels, two waits) is built
+    // first, while the column-tile tables may still be in the making on the
+    // host thread set_geometry started; after the far kernel its waits would
+    // hold the host for that whole kernel.
+    ensure_near_list();
     ensure_tiles(precision);
     k = kk;
     prec = precision;
@@ -540,7 +572,6 @@ void bem_solver_s::assemble(double kk, int precision) {
                             stream, variant);
     far_variant_used = variant;
     d_beta.ensure(sizeof(double2) * (size_t)R);
-    ensure_near_list();
     launch_near_assembly(precision, row_points(), N, geo_tables(), ph, d_A.p, lda, d_cpart.p, d_bpart.p,
                          T.ntiles, d_srcs.as<DevSource>(), S, d_B.as<double2>(), d_beta.as<double2>(),
                          d_near_ptr.as<int>(), d_near_ids.as<int>(), stream);

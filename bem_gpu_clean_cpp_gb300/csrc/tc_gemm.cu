@@ -596,14 +596,16 @@ size_t tc_gemm_part_floats_bound(int M, int ncols) {
 }
 
 void tc_gemm(const float *A, size_t lda, bool trans, int M, int K, const float *a_scale, const TcOperand &B, float *C,
-             size_t ldc, float *part, int *status, cudaStream_t st, bool subtract) {
+             size_t ldc, float *part, size_t part_floats, int *status, cudaStream_t st, bool subtract) {
     BEM_CHECK_ARG(B.K == K && M > 0 && K > 0 && B.ncols > 0, "tc_gemm: shapes");
     BEM_CHECK_ARG(lda % 4 == 0 && (reinterpret_cast<uintptr_t>(A) & 15) == 0, "tc_gemm: A alignment");
     BEM_CHECK_ARG(trans ? lda >= (size_t)M : lda >= (size_t)((K + 3) & ~3), "tc_gemm: lda");
     BEM_CHECK_ARG(B.P == 2 || B.P == 3, "tc_gemm: parts");
     BEM_CHECK_ARG(status != nullptr && a_scale != nullptr, "tc_gemm: status and scale words");
     const TcPlan p = tc_plan(M, K, B.ncols, B.P);
-    if (p.splits > 1) BEM_CHECK_ARG(part != nullptr, "tc_gemm: split-K scratch missing");
+    if (p.splits > 1)
+        BEM_CHECK_ARG(part != nullptr && part_floats >= (size_t)p.splits * M * B.ncols,
+                      "tc_gemm: split-K scratch missing or smaller than the plan's partial sums");
     CUtensorMap tm;
     const cuuint64_t gdim[2] = {(cuuint64_t)B.Kp, (cuuint64_t)B.P * B.ncols_pad};
     const cuuint64_t gstride[1] = {(cuuint64_t)B.Kp * sizeof(__half)};
@@ -662,7 +664,7 @@ extern "C" int bem_tc_gemm_f32(int trans, int m, int k, int n, const float *A, i
     tc_a_scale(dA.as<float>(), lda, (int)arows, trans ? m : k, scal, st);
     TcOperand op = tc_operand_view(dOp.p, k, n, parts);
     tc_pack_real(dB.as<float>(), ldb, op, st);
-    tc_gemm(dA.as<float>(), lda, trans != 0, m, k, scal, op, dC.as<float>(), ldc, dPart.as<float>(), status, st);
+    tc_gemm(dA.as<float>(), lda, trans != 0, m, k, scal, op, dC.as<float>(), ldc, dPart.as<float>(), pf, status, st);
     CUDA_TRY(cudaStreamSynchronize(st));
     int h_status = 0;
     CUDA_TRY(cudaMemcpy(&h_status, status, sizeof(int), cudaMemcpyDeviceToHost));

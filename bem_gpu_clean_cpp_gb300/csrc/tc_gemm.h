@@ -52,13 +52,15 @@ void tc_a_scale(const float *A, size_t ld, int rows, int cols, float *scale, cud
 // real FP32 matrix with row stride lda (floats; a multiple of 4) read
 // directly from global memory: trans = false: op(A) = A (M x K); trans =
 // true: op(A) = A^T with A stored K x M.  a_scale: tc_a_scale's pair (device).
-// B: a packed operand (B.K == K).  part: scratch of tc_gemm_part_floats()
-// floats for split-K partial sums (may be null when that is 0).  status:
+// B: a packed operand (B.K == K).  part: scratch of part_floats floats for
+// split-K partial sums, at least tc_gemm_part_floats() of this shape (may be
+// null when that is 0; a plan that needs more is refused).  status:
 // device word set to 1 if a bounded wait of the kernel timed out (the result
 // is then invalid).  Deterministic: the same inputs give the same bits.
 // subtract: C -= op(A) B instead of C = op(A) B.
 void tc_gemm(const float *A, size_t lda, bool trans, int M, int K, const float *a_scale, const TcOperand &B,
-             float *C, size_t ldc, float *part, int *status, cudaStream_t st, bool subtract = false);
+             float *C, size_t ldc, float *part, size_t part_floats, int *status, cudaStream_t st,
+             bool subtract = false);
 size_t tc_gemm_part_floats(int M, int K, int ncols, int P);
 // Upper bound of tc_gemm_part_floats over K, P and the device's SM count.
 size_t tc_gemm_part_floats_bound(int M, int ncols);

@@ -100,7 +100,7 @@ def run_profile(args):
         info = s.solve(method)
     s.sync()
     print(json.dumps({"mode": "profile", "iterations": info.iterations, "refinements": info.refinements,
-                      "rel_residual": info.rel_residual}))
+                      "rel_residual": info.rel_residual, "far_variant": s.far_variant()}))
     return 0
 
 
@@ -764,6 +764,7 @@ def run_ours(args):
         "roofline_hbm": roofline_hbm,
         "kernels": per_kernel,
         "dominant_kernel": dom,
+        "far_variant": s.far_variant() if args.config == "precision" or args.config == "rhs" else None,
         "gpu_launches": launches,
         "clocks": clk,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},

@@ -304,6 +304,10 @@ int bem_solver_sizes(bem_solver_t s, int *n, int *m, int *num_elems, int *num_sr
  * products in (AUTO's choice), or BEM_GEMM_AUTO before any block solve (no
  * reference counterpart). */
 int bem_solver_block_gemm_mode(bem_solver_t s, int *mode);
+/* The far-field kernel's launch shape the handle's last c64 assembly ran
+ * (the autotuner's choice unless options fix it; 0 .. 6), or -1 before any
+ * (no reference counterpart). */
+int bem_solver_far_variant(bem_solver_t s, int *variant);
 
 /* ------------------------------------------------------------------ */
 /* Request server (no reference counterpart: the reference solves one   */
