@@ -23,9 +23,11 @@
 // * X = R^{-1} (Q^H B)[0:n] by blocked back substitution.
 // * Refinement to the FP64 least-squares solution (semi-normal equations,
 //   corrected): r = b - A x and g = A^H r with FP64-accurate products (c128
-//   A, or c64 A with double-float sums), R^H R dx = g by two triangular
-//   solves with the FP32 factor, x += dx, until ||g|| <= tol ||A^H b||.  It
-//   converges by a factor of about kappa(A)^2 x 6e-8 per step.
+//   A, or c64 A with double-float sums), R^H R dx = g by two FP32 triangular
+//   solves with the FP32 factor (g scaled to order one), x += dx, until
+//   ||g|| <= tol ||A^H b||.  It converges by a factor of about
+//   kappa(A)^2 x 6e-8 per step; FP32 arithmetic in the solves adds errors of
+//   the factor's own order.
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
@@ -64,12 +66,6 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
 // conj(a) b
 __device__ __forceinline__ float2 cjmul(float2 a, float2 b) {
     return make_float2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
-}
-__device__ __forceinline__ double2 zmul(double2 a, double2 b) {
-    return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
-}
-__device__ __forceinline__ double2 zjmul(double2 a, double2 b) {
-    return make_double2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
 }
 
 // Shared-memory layout of the panel kernel (float2 units): the leaf L[W][lds]
@@ -479,182 +475,359 @@ __global__ void qr_vrr_kernel(int mr, int pc, const float2 *__restrict__ Vf, siz
 }
 
 // T (pc x pc, row-major, ld kQrNB, upper triangular) of the panel's block
-// reflector H_1 ... H_pc = I - V T V^H (forward, column by column: T_kk =
-// tau_k, T[0:k, k] = -tau_k T[0:k, 0:k] G[0:k, k]) from the Gram matrix
-// G = V^H V (Greal: pc x 2pc column-major, [Re G | Im G]); one CTA, thread =
-// row of T.  T is built in shared memory (FP32, column-major: the threads'
-// reads of one column are consecutive) with FP64 sums, then written out.
-__global__ void __launch_bounds__(kQrNB)
+// reflector H_1 ... H_pc = I - V T V^H from the Gram matrix G = V^H V
+// (Greal: pc x 2pc column-major, [Re G | Im G]) and the taus, by doubling:
+// the T of 16-column leaves by the column recurrence (T_kk = tau_k,
+// T[0:k, k] = -tau_k T[0:k, 0:k] G[0:k, k]), one warp per leaf, then
+// adjacent blocks merged at widths 32, 64 and 128 through
+// (I - V1 T1 V1^H)(I - V2 T2 V2^H) = I - [V1 V2] [[T1, -T1 G12 T2], [0, T2]] [V1 V2]^H,
+// all pairs of a level at once (two triangular products).  Columns past pc
+// act as tau = 0, G = 0 (their T columns come out zero).  FP32 throughout,
+// like the factor it serves; one CTA, T in shared memory as [col][row].
+constexpr int kQrLeafT = 16;
+constexpr int kQrLarftNT = 512;
+constexpr size_t kQrLarftSmem = sizeof(float2) * ((size_t)kQrNB * kQrNB + (size_t)kQrNB * kQrNB / 4);
+__global__ void __launch_bounds__(kQrLarftNT)
 qr_larft_kernel(int pc, const float *__restrict__ Greal, const float2 *__restrict__ tau, float2 *__restrict__ T) {
-    extern __shared__ float2 Ts[];     // [k][r]: column k, row r (kQrNB x kQrNB)
-    __shared__ float2 gk[kQrNB];
-    const int r = threadIdx.x;
-    for (int k = 0; k < pc; k++) {
-        if (r < k) gk[r] = make_float2(Greal[(size_t)k * pc + r], Greal[(size_t)(pc + k) * pc + r]);
-        __syncthreads();
-        double2 t = make_double2(0.0, 0.0);
-        for (int l = r; l < k; l++) {
-            const float2 trl = Ts[(size_t)l * kQrNB + r], g = gk[l];
-            const double2 u = zmul(make_double2(trl.x, trl.y), make_double2(g.x, g.y));
-            t.x += u.x;
-            t.y += u.y;
+    extern __shared__ float2 lt_smem[];
+    float2 *Ts = lt_smem;                        // T[row][col] at Ts[col * kQrNB + row]
+    float2 *Ys = lt_smem + kQrNB * kQrNB;        // G12 T2 per pair of the current level
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    auto G = [&](int r, int c) {
+        return (r < pc && c < pc) ? make_float2(Greal[(size_t)c * pc + r], Greal[(size_t)(pc + c) * pc + r])
+                                  : make_float2(0.f, 0.f);
+    };
+    for (int e = tid; e < kQrNB * kQrNB; e += kQrLarftNT) Ts[e] = make_float2(0.f, 0.f);
+    __syncthreads();
+    // leaves: warp w < kQrNB / kQrLeafT forms leaf w (lane r = row)
+    if (warp < kQrNB / kQrLeafT) {
+        const int o = warp * kQrLeafT, r = lane;
+        for (int k = 0; k < kQrLeafT; k++) {
+            const float2 tk = o + k < pc ? tau[o + k] : make_float2(0.f, 0.f);
+            float2 t = make_float2(0.f, 0.f);
+            if (r < k)
+                for (int l = r; l < k; l++) {
+                    const float2 trl = Ts[(size_t)(o + l) * kQrNB + o + r], g = G(o + l, o + k);
+                    t.x = fmaf(trl.x, g.x, fmaf(-trl.y, g.y, t.x));
+                    t.y = fmaf(trl.x, g.y, fmaf(trl.y, g.x, t.y));
+                }
+            __syncwarp();
+            if (r < k) Ts[(size_t)(o + k) * kQrNB + o + r] = make_float2(-(tk.x * t.x - tk.y * t.y), -(tk.x * t.y + tk.y * t.x));
+            else if (r == k) Ts[(size_t)(o + k) * kQrNB + o + k] = tk;
+            __syncwarp();
         }
-        const float2 tk = tau[k];
-        if (r < k) {
-            const double2 v = zmul(make_double2(-tk.x, -tk.y), t);
-            Ts[(size_t)k * kQrNB + r] = make_float2((float)v.x, (float)v.y);
-        } else if (r == k) {
-            Ts[(size_t)k * kQrNB + k] = tk;
-        } else if (r < pc) {
-            Ts[(size_t)k * kQrNB + r] = make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    for (int h = kQrLeafT; h < kQrNB; h *= 2) {
+        const int pairs = kQrNB / (2 * h), hh = h * h;
+        // Y = G12 T2 (T2 upper triangular): Y[r][c] = sum_{l <= c} G(o1 + r, o2 + l) T[o2 + l][o2 + c]
+        for (int e = tid; e < pairs * hh; e += kQrLarftNT) {
+            const int pr = e / hh, rem = e % hh, r = rem % h, c = rem / h;
+            const int o1 = 2 * pr * h, o2 = o1 + h;
+            float2 y = make_float2(0.f, 0.f);
+            for (int l = 0; l <= c; l++) {
+                const float2 g = G(o1 + r, o2 + l), t = Ts[(size_t)(o2 + c) * kQrNB + o2 + l];
+                y.x = fmaf(g.x, t.x, fmaf(-g.y, t.y, y.x));
+                y.y = fmaf(g.x, t.y, fmaf(g.y, t.x, y.y));
+            }
+            Ys[(size_t)pr * hh + (size_t)c * h + r] = y;
+        }
+        __syncthreads();
+        // T12 = -T1 Y (T1 upper triangular): T12[r][c] = -sum_{l >= r} T[o1 + r][o1 + l] Y[l][c]
+        for (int e = tid; e < pairs * hh; e += kQrLarftNT) {
+            const int pr = e / hh, rem = e % hh, r = rem % h, c = rem / h;
+            const int o1 = 2 * pr * h, o2 = o1 + h;
+            float2 t = make_float2(0.f, 0.f);
+            for (int l = r; l < h; l++) {
+                const float2 a = Ts[(size_t)(o1 + l) * kQrNB + o1 + r], y = Ys[(size_t)pr * hh + (size_t)c * h + l];
+                t.x = fmaf(a.x, y.x, fmaf(-a.y, y.y, t.x));
+                t.y = fmaf(a.x, y.y, fmaf(a.y, y.x, t.y));
+            }
+            Ts[(size_t)(o2 + c) * kQrNB + o1 + r] = make_float2(-t.x, -t.y);
         }
         __syncthreads();
     }
-    for (int k = 0; k < pc; k++)
-        if (r < pc) T[(size_t)r * kQrNB + k] = Ts[(size_t)k * kQrNB + r];
+    for (int e = tid; e < pc * pc; e += kQrLarftNT) {
+        const int r = e / pc, k = e % pc;
+        T[(size_t)r * kQrNB + k] = Ts[(size_t)k * kQrNB + r];
+    }
 }
 
 // The right-hand operand of the rank-pc update: for trailing column c, W'[:, c]
 // = T^H W[:, c] with W = V^H C = Z^H (Z = C^H V: Zreal nct x 2pc column-major,
 // [Re Z | Im Z]), i.e. W'[k, c] = conj(sum_{l <= k} T[l, k] Z[c, l]), packed
 // as rows 2k, 2k+1 = (Re, Im) of column c, scaled per column.  kQrTwCols
-// columns per CTA, thread = k.
-constexpr int kQrTwCols = 16;
+// columns per CTA with T and the CTA's rows of Z in shared memory; thread
+// (k = tid % kQrNB, group g = tid / kQrNB) forms row k of the group's
+// kQrTwPer columns (independent sums, Z values broadcast).
+constexpr int kQrTwPer = 16;
+constexpr int kQrTwGroups = 4;
+constexpr int kQrTwCols = kQrTwPer * kQrTwGroups;
+constexpr int kQrTwLdz = kQrNB + 1;
+constexpr size_t kQrTwSmem = sizeof(float2) * ((size_t)kQrNB * kQrNB + (size_t)kQrTwCols * kQrTwLdz);
 template <int P>
-__global__ void qr_pack_tw_kernel(int nct, int pc, const float *__restrict__ Zreal, const float2 *__restrict__ T,
-                                  int Kp, int ncols_pad, __half *__restrict__ planes, float *__restrict__ col_inv) {
-    __shared__ float2 z[kQrNB];
-    __shared__ float red[32];
-    const int k = threadIdx.x;
-    const size_t ps = (size_t)ncols_pad * Kp;
-    for (int cc = 0; cc < kQrTwCols; cc++) {
-        const int c = blockIdx.x * kQrTwCols + cc;
-        if (c >= nct) break;   // uniform over the CTA
-        if (k < pc) z[k] = make_float2(Zreal[(size_t)k * nct + c], Zreal[(size_t)(pc + k) * nct + c]);
-        __syncthreads();
-        float2 y = make_float2(0.f, 0.f);
-        if (k < pc)
-            for (int l = 0; l <= k; l++) {
-                const float2 u = cmul(T[(size_t)l * kQrNB + k], z[l]);
-                y.x += u.x;
-                y.y += u.y;
+__global__ void __launch_bounds__(kQrNB * kQrTwGroups)
+qr_pack_tw_kernel(int nct, int pc, const float *__restrict__ Zreal, const float2 *__restrict__ T, int Kp,
+                  int ncols_pad, __half *__restrict__ planes, float *__restrict__ col_inv) {
+    extern __shared__ float2 tw_smem[];
+    float2 *Ts = tw_smem;                         // T[l][k] (row-major, ld kQrNB)
+    float2 *zs = tw_smem + kQrNB * kQrNB;         // Z[c0 + c][l] as zs[c * kQrTwLdz + l]
+    __shared__ float red[kQrTwGroups][kQrNB / 32][kQrTwPer];
+    const int tid = threadIdx.x, k = tid % kQrNB, g = tid / kQrNB, lane = tid & 31, wg = k >> 5;
+    const int c0 = blockIdx.x * kQrTwCols;
+    for (int e = tid; e < pc * kQrNB; e += blockDim.x) Ts[e] = T[e];
+    for (int e = tid; e < pc * kQrTwCols; e += blockDim.x) {
+        const int c = e % kQrTwCols, l = e / kQrTwCols;
+        float2 z = make_float2(0.f, 0.f);
+        if (c0 + c < nct) z = make_float2(Zreal[(size_t)l * nct + c0 + c], Zreal[(size_t)(pc + l) * nct + c0 + c]);
+        zs[c * kQrTwLdz + l] = z;
+    }
+    __syncthreads();
+    float2 y[kQrTwPer];
+#pragma unroll
+    for (int j = 0; j < kQrTwPer; j++) y[j] = make_float2(0.f, 0.f);
+    const float2 *zg = zs + (size_t)(g * kQrTwPer) * kQrTwLdz;
+    if (k < pc)
+        for (int l = 0; l <= k; l++) {
+            const float2 t = Ts[l * kQrNB + k];
+#pragma unroll
+            for (int j = 0; j < kQrTwPer; j++) {
+                const float2 z = zg[j * kQrTwLdz + l];
+                y[j].x = fmaf(t.x, z.x, fmaf(-t.y, z.y, y[j].x));
+                y[j].y = fmaf(t.x, z.y, fmaf(t.y, z.x, y[j].y));
             }
-        y.y = -y.y;   // the conjugate
-        const float sc = pow2_scale(block_max(fmaxf(fabsf(y.x), fabsf(y.y)), red));
+        }
+    // per column, the largest |part| over the kQrNB rows (warp, then the
+    // group's warps)
+#pragma unroll
+    for (int j = 0; j < kQrTwPer; j++) {
+        float v = fmaxf(fabsf(y[j].x), fabsf(y[j].y));
+        for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (lane == 0) red[g][wg][j] = v;
+    }
+    __syncthreads();
+    const size_t ps = (size_t)ncols_pad * Kp;
+#pragma unroll
+    for (int j = 0; j < kQrTwPer; j++) {
+        const int c = c0 + g * kQrTwPer + j;
+        if (c >= nct) break;
+        float mx = 0.f;
+#pragma unroll
+        for (int w = 0; w < kQrNB / 32; w++) mx = fmaxf(mx, red[g][w][j]);
+        const float sc = pow2_scale(mx);
         if (k == 0) col_inv[c] = 1.f / sc;
-        if (k < pc) put_parts<P>(planes, ps, (size_t)c * Kp + 2 * k, y.x * sc, y.y * sc);
+        if (k < pc) put_parts<P>(planes, ps, (size_t)c * Kp + 2 * k, y[j].x * sc, -y[j].y * sc);   // the conjugate
         else if (2 * k < Kp) put_parts<P>(planes, ps, (size_t)c * Kp + 2 * k, 0.f, 0.f);
-        __syncthreads();
     }
 }
 
 // ---- triangular solves with the FP32 factor R (upper triangle of Q[0:n,
-// 0:n]) in FP64 arithmetic, blocks of kQrTB rows ----
+// 0:n]) in FP32, blocks of kQrTB rows, one launch per block ----
+//
+// The inverses of R's diagonal blocks are formed once per factorisation
+// (qr_diag_inv_kernel), so that solving a block is a matrix-vector product
+// rather than a chain of kQrTB dependent steps.
+//
+// Back substitution R x = y, block b = rows [b0, b1), the block solved
+// before it [b1, b2) (empty for the last block).  CTA 0 subtracts
+// R[b0:b1, b1:b2] x[b1:b2] from its rows and multiplies by the block's
+// inverse; the other CTAs subtract R[0:b0, b1:b2] x[b1:b2] from rows
+// [0, b0).  So when block b is solved, every block after it has been
+// subtracted from its rows: block b + 1 in this launch, the others in
+// theirs.  Forward substitution R^H x = y mirrors it (previous block
+// [bp, b0), the other CTAs updating rows [b1, n), the inverse's conjugate
+// transpose).  In place on X (float2, column s at X + s ldx; grid.y =
+// columns).  R's diagonal is nonzero (a Householder beta, real, of the
+// magnitude of the column it came from).
+constexpr int kQrTsNT = 256;
+constexpr int kQrTsP = kQrTsNT / kQrTB;   // partial sums per row in CTA 0
+static_assert(kQrTsNT % kQrTB == 0, "CTA 0 splits the block's columns evenly");
 
-// Back substitution on the diagonal block [b0, b1): X[b0:b1, s] from
-// Y[b0:b1, s] (in place).  One CTA (kQrTB threads) per right-hand side.
-__global__ void qr_trsv_back_diag_kernel(int b0, int b1, const float2 *__restrict__ Q, size_t ldq, double2 *X,
-                                         size_t ldx) {
-    __shared__ double2 xk;
-    __shared__ float2 Rb[kQrTB][kQrTB + 1];   // R[b0 + row][b0 + col] as [col][row]
-    double2 *x = X + (size_t)blockIdx.x * ldx;
-    const int nbk = b1 - b0;
-    for (int c = 0; c < nbk; c++)
-        if ((int)threadIdx.x < nbk) Rb[c][threadIdx.x] = Q[(size_t)(b0 + c) * ldq + b0 + threadIdx.x];
+// 1 / r with the division scaled by the larger part of r.
+__device__ __forceinline__ float2 qr_crecip(float2 r) {
+    const float s = fmaxf(fabsf(r.x), fabsf(r.y));
+    const float rx = r.x / s, ry = r.y / s;
+    const float inv = 1.f / (s * (rx * rx + ry * ry));
+    return make_float2(rx * inv, -ry * inv);
+}
+
+// Dinv + b kQrTB^2 (column-major: element (row, col) at col kQrTB + row) =
+// the inverse of R's diagonal block b, zero outside the block's nbk x nbk
+// upper triangle; one CTA of kQrTB threads per block, thread j forming
+// column j by back substitution (R_bb X = I).  R is read through the cache
+// (every thread reads the same entry at each step); the columns sit in
+// shared memory as Xs[row][col] (consecutive threads, consecutive words).
+__global__ void __launch_bounds__(kQrTB)
+qr_diag_inv_kernel(int n, const float2 *__restrict__ Q, size_t ldq, float2 *__restrict__ Dinv) {
+    __shared__ float2 Xs[kQrTB][kQrTB];
+    __shared__ float2 rinv[kQrTB];
+    const int b0 = blockIdx.x * kQrTB, nbk = min(kQrTB, n - b0), j = threadIdx.x;
+    const float2 *Rb = Q + (size_t)b0 * ldq + b0;   // R[b0 + i][b0 + l] at Rb[l ldq + i]
+    for (int i = 0; i < kQrTB; i++) Xs[i][j] = make_float2(0.f, 0.f);
+    if (j < nbk) rinv[j] = qr_crecip(Rb[(size_t)j * ldq + j]);
     __syncthreads();
-    const int i = b0 + threadIdx.x;
-    double2 y = i < b1 ? x[i] : make_double2(0.0, 0.0);
-    for (int k = b1 - 1; k >= b0; k--) {
-        if (i == k) {
-            const float2 rk = Rb[k - b0][k - b0];
-            const double d = (double)rk.x * rk.x + (double)rk.y * rk.y;
-            y = make_double2((y.x * rk.x + y.y * rk.y) / d, (y.y * rk.x - y.x * rk.y) / d);   // y / r_kk
-            xk = y;
+    if (j < nbk) {
+        Xs[j][j] = rinv[j];
+        for (int i = j - 1; i >= 0; i--) {
+            float2 t = make_float2(0.f, 0.f);
+            for (int l = i + 1; l <= j; l++) {
+                const float2 r = __ldg(Rb + (size_t)l * ldq + i), x = Xs[l][j];
+                t.x = fmaf(r.x, x.x, fmaf(-r.y, x.y, t.x));
+                t.y = fmaf(r.x, x.y, fmaf(r.y, x.x, t.y));
+            }
+            const float2 ri = rinv[i];
+            Xs[i][j] = make_float2(-(ri.x * t.x - ri.y * t.y), -(ri.x * t.y + ri.y * t.x));
         }
-        __syncthreads();
-        if (i < k) {
-            const float2 r = Rb[k - b0][i - b0];
-            const double2 u = zmul(make_double2(r.x, r.y), xk);
-            y.x -= u.x;
-            y.y -= u.y;
-        }
-        __syncthreads();
     }
-    if (i < b1) x[i] = y;
-}
-
-// Y[0:b0, s] -= R[0:b0, b0:b1] X[b0:b1, s]; grid (ceil(b0/256), S).
-__global__ void qr_trsv_back_update_kernel(int b0, int b1, const float2 *__restrict__ Q, size_t ldq, double2 *X,
-                                           size_t ldx) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double2 *x = X + (size_t)blockIdx.y * ldx;
-    if (i >= b0) return;
-    double2 y = x[i];
-    for (int k = b0; k < b1; k++) {
-        const float2 r = Q[(size_t)k * ldq + i];
-        const double2 u = zmul(make_double2(r.x, r.y), x[k]);
-        y.x -= u.x;
-        y.y -= u.y;
-    }
-    x[i] = y;
-}
-
-// Forward substitution with R^H on the diagonal block [b0, b1) (in place).
-__global__ void qr_trsv_fwd_diag_kernel(int b0, int b1, const float2 *__restrict__ Q, size_t ldq, double2 *X,
-                                        size_t ldx) {
-    __shared__ double2 xk;
-    __shared__ float2 Rb[kQrTB][kQrTB + 1];   // R[b0 + row][b0 + col] as [col][row]
-    double2 *x = X + (size_t)blockIdx.x * ldx;
-    const int nbk = b1 - b0;
-    for (int c = 0; c < nbk; c++)
-        if ((int)threadIdx.x < nbk) Rb[c][threadIdx.x] = Q[(size_t)(b0 + c) * ldq + b0 + threadIdx.x];
     __syncthreads();
-    const int i = b0 + threadIdx.x;
-    double2 y = i < b1 ? x[i] : make_double2(0.0, 0.0);
-    for (int k = b0; k < b1; k++) {
-        if (i == k) {
-            const float2 rk = Rb[k - b0][k - b0];                      // conj(r_kk) divides
-            const double d = (double)rk.x * rk.x + (double)rk.y * rk.y;
-            y = make_double2((y.x * rk.x - y.y * rk.y) / d, (y.y * rk.x + y.x * rk.y) / d);
-            xk = y;
-        }
-        __syncthreads();
-        if (i > k && i < b1) {
-            const float2 r = Rb[i - b0][k - b0];                       // (R^H)_{ik} = conj(R_ki)
-            const double2 u = zjmul(make_double2(r.x, r.y), xk);
-            y.x -= u.x;
-            y.y -= u.y;
-        }
-        __syncthreads();
-    }
-    if (i < b1) x[i] = y;
+    float2 *D = Dinv + (size_t)blockIdx.x * kQrTB * kQrTB;
+    for (int c = 0; c < kQrTB; c++) D[(size_t)c * kQrTB + j] = Xs[j][c];
 }
 
-// Y[b1:n, s] -= (R[b0:b1, b1:n])^H X[b0:b1, s]: one warp per row i, lanes over
-// the block's k (R's column i is contiguous in k).
-__global__ void qr_trsv_fwd_update_kernel(int b0, int b1, int n, const float2 *__restrict__ Q, size_t ldq,
-                                          double2 *X, size_t ldx) {
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    const int i = b1 + warp;
-    double2 *x = X + (size_t)blockIdx.y * ldx;
-    if (i >= n) return;
-    double2 acc = make_double2(0.0, 0.0);
-    for (int k = b0 + lane; k < b1; k += 32) {
-        const float2 r = Q[(size_t)i * ldq + k];
-        const double2 u = zjmul(make_double2(r.x, r.y), x[k]);
-        acc.x += u.x;
-        acc.y += u.y;
+__global__ void __launch_bounds__(kQrTsNT)
+qr_trsv_back_kernel(int b0, int b1, int b2, const float2 *__restrict__ Q, size_t ldq,
+                    const float2 *__restrict__ Dinv, float2 *X, size_t ldx) {
+    float2 *x = X + (size_t)blockIdx.y * ldx;
+    const int tid = threadIdx.x;
+    if (blockIdx.x > 0) {
+        const int i = (blockIdx.x - 1) * kQrTsNT + tid;
+        if (i >= b0 || b2 <= b1) return;
+        float2 acc = x[i];
+        for (int k = b1; k < b2; k++) {
+            const float2 r = Q[(size_t)k * ldq + i], xk = x[k];
+            acc.x -= r.x * xk.x - r.y * xk.y;
+            acc.y -= r.x * xk.y + r.y * xk.x;
+        }
+        x[i] = acc;
+        return;
     }
-    for (int o = 16; o > 0; o >>= 1) {
-        acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
-        acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+    __shared__ float2 xs[kQrTB], ys[kQrTB];
+    __shared__ float2 part[kQrTsP][kQrTB];
+    const int nbk = b1 - b0, np = b2 - b1, row = tid % kQrTB, p = tid / kQrTB;
+    for (int t = tid; t < np; t += kQrTsNT) xs[t] = x[b1 + t];
+    __syncthreads();
+    {
+        float2 acc = make_float2(0.f, 0.f);
+        if (row < nbk)
+            for (int k = p; k < np; k += kQrTsP) {
+                const float2 r = Q[(size_t)(b1 + k) * ldq + b0 + row], xk = xs[k];
+                acc.x += r.x * xk.x - r.y * xk.y;
+                acc.y += r.x * xk.y + r.y * xk.x;
+            }
+        part[p][row] = acc;
     }
-    if (lane == 0) {
-        x[i].x -= acc.x;
-        x[i].y -= acc.y;
+    __syncthreads();
+    if (tid < kQrTB) {
+        float2 y = make_float2(0.f, 0.f);
+        if (tid < nbk) {
+            y = x[b0 + tid];
+#pragma unroll
+            for (int q = 0; q < kQrTsP; q++) {
+                y.x -= part[q][tid].x;
+                y.y -= part[q][tid].y;
+            }
+        }
+        ys[tid] = y;
+    }
+    __syncthreads();
+    // x_b = Dinv_b y: thread (row, p) over the columns c = p mod kQrTsP
+    const float2 *D = Dinv + (size_t)(b0 / kQrTB) * kQrTB * kQrTB;
+    float2 acc = make_float2(0.f, 0.f);
+    for (int c = p; c < nbk; c += kQrTsP) {
+        const float2 d = D[(size_t)c * kQrTB + row], yc = ys[c];
+        acc.x += d.x * yc.x - d.y * yc.y;
+        acc.y += d.x * yc.y + d.y * yc.x;
+    }
+    part[p][row] = acc;
+    __syncthreads();
+    if (tid < nbk) {
+        float2 t = part[0][tid];
+#pragma unroll
+        for (int q = 1; q < kQrTsP; q++) {
+            t.x += part[q][tid].x;
+            t.y += part[q][tid].y;
+        }
+        x[b0 + tid] = t;
     }
 }
 
+__global__ void __launch_bounds__(kQrTsNT)
+qr_trsv_fwd_kernel(int bp, int b0, int b1, int n, const float2 *__restrict__ Q, size_t ldq,
+                   const float2 *__restrict__ Dinv, float2 *X, size_t ldx) {
+    float2 *x = X + (size_t)blockIdx.y * ldx;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int np = b0 - bp;
+    if (blockIdx.x > 0) {
+        // one warp per row i >= b1: y_i -= sum_k conj(R[k, i]) x_k over the
+        // previous block (R's column i is contiguous in k)
+        const int i = b1 + (blockIdx.x - 1) * (kQrTsNT / 32) + warp;
+        if (i >= n || np <= 0) return;
+        float2 acc = make_float2(0.f, 0.f);
+        for (int k = lane; k < np; k += 32) {
+            const float2 r = Q[(size_t)i * ldq + bp + k], xk = x[bp + k];
+            acc.x += r.x * xk.x + r.y * xk.y;
+            acc.y += r.x * xk.y - r.y * xk.x;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+            acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+        }
+        if (lane == 0) {
+            x[i].x -= acc.x;
+            x[i].y -= acc.y;
+        }
+        return;
+    }
+    __shared__ float2 xs[kQrTB], ys[kQrTB];
+    __shared__ float2 part[kQrTB];
+    const int nbk = b1 - b0;
+    for (int t = tid; t < np; t += kQrTsNT) xs[t] = x[bp + t];
+    __syncthreads();
+    // rows of this block: warp w takes rows w, w + 8, ...; lanes over k
+    for (int row = warp; row < kQrTB; row += kQrTsNT / 32) {
+        float2 acc = make_float2(0.f, 0.f);
+        if (row < nbk)
+            for (int k = lane; k < np; k += 32) {
+                const float2 r = Q[(size_t)(b0 + row) * ldq + bp + k], xk = xs[k];
+                acc.x += r.x * xk.x + r.y * xk.y;
+                acc.y += r.x * xk.y - r.y * xk.x;
+            }
+        for (int o = 16; o > 0; o >>= 1) {
+            acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+            acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+        }
+        if (lane == 0) part[row] = acc;
+    }
+    __syncthreads();
+    if (tid < kQrTB) {
+        float2 y = make_float2(0.f, 0.f);
+        if (tid < nbk) {
+            y = x[b0 + tid];
+            y.x -= part[tid].x;
+            y.y -= part[tid].y;
+        }
+        ys[tid] = y;
+    }
+    __syncthreads();
+    // x_b = Dinv_b^H y: warp per row, lanes over c (row r of Dinv^H is the
+    // conjugate of column r of Dinv, contiguous)
+    const float2 *D = Dinv + (size_t)(b0 / kQrTB) * kQrTB * kQrTB;
+    for (int row = warp; row < nbk; row += kQrTsNT / 32) {
+        float2 acc = make_float2(0.f, 0.f);
+        for (int c = lane; c < nbk; c += 32) {
+            const float2 d = D[(size_t)row * kQrTB + c], yc = ys[c];
+            acc.x += d.x * yc.x + d.y * yc.y;
+            acc.y += d.x * yc.y - d.y * yc.x;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+            acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+        }
+        if (lane == 0) x[b0 + row] = acc;
+    }
+}
+
+// X (FP64, n x S) from the solved FP32 columns (ld ldq).
 __global__ void qr_take_rhs_kernel(int n, int S, const float2 *__restrict__ Qb, size_t ldq, double2 *__restrict__ X) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
     if (i < n) {
@@ -663,34 +836,48 @@ __global__ void qr_take_rhs_kernel(int n, int S, const float2 *__restrict__ Qb, 
     }
 }
 
-__global__ void qr_axpy_kernel(int n, const double2 *__restrict__ d, double2 *__restrict__ x) {
+// gf = g 2^-e (FP32) with 2^e the power of two at or below *nrm (> 0), so the
+// FP32 solves run on entries of order one whatever the residual's size.
+__global__ void qr_g_to_f32_kernel(int n, const double2 *__restrict__ g, const double *__restrict__ nrm,
+                                   float2 *__restrict__ gf) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) {
-        x[i].x += d[i].x;
-        x[i].y += d[i].y;
+        const double s = scalbn(1.0, -ilogb(*nrm));
+        gf[i] = make_float2((float)(g[i].x * s), (float)(g[i].y * s));
     }
 }
 
-// R X = Y (back) or R^H X = Y (forward) for the S columns of X (ld ldx).
-void qr_trsv(bool forward, int n, int S, const float2 *Q, size_t ldq, double2 *X, size_t ldx, cudaStream_t st) {
+// x += d 2^e (the scale qr_g_to_f32_kernel took off).
+__global__ void qr_axpy_scaled_kernel(int n, const float2 *__restrict__ d, const double *__restrict__ nrm,
+                                      double2 *__restrict__ x) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const double s = scalbn(1.0, ilogb(*nrm));
+        x[i].x += (double)d[i].x * s;
+        x[i].y += (double)d[i].y * s;
+    }
+}
+
+// R X = Y (back) or R^H X = Y (forward) for the S columns of X (ld ldx);
+// Dinv from qr_diag_inv_kernel.
+void qr_trsv(bool forward, int n, int S, const float2 *Q, size_t ldq, const float2 *Dinv, float2 *X, size_t ldx,
+             cudaStream_t st) {
     const int nb = (n + kQrTB - 1) / kQrTB;
     if (!forward) {
         for (int b = nb - 1; b >= 0; b--) {
-            const int b0 = b * kQrTB, b1 = std::min(n, b0 + kQrTB);
-            qr_trsv_back_diag_kernel<<<S, kQrTB, 0, st>>>(b0, b1, Q, ldq, X, ldx);
-            if (b0 > 0)
-                qr_trsv_back_update_kernel<<<dim3((b0 + 255) / 256, S), 256, 0, st>>>(b0, b1, Q, ldq, X, ldx);
-            count_launch(b0 > 0 ? 2 : 1);
+            const int b0 = b * kQrTB, b1 = std::min(n, b0 + kQrTB), b2 = b == nb - 1 ? b1 : std::min(n, b1 + kQrTB);
+            const int others = b2 > b1 ? (b0 + kQrTsNT - 1) / kQrTsNT : 0;
+            qr_trsv_back_kernel<<<dim3(1 + others, S), kQrTsNT, 0, st>>>(b0, b1, b2, Q, ldq, Dinv, X, ldx);
         }
     } else {
+        constexpr int rows_per_cta = kQrTsNT / 32;
         for (int b = 0; b < nb; b++) {
-            const int b0 = b * kQrTB, b1 = std::min(n, b0 + kQrTB);
-            qr_trsv_fwd_diag_kernel<<<S, kQrTB, 0, st>>>(b0, b1, Q, ldq, X, ldx);
-            if (b1 < n)
-                qr_trsv_fwd_update_kernel<<<dim3((n - b1 + 7) / 8, S), 256, 0, st>>>(b0, b1, n, Q, ldq, X, ldx);
-            count_launch(b1 < n ? 2 : 1);
+            const int b0 = b * kQrTB, b1 = std::min(n, b0 + kQrTB), bp = b == 0 ? b0 : b0 - kQrTB;
+            const int others = b0 > bp ? (n - b1 + rows_per_cta - 1) / rows_per_cta : 0;
+            qr_trsv_fwd_kernel<<<dim3(1 + others, S), kQrTsNT, 0, st>>>(bp, b0, b1, n, Q, ldq, Dinv, X, ldx);
         }
     }
+    count_launch(nb);
     KERNEL_CHECK();
 }
 
@@ -710,7 +897,10 @@ int qr_cluster_size(size_t smem16) {
             err = cudaFuncSetAttribute(qr_panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, maxs);
         if (err == cudaSuccess)
             err = cudaFuncSetAttribute(qr_larft_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)(sizeof(float2) * kQrNB * kQrNB));
+                                       (int)kQrLarftSmem);
+        if (err == cudaSuccess)
+            err = cudaFuncSetAttribute(qr_pack_tw_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)kQrTwSmem);
         nonportable = cudaFuncSetAttribute(qr_panel_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
                       cudaSuccess;
         cudaGetLastError();
@@ -769,6 +959,7 @@ void bem_solver_s::solve_qr_tc(bem_solve_info_t *info) {
     if (pf) qt_part.ensure(sizeof(float) * pf);
     const size_t part_floats = qt_part.bytes / sizeof(float);
     qt_scal.ensure(sizeof(float) * 8);
+    qt_dinv.ensure(sizeof(float2) * (size_t)((n + kQrTB - 1) / kQrTB) * kQrTB * kQrTB);
     d_status.ensure(4 * sizeof(int));
     int *status = d_status.as<int>() + 1;
     CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), stream));
@@ -799,7 +990,8 @@ void bem_solver_s::solve_qr_tc(bem_solve_info_t *info) {
         return (size_t)v;
     }();
     auto smem_for = [](int rows, int cl) { return sizeof(float2) * PanelLayout((rows + cl - 1) / cl).total; };
-    const int CL = smem_for(m, 16) <= smax ? qr_cluster_size(smem_for(m, 16)) : 8;
+    const int CL16 = qr_cluster_size(smem_for(m, 16));   // also sets the kernels' shared-memory limits
+    const int CL = smem_for(m, 16) <= smax ? CL16 : 8;
     if (smem_for(m, CL) > smax)
         BEM_FAIL(BEM_ERR_TOO_LARGE, "QR_TC: " + std::to_string(m) + " rows do not fit the panel cluster's shared memory");
     for (int j0 = 0; j0 < n; j0 += kQrNB) {
@@ -834,7 +1026,7 @@ void bem_solver_s::solve_qr_tc(bem_solve_info_t *info) {
             // G = V^H V (pc x pc): conj(V^T) V with V^T's rows the columns of Vf
             tc_gemm(reinterpret_cast<const float *>(qt_v.p), 2 * ldv, false, pc, 2 * mr, sc + 2, opv, G, pc,
                     qt_part.as<float>(), part_floats, status, stream);
-            qr_larft_kernel<<<1, kQrNB, sizeof(float2) * kQrNB * kQrNB, stream>>>(pc, G, q_tau.as<float2>() + j0, T);
+            qr_larft_kernel<<<1, kQrLarftNT, kQrLarftSmem, stream>>>(pc, G, q_tau.as<float2>() + j0, T);
             count_launch(2);
         }
         {
@@ -844,7 +1036,7 @@ void bem_solver_s::solve_qr_tc(bem_solve_info_t *info) {
             tc_gemm(C, 2 * ldq, false, nct, 2 * mr, sc, opv, qt_z.as<float>(), nct, qt_part.as<float>(), part_floats,
                     status, stream);
             TcOperand opw = tc_operand_view(qt_opw.p, 2 * pc, nct, 2);
-            qr_pack_tw_kernel<2><<<(nct + kQrTwCols - 1) / kQrTwCols, kQrNB, 0, stream>>>(
+            qr_pack_tw_kernel<2><<<(nct + kQrTwCols - 1) / kQrTwCols, kQrNB * kQrTwGroups, kQrTwSmem, stream>>>(
                 nct, pc, qt_z.as<float>(), T, opw.Kp, opw.ncols_pad, opw.planes, opw.col_inv);
             qr_vrr_kernel<<<mr, kQrNB, 0, stream>>>(mr, pc, qt_v.as<float2>(), ldv, qt_vrr.as<float>(), ldk);
             count_launch(2);
@@ -857,9 +1049,11 @@ void bem_solver_s::solve_qr_tc(bem_solve_info_t *info) {
     double2 *X = d_x.as<double2>();
     {
         BEM_PROF("qr_trsv", stream);
+        qr_diag_inv_kernel<<<(n + kQrTB - 1) / kQrTB, kQrTB, 0, stream>>>(n, Q, ldq, qt_dinv.as<float2>());
+        count_launch();
+        qr_trsv(false, n, S, Q, ldq, qt_dinv.as<float2>(), Q + (size_t)n * ldq, ldq, stream);   // in place on (Q^H B)[0:n]
         qr_take_rhs_kernel<<<dim3((n + 255) / 256, S), 256, 0, stream>>>(n, S, Q + (size_t)n * ldq, ldq, X);
         count_launch();
-        qr_trsv(false, n, S, Q, ldq, X, n, stream);
     }
     // FP64 refinement through the semi-normal equations with the FP32 factor
     w_r.ensure(sizeof(double2) * (size_t)m);
@@ -904,10 +1098,14 @@ void bem_solver_s::solve_qr_tc(bem_solve_info_t *info) {
                 break;
             }
             prev = rel;
-            qr_trsv(true, n, 1, Q, ldq, w_gv.as<double2>(), n, stream);    // R^H y = g
-            qr_trsv(false, n, 1, Q, ldq, w_gv.as<double2>(), n, stream);   // R d = y
-            qr_axpy_kernel<<<(n + 255) / 256, 256, 0, stream>>>(n, w_gv.as<double2>(), x);
-            count_launch();
+            // R^H y = g, R d = y in FP32 on g scaled to order one (the free
+            // Z buffer), then x += d
+            float2 *gf = qt_z.as<float2>();
+            qr_g_to_f32_kernel<<<(n + 255) / 256, 256, 0, stream>>>(n, w_gv.as<double2>(), scal + 1, gf);
+            qr_trsv(true, n, 1, Q, ldq, qt_dinv.as<float2>(), gf, n, stream);
+            qr_trsv(false, n, 1, Q, ldq, qt_dinv.as<float2>(), gf, n, stream);
+            qr_axpy_scaled_kernel<<<(n + 255) / 256, 256, 0, stream>>>(n, gf, scal + 1, x);
+            count_launch(2);
         }
         steps_max = std::max(steps_max, it);
         worst = std::max(worst, rel);

@@ -718,6 +718,7 @@ size_t bem_solver_s::estimate_bytes(int N, int E, int M, int S, int method, cons
              tc_operand_bytes((int)(2 * nb), (int)(n + s), 2) + 4 * tc_gemm_part_floats_bound((int)(2 * r), (int)(n + s));
         b += 16 * r + 16 * n + 8 * (2 * std::max(n, r) + 2) +
              16 * n * (size_t)std::max(gemv_h_splits((int)r, N), gemv_h_f64_splits((int)r, N));
+        b += 8 * (n + 64) * 64;                                              // diagonal-block inverses
     } else {
         b += 8 * r * n + 8 * r * s + 64 * n + (64u << 20);               // QR copy, tau, library workspace
     }

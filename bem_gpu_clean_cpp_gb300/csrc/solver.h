@@ -119,7 +119,7 @@ struct bem_solver_s {
     // tensor-core QR (solve_qr_tc): the panel's V and its interleaved form, T
     // and V^H V, Z = C^H V, the packed right-hand operands, split-K partial
     // sums, scales
-    bem::DevMem qt_v, qt_vrr, qt_t, qt_z, qt_opv, qt_opw, qt_part, qt_scal;
+    bem::DevMem qt_v, qt_vrr, qt_t, qt_z, qt_opv, qt_opw, qt_part, qt_scal, qt_dinv;
     // field workspace
     bem::DevMem f_rows_f, f_rows_d, f_part, f_near, f_out, f_u;
 

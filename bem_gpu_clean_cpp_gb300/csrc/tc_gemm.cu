@@ -309,6 +309,14 @@ tc_gemm_kernel(const float *__restrict__ A, size_t lda, int M, int K, const floa
         }
         // epilogue
         const int quad = warp & 3, half = (warp - 2) >> 2;
+        const int row = m0 + 32 * quad + lane;
+        constexpr int HALF_N = NT / 2;
+        if (accum && row < M && !*abort_v) {
+            // C -= ...: bring this thread's C lines into L2 while the last
+            // MMAs run (a warp's 32 rows of one column are one or two lines)
+            for (int c = half * HALF_N; c < (half + 1) * HALF_N; c++)
+                if (n0 + c < ncols) asm volatile("prefetch.global.L2 [%0];" ::"l"(Cz + (size_t)(n0 + c) * ldc + row));
+        }
         bool ok = true;
         if (nkb > 0) {
             ok = tc_wait(&accum_full, 0u, abort_v);
@@ -316,9 +324,17 @@ tc_gemm_kernel(const float *__restrict__ A, size_t lda, int M, int K, const floa
         }
         tc_fence_after();
         const float inv_a = a_scale[1];
-        const int row = m0 + 32 * quad + lane;
-        constexpr int HALF_N = NT / 2;
         for (int c = half * HALF_N; c < (half + 1) * HALF_N; c += 16) {
+            // the 16 old values are loaded together (in flight at once)
+            // before any store, rather than one load-store round trip each
+            float old[16];
+#pragma unroll
+            for (int j = 0; j < 16; j++) old[j] = 0.f;
+            if (accum && ok && !*abort_v && row < M) {
+#pragma unroll
+                for (int j = 0; j < 16; j++)
+                    if (n0 + c + j < ncols) old[j] = Cz[(size_t)(n0 + c + j) * ldc + row];
+            }
             uint32_t v[16];
             if (nkb > 0) {
                 tmem_ld16(tmem + ((uint32_t)(32 * quad) << 16) + (uint32_t)c, v);
@@ -330,8 +346,7 @@ tc_gemm_kernel(const float *__restrict__ A, size_t lda, int M, int K, const floa
                     const int n = n0 + c + j;
                     if (n < ncols) {
                         const float r = nkb > 0 ? __uint_as_float(v[j]) * inv_a * col_inv[n] : 0.f;
-                        float *dst = Cz + (size_t)n * ldc + row;
-                        *dst = accum ? *dst - r : r;
+                        Cz[(size_t)n * ldc + row] = accum ? old[j] - r : r;
                     }
                 }
             }
@@ -463,9 +478,11 @@ int tc_nt(int ncols, int P) {
 
 // Splits of the K blocks: fill whole waves of one CTA per SM, at least 8 K
 // blocks per split, at most 8 CTAs per SM in all (bounds the partial sums),
-// fewer splits on near ties.
+// fewer splits on near ties.  When even the most splits leave part of one
+// wave idle (a few output tiles over a long K), the most are taken.
 int tc_splits(long long tiles, int nkb, int sms) {
     const int kmax = std::max(1, std::min({kTcMaxSplits, nkb / 8, (int)std::max(1LL, 8LL * sms / tiles)}));
+    if (tiles * kmax <= sms) return kmax;
     int best = 1;
     double best_score = -1.0;
     for (int k = 1; k <= kmax; k++) {

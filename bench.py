@@ -72,14 +72,20 @@ def parse_args():
     ap.add_argument("--requests", type=int, default=40, help="serve: requests in the stream")
     ap.add_argument("--gemm", type=int, default=-1, choices=[-1, 0, 1, 2, 3, 4, 5, 6],
                     help="block-solve GEMM mode (-1 auto, 0 FP32, 1 split-BF16 FP32-accurate, 2 TF32, 3 TF32x3, "
-                         "4 TF32x3 in the 3M form, 5 FP32 streaming kernels on the CUDA cores)")
+                         "4 TF32x3 in the 3M form, 5 FP32 streaming kernels on the CUDA cores, 6 tcgen05 "
+                         "tensor-core fp16 split products)")
     ap.add_argument("--far-variant", type=int, default=-1,
                     help="profile mode: fixed far-field launch shape (-1: autotuned)")
-    ap.add_argument("--mode", default="bench", choices=["bench", "profile", "cpu-validate", "products"],
+    ap.add_argument("--mode", default="bench",
+                    choices=["bench", "profile", "cpu-validate", "products", "qr-tc", "tc-gemm"],
                     help="profile: one warm-up solve and one more solve, nothing timed (for ncu captures); "
                          "cpu-validate: the CPU legs' sample extrapolation against full FP64 CPU solves of "
                          "the workload at icosphere subdivisions 3 and 4; products: the block solve's product "
-                         "pair per GEMM mode at 16, 64 and 256 sources on the rhs configuration's matrix")
+                         "pair per GEMM mode at 16, 64 and 256 sources on the rhs configuration's matrix; "
+                         "qr-tc: the tensor-core QR least squares on the workload's c64 system (--steps solves "
+                         "after one warm-up; phase times of the last, error against the FP64 QR); tc-gemm: "
+                         "the tensor-core GEMM on 4096 x 16384 x 512 and its transposed-A twin, twice each "
+                         "(a small case for ncu captures)")
     return ap.parse_args()
 
 
@@ -378,6 +384,58 @@ def cpu_sample(pts, elems, chief, srcs, k, bc, eta, depth, threads, rows=CPU_ROW
                       f"Householder LS-QR {m_s}x{n_qr} (x{flops(R, N, S) / flops(m_s, n_qr, 1):.0f} by flop "
                       f"count); extrapolated {total:.1f} s for {S} solve(s) (assembly {t_asm:.1f} s, "
                       f"QR {t_qr:.1f} s)"}
+
+
+def run_qr_tc(args):
+    """BEM_SOLVE_QR_TC on the workload's c64 system: one warm-up solve, then
+    --steps solves; the library's phase timer on the last one, its wall time,
+    refinement steps, and the relative difference from the FP64 QR solve."""
+    import bem_gpu_clean_cpp_gb300 as bem
+    pts, elems, chief, srcs, k, bc, _ = select_workload(args)
+    s = bem.Solver(near_eta=args.eta, near_depth=args.depth)
+    s.set_geometry(pts, elems, bc=bc, chief=chief)
+    s.set_sources(srcs)
+    s.assemble(k, bem.PREC_C64)
+    s.sync()
+    info = s.solve(bem.SOLVE_QR_TC)
+    s.sync()
+    walls = []
+    for rep in range(max(1, args.steps)):
+        last = rep == max(1, args.steps) - 1
+        if last:
+            bem.profile_enable(True)
+        t0 = time.perf_counter()
+        info = s.solve(bem.SOLVE_QR_TC)
+        s.sync()
+        walls.append((time.perf_counter() - t0) * 1e3)
+    prof = {n: [c, round(t, 3)] for n, (c, t) in bem.profile_report().items()}
+    bem.profile_enable(False)
+    x_tc = s.solution()
+    s.solve(bem.SOLVE_QR)
+    x_qr = s.solution()
+    print(json.dumps({"mode": "qr-tc", "wall_ms": walls, "wall_ms_median": statistics.median(walls),
+                      "refinements": info.refinements, "rel_residual": info.rel_residual,
+                      "rel_diff_vs_fp64_qr": float(np.linalg.norm(x_tc - x_qr) / np.linalg.norm(x_qr)),
+                      "phases_ms": prof}))
+    return 0
+
+
+def run_tc_gemm(args):
+    """The tensor-core GEMM on C = A B (4096 x 16384 by 16384 x 512) and
+    C = A^T B (A 8192 x 8192, B the first 8192 rows), two parts, twice each:
+    a small steady case for ncu captures of tc_gemm_kernel."""
+    import bem_gpu_clean_cpp_gb300 as bem
+    bem.lib()
+    rng = np.random.default_rng(0)
+    M, K, N = 4096, 16384, 512
+    A = rng.standard_normal((M, K)).astype(np.float32)
+    B = rng.standard_normal((K, N)).astype(np.float32)
+    At = rng.standard_normal((K // 2, 2 * M)).astype(np.float32)
+    for _ in range(2):
+        C = bem.tc_gemm(A, B, trans=False, parts=2)
+        C2 = bem.tc_gemm(At, B[:K // 2], trans=True, parts=2)
+    print(json.dumps({"mode": "tc-gemm", "shapes": [list(C.shape), list(C2.shape)]}))
+    return 0
 
 
 def run_products(args):
@@ -1084,6 +1142,10 @@ def main():
         return run_cpu_validate(args)
     if args.mode == "products":
         return run_products(args)
+    if args.mode == "qr-tc":
+        return run_qr_tc(args)
+    if args.mode == "tc-gemm":
+        return run_tc_gemm(args)
     return run_ours(args)
 
 
