@@ -73,20 +73,21 @@ __device__ __forceinline__ float2 cjmul(float2 a, float2 b) {
 // banks), then the reduction slots.
 struct PanelLayout {
     int lds;
-    size_t leaf, ssq, dot, gram, wpart, gsum, tmat, ysum, scratch, bcast, taus, total;
+    size_t leaf, red, sums, prev, gpart, gram, wpart, gsum, tmat, ysum, scratch, taus, total;
     __host__ __device__ PanelLayout(int rb) {
         lds = ((rb + 15) / 16) * 16 + 1;
         size_t o = 0;
         leaf = o;    o += (size_t)kQrW * lds;
-        ssq = o;     o += 2 * 2;                         // [parity][ssq, alpha]
-        dot = o;     o += 2 * kQrW;                      // [parity][column]
+        red = o;     o += 2 * 2 * kQrW;                  // [parity][d_c | pivot-row x_c]: this CTA's column sums
+        sums = o;    o += 2 * kQrW;                      // the cluster's sums of red
+        prev = o;    o += 2;                             // (scal, beta) of the column whose scaling is pending
+        gpart = o;   o += 2 * kQrW * kQrW;               // two row halves of this CTA's V^H V
         gram = o;    o += kQrW * kQrW;                   // this CTA's V^H V
         wpart = o;   o += (size_t)kQrW * kQrNB;          // this CTA's V^H P (leaf x rest of the panel)
         gsum = o;    o += kQrW * kQrW;
         tmat = o;    o += kQrW * kQrW;
         ysum = o;    o += (size_t)kQrW * kQrNB;
         scratch = o; o += (kQrNT / 32) * kQrW;
-        bcast = o;   o += 4;
         taus = o;    o += kQrW;                          // this leaf's taus (every CTA forms them)
         total = o;
     }
@@ -109,17 +110,40 @@ __device__ __forceinline__ float2 cluster_sum(const Peer &peer, size_t off, size
     return t;
 }
 
-// v_k at local row i of this CTA: 0 above the pivot row g_k, 1 on it, the
-// stored vector below.
-__device__ __forceinline__ float2 vval(const float2 *L, int lds, int k, int grow, int gk, int i) {
-    if (grow < gk) return make_float2(0.f, 0.f);
-    if (grow == gk) return make_float2(1.f, 0.f);
-    return L[(size_t)k * lds + i];
+// The reflector of a column from the cluster's sums (zlarfg's convention):
+// t = |x|^2 below the pivot, a = the pivot value; beta = -sign(Re a) |x|,
+// tau = (beta - a) / beta, scal = 1 / (a - beta) (v = x scal below the
+// pivot, 1 on it).  A column that is already reduced (t = 0, Im a = 0)
+// reflects nothing: tau = scal = 0, beta = a.
+__device__ __forceinline__ void qr_reflector(float t, float2 a, float2 &tau, float2 &scal, float &beta) {
+    if (t == 0.f && a.y == 0.f) {
+        tau = make_float2(0.f, 0.f);
+        scal = make_float2(0.f, 0.f);
+        beta = a.x;
+    } else {
+        beta = -copysignf(sqrtf(a.x * a.x + a.y * a.y + t), a.x);
+        tau = make_float2((beta - a.x) / beta, -a.y / beta);
+        const float2 d = make_float2(a.x - beta, a.y);
+        const float dd = d.x * d.x + d.y * d.y;
+        scal = make_float2(d.x / dd, -d.y / dd);
+    }
 }
 
 // Factors the panel Q[j0:m, j0:j0+pc] in place (Householder vectors below the
 // diagonal, R on and above it); tau_out[0..pc) receives the taus.  One
 // cluster of gridDim.x CTAs; CTA q owns the rows j0 + q rb .. + rb - 1.
+//
+// Per column one cluster-wide reduction: from the column x as it stands
+// (before scaling), every CTA sums over its rows below the pivot g the
+// products conj(x_i) x_c[i] for the column itself (|x|^2) and the leaf's
+// later columns (d_c), and the owner of row g adds the pivot-row values
+// x_c[g].  Then every CTA forms the reflector and, with
+// v^H x_c = x_c[g] + conj(scal) d_c, updates the later columns; the column's
+// own scaling (x_i scal below the pivot, beta on it) is done while the next
+// column is being summed (those sums do not read it).  A finished leaf is
+// written back, its shared copy turned into V itself (zeros above the unit
+// diagonal), and applied to the panel's remaining columns as a block
+// reflector (I - V T V^H)^H.
 __global__ void __launch_bounds__(kQrNT, 1)
 qr_panel_kernel(float2 *__restrict__ Q, size_t ldq, int m, int j0, int pc, int rb, float2 *__restrict__ tau_out) {
     cg::cluster_group cluster = cg::this_cluster();
@@ -132,99 +156,42 @@ qr_panel_kernel(float2 *__restrict__ Q, size_t ldq, int m, int j0, int pc, int r
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int r0 = j0 + q * rb;
     const int nrows = max(0, min(rb, m - r0));
-    float2 *scratch = ps + lay.scratch, *bcast = ps + lay.bcast;
+    float2 *scratch = ps + lay.scratch;
     auto peer = [&](size_t off, int p) -> const float2 * {
         return cluster.map_shared_rank(ps + off, p);
     };
+    // thread (column c of the leaf, row slice il) in the column loop
+    const int c = tid % kQrW, il = tid / kQrW;
+    constexpr int NIL = kQrNT / kQrW;
 
     for (int l0 = 0; l0 < pc; l0 += kQrW) {
-        const int lw = min(kQrW, pc - l0);
-        // load the leaf (this CTA's rows)
-        for (int c = 0; c < lw; c++)
-            for (int i = tid; i < nrows; i += kQrNT)
-                L[(size_t)c * lds + i] = Q[(size_t)(j0 + l0 + c) * ldq + r0 + i];
+        const int lw = min(kQrW, pc - l0), G0 = j0 + l0;
+        for (int cc = 0; cc < lw; cc++)
+            for (int i = tid; i < nrows; i += kQrNT) L[(size_t)cc * lds + i] = Q[(size_t)(G0 + cc) * ldq + r0 + i];
         __syncthreads();
         for (int jj = 0; jj < lw; jj++) {
             const int par = jj & 1;
-            const int g = j0 + l0 + jj;   // pivot row
-            // (1) partial |x|^2 below the pivot, and the pivot value
-            float ssq = 0.f;
-            for (int i = tid; i < nrows; i += kQrNT)
-                if (r0 + i > g) {
-                    const float2 x = L[(size_t)jj * lds + i];
-                    ssq = fmaf(x.x, x.x, fmaf(x.y, x.y, ssq));
-                }
-            for (int o = 16; o > 0; o >>= 1) ssq += __shfl_xor_sync(0xffffffffu, ssq, o);
-            if (lane == 0) scratch[warp].x = ssq;
-            __syncthreads();
-            if (tid == 0) {
-                float t = 0.f;
-                for (int w = 0; w < kQrNT / 32; w++) t += scratch[w].x;
-                ps[lay.ssq + 2 * par] = make_float2(t, 0.f);
-                ps[lay.ssq + 2 * par + 1] = (g >= r0 && g < r0 + nrows) ? L[(size_t)jj * lds + (g - r0)]
-                                                                          : make_float2(0.f, 0.f);
-            }
-            cluster.sync();
-            // (2) every CTA forms the reflector from the cluster sums
-            if (warp == 0) {
-                float t = 0.f;
-                float2 a = make_float2(0.f, 0.f);
-                if (lane < CL) {
-                    const float2 *pp = peer(lay.ssq + 2 * par, lane);
-                    t = pp[0].x;
-                    a = pp[1];
-                }
-                for (int o = 16; o > 0; o >>= 1) {
-                    t += __shfl_xor_sync(0xffffffffu, t, o);
-                    a.x += __shfl_xor_sync(0xffffffffu, a.x, o);
-                    a.y += __shfl_xor_sync(0xffffffffu, a.y, o);
-                }
-                if (lane == 0) {
-                    float2 tau, scal;
-                    float beta;
-                    if (t == 0.f && a.y == 0.f) {
-                        tau = make_float2(0.f, 0.f);
-                        scal = make_float2(0.f, 0.f);
-                        beta = a.x;
-                    } else {
-                        beta = -copysignf(sqrtf(a.x * a.x + a.y * a.y + t), a.x);
-                        tau = make_float2((beta - a.x) / beta, -a.y / beta);
-                        const float2 d = make_float2(a.x - beta, a.y);      // scal = 1 / (alpha - beta)
-                        const float dd = d.x * d.x + d.y * d.y;
-                        scal = make_float2(d.x / dd, -d.y / dd);
-                    }
-                    bcast[0] = tau;
-                    bcast[1] = scal;
-                    bcast[2] = make_float2(beta, 0.f);
-                    ps[lay.taus + jj] = tau;
-                    if (q == 0) tau_out[l0 + jj] = tau;
-                }
-            }
-            __syncthreads();
-            const float2 tau = bcast[0], scal = bcast[1];
-            const float beta = bcast[2].x;
-            for (int i = tid; i < nrows; i += kQrNT) {
-                const int grow = r0 + i;
-                if (grow > g) L[(size_t)jj * lds + i] = cmul(L[(size_t)jj * lds + i], scal);
-                else if (grow == g) L[(size_t)jj * lds + i] = make_float2(beta, 0.f);
-            }
-            __syncthreads();
-            // (3) partial w_c = v^H x_c for the leaf's later columns
-            const int c = tid % kQrW, il = tid / kQrW;
-            constexpr int NIL = kQrNT / kQrW;
+            const int g = G0 + jj;                        // pivot row
+            const int ib = max(0, g + 1 - r0);            // first local row below the pivot
+            const bool own = g >= r0 && g < r0 + nrows;   // this CTA holds the pivot row
+            const float2 *xj = L + (size_t)jj * lds;
+            // (1) sums over this CTA's rows below the pivot; the previous
+            // column's pending scaling meanwhile
             float2 acc = make_float2(0.f, 0.f);
-            if (c > jj && c < lw) {
-                for (int i = il; i < nrows; i += NIL) {
-                    const int grow = r0 + i;
-                    if (grow >= g) {
-                        const float2 u = cjmul(vval(L, lds, jj, grow, g, i), L[(size_t)c * lds + i]);
-                        acc.x += u.x;
-                        acc.y += u.y;
-                    }
+            if (c >= jj && c < lw) {
+                const float2 *xc = L + (size_t)c * lds;
+                for (int i = ib + il; i < nrows; i += NIL) {
+                    const float2 u = cjmul(xj[i], xc[i]);
+                    acc.x += u.x;
+                    acc.y += u.y;
                 }
+            } else if (jj > 0 && c == jj - 1) {
+                const float2 sc = ps[lay.prev];
+                float2 *xp = L + (size_t)(jj - 1) * lds;
+                for (int i = max(0, g - r0) + il; i < nrows; i += NIL) xp[i] = cmul(xp[i], sc);
+                if (il == 0 && g - 1 >= r0 && g - 1 < r0 + nrows) xp[g - 1 - r0] = make_float2(ps[lay.prev + 1].x, 0.f);
             }
-            // lanes c and c + 16 share a column
-            acc.x += __shfl_xor_sync(0xffffffffu, acc.x, 16);
+            acc.x += __shfl_xor_sync(0xffffffffu, acc.x, 16);   // lanes c and c + 16 share a column
             acc.y += __shfl_xor_sync(0xffffffffu, acc.y, 16);
             if (lane < kQrW) scratch[warp * kQrW + lane] = acc;
             __syncthreads();
@@ -234,66 +201,99 @@ qr_panel_kernel(float2 *__restrict__ Q, size_t ldq, int m, int j0, int pc, int r
                     t.x += scratch[w * kQrW + tid].x;
                     t.y += scratch[w * kQrW + tid].y;
                 }
-                ps[lay.dot + par * kQrW + tid] = t;
+                ps[lay.red + par * 2 * kQrW + tid] = t;
+                ps[lay.red + par * 2 * kQrW + kQrW + tid] =
+                    (own && tid >= jj && tid < lw) ? L[(size_t)tid * lds + (g - r0)] : make_float2(0.f, 0.f);
             }
             cluster.sync();
-            // (4) y_c = conj(tau) w_c; x_c -= v y_c
-            if (warp == 0 && lane < kQrW) {
-                float2 t = make_float2(0.f, 0.f);
-                if (lane > jj && lane < lw)
-                    t = cluster_sum(peer, lay.dot + par * kQrW, lane, CL);
-                scratch[lane] = cjmul(tau, t);
+            // (2) the cluster's sums
+            if (tid < 2 * kQrW) {
+                const int cc = tid % kQrW;
+                ps[lay.sums + tid] = (cc >= jj && cc < lw) ? cluster_sum(peer, lay.red + par * 2 * kQrW, tid, CL)
+                                                           : make_float2(0.f, 0.f);
             }
             __syncthreads();
+            // (3) the reflector (every thread), then x_c -= v y_c with
+            // y_c = conj(tau) v^H x_c for the leaf's later columns
+            float2 tau, scal;
+            float beta;
+            qr_reflector(ps[lay.sums + jj].x, ps[lay.sums + kQrW + jj], tau, scal, beta);
+            if (tid == 0) {
+                ps[lay.taus + jj] = tau;
+                if (q == 0) tau_out[l0 + jj] = tau;
+                ps[lay.prev] = scal;
+                ps[lay.prev + 1] = make_float2(beta, 0.f);
+            }
             if (c > jj && c < lw) {
-                const float2 y = scratch[c];
-                for (int i = il; i < nrows; i += NIL) {
-                    const int grow = r0 + i;
-                    if (grow >= g) {
-                        const float2 v = vval(L, lds, jj, grow, g, i);
-                        float2 &x = L[(size_t)c * lds + i];
-                        const float2 vy = cmul(v, y);
-                        x.x -= vy.x;
-                        x.y -= vy.y;
-                    }
+                const float2 d = ps[lay.sums + c], xg = ps[lay.sums + kQrW + c];
+                const float2 sd = cjmul(scal, d);
+                const float2 y = cjmul(tau, make_float2(xg.x + sd.x, xg.y + sd.y));
+                const float2 sy = cmul(scal, y);   // v_i y = x_i (scal y) below the pivot
+                float2 *xc = L + (size_t)c * lds;
+                if (il == 0 && own) {
+                    xc[g - r0].x -= y.x;
+                    xc[g - r0].y -= y.y;
+                }
+                for (int i = ib + il; i < nrows; i += NIL) {
+                    const float2 u = cmul(xj[i], sy);
+                    xc[i].x -= u.x;
+                    xc[i].y -= u.y;
                 }
             }
             __syncthreads();
         }
+        {
+            // the leaf's last column: its pending scaling
+            const int jl = lw - 1, gl = G0 + jl;
+            const float2 sc = ps[lay.prev];
+            float2 *xp = L + (size_t)jl * lds;
+            for (int i = max(0, gl + 1 - r0) + tid; i < nrows; i += kQrNT) xp[i] = cmul(xp[i], sc);
+            if (tid == 0 && gl >= r0 && gl < r0 + nrows) xp[gl - r0] = make_float2(ps[lay.prev + 1].x, 0.f);
+        }
+        __syncthreads();
         // the factored leaf back to Q
-        for (int c = 0; c < lw; c++)
-            for (int i = tid; i < nrows; i += kQrNT)
-                Q[(size_t)(j0 + l0 + c) * ldq + r0 + i] = L[(size_t)c * lds + i];
+        for (int cc = 0; cc < lw; cc++)
+            for (int i = tid; i < nrows; i += kQrNT) Q[(size_t)(G0 + cc) * ldq + r0 + i] = L[(size_t)cc * lds + i];
         const int c1 = l0 + lw, nrest = pc - c1;
         if (nrest <= 0) continue;
+        __syncthreads();
         // ---- the leaf's block reflector applied to the panel's later columns:
         // P -= V T^H (V^H P), P = Q[j0:m, j0+c1 : j0+pc] ----
-        // (a) this CTA's V^H V (lw x lw) and V^H P (lw x nrest)
-        for (int pr = tid; pr < lw * lw; pr += kQrNT) {
-            const int a = pr / lw, b = pr % lw;
-            const int ga = j0 + l0 + a, gb = j0 + l0 + b;
+        // L becomes V: zero above the unit diagonal in the leaf's pivot rows
+        // (rows above G0 are zero in every column and skipped below)
+        for (int e = tid; e < lw * lw; e += kQrNT) {
+            const int k = e / lw, d = e % lw, grow = G0 + d;
+            if (grow >= r0 && grow < r0 + nrows && d <= k)
+                L[(size_t)k * lds + (grow - r0)] = d == k ? make_float2(1.f, 0.f) : make_float2(0.f, 0.f);
+        }
+        __syncthreads();
+        const int i0 = max(0, G0 - r0);
+        // (a) this CTA's V^H V (lw x lw; thread = entry and row half) and V^H P (lw x nrest)
+        {
+            const int pr = tid % (kQrW * kQrW), h = tid / (kQrW * kQrW);
+            const int a = pr / kQrW, b = pr % kQrW;
             float2 t = make_float2(0.f, 0.f);
-            for (int i = 0; i < nrows; i++) {
-                const int grow = r0 + i;
-                const float2 va = vval(L, lds, a, grow, ga, i), vb = vval(L, lds, b, grow, gb, i);
-                const float2 u = cjmul(va, vb);
-                t.x += u.x;
-                t.y += u.y;
+            if (a < lw && b < lw) {
+                const float2 *va = L + (size_t)a * lds, *vb = L + (size_t)b * lds;
+                for (int i = i0 + h; i < nrows; i += kQrNT / (kQrW * kQrW)) {
+                    const float2 u = cjmul(va[i], vb[i]);
+                    t.x += u.x;
+                    t.y += u.y;
+                }
             }
-            ps[lay.gram + a * kQrW + b] = t;
+            ps[lay.gpart + tid] = t;
         }
         for (int cc = warp; cc < nrest; cc += kQrNT / 32) {
             const float2 *pcol = Q + (size_t)(j0 + c1 + cc) * ldq + r0;
             float2 acc[kQrW];
 #pragma unroll
             for (int k = 0; k < kQrW; k++) acc[k] = make_float2(0.f, 0.f);
-            for (int i = lane; i < nrows; i += 32) {
+            for (int i = i0 + lane; i < nrows; i += 32) {
                 const float2 x = pcol[i];
-                const int grow = r0 + i;
 #pragma unroll
                 for (int k = 0; k < kQrW; k++)
                     if (k < lw) {
-                        const float2 u = cjmul(vval(L, lds, k, grow, j0 + l0 + k, i), x);
+                        const float2 u = cjmul(L[(size_t)k * lds + i], x);
                         acc[k].x += u.x;
                         acc[k].y += u.y;
                     }
@@ -309,19 +309,24 @@ qr_panel_kernel(float2 *__restrict__ Q, size_t ldq, int m, int j0, int pc, int r
                 for (int k = 0; k < kQrW; k++)
                     if (k < lw) ps[lay.wpart + (size_t)k * kQrNB + cc] = acc[k];
         }
+        __syncthreads();
+        if (tid < kQrW * kQrW) {
+            float2 t = ps[lay.gpart + tid];
+            for (int h = 1; h < kQrNT / (kQrW * kQrW); h++) {
+                t.x += ps[lay.gpart + h * kQrW * kQrW + tid].x;
+                t.y += ps[lay.gpart + h * kQrW * kQrW + tid].y;
+            }
+            ps[lay.gram + tid] = t;   // entry (a, b) at a kQrW + b
+        }
         cluster.sync();
         // (b) the cluster sums
         for (int e = tid; e < lw * lw; e += kQrNT) {
             const int a = e / lw, b = e % lw;
-            float2 t = make_float2(0.f, 0.f);
-            t = cluster_sum(peer, lay.gram, a * kQrW + b, CL);
-            ps[lay.gsum + a * kQrW + b] = t;
+            ps[lay.gsum + a * kQrW + b] = cluster_sum(peer, lay.gram, a * kQrW + b, CL);
         }
         for (int e = tid; e < lw * nrest; e += kQrNT) {
             const int k = e / nrest, cc = e % nrest;
-            float2 t = make_float2(0.f, 0.f);
-            t = cluster_sum(peer, lay.wpart, (size_t)k * kQrNB + cc, CL);
-            ps[lay.ysum + (size_t)k * kQrNB + cc] = t;   // W = V^H P for now
+            ps[lay.ysum + (size_t)k * kQrNB + cc] = cluster_sum(peer, lay.wpart, (size_t)k * kQrNB + cc, CL);   // W = V^H P for now
         }
         __syncthreads();
         // (c) T (upper triangular, lw x lw): T_kk = tau_k, T[0:k, k] = -tau_k T[0:k, 0:k] G[0:k, k]
@@ -364,17 +369,21 @@ qr_panel_kernel(float2 *__restrict__ Q, size_t ldq, int m, int j0, int pc, int r
             }
         }
         __syncthreads();
-        // (e) P -= V Y (this CTA's rows)
+        // (e) P -= V Y (this CTA's rows from the leaf's first pivot row down)
         for (int cc = warp; cc < nrest; cc += kQrNT / 32) {
             float2 *pcol = Q + (size_t)(j0 + c1 + cc) * ldq + r0;
-            for (int i = lane; i < nrows; i += 32) {
-                const int grow = r0 + i;
+            float2 yk[kQrW];
+#pragma unroll
+            for (int k = 0; k < kQrW; k++) yk[k] = k < lw ? ps[lay.ysum + (size_t)k * kQrNB + cc] : make_float2(0.f, 0.f);
+            for (int i = i0 + lane; i < nrows; i += 32) {
                 float2 x = pcol[i];
-                for (int k = 0; k < lw; k++) {
-                    const float2 u = cmul(vval(L, lds, k, grow, j0 + l0 + k, i), ps[lay.ysum + (size_t)k * kQrNB + cc]);
-                    x.x -= u.x;
-                    x.y -= u.y;
-                }
+#pragma unroll
+                for (int k = 0; k < kQrW; k++)
+                    if (k < lw) {
+                        const float2 u = cmul(L[(size_t)k * lds + i], yk[k]);
+                        x.x -= u.x;
+                        x.y -= u.y;
+                    }
                 pcol[i] = x;
             }
         }
@@ -684,59 +693,90 @@ qr_diag_inv_kernel(int n, const float2 *__restrict__ Q, size_t ldq, float2 *__re
     for (int c = 0; c < kQrTB; c++) D[(size_t)c * kQrTB + j] = Xs[j][c];
 }
 
+// Each launch issues its loads that do not depend on the vector (R's blocks,
+// the inverse) before it reads the vector, so CTA 0 -- the chain from one
+// block to the next -- waits about one memory round trip.
+constexpr int kQrTsK = kQrTB / kQrTsP;   // columns per thread of a 64-row group
+
 __global__ void __launch_bounds__(kQrTsNT)
 qr_trsv_back_kernel(int b0, int b1, int b2, const float2 *__restrict__ Q, size_t ldq,
                     const float2 *__restrict__ Dinv, float2 *X, size_t ldx) {
     float2 *x = X + (size_t)blockIdx.y * ldx;
-    const int tid = threadIdx.x;
-    if (blockIdx.x > 0) {
-        const int i = (blockIdx.x - 1) * kQrTsNT + tid;
-        if (i >= b0 || b2 <= b1) return;
-        float2 acc = x[i];
-        for (int k = b1; k < b2; k++) {
-            const float2 r = Q[(size_t)k * ldq + i], xk = x[k];
-            acc.x -= r.x * xk.x - r.y * xk.y;
-            acc.y -= r.x * xk.y + r.y * xk.x;
-        }
-        x[i] = acc;
-        return;
-    }
+    const int tid = threadIdx.x, row = tid % kQrTB, p = tid / kQrTB;
+    const int np = b2 - b1;
     __shared__ float2 xs[kQrTB], ys[kQrTB];
     __shared__ float2 part[kQrTsP][kQrTB];
-    const int nbk = b1 - b0, np = b2 - b1, row = tid % kQrTB, p = tid / kQrTB;
-    for (int t = tid; t < np; t += kQrTsNT) xs[t] = x[b1 + t];
+    if (blockIdx.x > 0) {
+        // rows [0, b0) in groups of kQrTB: y_i -= R[i, b1:b2] x[b1:b2],
+        // thread (row, column group p)
+        const int i = (blockIdx.x - 1) * kQrTB + row;
+        float2 rv[kQrTsK];
+#pragma unroll
+        for (int t = 0; t < kQrTsK; t++) {
+            const int k = p + kQrTsP * t;
+            rv[t] = (i < b0 && k < np) ? Q[(size_t)(b1 + k) * ldq + i] : make_float2(0.f, 0.f);
+        }
+        if (tid < kQrTB) xs[tid] = tid < np ? x[b1 + tid] : make_float2(0.f, 0.f);
+        __syncthreads();
+        float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int t = 0; t < kQrTsK; t++) {
+            const float2 xk = xs[p + kQrTsP * t];
+            acc.x += rv[t].x * xk.x - rv[t].y * xk.y;
+            acc.y += rv[t].x * xk.y + rv[t].y * xk.x;
+        }
+        part[p][row] = acc;
+        __syncthreads();
+        if (p == 0 && i < b0) {
+            float2 y = x[i];
+#pragma unroll
+            for (int q = 0; q < kQrTsP; q++) {
+                y.x -= part[q][row].x;
+                y.y -= part[q][row].y;
+            }
+            x[i] = y;
+        }
+        return;
+    }
+    const int nbk = b1 - b0;
+    const float2 *D = Dinv + (size_t)(b0 / kQrTB) * kQrTB * kQrTB;
+    float2 rv[kQrTsK], dv[kQrTsK];
+#pragma unroll
+    for (int t = 0; t < kQrTsK; t++) {
+        const int k = p + kQrTsP * t;
+        rv[t] = (row < nbk && k < np) ? Q[(size_t)(b1 + k) * ldq + b0 + row] : make_float2(0.f, 0.f);
+        dv[t] = k < nbk ? D[(size_t)k * kQrTB + row] : make_float2(0.f, 0.f);   // Dinv(row, k)
+    }
+    const float2 y0 = (tid < nbk) ? x[b0 + tid] : make_float2(0.f, 0.f);
+    if (tid < kQrTB) xs[tid] = tid < np ? x[b1 + tid] : make_float2(0.f, 0.f);
     __syncthreads();
     {
         float2 acc = make_float2(0.f, 0.f);
-        if (row < nbk)
-            for (int k = p; k < np; k += kQrTsP) {
-                const float2 r = Q[(size_t)(b1 + k) * ldq + b0 + row], xk = xs[k];
-                acc.x += r.x * xk.x - r.y * xk.y;
-                acc.y += r.x * xk.y + r.y * xk.x;
-            }
+#pragma unroll
+        for (int t = 0; t < kQrTsK; t++) {
+            const float2 xk = xs[p + kQrTsP * t];
+            acc.x += rv[t].x * xk.x - rv[t].y * xk.y;
+            acc.y += rv[t].x * xk.y + rv[t].y * xk.x;
+        }
         part[p][row] = acc;
     }
     __syncthreads();
     if (tid < kQrTB) {
-        float2 y = make_float2(0.f, 0.f);
-        if (tid < nbk) {
-            y = x[b0 + tid];
+        float2 y = y0;
 #pragma unroll
-            for (int q = 0; q < kQrTsP; q++) {
-                y.x -= part[q][tid].x;
-                y.y -= part[q][tid].y;
-            }
+        for (int q = 0; q < kQrTsP; q++) {
+            y.x -= part[q][tid].x;
+            y.y -= part[q][tid].y;
         }
-        ys[tid] = y;
+        ys[tid] = tid < nbk ? y : make_float2(0.f, 0.f);
     }
     __syncthreads();
-    // x_b = Dinv_b y: thread (row, p) over the columns c = p mod kQrTsP
-    const float2 *D = Dinv + (size_t)(b0 / kQrTB) * kQrTB * kQrTB;
     float2 acc = make_float2(0.f, 0.f);
-    for (int c = p; c < nbk; c += kQrTsP) {
-        const float2 d = D[(size_t)c * kQrTB + row], yc = ys[c];
-        acc.x += d.x * yc.x - d.y * yc.y;
-        acc.y += d.x * yc.y + d.y * yc.x;
+#pragma unroll
+    for (int t = 0; t < kQrTsK; t++) {
+        const float2 yc = ys[p + kQrTsP * t];
+        acc.x += dv[t].x * yc.x - dv[t].y * yc.y;
+        acc.y += dv[t].x * yc.y + dv[t].y * yc.x;
     }
     part[p][row] = acc;
     __syncthreads();
@@ -778,52 +818,61 @@ qr_trsv_fwd_kernel(int bp, int b0, int b1, int n, const float2 *__restrict__ Q, 
         }
         return;
     }
+    // CTA 0: warp w owns rows w R8 .. + R8 - 1 of the block, lanes over k
+    constexpr int R8 = kQrTB / (kQrTsNT / 32);
+    static_assert(kQrTB == 64, "two columns per lane");
     __shared__ float2 xs[kQrTB], ys[kQrTB];
     __shared__ float2 part[kQrTB];
     const int nbk = b1 - b0;
-    for (int t = tid; t < np; t += kQrTsNT) xs[t] = x[bp + t];
-    __syncthreads();
-    // rows of this block: warp w takes rows w, w + 8, ...; lanes over k
-    for (int row = warp; row < kQrTB; row += kQrTsNT / 32) {
-        float2 acc = make_float2(0.f, 0.f);
-        if (row < nbk)
-            for (int k = lane; k < np; k += 32) {
-                const float2 r = Q[(size_t)(b0 + row) * ldq + bp + k], xk = xs[k];
-                acc.x += r.x * xk.x + r.y * xk.y;
-                acc.y += r.x * xk.y - r.y * xk.x;
-            }
-        for (int o = 16; o > 0; o >>= 1) {
-            acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
-            acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
-        }
-        if (lane == 0) part[row] = acc;
-    }
-    __syncthreads();
-    if (tid < kQrTB) {
-        float2 y = make_float2(0.f, 0.f);
-        if (tid < nbk) {
-            y = x[b0 + tid];
-            y.x -= part[tid].x;
-            y.y -= part[tid].y;
-        }
-        ys[tid] = y;
-    }
-    __syncthreads();
-    // x_b = Dinv_b^H y: warp per row, lanes over c (row r of Dinv^H is the
-    // conjugate of column r of Dinv, contiguous)
     const float2 *D = Dinv + (size_t)(b0 / kQrTB) * kQrTB * kQrTB;
-    for (int row = warp; row < nbk; row += kQrTsNT / 32) {
+    float2 rv[R8][2], dv[R8][2];
+#pragma unroll
+    for (int r = 0; r < R8; r++) {
+        const int row = warp * R8 + r;
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const int k = lane + 32 * h;
+            rv[r][h] = (row < nbk && k < np) ? Q[(size_t)(b0 + row) * ldq + bp + k] : make_float2(0.f, 0.f);
+            dv[r][h] = (row < nbk && k < nbk) ? D[(size_t)row * kQrTB + k] : make_float2(0.f, 0.f);   // Dinv(k, row)
+        }
+    }
+    const float2 y0 = (tid < nbk) ? x[b0 + tid] : make_float2(0.f, 0.f);
+    if (tid < kQrTB) xs[tid] = tid < np ? x[bp + tid] : make_float2(0.f, 0.f);
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < R8; r++) {
         float2 acc = make_float2(0.f, 0.f);
-        for (int c = lane; c < nbk; c += 32) {
-            const float2 d = D[(size_t)row * kQrTB + c], yc = ys[c];
-            acc.x += d.x * yc.x + d.y * yc.y;
-            acc.y += d.x * yc.y - d.y * yc.x;
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const float2 xk = xs[lane + 32 * h];
+            acc.x += rv[r][h].x * xk.x + rv[r][h].y * xk.y;   // conj(R[k, row]) x_k
+            acc.y += rv[r][h].x * xk.y - rv[r][h].y * xk.x;
         }
         for (int o = 16; o > 0; o >>= 1) {
             acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
             acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
         }
-        if (lane == 0) x[b0 + row] = acc;
+        if (lane == 0) part[warp * R8 + r] = acc;
+    }
+    __syncthreads();
+    if (tid < kQrTB) ys[tid] = tid < nbk ? make_float2(y0.x - part[tid].x, y0.y - part[tid].y) : make_float2(0.f, 0.f);
+    __syncthreads();
+    // x_b = Dinv_b^H y: (Dinv^H)(row, k) = conj(Dinv(k, row))
+#pragma unroll
+    for (int r = 0; r < R8; r++) {
+        float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const float2 yc = ys[lane + 32 * h];
+            acc.x += dv[r][h].x * yc.x + dv[r][h].y * yc.y;
+            acc.y += dv[r][h].x * yc.y - dv[r][h].y * yc.x;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+            acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+        }
+        const int row = warp * R8 + r;
+        if (lane == 0 && row < nbk) x[b0 + row] = acc;
     }
 }
 
@@ -866,7 +915,7 @@ void qr_trsv(bool forward, int n, int S, const float2 *Q, size_t ldq, const floa
     if (!forward) {
         for (int b = nb - 1; b >= 0; b--) {
             const int b0 = b * kQrTB, b1 = std::min(n, b0 + kQrTB), b2 = b == nb - 1 ? b1 : std::min(n, b1 + kQrTB);
-            const int others = b2 > b1 ? (b0 + kQrTsNT - 1) / kQrTsNT : 0;
+            const int others = b2 > b1 ? (b0 + kQrTB - 1) / kQrTB : 0;
             qr_trsv_back_kernel<<<dim3(1 + others, S), kQrTsNT, 0, st>>>(b0, b1, b2, Q, ldq, Dinv, X, ldx);
         }
     } else {
