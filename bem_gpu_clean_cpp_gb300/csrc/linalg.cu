@@ -797,14 +797,24 @@ normal_op_kernel(int R, int N, const float2 *__restrict__ A, size_t lda, const f
 // The same product with A streamed through shared memory by bulk
 // asynchronous copies (TMA).  CTA q of a cluster owns columns
 // [q W, (q+1) W), W = NT kNtCPT, with v and its partial w in registers
-// (kNtCPT columns per thread).  Thread 0 keeps kNtNS stages of kNtRPS row
-// segments in flight: stage g % kNtNS is refilled with group g + kNtNS once
-// every thread has copied group g into registers (the CTA barrier of the row
-// reduction; the refill is issued after the cluster barrier that follows),
-// so HBM streams on through the barriers the row sums need, where the
-// register-loading kernel above issues no loads.  The CTA barrier orders the
-// threads' shared-memory reads before the refill (no proxy fence is needed
-// for a write-after-read).  NT = 512: one CTA per SM; NT = 256: two.
+// (kNtCPT columns per thread).  Thread 0 keeps kNtNS row segments in flight
+// (one row per stage); a stage is refilled once every thread has copied its
+// row into registers (a CTA barrier orders those shared-memory reads before
+// the refill; no proxy fence is needed for a write-after-read).
+//
+// The row sums t_r = sum_c a_rc v_c need the cluster's CTAs together.  No
+// cluster barrier is used for them: each CTA pushes its partial sum of row g
+// into every CTA's receive slot g % kNtSlots with st.async, which completes
+// bytes on the receiver's mbarrier for that slot; a CTA waits on its own
+// mbarrier and adds the C partial sums in rank order (the same order in every
+// CTA).  It pushes row g + 1's partial sums before it waits for row g, so the
+// exchange overlaps a row of work, and it applies row g (w += conj(a_g) t_g)
+// from registers.  Four slots suffice: a peer sends row g + 4 only after
+// its wait for row g + 2, which needs this CTA's row g + 2 partial, which this
+// CTA sends only after all its threads have read row g; so slot g % 4 is
+// rewritten only after it has been read (and re-armed: thread 0 re-arms a
+// slot right after its own wait, before any of the next row's bytes can come).
+// NT = 512: one CTA per SM; NT = 256: two.
 //
 // A row segment starts at A + row lda + q W: 16-byte aligned because lda is
 // even (the launcher checks) and W is even; its length is rounded up to an
@@ -812,15 +822,46 @@ normal_op_kernel(int R, int N, const float2 *__restrict__ A, size_t lda, const f
 // columns past N are masked (never multiplied), so the padding's contents do
 // not matter.  Every wait is bounded; on a timeout the CTA records it in
 // *timeout_flag (a status word of the calling solver, so concurrent solves
-// see only their own), issues no further copies, keeps the same barrier
-// sequence as its peers, and drains its copies in flight (bounded again)
-// before exiting.
+// see only their own), issues no further copies, keeps sending its (now
+// meaningless) partial sums so that its peers' waits end, and drains its
+// copies in flight (bounded again) before exiting.
 constexpr int kNtCPT = 11;
-constexpr int kNtRPS = 2;              // rows per stage (one row group)
-constexpr int kNtNS = 2;               // stages
+constexpr int kNtRPS = 1;              // rows per stage (one row group)
+constexpr int kNtNS = 4;               // stages
+constexpr int kNtSlots = 4;            // receive slots of the row-sum exchange
+static_assert(kNtRPS == 1, "the pipelined row loop handles one row per group");
 template <int NT>
 constexpr size_t nt_smem() { return (size_t)kNtNS * kNtRPS * NT * kNtCPT * sizeof(float2); }
 constexpr long long kNtWaitCycles = 2000000000LL;                          // ~1 s at 2 GHz
+
+__device__ __forceinline__ uint32_t cluster_addr(const void *p, uint32_t rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(smem_u32(p)), "r"(rank));
+    return r;
+}
+// 8 bytes into another CTA's shared memory, completing on its mbarrier.
+__device__ __forceinline__ void st_async_f2(uint32_t addr, float2 v, uint32_t bar) {
+    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v2.f32 [%0], {%1, %2}, [%3];" ::"r"(addr),
+                 "f"(v.x), "f"(v.y), "r"(bar)
+                 : "memory");
+}
+// Bounded wait with cluster-scope acquire (the bytes came from other CTAs).
+__device__ __forceinline__ bool mbar_wait_cluster_bounded(uint64_t *bar, uint32_t parity, long long limit,
+                                                          volatile int *abort) {
+    const long long t0 = clock64();
+    for (;;) {
+        uint32_t ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok)
+            : "r"(smem_u32(bar)), "r"(parity)
+            : "memory");
+        if (ok) return true;
+        if (*abort || clock64() - t0 > limit) return false;
+    }
+}
 
 template <int NT>
 __global__ void __launch_bounds__(NT, 512 / NT)
@@ -833,10 +874,11 @@ normal_op_tma_kernel(int R, int N, const float2 *__restrict__ A, size_t lda, con
     const int q = (int)cluster.block_rank();
     const int cl = blockIdx.x / C;
     constexpr int kNtNT = NT, kNtW = NT * kNtCPT;
-    extern __shared__ __align__(128) float2 nt_stage[];   // [kNtNS][kNtRPS][kNtW]
+    extern __shared__ __align__(128) float2 nt_stage[];   // [kNtNS][kNtW]
     __shared__ __align__(8) uint64_t full[kNtNS];
-    __shared__ float red[kNtRPS][2][kNtNT / 32];
-    __shared__ float tot[2][kNtRPS * 2];
+    __shared__ __align__(8) uint64_t sum_bar[kNtSlots];
+    __shared__ float2 tin[kNtSlots][kNoMaxCluster];   // [slot][source CTA]: partial row sums received
+    __shared__ float red[2][2][kNtNT / 32];           // [row parity][re, im][warp]
     __shared__ int abort_flag;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int c0 = q * kNtW;
@@ -844,30 +886,27 @@ normal_op_tma_kernel(int R, int N, const float2 *__restrict__ A, size_t lda, con
     const uint32_t seg_bytes = (uint32_t)(((cnt + 1) & ~1) * sizeof(float2));
     const int r_begin = cl * rows_per_cluster;
     const int r_end = min(R, r_begin + rows_per_cluster);
-    auto group_rows = [&](int g) { return max(0, min(kNtRPS, r_end - (r_begin + g * kNtRPS))); };
-    int last_issued = -1;       // thread 0: the last group whose copies were issued
+    const int nrows = max(0, min(ngroups, r_end - r_begin));
+    int last_issued = -1;       // thread 0: the last row whose copy was issued
     auto issue = [&](int g) {   // thread 0 only
-        const int nr = group_rows(g);
-        if (nr == 0) return;
+        if (g >= nrows) return;
         const int s = g % kNtNS;
         last_issued = g;
         // extra_tx > 0 (a test of the timeout path only) announces bytes no copy
         // delivers: every copy completes, the phase never does, the waits run out
-        mbar_arrive_expect_tx(&full[s], nr * seg_bytes + extra_tx);
-        for (int rb = 0; rb < nr; rb++) {
-            const int row = r_begin + g * kNtRPS + rb;
-            bulk_copy_g2s(nt_stage + ((size_t)s * kNtRPS + rb) * kNtW, A + (size_t)row * lda + c0, seg_bytes,
-                          &full[s]);
-        }
+        mbar_arrive_expect_tx(&full[s], seg_bytes + extra_tx);
+        bulk_copy_g2s(nt_stage + (size_t)s * kNtW, A + (size_t)(r_begin + g) * lda + c0, seg_bytes, &full[s]);
     };
     if (tid == 0) {
         for (int s = 0; s < kNtNS; s++) mbar_init(&full[s], 1);
+        for (int s = 0; s < kNtSlots; s++) mbar_init(&sum_bar[s], 1);
         abort_flag = 0;
         mbar_fence_init();
+        for (int s = 0; s < kNtSlots; s++) mbar_arrive_expect_tx(&sum_bar[s], (uint32_t)(C * sizeof(float2)));
     }
-    __syncthreads();
+    cluster.sync();   // every CTA's barriers are initialised before any partial sum is sent
     if (tid == 0)
-        for (int g = 0; g < min(kNtNS, ngroups); g++) issue(g);
+        for (int g = 0; g < min(kNtNS, nrows); g++) issue(g);
     float2 vr[kNtCPT], wr[kNtCPT];
 #pragma unroll
     for (int i = 0; i < kNtCPT; i++) {
@@ -875,68 +914,83 @@ normal_op_tma_kernel(int R, int N, const float2 *__restrict__ A, size_t lda, con
         vr[i] = c < N ? v[c] : make_float2(0.f, 0.f);
         wr[i] = make_float2(0.f, 0.f);
     }
-    for (int g = 0; g < ngroups; g++) {
-        const int par = g & 1, s = g % kNtNS;
-        const int nr = group_rows(g);
-        if (nr > 0 && !*(volatile int *)&abort_flag) {
+    // row g into registers and its partial sum into red[g & 1]
+    auto load_row = [&](int g, float2 (&a)[kNtCPT]) {
+        const int s = g % kNtNS;
+        if (!*(volatile int *)&abort_flag) {
             if (!mbar_wait_bounded(&full[s], (uint32_t)((g / kNtNS) & 1), kNtWaitCycles, &abort_flag)) {
                 abort_flag = 1;
                 atomicExch(timeout_flag, 1);
             }
         }
-        const float2 *stg = nt_stage + (size_t)s * kNtRPS * kNtW;
-        float2 a[kNtRPS][kNtCPT];
-        float pr[kNtRPS], pim[kNtRPS];
+        const float2 *stg = nt_stage + (size_t)s * kNtW;
+        const bool ok = !*(volatile int *)&abort_flag;
+        float pr = 0.f, pim = 0.f;
 #pragma unroll
-        for (int rb = 0; rb < kNtRPS; rb++) {
-            pr[rb] = pim[rb] = 0.f;
-#pragma unroll
-            for (int i = 0; i < kNtCPT; i++) {
-                const int col = tid + i * kNtNT;
-                a[rb][i] = (rb < nr && c0 + col < N) ? stg[rb * kNtW + col] : make_float2(0.f, 0.f);
-                const float2 x = vr[i], y = a[rb][i];
-                pr[rb] = fmaf(y.x, x.x, fmaf(-y.y, x.y, pr[rb]));
-                pim[rb] = fmaf(y.x, x.y, fmaf(y.y, x.x, pim[rb]));
-            }
-            for (int o = 16; o > 0; o >>= 1) {
-                pr[rb] += __shfl_xor_sync(0xffffffffu, pr[rb], o);
-                pim[rb] += __shfl_xor_sync(0xffffffffu, pim[rb], o);
-            }
-            if (lane == 0) {
-                red[rb][0][warp] = pr[rb];
-                red[rb][1][warp] = pim[rb];
-            }
+        for (int i = 0; i < kNtCPT; i++) {
+            const int col = tid + i * kNtNT;
+            a[i] = (ok && c0 + col < N) ? stg[col] : make_float2(0.f, 0.f);
+            pr = fmaf(a[i].x, vr[i].x, fmaf(-a[i].y, vr[i].y, pr));
+            pim = fmaf(a[i].x, vr[i].y, fmaf(a[i].y, vr[i].x, pim));
         }
-        __syncthreads();   // stage s is in every thread's registers
-        if (tid < 2 * kNtRPS) {
-            float t = 0.f;
-            for (int w = 0; w < kNtNT / 32; w++) t += red[tid >> 1][tid & 1][w];
-            tot[par][tid] = t;
+        for (int o = 16; o > 0; o >>= 1) {
+            pr += __shfl_xor_sync(0xffffffffu, pr, o);
+            pim += __shfl_xor_sync(0xffffffffu, pim, o);
         }
-        cluster.sync();   // every CTA's row sums of this group are in its tot[par]
-        // the stage is free once every thread of this CTA has copied it (both
-        // barriers above).  Issuing the refill after the cluster barrier keeps
-        // thread 0's arrival on time; issued before it, the issuing thread
-        // arrived late and stalled every CTA of the cluster (0.156 -> 0.221 ms
-        // per product at 10274 x 10242 measured)
-        if (tid == 0 && g + kNtNS < ngroups && !abort_flag) issue(g + kNtNS);   // none after a timeout
-        float ts[2 * kNtRPS];
-#pragma unroll
-        for (int u = 0; u < 2 * kNtRPS; u++) ts[u] = 0.f;
+        if (lane == 0) {
+            red[g & 1][0][warp] = pr;
+            red[g & 1][1][warp] = pim;
+        }
+    };
+    auto publish = [&](int g) {   // thread 0, after a CTA barrier: row g's partial sum to every CTA
+        float2 t = make_float2(0.f, 0.f);
+        for (int w = 0; w < kNtNT / 32; w++) {
+            t.x += red[g & 1][0][w];
+            t.y += red[g & 1][1][w];
+        }
+        const int slot = g % kNtSlots;
+        for (int p = 0; p < C; p++)
+            st_async_f2(cluster_addr(&tin[slot][q], (uint32_t)p), t, cluster_addr(&sum_bar[slot], (uint32_t)p));
+    };
+    // one step: row g + 1's partial sums out, then row g's sums in and applied
+    auto step = [&](int g, float2 (&cur)[kNtCPT], float2 (&nxt)[kNtCPT]) {
+        const bool more = g + 1 < nrows;
+        if (more) load_row(g + 1, nxt);
+        __syncthreads();   // row g + 1's stage is in every thread's registers; red[(g + 1) & 1] is complete
+        if (more && tid == 0) {
+            if (!abort_flag) issue(g + 1 + kNtNS);   // none after a timeout
+            publish(g + 1);
+        }
+        const int slot = g % kNtSlots;
+        const bool got = mbar_wait_cluster_bounded(&sum_bar[slot], (uint32_t)((g / kNtSlots) & 1), kNtWaitCycles,
+                                                   &abort_flag);
+        if (!got && !abort_flag) {
+            abort_flag = 1;
+            atomicExch(timeout_flag, 1);
+        }
+        float tr = 0.f, ti = 0.f;
         for (int p = 0; p < C; p++) {
-            const float *peer = cluster.map_shared_rank(&tot[par][0], p);
-#pragma unroll
-            for (int u = 0; u < 2 * kNtRPS; u++) ts[u] += peer[u];
+            tr += tin[slot][p].x;
+            ti += tin[slot][p].y;
         }
+        if (tid == 0 && got) mbar_arrive_expect_tx(&sum_bar[slot], (uint32_t)(C * sizeof(float2)));   // row g + kNtSlots
 #pragma unroll
-        for (int rb = 0; rb < kNtRPS; rb++) {
-            const float tr = ts[2 * rb], ti = ts[2 * rb + 1];
-#pragma unroll
-            for (int i = 0; i < kNtCPT; i++) {
-                const float2 y = a[rb][i];
-                wr[i].x = fmaf(y.x, tr, fmaf(y.y, ti, wr[i].x));     // conj(a) t
-                wr[i].y = fmaf(y.x, ti, fmaf(-y.y, tr, wr[i].y));
-            }
+        for (int i = 0; i < kNtCPT; i++) {
+            wr[i].x = fmaf(cur[i].x, tr, fmaf(cur[i].y, ti, wr[i].x));   // conj(a) t
+            wr[i].y = fmaf(cur[i].x, ti, fmaf(-cur[i].y, tr, wr[i].y));
+        }
+    };
+    float2 a0[kNtCPT], a1[kNtCPT];
+    if (nrows > 0) {
+        load_row(0, a0);
+        __syncthreads();
+        if (tid == 0) {
+            if (!abort_flag) issue(kNtNS);
+            publish(0);
+        }
+        for (int g = 0; g < nrows; g += 2) {
+            step(g, a0, a1);
+            if (g + 1 < nrows) step(g + 1, a1, a0);
         }
     }
     if (tid == 0 && abort_flag) {
@@ -946,7 +1000,7 @@ normal_op_tma_kernel(int R, int N, const float2 *__restrict__ A, size_t lda, con
         for (int g = max(0, last_issued - kNtNS + 1); g <= last_issued; g++)
             mbar_wait_bounded(&full[g % kNtNS], (uint32_t)((g / kNtNS) & 1), kNtWaitCycles, &zero);
     }
-    cluster.sync();   // the peers have read tot; shared memory may go
+    cluster.sync();   // no partial sum is still in flight to a CTA that exits
 #pragma unroll
     for (int i = 0; i < kNtCPT; i++) {
         const int c = c0 + tid + i * kNtNT;

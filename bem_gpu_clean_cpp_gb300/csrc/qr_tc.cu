@@ -1138,7 +1138,12 @@ void bem_solver_s::solve_qr_tc(bem_solve_info_t *info) {
                               w_vf.as<float2>(), stream);
             launch_nrm2(n, w_gv.as<double2>(), scal + 1, nullptr, stream);
             rel = read_scalar(1) / bn;
-            if (!std::isfinite(rel)) BEM_FAIL(BEM_ERR_NUMERIC, "QR refinement residual is not finite");
+            if (!std::isfinite(rel)) {
+                int h_st = 0;   // a tensor-core GEMM that gave up on a wait explains it
+                CUDA_TRY(cudaMemcpy(&h_st, status, sizeof(int), cudaMemcpyDeviceToHost));
+                if (h_st) BEM_FAIL(BEM_ERR_TIMEOUT, "QR_TC: a bounded wait of the tensor-core GEMM timed out");
+                BEM_FAIL(BEM_ERR_NUMERIC, "QR refinement residual is not finite");
+            }
             if (rel <= tol) { conv = true; break; }
             if (rel > 0.5 * prev || it == opt.max_refine) {
                 // stagnated at the precision of the FP64-accurate products:

@@ -152,7 +152,12 @@ void bem_solver_s::solve_refined(bem_solve_info_t *info) {
                 CUDA_TRY(cudaMemcpyAsync(scal + 1, scal + 0, sizeof(double), cudaMemcpyDeviceToDevice, stream));
             }
             rel = gn / bn;
-            if (!std::isfinite(rel)) BEM_FAIL(BEM_ERR_NUMERIC, "refinement residual is not finite");
+            if (!std::isfinite(rel)) {
+                // a normal-operator launch that gave up on a copy explains it
+                if (normal_op_timed_out(op_status, stream))
+                    BEM_FAIL(BEM_ERR_TIMEOUT, "normal operator: a bulk copy of A did not complete in time");
+                BEM_FAIL(BEM_ERR_NUMERIC, "refinement residual is not finite");
+            }
             if (rel <= opt.tol) { conv = true; break; }
             if (ref >= opt.max_refine) break;
             // Inner GMRES on A^H A d = g, d accumulated into x.
