@@ -168,16 +168,17 @@ void launch_elem_setup(const double *d_nodes, const int4 *d_elems, const double 
 // singular pairs of atomicFuncs.cu:119-216) or, with eta > 0, when
 // |x - centroid|^2 < (eta*diam)^2.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ bool pair_is_near(int row, int N, int4 nd, float4 xh, const float4 *g) {
+__device__ __forceinline__ bool pair_is_near_v(int row, int N, int4 nd, float4 xh, float r2, float4 c) {
     if (row < N && (row == nd.x || row == nd.y || row == nd.z)) return true;
-    float r2 = g[1].w;
     if (r2 > 0.0f) {
-        float4 c = g[6];
         float dx = __fsub_rn(xh.x, c.x), dy = __fsub_rn(xh.y, c.y), dz = __fsub_rn(xh.z, c.z);
         float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
         return d2 < r2;
     }
     return false;
+}
+__device__ __forceinline__ bool pair_is_near(int row, int N, int4 nd, float4 xh, const float4 *g) {
+    return pair_is_near_v(row, N, nd, xh, g[1].w, g[6]);
 }
 
 // ---------------------------------------------------------------------------
@@ -674,6 +675,10 @@ far_assembly_f32(RowPoints rows, int N, GeoTables geo, TileSet tiles, float k, f
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2 *acc = reinterpret_cast<float2 *>(smem_raw);
     __shared__ float red[NT / 32][3];
+    const int tc_s = tiles.col_cnt[blockIdx.y];
+    // this thread's c and beta sums of row t: cb[(q TR + t) NT + tid], q = c, Re beta, Im beta
+    // (in shared memory rather than registers: they are touched once per owned record)
+    float *cb = reinterpret_cast<float *>(acc + (size_t)TR * tc_s);
     __shared__ __align__(8) uint64_t batch_done;   // phase i completes when every thread added batch i
     __shared__ int wait_abort;
     const int tile = blockIdx.y;
@@ -701,9 +706,8 @@ far_assembly_f32(RowPoints rows, int N, GeoTables geo, TileSet tiles, float k, f
     // thread has added batch i - 1, adds, and arrives; so every column of a
     // row receives its terms in batch order while the wait overlaps the
     // integration.  The c and beta sums are per thread and row.
-    float csum[TR], bsr[TR], bsi[TR];
 #pragma unroll
-    for (int t = 0; t < TR; t++) csum[t] = bsr[t] = bsi[t] = 0.f;
+    for (int q = 0; q < 3 * TR; q++) cb[q * NT + threadIdx.x] = 0.f;
     auto wait_batch = [&](int i) {   // batch i (counted from the tile's first) added by every thread
         if (!mbar_wait_bounded(&batch_done, (uint32_t)(i & 1), kFarWaitCycles, &wait_abort)) {
             wait_abort = 1;
@@ -721,11 +725,12 @@ far_assembly_f32(RowPoints rows, int N, GeoTables geo, TileSet tiles, float k, f
             const int row = r0 + t;
             const float4 xh = rows.f[2 * (size_t)row], xl = rows.f[2 * (size_t)row + 1];
             float2 *arow = acc + (size_t)t * tc;
-            const TileRec rec = tiles.recs[i];
-            const float4 *g = geo.geo_f + (size_t)kGeoF * rec.eid;
-            const int4 nd = make_int4(rec.node[0], rec.node[1], rec.node[2], 0);
-            if (pair_is_near(row, N, nd, xh, g)) continue;
-            const float4 g0 = g[0], g1 = g[1], g2 = g[2], g3 = g[3], g4 = g[4], g5 = g[5];
+            const FarRec *fr = tiles.frecs + i;
+            const int4 nd = fr->nodes;
+            const float4 g1 = fr->g[1];
+            if (pair_is_near_v(row, N, nd, xh, g1.w, fr->g[6])) continue;
+            const float4 g0 = fr->g[0], g2 = fr->g[2], g3 = fr->g[3], g4 = fr->g[4], g5 = fr->g[5];
+            const int4 sl = fr->slots;
             const float3 e1 = make_float3(g2.x, g2.y, g2.z), e2 = make_float3(g3.x, g3.y, g3.z);
             const float3 d3 = make_float3((g0.x - xh.x) + (g1.x - xl.x), (g0.y - xh.y) + (g1.y - xl.y),
                                           (g0.z - xh.z) + (g1.z - xl.z));
@@ -745,22 +750,19 @@ far_assembly_f32(RowPoints rows, int N, GeoTables geo, TileSet tiles, float k, f
                 wait_batch(b - b0 - 1);
                 waited = true;
             }
+            const int slot[3] = {sl.x, sl.y, sl.z};
 #pragma unroll
             for (int j = 0; j < 3; j++) {
-                const int s = rec.slot[j];
+                const int s = slot[j];
                 if (s >= 0) {
                     arow[s].x += o.ar[j];
                     arow[s].y += o.ai[j];
                 }
             }
-            if (rec.owner) {
-#pragma unroll
-                for (int u = 0; u < TR; u++)
-                    if (u == t) {
-                        csum[u] += o.c;
-                        bsr[u] += o.br;
-                        bsi[u] += o.bi;
-                    }
+            if (nd.w) {   // this tile counts the element's c and beta terms
+                cb[(0 * TR + t) * NT + threadIdx.x] += o.c;
+                cb[(1 * TR + t) * NT + threadIdx.x] += o.br;
+                cb[(2 * TR + t) * NT + threadIdx.x] += o.bi;
             }
         }
         if (!waited) wait_batch(b - b0 - 1);   // arrivals for batch i only after batch i - 1 completed
@@ -771,7 +773,8 @@ far_assembly_f32(RowPoints rows, int N, GeoTables geo, TileSet tiles, float k, f
 #pragma unroll
     for (int t = 0; t < TR; t++) {
         if (t >= nr) break;                               // uniform over the CTA
-        float cs = csum[t], br = bsr[t], bi = bsi[t];
+        float cs = cb[(0 * TR + t) * NT + threadIdx.x], br = cb[(1 * TR + t) * NT + threadIdx.x],
+              bi = cb[(2 * TR + t) * NT + threadIdx.x];
         for (int off = 16; off > 0; off >>= 1) {
             cs += __shfl_xor_sync(0xffffffffu, cs, off);
             br += __shfl_xor_sync(0xffffffffu, br, off);
@@ -885,8 +888,11 @@ int far_rows_per_cta(int prec, int variant) {
     return prec == BEM_PREC_C64 ? kFarShapes[variant].tr : 1;
 }
 
+// c64: the rows' accumulators (tr x tc) and each thread's c and beta sums of
+// its rows (3 x tr x nt floats); c128: one row's accumulators.
 size_t far_smem_bytes(int prec, int tc, int variant) {
-    return prec == BEM_PREC_C64 ? (size_t)kFarShapes[variant].tr * tc * sizeof(float2)
+    return prec == BEM_PREC_C64 ? (size_t)kFarShapes[variant].tr * tc * sizeof(float2) +
+                                      (size_t)3 * kFarShapes[variant].tr * kFarShapes[variant].nt * sizeof(float)
                                 : (size_t)tc * sizeof(double2);
 }
 
@@ -952,6 +958,27 @@ static void launch_far_f32(const RowPoints &rows, int N, const GeoTables &geo, c
                                  (float *)c_part, (float2 *)beta_part);
 }
 
+__global__ void far_recs_kernel(const TileRec *__restrict__ recs, int nrec, const float4 *__restrict__ geo_f,
+                                FarRec *__restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nrec) return;
+    const TileRec r = recs[i];
+    FarRec f;
+#pragma unroll
+    for (int k = 0; k < kGeoF; k++) f.g[k] = geo_f[(size_t)kGeoF * r.eid + k];
+    f.nodes = make_int4(r.node[0], r.node[1], r.node[2], r.owner);
+    f.slots = make_int4(r.slot[0], r.slot[1], r.slot[2], 0);
+    out[i] = f;
+}
+
+void launch_far_recs(const TileRec *recs, int nrec, const float4 *geo_f, FarRec *frecs, cudaStream_t st) {
+    static_assert(sizeof(FarRec) == 144 && kGeoF == 7, "far record layout");
+    if (nrec <= 0) return;
+    far_recs_kernel<<<(nrec + 255) / 256, 256, 0, st>>>(recs, nrec, geo_f, frecs);
+    count_launch();
+    KERNEL_CHECK();
+}
+
 void launch_far_assembly(int prec, const RowPoints &rows, int N, const GeoTables &geo,
                          const TileSet &tiles, const Physics &ph, void *A, size_t lda,
                          void *c_part, void *beta_part, cudaStream_t st, int variant) {
@@ -962,6 +989,7 @@ void launch_far_assembly(int prec, const RowPoints &rows, int N, const GeoTables
         BEM_FAIL(BEM_ERR_TOO_LARGE, "column tile does not fit in shared memory");
     const size_t smem = far_smem_bytes(prec, tiles.tc_max, variant);
     if (prec == BEM_PREC_C64) {
+        BEM_CHECK_ARG(tiles.frecs != nullptr, "far kernel: records with geometry not formed");
         switch (variant) {
             case 0: launch_far_f32<2, 512, 1>(rows, N, geo, tiles, ph, A, lda, c_part, beta_part, smem, st); break;
             case 1: launch_far_f32<2, 1024, 1>(rows, N, geo, tiles, ph, A, lda, c_part, beta_part, smem, st); break;

@@ -37,6 +37,16 @@ struct RowPoints {
 constexpr int kFarBatch = 1024;
 constexpr long long kFarWaitCycles = 2000000000LL;   // bound of the far kernel's batch waits (~1 s)
 
+// A far-kernel record with its element's geometry gathered in record order
+// (the seven float4 of GeoTables::geo_f), so that an item's data is one
+// contiguous 144-byte read instead of a record read followed by a dependent
+// read of the element's table.  nodes.w = owner; slots.w unused.
+struct FarRec {
+    float4 g[7];
+    int4 nodes;
+    int4 slots;
+};
+
 struct TileSet {
     const TileRec *recs;      // all tiles' records
     const int *rec_ptr;       // ntiles + 1 offsets into recs
@@ -47,6 +57,7 @@ struct TileSet {
     const int *col_cnt;       // ntiles: columns in each tile
     int ntiles;
     int tc_max;
+    const FarRec *frecs;      // recs with their geometry (FP32 far kernel); filled by launch_far_recs
 };
 
 struct Physics {
@@ -80,6 +91,8 @@ int far_variants(int prec);
 int far_rows_per_cta(int prec, int variant);
 size_t far_smem_bytes(int prec, int tc, int variant);
 bool far_variant_fits(int prec, int tc, int variant);
+// frecs[i] = recs[i] with the geometry of element recs[i].eid (nrec records).
+void launch_far_recs(const TileRec *recs, int nrec, const float4 *geo_f, FarRec *frecs, cudaStream_t st);
 void launch_far_assembly(int prec, const RowPoints &rows, int N, const GeoTables &geo,
                          const TileSet &tiles, const Physics &ph, void *A, size_t lda,
                          void *c_part, void *beta_part, cudaStream_t st, int variant);

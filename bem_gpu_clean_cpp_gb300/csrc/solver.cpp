@@ -472,6 +472,7 @@ void bem_solver_s::ensure_tiles(int precision) {
     CUDA_TRY(cudaStreamSynchronize(stream));
     T.ntiles = ntiles;
     T.tc_max = per;
+    T.nrec = (int)recs.size();
     T.valid = true;
 }
 
@@ -501,7 +502,7 @@ void bem_solver_s::assemble(double kk, int precision) {
     ensure_tiles(precision);
     k = kk;
     prec = precision;
-    const Tiles &T = tiles[precision];
+    Tiles &T = tiles[precision];
     size_t esz = precision == BEM_PREC_C64 ? sizeof(float2) : sizeof(double2);
     size_t rsz = precision == BEM_PREC_C64 ? sizeof(float) : sizeof(double);
     lda = round_up(N, 8);
@@ -511,8 +512,16 @@ void bem_solver_s::assemble(double kk, int precision) {
     d_bpart.ensure(2 * rsz * (size_t)T.ntiles * R);
     d_status.ensure(4 * sizeof(int));
     CUDA_TRY(cudaMemsetAsync(d_status.as<int>() + 2, 0, sizeof(int), stream));
+    const FarRec *frecs = nullptr;
+    if (precision == BEM_PREC_C64) {
+        // the records with their elements' geometry in record order (the
+        // geometry depends on near_eta as well as the mesh: formed every time)
+        T.frecs.ensure(sizeof(FarRec) * (size_t)std::max(1, T.nrec));
+        launch_far_recs(T.recs.as<TileRec>(), T.nrec, d_geo_f.as<float4>(), T.frecs.as<FarRec>(), stream);
+        frecs = T.frecs.as<FarRec>();
+    }
     TileSet ts{T.recs.as<TileRec>(), T.rec_ptr.as<int>(), T.batch_ptr.as<int>(), T.tile_batch.as<int>(),
-               d_status.as<int>() + 2, T.cols.as<int>(), T.col_cnt.as<int>(), T.ntiles, T.tc_max};
+               d_status.as<int>() + 2, T.cols.as<int>(), T.col_cnt.as<int>(), T.ntiles, T.tc_max, frecs};
     Physics ph = physics();
     int variant = opt.far_variant;
     bool done = false;
@@ -679,7 +688,7 @@ size_t bem_solver_s::estimate_bytes(int N, int E, int M, int S, int method, cons
     size_t b = 0;
     b += 24 * n + 24 * r + 32 * r + 16 * e + 48 * e;                  // nodes, rows, elements, bc
     b += sizeof(float4) * kGeoFloat4 * e + sizeof(double) * kGeoDouble * e;
-    b += 3 * e * sizeof(TileRec) + 4 * (ntiles + 1) + 4 * n + 4 * ntiles;   // an element touches <= 3 tiles
+    b += 3 * e * (sizeof(TileRec) + sizeof(FarRec)) + 4 * (ntiles + 1) + 4 * n + 4 * ntiles;   // <= 3 tiles per element
     b += 4 * (3 * e + 2 * ntiles + 2);                                     // record batches (>= 1 record each)
     b += 4 * (r + 1) + 256 * r + 4 * e + (16u << 20);                       // near-pair list and search grid
     b += 8 * lda * r + 16 * r * s + 12 * ntiles * r + 16 * n * s + 16 * r + 48 * s;

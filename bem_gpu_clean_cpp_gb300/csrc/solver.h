@@ -81,6 +81,8 @@ struct bem_solver_s {
         bool valid = false;
         int ntiles = 0, tc_max = 0;
         bem::DevMem recs, rec_ptr, cols, col_cnt, batch_ptr, tile_batch;
+        bem::DevMem frecs;   // recs with their geometry (FP32 far kernel), re-formed by every c64 assembly
+        int nrec = 0;
     } tiles[2];
 
     int far_variant_used = -1;
