@@ -505,12 +505,15 @@ __device__ __forceinline__ uint64_t add2(uint64_t a, uint64_t b) {
 }
 
 // far_sums_f32_o6 for the shift and wrap phase modes with the two lanes of
-// f32x2 arithmetic carrying two Duffy points of a line (points 2p and
-// 2p + 1): the same operations per point, half the instructions for all but
-// rsqrt, sin and cos.  The per-point partial sums of a line add the even and
-// the odd points separately and then the two; the dG/dn imaginary sums
-// collect -hb (fma(-k, c, gs) = -fma(k, c, -gs) exactly) and take the sign
-// with the height at the end.
+// f32x2 arithmetic carrying the mirror lines n and 5 - n at the same point m
+// (theta_{5-n} = 1 - theta_n and equal weights, the Gauss rule being
+// symmetric): the same operations per point with the point's constants
+// shared by both lanes, half the instructions for all but rsqrt, sin and cos.
+// The line-pair tail needs no lane reduction but S0's: the lanes' xi1 and
+// xi2 weights are each other's (a (1 - theta) for one line is a theta' for
+// the other), so S1 += b U1_n + c U1_{5-n} and S2 += c U1_n + b U1_{5-n}.
+// The dG/dn imaginary sums collect -hb (fma(-k, c, gs) = -fma(k, c, -gs)
+// exactly) and take the sign with the height at the end.
 template <int PH>
 __device__ __forceinline__ void far_sums_f32_o6x2(float3 d3, float3 e1, float3 e2, float hgt, float k,
                                                   const PairPhase &pp, SumsF &S) {
@@ -535,18 +538,17 @@ __device__ __forceinline__ void far_sums_f32_o6x2(float3 d3, float3 e1, float3 e
     const uint64_t dd2 = f2(dd, dd), k2 = f2(k, k), nk2 = f2(-k, -k);
     const uint64_t c1 = f2(pp.c1, pp.c1), c2 = f2(pp.c2, pp.c2);
 #pragma unroll
-    for (int n = 0; n < 6; n++) {
-        const float th = 0.5f + 0.5f * gl6_x(n);
-        const float qa = fmaf(th * th, a2, fmaf(th, a1, a0));
-        const float qb = fmaf(th, b1, b0);
-        const uint64_t qa2 = f2(qa, qa), qb2 = f2(qb, qb);
+    for (int n = 0; n < 3; n++) {
+        const float th = 0.5f + 0.5f * gl6_x(n), tm = 0.5f + 0.5f * gl6_x(5 - n);   // tm = 1 - th
+        const uint64_t qa2 = f2(fmaf(th * th, a2, fmaf(th, a1, a0)), fmaf(tm * tm, a2, fmaf(tm, a1, a0)));
+        const uint64_t qb2 = f2(fmaf(th, b1, b0), fmaf(tm, b1, b0));
         uint64_t u0gr = 0, u1gr = 0, u0gs = 0, u1gs = 0, u0ha = 0, u1ha = 0, u0hb = 0, u1hb = 0, u0c = 0;
 #pragma unroll
-        for (int p = 0; p < 3; p++) {
-            const float rho0 = 0.5f + 0.5f * gl6_x(2 * p), rho1 = 0.5f + 0.5f * gl6_x(2 * p + 1);
-            const uint64_t rho = f2(rho0, rho1);
-            const uint64_t wr1 = f2(gl6_w(2 * p) * rho0, gl6_w(2 * p + 1) * rho1);
-            const uint64_t wr2 = f2(gl6_w(2 * p) * rho0 * rho0, gl6_w(2 * p + 1) * rho1 * rho1);
+        for (int m = 0; m < 6; m++) {
+            const float rho_m = 0.5f + 0.5f * gl6_x(m);
+            const uint64_t rho = f2(rho_m, rho_m);
+            const uint64_t wr1 = f2(gl6_w(m) * rho_m, gl6_w(m) * rho_m);
+            const uint64_t wr2 = f2(gl6_w(m) * rho_m * rho_m, gl6_w(m) * rho_m * rho_m);
             const uint64_t r2 = fma2(fma2(qa2, rho, qb2), rho, dd2);   // (qa rho + qb) rho + |d3|^2
             float ra, rb;
             f2_split(r2, ra, rb);
@@ -575,14 +577,19 @@ __device__ __forceinline__ void far_sums_f32_o6x2(float3 d3, float3 e1, float3 e
             u0hb = fma2(wr1, hbn, u0hb); u1hb = fma2(wr2, hbn, u1hb);
             u0c = fma2(wr1, ri3, u0c);
         }
+        // lane 0 = line n (weights a, b = a (1 - th), c = a th), lane 1 = line
+        // 5 - n (a, c, b)
         const float a = 0.25f * gl6_w(n), b = a * (1.0f - th), c = a * th;
-        const float v0gr = f2_sum(u0gr), v1gr = f2_sum(u1gr), v0gs = f2_sum(u0gs), v1gs = f2_sum(u1gs);
-        const float v0ha = f2_sum(u0ha), v1ha = f2_sum(u1ha), v0hb = f2_sum(u0hb), v1hb = f2_sum(u1hb);
-        S.g0r = fmaf(a, v0gr, S.g0r); S.g1r = fmaf(b, v1gr, S.g1r); S.g2r = fmaf(c, v1gr, S.g2r);
-        S.g0i = fmaf(a, v0gs, S.g0i); S.g1i = fmaf(b, v1gs, S.g1i); S.g2i = fmaf(c, v1gs, S.g2i);
-        S.h0r = fmaf(a, v0ha, S.h0r); S.h1r = fmaf(b, v1ha, S.h1r); S.h2r = fmaf(c, v1ha, S.h2r);
-        S.h0i = fmaf(a, v0hb, S.h0i); S.h1i = fmaf(b, v1hb, S.h1i); S.h2i = fmaf(c, v1hb, S.h2i);
-        S.c = fmaf(a, f2_sum(u0c), S.c);
+        float p0, p1;
+        f2_split(u0gr, p0, p1); S.g0r = fmaf(a, p0 + p1, S.g0r);
+        f2_split(u1gr, p0, p1); S.g1r = fmaf(b, p0, fmaf(c, p1, S.g1r)); S.g2r = fmaf(c, p0, fmaf(b, p1, S.g2r));
+        f2_split(u0gs, p0, p1); S.g0i = fmaf(a, p0 + p1, S.g0i);
+        f2_split(u1gs, p0, p1); S.g1i = fmaf(b, p0, fmaf(c, p1, S.g1i)); S.g2i = fmaf(c, p0, fmaf(b, p1, S.g2i));
+        f2_split(u0ha, p0, p1); S.h0r = fmaf(a, p0 + p1, S.h0r);
+        f2_split(u1ha, p0, p1); S.h1r = fmaf(b, p0, fmaf(c, p1, S.h1r)); S.h2r = fmaf(c, p0, fmaf(b, p1, S.h2r));
+        f2_split(u0hb, p0, p1); S.h0i = fmaf(a, p0 + p1, S.h0i);
+        f2_split(u1hb, p0, p1); S.h1i = fmaf(b, p0, fmaf(c, p1, S.h1i)); S.h2i = fmaf(c, p0, fmaf(b, p1, S.h2i));
+        f2_split(u0c, p0, p1); S.c = fmaf(a, p0 + p1, S.c);
     }
     // G = (gr, -gs); dG/dn = -hgt (ha, hb) = (-hgt ha, hgt (-hb)); dG0/dn = -hgt c
     const float mh = -hgt;
