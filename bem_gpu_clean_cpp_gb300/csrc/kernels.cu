@@ -15,6 +15,7 @@
 #include <cmath>
 #include <cstdio>
 #include <mutex>
+#include <type_traits>
 #include <vector>
 
 #include "bem_common.h"
@@ -33,6 +34,10 @@ namespace bem {
 // ---------------------------------------------------------------------------
 __constant__ float4 c_qf[kMaxQ];
 __constant__ double c_qd[3][kMaxQ][3];
+// c_qs[v][q] = (xi1 - v1, xi2 - v2, w) in float for the map collapsed at
+// vertex v (reference coordinates (v1, v2)): the offsets from the collapse
+// vertex, formed in double (1 - rho minus 1 would cancel in float)
+__constant__ float4 c_qs[3][kMaxQ];
 __constant__ int c_nq;
 
 namespace {
@@ -57,6 +62,7 @@ void ensure_quadrature(int order) {
     int nq = order * order;
     std::vector<float4> qf(nq);
     std::vector<double> qd(3 * kMaxQ * 3, 0.0);
+    std::vector<float4> qs(3 * kMaxQ, make_float4(0.f, 0.f, 0.f, 0.f));
     int q = 0;
     for (int n = 0; n < order; n++) {
         double theta = 0.5 + 0.5 * gx[n];
@@ -68,15 +74,18 @@ void ensure_quadrature(int order) {
             double x2a = rho * theta, x2b = 1.0 - rho;                  // at vertex 2
             qf[q] = make_float4((float)x3a, (float)x3b, (float)w, 0.0f);
             double v[3][2] = {{x1a, x1b}, {x2a, x2b}, {x3a, x3b}};
+            const double off[3][2] = {{-rho, x1b}, {x2a, -rho}, {x3a, x3b}};   // minus (1, 0), (0, 1), (0, 0)
             for (int c = 0; c < 3; c++) {
                 qd[(c * kMaxQ + q) * 3 + 0] = v[c][0];
                 qd[(c * kMaxQ + q) * 3 + 1] = v[c][1];
                 qd[(c * kMaxQ + q) * 3 + 2] = w;
+                qs[c * kMaxQ + q] = make_float4((float)off[c][0], (float)off[c][1], (float)w, 0.0f);
             }
         }
     }
     CUDA_TRY(cudaMemcpyToSymbol(c_qf, qf.data(), sizeof(float4) * nq));
     CUDA_TRY(cudaMemcpyToSymbol(c_qd, qd.data(), sizeof(double) * qd.size()));
+    CUDA_TRY(cudaMemcpyToSymbol(c_qs, qs.data(), sizeof(float4) * qs.size()));
     CUDA_TRY(cudaMemcpyToSymbol(c_nq, &nq, sizeof(int)));
     if (dev < 64) g_quad_order[dev] = order;
     g_nq_host = nq;
@@ -1240,6 +1249,127 @@ __device__ void near_integrate(const double *h, const double *x, double k, int c
     o.c = scale * acc[12];
 }
 
+// The same integrals for the c64 assembly with FP32 point arithmetic (the
+// FP64 pipe runs at ~1/64 of FP32 on this part).  The pair's geometry is
+// prepared in FP64 so that no FP32 difference cancels:
+//   * singular pair (x is vertex v of the element, one leaf): d = dxi1 e1 +
+//     dxi2 e2 with the point's offsets from v (c_qs, formed in double), and
+//     the FP64 remainder p_v - x (zero up to the rounding of the edges);
+//   * near-singular leaf: d = d_l + s1 E1 + s2 E2 with d_l = (leaf corner -
+//     x) and the leaf's edge vectors E1, E2 formed in FP64 per leaf, so d's
+//     rounding is relative to the leaf's size, which the subdivision keeps
+//     comparable to r.
+// sin and cos are CUDA's full-accuracy sincosf (k r is of order one here),
+// the 13 sums are compensated (TwoSum with round-to-nearest intrinsics, so
+// nothing is contracted), and the lanes' sums are added in FP64.  At most
+// kNearF32Leaves leaves (their FP32 data go into the warp's leaf-code
+// scratch, free once the leaves are built); the caller takes the FP64
+// routine beyond that.
+constexpr int kNearF32Leaves = 48;
+constexpr int kNearLeafF = 10;   // floats per leaf: d_l (3), E1 (3), E2 (3), area
+static_assert(kNearF32Leaves * kNearLeafF <= 2 * kMaxLeaves, "leaf data fit the leaf-code scratch");
+
+__device__ __forceinline__ void ksum(float &s, float &c, float t) {
+    const float u = __fadd_rn(s, t), bb = __fsub_rn(u, s);
+    c = __fadd_rn(c, __fadd_rn(__fsub_rn(s, __fsub_rn(u, bb)), __fsub_rn(t, bb)));
+    s = u;
+}
+
+__device__ void near_integrate_f32(const double *h, const double *x, double k, int collapse, bool sing,
+                                   const Leaf *leaves, int nl, int nq, float *lg, NearOut &o) {
+    const int lane = threadIdx.x & 31;
+    const double *n = h + 9;
+    const double d3[3] = {h[0] - x[0], h[1] - x[1], h[2] - x[2]};
+    const double hgt = d3[0] * n[0] + d3[1] * n[1] + d3[2] * n[2];
+    const float3 e1 = make_float3((float)h[3], (float)h[4], (float)h[5]);
+    const float3 e2 = make_float3((float)h[6], (float)h[7], (float)h[8]);
+    const int cv = collapse - 1;
+    float3 dv = make_float3(0.f, 0.f, 0.f);   // singular: p_v - x
+    if (sing) {
+        const double v1 = cv == 0 ? 1.0 : 0.0, v2 = cv == 1 ? 1.0 : 0.0;
+        dv = make_float3((float)(d3[0] + v1 * h[3] + v2 * h[6]), (float)(d3[1] + v1 * h[4] + v2 * h[7]),
+                         (float)(d3[2] + v1 * h[5] + v2 * h[8]));
+    } else {
+        // per leaf (lanes over leaves): d_l, E1, E2 in FP64, then float
+        for (int l = lane; l < nl; l += 32) {
+            const Leaf t = leaves[l];
+            const double ea0 = (double)t.a[0] - t.c[0], ea1 = (double)t.a[1] - t.c[1];
+            const double eb0 = (double)t.b[0] - t.c[0], eb1 = (double)t.b[1] - t.c[1];
+            float *g = lg + (size_t)l * kNearLeafF;
+#pragma unroll
+            for (int dd = 0; dd < 3; dd++) {
+                g[dd] = (float)(d3[dd] + (double)t.c[0] * h[3 + dd] + (double)t.c[1] * h[6 + dd]);
+                g[3 + dd] = (float)(ea0 * h[3 + dd] + ea1 * h[6 + dd]);
+                g[6 + dd] = (float)(eb0 * h[3 + dd] + eb1 * h[6 + dd]);
+            }
+            g[9] = (float)fabs(ea0 * eb1 - ea1 * eb0);
+        }
+        __syncwarp();
+    }
+    float s[13], c[13];
+#pragma unroll
+    for (int i = 0; i < 13; i++) s[i] = c[i] = 0.f;
+    const float kf = (float)k;
+    for (int idx = lane; idx < nl * nq; idx += 32) {
+        const int l = idx / nq, q = idx - l * nq;
+        float3 d;
+        float x1, x2, w;
+        if (sing) {
+            const float4 t = c_qs[cv][q];
+            d = make_float3(fmaf(t.y, e2.x, fmaf(t.x, e1.x, dv.x)), fmaf(t.y, e2.y, fmaf(t.x, e1.y, dv.y)),
+                            fmaf(t.y, e2.z, fmaf(t.x, e1.z, dv.z)));
+            x1 = (cv == 0 ? 1.f : 0.f) + t.x;
+            x2 = (cv == 1 ? 1.f : 0.f) + t.y;
+            w = t.z;
+        } else {
+            const float4 t = c_qf[q];
+            const float *g = lg + (size_t)l * kNearLeafF;
+            d = make_float3(fmaf(t.y, g[6], fmaf(t.x, g[3], g[0])), fmaf(t.y, g[7], fmaf(t.x, g[4], g[1])),
+                            fmaf(t.y, g[8], fmaf(t.x, g[5], g[2])));
+            const Leaf &lf = leaves[l];
+            x1 = fmaf(t.y, lf.b[0] - lf.c[0], fmaf(t.x, lf.a[0] - lf.c[0], lf.c[0]));
+            x2 = fmaf(t.y, lf.b[1] - lf.c[1], fmaf(t.x, lf.a[1] - lf.c[1], lf.c[1]));
+            w = t.z * g[9];
+        }
+        const float r2 = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
+        const float r = sqrtf(r2), ri = 1.0f / r;
+        float sn, cs;
+        sincosf(kf * r, &sn, &cs);
+        const float ri2 = ri * ri;
+        const float gr = cs * ri, gs = sn * ri;
+        const float ha = ri2 * fmaf(kf, sn, gr), hb = ri2 * fmaf(kf, cs, -gs);
+        const float ri3 = ri2 * ri;
+        const float wn[3] = {w * x1, w * x2, w * (1.0f - x1 - x2)};
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            ksum(s[j], c[j], wn[j] * gr);
+            ksum(s[3 + j], c[3 + j], wn[j] * gs);
+            ksum(s[6 + j], c[6 + j], wn[j] * ha);
+            ksum(s[9 + j], c[9 + j], wn[j] * hb);
+        }
+        ksum(s[12], c[12], w * ri3);
+    }
+    double acc[13];
+#pragma unroll
+    for (int i = 0; i < 13; i++) {
+        acc[i] = (double)s[i] + (double)c[i];
+        for (int off = 16; off > 0; off >>= 1) acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], off);
+    }
+    // signs and the height: G = (gr, -gs), dG/dn = -hgt (ha, hb), dG0/dn = -hgt ri3
+#pragma unroll
+    for (int j = 0; j < 3; j++) acc[3 + j] = -acc[3 + j];
+#pragma unroll
+    for (int i = 6; i < 13; i++) acc[i] *= -hgt;
+    const double scale = h[12] / (4.0 * kPi);
+    for (int j = 0; j < 3; j++) {
+        o.gr[j] = scale * acc[j];
+        o.gi[j] = scale * acc[3 + j];
+        o.hr[j] = scale * acc[6 + j];
+        o.hi[j] = scale * acc[9 + j];
+    }
+    o.c = scale * acc[12];
+}
+
 __device__ __forceinline__ double2 incident_field(const DevSource &s, double k, const double *x) {
     double ph, amp_scale = 1.0;
     if (s.kind == BEM_SRC_PLANE) {
@@ -1308,7 +1438,11 @@ near_assembly_kernel(RowPoints rows, int N, GeoTables geo, Physics ph, int nq, T
             }
             __syncwarp();
             NearOut o;
-            near_integrate(h, x, ph.k, collapse, leaves, nl, nq, o);
+            if (std::is_same<TA, float2>::value && nl <= kNearF32Leaves)
+                near_integrate_f32(h, x, ph.k, collapse, vtx != 0, leaves, nl, nq,
+                                   reinterpret_cast<float *>(&codes_all[warp][0][0]), o);
+            else
+                near_integrate(h, x, ph.k, collapse, leaves, nl, nq, o);
             __syncwarp();
             if (lane == 0) {
                 const double bAr = h[13], bAi = h[14], bCr = h[15], bCi = h[16];
@@ -1434,7 +1568,7 @@ void launch_near_assembly(int prec, const RowPoints &rows, int N, const GeoTable
                           const void *beta_part, int ntiles, const DevSource *srcs, int S,
                           double2 *B, double2 *beta_out, const int *near_ptr, const int *near_ids,
                           cudaStream_t st) {
-    BEM_PROF("near_assembly_f64", st);
+    BEM_PROF("near_assembly", st);   // both precisions
     if (rows.R <= 0) return;
     BEM_CHECK_ARG(ph.near_depth >= 0 && ph.near_depth <= kMaxDepth, "near_depth must be in [0, 4]");
     int nq = quadrature_points();

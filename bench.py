@@ -793,7 +793,7 @@ def run_ours(args):
     A_bytes = 8.0 * R * N
     B_bytes = 16.0 * R
     asm_ms = (per_kernel.get("far_assembly_f32", {"avg_ms": 0})["avg_ms"] +
-              per_kernel.get("near_assembly_f64", {"avg_ms": 0})["avg_ms"])
+              per_kernel.get("near_assembly", {"avg_ms": 0})["avg_ms"])
 
     cpu = None
     if dist.rank == 0 and not args.no_cpu:
