@@ -1082,6 +1082,12 @@ __device__ __forceinline__ Leaf leaf_from_code(int code, int depth) {
 // reference-style recursion does), leaves and children are compacted with
 // ballots.  cur/nxt: per-warp scratch of kMaxLeaves codes each.  Returns the
 // number of leaves in every lane.
+// With fast32 (the c64 assembly) the split test is first evaluated in FP32
+// as |c - x|^2 against (eta d)^2 from the pair's offset p3 - x (rounded from
+// FP64) and the element's edges; outside a relative band of 1e-4 around the
+// threshold (FP32's error here is a few 1e-6) that decides, inside it the
+// FP64 test below does, so the leaves are the FP64 rule's.
+template <bool fast32>
 __device__ int build_leaves_warp(const double *h, const double *x, double eta, int depth_max, Leaf *leaves,
                                  int *cur, int *nxt) {
     const int lane = threadIdx.x & 31;
@@ -1089,6 +1095,13 @@ __device__ int build_leaves_warp(const double *h, const double *x, double eta, i
     if (lane == 0) cur[0] = 0;
     __syncwarp();
     int ncur = 1, nl = 0;
+    float3 d3f = make_float3(0.f, 0.f, 0.f), e1f = d3f, e2f = d3f;
+    if (fast32) {
+        d3f = make_float3((float)(h[0] - x[0]), (float)(h[1] - x[1]), (float)(h[2] - x[2]));
+        e1f = make_float3((float)h[3], (float)h[4], (float)h[5]);
+        e2f = make_float3((float)h[6], (float)h[7], (float)h[8]);
+    }
+    const float eta2f = (float)(eta * eta);
     for (int depth = 0; depth <= depth_max && ncur > 0; depth++) {
         int nnext = 0;
         for (int base = 0; base < ncur; base += 32) {
@@ -1097,7 +1110,27 @@ __device__ int build_leaves_warp(const double *h, const double *x, double eta, i
             const int code = valid ? cur[i] : 0;
             const Leaf t = leaf_from_code(code, depth);
             bool split = false;
-            if (valid && depth < depth_max) {
+            bool decided = false;
+            if (fast32 && valid && depth < depth_max) {
+                auto sq = [&](float u1, float u2) {   // |u1 e1 + u2 e2|^2
+                    const float vx = fmaf(u2, e2f.x, u1 * e1f.x), vy = fmaf(u2, e2f.y, u1 * e1f.y),
+                                vz = fmaf(u2, e2f.z, u1 * e1f.z);
+                    return fmaf(vz, vz, fmaf(vy, vy, vx * vx));
+                };
+                const float lab = sq(t.a[0] - t.b[0], t.a[1] - t.b[1]);
+                const float lbc = sq(t.b[0] - t.c[0], t.b[1] - t.c[1]);
+                const float lca = sq(t.c[0] - t.a[0], t.c[1] - t.a[1]);
+                const float c1 = (t.a[0] + t.b[0] + t.c[0]) * (1.0f / 3.0f), c2 = (t.a[1] + t.b[1] + t.c[1]) * (1.0f / 3.0f);
+                const float qx = fmaf(c2, e2f.x, fmaf(c1, e1f.x, d3f.x)), qy = fmaf(c2, e2f.y, fmaf(c1, e1f.y, d3f.y)),
+                            qz = fmaf(c2, e2f.z, fmaf(c1, e1f.z, d3f.z));
+                const float dc = fmaf(qz, qz, fmaf(qy, qy, qx * qx));
+                const float rhs = eta2f * fmaxf(lab, fmaxf(lbc, lca));
+                if (fabsf(dc - rhs) > 1e-4f * (dc + rhs)) {
+                    split = dc < rhs;
+                    decided = true;
+                }
+            }
+            if (!decided && valid && depth < depth_max) {
                 double ya[3], yb[3], yc[3], cen[3];
                 xi_point(h, t.a[0], t.a[1], ya);
                 xi_point(h, t.b[0], t.b[1], yb);
@@ -1261,7 +1294,7 @@ __device__ void near_integrate(const double *h, const double *x, double k, int c
 //     comparable to r.
 // sin and cos are CUDA's full-accuracy sincosf (k r is of order one here),
 // the 13 sums are compensated (TwoSum with round-to-nearest intrinsics, so
-// nothing is contracted), and the lanes' sums are added in FP64.  At most
+// nothing is contracted), also across the warp's lanes.  At most
 // kNearF32Leaves leaves (their FP32 data go into the warp's leaf-code
 // scratch, free once the leaves are built); the caller takes the FP64
 // routine beyond that.
@@ -1349,18 +1382,24 @@ __device__ void near_integrate_f32(const double *h, const double *x, double k, i
         }
         ksum(s[12], c[12], w * ri3);
     }
+    // lanes' (sum, compensation) pairs added by TwoSum across the warp, in FP32
     double acc[13];
 #pragma unroll
     for (int i = 0; i < 13; i++) {
-        acc[i] = (double)s[i] + (double)c[i];
-        for (int off = 16; off > 0; off >>= 1) acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], off);
+        float hi = s[i], lo = c[i];
+        for (int off = 16; off > 0; off >>= 1) {
+            const float h2 = __shfl_xor_sync(0xffffffffu, hi, off), l2 = __shfl_xor_sync(0xffffffffu, lo, off);
+            ksum(hi, lo, h2);
+            lo = __fadd_rn(lo, l2);
+        }
+        acc[i] = (double)hi + (double)lo;
     }
     // signs and the height: G = (gr, -gs), dG/dn = -hgt (ha, hb), dG0/dn = -hgt ri3
 #pragma unroll
     for (int j = 0; j < 3; j++) acc[3 + j] = -acc[3 + j];
 #pragma unroll
     for (int i = 6; i < 13; i++) acc[i] *= -hgt;
-    const double scale = h[12] / (4.0 * kPi);
+    const double scale = h[12] * (1.0 / (4.0 * kPi));   // a constant reciprocal: no FP64 division
     for (int j = 0; j < 3; j++) {
         o.gr[j] = scale * acc[j];
         o.gi[j] = scale * acc[3 + j];
@@ -1433,8 +1472,8 @@ near_assembly_kernel(RowPoints rows, int N, GeoTables geo, Physics ph, int nq, T
                 collapse = vtx;
                 if (lane == 0) leaves[0] = {{1.f, 0.f}, {0.f, 1.f}, {0.f, 0.f}};
             } else {
-                nl = build_leaves_warp(h, x, ph.near_eta, ph.near_depth, leaves, codes_all[warp][0],
-                                       codes_all[warp][1]);
+                nl = build_leaves_warp<std::is_same<TA, float2>::value>(h, x, ph.near_eta, ph.near_depth, leaves,
+                                                                         codes_all[warp][0], codes_all[warp][1]);
             }
             __syncwarp();
             NearOut o;
@@ -1711,7 +1750,7 @@ field_near_kernel(RowPoints pts, GeoTables geo, Physics ph, int nq, const TU *__
                                  __shfl_sync(0xffffffffu, nd.z, b)};
             const double *h = geo.geo_d + (size_t)kGeoD * eb;
             int nl = 0;
-            nl = build_leaves_warp(h, x, ph.near_eta, ph.near_depth, leaves, codes_all[warp][0], codes_all[warp][1]);
+            nl = build_leaves_warp<false>(h, x, ph.near_eta, ph.near_depth, leaves, codes_all[warp][0], codes_all[warp][1]);
             __syncwarp();
             NearOut o;
             near_integrate(h, x, ph.k, 3, leaves, nl, nq, o);
