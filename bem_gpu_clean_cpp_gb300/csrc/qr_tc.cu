@@ -990,23 +990,47 @@ void bem_solver_s::solve_qr_tc(bem_solve_info_t *info) {
     const int ldk = ((2 * kQrNB + 3) / 4) * 4;
     q_A.ensure(sizeof(float2) * (ldq * ncq + 8));
     q_tau.ensure(sizeof(float2) * (size_t)n);
-    qt_v.ensure(sizeof(float2) * ldv * kQrNB);
-    qt_vrr.ensure(sizeof(float) * 2 * (size_t)m * ldk);
-    qt_t.ensure(sizeof(float2) * kQrNB * kQrNB + sizeof(float) * 2 * kQrNB * kQrNB);
-    qt_z.ensure(sizeof(float) * 2 * kQrNB * ncq);
-    qt_opv.ensure(tc_operand_bytes(2 * m, 2 * kQrNB, 2));
-    qt_opw.ensure(tc_operand_bytes(2 * kQrNB, (int)ncq, 2));
-    // split-K partial sums: the largest any panel's three products plan (a
+    // Look-ahead: panel j + 1 is factored (on a high-priority stream) while
+    // the trailing update of panel j runs on the solver's stream, so the
+    // panel's buffers (V, its interleaved form, T and G, the packed V) come
+    // twice, by panel parity, and the update's (Z, the packed W', split-K
+    // partial sums) twice, one set per stream.
+    auto r256 = [](size_t b) { return (b + 255) & ~size_t(255); };
+    const size_t v_b = r256(sizeof(float2) * ldv * kQrNB), vrr_b = r256(sizeof(float) * 2 * (size_t)m * ldk),
+                 t_b = r256(sizeof(float2) * kQrNB * kQrNB + sizeof(float) * 2 * kQrNB * kQrNB),
+                 opv_b = r256(tc_operand_bytes(2 * m, 2 * kQrNB, 2)), z_b = r256(sizeof(float) * 2 * kQrNB * ncq),
+                 opw_b = r256(tc_operand_bytes(2 * kQrNB, (int)ncq, 2));
+    qt_v.ensure(2 * v_b);
+    qt_vrr.ensure(2 * vrr_b);
+    qt_t.ensure(2 * t_b);
+    qt_opv.ensure(2 * opv_b);
+    qt_z.ensure(2 * z_b);
+    qt_opw.ensure(2 * opw_b);
+    auto at = [](DevMem &d, size_t b, int i) { return static_cast<void *>(static_cast<char *>(d.p) + b * i); };
+    // split-K partial sums: the largest any panel's products plan, per set (a
     // later panel with fewer tiles may split more than the first)
-    size_t pf = 0;
+    size_t pf_n = 1, pf_w = 1;
     for (int j0 = 0; j0 < n; j0 += kQrNB) {
-        const int pc = std::min(kQrNB, n - j0), mr = m - j0, nct = (int)ncq - j0 - pc;
-        pf = std::max(pf, tc_gemm_part_floats(pc, 2 * mr, 2 * pc, 2));
-        if (nct > 0)
-            pf = std::max({pf, tc_gemm_part_floats(nct, 2 * mr, 2 * pc, 2), tc_gemm_part_floats(2 * mr, 2 * pc, nct, 2)});
+        const int pc = std::min(kQrNB, n - j0), mr = m - j0, c1 = j0 + pc;
+        const int pc2 = c1 < n ? std::min(kQrNB, n - c1) : 0, nw = (int)ncq - c1 - pc2;
+        pf_n = std::max(pf_n, tc_gemm_part_floats(pc, 2 * mr, 2 * pc, 2));
+        if (pc2 > 0)
+            pf_n = std::max({pf_n, tc_gemm_part_floats(pc2, 2 * mr, 2 * pc, 2), tc_gemm_part_floats(2 * mr, 2 * pc, pc2, 2)});
+        if (nw > 0)
+            pf_w = std::max({pf_w, tc_gemm_part_floats(nw, 2 * mr, 2 * pc, 2), tc_gemm_part_floats(2 * mr, 2 * pc, nw, 2)});
     }
-    if (pf) qt_part.ensure(sizeof(float) * pf);
-    const size_t part_floats = qt_part.bytes / sizeof(float);
+    const size_t pn_b = r256(sizeof(float) * pf_n), pw_b = r256(sizeof(float) * pf_w);
+    qt_part.ensure(pn_b + pw_b);
+    float *const part_set[2] = {qt_part.as<float>(), reinterpret_cast<float *>(static_cast<char *>(qt_part.p) + pn_b)};
+    const size_t part_cap[2] = {pn_b / sizeof(float), pw_b / sizeof(float)};
+    if (!qr_aux) {
+        int least = 0, greatest = 0;
+        CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        CUDA_TRY(cudaStreamCreateWithPriority(&qr_aux, cudaStreamNonBlocking, greatest));
+        for (auto &e : qr_ev) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    cudaEvent_t ev_in = qr_ev[0], ev_out = qr_ev[1], ev_ready[2] = {qr_ev[2], qr_ev[3]},
+                ev_wide[2] = {qr_ev[4], qr_ev[5]};
     qt_scal.ensure(sizeof(float) * 8);
     qt_dinv.ensure(sizeof(float2) * (size_t)((n + kQrTB - 1) / kQrTB) * kQrTB * kQrTB);
     d_status.ensure(4 * sizeof(int));
@@ -1014,8 +1038,6 @@ void bem_solver_s::solve_qr_tc(bem_solve_info_t *info) {
     CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), stream));
     float2 *Q = q_A.as<float2>();
     float *sc = qt_scal.as<float>();
-    float2 *T = qt_t.as<float2>();
-    float *G = reinterpret_cast<float *>(T + kQrNB * kQrNB);
     {
         BEM_PROF("qr_copy", stream);
         const dim3 g((n + 31) / 32, (m + 31) / 32);
@@ -1043,57 +1065,85 @@ void bem_solver_s::solve_qr_tc(bem_solve_info_t *info) {
     const int CL = smem_for(m, 16) <= smax ? CL16 : 8;
     if (smem_for(m, CL) > smax)
         BEM_FAIL(BEM_ERR_TOO_LARGE, "QR_TC: " + std::to_string(m) + " rows do not fit the panel cluster's shared memory");
-    for (int j0 = 0; j0 < n; j0 += kQrNB) {
-        const int pc = std::min(kQrNB, n - j0), mr = m - j0;
-        const int nct = (int)ncq - j0 - pc;
+    // C -= V T^H (V^H C) for the trailing columns C (ncols of them, interleaved
+    // real, leading dimension 2 ldq) with update set u on stream st
+    auto update = [&](cudaStream_t st, int u, float *C, int ncols, int mr, int pc, const TcOperand &opv,
+                      const float2 *Tp, const float *Vrr) {
+        BEM_PROF("qr_update", st);
+        float *Z = static_cast<float *>(at(qt_z, z_b, u));
+        tc_gemm(C, 2 * ldq, false, ncols, 2 * mr, sc, opv, Z, ncols, part_set[u], part_cap[u], status, st);
+        TcOperand opw = tc_operand_view(at(qt_opw, opw_b, u), 2 * pc, ncols, 2);
+        qr_pack_tw_kernel<2><<<(ncols + kQrTwCols - 1) / kQrTwCols, kQrNB * kQrTwGroups, kQrTwSmem, st>>>(
+            ncols, pc, Z, Tp, opw.Kp, opw.ncols_pad, opw.planes, opw.col_inv);
+        count_launch();
+        tc_gemm(Vrr, ldk, false, 2 * mr, 2 * pc, sc + 2, opw, C, 2 * ldq, part_set[u], part_cap[u], status, st, true);
+    };
+    // Panel j on qr_aux, its T and the update of panel j + 1's columns
+    // (narrow) there too, the update of the rest (wide, B included) on the
+    // solver's stream.  The narrow update of panel j waits for the wide
+    // update of panel j - 1 (it also updated those columns); so does
+    // everything after it on qr_aux, including panel j + 1, whose columns the
+    // wide update of panel j - 1 touched too, and the reuse of panel j - 1's
+    // buffers by panel j + 1.
+    cudaStream_t sa = qr_aux;
+    CUDA_TRY(cudaEventRecord(ev_in, stream));
+    CUDA_TRY(cudaStreamWaitEvent(sa, ev_in, 0));
+    bool wide_prev = false;
+    for (int j0 = 0, step = 0; j0 < n; j0 += kQrNB, step++) {
+        const int pc = std::min(kQrNB, n - j0), mr = m - j0, par = step & 1;
+        const int c1 = j0 + pc;
+        const int pc2 = c1 < n ? std::min(kQrNB, n - c1) : 0;   // the next panel's columns
+        const int nw = (int)ncq - c1 - pc2;                      // the rest, B included
         {
-            BEM_PROF("qr_panel", stream);
+            BEM_PROF("qr_panel", sa);
             const int rb = (mr + CL - 1) / CL;
             cudaLaunchConfig_t cfg = {};
             cfg.gridDim = dim3(CL);
             cfg.blockDim = dim3(kQrNT);
             cfg.dynamicSmemBytes = smem_for(mr, CL);
-            cfg.stream = stream;
-            cudaLaunchAttribute at[1];
-            at[0].id = cudaLaunchAttributeClusterDimension;
-            at[0].val.clusterDim.x = CL;
-            at[0].val.clusterDim.y = 1;
-            at[0].val.clusterDim.z = 1;
-            cfg.attrs = at;
+            cfg.stream = sa;
+            cudaLaunchAttribute at_[1];
+            at_[0].id = cudaLaunchAttributeClusterDimension;
+            at_[0].val.clusterDim.x = CL;
+            at_[0].val.clusterDim.y = 1;
+            at_[0].val.clusterDim.z = 1;
+            cfg.attrs = at_;
             cfg.numAttrs = 1;
             CUDA_TRY(cudaLaunchKernelEx(&cfg, qr_panel_kernel, Q, ldq, m, j0, pc, rb, q_tau.as<float2>() + j0));
             count_launch();
         }
-        if (nct <= 0) continue;
-        float2 *P = Q + (size_t)j0 * ldq + j0;             // the panel
-        float *C = reinterpret_cast<float *>(P + (size_t)pc * ldq);   // the trailing columns (interleaved real)
+        if (pc2 + nw <= 0) continue;
+        float2 *P = Q + (size_t)j0 * ldq + j0;   // the panel
+        float2 *Vp = static_cast<float2 *>(at(qt_v, v_b, par));
+        float *Vrr = static_cast<float *>(at(qt_vrr, vrr_b, par));
+        float2 *Tp = static_cast<float2 *>(at(qt_t, t_b, par));
+        float *Gp = reinterpret_cast<float *>(Tp + kQrNB * kQrNB);
+        const TcOperand opv = tc_operand_view(at(qt_opv, opv_b, par), 2 * mr, 2 * pc, 2);
         {
-            BEM_PROF("qr_t", stream);
-            qr_vfull_kernel<<<dim3((mr + 255) / 256, pc), 256, 0, stream>>>(mr, pc, P, ldq, qt_v.as<float2>(), ldv);
-            TcOperand opv = tc_operand_view(qt_opv.p, 2 * mr, 2 * pc, 2);
-            tc_pack_cplx_f32(qt_v.as<float2>(), mr, pc, opv, stream, ldv, true);
+            BEM_PROF("qr_t", sa);
+            qr_vfull_kernel<<<dim3((mr + 255) / 256, pc), 256, 0, sa>>>(mr, pc, P, ldq, Vp, ldv);
+            TcOperand opvw = opv;
+            tc_pack_cplx_f32(Vp, mr, pc, opvw, sa, ldv, true);
             // G = V^H V (pc x pc): conj(V^T) V with V^T's rows the columns of Vf
-            tc_gemm(reinterpret_cast<const float *>(qt_v.p), 2 * ldv, false, pc, 2 * mr, sc + 2, opv, G, pc,
-                    qt_part.as<float>(), part_floats, status, stream);
-            qr_larft_kernel<<<1, kQrLarftNT, kQrLarftSmem, stream>>>(pc, G, q_tau.as<float2>() + j0, T);
-            count_launch(2);
+            tc_gemm(reinterpret_cast<const float *>(Vp), 2 * ldv, false, pc, 2 * mr, sc + 2, opv, Gp, pc,
+                    part_set[0], part_cap[0], status, sa);
+            qr_larft_kernel<<<1, kQrLarftNT, kQrLarftSmem, sa>>>(pc, Gp, q_tau.as<float2>() + j0, Tp);
+            qr_vrr_kernel<<<mr, kQrNB, 0, sa>>>(mr, pc, Vp, ldv, Vrr, ldk);
+            count_launch(3);
         }
-        {
-            BEM_PROF("qr_update", stream);
-            // Z = C^H V (nct x pc), W' = T^H Z^H packed, C -= V W'
-            TcOperand opv = tc_operand_view(qt_opv.p, 2 * mr, 2 * pc, 2);
-            tc_gemm(C, 2 * ldq, false, nct, 2 * mr, sc, opv, qt_z.as<float>(), nct, qt_part.as<float>(), part_floats,
-                    status, stream);
-            TcOperand opw = tc_operand_view(qt_opw.p, 2 * pc, nct, 2);
-            qr_pack_tw_kernel<2><<<(nct + kQrTwCols - 1) / kQrTwCols, kQrNB * kQrTwGroups, kQrTwSmem, stream>>>(
-                nct, pc, qt_z.as<float>(), T, opw.Kp, opw.ncols_pad, opw.planes, opw.col_inv);
-            qr_vrr_kernel<<<mr, kQrNB, 0, stream>>>(mr, pc, qt_v.as<float2>(), ldv, qt_vrr.as<float>(), ldk);
-            count_launch(2);
-            tc_gemm(qt_vrr.as<float>(), ldk, false, 2 * mr, 2 * pc, sc + 2, opw, C, 2 * ldq, qt_part.as<float>(),
-                    part_floats, status, stream, true);
+        if (wide_prev) CUDA_TRY(cudaStreamWaitEvent(sa, ev_wide[par ^ 1], 0));
+        if (pc2 > 0) update(sa, 0, reinterpret_cast<float *>(P + (size_t)pc * ldq), pc2, mr, pc, opv, Tp, Vrr);
+        CUDA_TRY(cudaEventRecord(ev_ready[par], sa));
+        wide_prev = nw > 0;
+        if (nw > 0) {
+            CUDA_TRY(cudaStreamWaitEvent(stream, ev_ready[par], 0));
+            update(stream, 1, reinterpret_cast<float *>(P + (size_t)(pc + pc2) * ldq), nw, mr, pc, opv, Tp, Vrr);
+            CUDA_TRY(cudaEventRecord(ev_wide[par], stream));
         }
         KERNEL_CHECK();
     }
+    CUDA_TRY(cudaEventRecord(ev_out, sa));
+    CUDA_TRY(cudaStreamWaitEvent(stream, ev_out, 0));
     // X = R^{-1} (Q^H B)[0:n]
     double2 *X = d_x.as<double2>();
     {

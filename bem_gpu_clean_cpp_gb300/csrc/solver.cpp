@@ -171,6 +171,10 @@ bem_solver_s::~bem_solver_s() {
     for (auto &e : ev_res)
         if (e) cudaEventDestroy(e);
     if (h_stage) cudaFreeHost(h_stage);
+    if (qr_aux) cudaStreamSynchronize(qr_aux);
+    for (auto &e : qr_ev)
+        if (e) cudaEventDestroy(e);
+    if (qr_aux) cudaStreamDestroy(qr_aux);
     if (stream) cudaStreamDestroy(stream);
     if (cur >= 0 && cur != device) cudaSetDevice(cur);
 }
@@ -721,10 +725,11 @@ size_t bem_solver_s::estimate_bytes(int N, int E, int M, int S, int method, cons
         b += 48 * (m + 1) * 160;                                                     // Arnoldi step partials
     } else if (method == BEM_SOLVE_QR_TC) {
         const size_t nb = 128, rp = r + 1;
-        b += 8 * (rp * (n + s) + 8) + 8 * n;                               // [A | B] c64, taus
-        b += 8 * rp * nb + 4 * 2 * r * 256 + 8 * nb * nb + 8 * nb * nb;  // V, Vrr, T, G
-        b += 4 * 2 * nb * (n + s) + tc_operand_bytes((int)(2 * r), (int)(2 * nb), 2) +
-             tc_operand_bytes((int)(2 * nb), (int)(n + s), 2) + 4 * tc_gemm_part_floats_bound((int)(2 * r), (int)(n + s));
+        b += 8 * (rp * (n + s) + 8) + 8 * n;                                     // [A | B] c64, taus
+        b += 2 * (8 * rp * nb + 4 * 2 * r * 256 + 8 * nb * nb + 8 * nb * nb);  // V, Vrr, T, G: per panel parity
+        b += 2 * (4 * 2 * nb * (n + s) + tc_operand_bytes((int)(2 * r), (int)(2 * nb), 2) +
+                  tc_operand_bytes((int)(2 * nb), (int)(n + s), 2) +
+                  4 * tc_gemm_part_floats_bound((int)(2 * r), (int)(n + s))) + 4096;   // per update set
         b += 16 * r + 16 * n + 8 * (2 * std::max(n, r) + 2) +
              16 * n * (size_t)std::max(gemv_h_splits((int)r, N), gemv_h_f64_splits((int)r, N));
         b += 8 * (n + 64) * 64;                                              // diagonal-block inverses

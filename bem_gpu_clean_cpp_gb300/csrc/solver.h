@@ -122,6 +122,10 @@ struct bem_solver_s {
     // and V^H V, Z = C^H V, the packed right-hand operands, split-K partial
     // sums, scales
     bem::DevMem qt_v, qt_vrr, qt_t, qt_z, qt_opv, qt_opw, qt_part, qt_scal, qt_dinv;
+    // QR_TC look-ahead: a high-priority stream for the panel chain and its
+    // events (created on first use)
+    cudaStream_t qr_aux = nullptr;
+    cudaEvent_t qr_ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     // field workspace
     bem::DevMem f_rows_f, f_rows_d, f_part, f_near, f_out, f_u;
 
