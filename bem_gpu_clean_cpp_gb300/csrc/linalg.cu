@@ -834,35 +834,6 @@ template <int NT>
 constexpr size_t nt_smem() { return (size_t)kNtNS * kNtRPS * NT * kNtCPT * sizeof(float2); }
 constexpr long long kNtWaitCycles = 2000000000LL;                          // ~1 s at 2 GHz
 
-__device__ __forceinline__ uint32_t cluster_addr(const void *p, uint32_t rank) {
-    uint32_t r;
-    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(smem_u32(p)), "r"(rank));
-    return r;
-}
-// 8 bytes into another CTA's shared memory, completing on its mbarrier.
-__device__ __forceinline__ void st_async_f2(uint32_t addr, float2 v, uint32_t bar) {
-    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.v2.f32 [%0], {%1, %2}, [%3];" ::"r"(addr),
-                 "f"(v.x), "f"(v.y), "r"(bar)
-                 : "memory");
-}
-// Bounded wait with cluster-scope acquire (the bytes came from other CTAs).
-__device__ __forceinline__ bool mbar_wait_cluster_bounded(uint64_t *bar, uint32_t parity, long long limit,
-                                                          volatile int *abort) {
-    const long long t0 = clock64();
-    for (;;) {
-        uint32_t ok;
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n\t"
-            "selp.u32 %0, 1, 0, p;\n\t}"
-            : "=r"(ok)
-            : "r"(smem_u32(bar)), "r"(parity)
-            : "memory");
-        if (ok) return true;
-        if (*abort || clock64() - t0 > limit) return false;
-    }
-}
-
 template <int NT>
 __global__ void __launch_bounds__(NT, 512 / NT)
 normal_op_tma_kernel(int R, int N, const float2 *__restrict__ A, size_t lda, const float2 *__restrict__ v,

@@ -42,6 +42,7 @@
 #include "solver.h"
 #include "tc_gemm.h"
 #include "tc_split.cuh"
+#include "tma.h"
 
 namespace bem {
 namespace {
@@ -56,6 +57,7 @@ constexpr int kQrTB = 64;       // block of the triangular solves
 // Refinement target: relative normal-equation residual ||A^H (b - A x)|| /
 // ||A^H b|| (stagnation at the precision of the FP64-accurate products ends
 // it earlier).
+constexpr long long kQrWaitCycles = 2000000000LL;   // ~1 s at 2 GHz: the panel's bounded waits
 constexpr double kQrRefineTol = 1e-14;
 constexpr double kQrStagnationOk = 1e-11;
 static_assert(kQrW == 16, "the panel kernel pairs lanes c and c + 16 of a warp on one leaf column");
@@ -73,12 +75,12 @@ __device__ __forceinline__ float2 cjmul(float2 a, float2 b) {
 // banks), then the reduction slots.
 struct PanelLayout {
     int lds;
-    size_t leaf, red, sums, prev, gpart, gram, wpart, gsum, tmat, ysum, scratch, taus, total;
+    size_t leaf, tin, sums, prev, gpart, gram, wpart, gsum, tmat, ysum, scratch, taus, total;
     __host__ __device__ PanelLayout(int rb) {
         lds = ((rb + 15) / 16) * 16 + 1;
         size_t o = 0;
         leaf = o;    o += (size_t)kQrW * lds;
-        red = o;     o += 2 * 2 * kQrW;                  // [parity][d_c | pivot-row x_c]: this CTA's column sums
+        tin = o;     o += 2 * kQrCL * 2 * kQrW;          // [slot][source CTA][d_c | pivot-row x_c]: column sums received
         sums = o;    o += 2 * kQrW;                      // the cluster's sums of red
         prev = o;    o += 2;                             // (scal, beta) of the column whose scaling is pending
         gpart = o;   o += 2 * kQrW * kQrW;               // two row halves of this CTA's V^H V
@@ -133,7 +135,8 @@ __device__ __forceinline__ void qr_reflector(float t, float2 a, float2 &tau, flo
 // diagonal, R on and above it); tau_out[0..pc) receives the taus.  One
 // cluster of gridDim.x CTAs; CTA q owns the rows j0 + q rb .. + rb - 1.
 //
-// Per column one cluster-wide reduction: from the column x as it stands
+// Per column one cluster-wide reduction (pushed by st.async into every CTA's
+// mbarrier-tracked receive slot, no cluster barrier): from the column x as it stands
 // (before scaling), every CTA sums over its rows below the pivot g the
 // products conj(x_i) x_c[i] for the column itself (|x|^2) and the leaf's
 // later columns (d_c), and the owner of row g adds the pivot-row values
@@ -145,11 +148,27 @@ __device__ __forceinline__ void qr_reflector(float t, float2 a, float2 &tau, flo
 // diagonal), and applied to the panel's remaining columns as a block
 // reflector (I - V T V^H)^H.
 __global__ void __launch_bounds__(kQrNT, 1)
-qr_panel_kernel(float2 *__restrict__ Q, size_t ldq, int m, int j0, int pc, int rb, float2 *__restrict__ tau_out) {
+qr_panel_kernel(float2 *__restrict__ Q, size_t ldq, int m, int j0, int pc, int rb, float2 *__restrict__ tau_out,
+                int *status) {
     cg::cluster_group cluster = cg::this_cluster();
     const int CL = (int)cluster.num_blocks();
     const int q = (int)cluster.block_rank();
     extern __shared__ __align__(16) float2 ps[];
+    // the per-column exchange: every CTA pushes its 2 kQrW partial sums into
+    // every CTA's receive slot (column k into slot k % 2) with st.async,
+    // completing bytes on that slot's mbarrier
+    __shared__ __align__(8) uint64_t col_bar[2];
+    __shared__ int col_abort;
+    const uint32_t col_bytes = (uint32_t)(CL * 2 * kQrW * sizeof(float2));
+    if (threadIdx.x == 0) {
+        mbar_init(&col_bar[0], 1);
+        mbar_init(&col_bar[1], 1);
+        col_abort = 0;
+        mbar_fence_init();
+        mbar_arrive_expect_tx(&col_bar[0], col_bytes);
+        mbar_arrive_expect_tx(&col_bar[1], col_bytes);
+    }
+    cluster.sync();   // every CTA's barriers are armed before any column sum is sent
     const PanelLayout lay(rb);
     const int lds = lay.lds;
     float2 *L = ps + lay.leaf;
@@ -170,7 +189,6 @@ qr_panel_kernel(float2 *__restrict__ Q, size_t ldq, int m, int j0, int pc, int r
             for (int i = tid; i < nrows; i += kQrNT) L[(size_t)cc * lds + i] = Q[(size_t)(G0 + cc) * ldq + r0 + i];
         __syncthreads();
         for (int jj = 0; jj < lw; jj++) {
-            const int par = jj & 1;
             const int g = G0 + jj;                        // pivot row
             const int ib = max(0, g + 1 - r0);            // first local row below the pivot
             const bool own = g >= r0 && g < r0 + nrows;   // this CTA holds the pivot row
@@ -195,22 +213,37 @@ qr_panel_kernel(float2 *__restrict__ Q, size_t ldq, int m, int j0, int pc, int r
             acc.y += __shfl_xor_sync(0xffffffffu, acc.y, 16);
             if (lane < kQrW) scratch[warp * kQrW + lane] = acc;
             __syncthreads();
-            if (tid < kQrW) {
-                float2 t = make_float2(0.f, 0.f);
-                for (int w = 0; w < kQrNT / 32; w++) {
-                    t.x += scratch[w * kQrW + tid].x;
-                    t.y += scratch[w * kQrW + tid].y;
-                }
-                ps[lay.red + par * 2 * kQrW + tid] = t;
-                ps[lay.red + par * 2 * kQrW + kQrW + tid] =
-                    (own && tid >= jj && tid < lw) ? L[(size_t)tid * lds + (g - r0)] : make_float2(0.f, 0.f);
-            }
-            cluster.sync();
-            // (2) the cluster's sums
+            // (2) exchange: warp 0 pushes this CTA's 2 kQrW values (the d_c
+            // sums, then the pivot row's x_c) to every CTA, waits for the
+            // cluster's and adds them in rank order (the same order everywhere)
             if (tid < 2 * kQrW) {
-                const int cc = tid % kQrW;
-                ps[lay.sums + tid] = (cc >= jj && cc < lw) ? cluster_sum(peer, lay.red + par * 2 * kQrW, tid, CL)
-                                                           : make_float2(0.f, 0.f);
+                const int cc = tid % kQrW, kx = l0 + jj, slot = kx & 1;
+                float2 t = make_float2(0.f, 0.f);
+                if (tid < kQrW) {
+                    for (int w = 0; w < kQrNT / 32; w++) {
+                        t.x += scratch[w * kQrW + tid].x;
+                        t.y += scratch[w * kQrW + tid].y;
+                    }
+                } else if (own && cc >= jj && cc < lw) {
+                    t = L[(size_t)cc * lds + (g - r0)];
+                }
+                const float2 *mine = ps + lay.tin + ((size_t)slot * kQrCL + q) * 2 * kQrW + tid;
+                for (int p = 0; p < CL; p++)
+                    st_async_f2(cluster_addr(mine, (uint32_t)p), t, cluster_addr(&col_bar[slot], (uint32_t)p));
+                if (!mbar_wait_cluster_bounded(&col_bar[slot], (uint32_t)((kx >> 1) & 1), kQrWaitCycles, &col_abort)) {
+                    col_abort = 1;
+                    atomicExch(status, 1);
+                }
+                float2 u = make_float2(0.f, 0.f);
+                for (int p = 0; p < CL; p++) {
+                    const float2 v = ps[lay.tin + ((size_t)slot * kQrCL + p) * 2 * kQrW + tid];
+                    u.x += v.x;
+                    u.y += v.y;
+                }
+                ps[lay.sums + tid] = (cc >= jj && cc < lw) ? u : make_float2(0.f, 0.f);
+                // re-arm the slot for column kx + 2: its bytes can come only
+                // after this CTA's column kx + 1 push, which follows
+                if (tid == 0 && !col_abort) mbar_arrive_expect_tx(&col_bar[slot], col_bytes);
             }
             __syncthreads();
             // (3) the reflector (every thread), then x_c -= v y_c with
@@ -942,8 +975,11 @@ int qr_cluster_size(size_t smem16) {
         int maxs = 0, dev = 0;
         err = cudaGetDevice(&dev);
         if (err == cudaSuccess) err = cudaDeviceGetAttribute(&maxs, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        cudaFuncAttributes fa{};
+        if (err == cudaSuccess) err = cudaFuncGetAttributes(&fa, qr_panel_kernel);   // its static shared memory
         if (err == cudaSuccess)
-            err = cudaFuncSetAttribute(qr_panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, maxs);
+            err = cudaFuncSetAttribute(qr_panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       maxs - (int)fa.sharedSizeBytes);
         if (err == cudaSuccess)
             err = cudaFuncSetAttribute(qr_larft_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)kQrLarftSmem);
@@ -1054,11 +1090,13 @@ void bem_solver_s::solve_qr_tc(bem_solve_info_t *info) {
         KERNEL_CHECK();
     }
     // panel cluster: 16 CTAs when schedulable and the rows fit
-    const size_t smax = [] {
+    const size_t smax = [] {   // the panel kernel's dynamic shared memory at most
         int dev = 0, v = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        return (size_t)v;
+        cudaFuncAttributes fa{};
+        cudaFuncGetAttributes(&fa, qr_panel_kernel);
+        return (size_t)v - fa.sharedSizeBytes;
     }();
     auto smem_for = [](int rows, int cl) { return sizeof(float2) * PanelLayout((rows + cl - 1) / cl).total; };
     const int CL16 = qr_cluster_size(smem_for(m, 16));   // also sets the kernels' shared-memory limits
@@ -1109,7 +1147,8 @@ void bem_solver_s::solve_qr_tc(bem_solve_info_t *info) {
             at_[0].val.clusterDim.z = 1;
             cfg.attrs = at_;
             cfg.numAttrs = 1;
-            CUDA_TRY(cudaLaunchKernelEx(&cfg, qr_panel_kernel, Q, ldq, m, j0, pc, rb, q_tau.as<float2>() + j0));
+            CUDA_TRY(cudaLaunchKernelEx(&cfg, qr_panel_kernel, Q, ldq, m, j0, pc, rb, q_tau.as<float2>() + j0,
+                                        status));
             count_launch();
         }
         if (pc2 + nw <= 0) continue;
