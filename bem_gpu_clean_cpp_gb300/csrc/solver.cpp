@@ -203,14 +203,18 @@ void bem_solver_s::set_geometry(const double *pnts, int num_pnts, const int *ele
             return build_host_tiles(N, E, h_nodes, h_elems, cap);
         });
     }
-    max_edge = 0.0;
-    for (int e = 0; e < E; e++)
+    // the longest edge: the largest squared length, one square root
+    double max_edge2 = 0.0;
+    for (int e = 0; e < E; e++) {
+        const double *v[3] = {&h_nodes[3 * (size_t)h_elems[3 * e]], &h_nodes[3 * (size_t)h_elems[3 * e + 1]],
+                              &h_nodes[3 * (size_t)h_elems[3 * e + 2]]};
         for (int a = 0; a < 3; a++) {
-            const double *p = &h_nodes[3 * (size_t)h_elems[3 * e + a]];
-            const double *q = &h_nodes[3 * (size_t)h_elems[3 * e + (a + 1) % 3]];
-            max_edge = std::max(max_edge, std::sqrt((p[0] - q[0]) * (p[0] - q[0]) + (p[1] - q[1]) * (p[1] - q[1]) +
-                                                    (p[2] - q[2]) * (p[2] - q[2])));
+            const double *p = v[a], *q = v[a == 2 ? 0 : a + 1];
+            max_edge2 = std::max(max_edge2, (p[0] - q[0]) * (p[0] - q[0]) + (p[1] - q[1]) * (p[1] - q[1]) +
+                                                (p[2] - q[2]) * (p[2] - q[2]));
         }
+    }
+    max_edge = std::sqrt(max_edge2);
     h_bc.resize(6 * (size_t)E);
     if (bc) {
         std::memcpy(h_bc.data(), bc, sizeof(double) * 6 * (size_t)E);
@@ -225,11 +229,16 @@ void bem_solver_s::set_geometry(const double *pnts, int num_pnts, const int *ele
     h_rows.assign(h_nodes.begin(), h_nodes.end());
     if (M) h_rows.insert(h_rows.end(), chief, chief + 3 * (size_t)M);
     {
-        double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-        for (size_t i = 0; i < h_rows.size(); i++) {
-            lo[i % 3] = std::min(lo[i % 3], h_rows[i]);
-            hi[i % 3] = std::max(hi[i % 3], h_rows[i]);
+        double *lo = row_lo, *hi = row_hi;   // the box of the row points (nodes and CHIEF points)
+        for (int d = 0; d < 3; d++) {
+            lo[d] = 1e300;
+            hi[d] = -1e300;
         }
+        for (size_t i = 0; i + 2 < h_rows.size(); i += 3)
+            for (int d = 0; d < 3; d++) {
+                lo[d] = std::min(lo[d], h_rows[i + d]);
+                hi[d] = std::max(hi[d], h_rows[i + d]);
+            }
         extent = std::sqrt((hi[0] - lo[0]) * (hi[0] - lo[0]) + (hi[1] - lo[1]) * (hi[1] - lo[1]) +
                            (hi[2] - lo[2]) * (hi[2] - lo[2]));
     }
@@ -314,11 +323,7 @@ void bem_solver_s::ensure_near_list() {
     // Grid of element centroids: cell edge >= the largest near radius
     // (near_eta x element diameter) and >= the longest element (vertex pairs),
     // over the box of all row points and nodes; at most ~4M cells.
-    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-    for (size_t i = 0; i < h_rows.size(); i++) {
-        lo[i % 3] = std::min(lo[i % 3], h_rows[i]);
-        hi[i % 3] = std::max(hi[i % 3], h_rows[i]);
-    }
+    const double *lo = row_lo, *hi = row_hi;   // formed by set_geometry
     double cell = std::max(1.0, opt.near_eta) * max_edge * 1.01 + 1e-12;
     const double span = std::max({hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2], 1e-12});
     cell = std::max(cell, span / 160.0);

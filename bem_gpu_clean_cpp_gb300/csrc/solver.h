@@ -76,6 +76,7 @@ struct bem_solver_s {
     bem::DevMem d_near_ptr, d_near_ids, d_grid_start, d_grid_elems;
     double max_edge = 0.0;   // longest element edge
     double extent = 0.0;     // diagonal of the box around nodes and CHIEF points
+    double row_lo[3] = {0.0, 0.0, 0.0}, row_hi[3] = {0.0, 0.0, 0.0};   // that box
 
     struct Tiles {
         bool valid = false;
