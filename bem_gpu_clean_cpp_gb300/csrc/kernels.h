@@ -155,9 +155,11 @@ void launch_gemv_h_c64(int R, int N, const float2 *A, size_t lda, const void *u,
 // c128.  Returns false (nothing launched) when a cooperative launch is not
 // available, then the caller runs the separate kernels.
 int arnoldi_step_blocks();
+// With wpart, w is first formed as the sum of nsplit partial products
+// (wpart[t N + i], FP64 in split order), in the same launch.
 bool launch_arnoldi_step(int n, int j, double2 *V, size_t ldv, double2 *w, float2 *vf, double2 *h1, double2 *h2,
                          double2 *H, int ldh, double2 *cs, double2 *sn, double2 *g, double *res, double2 *part,
-                         cudaStream_t st);
+                         cudaStream_t st, const float2 *wpart = nullptr, int nsplit = 0);
 // w = A^H (A v) for c64 A with A read once (cluster kernel, A streamed by
 // TMA bulk copies); v c64, w c128; part: scratch of normal_op_clusters(N) x N
 // c64.  Returns false (nothing launched) when N is above what one cluster
@@ -165,8 +167,12 @@ bool launch_arnoldi_step(int n, int j, double2 *V, size_t ldv, double2 *w, float
 int normal_op_clusters(int N);
 // status: the calling solver's status word (device int), set to 1 when a
 // bounded wait of the kernel times out.
+// With nsplit_out, the clusters' partial products are left in part (nsplit_out
+// of them, stride N) for the caller to sum (launch_normal_op_sum, or the
+// Arnoldi step), and w is not written.
 bool launch_normal_op(int R, int N, const float2 *A, size_t lda, const float2 *v, double2 *w, float2 *part,
-                      int *status, cudaStream_t st);
+                      int *status, cudaStream_t st, int *nsplit_out = nullptr);
+void launch_normal_op_sum(int N, int nsplit, const float2 *part, double2 *w, cudaStream_t st);
 // True (and the word cleared) when a normal-operator launch gave up waiting
 // for one of its copies and recorded it in *status; synchronises the stream.
 bool normal_op_timed_out(int *status, cudaStream_t st);

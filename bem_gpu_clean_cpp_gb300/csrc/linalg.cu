@@ -528,7 +528,8 @@ __global__ void __launch_bounds__(kArNT)
 arnoldi_step_kernel(int n, int j, double2 *__restrict__ V, size_t ldv, double2 *__restrict__ w,
                     float2 *__restrict__ vf, double2 *__restrict__ h1, double2 *__restrict__ h2,
                     double2 *__restrict__ H, int ldh, double2 *__restrict__ cs, double2 *__restrict__ sn,
-                    double2 *__restrict__ g, double *__restrict__ res, double2 *__restrict__ part) {
+                    double2 *__restrict__ g, double *__restrict__ res, double2 *__restrict__ part,
+                    const float2 *__restrict__ wpart, int nsplit) {
     namespace cg = cooperative_groups;
     cg::grid_group grid = cg::this_grid();
     const int nb = gridDim.x, b = blockIdx.x, tid = threadIdx.x;
@@ -609,6 +610,19 @@ arnoldi_step_kernel(int n, int j, double2 *__restrict__ V, size_t ldv, double2 *
         __syncthreads();
     };
     double2 *p1 = part, *p2 = part + (size_t)k * nb, *p3 = part + 2 * (size_t)k * nb;
+    if (wpart) {
+        // w = the sum of the normal operator's nsplit partial products (FP64,
+        // in split order), this CTA's slice, by the threads that read it next
+        for (int i = i0 + tid; i < i1; i += kArNT) {
+            double a = 0.0, c = 0.0;
+            for (int t = 0; t < nsplit; t++) {
+                const float2 v = wpart[(size_t)t * n + i];
+                a += v.x;
+                c += v.y;
+            }
+            w[i] = make_double2(a, c);
+        }
+    }
     partial_dots(p1);
     grid.sync();
     reduce_dots(p1, h1);
@@ -1043,12 +1057,12 @@ int arnoldi_step_blocks() {
 
 bool launch_arnoldi_step(int n, int j, double2 *V, size_t ldv, double2 *w, float2 *vf, double2 *h1, double2 *h2,
                          double2 *H, int ldh, double2 *cs, double2 *sn, double2 *g, double *res, double2 *part,
-                         cudaStream_t st) {
+                         cudaStream_t st, const float2 *wpart, int nsplit) {
     const int nb = arnoldi_step_blocks();
     if (nb <= 0 || j + 1 > kArnoldiMaxK || n < 1) return false;
     BEM_PROF("arnoldi_step", st);
     const size_t smem = (size_t)(j + 1) * sizeof(double2);
-    void *args[] = {&n, &j, &V, &ldv, &w, &vf, &h1, &h2, &H, &ldh, &cs, &sn, &g, &res, &part};
+    void *args[] = {&n, &j, &V, &ldv, &w, &vf, &h1, &h2, &H, &ldh, &cs, &sn, &g, &res, &part, &wpart, &nsplit};
     const cudaError_t e = cudaLaunchCooperativeKernel((const void *)arnoldi_step_kernel, dim3(nb), dim3(kArNT),
                                                       args, smem, st);
     if (e != cudaSuccess) {
@@ -1129,8 +1143,15 @@ bool normal_op_timed_out(int *status, cudaStream_t st) {
     return h != 0;
 }
 
+void launch_normal_op_sum(int N, int nsplit, const float2 *part, double2 *w, cudaStream_t st) {
+    BEM_PROF("normal_op_sum", st);
+    sum_many_splits_kernel<<<blocks(N, 32), 256, 0, st>>>(N, nsplit, part, w);
+    count_launch();
+    KERNEL_CHECK();
+}
+
 bool launch_normal_op(int R, int N, const float2 *A, size_t lda, const float2 *v, double2 *w, float2 *part,
-                      int *status, cudaStream_t st) {
+                      int *status, cudaStream_t st, int *nsplit_out) {
     if (N <= 0 || R <= 0 || (N + kNoW - 1) / kNoW > kNoMaxCluster) return false;
     static std::once_flag once;
     static cudaError_t attr_err = cudaSuccess;
@@ -1188,7 +1209,9 @@ bool launch_normal_op(int R, int N, const float2 *A, size_t lda, const float2 *v
             CUDA_TRY(cudaLaunchKernelEx(&cfg, normal_op_kernel, R, N, A, lda, v, rpc, ngroups, part));
         count_launch();
     }
-    {
+    if (nsplit_out) {
+        *nsplit_out = ncl;   // the caller sums the clusters' partial w
+    } else {
         BEM_PROF("normal_op_sum", st);   // FP64 sum of the clusters' partial w
         sum_many_splits_kernel<<<blocks(N, 32), 256, 0, st>>>(N, ncl, part, w);
         count_launch();

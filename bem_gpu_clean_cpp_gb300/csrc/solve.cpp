@@ -169,15 +169,23 @@ void bem_solver_s::solve_refined(bem_solve_info_t *info) {
             // then the residual estimate to h_pinned[4 + (j & 1)], signalled by
             // ev_res[j & 1].
             auto launch_step = [&](int j) {
-                if (!launch_normal_op(R, n, A, lda, w_vf.as<float2>(), w_w.as<double2>(), w_part.as<float2>(),
-                                      op_status, stream)) {
+                // the normal operator's cluster partials are summed by the
+                // Arnoldi step itself (one launch less per iteration)
+                int nsplit = 0;
+                const bool fused = launch_normal_op(R, n, A, lda, w_vf.as<float2>(), w_w.as<double2>(),
+                                                    w_part.as<float2>(), op_status, stream, &nsplit);
+                if (!fused) {
                     launch_gemv_c64(R, n, A, lda, w_vf.p, 0, w_t.p, 0, stream);              // t = A v_j
                     launch_gemv_h_c64(R, n, A, lda, w_t.p, 0, w_w.p, 1, w_part.p, stream);  // w = A^H t
                 }
-                if (!launch_arnoldi_step(n, j, V, n, w_w.as<double2>(), w_vf.as<float2>(), w_h1.as<double2>(),
-                                         w_h2.as<double2>(), w_H.as<double2>(), ldh, w_cs.as<double2>(),
-                                         w_sn.as<double2>(), w_g.as<double2>(), scal + 3, w_ap.as<double2>(),
-                                         stream)) {
+                const float2 *wpart = fused ? w_part.as<float2>() : nullptr;
+                const bool stepped = launch_arnoldi_step(n, j, V, n, w_w.as<double2>(), w_vf.as<float2>(),
+                                                         w_h1.as<double2>(), w_h2.as<double2>(), w_H.as<double2>(),
+                                                         ldh, w_cs.as<double2>(), w_sn.as<double2>(),
+                                                         w_g.as<double2>(), scal + 3, w_ap.as<double2>(), stream,
+                                                         wpart, nsplit);
+                if (!stepped && fused) launch_normal_op_sum(n, nsplit, w_part.as<float2>(), w_w.as<double2>(), stream);
+                if (!stepped) {
                     launch_dots(n, j + 1, V, n, w_w.as<double2>(), w_h1.as<double2>(), nullptr, stream);
                     launch_update(n, j + 1, V, n, w_h1.as<double2>(), w_w.as<double2>(), stream);
                     launch_dots(n, j + 1, V, n, w_w.as<double2>(), w_h2.as<double2>(), nullptr, stream);
