@@ -1103,13 +1103,15 @@ int clusters_resident(const void *kern, int C, int nt, size_t smem, int want) {
 
 // Which normal-operator kernel runs (environment variable
 // BEM_NORMAL_OP_KERNEL): 0 = "regs" (A loaded into registers), 512 = "tma"
-// (TMA-streamed, 512 threads, one CTA per SM; the default), 256 = "tma256"
-// (256 threads, two CTAs per SM).
+// (TMA-streamed, 512 threads, one CTA per SM), 256 = "tma256" (256 threads,
+// two CTAs per SM; the default: 0.136 against 0.141 ms at 10274 x 10242 with
+// the st.async row-sum exchange; the launcher takes 512 where the 256-thread
+// clusters would exceed the cluster size limit).
 int normal_op_variant() {
     static const int var = [] {
         const char *e = std::getenv("BEM_NORMAL_OP_KERNEL");
         const std::string v = e ? e : "";
-        return v == "regs" ? 0 : v == "tma256" ? 256 : 512;
+        return v == "regs" ? 0 : v == "tma" ? 512 : 256;
     }();
     return var;
 }

@@ -182,11 +182,15 @@ bem_solver_s::~bem_solver_s() {
 void bem_solver_s::set_geometry(const double *pnts, int num_pnts, const int *elems, int num_elems,
                                 const double *bc, const double *chief, int num_chief) {
     BEM_HOST_PROF("set_geometry");
-    if (tile_future.valid()) tile_future.wait();   // it reads h_nodes and h_elems
+    if (tile_future.valid()) tile_future.wait();   // they read h_nodes and h_elems
+    if (grid_future.valid()) grid_future.wait();
     BEM_CHECK_ARG(pnts && elems && num_pnts > 0 && num_elems > 0, "empty geometry");
     BEM_CHECK_ARG(num_chief >= 0 && (num_chief == 0 || chief), "bad CHIEF points");
     for (long long i = 0; i < 3LL * num_elems; i++)
         BEM_CHECK_ARG(elems[i] >= 0 && elems[i] < num_pnts, "element node index out of range");
+    if (bc)   // checked before any state changes (the default BC has cb = 1)
+        for (int e = 0; e < num_elems; e++)
+            BEM_CHECK_ARG(bc[6 * (size_t)e + 2] != 0.0 || bc[6 * (size_t)e + 3] != 0.0, "element with cb = 0");
     N = num_pnts;
     E = num_elems;
     M = num_chief;
@@ -215,17 +219,13 @@ void bem_solver_s::set_geometry(const double *pnts, int num_pnts, const int *ele
         }
     }
     max_edge = std::sqrt(max_edge2);
-    h_bc.resize(6 * (size_t)E);
-    if (bc) {
-        std::memcpy(h_bc.data(), bc, sizeof(double) * 6 * (size_t)E);
-    } else {
+    if (!bc) {   // the default BC (0, 1, -1) per element, uploaded from here
+        h_bc.resize(6 * (size_t)E);
         for (int e = 0; e < E; e++) {
             double d[6] = {0, 0, 1, 0, -1, 0};
             std::memcpy(&h_bc[6 * (size_t)e], d, sizeof(d));
         }
     }
-    for (int e = 0; e < E; e++)
-        BEM_CHECK_ARG(h_bc[6 * (size_t)e + 2] != 0.0 || h_bc[6 * (size_t)e + 3] != 0.0, "element with cb = 0");
     h_rows.assign(h_nodes.begin(), h_nodes.end());
     if (M) h_rows.insert(h_rows.end(), chief, chief + 3 * (size_t)M);
     {
@@ -242,6 +242,11 @@ void bem_solver_s::set_geometry(const double *pnts, int num_pnts, const int *ele
         extent = std::sqrt((hi[0] - lo[0]) * (hi[0] - lo[0]) + (hi[1] - lo[1]) * (hi[1] - lo[1]) +
                            (hi[2] - lo[2]) * (hi[2] - lo[2]));
     }
+    // the near-pair grid's host part on another host thread (ensure_near_list
+    // takes it when near_eta is still the one it was built for)
+    grid_future = std::async(std::launch::async, [this, eta = opt.near_eta] {
+        return build_near_grid(E, h_nodes, h_elems, row_lo, row_hi, max_edge, eta);
+    });
 
     // The float head/tail rows and the int4 element table are built in a
     // pinned staging buffer; nodes, CHIEF points and BCs go up straight from
@@ -320,32 +325,17 @@ void bem_solver_s::ensure_near_list() {
     ensure_geo();
     if (near_valid) return;
     BEM_HOST_PROF("near_list");
-    // Grid of element centroids: cell edge >= the largest near radius
-    // (near_eta x element diameter) and >= the longest element (vertex pairs),
-    // over the box of all row points and nodes; at most ~4M cells.
-    const double *lo = row_lo, *hi = row_hi;   // formed by set_geometry
-    double cell = std::max(1.0, opt.near_eta) * max_edge * 1.01 + 1e-12;
-    const double span = std::max({hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2], 1e-12});
-    cell = std::max(cell, span / 160.0);
-    int dim[3];
-    for (int a = 0; a < 3; a++) dim[a] = std::max(1, (int)std::floor((hi[a] - lo[a]) / cell) + 1);
-    const size_t ncell = (size_t)dim[0] * dim[1] * dim[2];
-    std::vector<int> cid(E), start(ncell + 1, 0), order(E);
-    for (int e = 0; e < E; e++) {
-        int c[3];
-        for (int a = 0; a < 3; a++) {
-            const double m = (h_nodes[3 * (size_t)h_elems[3 * e] + a] + h_nodes[3 * (size_t)h_elems[3 * e + 1] + a] +
-                              h_nodes[3 * (size_t)h_elems[3 * e + 2] + a]) / 3.0;
-            c[a] = std::min(std::max((int)std::floor((m - lo[a]) / cell), 0), dim[a] - 1);
-        }
-        cid[e] = (int)(((size_t)c[2] * dim[1] + c[1]) * dim[0] + c[0]);
-        start[cid[e] + 1]++;
-    }
-    for (size_t c = 0; c < ncell; c++) start[c + 1] += start[c];
-    {
-        std::vector<int> fill(start.begin(), start.end() - 1);
-        for (int e = 0; e < E; e++) order[fill[cid[e]]++] = e;   // increasing e within a cell
-    }
+    // (the host arrays of the uploads below stay members until the next
+    // geometry, whose set_geometry ends with a stream synchronisation)
+    NearGridHost &gh = near_grid_h;
+    gh = NearGridHost{};
+    if (grid_future.valid()) gh = grid_future.get();
+    if (gh.eta != opt.near_eta || gh.start.empty())
+        gh = build_near_grid(E, h_nodes, h_elems, row_lo, row_hi, max_edge, opt.near_eta);
+    const double *lo = gh.lo, cell = gh.cell;
+    const int *dim = gh.dim;
+    const size_t ncell = gh.start.size() - 1;
+    const std::vector<int> &start = gh.start, &order = gh.order;
     d_grid_start.ensure(sizeof(int) * (ncell + 1));
     d_grid_elems.ensure(sizeof(int) * std::max(1, E));
     CUDA_TRY(cudaMemcpyAsync(d_grid_start.p, start.data(), sizeof(int) * (ncell + 1), cudaMemcpyHostToDevice, stream));
@@ -357,7 +347,8 @@ void bem_solver_s::ensure_near_list() {
     std::vector<int> cnt(R);
     CUDA_TRY(cudaMemcpyAsync(cnt.data(), d_near_ptr.p, sizeof(int) * R, cudaMemcpyDeviceToHost, stream));
     CUDA_TRY(cudaStreamSynchronize(stream));
-    std::vector<int> ptr(R + 1, 0);
+    std::vector<int> &ptr = near_ptr_h;
+    ptr.assign(R + 1, 0);
     for (int r = 0; r < R; r++) {
         if (ptr[r] > 0x7fffffff - cnt[r]) BEM_FAIL(BEM_ERR_TOO_LARGE, "too many near pairs");
         ptr[r + 1] = ptr[r] + cnt[r];
@@ -366,7 +357,6 @@ void bem_solver_s::ensure_near_list() {
     d_near_ids.ensure(sizeof(int) * std::max(1, ptr[R]));
     launch_near_list(row_points(), N, geo_tables(), grid, d_near_ptr.as<int>(), nullptr, d_near_ids.as<int>(),
                      stream);
-    CUDA_TRY(cudaStreamSynchronize(stream));   // host arrays must outlive the copies
     near_valid = true;
 }
 
@@ -376,6 +366,41 @@ void bem_solver_s::ensure_near_list() {
 // cut into equal tiles, and each tile lists every element with a node in it;
 // an element straddling tiles is integrated once per tile it touches and
 // counted for the c and beta sums only in the tile of its first node.
+// Grid of element centroids: cell edge >= the largest near radius (near_eta
+// x element diameter) and >= the longest element (vertex pairs), over the box
+// of all row points; at most ~4M cells.
+bem::NearGridHost bem::build_near_grid(int E, const std::vector<double> &h_nodes, const std::vector<int> &h_elems,
+                                       const double *lo, const double *hi, double max_edge, double eta) {
+    NearGridHost g;
+    g.eta = eta;
+    double cell = std::max(1.0, eta) * max_edge * 1.01 + 1e-12;
+    const double span = std::max({hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2], 1e-12});
+    cell = std::max(cell, span / 160.0);
+    g.cell = cell;
+    for (int a = 0; a < 3; a++) {
+        g.lo[a] = lo[a];
+        g.dim[a] = std::max(1, (int)std::floor((hi[a] - lo[a]) / cell) + 1);
+    }
+    const size_t ncell = (size_t)g.dim[0] * g.dim[1] * g.dim[2];
+    std::vector<int> cid(E);
+    g.start.assign(ncell + 1, 0);
+    g.order.resize(E);
+    for (int e = 0; e < E; e++) {
+        int c[3];
+        for (int a = 0; a < 3; a++) {
+            const double m = (h_nodes[3 * (size_t)h_elems[3 * e] + a] + h_nodes[3 * (size_t)h_elems[3 * e + 1] + a] +
+                              h_nodes[3 * (size_t)h_elems[3 * e + 2] + a]) / 3.0;
+            c[a] = std::min(std::max((int)std::floor((m - lo[a]) / cell), 0), g.dim[a] - 1);
+        }
+        cid[e] = (int)(((size_t)c[2] * g.dim[1] + c[1]) * g.dim[0] + c[0]);
+        g.start[cid[e] + 1]++;
+    }
+    for (size_t c = 0; c < ncell; c++) g.start[c + 1] += g.start[c];
+    std::vector<int> fill(g.start.begin(), g.start.end() - 1);
+    for (int e = 0; e < E; e++) g.order[fill[cid[e]]++] = e;   // increasing e within a cell
+    return g;
+}
+
 bem::HostTiles bem::build_host_tiles(int N, int E, const std::vector<double> &h_nodes,
                                      const std::vector<int> &h_elems, int cap) {
     HostTiles out;

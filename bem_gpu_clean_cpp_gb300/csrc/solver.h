@@ -48,6 +48,16 @@ struct HostTiles {
     std::vector<int> ptr, cols, cnt;
     std::vector<int> bptr, tbatch;   // node-disjoint batches of records (TileSet::batch_ptr, tile_batch)
 };
+// The near-pair search grid's host part: element centroids binned into cells
+// of edge >= max(1, eta) x the longest edge x 1.01 (and >= the box's span /
+// 160) over the row points' box, elements in increasing order within a cell.
+struct NearGridHost {
+    double eta = -1.0, cell = 0.0, lo[3] = {0.0, 0.0, 0.0};
+    int dim[3] = {0, 0, 0};
+    std::vector<int> start, order;   // ncell + 1 cell offsets, E element ids
+};
+NearGridHost build_near_grid(int E, const std::vector<double> &h_nodes, const std::vector<int> &h_elems,
+                             const double *lo, const double *hi, double max_edge, double eta);
 HostTiles build_host_tiles(int N, int E, const std::vector<double> &h_nodes, const std::vector<int> &h_elems,
                            int cap);
 // Block-solve GEMM mode chosen by timing for (device, R, N, S), shared by
@@ -135,6 +145,11 @@ struct bem_solver_s {
     // (whose destructor waits for its task) goes first
     bem::HostTiles host_tiles;
     std::future<bem::HostTiles> tile_future;
+    // the near-pair grid's host part, built beside set_geometry too; the last
+    // one used and the row offsets stay here while their uploads are in flight
+    std::future<bem::NearGridHost> grid_future;
+    bem::NearGridHost near_grid_h;
+    std::vector<int> near_ptr_h;
 
     bem_solver_s();
     ~bem_solver_s();

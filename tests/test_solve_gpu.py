@@ -229,12 +229,13 @@ print("RESULT", int(info.converged), err)
 """
 
 
-@pytest.mark.parametrize("variant", ["regs", "tma256"])
+@pytest.mark.parametrize("variant", ["regs", "tma"])
 def test_normal_op_variants(bemlib, variant):
     """The other two normal-operator kernels, chosen per process by
-    BEM_NORMAL_OP_KERNEL (register-loading, and the 256-thread TMA kernel
-    with two CTAs per SM and four-CTA clusters at 10892 nodes), give a
-    refined solve within 1e-5 of the FP64 solve, like the default one."""
+    BEM_NORMAL_OP_KERNEL (register-loading, and the 512-thread TMA kernel
+    with one CTA per SM and two-CTA clusters at 10892 nodes), give a
+    refined solve within 1e-5 of the FP64 solve, like the default 256-thread
+    one (two CTAs per SM, four-CTA clusters)."""
     import os
     import subprocess
     import sys
