@@ -611,17 +611,32 @@ arnoldi_step_kernel(int n, int j, double2 *__restrict__ V, size_t ldv, double2 *
     };
     double2 *p1 = part, *p2 = part + (size_t)k * nb, *p3 = part + 2 * (size_t)k * nb;
     if (wpart) {
-        // w = the sum of the normal operator's nsplit partial products (FP64,
-        // in split order), this CTA's slice, by the threads that read it next
-        for (int i = i0 + tid; i < i1; i += kArNT) {
+        // w = the sum of the normal operator's nsplit partial products (FP64),
+        // this CTA's slice: four consecutive threads per entry, each adding a
+        // quarter of the partials in order, then the quarters in order (a fixed
+        // order; the loads of an entry are spread over four threads)
+        constexpr int kQ = 4;
+        const int q = tid % kQ, per_q = (nsplit + kQ - 1) / kQ;
+        const int t0 = min(nsplit, q * per_q), t1 = min(nsplit, t0 + per_q);
+        for (int base = i0; base < i1; base += kArNT / kQ) {
+            const int i = base + tid / kQ;
             double a = 0.0, c = 0.0;
-            for (int t = 0; t < nsplit; t++) {
-                const float2 v = wpart[(size_t)t * n + i];
-                a += v.x;
-                c += v.y;
+            if (i < i1) {
+#pragma unroll 4
+                for (int t = t0; t < t1; t++) {
+                    const float2 v = wpart[(size_t)t * n + i];
+                    a += v.x;
+                    c += v.y;
+                }
             }
-            w[i] = make_double2(a, c);
+#pragma unroll
+            for (int o = 1; o < kQ; o <<= 1) {   // quarters 0+1, 2+3, then (0+1)+(2+3)
+                a += __shfl_xor_sync(0xffffffffu, a, o);
+                c += __shfl_xor_sync(0xffffffffu, c, o);
+            }
+            if (q == 0 && i < i1) w[i] = make_double2(a, c);
         }
+        __syncthreads();   // partial_dots reads w with another thread-to-entry map
     }
     partial_dots(p1);
     grid.sync();
