@@ -523,8 +523,15 @@ __device__ __forceinline__ uint64_t add2(uint64_t a, uint64_t b) {
 // the other), so S1 += b U1_n + c U1_{5-n} and S2 += c U1_n + b U1_{5-n}.
 // The dG/dn imaginary sums collect -hb (fma(-k, c, gs) = -fma(k, c, -gs)
 // exactly) and take the sign with the height at the end.
-template <int PH>
-__device__ __forceinline__ void far_sums_f32_o6x2(float3 d3, float3 e1, float3 e2, float hgt, float k,
+// The phase shift's second constant is folded into r: y = k (r + c2 / k) + c1
+// with r + c2 / k formed by one FMA from r^2 and 1/r (one operation less per
+// point than k r + c1 + c2; r + c2 / k is rounded once, as r was).
+// GM (which sums of G the BCs need): 2 = all (some element has bcA != 0, so
+// G enters A); 1 = S0 only (bcA = 0 everywhere, e.g. the BC (0, 1, gamma):
+// beta needs sum_j g_j = S0); 0 = none (bcA = bcC = 0 everywhere, the rigid
+// BC (0, 1, 0)).  The sums not formed are left zero.
+template <int PH, int GM>
+__device__ __forceinline__ void far_sums_f32_o6x2(float3 d3, float3 e1, float3 e2, float hgt, float k, float kinv,
                                                   const PairPhase &pp, SumsF &S) {
     static_assert(PH != kPhaseAcc, "the accurate phase mode has its own per-point arithmetic");
     S.g0r = S.g0i = S.g1r = S.g1i = S.g2r = S.g2i = 0.0f;
@@ -545,7 +552,8 @@ __device__ __forceinline__ void far_sums_f32_o6x2(float3 d3, float3 e1, float3 e
     const float b1 = 2.0f * fmaf(e21.z, d3.z, fmaf(e21.y, d3.y, e21.x * d3.x));
     const float dd = fmaf(d3.z, d3.z, fmaf(d3.y, d3.y, d3.x * d3.x));
     const uint64_t dd2 = f2(dd, dd), k2 = f2(k, k), nk2 = f2(-k, -k);
-    const uint64_t c1 = f2(pp.c1, pp.c1), c2 = f2(pp.c2, pp.c2);
+    const float dr = pp.c2 * kinv;
+    const uint64_t c1 = f2(pp.c1, pp.c1), dr2 = f2(dr, dr);
 #pragma unroll
     for (int n = 0; n < 3; n++) {
         const float th = 0.5f + 0.5f * gl6_x(n), tm = 0.5f + 0.5f * gl6_x(5 - n);   // tm = 1 - th
@@ -562,8 +570,8 @@ __device__ __forceinline__ void far_sums_f32_o6x2(float3 d3, float3 e1, float3 e
             float ra, rb;
             f2_split(r2, ra, rb);
             const uint64_t ri = f2(rsqrt_ftz(ra), rsqrt_ftz(rb));
-            const uint64_t r = mul2(r2, ri);
-            uint64_t y = add2(fma2(k2, r, c1), c2);
+            const uint64_t r = fma2(r2, ri, dr2);   // r + c2 / k
+            uint64_t y = fma2(k2, r, c1);
             if (PH == kPhaseWrap) {
                 // wrap_phase on both lanes
                 const uint64_t kr = f2(12582912.0f, 12582912.0f);
@@ -580,8 +588,14 @@ __device__ __forceinline__ void far_sums_f32_o6x2(float3 d3, float3 e1, float3 e
             const uint64_t ha = mul2(ri2, fma2(k2, sn, gr));
             const uint64_t hbn = mul2(ri2, fma2(nk2, cs, gs));
             const uint64_t ri3 = mul2(ri2, ri);
-            u0gr = fma2(wr1, gr, u0gr); u1gr = fma2(wr2, gr, u1gr);
-            u0gs = fma2(wr1, gs, u0gs); u1gs = fma2(wr2, gs, u1gs);
+            if constexpr (GM >= 1) {
+                u0gr = fma2(wr1, gr, u0gr);
+                u0gs = fma2(wr1, gs, u0gs);
+            }
+            if constexpr (GM == 2) {
+                u1gr = fma2(wr2, gr, u1gr);
+                u1gs = fma2(wr2, gs, u1gs);
+            }
             u0ha = fma2(wr1, ha, u0ha); u1ha = fma2(wr2, ha, u1ha);
             u0hb = fma2(wr1, hbn, u0hb); u1hb = fma2(wr2, hbn, u1hb);
             u0c = fma2(wr1, ri3, u0c);
@@ -590,10 +604,14 @@ __device__ __forceinline__ void far_sums_f32_o6x2(float3 d3, float3 e1, float3 e
         // 5 - n (a, c, b)
         const float a = 0.25f * gl6_w(n), b = a * (1.0f - th), c = a * th;
         float p0, p1;
-        f2_split(u0gr, p0, p1); S.g0r = fmaf(a, p0 + p1, S.g0r);
-        f2_split(u1gr, p0, p1); S.g1r = fmaf(b, p0, fmaf(c, p1, S.g1r)); S.g2r = fmaf(c, p0, fmaf(b, p1, S.g2r));
-        f2_split(u0gs, p0, p1); S.g0i = fmaf(a, p0 + p1, S.g0i);
-        f2_split(u1gs, p0, p1); S.g1i = fmaf(b, p0, fmaf(c, p1, S.g1i)); S.g2i = fmaf(c, p0, fmaf(b, p1, S.g2i));
+        if constexpr (GM >= 1) {
+            f2_split(u0gr, p0, p1); S.g0r = fmaf(a, p0 + p1, S.g0r);
+            f2_split(u0gs, p0, p1); S.g0i = fmaf(a, p0 + p1, S.g0i);
+        }
+        if constexpr (GM == 2) {
+            f2_split(u1gr, p0, p1); S.g1r = fmaf(b, p0, fmaf(c, p1, S.g1r)); S.g2r = fmaf(c, p0, fmaf(b, p1, S.g2r));
+            f2_split(u1gs, p0, p1); S.g1i = fmaf(b, p0, fmaf(c, p1, S.g1i)); S.g2i = fmaf(c, p0, fmaf(b, p1, S.g2i));
+        }
         f2_split(u0ha, p0, p1); S.h0r = fmaf(a, p0 + p1, S.h0r);
         f2_split(u1ha, p0, p1); S.h1r = fmaf(b, p0, fmaf(c, p1, S.h1r)); S.h2r = fmaf(c, p0, fmaf(b, p1, S.h2r));
         f2_split(u0hb, p0, p1); S.h0i = fmaf(a, p0 + p1, S.h0i);
@@ -656,9 +674,28 @@ struct Coeffs {
     T c;
 };
 
-template <typename T, typename SUMS>
+// GM < 2 (bcA = 0 for the element): a_j = h_j, and beta takes
+// sum_j g_j = i rw scale G0 from the S0 sums alone (GM = 0: bcC = 0 too,
+// beta = 0).
+template <typename T, typename SUMS, int GM = 2>
 __device__ __forceinline__ void finish_coeffs(const SUMS &S, T scale, T rw, T bAr, T bAi, T bCr,
                                               T bCi, Coeffs<T, SUMS> &o) {
+    if constexpr (GM < 2) {
+#pragma unroll
+        for (int j = 0; j < 3; j++) {
+            o.ar[j] = scale * (j == 0 ? S.h1r : j == 1 ? S.h2r : S.h0r - S.h1r - S.h2r);
+            o.ai[j] = scale * (j == 0 ? S.h1i : j == 1 ? S.h2i : S.h0i - S.h1i - S.h2i);
+        }
+        if constexpr (GM == 1) {
+            const T sgr = -rw * scale * S.g0i, sgi = rw * scale * S.g0r;
+            o.br = bCr * sgr - bCi * sgi;
+            o.bi = bCr * sgi + bCi * sgr;
+        } else {
+            o.br = o.bi = T(0);
+        }
+        o.c = scale * S.c;
+        return;
+    }
     T gr[3] = {S.g1r, S.g2r, S.g0r - S.g1r - S.g2r};
     T gi[3] = {S.g1i, S.g2i, S.g0i - S.g1i - S.g2i};
     T hr[3] = {S.h1r, S.h2r, S.h0r - S.h1r - S.h2r};
@@ -683,11 +720,14 @@ __device__ __forceinline__ void finish_coeffs(const SUMS &S, T scale, T rw, T bA
 // Far-field assembly kernel.
 // grid = (ceil(R/TR), ntiles), block = NT threads, dynamic smem = acc[TR][tc].
 // ---------------------------------------------------------------------------
-template <int TR, int NT, int MINB, bool O6, int PH>
+// GM < 2: the G sums that no BC needs are not formed (far_sums_f32_o6x2);
+// only the O6 shift/wrap path is instantiated that way.
+template <int TR, int NT, int MINB, bool O6, int PH, int GM>
 __global__ void __launch_bounds__(NT, MINB)
 far_assembly_f32(RowPoints rows, int N, GeoTables geo, TileSet tiles, float k, float k_lo, float rw,
                  float2 *__restrict__ A, size_t lda, float *__restrict__ c_part,
                  float2 *__restrict__ beta_part) {
+    static_assert(GM == 2 || (O6 && PH != kPhaseAcc), "the reduced G sums exist for the order-6 shift/wrap path");
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float2 *acc = reinterpret_cast<float2 *>(smem_raw);
     __shared__ float red[NT / 32][3];
@@ -711,6 +751,7 @@ far_assembly_f32(RowPoints rows, int N, GeoTables geo, TileSet tiles, float k, f
 
     const int nq = c_nq;
     const float inv4pi = (float)(1.0 / (4.0 * kPi));
+    const float kinv = 1.0f / k;
     const int b0 = tiles.tile_batch[tile], b1 = tiles.tile_batch[tile + 1];
     const int nr = min(TR, R - r0);                       // rows of this CTA
     // Records come in node-disjoint batches.  Per batch the CTA's threads
@@ -757,11 +798,11 @@ far_assembly_f32(RowPoints rows, int N, GeoTables geo, TileSet tiles, float k, f
                                      ? pair_phase_acc(k, k_lo, make_float3(g0.x, g0.y, g0.z),
                                                       make_float3(g1.x, g1.y, g1.z), xh, xl, d3, coff)
                                      : pair_phase_shift(k, d3, coff);
-            if constexpr (O6 && PH != kPhaseAcc) far_sums_f32_o6x2<PH>(d3, e1, e2, hgt, k, pp, S);
+            if constexpr (O6 && PH != kPhaseAcc) far_sums_f32_o6x2<PH, GM>(d3, e1, e2, hgt, k, kinv, pp, S);
             else if (O6) far_sums_f32_o6<PH>(d3, e1, e2, coff, hgt, k, pp, S);
             else far_sums_f32<PH>(d3, e1, e2, coff, hgt, k, pp, nq, S);
             Coeffs<float, SumsF> o;
-            finish_coeffs<float, SumsF>(S, g0.w * inv4pi, rw, g5.x, g5.y, g5.z, g5.w, o);
+            finish_coeffs<float, SumsF, GM>(S, g0.w * inv4pi, rw, g5.x, g5.y, g5.z, g5.w, o);
             if (!waited) {
                 wait_batch(b - b0 - 1);
                 waited = true;
@@ -777,8 +818,10 @@ far_assembly_f32(RowPoints rows, int N, GeoTables geo, TileSet tiles, float k, f
             }
             if (nd.w) {   // this tile counts the element's c and beta terms
                 cb[(0 * TR + t) * NT + threadIdx.x] += o.c;
-                cb[(1 * TR + t) * NT + threadIdx.x] += o.br;
-                cb[(2 * TR + t) * NT + threadIdx.x] += o.bi;
+                if constexpr (GM > 0) {
+                    cb[(1 * TR + t) * NT + threadIdx.x] += o.br;
+                    cb[(2 * TR + t) * NT + threadIdx.x] += o.bi;
+                }
             }
         }
         if (!waited) wait_batch(b - b0 - 1);   // arrivals for batch i only after batch i - 1 completed
@@ -954,20 +997,27 @@ static void launch_far_f32(const RowPoints &rows, int N, const GeoTables &geo, c
                            size_t smem, cudaStream_t st) {
     const bool o6 = quadrature_points() == 36;
     const int mode = far_phase_mode(ph);
-    decltype(&far_assembly_f32<TR, NT, MINB, true, kPhaseShift>) kern;
-    if (!o6) {   // other Gauss orders: always the accurate phase (not the tuned path)
-        kern = far_assembly_f32<TR, NT, MINB, false, kPhaseAcc>;
-        allow_max_smem<far_assembly_f32<TR, NT, MINB, false, kPhaseAcc>>();
-    } else if (mode == kPhaseAcc) {
-        kern = far_assembly_f32<TR, NT, MINB, true, kPhaseAcc>;
-        allow_max_smem<far_assembly_f32<TR, NT, MINB, true, kPhaseAcc>>();
-    } else if (mode == kPhaseWrap) {
-        kern = far_assembly_f32<TR, NT, MINB, true, kPhaseWrap>;
-        allow_max_smem<far_assembly_f32<TR, NT, MINB, true, kPhaseWrap>>();
+    decltype(&far_assembly_f32<TR, NT, MINB, true, kPhaseShift, 2>) kern;
+#define BEM_FAR_PICK(O6_, PH_, GM_)                                   \
+    do {                                                              \
+        kern = far_assembly_f32<TR, NT, MINB, O6_, PH_, GM_>;          \
+        allow_max_smem<far_assembly_f32<TR, NT, MINB, O6_, PH_, GM_>>(); \
+    } while (0)
+    const int gm = ph.g_sums;
+    if (!o6)   // other Gauss orders: always the accurate phase (not the tuned path)
+        BEM_FAR_PICK(false, kPhaseAcc, 2);
+    else if (mode == kPhaseAcc)
+        BEM_FAR_PICK(true, kPhaseAcc, 2);
+    else if (mode == kPhaseWrap) {
+        if (gm == 2) BEM_FAR_PICK(true, kPhaseWrap, 2);
+        else if (gm == 1) BEM_FAR_PICK(true, kPhaseWrap, 1);
+        else BEM_FAR_PICK(true, kPhaseWrap, 0);
     } else {
-        kern = far_assembly_f32<TR, NT, MINB, true, kPhaseShift>;
-        allow_max_smem<far_assembly_f32<TR, NT, MINB, true, kPhaseShift>>();
+        if (gm == 2) BEM_FAR_PICK(true, kPhaseShift, 2);
+        else if (gm == 1) BEM_FAR_PICK(true, kPhaseShift, 1);
+        else BEM_FAR_PICK(true, kPhaseShift, 0);
     }
+#undef BEM_FAR_PICK
     const float kh = (float)ph.k, kl = (float)(ph.k - (double)kh);
     dim3 grid((rows.R + TR - 1) / TR, tiles.ntiles);
     kern<<<grid, NT, smem, st>>>(rows, N, geo, tiles, kh, kl, (float)ph.rw, (float2 *)A, lda,

@@ -67,6 +67,10 @@ struct Physics {
     double near_eta;
     double max_edge = 0.0;    // longest element edge } select the phase mode of the
     double extent = 0.0;      // diagonal of the rows' and nodes' box } FP32 quadrature
+    // which single-layer (G) sums the BCs need: 2 = all (some element has
+    // bcA != 0), 1 = S0 only (bcA = 0 everywhere; beta needs sum_j g_j),
+    // 0 = none (bcA = bcC = 0 everywhere)
+    int g_sums = 2;
 };
 // Phase mode of the FP32 far kernel for this problem (kernels.cu).
 int far_phase_mode(const Physics &ph);

@@ -226,6 +226,17 @@ void bem_solver_s::set_geometry(const double *pnts, int num_pnts, const int *ele
             std::memcpy(&h_bc[6 * (size_t)e], d, sizeof(d));
         }
     }
+    // alpha = 0 on every element (bcA = 0: the far kernel forms no G sums
+    // for A), and gamma = 0 too (bcC = 0: none for beta either)
+    {
+        bool a_nz = false, c_nz = !bc;   // the default BC: alpha = 0, gamma = -1
+        for (int e = 0; bc && e < E && !a_nz; e++) {
+            const double *b = bc + 6 * (size_t)e;
+            a_nz = b[0] != 0.0 || b[1] != 0.0;
+            c_nz = c_nz || b[4] != 0.0 || b[5] != 0.0;
+        }
+        g_sums = a_nz ? 2 : c_nz ? 1 : 0;
+    }
     h_rows.assign(h_nodes.begin(), h_nodes.end());
     if (M) h_rows.insert(h_rows.end(), chief, chief + 3 * (size_t)M);
     {
@@ -517,7 +528,7 @@ GeoTables bem_solver_s::geo_tables() const {
 RowPoints bem_solver_s::row_points() const { return RowPoints{d_rows_f.as<float4>(), d_rows_d.as<double>(), R}; }
 
 Physics bem_solver_s::physics() const {
-    return Physics{k, opt.density * k * opt.speed, opt.near_depth, opt.near_eta, max_edge, extent};
+    return Physics{k, opt.density * k * opt.speed, opt.near_depth, opt.near_eta, max_edge, extent, g_sums};
 }
 
 void bem_solver_s::assemble(double kk, int precision) {

@@ -87,6 +87,7 @@ struct bem_solver_s {
     double max_edge = 0.0;   // longest element edge
     double extent = 0.0;     // diagonal of the box around nodes and CHIEF points
     double row_lo[3] = {0.0, 0.0, 0.0}, row_hi[3] = {0.0, 0.0, 0.0};   // that box
+    int g_sums = 2;   // Physics::g_sums of the BCs: 2 some alpha != 0, 1 alpha = 0 everywhere, 0 gamma = 0 too
 
     struct Tiles {
         bool valid = false;

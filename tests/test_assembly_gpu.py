@@ -34,18 +34,23 @@ def _problem(kind):
 SRCS = [("plane", (0.0, 0.6, 0.8), 1.0), ("point", (3.0, -1.0, 0.5), 2.0 - 1.0j)]
 
 
+def _bc(bckind, E):
+    """default: None, the BC (0, 1, -1) (alpha = 0, gamma != 0: the FP32 far
+    kernel forms the S0 sums of G only); rigid: (0, 1, 0) (no G sums at
+    all); impedance: random alpha, beta, gamma per element (all G sums)."""
+    if bckind == "default":
+        return None
+    if bckind == "rigid":
+        return np.tile(np.array([0, 1, 0], dtype=np.complex128), (E, 1))
+    rng = np.random.default_rng(7)
+    return np.stack([0.3 + 0.1j * rng.random(E), 1.0 + 0.2j * rng.random(E), -1.0 + 0.5j * rng.random(E)], axis=1)
+
+
 @pytest.mark.parametrize("kind", ["test.obj", "cube.obj", "ico2"])
 @pytest.mark.parametrize("bckind", ["default", "rigid", "impedance"])
 def test_c128_assembly_matches_oracle(bemlib, orc, kind, bckind):
     p, f, chief = _problem(kind)
-    E = f.shape[0]
-    if bckind == "default":
-        bc = None
-    elif bckind == "rigid":
-        bc = np.tile(np.array([0, 1, 0], dtype=np.complex128), (E, 1))
-    else:
-        rng = np.random.default_rng(7)
-        bc = np.stack([0.3 + 0.1j * rng.random(E), 1.0 + 0.2j * rng.random(E), -1.0 + 0.5j * rng.random(E)], axis=1)
+    bc = _bc(bckind, f.shape[0])
     k = 2.3
     s = bemlib.Solver()
     s.set_geometry(p, f, bc=bc, chief=chief)
@@ -58,15 +63,17 @@ def test_c128_assembly_matches_oracle(bemlib, orc, kind, bckind):
 
 
 @pytest.mark.parametrize("kind", ["test.obj", "ico2"])
-def test_c64_assembly_matches_oracle(bemlib, orc, kind):
+@pytest.mark.parametrize("bckind", ["default", "rigid", "impedance"])
+def test_c64_assembly_matches_oracle(bemlib, orc, kind, bckind):
     p, f, chief = _problem(kind)
+    bc = _bc(bckind, f.shape[0])
     k = 4.0
     s = bemlib.Solver()
-    s.set_geometry(p, f, chief=chief)
+    s.set_geometry(p, f, bc=bc, chief=chief)
     s.set_sources(SRCS)
     s.assemble(k, bemlib.PREC_C64)
     A, B = s.system(bemlib.PREC_C128)
-    Ao, Bo = orc.assemble(np.vstack([p, chief]), f, k, p.shape[0], SRCS)
+    Ao, Bo = orc.assemble(np.vstack([p, chief]), f, k, p.shape[0], SRCS, bc=bc)
     assert rel_err(A, Ao) < TOL32
     assert rel_err(B, Bo) < TOL32
 
