@@ -25,4 +25,23 @@ __device__ __forceinline__ void df_mac(float &hi, float &lo, float a, float xh, 
     lo = fmaf(a, xl, __fadd_rn(lo, __fadd_rn(err, e)));
 }
 
+// hi + lo += v: v added to the head by TwoSum, the rounding error into the
+// tail (a sum of n floats accurate to ~n u^2 of the sum of magnitudes).
+__device__ __forceinline__ void df_add(float &hi, float &lo, float v) {
+    const float s = __fadd_rn(hi, v);
+    const float bb = __fsub_rn(s, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(v, bb));
+    hi = s;
+    lo = __fadd_rn(lo, err);
+}
+// (hi, lo) += (hi2, lo2); the same result with the operands swapped (TwoSum's
+// error term is exact, the tails' sum commutative).
+__device__ __forceinline__ void df_add2(float &hi, float &lo, float hi2, float lo2) {
+    const float s = __fadd_rn(hi, hi2);
+    const float bb = __fsub_rn(s, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(hi2, bb));
+    hi = s;
+    lo = __fadd_rn(__fadd_rn(lo, lo2), err);
+}
+
 }  // namespace bem

@@ -536,43 +536,25 @@ arnoldi_step_kernel(int n, int j, double2 *__restrict__ V, size_t ldv, double2 *
     const int per = (n + nb - 1) / nb;
     const int i0 = min(n, b * per), i1 = min(n, i0 + per);
     const int k = j + 1;                              // basis vectors in use
-    constexpr int kQB = 8;                            // dot products per block reduction
-    __shared__ double sr_[kQB][kArNT / 32], si_[kQB][kArNT / 32];
+    __shared__ double sr_[kArNT / 32];                // per-warp partials of |w|^2
     extern __shared__ double2 hs[];                   // k coefficients
     const int lane = tid & 31, warp = tid >> 5;
-    // partial dots of this CTA's slice, kQB basis vectors per pass:
-    // out_part[q * nb + b] for q < k
+    // partial dots of this CTA's slice: warp w takes basis vectors w, w + 8,
+    // ..., its lanes the slice's entries (fixed order), out_part[q * nb + b]
     auto partial_dots = [&](double2 *out_part) {
-        for (int q0 = 0; q0 < k; q0 += kQB) {
-            double a[kQB], c[kQB];
-#pragma unroll
-            for (int u = 0; u < kQB; u++) a[u] = c[u] = 0.0;
-            for (int i = i0 + tid; i < i1; i += kArNT) {
-                const double2 y = w[i];
-#pragma unroll
-                for (int u = 0; u < kQB; u++) {
-                    if (q0 + u < k) {
-                        const double2 x = V[(size_t)(q0 + u) * ldv + i];
-                        a[u] += x.x * y.x + x.y * y.y;   // conj(v) w
-                        c[u] += x.x * y.y - x.y * y.x;
-                    }
-                }
+        for (int q = warp; q < k; q += kArNT / 32) {
+            const double2 *vq = V + (size_t)q * ldv;
+            double a = 0.0, c = 0.0;
+            for (int i = i0 + lane; i < i1; i += 32) {
+                const double2 x = vq[i], y = w[i];
+                a += x.x * y.x + x.y * y.y;   // conj(v) w
+                c += x.x * y.y - x.y * y.x;
             }
-#pragma unroll
-            for (int u = 0; u < kQB; u++) {
-                for (int o = 16; o > 0; o >>= 1) {
-                    a[u] += __shfl_xor_sync(0xffffffffu, a[u], o);
-                    c[u] += __shfl_xor_sync(0xffffffffu, c[u], o);
-                }
-                if (lane == 0) { sr_[u][warp] = a[u]; si_[u][warp] = c[u]; }
+            for (int o = 16; o > 0; o >>= 1) {
+                a += __shfl_xor_sync(0xffffffffu, a, o);
+                c += __shfl_xor_sync(0xffffffffu, c, o);
             }
-            __syncthreads();
-            if (tid < kQB && q0 + tid < k) {
-                double ta = 0.0, tc = 0.0;
-                for (int t = 0; t < kArNT / 32; t++) { ta += sr_[tid][t]; tc += si_[tid][t]; }
-                out_part[(size_t)(q0 + tid) * nb + b] = make_double2(ta, tc);
-            }
-            __syncthreads();
+            if (lane == 0) out_part[(size_t)q * nb + b] = make_double2(a, c);
         }
     };
     // h[q] = sum over the CTAs' partials (one warp per q, fixed order), into
@@ -596,45 +578,65 @@ arnoldi_step_kernel(int n, int j, double2 *__restrict__ V, size_t ldv, double2 *
         }
         __syncthreads();
     };
+    // w -= V h: four consecutive threads per entry, each over every fourth
+    // basis vector, then the four sums in a fixed order
     auto subtract = [&]() {
-        for (int i = i0 + tid; i < i1; i += kArNT) {
+        constexpr int kQ = 4;
+        const int r = tid % kQ;
+        for (int base = i0; base < i1; base += kArNT / kQ) {
+            const int i = base + tid / kQ;
             double a = 0.0, c = 0.0;
-            for (int q = 0; q < k; q++) {
-                const double2 x = V[(size_t)q * ldv + i], y = hs[q];
-                a += x.x * y.x - x.y * y.y;
-                c += x.x * y.y + x.y * y.x;
+            if (i < i1) {
+                for (int q = r; q < k; q += kQ) {
+                    const double2 x = V[(size_t)q * ldv + i], y = hs[q];
+                    a += x.x * y.x - x.y * y.y;
+                    c += x.x * y.y + x.y * y.x;
+                }
             }
-            const double2 ww = w[i];
-            w[i] = make_double2(ww.x - a, ww.y - c);
+#pragma unroll
+            for (int o = 1; o < kQ; o <<= 1) {
+                a += __shfl_xor_sync(0xffffffffu, a, o);
+                c += __shfl_xor_sync(0xffffffffu, c, o);
+            }
+            if (r == 0 && i < i1) {
+                const double2 ww = w[i];
+                w[i] = make_double2(ww.x - a, ww.y - c);
+            }
         }
         __syncthreads();
     };
     double2 *p1 = part, *p2 = part + (size_t)k * nb, *p3 = part + 2 * (size_t)k * nb;
     if (wpart) {
-        // w = the sum of the normal operator's nsplit partial products (FP64),
-        // this CTA's slice: four consecutive threads per entry, each adding a
+        // w = the sum of the normal operator's nsplit partial products, this
+        // CTA's slice: four consecutive threads per entry, each adding a
         // quarter of the partials in order, then the quarters in order (a fixed
-        // order; the loads of an entry are spread over four threads)
+        // order; the loads of an entry are spread over four threads).  The
+        // partials are floats; they are summed in double-float on the FP32 pipe
+        // (TwoSum, error ~1e-14 of the sum of magnitudes) and the head and tail
+        // added in FP64 once per entry: this device's FP64 rate is a small
+        // fraction of its FP32 rate.
         constexpr int kQ = 4;
         const int q = tid % kQ, per_q = (nsplit + kQ - 1) / kQ;
         const int t0 = min(nsplit, q * per_q), t1 = min(nsplit, t0 + per_q);
         for (int base = i0; base < i1; base += kArNT / kQ) {
             const int i = base + tid / kQ;
-            double a = 0.0, c = 0.0;
+            float hr = 0.f, lr = 0.f, hm = 0.f, lm = 0.f;
             if (i < i1) {
 #pragma unroll 4
                 for (int t = t0; t < t1; t++) {
                     const float2 v = wpart[(size_t)t * n + i];
-                    a += v.x;
-                    c += v.y;
+                    df_add(hr, lr, v.x);
+                    df_add(hm, lm, v.y);
                 }
             }
 #pragma unroll
             for (int o = 1; o < kQ; o <<= 1) {   // quarters 0+1, 2+3, then (0+1)+(2+3)
-                a += __shfl_xor_sync(0xffffffffu, a, o);
-                c += __shfl_xor_sync(0xffffffffu, c, o);
+                const float ohr = __shfl_xor_sync(0xffffffffu, hr, o), olr = __shfl_xor_sync(0xffffffffu, lr, o);
+                const float ohm = __shfl_xor_sync(0xffffffffu, hm, o), olm = __shfl_xor_sync(0xffffffffu, lm, o);
+                df_add2(hr, lr, ohr, olr);
+                df_add2(hm, lm, ohm, olm);
             }
-            if (q == 0 && i < i1) w[i] = make_double2(a, c);
+            if (q == 0 && i < i1) w[i] = make_double2((double)hr + (double)lr, (double)hm + (double)lm);
         }
         __syncthreads();   // partial_dots reads w with another thread-to-entry map
     }
@@ -651,11 +653,11 @@ arnoldi_step_kernel(int n, int j, double2 *__restrict__ V, size_t ldv, double2 *
         double a = 0.0;
         for (int i = i0 + tid; i < i1; i += kArNT) a += w[i].x * w[i].x + w[i].y * w[i].y;
         for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-        if (lane == 0) sr_[0][warp] = a;
+        if (lane == 0) sr_[warp] = a;
         __syncthreads();
         if (tid == 0) {
             double t = 0.0;
-            for (int q = 0; q < kArNT / 32; q++) t += sr_[0][q];
+            for (int q = 0; q < kArNT / 32; q++) t += sr_[q];
             p3[b] = make_double2(t, 0.0);
         }
     }
