@@ -213,7 +213,10 @@ void launch_dots(int n, int k, const double2 *V, size_t ldv, const double2 *w, d
                  double2 *part, cudaStream_t st);            // h[j] = V_j^H w, j < k
 void launch_update(int n, int k, const double2 *V, size_t ldv, const double2 *h, double2 *w,
                    cudaStream_t st);                          // w -= V h
+// |w| into *out; part: nrm2_parts() doubles of scratch for the per-CTA
+// partial sums (null: one CTA does it all)
 void launch_nrm2(int n, const double2 *w, double *out, double *part, cudaStream_t st);
+int nrm2_parts();
 // v = w / *nrm; also writes a c64 copy to vf when vf is not null.
 void launch_scale_copy(int n, const double2 *w, const double *nrm, double2 *v, cudaStream_t st,
                        float2 *vf = nullptr);

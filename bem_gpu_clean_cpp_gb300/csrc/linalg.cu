@@ -369,6 +369,36 @@ __global__ void axpy_combo_kernel(int n, int k, const double2 *__restrict__ V, s
     x[i] = make_double2(xx.x + sr, xx.y + si);
 }
 
+// |w| over several CTAs: each CTA's partial sum of squares (grid-stride,
+// fixed order) into part[b], then one warp adds the partials in order and
+// takes the square root.  Spreads the FP64 work over the SMs (one CTA alone
+// is bound by its SM's FP64 rate).
+constexpr int kNrmNT = 256;
+__global__ void __launch_bounds__(kNrmNT)
+nrm2_part_kernel(int n, const double2 *__restrict__ w, double *__restrict__ part) {
+    double s = 0.0;
+    for (int i = blockIdx.x * kNrmNT + threadIdx.x; i < n; i += gridDim.x * kNrmNT) {
+        const double2 v = w[i];
+        s += v.x * v.x + v.y * v.y;
+    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    __shared__ double red[kNrmNT / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) red[warp] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0;
+        for (int t = 0; t < kNrmNT / 32; t++) a += red[t];
+        part[blockIdx.x] = a;
+    }
+}
+__global__ void nrm2_final_kernel(int nb, const double *__restrict__ part, double *__restrict__ out) {
+    double s = 0.0;
+    for (int t = threadIdx.x; t < nb; t += 32) s += part[t];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (threadIdx.x == 0) *out = sqrt(s);
+}
+
 __global__ void nrm2_kernel(int n, const double2 *__restrict__ w, double *__restrict__ out) {
     double s = 0;
     for (int i = threadIdx.x; i < n; i += blockDim.x) s += w[i].x * w[i].x + w[i].y * w[i].y;
@@ -460,6 +490,43 @@ __global__ void givens_kernel(int j, double2 *__restrict__ H, int ldh, double2 *
 }
 
 // Back substitution R y = g (Rsolver, GMRES.cu:26-42).
+// Back substitution H y = g for the k x k upper triangle of H (column-major,
+// ld ldh), column by column: the CTA stages the triangle (packed by column)
+// and g in shared memory and the diagonal's reciprocals, then one warp takes
+// y_i = s_i / H_ii and s_t -= H_ti y_i for t < i, its lanes over t.  For k up
+// to kTriStage; larger k use trisolve_kernel.
+constexpr int kTriStage = 64;
+constexpr int kTriNT = 256;
+__global__ void __launch_bounds__(kTriNT)
+trisolve_staged_kernel(int k, const double2 *__restrict__ H, int ldh, const double2 *__restrict__ g,
+                       double2 *__restrict__ y) {
+    __shared__ double2 tri[kTriStage * (kTriStage + 1) / 2], s[kTriStage], rinv[kTriStage];
+    for (int e = threadIdx.x; e < k * k; e += kTriNT) {   // column i, rows 0..i at i (i + 1) / 2
+        const int i = e / k, t = e - i * k;
+        if (t <= i) tri[i * (i + 1) / 2 + t] = H[(size_t)i * ldh + t];
+    }
+    for (int t = threadIdx.x; t < k; t += kTriNT) {
+        s[t] = g[t];
+        const double2 d = H[(size_t)t * ldh + t];
+        const double den = d.x * d.x + d.y * d.y;
+        rinv[t] = make_double2(d.x / den, -d.y / den);
+    }
+    __syncthreads();
+    if (threadIdx.x >= 32) return;
+    const int lane = threadIdx.x;
+    for (int i = k - 1; i >= 0; i--) {
+        const double2 a = s[i], r = rinv[i];
+        const double2 yi = make_double2(a.x * r.x - a.y * r.y, a.x * r.y + a.y * r.x);
+        if (lane == 0) y[i] = yi;
+        const double2 *col = tri + i * (i + 1) / 2;
+        for (int t = lane; t < i; t += 32) {
+            const double2 h = col[t];
+            s[t] = make_double2(s[t].x - (h.x * yi.x - h.y * yi.y), s[t].y - (h.x * yi.y + h.y * yi.x));
+        }
+        __syncwarp();
+    }
+}
+
 __global__ void trisolve_kernel(int k, const double2 *__restrict__ H, int ldh, const double2 *__restrict__ g,
                                 double2 *__restrict__ y) {
     if (threadIdx.x != 0) return;
@@ -518,7 +585,7 @@ sum_many_splits_kernel(int N, int ns, const float2 *__restrict__ part, double2 *
 // column and its Givens rotation (GMRES.cu:44-88) with the residual estimate
 // |g_{j+1}| in *res.  Each CTA owns a contiguous slice of the n entries; the
 // dot products and the norm are per-CTA partial sums reduced after a grid
-// barrier, in the same order by every CTA.  Every CTA passes the same three
+// barrier, in the same order by every CTA.  Every CTA passes the same two
 // grid barriers (no early exit), and the launch is cooperative, so all CTAs
 // are resident.
 constexpr int kArNT = 256;
@@ -536,14 +603,14 @@ arnoldi_step_kernel(int n, int j, double2 *__restrict__ V, size_t ldv, double2 *
     const int per = (n + nb - 1) / nb;
     const int i0 = min(n, b * per), i1 = min(n, i0 + per);
     const int k = j + 1;                              // basis vectors in use
-    __shared__ double sr_[kArNT / 32];                // per-warp partials of |w|^2
     extern __shared__ double2 hs[];                   // k coefficients
     const int lane = tid & 31, warp = tid >> 5;
     // partial dots of this CTA's slice: warp w takes basis vectors w, w + 8,
-    // ..., its lanes the slice's entries (fixed order), out_part[q * nb + b]
-    auto partial_dots = [&](double2 *out_part) {
-        for (int q = warp; q < k; q += kArNT / 32) {
-            const double2 *vq = V + (size_t)q * ldv;
+    // ..., its lanes the slice's entries (fixed order), out_part[q * nb + b];
+    // with nq = k + 1 the last "basis vector" is w itself (|w|^2 partials)
+    auto partial_dots = [&](double2 *out_part, int nq) {
+        for (int q = warp; q < nq; q += kArNT / 32) {
+            const double2 *vq = q < k ? V + (size_t)q * ldv : w;
             double a = 0.0, c = 0.0;
             for (int i = i0 + lane; i < i1; i += 32) {
                 const double2 x = vq[i], y = w[i];
@@ -558,9 +625,9 @@ arnoldi_step_kernel(int n, int j, double2 *__restrict__ V, size_t ldv, double2 *
         }
     };
     // h[q] = sum over the CTAs' partials (one warp per q, fixed order), into
-    // shared memory and, from CTA 0, into hout
-    auto reduce_dots = [&](const double2 *in_part, double2 *hout) {
-        for (int q = warp; q < k; q += kArNT / 32) {
+    // shared memory and, from CTA 0 and for q < k, into hout
+    auto reduce_dots = [&](const double2 *in_part, double2 *hout, int nq) {
+        for (int q = warp; q < nq; q += kArNT / 32) {
             double a = 0.0, c = 0.0;
             for (int t = lane; t < nb; t += 32) {
                 const double2 p = in_part[(size_t)q * nb + t];
@@ -573,14 +640,17 @@ arnoldi_step_kernel(int n, int j, double2 *__restrict__ V, size_t ldv, double2 *
             }
             if (lane == 0) {
                 hs[q] = make_double2(a, c);
-                if (b == 0) hout[q] = hs[q];
+                if (b == 0 && q < k) hout[q] = hs[q];
             }
         }
         __syncthreads();
     };
     // w -= V h: four consecutive threads per entry, each over every fourth
-    // basis vector, then the four sums in a fixed order
-    auto subtract = [&]() {
+    // basis vector, then the four sums in a fixed order; with inv >= 0 the
+    // result is the next basis vector (w - V h) inv, written to vn and vf
+    // instead of w
+    double2 *vn = V + (size_t)k * ldv;
+    auto subtract = [&](double inv) {
         constexpr int kQ = 4;
         const int r = tid % kQ;
         for (int base = i0; base < i1; base += kArNT / kQ) {
@@ -600,12 +670,18 @@ arnoldi_step_kernel(int n, int j, double2 *__restrict__ V, size_t ldv, double2 *
             }
             if (r == 0 && i < i1) {
                 const double2 ww = w[i];
-                w[i] = make_double2(ww.x - a, ww.y - c);
+                if (inv < 0.0) {
+                    w[i] = make_double2(ww.x - a, ww.y - c);
+                } else {
+                    const double2 o = make_double2((ww.x - a) * inv, (ww.y - c) * inv);
+                    vn[i] = o;
+                    vf[i] = make_float2((float)o.x, (float)o.y);
+                }
             }
         }
         __syncthreads();
     };
-    double2 *p1 = part, *p2 = part + (size_t)k * nb, *p3 = part + 2 * (size_t)k * nb;
+    double2 *p1 = part, *p2 = part + (size_t)k * nb;   // k and k + 1 partials per CTA
     if (wpart) {
         // w = the sum of the normal operator's nsplit partial products, this
         // CTA's slice: four consecutive threads per entry, each adding a
@@ -640,44 +716,28 @@ arnoldi_step_kernel(int n, int j, double2 *__restrict__ V, size_t ldv, double2 *
         }
         __syncthreads();   // partial_dots reads w with another thread-to-entry map
     }
-    partial_dots(p1);
+    partial_dots(p1, k);
     grid.sync();
-    reduce_dots(p1, h1);
-    subtract();
-    partial_dots(p2);
+    reduce_dots(p1, h1, k);
+    subtract(-1.0);
+    // second pass: h2 = V^H w and |w|^2 in the same reduction; the norm of
+    // w - V h2 is sqrt(|w|^2 - |h2|^2) (V orthonormal; h2 is at the level of
+    // the first pass's rounding, so the difference does not cancel), which
+    // saves a third grid barrier
+    partial_dots(p2, k + 1);
     grid.sync();
-    reduce_dots(p2, h2);
-    subtract();
-    // |w|^2 partials
-    {
-        double a = 0.0;
-        for (int i = i0 + tid; i < i1; i += kArNT) a += w[i].x * w[i].x + w[i].y * w[i].y;
-        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-        if (lane == 0) sr_[warp] = a;
-        __syncthreads();
-        if (tid == 0) {
-            double t = 0.0;
-            for (int q = 0; q < kArNT / 32; q++) t += sr_[q];
-            p3[b] = make_double2(t, 0.0);
-        }
-    }
-    grid.sync();
+    reduce_dots(p2, h2, k + 1);
     __shared__ double nrm_s;
     if (warp == 0) {
         double t = 0.0;
-        for (int q = lane; q < nb; q += 32) t += p3[q].x;
+        for (int q = lane; q < k; q += 32) t += hs[q].x * hs[q].x + hs[q].y * hs[q].y;
         for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-        if (lane == 0) nrm_s = sqrt(t);
+        if (lane == 0) nrm_s = sqrt(fmax(hs[k].x - t, 0.0));
     }
     __syncthreads();
     const double nrm = nrm_s;
     const double inv = nrm > 0 ? 1.0 / nrm : 0.0;
-    double2 *vn = V + (size_t)k * ldv;
-    for (int i = i0 + tid; i < i1; i += kArNT) {
-        const double2 o = make_double2(w[i].x * inv, w[i].y * inv);
-        vn[i] = o;
-        vf[i] = make_float2((float)o.x, (float)o.y);
-    }
+    subtract(inv);   // v_{j+1} = (w - V h2) / |w - V h2|
     if (b == 0 && tid == 0) {
         // Hessenberg column j = h1 + h2, H[j+1, j] = |w|, then the rotations
         double2 *h = H + (size_t)j * ldh;
@@ -1061,7 +1121,7 @@ int arnoldi_step_blocks() {
         if (cudaGetDevice(&dev) != cudaSuccess ||
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, arnoldi_step_kernel, kArNT,
-                                                          (size_t)kArnoldiMaxK * sizeof(double2)) != cudaSuccess ||
+                                                          (size_t)(kArnoldiMaxK + 1) * sizeof(double2)) != cudaSuccess ||
             per < 1) {
             cudaGetLastError();
             nb = 0;
@@ -1078,7 +1138,7 @@ bool launch_arnoldi_step(int n, int j, double2 *V, size_t ldv, double2 *w, float
     const int nb = arnoldi_step_blocks();
     if (nb <= 0 || j + 1 > kArnoldiMaxK || n < 1) return false;
     BEM_PROF("arnoldi_step", st);
-    const size_t smem = (size_t)(j + 1) * sizeof(double2);
+    const size_t smem = (size_t)(j + 2) * sizeof(double2);   // h and |w|^2
     void *args[] = {&n, &j, &V, &ldv, &w, &vf, &h1, &h2, &H, &ldh, &cs, &sn, &g, &res, &part, &wpart, &nsplit};
     const cudaError_t e = cudaLaunchCooperativeKernel((const void *)arnoldi_step_kernel, dim3(nb), dim3(kArNT),
                                                       args, smem, st);
@@ -1326,9 +1386,19 @@ void launch_update(int n, int k, const double2 *V, size_t ldv, const double2 *h,
     KERNEL_CHECK();
 }
 
-void launch_nrm2(int n, const double2 *w, double *out, double *, cudaStream_t st) {
+int nrm2_parts() { return device_sm_count(); }
+
+void launch_nrm2(int n, const double2 *w, double *out, double *part, cudaStream_t st) {
     BEM_PROF("nrm2", st);
-    nrm2_kernel<<<1, 1024, 0, st>>>(n, w, out);
+    const int nb = std::min(nrm2_parts(), blocks(n, kNrmNT));
+    if (part && nb > 1) {
+        nrm2_part_kernel<<<nb, kNrmNT, 0, st>>>(n, w, part);
+        count_launch();
+        KERNEL_CHECK();
+        nrm2_final_kernel<<<1, 32, 0, st>>>(nb, part, out);
+    } else {
+        nrm2_kernel<<<1, 1024, 0, st>>>(n, w, out);
+    }
     count_launch();
     KERNEL_CHECK();
 }
@@ -1397,7 +1467,8 @@ void launch_givens(int j, double2 *H, int ldh, double2 *cs, double2 *sn, double2
 
 void launch_trisolve(int k, const double2 *H, int ldh, const double2 *g, double2 *y, cudaStream_t st) {
     BEM_PROF("trisolve", st);
-    trisolve_kernel<<<1, 32, 0, st>>>(k, H, ldh, g, y);
+    if (k <= kTriStage) trisolve_staged_kernel<<<1, kTriNT, 0, st>>>(k, H, ldh, g, y);
+    else trisolve_kernel<<<1, 32, 0, st>>>(k, H, ldh, g, y);
     count_launch();
     KERNEL_CHECK();
 }

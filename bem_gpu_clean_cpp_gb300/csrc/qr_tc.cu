@@ -1215,7 +1215,7 @@ void bem_solver_s::solve_qr_tc(bem_solve_info_t *info) {
         double2 *x = X + (size_t)s * n;
         launch_gemv_h_f64(prec, m, n, d_A.p, lda, b, w_gv.as<double2>(), w_part.as<double2>(), w_vf.as<float2>(),
                           stream);
-        launch_nrm2(n, w_gv.as<double2>(), scal + 0, nullptr, stream);
+        launch_nrm2(n, w_gv.as<double2>(), scal + 0, w_part.as<double>(), stream);
         const double bn = read_scalar(0);
         double rel = 0.0, prev = 1e300;
         int it = 0;
@@ -1225,7 +1225,7 @@ void bem_solver_s::solve_qr_tc(bem_solve_info_t *info) {
             launch_resid(prec, m, n, d_A.p, lda, x, b, w_r.as<double2>(), w_vf.as<float2>(), stream);
             launch_gemv_h_f64(prec, m, n, d_A.p, lda, w_r.as<double2>(), w_gv.as<double2>(), w_part.as<double2>(),
                               w_vf.as<float2>(), stream);
-            launch_nrm2(n, w_gv.as<double2>(), scal + 1, nullptr, stream);
+            launch_nrm2(n, w_gv.as<double2>(), scal + 1, w_part.as<double>(), stream);
             rel = read_scalar(1) / bn;
             if (!std::isfinite(rel)) {
                 int h_st = 0;   // a tensor-core GEMM that gave up on a wait explains it

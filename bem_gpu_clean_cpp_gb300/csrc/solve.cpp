@@ -133,7 +133,7 @@ void bem_solver_s::solve_refined(bem_solve_info_t *info) {
         double2 *x = d_x.as<double2>() + (size_t)s * n;
         launch_zero_f64(n, x, stream);
         launch_gemv_h_f64(prec, R, n, A, lda, b, w_gv.as<double2>(), w_part.as<double2>(), w_vf.as<float2>(), stream);
-        launch_nrm2(n, w_gv.as<double2>(), scal + 0, nullptr, stream);
+        launch_nrm2(n, w_gv.as<double2>(), scal + 0, w_part.as<double>(), stream);
         const double bn = read_scalar(0);
         if (!(bn > 0.0)) continue;
         double rel = 1.0;
@@ -146,7 +146,7 @@ void bem_solver_s::solve_refined(bem_solve_info_t *info) {
                 launch_resid(prec, R, n, A, lda, x, b, w_r.as<double2>(), w_vf.as<float2>(), stream);
                 launch_gemv_h_f64(prec, R, n, A, lda, w_r.as<double2>(), w_gv.as<double2>(),
                                   w_part.as<double2>(), w_vf.as<float2>(), stream);
-                launch_nrm2(n, w_gv.as<double2>(), scal + 1, nullptr, stream);
+                launch_nrm2(n, w_gv.as<double2>(), scal + 1, w_part.as<double>(), stream);
                 gn = read_scalar(1);
             } else {
                 CUDA_TRY(cudaMemcpyAsync(scal + 1, scal + 0, sizeof(double), cudaMemcpyDeviceToDevice, stream));
