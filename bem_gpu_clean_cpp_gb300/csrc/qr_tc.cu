@@ -1059,12 +1059,7 @@ void bem_solver_s::solve_qr_tc(bem_solve_info_t *info) {
     qt_part.ensure(pn_b + pw_b);
     float *const part_set[2] = {qt_part.as<float>(), reinterpret_cast<float *>(static_cast<char *>(qt_part.p) + pn_b)};
     const size_t part_cap[2] = {pn_b / sizeof(float), pw_b / sizeof(float)};
-    if (!qr_aux) {
-        int least = 0, greatest = 0;
-        CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
-        CUDA_TRY(cudaStreamCreateWithPriority(&qr_aux, cudaStreamNonBlocking, greatest));
-        for (auto &e : qr_ev) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    }
+    ensure_aux();
     cudaEvent_t ev_in = qr_ev[0], ev_out = qr_ev[1], ev_ready[2] = {qr_ev[2], qr_ev[3]},
                 ev_wide[2] = {qr_ev[4], qr_ev[5]};
     qt_scal.ensure(sizeof(float) * 8);

@@ -132,7 +132,15 @@ void bem_solver_s::solve_refined(bem_solve_info_t *info) {
         const double2 *b = d_B.as<double2>() + (size_t)s * R;
         double2 *x = d_x.as<double2>() + (size_t)s * n;
         launch_zero_f64(n, x, stream);
-        launch_gemv_h_f64(prec, R, n, A, lda, b, w_gv.as<double2>(), w_part.as<double2>(), w_vf.as<float2>(), stream);
+        // g0 = A^H b only starts the first inner solve from x = 0, to a relative
+        // tolerance far above FP32 rounding, and scales the stopping test; every
+        // later A^H r is FP64-accurate, so for c64 A the single-pass FP32
+        // product suffices here (the refined solution does not depend on it)
+        if (prec == BEM_PREC_C64)
+            launch_gemv_h_c64(R, n, A, lda, b, 1, w_gv.p, 1, w_part.p, stream);
+        else
+            launch_gemv_h_f64(prec, R, n, A, lda, b, w_gv.as<double2>(), w_part.as<double2>(), w_vf.as<float2>(),
+                              stream);
         launch_nrm2(n, w_gv.as<double2>(), scal + 0, w_part.as<double>(), stream);
         const double bn = read_scalar(0);
         if (!(bn > 0.0)) continue;

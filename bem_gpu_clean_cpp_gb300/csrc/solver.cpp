@@ -174,6 +174,8 @@ bem_solver_s::~bem_solver_s() {
     if (qr_aux) cudaStreamSynchronize(qr_aux);
     for (auto &e : qr_ev)
         if (e) cudaEventDestroy(e);
+    for (auto &e : asm_ev)
+        if (e) cudaEventDestroy(e);
     if (qr_aux) cudaStreamDestroy(qr_aux);
     if (stream) cudaStreamDestroy(stream);
     if (cur >= 0 && cur != device) cudaSetDevice(cur);
@@ -207,6 +209,32 @@ void bem_solver_s::set_geometry(const double *pnts, int num_pnts, const int *ele
             return build_host_tiles(N, E, h_nodes, h_elems, cap);
         });
     }
+    // Nodes, CHIEF points and BCs go up straight from the caller's arrays (no
+    // host copy; a pinned caller buffer is a direct DMA) while the host work
+    // below goes on; the float head/tail rows and the int4 element table
+    // follow from a pinned staging buffer.  The caller's arrays are only read
+    // until this call returns.
+    if (!bc) {   // the default BC (0, 1, -1) per element, uploaded from here
+        h_bc.resize(6 * (size_t)E);
+        for (int e = 0; e < E; e++) {
+            double d[6] = {0, 0, 1, 0, -1, 0};
+            std::memcpy(&h_bc[6 * (size_t)e], d, sizeof(d));
+        }
+    }
+    d_nodes.ensure(sizeof(double) * 3 * N);
+    d_rows_d.ensure(sizeof(double) * 3 * (size_t)R);
+    d_rows_f.ensure(sizeof(float4) * 2 * (size_t)R);
+    d_elems.ensure(sizeof(int4) * E);
+    d_bc.ensure(sizeof(double) * 6 * (size_t)E);
+    d_geo_f.ensure(sizeof(float4) * kGeoFloat4 * (size_t)E);
+    d_geo_d.ensure(sizeof(double) * kGeoDouble * (size_t)E);
+    CUDA_TRY(cudaMemcpyAsync(d_nodes.p, pnts, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemcpyAsync(d_rows_d.p, pnts, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, stream));
+    if (M)
+        CUDA_TRY(cudaMemcpyAsync(d_rows_d.as<double>() + 3 * (size_t)N, chief, sizeof(double) * 3 * (size_t)M,
+                                 cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemcpyAsync(d_bc.p, bc ? bc : h_bc.data(), sizeof(double) * 6 * (size_t)E, cudaMemcpyHostToDevice,
+                             stream));
     // the longest edge: the largest squared length, one square root
     double max_edge2 = 0.0;
     for (int e = 0; e < E; e++) {
@@ -219,13 +247,6 @@ void bem_solver_s::set_geometry(const double *pnts, int num_pnts, const int *ele
         }
     }
     max_edge = std::sqrt(max_edge2);
-    if (!bc) {   // the default BC (0, 1, -1) per element, uploaded from here
-        h_bc.resize(6 * (size_t)E);
-        for (int e = 0; e < E; e++) {
-            double d[6] = {0, 0, 1, 0, -1, 0};
-            std::memcpy(&h_bc[6 * (size_t)e], d, sizeof(d));
-        }
-    }
     // alpha = 0 on every element (bcA = 0: the far kernel forms no G sums
     // for A), and gamma = 0 too (bcC = 0: none for beta either)
     {
@@ -259,10 +280,7 @@ void bem_solver_s::set_geometry(const double *pnts, int num_pnts, const int *ele
         return build_near_grid(E, h_nodes, h_elems, row_lo, row_hi, max_edge, eta);
     });
 
-    // The float head/tail rows and the int4 element table are built in a
-    // pinned staging buffer; nodes, CHIEF points and BCs go up straight from
-    // the caller's arrays (no host copy; a pinned caller buffer is a direct
-    // DMA).  The caller's arrays are only read until this call returns.
+    // the float head/tail rows and the int4 element table, staged
     const size_t rf_bytes = sizeof(float4) * 2 * (size_t)R, el_bytes = sizeof(int4) * (size_t)E;
     if (h_stage_bytes < rf_bytes + el_bytes) {
         if (h_stage) CUDA_TRY(cudaFreeHost(h_stage));
@@ -280,24 +298,12 @@ void bem_solver_s::set_geometry(const double *pnts, int num_pnts, const int *ele
                                     (float)(h_rows[3 * i + 2] - hz), 0.f);
     }
     for (int e = 0; e < E; e++) el[e] = make_int4(h_elems[3 * e], h_elems[3 * e + 1], h_elems[3 * e + 2], 0);
-    d_nodes.ensure(sizeof(double) * 3 * N);
-    d_rows_d.ensure(sizeof(double) * 3 * (size_t)R);
-    d_rows_f.ensure(sizeof(float4) * 2 * (size_t)R);
-    d_elems.ensure(sizeof(int4) * E);
-    d_bc.ensure(sizeof(double) * 6 * (size_t)E);
-    d_geo_f.ensure(sizeof(float4) * kGeoFloat4 * (size_t)E);
-    d_geo_d.ensure(sizeof(double) * kGeoDouble * (size_t)E);
-    CUDA_TRY(cudaMemcpyAsync(d_nodes.p, pnts, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, stream));
-    CUDA_TRY(cudaMemcpyAsync(d_rows_d.p, pnts, sizeof(double) * 3 * N, cudaMemcpyHostToDevice, stream));
-    if (M)
-        CUDA_TRY(cudaMemcpyAsync(d_rows_d.as<double>() + 3 * (size_t)N, chief, sizeof(double) * 3 * (size_t)M,
-                                 cudaMemcpyHostToDevice, stream));
     CUDA_TRY(cudaMemcpyAsync(d_rows_f.p, rf, rf_bytes, cudaMemcpyHostToDevice, stream));
     CUDA_TRY(cudaMemcpyAsync(d_elems.p, el, el_bytes, cudaMemcpyHostToDevice, stream));
-    CUDA_TRY(cudaMemcpyAsync(d_bc.p, bc ? bc : h_bc.data(), sizeof(double) * 6 * (size_t)E, cudaMemcpyHostToDevice,
-                             stream));
-    CUDA_TRY(cudaStreamSynchronize(stream));   // the caller's arrays and the staging buffer are free again
+    // the element tables for the current near_eta, queued behind the uploads
     geo_eta = -1.0;
+    ensure_geo();
+    CUDA_TRY(cudaStreamSynchronize(stream));   // the caller's arrays and the staging buffer are free again
     tiles[0].valid = tiles[1].valid = false;
     assembled = solved = false;
 }
@@ -321,6 +327,15 @@ void bem_solver_s::set_sources(const bem_source_t *srcs, int num) {
     solved = false;
 }
 
+void bem_solver_s::ensure_aux() {
+    if (qr_aux) return;
+    int least = 0, greatest = 0;
+    CUDA_TRY(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    CUDA_TRY(cudaStreamCreateWithPriority(&qr_aux, cudaStreamNonBlocking, greatest));
+    for (auto &e : qr_ev) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    for (auto &e : asm_ev) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+}
+
 void bem_solver_s::ensure_geo() {
     if (E == 0) BEM_FAIL(BEM_ERR_STATE, "no geometry set");
     if (geo_eta == opt.near_eta) return;
@@ -332,8 +347,7 @@ void bem_solver_s::ensure_geo() {
 
 // The near-pair list depends on the geometry and near_eta only, so every
 // assembly of one geometry (any wavenumber, any sources) reuses it.
-void bem_solver_s::ensure_near_list() {
-    ensure_geo();
+void bem_solver_s::ensure_near_list(cudaStream_t st) {
     if (near_valid) return;
     BEM_HOST_PROF("near_list");
     // (the host arrays of the uploads below stay members until the next
@@ -349,25 +363,24 @@ void bem_solver_s::ensure_near_list() {
     const std::vector<int> &start = gh.start, &order = gh.order;
     d_grid_start.ensure(sizeof(int) * (ncell + 1));
     d_grid_elems.ensure(sizeof(int) * std::max(1, E));
-    CUDA_TRY(cudaMemcpyAsync(d_grid_start.p, start.data(), sizeof(int) * (ncell + 1), cudaMemcpyHostToDevice, stream));
-    CUDA_TRY(cudaMemcpyAsync(d_grid_elems.p, order.data(), sizeof(int) * E, cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemcpyAsync(d_grid_start.p, start.data(), sizeof(int) * (ncell + 1), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaMemcpyAsync(d_grid_elems.p, order.data(), sizeof(int) * E, cudaMemcpyHostToDevice, st));
     NearGrid grid{{lo[0], lo[1], lo[2]}, 1.0 / cell, {dim[0], dim[1], dim[2]}, d_grid_start.as<int>(),
                   d_grid_elems.as<int>()};
     d_near_ptr.ensure(sizeof(int) * ((size_t)R + 1));
-    launch_near_list(row_points(), N, geo_tables(), grid, nullptr, d_near_ptr.as<int>(), nullptr, stream);
+    launch_near_list(row_points(), N, geo_tables(), grid, nullptr, d_near_ptr.as<int>(), nullptr, st);
     std::vector<int> cnt(R);
-    CUDA_TRY(cudaMemcpyAsync(cnt.data(), d_near_ptr.p, sizeof(int) * R, cudaMemcpyDeviceToHost, stream));
-    CUDA_TRY(cudaStreamSynchronize(stream));
+    CUDA_TRY(cudaMemcpyAsync(cnt.data(), d_near_ptr.p, sizeof(int) * R, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaStreamSynchronize(st));
     std::vector<int> &ptr = near_ptr_h;
     ptr.assign(R + 1, 0);
     for (int r = 0; r < R; r++) {
         if (ptr[r] > 0x7fffffff - cnt[r]) BEM_FAIL(BEM_ERR_TOO_LARGE, "too many near pairs");
         ptr[r + 1] = ptr[r] + cnt[r];
     }
-    CUDA_TRY(cudaMemcpyAsync(d_near_ptr.p, ptr.data(), sizeof(int) * (R + 1), cudaMemcpyHostToDevice, stream));
+    CUDA_TRY(cudaMemcpyAsync(d_near_ptr.p, ptr.data(), sizeof(int) * (R + 1), cudaMemcpyHostToDevice, st));
     d_near_ids.ensure(sizeof(int) * std::max(1, ptr[R]));
-    launch_near_list(row_points(), N, geo_tables(), grid, d_near_ptr.as<int>(), nullptr, d_near_ids.as<int>(),
-                     stream);
+    launch_near_list(row_points(), N, geo_tables(), grid, d_near_ptr.as<int>(), nullptr, d_near_ids.as<int>(), st);
     near_valid = true;
 }
 
@@ -539,11 +552,15 @@ void bem_solver_s::assemble(double kk, int precision) {
     if (S == 0) BEM_FAIL(BEM_ERR_STATE, "no sources set");
     ensure_quadrature(opt.order);
     ensure_geo();
-    // The near-pair list (host grid, two small kernels, two waits) is built
-    // first, while the column-tile tables may still be in the making on the
-    // host thread set_geometry started; after the far kernel its waits would
-    // hold the host for that whole kernel.
-    ensure_near_list();
+    // The near-pair list (two small kernels and a read-back of the per-row
+    // counts) is built on the handle's second, high-priority stream while the
+    // far kernel runs: that stream starts after the element tables, and the
+    // near kernel waits for the list.
+    const bool near_build = !near_valid;
+    if (near_build) {
+        ensure_aux();
+        CUDA_TRY(cudaEventRecord(asm_ev[0], stream));
+    }
     ensure_tiles(precision);
     k = kk;
     prec = precision;
@@ -625,6 +642,12 @@ void bem_solver_s::assemble(double kk, int precision) {
         launch_far_assembly(precision, row_points(), N, geo_tables(), ts, ph, d_A.p, lda, d_cpart.p, d_bpart.p,
                             stream, variant);
     far_variant_used = variant;
+    if (near_build) {
+        CUDA_TRY(cudaStreamWaitEvent(qr_aux, asm_ev[0], 0));
+        ensure_near_list(qr_aux);
+        CUDA_TRY(cudaEventRecord(asm_ev[1], qr_aux));
+        CUDA_TRY(cudaStreamWaitEvent(stream, asm_ev[1], 0));
+    }
     d_beta.ensure(sizeof(double2) * (size_t)R);
     launch_near_assembly(precision, row_points(), N, geo_tables(), ph, d_A.p, lda, d_cpart.p, d_bpart.p,
                          T.ntiles, d_srcs.as<DevSource>(), S, d_B.as<double2>(), d_beta.as<double2>(),

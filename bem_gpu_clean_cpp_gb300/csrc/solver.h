@@ -134,10 +134,14 @@ struct bem_solver_s {
     // and V^H V, Z = C^H V, the packed right-hand operands, split-K partial
     // sums, scales
     bem::DevMem qt_v, qt_vrr, qt_t, qt_z, qt_opv, qt_opw, qt_part, qt_scal, qt_dinv;
-    // QR_TC look-ahead: a high-priority stream for the panel chain and its
-    // events (created on first use)
+    // A high-priority second stream of the handle (created on first use by
+    // ensure_aux): the QR_TC look-ahead's panel chain, and the near-pair list
+    // built beside the far kernel; the QR's events and the assembly's two
+    // (element tables ready, near list ready)
     cudaStream_t qr_aux = nullptr;
     cudaEvent_t qr_ev[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t asm_ev[2] = {nullptr, nullptr};
+    void ensure_aux();
     // field workspace
     bem::DevMem f_rows_f, f_rows_d, f_part, f_near, f_out, f_u;
 
@@ -175,7 +179,7 @@ struct bem_solver_s {
     static size_t estimate_bytes(int N, int E, int M, int S, int method, const bem_options_t &o);
 
     void ensure_geo();
-    void ensure_near_list();
+    void ensure_near_list(cudaStream_t st);   // its uploads, kernels and read-back on st
     void ensure_tiles(int precision);
     bem::GeoTables geo_tables() const;
     bem::RowPoints row_points() const;
