@@ -61,7 +61,7 @@ uint32_t morton_key(const double *p, const double *lo, const double *inv) {
 // meshes: at least 13).  Appends the records batch by batch to `out` and the
 // batch boundaries (offsets into `out`) to `bptr`.
 void pack_batches(const std::vector<TileRec> &list, int tile_cols, std::vector<TileRec> &out,
-                  std::vector<int> &bptr) {
+                  std::vector<int> &bptr, HostScratch &scr) {
     // Bit sets, 64 batches per word: per slot, the batches already holding a
     // record on it (`used`); per fill level s, the batches holding s records
     // (`level`).  A record's allowed batches are the complement of its slots'
@@ -71,12 +71,15 @@ void pack_batches(const std::vector<TileRec> &list, int tile_cols, std::vector<T
     // other: a handful of word operations per record.
     const int nb0 = (int)((list.size() + kFarBatch - 1) / kFarBatch);
     int words = std::max(1, (nb0 + 8 + 63) / 64);
-    std::vector<uint64_t> used((size_t)tile_cols * words, 0);
-    std::vector<uint64_t> level((size_t)(kFarBatch + 1) * words, 0);
-    std::vector<int> size(nb0, 0), batch_of(list.size());
+    std::vector<uint64_t> &used = scr.used, &level = scr.level, &busy = scr.busy;
+    std::vector<int> &size = scr.size, &batch_of = scr.batch_of;
+    used.assign((size_t)tile_cols * words, 0);
+    level.assign((size_t)(kFarBatch + 1) * words, 0);
+    size.assign(nb0, 0);
+    batch_of.resize(list.size());
     for (int b = 0; b < nb0; b++) level[b / 64] |= 1ull << (b % 64);
     int low = 0, high = 0;   // lowest and highest fill levels holding a batch
-    std::vector<uint64_t> busy(words);
+    busy.assign(words, 0);
     for (size_t r = 0; r < list.size(); r++) {
         const TileRec &rec = list[r];
         for (int w = 0; w < words; w++) {
@@ -129,7 +132,8 @@ void pack_batches(const std::vector<TileRec> &list, int tile_cols, std::vector<T
             if (rec.slot[j] >= 0) used[(size_t)rec.slot[j] * words + best / 64] |= bit;
     }
     // stable counting sort of the records by batch
-    std::vector<int> start(size.size() + 1, 0);
+    std::vector<int> &start = scr.start;
+    start.assign(size.size() + 1, 0);
     for (size_t b = 0; b < size.size(); b++) start[b + 1] = start[b] + size[b];
     const size_t base = out.size();
     out.resize(base + list.size());
@@ -202,11 +206,11 @@ void bem_solver_s::set_geometry(const double *pnts, int num_pnts, const int *ele
     // The column-tile tables (host work of ~1 ms at 20480 elements) are
     // built on another host thread while this call and the assembly's first
     // steps go on; ensure_tiles takes them.
-    host_tiles = HostTiles{};
+    host_tiles.cap = -1;   // (its storage is kept for reuse)
     {
         const int cap = opt.tile_cols > 0 ? std::min(opt.tile_cols, kTileColsMax) : kTileColsMax;
         tile_future = std::async(std::launch::async, [this, cap] {
-            return build_host_tiles(N, E, h_nodes, h_elems, cap);
+            build_host_tiles(N, E, h_nodes, h_elems, cap, tiles_next, tile_scratch);
         });
     }
     // Nodes, CHIEF points and BCs go up straight from the caller's arrays (no
@@ -276,8 +280,9 @@ void bem_solver_s::set_geometry(const double *pnts, int num_pnts, const int *ele
     }
     // the near-pair grid's host part on another host thread (ensure_near_list
     // takes it when near_eta is still the one it was built for)
+    grid_next.eta = -1.0;
     grid_future = std::async(std::launch::async, [this, eta = opt.near_eta] {
-        return build_near_grid(E, h_nodes, h_elems, row_lo, row_hi, max_edge, eta);
+        build_near_grid(E, h_nodes, h_elems, row_lo, row_hi, max_edge, eta, grid_next, grid_scratch);
     });
 
     // the float head/tail rows and the int4 element table, staged
@@ -353,10 +358,12 @@ void bem_solver_s::ensure_near_list(cudaStream_t st) {
     // (the host arrays of the uploads below stay members until the next
     // geometry, whose set_geometry ends with a stream synchronisation)
     NearGridHost &gh = near_grid_h;
-    gh = NearGridHost{};
-    if (grid_future.valid()) gh = grid_future.get();
+    if (grid_future.valid()) {
+        grid_future.get();
+        std::swap(gh, grid_next);
+    }
     if (gh.eta != opt.near_eta || gh.start.empty())
-        gh = build_near_grid(E, h_nodes, h_elems, row_lo, row_hi, max_edge, opt.near_eta);
+        build_near_grid(E, h_nodes, h_elems, row_lo, row_hi, max_edge, opt.near_eta, gh, grid_scratch);
     const double *lo = gh.lo, cell = gh.cell;
     const int *dim = gh.dim;
     const size_t ncell = gh.start.size() - 1;
@@ -369,7 +376,8 @@ void bem_solver_s::ensure_near_list(cudaStream_t st) {
                   d_grid_elems.as<int>()};
     d_near_ptr.ensure(sizeof(int) * ((size_t)R + 1));
     launch_near_list(row_points(), N, geo_tables(), grid, nullptr, d_near_ptr.as<int>(), nullptr, st);
-    std::vector<int> cnt(R);
+    std::vector<int> &cnt = near_cnt_h;
+    cnt.resize(R);
     CUDA_TRY(cudaMemcpyAsync(cnt.data(), d_near_ptr.p, sizeof(int) * R, cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaStreamSynchronize(st));
     std::vector<int> &ptr = near_ptr_h;
@@ -393,9 +401,8 @@ void bem_solver_s::ensure_near_list(cudaStream_t st) {
 // Grid of element centroids: cell edge >= the largest near radius (near_eta
 // x element diameter) and >= the longest element (vertex pairs), over the box
 // of all row points; at most ~4M cells.
-bem::NearGridHost bem::build_near_grid(int E, const std::vector<double> &h_nodes, const std::vector<int> &h_elems,
-                                       const double *lo, const double *hi, double max_edge, double eta) {
-    NearGridHost g;
+void bem::build_near_grid(int E, const std::vector<double> &h_nodes, const std::vector<int> &h_elems, const double *lo,
+                          const double *hi, double max_edge, double eta, NearGridHost &g, HostScratch &scr) {
     g.eta = eta;
     double cell = std::max(1.0, eta) * max_edge * 1.01 + 1e-12;
     const double span = std::max({hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2], 1e-12});
@@ -406,32 +413,36 @@ bem::NearGridHost bem::build_near_grid(int E, const std::vector<double> &h_nodes
         g.dim[a] = std::max(1, (int)std::floor((hi[a] - lo[a]) / cell) + 1);
     }
     const size_t ncell = (size_t)g.dim[0] * g.dim[1] * g.dim[2];
-    std::vector<int> cid(E);
+    std::vector<int> &cid = scr.cid, &fill = scr.fill;
+    cid.resize(E);
     g.start.assign(ncell + 1, 0);
     g.order.resize(E);
+    // (the cell size has a 1% margin over the near radius, so binning by a
+    // reciprocal instead of a division moves nothing out of a row's 27 cells)
+    const double inv = 1.0 / cell, third = 1.0 / 3.0;
     for (int e = 0; e < E; e++) {
         int c[3];
+        const double *p0 = &h_nodes[3 * (size_t)h_elems[3 * e]], *p1 = &h_nodes[3 * (size_t)h_elems[3 * e + 1]],
+                     *p2 = &h_nodes[3 * (size_t)h_elems[3 * e + 2]];
         for (int a = 0; a < 3; a++) {
-            const double m = (h_nodes[3 * (size_t)h_elems[3 * e] + a] + h_nodes[3 * (size_t)h_elems[3 * e + 1] + a] +
-                              h_nodes[3 * (size_t)h_elems[3 * e + 2] + a]) / 3.0;
-            c[a] = std::min(std::max((int)std::floor((m - lo[a]) / cell), 0), g.dim[a] - 1);
+            const double m = (p0[a] + p1[a] + p2[a]) * third;
+            c[a] = std::min(std::max((int)std::floor((m - lo[a]) * inv), 0), g.dim[a] - 1);
         }
         cid[e] = (int)(((size_t)c[2] * g.dim[1] + c[1]) * g.dim[0] + c[0]);
         g.start[cid[e] + 1]++;
     }
     for (size_t c = 0; c < ncell; c++) g.start[c + 1] += g.start[c];
-    std::vector<int> fill(g.start.begin(), g.start.end() - 1);
+    fill.assign(g.start.begin(), g.start.end() - 1);
     for (int e = 0; e < E; e++) g.order[fill[cid[e]]++] = e;   // increasing e within a cell
-    return g;
 }
 
-bem::HostTiles bem::build_host_tiles(int N, int E, const std::vector<double> &h_nodes,
-                                     const std::vector<int> &h_elems, int cap) {
-    HostTiles out;
+void bem::build_host_tiles(int N, int E, const std::vector<double> &h_nodes, const std::vector<int> &h_elems,
+                           int cap, HostTiles &out, HostScratch &scr) {
     out.cap = cap;
     int ntiles = (N + cap - 1) / cap;
     int per = (N + ntiles - 1) / ntiles;
-    std::vector<int> order(N);
+    std::vector<int> &order = scr.order;
+    order.resize(N);
     std::iota(order.begin(), order.end(), 0);
     if (ntiles > 1) {
         double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300}, inv[3];
@@ -441,11 +452,14 @@ bem::HostTiles bem::build_host_tiles(int N, int E, const std::vector<double> &h_
                 hi[d] = std::max(hi[d], h_nodes[3 * i + d]);
             }
         for (int d = 0; d < 3; d++) inv[d] = hi[d] > lo[d] ? 1023.0 / (hi[d] - lo[d]) : 0.0;
-        std::vector<uint32_t> key(N);
+        std::vector<uint32_t> &key = scr.key;
+        key.resize(N);
         for (int i = 0; i < N; i++) key[i] = morton_key(&h_nodes[3 * i], lo, inv);
         std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return key[a] < key[b]; });
     }
-    std::vector<int> tile_of(N), slot_of(N);
+    std::vector<int> &tile_of = scr.tile_of, &slot_of = scr.slot_of;
+    tile_of.resize(N);
+    slot_of.resize(N);
     std::vector<int> &cols = out.cols, &cnt = out.cnt;
     cols.assign((size_t)ntiles * per, 0);
     cnt.assign(ntiles, 0);
@@ -456,7 +470,9 @@ bem::HostTiles bem::build_host_tiles(int N, int E, const std::vector<double> &h_
         cols[(size_t)t * per + s] = order[i];
         cnt[t]++;
     }
-    std::vector<std::vector<TileRec>> lists(ntiles);
+    std::vector<std::vector<TileRec>> &lists = scr.lists;
+    if ((int)lists.size() < ntiles) lists.resize(ntiles);
+    for (int t = 0; t < ntiles; t++) lists[t].clear();
     if (ntiles == 1) lists[0].reserve(E);
     for (int e = 0; e < E; e++) {
         const int *nd = &h_elems[3 * (size_t)e];
@@ -479,18 +495,18 @@ bem::HostTiles bem::build_host_tiles(int N, int E, const std::vector<double> &h_
     }
     std::vector<TileRec> &recs = out.recs;
     std::vector<int> &ptr = out.ptr;
+    recs.clear();
     ptr.assign(ntiles + 1, 0);
     out.bptr.assign(1, 0);
     out.tbatch.assign(ntiles + 1, 0);
     recs.reserve(lists[0].size() * ntiles);
     for (int t = 0; t < ntiles; t++) {
-        pack_batches(lists[t], per, recs, out.bptr);
+        pack_batches(lists[t], per, recs, out.bptr, scr);
         ptr[t + 1] = (int)recs.size();
         out.tbatch[t + 1] = (int)out.bptr.size() - 1;
     }
     out.ntiles = ntiles;
     out.per = per;
-    return out;
 }
 
 void bem_solver_s::ensure_tiles(int precision) {
@@ -499,17 +515,13 @@ void bem_solver_s::ensure_tiles(int precision) {
     BEM_HOST_PROF("tiles");
     const int cap = opt.tile_cols > 0 ? std::min(opt.tile_cols, kTileColsMax) : kTileColsMax;
     // the host tables, built beside set_geometry when the column cap matches
-    HostTiles ht;
-    bool have = false;
     if (tile_future.valid()) {
-        ht = tile_future.get();
-        have = ht.cap == cap;
-    } else if (host_tiles.cap == cap && !host_tiles.ptr.empty()) {
-        ht = host_tiles;
-        have = true;
+        tile_future.get();
+        std::swap(host_tiles, tiles_next);
     }
-    if (!have) ht = build_host_tiles(N, E, h_nodes, h_elems, cap);
-    host_tiles = ht;
+    if (host_tiles.cap != cap || host_tiles.ptr.empty())
+        build_host_tiles(N, E, h_nodes, h_elems, cap, host_tiles, tile_scratch);
+    const HostTiles &ht = host_tiles;
     const std::vector<TileRec> &recs = ht.recs;
     const std::vector<int> &ptr = ht.ptr, &cols = ht.cols, &cnt = ht.cnt;
     const int ntiles = ht.ntiles, per = ht.per;

@@ -56,10 +56,21 @@ struct NearGridHost {
     int dim[3] = {0, 0, 0};
     std::vector<int> start, order;   // ncell + 1 cell offsets, E element ids
 };
-NearGridHost build_near_grid(int E, const std::vector<double> &h_nodes, const std::vector<int> &h_elems,
-                             const double *lo, const double *hi, double max_edge, double eta);
-HostTiles build_host_tiles(int N, int E, const std::vector<double> &h_nodes, const std::vector<int> &h_elems,
-                           int cap);
+// Host scratch of the table builders, kept by the solver across geometries:
+// the vectors keep their capacity, so a new geometry of the same size writes
+// into pages already mapped instead of faulting in fresh allocations (which
+// cost more than the builders' arithmetic at 20480 elements).
+struct HostScratch {
+    std::vector<int> order, tile_of, slot_of, size, batch_of, start, cid, fill;
+    std::vector<uint32_t> key;
+    std::vector<uint64_t> used, level, busy;
+    std::vector<std::vector<TileRec>> lists;
+};
+// Both fill `out`, reusing its vectors' storage.
+void build_near_grid(int E, const std::vector<double> &h_nodes, const std::vector<int> &h_elems, const double *lo,
+                     const double *hi, double max_edge, double eta, NearGridHost &out, HostScratch &scr);
+void build_host_tiles(int N, int E, const std::vector<double> &h_nodes, const std::vector<int> &h_elems, int cap,
+                      HostTiles &out, HostScratch &scr);
 // Block-solve GEMM mode chosen by timing for (device, R, N, S), shared by
 // every handle of the process: -1 while none is stored.
 int block_mode_cached(int device, int R, int N, int S);
@@ -145,16 +156,16 @@ struct bem_solver_s {
     // field workspace
     bem::DevMem f_rows_f, f_rows_d, f_part, f_near, f_out, f_u;
 
-    // column-tile host tables: being built beside set_geometry (tile_future),
-    // or the last ones built; declared after h_nodes/h_elems, so the future
-    // (whose destructor waits for its task) goes first
-    bem::HostTiles host_tiles;
-    std::future<bem::HostTiles> tile_future;
-    // the near-pair grid's host part, built beside set_geometry too; the last
-    // one used and the row offsets stay here while their uploads are in flight
-    std::future<bem::NearGridHost> grid_future;
-    bem::NearGridHost near_grid_h;
-    std::vector<int> near_ptr_h;
+    // column-tile host tables: the ones in use (host_tiles) and the ones being
+    // built beside set_geometry (tiles_next, by tile_future's task), swapped
+    // when ensure_tiles takes them; likewise the near-pair grid's host part.
+    // The futures are declared after everything their tasks touch, so they
+    // are destroyed (their destructors wait for the tasks) first.
+    bem::HostTiles host_tiles, tiles_next;
+    bem::NearGridHost near_grid_h, grid_next;
+    bem::HostScratch tile_scratch, grid_scratch;
+    std::vector<int> near_ptr_h, near_cnt_h;
+    std::future<void> tile_future, grid_future;
 
     bem_solver_s();
     ~bem_solver_s();
