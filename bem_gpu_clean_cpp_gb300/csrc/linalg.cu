@@ -215,6 +215,7 @@ gemv_h_part_kernel(int R, int N, const float2 *__restrict__ A, size_t lda, const
     const int r0 = split * per, r1 = min(R, r0 + per);
     float s0r = 0, s0i = 0, s1r = 0, s1i = 0;
     if (c + 1 < N) {
+#pragma unroll 8   // eight rows' loads in flight per thread
         for (int r = r0; r < r1; r++) {
             float4 v = __ldcs(reinterpret_cast<const float4 *>(A + (size_t)r * lda + c));
             if (!CONJ) { v.y = -v.y; v.w = -v.w; }
