@@ -1358,8 +1358,19 @@ __device__ __forceinline__ void ksum(float &s, float &c, float t) {
     s = u;
 }
 
+// Outputs of the FP32 near integration: the dG/dn parts of the three A
+// coefficients in FP32 (the c64 entries they are added to are FP32), the G
+// sums (for beta and bcA terms) and the free-term sum in FP64.
+struct NearOutF {
+    float hr[3], hi[3];
+    double gr[3], gi[3], c;
+};
+
+// GM as in far_sums_f32_o6x2: the G sums are formed only when some BC needs
+// them (GM > 0); the FP64 work left per pair is the geometry and the c sum.
+template <int GM>
 __device__ void near_integrate_f32(const double *h, const double *x, double k, int collapse, bool sing,
-                                   const Leaf *leaves, int nl, int nq, float *lg, NearOut &o) {
+                                   const Leaf *leaves, int nl, int nq, float *lg, NearOutF &o) {
     const int lane = threadIdx.x & 31;
     const double *n = h + 9;
     const double d3[3] = {h[0] - x[0], h[1] - x[1], h[2] - x[2]};
@@ -1425,38 +1436,49 @@ __device__ void near_integrate_f32(const double *h, const double *x, double k, i
         const float wn[3] = {w * x1, w * x2, w * (1.0f - x1 - x2)};
 #pragma unroll
         for (int j = 0; j < 3; j++) {
-            ksum(s[j], c[j], wn[j] * gr);
-            ksum(s[3 + j], c[3 + j], wn[j] * gs);
+            if constexpr (GM == 2) {
+                ksum(s[j], c[j], wn[j] * gr);
+                ksum(s[3 + j], c[3 + j], wn[j] * gs);
+            }
             ksum(s[6 + j], c[6 + j], wn[j] * ha);
             ksum(s[9 + j], c[9 + j], wn[j] * hb);
+        }
+        if constexpr (GM == 1) {   // beta needs sum_j g_j only: the weights' sum is w
+            ksum(s[0], c[0], w * gr);
+            ksum(s[3], c[3], w * gs);
         }
         ksum(s[12], c[12], w * ri3);
     }
     // lanes' (sum, compensation) pairs added by TwoSum across the warp, in FP32
-    double acc[13];
 #pragma unroll
-    for (int i = 0; i < 13; i++) {
+    for (int i = GM > 0 ? 0 : 6; i < 13; i++) {
+        if (GM == 1 && (i == 1 || i == 2 || i == 4 || i == 5)) continue;
         float hi = s[i], lo = c[i];
         for (int off = 16; off > 0; off >>= 1) {
             const float h2 = __shfl_xor_sync(0xffffffffu, hi, off), l2 = __shfl_xor_sync(0xffffffffu, lo, off);
             ksum(hi, lo, h2);
             lo = __fadd_rn(lo, l2);
         }
-        acc[i] = (double)hi + (double)lo;
+        s[i] = hi;
+        c[i] = lo;
     }
-    // signs and the height: G = (gr, -gs), dG/dn = -hgt (ha, hb), dG0/dn = -hgt ri3
-#pragma unroll
-    for (int j = 0; j < 3; j++) acc[3 + j] = -acc[3 + j];
-#pragma unroll
-    for (int i = 6; i < 13; i++) acc[i] *= -hgt;
+    // signs, height and scale: G = (gr, -gs), dG/dn = -hgt (ha, hb), dG0/dn =
+    // -hgt ri3; the dG/dn coefficients in FP32 from the head and tail
     const double scale = h[12] * (1.0 / (4.0 * kPi));   // a constant reciprocal: no FP64 division
+    const double sh = -hgt * scale;
+    const float fsh = (float)sh;
+#pragma unroll
     for (int j = 0; j < 3; j++) {
-        o.gr[j] = scale * acc[j];
-        o.gi[j] = scale * acc[3 + j];
-        o.hr[j] = scale * acc[6 + j];
-        o.hi[j] = scale * acc[9 + j];
+        o.hr[j] = fmaf(fsh, s[6 + j], fsh * c[6 + j]);
+        o.hi[j] = fmaf(fsh, s[9 + j], fsh * c[9 + j]);
+        if (GM == 2 || (GM == 1 && j == 0)) {   // GM = 1: the sum over j in entry 0
+            o.gr[j] = scale * ((double)s[j] + (double)c[j]);
+            o.gi[j] = -scale * ((double)s[3 + j] + (double)c[3 + j]);
+        } else {
+            o.gr[j] = o.gi[j] = 0.0;
+        }
     }
-    o.c = scale * acc[12];
+    o.c = sh * ((double)s[12] + (double)c[12]);
 }
 
 __device__ __forceinline__ double2 incident_field(const DevSource &s, double k, const double *x) {
@@ -1486,7 +1508,9 @@ template <> __device__ __forceinline__ void add_entry<double2>(double2 *p, doubl
     *p = make_double2(v.x + re, v.y + im);
 }
 
-template <typename TA, typename TP, typename TP2>
+// GM: which G sums the BCs need (as in far_sums_f32_o6x2), used by the c64
+// (TA = float2) FP32 path; the c128 kernel is instantiated with GM = 2.
+template <typename TA, typename TP, typename TP2, int GM>
 __global__ void __launch_bounds__(32 * kNearWarps)
 near_assembly_kernel(RowPoints rows, int N, GeoTables geo, Physics ph, int nq, TA *__restrict__ A,
                      size_t lda, const TP *__restrict__ c_part, const TP2 *__restrict__ beta_part,
@@ -1527,16 +1551,50 @@ near_assembly_kernel(RowPoints rows, int N, GeoTables geo, Physics ph, int nq, T
             }
             __syncwarp();
             NearOut o;
-            if (std::is_same<TA, float2>::value && nl <= kNearF32Leaves)
-                near_integrate_f32(h, x, ph.k, collapse, vtx != 0, leaves, nl, nq,
-                                   reinterpret_cast<float *>(&codes_all[warp][0][0]), o);
-            else
+            const int node[3] = {ndb.x, ndb.y, ndb.z};
+            if (std::is_same<TA, float2>::value && nl <= kNearF32Leaves) {
+                NearOutF of;
+                near_integrate_f32<GM>(h, x, ph.k, collapse, vtx != 0, leaves, nl, nq,
+                                       reinterpret_cast<float *>(&codes_all[warp][0][0]), of);
+                __syncwarp();
+                if constexpr (GM < 2 && std::is_same<TA, float2>::value) {
+                    // bcA = 0: the coefficients are the dG/dn parts, added in
+                    // FP32 to the FP32 entries (one rounding, as the FP64 add
+                    // and conversion gave)
+                    if (lane == 0) {
+                        double sgr = 0, sgi = 0;
+                        for (int j = 0; j < 3; j++) {
+                            float2 *p = A + (size_t)row * lda + node[j];
+                            const float2 v = *p;
+                            *p = make_float2(__fadd_rn(v.x, of.hr[j]), __fadd_rn(v.y, of.hi[j]));
+                            if constexpr (GM == 1) {
+                                sgr -= ph.rw * of.gi[j];
+                                sgi += ph.rw * of.gr[j];
+                            }
+                        }
+                        if (row < N) cn += of.c;
+                        if constexpr (GM == 1) {
+                            const double bCr = h[15], bCi = h[16];
+                            bnr += bCr * sgr - bCi * sgi;
+                            bni += bCr * sgi + bCi * sgr;
+                        }
+                    }
+                    continue;
+                }
+                for (int j = 0; j < 3; j++) {
+                    o.hr[j] = of.hr[j];
+                    o.hi[j] = of.hi[j];
+                    o.gr[j] = of.gr[j];
+                    o.gi[j] = of.gi[j];
+                }
+                o.c = of.c;
+            } else {
                 near_integrate(h, x, ph.k, collapse, leaves, nl, nq, o);
-            __syncwarp();
+                __syncwarp();
+            }
             if (lane == 0) {
                 const double bAr = h[13], bAi = h[14], bCr = h[15], bCi = h[16];
                 double sgr = 0, sgi = 0;
-                const int node[3] = {ndb.x, ndb.y, ndb.z};
                 for (int j = 0; j < 3; j++) {
                     double g_r = -ph.rw * o.gi[j], g_i = ph.rw * o.gr[j];
                     double a_r = o.hr[j] - (bAr * g_r - bAi * g_i);
@@ -1663,11 +1721,14 @@ void launch_near_assembly(int prec, const RowPoints &rows, int N, const GeoTable
     int nq = quadrature_points();
     dim3 grid((rows.R + kNearWarps - 1) / kNearWarps);
     if (prec == BEM_PREC_C64) {
-        near_assembly_kernel<float2, float, float2><<<grid, 32 * kNearWarps, 0, st>>>(
-            rows, N, geo, ph, nq, (float2 *)A, lda, (const float *)c_part,
-            (const float2 *)beta_part, ntiles, srcs, S, B, beta_out, near_ptr, near_ids);
+        auto kern = ph.g_sums == 0   ? near_assembly_kernel<float2, float, float2, 0>
+                    : ph.g_sums == 1 ? near_assembly_kernel<float2, float, float2, 1>
+                                     : near_assembly_kernel<float2, float, float2, 2>;
+        kern<<<grid, 32 * kNearWarps, 0, st>>>(rows, N, geo, ph, nq, (float2 *)A, lda, (const float *)c_part,
+                                                (const float2 *)beta_part, ntiles, srcs, S, B, beta_out, near_ptr,
+                                                near_ids);
     } else {
-        near_assembly_kernel<double2, double, double2><<<grid, 32 * kNearWarps, 0, st>>>(
+        near_assembly_kernel<double2, double, double2, 2><<<grid, 32 * kNearWarps, 0, st>>>(
             rows, N, geo, ph, nq, (double2 *)A, lda, (const double *)c_part,
             (const double2 *)beta_part, ntiles, srcs, S, B, beta_out, near_ptr, near_ids);
     }
