@@ -142,8 +142,11 @@ void bem_solver_s::solve_refined(bem_solve_info_t *info) {
             launch_gemv_h_f64(prec, R, n, A, lda, b, w_gv.as<double2>(), w_part.as<double2>(), w_vf.as<float2>(),
                               stream);
         launch_nrm2(n, w_gv.as<double2>(), scal + 0, w_part.as<double>(), stream);
-        const double bn = read_scalar(0);
-        if (!(bn > 0.0)) continue;
+        // |A^H b| reaches the host with the first inner step's result (no wait
+        // of its own); a zero right-hand side is recognised there
+        CUDA_TRY(cudaMemcpyAsync(h_pinned + 0, scal + 0, sizeof(double), cudaMemcpyDeviceToHost, stream));
+        double bn = -1.0;
+        bool zero_rhs = false;
         double rel = 1.0;
         bool conv = false;
         int ref = 0;
@@ -159,7 +162,7 @@ void bem_solver_s::solve_refined(bem_solve_info_t *info) {
             } else {
                 CUDA_TRY(cudaMemcpyAsync(scal + 1, scal + 0, sizeof(double), cudaMemcpyDeviceToDevice, stream));
             }
-            rel = gn / bn;
+            rel = ref > 0 ? gn / bn : 1.0;
             if (!std::isfinite(rel)) {
                 // a normal-operator launch that gave up on a copy explains it
                 if (normal_op_timed_out(op_status, stream))
@@ -224,16 +227,29 @@ void bem_solver_s::solve_refined(bem_solve_info_t *info) {
                 const bool ahead = j + 1 < m && prev > kSpeculate * opt.inner_tol;
                 if (ahead) launch_step(j + 1);
                 CUDA_TRY(cudaEventSynchronize(ev_res[j & 1]));
+                if (bn < 0.0) {   // the first step of the first inner solve
+                    bn = gn = h_pinned[0];
+                    if (!(bn > 0.0)) {
+                        zero_rhs = true;   // x stays zero
+                        break;
+                    }
+                }
                 const double res = h_pinned[4 + (j & 1)];
                 jdone = j + 1;
                 if (!(res / gn > opt.inner_tol)) break;
                 prev = res / gn;
                 if (!ahead && j + 1 < m) launch_step(j + 1);
             }
+            if (zero_rhs) break;
             launch_trisolve(jdone, w_H.as<double2>(), ldh, w_g.as<double2>(), w_y.as<double2>(), stream);
             launch_axpy_combo(n, jdone, V, n, w_y.as<double2>(), x, stream);
             total_it += jdone;
         }
+        if (bn < 0.0) {   // no inner step ran (max_refine = 0): read |A^H b| now
+            bn = read_scalar(0);
+            zero_rhs = !(bn > 0.0);
+        }
+        if (zero_rhs) continue;
         max_ref = std::max(max_ref, ref);
         worst = std::max(worst, rel);
         all_conv &= conv ? 1 : 0;

@@ -24,6 +24,34 @@ def _rigid_ico(subdiv, n_chief, seed=1):
     return p, f, chief, bc
 
 
+def test_refined_solve_zero_rhs(bemlib):
+    """A source of zero strength next to a real one: its surface pressure
+    is zero (|A^H b| = 0 is recognised with the first inner step's result),
+    the other one converges as alone; with no refinement allowed the
+    solution stays zero and is reported unconverged."""
+    p, f, chief, bc = _rigid_ico(2, 4)
+    srcs = [("point", (2.0, 1.0, 0.5), 0.0), ("plane", (0, 0, 1), 1.0)]
+    s = bemlib.Solver()
+    s.set_geometry(p, f, bc=bc, chief=chief)
+    s.set_sources(srcs)
+    s.assemble(1.3, bemlib.PREC_C64)
+    info = s.solve(bemlib.SOLVE_GMRES_REFINED)
+    x = s.solution()
+    assert info.converged and np.all(x[:, 0] == 0) and np.all(np.isfinite(x))
+    alone = bemlib.Solver()
+    alone.set_geometry(p, f, bc=bc, chief=chief)
+    alone.set_sources(srcs[1:])
+    alone.assemble(1.3, bemlib.PREC_C64)
+    alone.solve(bemlib.SOLVE_GMRES_REFINED)
+    assert rel_err(x[:, 1], alone.solution()[:, 0]) < 1e-10
+    none = bemlib.Solver(max_refine=0)
+    none.set_geometry(p, f, bc=bc, chief=chief)
+    none.set_sources(srcs[1:])
+    none.assemble(1.3, bemlib.PREC_C64)
+    info0 = none.solve(bemlib.SOLVE_GMRES_REFINED, check=False)   # BEM_ERR_NOT_CONVERGED, reported in info
+    assert not info0.converged and np.all(none.solution() == 0)
+
+
 def test_qr_c128_matches_oracle(bemlib, orc):
     p, f, chief, bc = _rigid_ico(2, 4)
     srcs = [("plane", (0, 0, 1), 1.0), ("point", (2, 1, 0), 1.0)]
