@@ -185,6 +185,23 @@ bem_solver_s::~bem_solver_s() {
     if (cur >= 0 && cur != device) cudaSetDevice(cur);
 }
 
+namespace {
+// The longest element edge: the largest squared length, one square root.
+double longest_edge(int E, const std::vector<double> &h_nodes, const std::vector<int> &h_elems) {
+    double m2 = 0.0;
+    for (int e = 0; e < E; e++) {
+        const double *v[3] = {&h_nodes[3 * (size_t)h_elems[3 * e]], &h_nodes[3 * (size_t)h_elems[3 * e + 1]],
+                              &h_nodes[3 * (size_t)h_elems[3 * e + 2]]};
+        for (int a = 0; a < 3; a++) {
+            const double *p = v[a], *q = v[a == 2 ? 0 : a + 1];
+            m2 = std::max(m2, (p[0] - q[0]) * (p[0] - q[0]) + (p[1] - q[1]) * (p[1] - q[1]) +
+                                  (p[2] - q[2]) * (p[2] - q[2]));
+        }
+    }
+    return std::sqrt(m2);
+}
+}  // namespace
+
 void bem_solver_s::set_geometry(const double *pnts, int num_pnts, const int *elems, int num_elems,
                                 const double *bc, const double *chief, int num_chief) {
     BEM_HOST_PROF("set_geometry");
@@ -239,18 +256,6 @@ void bem_solver_s::set_geometry(const double *pnts, int num_pnts, const int *ele
                                  cudaMemcpyHostToDevice, stream));
     CUDA_TRY(cudaMemcpyAsync(d_bc.p, bc ? bc : h_bc.data(), sizeof(double) * 6 * (size_t)E, cudaMemcpyHostToDevice,
                              stream));
-    // the longest edge: the largest squared length, one square root
-    double max_edge2 = 0.0;
-    for (int e = 0; e < E; e++) {
-        const double *v[3] = {&h_nodes[3 * (size_t)h_elems[3 * e]], &h_nodes[3 * (size_t)h_elems[3 * e + 1]],
-                              &h_nodes[3 * (size_t)h_elems[3 * e + 2]]};
-        for (int a = 0; a < 3; a++) {
-            const double *p = v[a], *q = v[a == 2 ? 0 : a + 1];
-            max_edge2 = std::max(max_edge2, (p[0] - q[0]) * (p[0] - q[0]) + (p[1] - q[1]) * (p[1] - q[1]) +
-                                                (p[2] - q[2]) * (p[2] - q[2]));
-        }
-    }
-    max_edge = std::sqrt(max_edge2);
     // alpha = 0 on every element (bcA = 0: the far kernel forms no G sums
     // for A), and gamma = 0 too (bcC = 0: none for beta either)
     {
@@ -278,10 +283,12 @@ void bem_solver_s::set_geometry(const double *pnts, int num_pnts, const int *ele
         extent = std::sqrt((hi[0] - lo[0]) * (hi[0] - lo[0]) + (hi[1] - lo[1]) * (hi[1] - lo[1]) +
                            (hi[2] - lo[2]) * (hi[2] - lo[2]));
     }
-    // the near-pair grid's host part on another host thread (ensure_near_list
-    // takes it when near_eta is still the one it was built for)
+    // the longest edge and the near-pair grid's host part on another host
+    // thread (physics() waits for the edge; ensure_near_list takes the grid
+    // when near_eta is still the one it was built for)
     grid_next.eta = -1.0;
     grid_future = std::async(std::launch::async, [this, eta = opt.near_eta] {
+        max_edge = longest_edge(E, h_nodes, h_elems);
         build_near_grid(E, h_nodes, h_elems, row_lo, row_hi, max_edge, eta, grid_next, grid_scratch);
     });
 
@@ -553,6 +560,7 @@ GeoTables bem_solver_s::geo_tables() const {
 RowPoints bem_solver_s::row_points() const { return RowPoints{d_rows_f.as<float4>(), d_rows_d.as<double>(), R}; }
 
 Physics bem_solver_s::physics() const {
+    if (grid_future.valid()) grid_future.wait();   // max_edge is formed by set_geometry's grid task
     return Physics{k, opt.density * k * opt.speed, opt.near_depth, opt.near_eta, max_edge, extent, g_sums};
 }
 

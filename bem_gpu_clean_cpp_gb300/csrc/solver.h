@@ -95,7 +95,7 @@ struct bem_solver_s {
     // near pairs per row (CSR), valid for the current geometry and geo_eta
     bool near_valid = false;
     bem::DevMem d_near_ptr, d_near_ids, d_grid_start, d_grid_elems;
-    double max_edge = 0.0;   // longest element edge
+    double max_edge = 0.0;   // longest element edge (written by set_geometry's grid task: read through physics())
     double extent = 0.0;     // diagonal of the box around nodes and CHIEF points
     double row_lo[3] = {0.0, 0.0, 0.0}, row_hi[3] = {0.0, 0.0, 0.0};   // that box
     int g_sums = 2;   // Physics::g_sums of the BCs: 2 some alpha != 0, 1 alpha = 0 everywhere, 0 gamma = 0 too
