@@ -60,19 +60,60 @@ uint32_t morton_key(const double *p, const double *lo, const double *inv) {
 // batches come out equal (icosphere subdivision 5: 20 batches of 1024; small
 // meshes: at least 13).  Appends the records batch by batch to `out` and the
 // batch boundaries (offsets into `out`) to `bptr`.
-void pack_batches(const std::vector<TileRec> &list, int tile_cols, std::vector<TileRec> &out,
-                  std::vector<int> &bptr, HostScratch &scr) {
-    // Bit sets, 64 batches per word: per slot, the batches already holding a
-    // record on it (`used`); per fill level s, the batches holding s records
-    // (`level`).  A record's allowed batches are the complement of its slots'
-    // union; the occupied levels are scanned upward from the lowest, so
-    // the first allowed batch found is the least-filled (lowest index among
-    // equals) with room, and the fills stay within a few levels of each
-    // other: a handful of word operations per record.
-    const int nb0 = (int)((list.size() + kFarBatch - 1) / kFarBatch);
-    int words = std::max(1, (nb0 + 8 + 63) / 64);
+// The assignment loop of pack_batches with every batch in one word (up to
+// 64 batches: the bit sets are single words, no inner loops over words); the
+// same choices as the general loop.  False when a 65th batch would be needed.
+bool assign_batches_1w(const std::vector<TileRec> &list, int tile_cols, int nb0, HostScratch &scr) {
+    if (nb0 > 64) return false;
+    std::vector<uint64_t> &used = scr.used, &level = scr.level;
+    std::vector<int> &size = scr.size, &batch_of = scr.batch_of;
+    used.assign(tile_cols, 0);
+    level.assign(kFarBatch + 1, 0);
+    size.assign(nb0, 0);
+    batch_of.resize(list.size());
+    uint64_t *U = used.data(), *L = level.data();
+    L[0] = nb0 == 64 ? ~0ull : (1ull << nb0) - 1;
+    int low = 0, high = 0, nb = nb0;
+    for (size_t r = 0; r < list.size(); r++) {
+        const TileRec &rec = list[r];
+        uint64_t busy = 0;
+        for (int j = 0; j < 3; j++)
+            if (rec.slot[j] >= 0) busy |= U[rec.slot[j]];
+        int best = -1;
+        const int top = std::min(high, kFarBatch - 1);
+        for (int s = low; s <= top; s++) {
+            const uint64_t m = L[s] & ~busy;
+            if (m) {
+                best = __builtin_ctzll(m);
+                break;
+            }
+        }
+        if (best < 0) {
+            best = nb++;
+            if (best >= 64) return false;
+            size.push_back(0);
+            L[0] |= 1ull << best;
+            low = 0;
+        }
+        const int s = size[best]++;
+        high = std::max(high, s + 1);
+        const uint64_t bit = 1ull << best;
+        L[s] &= ~bit;
+        L[s + 1] |= bit;
+        while (low < kFarBatch && L[low] == 0) low++;
+        batch_of[r] = best;
+        for (int j = 0; j < 3; j++)
+            if (rec.slot[j] >= 0) U[rec.slot[j]] |= bit;
+    }
+    return true;
+}
+
+// The general assignment loop (any number of batches; the bit sets widen
+// as batches are added).
+void general_assign(const std::vector<TileRec> &list, int tile_cols, int nb0, HostScratch &scr) {
     std::vector<uint64_t> &used = scr.used, &level = scr.level, &busy = scr.busy;
     std::vector<int> &size = scr.size, &batch_of = scr.batch_of;
+    int words = std::max(1, (nb0 + 8 + 63) / 64);
     used.assign((size_t)tile_cols * words, 0);
     level.assign((size_t)(kFarBatch + 1) * words, 0);
     size.assign(nb0, 0);
@@ -131,6 +172,20 @@ void pack_batches(const std::vector<TileRec> &list, int tile_cols, std::vector<T
         for (int j = 0; j < 3; j++)
             if (rec.slot[j] >= 0) used[(size_t)rec.slot[j] * words + best / 64] |= bit;
     }
+}
+
+void pack_batches(const std::vector<TileRec> &list, int tile_cols, std::vector<TileRec> &out,
+                  std::vector<int> &bptr, HostScratch &scr) {
+    // Bit sets, 64 batches per word: per slot, the batches already holding a
+    // record on it (`used`); per fill level s, the batches holding s records
+    // (`level`).  A record's allowed batches are the complement of its slots'
+    // union; the occupied levels are scanned upward from the lowest, so
+    // the first allowed batch found is the least-filled (lowest index among
+    // equals) with room, and the fills stay within a few levels of each
+    // other: a handful of word operations per record.
+    const int nb0 = (int)((list.size() + kFarBatch - 1) / kFarBatch);
+    if (!assign_batches_1w(list, tile_cols, nb0, scr)) general_assign(list, tile_cols, nb0, scr);
+    const std::vector<int> &size = scr.size, &batch_of = scr.batch_of;
     // stable counting sort of the records by batch
     std::vector<int> &start = scr.start;
     start.assign(size.size() + 1, 0);
