@@ -146,6 +146,8 @@ void launch_field(int prec, const RowPoints &pts, const GeoTables &geo, const Ph
 // are c64 or c128 (xd/yd flags: 1 means c128).
 void launch_gemv_c64(int R, int N, const float2 *A, size_t lda, const void *x, int xd, void *y,
                      int yd, cudaStream_t st);
+// y = x rounded to c64 (n entries)
+void launch_to_c64(int n, const double2 *x, float2 *y, cudaStream_t st);
 // w = A^H u (N), two-pass column-block reduction through `part`
 // (nsplit x N c64 or c128).
 int gemv_h_splits(int R, int N);

@@ -108,6 +108,11 @@ __global__ void split_f64_kernel(int n, const double2 *__restrict__ x, float2 *_
     xl[i] = make_float2((float)(v.x - (double)hr), (float)(v.y - (double)hi));
 }
 
+__global__ void to_c64_kernel(int n, const double2 *__restrict__ x, float2 *__restrict__ y) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = make_float2((float)x[i].x, (float)x[i].y);
+}
+
 // r = b - A x for c64 A, FP64-accurate (x given as head/tail floats).
 __global__ void __launch_bounds__(32 * kMvWPC)
 resid_df_kernel(int R, int N, const float2 *__restrict__ A, size_t lda, const float2 *__restrict__ xh,
@@ -1091,6 +1096,13 @@ int gemv_h_splits(int R, int N) {
     const int sms = device_sm_count();
     int want = (8 * sms + cb - 1) / cb;
     return std::max(1, std::min(want, std::max(1, R / 32)));
+}
+
+void launch_to_c64(int n, const double2 *x, float2 *y, cudaStream_t st) {
+    if (n <= 0) return;
+    to_c64_kernel<<<blocks(n, 256), 256, 0, st>>>(n, x, y);
+    count_launch();
+    KERNEL_CHECK();
 }
 
 void launch_gemv_h_c64(int R, int N, const float2 *A, size_t lda, const void *u, int ud, void *w,

@@ -136,8 +136,11 @@ void bem_solver_s::solve_refined(bem_solve_info_t *info) {
         // tolerance far above FP32 rounding, and scales the stopping test; every
         // later A^H r is FP64-accurate, so for c64 A the single-pass FP32
         // product suffices here (the refined solution does not depend on it)
-        if (prec == BEM_PREC_C64)
-            launch_gemv_h_c64(R, n, A, lda, b, 1, w_gv.p, 1, w_part.p, stream);
+        if (prec == BEM_PREC_C64) {
+            // b rounded to c64 once (not once per row and thread inside the product)
+            launch_to_c64(R, b, w_vf.as<float2>(), stream);
+            launch_gemv_h_c64(R, n, A, lda, w_vf.p, 0, w_gv.p, 1, w_part.p, stream);
+        }
         else
             launch_gemv_h_f64(prec, R, n, A, lda, b, w_gv.as<double2>(), w_part.as<double2>(), w_vf.as<float2>(),
                               stream);
