@@ -216,6 +216,7 @@ bem_solver_s::bem_solver_s() {
     cublasSetStream(cublas, stream);
     CUDA_TRY(cudaMallocHost(&h_pinned, 64 * sizeof(double)));
     for (auto &e : ev_res) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    CUDA_TRY(cudaEventCreateWithFlags(&ev_up, cudaEventDisableTiming));
     bem_options_default(&opt);
 }
 
@@ -229,6 +230,7 @@ bem_solver_s::~bem_solver_s() {
     if (h_pinned) cudaFreeHost(h_pinned);
     for (auto &e : ev_res)
         if (e) cudaEventDestroy(e);
+    if (ev_up) cudaEventDestroy(ev_up);
     if (h_stage) cudaFreeHost(h_stage);
     if (qr_aux) cudaStreamSynchronize(qr_aux);
     for (auto &e : qr_ev)
@@ -367,10 +369,13 @@ void bem_solver_s::set_geometry(const double *pnts, int num_pnts, const int *ele
     for (int e = 0; e < E; e++) el[e] = make_int4(h_elems[3 * e], h_elems[3 * e + 1], h_elems[3 * e + 2], 0);
     CUDA_TRY(cudaMemcpyAsync(d_rows_f.p, rf, rf_bytes, cudaMemcpyHostToDevice, stream));
     CUDA_TRY(cudaMemcpyAsync(d_elems.p, el, el_bytes, cudaMemcpyHostToDevice, stream));
-    // the element tables for the current near_eta, queued behind the uploads
+    // the element tables for the current near_eta, queued behind the uploads;
+    // the call returns once the copies (not the kernel) are done: the
+    // caller's arrays and the staging buffer are free again then
+    CUDA_TRY(cudaEventRecord(ev_up, stream));
     geo_eta = -1.0;
     ensure_geo();
-    CUDA_TRY(cudaStreamSynchronize(stream));   // the caller's arrays and the staging buffer are free again
+    CUDA_TRY(cudaEventSynchronize(ev_up));
     tiles[0].valid = tiles[1].valid = false;
     assembled = solved = false;
 }
@@ -417,8 +422,8 @@ void bem_solver_s::ensure_geo() {
 void bem_solver_s::ensure_near_list(cudaStream_t st) {
     if (near_valid) return;
     BEM_HOST_PROF("near_list");
-    // (the host arrays of the uploads below stay members until the next
-    // geometry, whose set_geometry ends with a stream synchronisation)
+    // (the uploads below are from pageable host memory, which the copy
+    // stages before it returns: the arrays may be reused right after)
     NearGridHost &gh = near_grid_h;
     if (grid_future.valid()) {
         grid_future.get();

@@ -137,6 +137,7 @@ struct bem_solver_s {
     bem::DevMem d_status;
     double *h_pinned = nullptr;
     cudaEvent_t ev_res[2] = {nullptr, nullptr};   // refined GMRES: residual estimate of step j in h_pinned[4 + (j & 1)]
+    cudaEvent_t ev_up = nullptr;                  // set_geometry: its host-to-device copies have landed
     void *h_stage = nullptr;     // pinned staging for geometry uploads
     size_t h_stage_bytes = 0;
     // QR workspace
