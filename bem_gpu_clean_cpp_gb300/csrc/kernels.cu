@@ -95,16 +95,19 @@ int quadrature_points() { return g_nq_host; }
 
 // ---------------------------------------------------------------------------
 // Element tables.
-// Float table, 7 float4 per element:
+// Float table, 9 float4 per element:
 //   [0] (p3hi.xyz, J)   [1] (p3lo.xyz, near_r2)   [2] (e1, coff.x)   [3] (e2, coff.y)
-//   [4] (n, coff.z)     [5] (bcA.re, bcA.im, bcC.re, bcC.im)    [6] (centroid, 0)
-//   with coff = centroid - p3 = (e1 + e2) / 3
+//   [4] (n, coff.z)     [5] (bcA.re, bcA.im, bcC.re, bcC.im)    [6] (centroid, n tail z)
+//   [7] (e1 tail, n tail x)   [8] (e2 tail, n tail y)
+//   with coff = centroid - p3 = (e1 + e2) / 3; the tails are the remainders
+//   of e1, e2 and n after rounding to float (heads in [2]-[4])
 // p3 is split into hi + lo floats so that p3 - x keeps full float precision
 // for nearby pairs.  e1 = p1-p3, e2 = p2-p3, n = e1 x e2 / J, J = |e1 x e2|
 // (mesh.cu:612-617), near_r2 = (eta * longest edge)^2.
 // Double table, 18 doubles: p3[3] e1[3] e2[3] n[3] J bcA[2] bcC[2] diam.
 // ---------------------------------------------------------------------------
-constexpr int kGeoF = 7;
+constexpr int kGeoF = 9;
+constexpr int kFarRecG = 7;   // the leading float4 of an element's entry that a far record carries
 constexpr int kGeoD = 18;
 
 __global__ void elem_setup_kernel(const double *__restrict__ nodes, const int4 *__restrict__ elems,
@@ -148,7 +151,18 @@ __global__ void elem_setup_kernel(const double *__restrict__ nodes, const int4 *
     g[3] = make_float4((float)e2[0], (float)e2[1], (float)e2[2], (float)((e1[1] + e2[1]) / 3.0));
     g[4] = make_float4((float)n[0], (float)n[1], (float)n[2], (float)((e1[2] + e2[2]) / 3.0));
     g[5] = make_float4((float)aR, (float)aI, (float)cR, (float)cI);
-    g[6] = make_float4((float)cen[0], (float)cen[1], (float)cen[2], 0.0f);
+    // tails of e1, e2 and n (the FP32 near path forms its pair geometry in
+    // double float from heads and tails): g[7] = (e1 tail, n tail x),
+    // g[8] = (e2 tail, n tail y), g[6].w = n tail z
+    float lo[9];
+    for (int d = 0; d < 3; d++) {
+        lo[d] = (float)(e1[d] - (double)(float)e1[d]);
+        lo[3 + d] = (float)(e2[d] - (double)(float)e2[d]);
+        lo[6 + d] = (float)(n[d] - (double)(float)n[d]);
+    }
+    g[6] = make_float4((float)cen[0], (float)cen[1], (float)cen[2], lo[8]);
+    g[7] = make_float4(lo[0], lo[1], lo[2], lo[6]);
+    g[8] = make_float4(lo[3], lo[4], lo[5], lo[7]);
     double *h = gd + (size_t)kGeoD * e;
     for (int d = 0; d < 3; d++) {
         h[d] = p3[d];
@@ -1031,14 +1045,14 @@ __global__ void far_recs_kernel(const TileRec *__restrict__ recs, int nrec, cons
     const TileRec r = recs[i];
     FarRec f;
 #pragma unroll
-    for (int k = 0; k < kGeoF; k++) f.g[k] = geo_f[(size_t)kGeoF * r.eid + k];
+    for (int k = 0; k < kFarRecG; k++) f.g[k] = geo_f[(size_t)kGeoF * r.eid + k];
     f.nodes = make_int4(r.node[0], r.node[1], r.node[2], r.owner);
     f.slots = make_int4(r.slot[0], r.slot[1], r.slot[2], 0);
     out[i] = f;
 }
 
 void launch_far_recs(const TileRec *recs, int nrec, const float4 *geo_f, FarRec *frecs, cudaStream_t st) {
-    static_assert(sizeof(FarRec) == 144 && kGeoF == 7, "far record layout");
+    static_assert(sizeof(FarRec) == 16 * (kFarRecG + 2) && kGeoF >= kFarRecG, "far record layout");
     if (nrec <= 0) return;
     far_recs_kernel<<<(nrec + 255) / 256, 256, 0, st>>>(recs, nrec, geo_f, frecs);
     count_launch();
@@ -1137,9 +1151,46 @@ __device__ __forceinline__ Leaf leaf_from_code(int code, int depth) {
 // FP64) and the element's edges; outside a relative band of 1e-4 around the
 // threshold (FP32's error here is a few 1e-6) that decides, inside it the
 // FP64 test below does, so the leaves are the FP64 rule's.
+// A near pair's geometry for the FP32 path, in double float on the FP32 pipe
+// from the element table's heads and tails and the row point's head and tail
+// (no FP64 operation): d3 = p3 - x, e1, e2 as head + tail, the height of x
+// over the element (d3 . n) and |J| / (4 pi).
+struct PairGeoF {
+    float dh[3], dl[3], e1h[3], e1l[3], e2h[3], e2l[3];
+    float hgt, scale;
+};
+__device__ __forceinline__ PairGeoF pair_geo_f(const float4 *__restrict__ gf, float4 xh, float4 xl) {
+    const float4 g0 = gf[0], g1 = gf[1], g2 = gf[2], g3 = gf[3], g4 = gf[4], g6 = gf[6], g7 = gf[7], g8 = gf[8];
+    PairGeoF p;
+    const float ph[3] = {g0.x, g0.y, g0.z}, pl[3] = {g1.x, g1.y, g1.z};
+    const float xhh[3] = {xh.x, xh.y, xh.z}, xll[3] = {xl.x, xl.y, xl.z};
+    const float nh[3] = {g4.x, g4.y, g4.z}, nt[3] = {g7.w, g8.w, g6.w};
+    p.e1h[0] = g2.x; p.e1h[1] = g2.y; p.e1h[2] = g2.z;
+    p.e2h[0] = g3.x; p.e2h[1] = g3.y; p.e2h[2] = g3.z;
+    p.e1l[0] = g7.x; p.e1l[1] = g7.y; p.e1l[2] = g7.z;
+    p.e2l[0] = g8.x; p.e2l[1] = g8.y; p.e2l[2] = g8.z;
+    float hh = 0.f, hl = 0.f;
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        float e;
+        p.dh[a] = two_sum(ph[a], -xhh[a], e);
+        p.dl[a] = __fadd_rn(e, __fsub_rn(pl[a], xll[a]));
+        const float pr = __fmul_rn(p.dh[a], nh[a]), pe = __fmaf_rn(p.dh[a], nh[a], -pr);
+        float t;
+        hh = two_sum(hh, pr, t);
+        hl += t + pe + p.dh[a] * nt[a] + p.dl[a] * nh[a];
+    }
+    p.hgt = hh + hl;
+    p.scale = g0.w * (float)(1.0 / (4.0 * kPi));
+    return p;
+}
+
+// The warp's leaves of a near-singular pair.  fast32: the split tests in FP32
+// from the pair's double-float geometry (pg), with the FP64 test on h and x
+// inside a relative guard band of the threshold.
 template <bool fast32>
 __device__ int build_leaves_warp(const double *h, const double *x, double eta, int depth_max, Leaf *leaves,
-                                 int *cur, int *nxt) {
+                                 int *cur, int *nxt, const PairGeoF *pg = nullptr) {
     const int lane = threadIdx.x & 31;
     const unsigned below = (1u << lane) - 1u;
     if (lane == 0) cur[0] = 0;
@@ -1147,11 +1198,11 @@ __device__ int build_leaves_warp(const double *h, const double *x, double eta, i
     int ncur = 1, nl = 0;
     float3 d3f = make_float3(0.f, 0.f, 0.f), e1f = d3f, e2f = d3f;
     if (fast32) {
-        d3f = make_float3((float)(h[0] - x[0]), (float)(h[1] - x[1]), (float)(h[2] - x[2]));
-        e1f = make_float3((float)h[3], (float)h[4], (float)h[5]);
-        e2f = make_float3((float)h[6], (float)h[7], (float)h[8]);
+        d3f = make_float3(pg->dh[0] + pg->dl[0], pg->dh[1] + pg->dl[1], pg->dh[2] + pg->dl[2]);
+        e1f = make_float3(pg->e1h[0], pg->e1h[1], pg->e1h[2]);
+        e2f = make_float3(pg->e2h[0], pg->e2h[1], pg->e2h[2]);
     }
-    const float eta2f = (float)(eta * eta);
+    const float eta2f = fast32 ? (float)eta * (float)eta : 0.f;
     for (int depth = 0; depth <= depth_max && ncur > 0; depth++) {
         int nnext = 0;
         for (int base = 0; base < ncur; base += 32) {
@@ -1369,41 +1420,50 @@ struct NearOutF {
 // GM as in far_sums_f32_o6x2: the G sums are formed only when some BC needs
 // them (GM > 0); the FP64 work left per pair is the geometry and the c sum.
 template <int GM>
-__device__ void near_integrate_f32(const double *h, const double *x, double k, int collapse, bool sing,
+__device__ void near_integrate_f32(const double *h, const PairGeoF &pg, float kf, int collapse, bool sing,
                                    const Leaf *leaves, int nl, int nq, float *lg, NearOutF &o) {
     const int lane = threadIdx.x & 31;
-    const double *n = h + 9;
-    const double d3[3] = {h[0] - x[0], h[1] - x[1], h[2] - x[2]};
-    const double hgt = d3[0] * n[0] + d3[1] * n[1] + d3[2] * n[2];
-    const float3 e1 = make_float3((float)h[3], (float)h[4], (float)h[5]);
-    const float3 e2 = make_float3((float)h[6], (float)h[7], (float)h[8]);
+    const float3 e1 = make_float3(pg.e1h[0], pg.e1h[1], pg.e1h[2]);
+    const float3 e2 = make_float3(pg.e2h[0], pg.e2h[1], pg.e2h[2]);
     const int cv = collapse - 1;
+    // u e1 + v e2 + w (head, tail) as a float, in double float: u and v are
+    // exact floats with few bits (0, 1 or dyadic leaf coordinates), so the
+    // heads' products are split exactly (TwoProduct) and summed by TwoSum
+    auto comb = [&](float u, float v, float wh, float wl, int a) {
+        const float p1 = __fmul_rn(u, pg.e1h[a]), q1 = __fmaf_rn(u, pg.e1h[a], -p1);
+        const float p2 = __fmul_rn(v, pg.e2h[a]), q2 = __fmaf_rn(v, pg.e2h[a], -p2);
+        float t1, t2;
+        const float s1 = two_sum(wh, p1, t1);
+        const float s2 = two_sum(s1, p2, t2);
+        return s2 + (wl + q1 + q2 + t1 + t2 + u * pg.e1l[a] + v * pg.e2l[a]);
+    };
     float3 dv = make_float3(0.f, 0.f, 0.f);   // singular: p_v - x
     if (sing) {
-        const double v1 = cv == 0 ? 1.0 : 0.0, v2 = cv == 1 ? 1.0 : 0.0;
-        dv = make_float3((float)(d3[0] + v1 * h[3] + v2 * h[6]), (float)(d3[1] + v1 * h[4] + v2 * h[7]),
-                         (float)(d3[2] + v1 * h[5] + v2 * h[8]));
+        const float v1 = cv == 0 ? 1.f : 0.f, v2 = cv == 1 ? 1.f : 0.f;
+        dv = make_float3(comb(v1, v2, pg.dh[0], pg.dl[0], 0), comb(v1, v2, pg.dh[1], pg.dl[1], 1),
+                         comb(v1, v2, pg.dh[2], pg.dl[2], 2));
     } else {
-        // per leaf (lanes over leaves): d_l, E1, E2 in FP64, then float
+        // per leaf (lanes over leaves): the corner's offset d_l and the edges
+        // E1, E2 in double float, then float; the corners are dyadic, so the
+        // edge coordinates and the area are exact in float
         for (int l = lane; l < nl; l += 32) {
             const Leaf t = leaves[l];
-            const double ea0 = (double)t.a[0] - t.c[0], ea1 = (double)t.a[1] - t.c[1];
-            const double eb0 = (double)t.b[0] - t.c[0], eb1 = (double)t.b[1] - t.c[1];
+            const float ea0 = t.a[0] - t.c[0], ea1 = t.a[1] - t.c[1];
+            const float eb0 = t.b[0] - t.c[0], eb1 = t.b[1] - t.c[1];
             float *g = lg + (size_t)l * kNearLeafF;
 #pragma unroll
             for (int dd = 0; dd < 3; dd++) {
-                g[dd] = (float)(d3[dd] + (double)t.c[0] * h[3 + dd] + (double)t.c[1] * h[6 + dd]);
-                g[3 + dd] = (float)(ea0 * h[3 + dd] + ea1 * h[6 + dd]);
-                g[6 + dd] = (float)(eb0 * h[3 + dd] + eb1 * h[6 + dd]);
+                g[dd] = comb(t.c[0], t.c[1], pg.dh[dd], pg.dl[dd], dd);
+                g[3 + dd] = comb(ea0, ea1, 0.f, 0.f, dd);
+                g[6 + dd] = comb(eb0, eb1, 0.f, 0.f, dd);
             }
-            g[9] = (float)fabs(ea0 * eb1 - ea1 * eb0);
+            g[9] = fabsf(__fsub_rn(__fmul_rn(ea0, eb1), __fmul_rn(ea1, eb0)));
         }
         __syncwarp();
     }
     float s[13], c[13];
 #pragma unroll
     for (int i = 0; i < 13; i++) s[i] = c[i] = 0.f;
-    const float kf = (float)k;
     for (int idx = lane; idx < nl * nq; idx += 32) {
         const int l = idx / nq, q = idx - l * nq;
         float3 d;
@@ -1463,22 +1523,22 @@ __device__ void near_integrate_f32(const double *h, const double *x, double k, i
         c[i] = lo;
     }
     // signs, height and scale: G = (gr, -gs), dG/dn = -hgt (ha, hb), dG0/dn =
-    // -hgt ri3; the dG/dn coefficients in FP32 from the head and tail
-    const double scale = h[12] * (1.0 / (4.0 * kPi));   // a constant reciprocal: no FP64 division
-    const double sh = -hgt * scale;
-    const float fsh = (float)sh;
+    // -hgt ri3; the dG/dn coefficients and the free-term contribution in FP32
+    // from the heads and tails (the entries they go into are FP32)
+    const float fsh = -pg.hgt * pg.scale;
 #pragma unroll
     for (int j = 0; j < 3; j++) {
         o.hr[j] = fmaf(fsh, s[6 + j], fsh * c[6 + j]);
         o.hi[j] = fmaf(fsh, s[9 + j], fsh * c[9 + j]);
         if (GM == 2 || (GM == 1 && j == 0)) {   // GM = 1: the sum over j in entry 0
+            const double scale = h[12] * (1.0 / (4.0 * kPi));   // beta's terms stay FP64
             o.gr[j] = scale * ((double)s[j] + (double)c[j]);
             o.gi[j] = -scale * ((double)s[3 + j] + (double)c[3 + j]);
         } else {
             o.gr[j] = o.gi[j] = 0.0;
         }
     }
-    o.c = sh * ((double)s[12] + (double)c[12]);
+    o.c = fmaf(fsh, s[12], fsh * c[12]);
 }
 
 __device__ __forceinline__ double2 incident_field(const DevSource &s, double k, const double *x) {
@@ -1511,7 +1571,7 @@ template <> __device__ __forceinline__ void add_entry<double2>(double2 *p, doubl
 // GM: which G sums the BCs need (as in far_sums_f32_o6x2), used by the c64
 // (TA = float2) FP32 path; the c128 kernel is instantiated with GM = 2.
 template <typename TA, typename TP, typename TP2, int GM>
-__global__ void __launch_bounds__(32 * kNearWarps)
+__global__ void __launch_bounds__(32 * kNearWarps, 4)
 near_assembly_kernel(RowPoints rows, int N, GeoTables geo, Physics ph, int nq, TA *__restrict__ A,
                      size_t lda, const TP *__restrict__ c_part, const TP2 *__restrict__ beta_part,
                      int ntiles, const DevSource *__restrict__ srcs, int S, double2 *__restrict__ B,
@@ -1524,6 +1584,13 @@ near_assembly_kernel(RowPoints rows, int N, GeoTables geo, Physics ph, int nq, T
     if (row >= rows.R) return;
     Leaf *leaves = leaves_all[warp];
     const double x[3] = {rows.d[3 * (size_t)row], rows.d[3 * (size_t)row + 1], rows.d[3 * (size_t)row + 2]};
+    constexpr bool f32 = std::is_same<TA, float2>::value;
+    float4 xh = make_float4(0.f, 0.f, 0.f, 0.f), xl = xh;   // the row point's head and tail (FP32 path)
+    if (f32) {
+        xh = rows.f[2 * (size_t)row];
+        xl = rows.f[2 * (size_t)row + 1];
+    }
+    const float kf = (float)ph.k;
     double cn = 0.0, bnr = 0.0, bni = 0.0;
     // The row's near elements, in increasing element order (near_list_kernel).
     const int pe = near_ptr[row + 1];
@@ -1542,19 +1609,23 @@ near_assembly_kernel(RowPoints rows, int N, GeoTables geo, Physics ph, int nq, T
             const double *h = geo.geo_d + (size_t)kGeoD * eb;
             int collapse = 3, nl = 1;
             const int vtx = (row < N) ? (row == ndb.x ? 1 : row == ndb.y ? 2 : row == ndb.z ? 3 : 0) : 0;
+            const float4 *gfe = geo.geo_f + (size_t)kGeoF * eb;
             if (vtx) {
                 collapse = vtx;
                 if (lane == 0) leaves[0] = {{1.f, 0.f}, {0.f, 1.f}, {0.f, 0.f}};
             } else {
-                nl = build_leaves_warp<std::is_same<TA, float2>::value>(h, x, ph.near_eta, ph.near_depth, leaves,
-                                                                         codes_all[warp][0], codes_all[warp][1]);
+                PairGeoF pg0;   // (formed again below rather than kept live through the leaf builder)
+                if (f32) pg0 = pair_geo_f(gfe, xh, xl);
+                nl = build_leaves_warp<f32>(h, x, ph.near_eta, ph.near_depth, leaves, codes_all[warp][0],
+                                            codes_all[warp][1], &pg0);
             }
             __syncwarp();
             NearOut o;
             const int node[3] = {ndb.x, ndb.y, ndb.z};
-            if (std::is_same<TA, float2>::value && nl <= kNearF32Leaves) {
+            if (f32 && nl <= kNearF32Leaves) {
                 NearOutF of;
-                near_integrate_f32<GM>(h, x, ph.k, collapse, vtx != 0, leaves, nl, nq,
+                const PairGeoF pg = pair_geo_f(gfe, xh, xl);
+                near_integrate_f32<GM>(h, pg, kf, collapse, vtx != 0, leaves, nl, nq,
                                        reinterpret_cast<float *>(&codes_all[warp][0][0]), of);
                 __syncwarp();
                 if constexpr (GM < 2 && std::is_same<TA, float2>::value) {

@@ -16,7 +16,7 @@ struct DevSource {
 };
 
 struct GeoTables {
-    const float4 *geo_f;      // 7 float4 per element (layout in kernels.cu)
+    const float4 *geo_f;      // 9 float4 per element (layout in kernels.cu)
     const double *geo_d;      // 18 doubles per element
     const int4 *elems;        // (n0, n1, n2, 0)
     int E;
@@ -86,7 +86,7 @@ void launch_elem_setup(const double *d_nodes, const int4 *d_elems, const double 
                        double near_eta, float4 *geo_f, double *geo_d, cudaStream_t st);
 
 // Far-field assembly.  c64: FP32 quadrature, acc/partials in float.  c128: FP64.
-constexpr int kGeoFloat4 = 7;     // float4 per element in GeoTables::geo_f
+constexpr int kGeoFloat4 = 9;     // float4 per element in GeoTables::geo_f
 constexpr int kGeoDouble = 18;    // doubles per element in GeoTables::geo_d
 // `variant` selects a launch shape (rows per CTA, threads, CTAs per SM);
 // far_variants(prec) shapes exist, far_variant_fits says whether the
