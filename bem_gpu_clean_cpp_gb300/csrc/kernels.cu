@@ -1411,14 +1411,16 @@ __device__ __forceinline__ void ksum(float &s, float &c, float t) {
 
 // Outputs of the FP32 near integration: the dG/dn parts of the three A
 // coefficients in FP32 (the c64 entries they are added to are FP32), the G
-// sums (for beta and bcA terms) and the free-term sum in FP64.
+// sums (for beta and bcA terms) in FP64, and the pair's free-term
+// contribution (formed in FP32, added to the row's FP64 sum).
 struct NearOutF {
     float hr[3], hi[3];
     double gr[3], gi[3], c;
 };
 
 // GM as in far_sums_f32_o6x2: the G sums are formed only when some BC needs
-// them (GM > 0); the FP64 work left per pair is the geometry and the c sum.
+// them (GM > 0).  The pair geometry comes in double float (PairGeoF); no FP64
+// operation is left per pair but those of the G sums.
 template <int GM>
 __device__ void near_integrate_f32(const double *h, const PairGeoF &pg, float kf, int collapse, bool sing,
                                    const Leaf *leaves, int nl, int nq, float *lg, NearOutF &o) {
