@@ -44,4 +44,32 @@ __device__ __forceinline__ void df_add2(float &hi, float &lo, float hi2, float l
     lo = __fadd_rn(__fadd_rn(lo, lo2), err);
 }
 
+// ---- double-float values (head, tail) as float2 ----
+// a + b, with the result renormalised by TwoSum (no magnitude assumption).
+__device__ __forceinline__ float2 ff_add(float2 a, float2 b) {
+    float e1, e2;
+    const float s = __fadd_rn(a.x, b.x);
+    {
+        const float bb = __fsub_rn(s, a.x);
+        e1 = __fadd_rn(__fsub_rn(a.x, __fsub_rn(s, bb)), __fsub_rn(b.x, bb));
+    }
+    const float t = __fadd_rn(e1, __fadd_rn(a.y, b.y));
+    const float u = __fadd_rn(s, t);
+    {
+        const float bb = __fsub_rn(u, s);
+        e2 = __fadd_rn(__fsub_rn(s, __fsub_rn(u, bb)), __fsub_rn(t, bb));
+    }
+    return make_float2(u, e2);
+}
+__device__ __forceinline__ float2 ff_neg(float2 a) { return make_float2(-a.x, -a.y); }
+// a b: the heads' product split exactly (FMA), the cross terms added to its
+// error, renormalised by TwoSum.
+__device__ __forceinline__ float2 ff_mul(float2 a, float2 b) {
+    const float p = __fmul_rn(a.x, b.x);
+    const float e = __fmaf_rn(a.x, b.y, __fmaf_rn(a.y, b.x, __fmaf_rn(a.x, b.x, -p)));
+    const float u = __fadd_rn(p, e);
+    const float bb = __fsub_rn(u, p);
+    return make_float2(u, __fadd_rn(__fsub_rn(p, __fsub_rn(u, bb)), __fsub_rn(e, bb)));
+}
+
 }  // namespace bem

@@ -162,10 +162,14 @@ void launch_gemv_h_c64(int R, int N, const float2 *A, size_t lda, const void *u,
 // available, then the caller runs the separate kernels.
 int arnoldi_step_blocks();
 // With wpart, w is first formed as the sum of nsplit partial products
-// (wpart[t N + i], FP64 in split order), in the same launch.
-bool launch_arnoldi_step(int n, int j, double2 *V, size_t ldv, double2 *w, float2 *vf, double2 *h1, double2 *h2,
-                         double2 *H, int ldh, double2 *cs, double2 *sn, double2 *g, double *res, double2 *part,
-                         cudaStream_t st, const float2 *wpart = nullptr, int nsplit = 0);
+// (wpart[t N + i], double float in split order), in the same launch; without
+// it w holds A^H A v_j in FP64.  Vff: the basis in double float (float4 per
+// entry: re head, im head, re tail, im tail; same stride as V), kept beside
+// V by this step and by launch_scale_copy; w and part are used as double
+// float in place.
+bool launch_arnoldi_step(int n, int j, double2 *V, size_t ldv, float4 *Vff, double2 *w, float2 *vf, double2 *h1,
+                         double2 *h2, double2 *H, int ldh, double2 *cs, double2 *sn, double2 *g, double *res,
+                         double2 *part, cudaStream_t st, const float2 *wpart = nullptr, int nsplit = 0);
 // w = A^H (A v) for c64 A with A read once (cluster kernel, A streamed by
 // TMA bulk copies); v c64, w c128; part: scratch of normal_op_clusters(N) x N
 // c64.  Returns false (nothing launched) when N is above what one cluster
@@ -219,9 +223,10 @@ void launch_update(int n, int k, const double2 *V, size_t ldv, const double2 *h,
 // partial sums (null: one CTA does it all)
 void launch_nrm2(int n, const double2 *w, double *out, double *part, cudaStream_t st);
 int nrm2_parts();
-// v = w / *nrm; also writes a c64 copy to vf when vf is not null.
+// v = w / *nrm; also writes a c64 copy to vf and a double-float copy to vff
+// when they are not null.
 void launch_scale_copy(int n, const double2 *w, const double *nrm, double2 *v, cudaStream_t st,
-                       float2 *vf = nullptr);
+                       float2 *vf = nullptr, float4 *vff = nullptr);
 void launch_axpy_combo(int n, int k, const double2 *V, size_t ldv, const double2 *y, double2 *x,
                        cudaStream_t st);                      // x += V y
 void launch_copy_f64(int n, const double2 *src, double2 *dst, cudaStream_t st);

@@ -421,14 +421,16 @@ __global__ void nrm2_kernel(int n, const double2 *__restrict__ w, double *__rest
 }
 
 __global__ void scale_copy_kernel(int n, const double2 *__restrict__ w, const double *__restrict__ nrm,
-                                  double2 *__restrict__ v, float2 *__restrict__ vf) {
+                                  double2 *__restrict__ v, float2 *__restrict__ vf, float4 *__restrict__ vff) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double s = *nrm;
     double inv = s > 0 ? 1.0 / s : 0.0;
     const double2 o = make_double2(w[i].x * inv, w[i].y * inv);
     v[i] = o;
-    if (vf) vf[i] = make_float2((float)o.x, (float)o.y);
+    const float hr = (float)o.x, hm = (float)o.y;
+    if (vf) vf[i] = make_float2(hr, hm);
+    if (vff) vff[i] = make_float4(hr, hm, (float)(o.x - (double)hr), (float)(o.y - (double)hm));
 }
 
 __global__ void copy_f64_kernel(int n, const double2 *__restrict__ s, double2 *__restrict__ d) {
@@ -585,11 +587,13 @@ sum_many_splits_kernel(int N, int ns, const float2 *__restrict__ part, double2 *
 }
 
 // ---- one Arnoldi step of the refined solver in one cooperative launch ----
-// For basis vectors V_0..V_j (FP64, column stride ldv) and w = A^H A v_j:
-// classical Gram-Schmidt twice (h1 = V^H w, w -= V h1, h2 = V^H w,
-// w -= V h2), |w|, v_{j+1} = w/|w| (and its c64 copy), then the Hessenberg
-// column and its Givens rotation (GMRES.cu:44-88) with the residual estimate
-// |g_{j+1}| in *res.  Each CTA owns a contiguous slice of the n entries; the
+// For basis vectors V_0..V_j (column stride ldv; FP64 in V and double float
+// in Vff) and w = A^H A v_j: classical Gram-Schmidt twice (h1 = V^H w,
+// w -= V h1, h2 = V^H w, w -= V h2), |w|, v_{j+1} = w/|w| (into V, Vff and
+// its c64 copy vf), then the Hessenberg column and its Givens rotation
+// (GMRES.cu:44-88, FP64) with the residual estimate |g_{j+1}| in *res.  The
+// Gram-Schmidt products and sums are double float on the FP32 pipe (~48
+// significant bits; this part's FP64 rate is a small fraction of FP32).  Each CTA owns a contiguous slice of the n entries; the
 // dot products and the norm are per-CTA partial sums reduced after a grid
 // barrier, in the same order by every CTA.  Every CTA passes the same two
 // grid barriers (no early exit), and the launch is cooperative, so all CTAs
@@ -598,105 +602,115 @@ constexpr int kArNT = 256;
 constexpr int kArnoldiMaxK = 1024;   // basis vectors per step (shared-memory coefficients)
 
 __global__ void __launch_bounds__(kArNT)
-arnoldi_step_kernel(int n, int j, double2 *__restrict__ V, size_t ldv, double2 *__restrict__ w,
-                    float2 *__restrict__ vf, double2 *__restrict__ h1, double2 *__restrict__ h2,
-                    double2 *__restrict__ H, int ldh, double2 *__restrict__ cs, double2 *__restrict__ sn,
-                    double2 *__restrict__ g, double *__restrict__ res, double2 *__restrict__ part,
-                    const float2 *__restrict__ wpart, int nsplit) {
+arnoldi_step_kernel(int n, int j, double2 *__restrict__ V, size_t ldv, float4 *__restrict__ Vff,
+                    float4 *__restrict__ w, float2 *__restrict__ vf, double2 *__restrict__ h1,
+                    double2 *__restrict__ h2, double2 *__restrict__ H, int ldh, double2 *__restrict__ cs,
+                    double2 *__restrict__ sn, double2 *__restrict__ g, double *__restrict__ res,
+                    float4 *__restrict__ part, const float2 *__restrict__ wpart, int nsplit) {
     namespace cg = cooperative_groups;
     cg::grid_group grid = cg::this_grid();
     const int nb = gridDim.x, b = blockIdx.x, tid = threadIdx.x;
     const int per = (n + nb - 1) / nb;
     const int i0 = min(n, b * per), i1 = min(n, i0 + per);
     const int k = j + 1;                              // basis vectors in use
-    extern __shared__ double2 hs[];                   // k coefficients
+    extern __shared__ float4 hs[];                    // k coefficients (and |w|^2), double float
     const int lane = tid & 31, warp = tid >> 5;
+    // complex double-float values as float4 (re head, im head, re tail, im tail)
+    auto re = [](float4 v) { return make_float2(v.x, v.z); };
+    auto im = [](float4 v) { return make_float2(v.y, v.w); };
+    auto pack = [](float2 r, float2 i) { return make_float4(r.x, i.x, r.y, i.y); };
+    auto xor_add = [&](float2 &a, int o) {   // a += lane (this ^ o)'s a (the same in both lanes)
+        const float2 t = make_float2(__shfl_xor_sync(0xffffffffu, a.x, o), __shfl_xor_sync(0xffffffffu, a.y, o));
+        a = ff_add(a, t);
+    };
     // partial dots of this CTA's slice: warp w takes basis vectors w, w + 8,
     // ..., its lanes the slice's entries (fixed order), out_part[q * nb + b];
     // with nq = k + 1 the last "basis vector" is w itself (|w|^2 partials)
-    auto partial_dots = [&](double2 *out_part, int nq) {
+    auto partial_dots = [&](float4 *out_part, int nq) {
         for (int q = warp; q < nq; q += kArNT / 32) {
-            const double2 *vq = q < k ? V + (size_t)q * ldv : w;
-            double a = 0.0, c = 0.0;
+            const float4 *vq = q < k ? Vff + (size_t)q * ldv : w;
+            float2 ar = make_float2(0.f, 0.f), ai = ar;
             for (int i = i0 + lane; i < i1; i += 32) {
-                const double2 x = vq[i], y = w[i];
-                a += x.x * y.x + x.y * y.y;   // conj(v) w
-                c += x.x * y.y - x.y * y.x;
+                const float4 x = vq[i], y = w[i];
+                // conj(v) w
+                ar = ff_add(ar, ff_add(ff_mul(re(x), re(y)), ff_mul(im(x), im(y))));
+                ai = ff_add(ai, ff_add(ff_mul(re(x), im(y)), ff_neg(ff_mul(im(x), re(y)))));
             }
             for (int o = 16; o > 0; o >>= 1) {
-                a += __shfl_xor_sync(0xffffffffu, a, o);
-                c += __shfl_xor_sync(0xffffffffu, c, o);
+                xor_add(ar, o);
+                xor_add(ai, o);
             }
-            if (lane == 0) out_part[(size_t)q * nb + b] = make_double2(a, c);
+            if (lane == 0) out_part[(size_t)q * nb + b] = pack(ar, ai);
         }
     };
     // h[q] = sum over the CTAs' partials (one warp per q, fixed order), into
-    // shared memory and, from CTA 0 and for q < k, into hout
-    auto reduce_dots = [&](const double2 *in_part, double2 *hout, int nq) {
+    // shared memory and, from CTA 0 and for q < k, into hout (FP64)
+    auto reduce_dots = [&](const float4 *in_part, double2 *hout, int nq) {
         for (int q = warp; q < nq; q += kArNT / 32) {
-            double a = 0.0, c = 0.0;
+            float2 ar = make_float2(0.f, 0.f), ai = ar;
             for (int t = lane; t < nb; t += 32) {
-                const double2 p = in_part[(size_t)q * nb + t];
-                a += p.x;
-                c += p.y;
+                const float4 p = in_part[(size_t)q * nb + t];
+                ar = ff_add(ar, re(p));
+                ai = ff_add(ai, im(p));
             }
             for (int o = 16; o > 0; o >>= 1) {
-                a += __shfl_xor_sync(0xffffffffu, a, o);
-                c += __shfl_xor_sync(0xffffffffu, c, o);
+                xor_add(ar, o);
+                xor_add(ai, o);
             }
             if (lane == 0) {
-                hs[q] = make_double2(a, c);
-                if (b == 0 && q < k) hout[q] = hs[q];
+                hs[q] = pack(ar, ai);
+                if (b == 0 && q < k) hout[q] = make_double2((double)ar.x + (double)ar.y, (double)ai.x + (double)ai.y);
             }
         }
         __syncthreads();
     };
     // w -= V h: four consecutive threads per entry, each over every fourth
-    // basis vector, then the four sums in a fixed order; with inv >= 0 the
-    // result is the next basis vector (w - V h) inv, written to vn and vf
-    // instead of w
-    double2 *vn = V + (size_t)k * ldv;
-    auto subtract = [&](double inv) {
+    // basis vector, then the four sums in a fixed order; with normalise the
+    // result times inv is the next basis vector, written to Vff (double
+    // float), V (FP64) and vf (its float head) instead of w
+    __shared__ float2 inv_s;
+    auto subtract = [&](bool normalise) {
         constexpr int kQ = 4;
         const int r = tid % kQ;
+        double2 *vn = V + (size_t)k * ldv;
+        float4 *vnf = Vff + (size_t)k * ldv;
         for (int base = i0; base < i1; base += kArNT / kQ) {
             const int i = base + tid / kQ;
-            double a = 0.0, c = 0.0;
+            float2 sr = make_float2(0.f, 0.f), si = sr;
             if (i < i1) {
                 for (int q = r; q < k; q += kQ) {
-                    const double2 x = V[(size_t)q * ldv + i], y = hs[q];
-                    a += x.x * y.x - x.y * y.y;
-                    c += x.x * y.y + x.y * y.x;
+                    const float4 x = Vff[(size_t)q * ldv + i], y = hs[q];
+                    sr = ff_add(sr, ff_add(ff_mul(re(x), re(y)), ff_neg(ff_mul(im(x), im(y)))));
+                    si = ff_add(si, ff_add(ff_mul(re(x), im(y)), ff_mul(im(x), re(y))));
                 }
             }
 #pragma unroll
             for (int o = 1; o < kQ; o <<= 1) {
-                a += __shfl_xor_sync(0xffffffffu, a, o);
-                c += __shfl_xor_sync(0xffffffffu, c, o);
+                xor_add(sr, o);
+                xor_add(si, o);
             }
             if (r == 0 && i < i1) {
-                const double2 ww = w[i];
-                if (inv < 0.0) {
-                    w[i] = make_double2(ww.x - a, ww.y - c);
+                const float4 ww = w[i];
+                const float2 nr = ff_add(re(ww), ff_neg(sr)), ni = ff_add(im(ww), ff_neg(si));
+                if (!normalise) {
+                    w[i] = pack(nr, ni);
                 } else {
-                    const double2 o = make_double2((ww.x - a) * inv, (ww.y - c) * inv);
-                    vn[i] = o;
-                    vf[i] = make_float2((float)o.x, (float)o.y);
+                    const float2 vr = ff_mul(nr, inv_s), vi = ff_mul(ni, inv_s);
+                    vnf[i] = pack(vr, vi);
+                    vn[i] = make_double2((double)vr.x + (double)vr.y, (double)vi.x + (double)vi.y);
+                    vf[i] = make_float2(vr.x, vi.x);
                 }
             }
         }
         __syncthreads();
     };
-    double2 *p1 = part, *p2 = part + (size_t)k * nb;   // k and k + 1 partials per CTA
+    float4 *p1 = part, *p2 = part + (size_t)k * nb;   // k and k + 1 partials per CTA
     if (wpart) {
         // w = the sum of the normal operator's nsplit partial products, this
         // CTA's slice: four consecutive threads per entry, each adding a
         // quarter of the partials in order, then the quarters in order (a fixed
-        // order; the loads of an entry are spread over four threads).  The
-        // partials are floats; they are summed in double-float on the FP32 pipe
-        // (TwoSum, error ~1e-14 of the sum of magnitudes) and the head and tail
-        // added in FP64 once per entry: this device's FP64 rate is a small
-        // fraction of its FP32 rate.
+        // order; the loads of an entry are spread over four threads), in
+        // double float
         constexpr int kQ = 4;
         const int q = tid % kQ, per_q = (nsplit + kQ - 1) / kQ;
         const int t0 = min(nsplit, q * per_q), t1 = min(nsplit, t0 + per_q);
@@ -718,14 +732,21 @@ arnoldi_step_kernel(int n, int j, double2 *__restrict__ V, size_t ldv, double2 *
                 df_add2(hr, lr, ohr, olr);
                 df_add2(hm, lm, ohm, olm);
             }
-            if (q == 0 && i < i1) w[i] = make_double2((double)hr + (double)lr, (double)hm + (double)lm);
+            if (q == 0 && i < i1) w[i] = make_float4(hr, hm, lr, lm);
         }
-        __syncthreads();   // partial_dots reads w with another thread-to-entry map
+    } else {
+        // w = A^H A v_j came as FP64 (the two-kernel product): split in place
+        for (int i = i0 + tid; i < i1; i += kArNT) {
+            const double2 d = reinterpret_cast<const double2 *>(w)[i];
+            const float hr = (float)d.x, hm = (float)d.y;
+            w[i] = make_float4(hr, hm, (float)(d.x - (double)hr), (float)(d.y - (double)hm));
+        }
     }
+    __syncthreads();   // partial_dots reads w with another thread-to-entry map
     partial_dots(p1, k);
     grid.sync();
     reduce_dots(p1, h1, k);
-    subtract(-1.0);
+    subtract(false);
     // second pass: h2 = V^H w and |w|^2 in the same reduction; the norm of
     // w - V h2 is sqrt(|w|^2 - |h2|^2) (V orthonormal; h2 is at the level of
     // the first pass's rounding, so the difference does not cancel), which
@@ -735,15 +756,21 @@ arnoldi_step_kernel(int n, int j, double2 *__restrict__ V, size_t ldv, double2 *
     reduce_dots(p2, h2, k + 1);
     __shared__ double nrm_s;
     if (warp == 0) {
-        double t = 0.0;
-        for (int q = lane; q < k; q += 32) t += hs[q].x * hs[q].x + hs[q].y * hs[q].y;
-        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-        if (lane == 0) nrm_s = sqrt(fmax(hs[k].x - t, 0.0));
+        float2 t = make_float2(0.f, 0.f);
+        for (int q = lane; q < k; q += 32) t = ff_add(t, ff_add(ff_mul(re(hs[q]), re(hs[q])), ff_mul(im(hs[q]), im(hs[q]))));
+        for (int o = 16; o > 0; o >>= 1) xor_add(t, o);
+        if (lane == 0) {
+            const float2 d = ff_add(re(hs[k]), ff_neg(t));
+            const double nrm = sqrt(fmax((double)d.x + (double)d.y, 0.0));
+            const double inv = nrm > 0 ? 1.0 / nrm : 0.0;
+            const float ih = (float)inv;
+            nrm_s = nrm;
+            inv_s = make_float2(ih, (float)(inv - (double)ih));
+        }
     }
     __syncthreads();
     const double nrm = nrm_s;
-    const double inv = nrm > 0 ? 1.0 / nrm : 0.0;
-    subtract(inv);   // v_{j+1} = (w - V h2) / |w - V h2|
+    subtract(true);   // v_{j+1} = (w - V h2) / |w - V h2|
     if (b == 0 && tid == 0) {
         // Hessenberg column j = h1 + h2, H[j+1, j] = |w|, then the rotations
         double2 *h = H + (size_t)j * ldh;
@@ -1134,7 +1161,7 @@ int arnoldi_step_blocks() {
         if (cudaGetDevice(&dev) != cudaSuccess ||
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, arnoldi_step_kernel, kArNT,
-                                                          (size_t)(kArnoldiMaxK + 1) * sizeof(double2)) != cudaSuccess ||
+                                                          (size_t)(kArnoldiMaxK + 1) * sizeof(float4)) != cudaSuccess ||
             per < 1) {
             cudaGetLastError();
             nb = 0;
@@ -1145,14 +1172,17 @@ int arnoldi_step_blocks() {
     return nb;
 }
 
-bool launch_arnoldi_step(int n, int j, double2 *V, size_t ldv, double2 *w, float2 *vf, double2 *h1, double2 *h2,
-                         double2 *H, int ldh, double2 *cs, double2 *sn, double2 *g, double *res, double2 *part,
-                         cudaStream_t st, const float2 *wpart, int nsplit) {
+bool launch_arnoldi_step(int n, int j, double2 *V, size_t ldv, float4 *Vff, double2 *w, float2 *vf, double2 *h1,
+                         double2 *h2, double2 *H, int ldh, double2 *cs, double2 *sn, double2 *g, double *res,
+                         double2 *part, cudaStream_t st, const float2 *wpart, int nsplit) {
     const int nb = arnoldi_step_blocks();
-    if (nb <= 0 || j + 1 > kArnoldiMaxK || n < 1) return false;
+    if (nb <= 0 || j + 1 > kArnoldiMaxK || n < 1 || !Vff) return false;
     BEM_PROF("arnoldi_step", st);
-    const size_t smem = (size_t)(j + 2) * sizeof(double2);   // h and |w|^2
-    void *args[] = {&n, &j, &V, &ldv, &w, &vf, &h1, &h2, &H, &ldh, &cs, &sn, &g, &res, &part, &wpart, &nsplit};
+    const size_t smem = (size_t)(j + 2) * sizeof(float4);   // h and |w|^2
+    // w and the partial dots are held in double float (16 bytes an entry, as
+    // their FP64 form)
+    float4 *wf = reinterpret_cast<float4 *>(w), *pf = reinterpret_cast<float4 *>(part);
+    void *args[] = {&n, &j, &V, &ldv, &Vff, &wf, &vf, &h1, &h2, &H, &ldh, &cs, &sn, &g, &res, &pf, &wpart, &nsplit};
     const cudaError_t e = cudaLaunchCooperativeKernel((const void *)arnoldi_step_kernel, dim3(nb), dim3(kArNT),
                                                       args, smem, st);
     if (e != cudaSuccess) {
@@ -1416,9 +1446,10 @@ void launch_nrm2(int n, const double2 *w, double *out, double *part, cudaStream_
     KERNEL_CHECK();
 }
 
-void launch_scale_copy(int n, const double2 *w, const double *nrm, double2 *v, cudaStream_t st, float2 *vf) {
+void launch_scale_copy(int n, const double2 *w, const double *nrm, double2 *v, cudaStream_t st, float2 *vf,
+                       float4 *vff) {
     BEM_PROF("scale_copy", st);
-    scale_copy_kernel<<<blocks(n, 256), 256, 0, st>>>(n, w, nrm, v, vf);
+    scale_copy_kernel<<<blocks(n, 256), 256, 0, st>>>(n, w, nrm, v, vf, vff);
     count_launch();
     KERNEL_CHECK();
 }

@@ -97,6 +97,8 @@ void bem_solver_s::solve_refined(bem_solve_info_t *info) {
     const int ldh = m + 1;
     const float2 *A = d_A.as<float2>();
     w_V.ensure(sizeof(double2) * (size_t)n * (m + 1));
+    w_Vff.ensure(sizeof(float4) * (size_t)n * (m + 1));
+    float4 *Vff = w_Vff.as<float4>();
     w_H.ensure(sizeof(double2) * (size_t)ldh * m);
     w_cs.ensure(sizeof(double2) * m);
     w_sn.ensure(sizeof(double2) * m);
@@ -175,7 +177,7 @@ void bem_solver_s::solve_refined(bem_solve_info_t *info) {
             if (rel <= opt.tol) { conv = true; break; }
             if (ref >= opt.max_refine) break;
             // Inner GMRES on A^H A d = g, d accumulated into x.
-            launch_scale_copy(n, w_gv.as<double2>(), scal + 1, V, stream, w_vf.as<float2>());
+            launch_scale_copy(n, w_gv.as<double2>(), scal + 1, V, stream, w_vf.as<float2>(), Vff);
             launch_zero_f64(m + 1, w_g.as<double2>(), stream);
             launch_set_scalar_c(w_g.as<double2>(), scal + 1, stream);
             // One GMRES step: w = A^H A v_j (c64 copy of v_j; one pass over A
@@ -193,7 +195,7 @@ void bem_solver_s::solve_refined(bem_solve_info_t *info) {
                     launch_gemv_h_c64(R, n, A, lda, w_t.p, 0, w_w.p, 1, w_part.p, stream);  // w = A^H t
                 }
                 const float2 *wpart = fused ? w_part.as<float2>() : nullptr;
-                const bool stepped = launch_arnoldi_step(n, j, V, n, w_w.as<double2>(), w_vf.as<float2>(),
+                const bool stepped = launch_arnoldi_step(n, j, V, n, Vff, w_w.as<double2>(), w_vf.as<float2>(),
                                                          w_h1.as<double2>(), w_h2.as<double2>(), w_H.as<double2>(),
                                                          ldh, w_cs.as<double2>(), w_sn.as<double2>(),
                                                          w_g.as<double2>(), scal + 3, w_ap.as<double2>(), stream,
@@ -208,7 +210,7 @@ void bem_solver_s::solve_refined(bem_solve_info_t *info) {
                     launch_hcol_finish(j, w_h1.as<double2>(), w_h2.as<double2>(), scal + 2, w_H.as<double2>(), ldh,
                                        stream);
                     launch_scale_copy(n, w_w.as<double2>(), scal + 2, V + (size_t)(j + 1) * n, stream,
-                                      w_vf.as<float2>());
+                                      w_vf.as<float2>(), Vff + (size_t)(j + 1) * n);
                     launch_givens(j, w_H.as<double2>(), ldh, w_cs.as<double2>(), w_sn.as<double2>(),
                                   w_g.as<double2>(), scal + 3, stream);
                 }

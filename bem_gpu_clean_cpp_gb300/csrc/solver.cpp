@@ -862,7 +862,7 @@ size_t bem_solver_s::estimate_bytes(int N, int E, int M, int S, int method, cons
         b += extra;
     } else if (method == BEM_SOLVE_GMRES_REFINED) {
         const size_t m = (size_t)std::max(1, o.max_iter);
-        b += 16 * n * (m + 1) + 16 * (m + 1) * m + 16 * 6 * (m + 1);
+        b += 2 * 16 * n * (m + 1) + 16 * (m + 1) * m + 16 * 6 * (m + 1);   // the basis in FP64 and double float
         b += 16 * n * 2 + 8 * r + 16 * r + 16 * std::max(n, r);
         b += 16 * n * (size_t)std::max(gemv_h_splits((int)r, N), gemv_h_f64_splits((int)r, N)) + 64;
         b += 8 * n * (size_t)std::max(0, normal_op_clusters(N) - 2 * gemv_h_splits((int)r, N));

@@ -124,6 +124,7 @@ struct bem_solver_s {
     // packed operand and the split products' partial sums)
     bem::DevMem x_Ahi, x_Alo, x_vlo, x_tlo, w_d;
     bem::DevMem w_ap;   // partial sums of the cooperative Arnoldi step
+    bem::DevMem w_Vff;  // the refined GMRES basis in double float (float4 an entry), beside w_V
     int tf32_split_mode = -1;   // BEM_GEMM_* the planes of A were built for (this assembly), -1 none
     // tensor-core products (BEM_GEMM_TC): the power-of-two scale of A ([0]
     // scale, [1] inverse, [2] scratch), valid for this assembly
