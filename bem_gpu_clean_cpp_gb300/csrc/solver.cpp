@@ -5,7 +5,6 @@
 #include "tc_gemm.h"
 
 #include <algorithm>
-#include <chrono>
 #include <future>
 #include <cmath>
 #include <cstring>
@@ -634,26 +633,13 @@ void bem_solver_s::assemble(double kk, int precision) {
     ensure_quadrature(opt.order);
     ensure_geo();
     // The near-pair list (two small kernels and a read-back of the per-row
-    // counts) is built on the handle's second, high-priority stream, so that
-    // its host wait overlaps other work: that stream starts after the element
-    // tables, and the near kernel waits for the list.
+    // counts) is built on the handle's second, high-priority stream while the
+    // far kernel runs: that stream starts after the element tables, and the
+    // near kernel waits for the list.
     const bool near_build = !near_valid;
-    auto build_near = [&]() {   // on the second stream, after the element tables
-        CUDA_TRY(cudaStreamWaitEvent(qr_aux, asm_ev[0], 0));
-        ensure_near_list(qr_aux);
-        CUDA_TRY(cudaEventRecord(asm_ev[1], qr_aux));
-    };
-    bool near_queued = false;
     if (near_build) {
         ensure_aux();
         CUDA_TRY(cudaEventRecord(asm_ev[0], stream));
-        // while the column-tile tables are still being built on the host
-        // thread set_geometry started, the near list's host wait goes beside
-        // that one; otherwise it goes beside the far kernel (below)
-        if (tile_future.valid() && tile_future.wait_for(std::chrono::seconds(0)) != std::future_status::ready) {
-            build_near();
-            near_queued = true;
-        }
     }
     ensure_tiles(precision);
     k = kk;
@@ -737,8 +723,10 @@ void bem_solver_s::assemble(double kk, int precision) {
                             stream, variant);
     far_variant_used = variant;
     if (near_build) {
-        if (!near_queued) build_near();
-        CUDA_TRY(cudaStreamWaitEvent(stream, asm_ev[1], 0));   // the near kernel reads the list
+        CUDA_TRY(cudaStreamWaitEvent(qr_aux, asm_ev[0], 0));
+        ensure_near_list(qr_aux);
+        CUDA_TRY(cudaEventRecord(asm_ev[1], qr_aux));
+        CUDA_TRY(cudaStreamWaitEvent(stream, asm_ev[1], 0));
     }
     d_beta.ensure(sizeof(double2) * (size_t)R);
     launch_near_assembly(precision, row_points(), N, geo_tables(), ph, d_A.p, lda, d_cpart.p, d_bpart.p,
