@@ -224,9 +224,10 @@ void launch_update(int n, int k, const double2 *V, size_t ldv, const double2 *h,
 void launch_nrm2(int n, const double2 *w, double *out, double *part, cudaStream_t st);
 int nrm2_parts();
 // v = w / *nrm; also writes a c64 copy to vf and a double-float copy to vff
-// when they are not null.
+// when they are not null, and with g0 the GMRES right-hand side g0 = *nrm e_1
+// (gn entries).
 void launch_scale_copy(int n, const double2 *w, const double *nrm, double2 *v, cudaStream_t st,
-                       float2 *vf = nullptr, float4 *vff = nullptr);
+                       float2 *vf = nullptr, float4 *vff = nullptr, double2 *g0 = nullptr, int gn = 0);
 void launch_axpy_combo(int n, int k, const double2 *V, size_t ldv, const double2 *y, double2 *x,
                        cudaStream_t st);                      // x += V y
 void launch_copy_f64(int n, const double2 *src, double2 *dst, cudaStream_t st);

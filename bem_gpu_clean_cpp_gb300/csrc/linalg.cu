@@ -421,10 +421,12 @@ __global__ void nrm2_kernel(int n, const double2 *__restrict__ w, double *__rest
 }
 
 __global__ void scale_copy_kernel(int n, const double2 *__restrict__ w, const double *__restrict__ nrm,
-                                  double2 *__restrict__ v, float2 *__restrict__ vf, float4 *__restrict__ vff) {
+                                  double2 *__restrict__ v, float2 *__restrict__ vf, float4 *__restrict__ vff,
+                                  double2 *__restrict__ g0, int gn) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
     double s = *nrm;
+    if (g0 && i < gn) g0[i] = make_double2(i == 0 ? s : 0.0, 0.0);   // g = |w| e_1
+    if (i >= n) return;
     double inv = s > 0 ? 1.0 / s : 0.0;
     const double2 o = make_double2(w[i].x * inv, w[i].y * inv);
     v[i] = o;
@@ -1447,9 +1449,9 @@ void launch_nrm2(int n, const double2 *w, double *out, double *part, cudaStream_
 }
 
 void launch_scale_copy(int n, const double2 *w, const double *nrm, double2 *v, cudaStream_t st, float2 *vf,
-                       float4 *vff) {
+                       float4 *vff, double2 *g0, int gn) {
     BEM_PROF("scale_copy", st);
-    scale_copy_kernel<<<blocks(n, 256), 256, 0, st>>>(n, w, nrm, v, vf, vff);
+    scale_copy_kernel<<<blocks(std::max(n, g0 ? gn : 0), 256), 256, 0, st>>>(n, w, nrm, v, vf, vff, g0, gn);
     count_launch();
     KERNEL_CHECK();
 }

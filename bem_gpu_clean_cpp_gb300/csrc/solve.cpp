@@ -177,9 +177,8 @@ void bem_solver_s::solve_refined(bem_solve_info_t *info) {
             if (rel <= opt.tol) { conv = true; break; }
             if (ref >= opt.max_refine) break;
             // Inner GMRES on A^H A d = g, d accumulated into x.
-            launch_scale_copy(n, w_gv.as<double2>(), scal + 1, V, stream, w_vf.as<float2>(), Vff);
-            launch_zero_f64(m + 1, w_g.as<double2>(), stream);
-            launch_set_scalar_c(w_g.as<double2>(), scal + 1, stream);
+            launch_scale_copy(n, w_gv.as<double2>(), scal + 1, V, stream, w_vf.as<float2>(), Vff, w_g.as<double2>(),
+                              m + 1);
             // One GMRES step: w = A^H A v_j (c64 copy of v_j; one pass over A
             // when a cluster covers N), the Arnoldi step and Givens rotation,
             // then the residual estimate to h_pinned[4 + (j & 1)], signalled by
