@@ -223,12 +223,15 @@ void bem_solver_s::solve_refined(bem_solve_info_t *info) {
             // all, step j + 1 has only written basis vector j + 2, Hessenberg
             // column j + 1, rotation j + 1 and g[j + 1], g[j + 2], none of
             // which the solution over the first j + 1 columns reads.
-            constexpr double kSpeculate = 20.0;
+            // "Well above": step j's estimate, extrapolated from the last two
+            // at their rate of decrease, still kSpeculate times the tolerance.
+            constexpr double kSpeculate = 2.5;
             int jdone = 0;
-            double prev = 1.0;   // estimate / |g| of the previous step (1 before the first)
+            double prev = 1.0, prev2 = 1.0;   // estimates / |g| of the last two steps (1 before the first)
             launch_step(0);
             for (int j = 0; j < m; j++) {
-                const bool ahead = j + 1 < m && prev > kSpeculate * opt.inner_tol;
+                const double rate = std::min(1.0, prev2 > 0.0 ? prev / prev2 : 1.0);
+                const bool ahead = j + 1 < m && prev * rate > kSpeculate * opt.inner_tol;
                 if (ahead) launch_step(j + 1);
                 CUDA_TRY(cudaEventSynchronize(ev_res[j & 1]));
                 if (bn < 0.0) {   // the first step of the first inner solve
@@ -241,6 +244,7 @@ void bem_solver_s::solve_refined(bem_solve_info_t *info) {
                 const double res = h_pinned[4 + (j & 1)];
                 jdone = j + 1;
                 if (!(res / gn > opt.inner_tol)) break;
+                prev2 = prev;
                 prev = res / gn;
                 if (!ahead && j + 1 < m) launch_step(j + 1);
             }
