@@ -38,6 +38,7 @@ PREC_C64, PREC_C128 = 0, 1
 SOLVE_QR, SOLVE_GMRES_REFINED, SOLVE_BLOCK_GMRES, SOLVE_QR_TC = 0, 1, 2, 3
 GEMM_AUTO, GEMM_FP32, GEMM_SPLIT_BF16, GEMM_TF32, GEMM_TF32X3, GEMM_TF32X3_3M, GEMM_SIMT, GEMM_TC = -1, 0, 1, 2, 3, 4, 5, 6
 SRC_POINT, SRC_PLANE = 0, 1
+ERR_INVALID_ARG = 2
 ERR_NOT_CONVERGED = 5
 ERR_TOO_LARGE = 8
 ERR_TIMEOUT = 10
@@ -139,6 +140,7 @@ SIGNATURES = {
     "bem_mesh_geodesic": (_I, [_VP, _I, _D]),
     "bem_mesh_perturbed_ellipsoid": (_I, [_VP, _D, _D, _D, _I, _D, ctypes.c_ulonglong]),
     "bem_fibonacci_sphere": (_I, [_I, _D, _VP]),
+    "bem_hmat_partition": (_I, [_VP, _I, _VP, _I, _I, _D, _VP, _VP, _VP, _I, ctypes.POINTER(_I)]),
     "bem_system_c64": (_I, [_VP, _F, _VP, _I, _VP, _I, _VP, _I]),
     "bem_qr_solve_c64": (_I, [_VP, _I, _I, _I, _VP, _I, _I]),
     "bem_gmres_c64": (_I, [_VP, _VP, _I, _I, _F, _VP]),
@@ -264,6 +266,27 @@ def fibonacci_sphere(n: int, radius: float = 1.0) -> np.ndarray:
     out = np.zeros((n, 3))
     _check(lib().bem_fibonacci_sphere(int(n), float(radius), _ptr(out)))
     return out
+
+
+def hmat_partition(rows, cols, leaf: int = 128, eta: float = 1.0):
+    """Block partition of the (rows x cols) collocation matrix for a
+    hierarchical representation (bem_hmat_partition).  Returns (row_perm,
+    col_perm, blocks): the clustered orders (position -> original index) and
+    an int array of (row_begin, row_count, col_begin, col_count, admissible)
+    per block, in clustered positions."""
+    rows = np.ascontiguousarray(rows, dtype=np.float64).reshape(-1, 3)
+    cols = np.ascontiguousarray(cols, dtype=np.float64).reshape(-1, 3)
+    R, N = rows.shape[0], cols.shape[0]
+    n = _I(0)
+    L = lib()
+    _check(L.bem_hmat_partition(_ptr(rows), R, _ptr(cols), N, int(leaf), float(eta), None, None, None, 0,
+                                ctypes.byref(n)))
+    row_perm = np.zeros(R, dtype=np.int32)
+    col_perm = np.zeros(N, dtype=np.int32)
+    blocks = np.zeros((max(n.value, 1), 5), dtype=np.int32)
+    _check(L.bem_hmat_partition(_ptr(rows), R, _ptr(cols), N, int(leaf), float(eta), _ptr(row_perm),
+                                _ptr(col_perm), _ptr(blocks), n.value, ctypes.byref(n)))
+    return row_perm, col_perm, blocks[:n.value]
 
 
 def set_medium(density: float, speed: float) -> None:

@@ -131,6 +131,24 @@ int bem_mesh_perturbed_ellipsoid(bem_mesh_t m, double a, double b, double c, int
                                  unsigned long long seed);
 /* n points (3 doubles each) of a Fibonacci lattice on a sphere. */
 int bem_fibonacci_sphere(int n, double radius, double *pts);
+/* Block partition of the collocation matrix for a hierarchical (H-matrix)
+ * representation (no reference counterpart: the reference stores A dense,
+ * mesh.cu:985-1006).  Host only.  rows: num_rows points (3 doubles each:
+ * the nodes, then the CHIEF points); cols: num_cols points (the nodes).  Each
+ * set is clustered by median bisection along the longest axis of the
+ * cluster's bounding box down to clusters of at most leaf points (clusters of
+ * coincident points stay whole).  A block pairs a row cluster I with a
+ * column cluster J: admissible (low rank, flag 1) when the boxes are apart
+ * and min(diam I, diam J) <= eta * dist(I, J), dense (flag 0) when neither
+ * can be split further.  row_perm[num_rows] and col_perm[num_cols] (may be
+ * NULL) receive the clustered order (position -> original index); blocks
+ * (may be NULL) receives 5 ints per block, (row_begin, row_count, col_begin,
+ * col_count, admissible) in clustered positions.  The blocks tile the
+ * num_rows x num_cols index space exactly once.  *num_blocks is always set;
+ * BEM_ERR_TOO_LARGE when blocks is not NULL and max_blocks is smaller. */
+int bem_hmat_partition(const double *rows, int num_rows, const double *cols, int num_cols, int leaf,
+                       double eta, int *row_perm, int *col_perm, int *blocks, int max_blocks,
+                       int *num_blocks);
 
 /* ------------------------------------------------------------------ */
 /* Drop-in calls with host buffers (the reference's call surface)       */
