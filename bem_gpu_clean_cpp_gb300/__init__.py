@@ -141,6 +141,11 @@ SIGNATURES = {
     "bem_mesh_perturbed_ellipsoid": (_I, [_VP, _D, _D, _D, _I, _D, ctypes.c_ulonglong]),
     "bem_fibonacci_sphere": (_I, [_I, _D, _VP]),
     "bem_hmat_partition": (_I, [_VP, _I, _VP, _I, _I, _D, _VP, _VP, _VP, _I, ctypes.POINTER(_I)]),
+    "bem_hmat_compress_c64": (_I, [_VP, _I, _I, _I, _VP, _I, _D, _I, _VP, ctypes.POINTER(_VP)]),
+    "bem_hmat_matvec_c64": (_I, [_VP, _I, _VP, _VP, _VP]),
+    "bem_hmat_info": (_I, [_VP, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(_I), ctypes.POINTER(_I),
+                           ctypes.POINTER(_I)]),
+    "bem_hmat_destroy": (_I, [_VP]),
     "bem_system_c64": (_I, [_VP, _F, _VP, _I, _VP, _I, _VP, _I]),
     "bem_qr_solve_c64": (_I, [_VP, _I, _I, _I, _VP, _I, _I]),
     "bem_gmres_c64": (_I, [_VP, _VP, _I, _I, _F, _VP]),
@@ -287,6 +292,42 @@ def hmat_partition(rows, cols, leaf: int = 128, eta: float = 1.0):
     _check(L.bem_hmat_partition(_ptr(rows), R, _ptr(cols), N, int(leaf), float(eta), _ptr(row_perm),
                                 _ptr(col_perm), _ptr(blocks), n.value, ctypes.byref(n)))
     return row_perm, col_perm, blocks[:n.value]
+
+
+class HMatrix:
+    """Hierarchical form of a c64 matrix on the device (``bem_hmat_*``).
+    ``A_ptr``: device address of an R x N row-major matrix (row stride
+    ``lda``) in the clustered order of ``blocks`` (from ``hmat_partition``);
+    admissible blocks are compressed by adaptive cross approximation to
+    relative tolerance ``tol`` with at most ``kmax`` terms.  ``stream`` is a
+    cudaStream_t address (0: the legacy default stream)."""
+
+    def __init__(self, A_ptr: int, R: int, N: int, lda: int, blocks, tol: float = 1e-5, kmax: int = 64,
+                 stream: int = 0):
+        b = np.ascontiguousarray(blocks, dtype=np.int32).reshape(-1, 5)
+        h = ctypes.c_void_p()
+        _check(lib().bem_hmat_compress_c64(A_ptr, int(R), int(N), int(lda), _ptr(b), b.shape[0], float(tol),
+                                           int(kmax), stream or None, ctypes.byref(h)))
+        self._h = h
+        self.R, self.N = int(R), int(N)
+
+    def matvec(self, x_ptr: int, y_ptr: int, trans: int = 0, stream: int = 0) -> None:
+        """y = H x (trans 0) or H^H x (trans 1), device addresses, queued on stream."""
+        _check(lib().bem_hmat_matvec_c64(self._h, int(trans), x_ptr, y_ptr, stream or None))
+
+    def info(self) -> dict:
+        e = ctypes.c_longlong()
+        k, nl, nd = _I(), _I(), _I()
+        _check(lib().bem_hmat_info(self._h, ctypes.byref(e), ctypes.byref(k), ctypes.byref(nl), ctypes.byref(nd)))
+        return {"entries": e.value, "max_rank": k.value, "lowrank_blocks": nl.value, "dense_blocks": nd.value}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().bem_hmat_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
 
 
 def set_medium(density: float, speed: float) -> None:

@@ -12,7 +12,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libbem_gb300.so")
 
-SOURCES = ["kernels.cu", "linalg.cu", "block.cu", "block_simt.cu", "tc_gemm.cu", "qr_tc.cu", "chief.cu", "noalloc.cu", "mesh.cpp", "mesh_io.cpp", "generators.cpp", "hmat.cpp",
+SOURCES = ["kernels.cu", "linalg.cu", "block.cu", "block_simt.cu", "tc_gemm.cu", "qr_tc.cu", "chief.cu", "noalloc.cu", "hmat_gpu.cu", "mesh.cpp", "mesh_io.cpp", "generators.cpp", "hmat.cpp",
            "solver.cpp", "solve.cpp", "server.cpp", "capi.cpp"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -149,6 +149,28 @@ int bem_fibonacci_sphere(int n, double radius, double *pts);
 int bem_hmat_partition(const double *rows, int num_rows, const double *cols, int num_cols, int leaf,
                        double eta, int *row_perm, int *col_perm, int *blocks, int max_blocks,
                        int *num_blocks);
+/* Hierarchical form of a c64 matrix already on the device (no reference
+ * counterpart).  A_dev: R x N, row-major with row stride lda, rows and
+ * columns in the clustered order of the partition (A[row_perm][:, col_perm]);
+ * blocks: num_blocks x 5 ints from bem_hmat_partition.  Admissible blocks are
+ * compressed by partially pivoted adaptive cross approximation to relative
+ * tolerance tol (|u_k| |v_k| <= tol ||S_k||_F) with at most kmax <= 128 terms;
+ * a block whose approximation needs more terms, or as many as the dense block
+ * would hold, is stored dense, as are the inadmissible blocks.  The handle
+ * owns its device memory (A may be freed afterwards).  Work is queued on
+ * stream (a cudaStream_t, NULL for the legacy stream) and the call returns
+ * once it is complete. */
+typedef struct bem_hmat_s *bem_hmat_t;
+int bem_hmat_compress_c64(const void *A_dev, int R, int N, int lda, const int *blocks, int num_blocks,
+                          double tol, int kmax, void *stream, bem_hmat_t *out);
+/* y = H x (trans 0: x has N entries, y R) or y = H^H x (trans 1: x has R
+ * entries, y N); c64 device vectors in the clustered order, queued on stream.
+ * One product at a time per handle (it keeps one work vector).  The result is
+ * bitwise repeatable: every output entry has one writer and a fixed order. */
+int bem_hmat_matvec_c64(bem_hmat_t h, int trans, const void *x_dev, void *y_dev, void *stream);
+/* Stored complex entries, largest rank, low-rank and dense block counts. */
+int bem_hmat_info(bem_hmat_t h, long long *entries, int *max_rank, int *lowrank_blocks, int *dense_blocks);
+int bem_hmat_destroy(bem_hmat_t h);
 
 /* ------------------------------------------------------------------ */
 /* Drop-in calls with host buffers (the reference's call surface)       */
