@@ -9,13 +9,14 @@
 //   dense block   rc x cc, row-major;
 //   low-rank block of rank k: U (rc x k) then V (cc x k), both column-major,
 //   block ~= U V^T (ACA's cross approximation, no conjugation).
-// Products, two launches each:
+// Products, three launches each:
 //   project: per low-rank block t = V^T x_J (H x) or t = U^H x_I (H^H x),
 //            one warp per rank column;
 //   apply:   per output segment (the finest intervals cut by the block edges
 //            on that side) the dense and low-rank terms of every block
-//            covering it, in block order: each output entry has one writer
-//            and a fixed summation order, so the product is bitwise
+//            covering it, split over a few CTAs and their warps in a fixed
+//            assignment; combine: the CTAs' partials added in order.  No
+//            atomics and fixed summation orders: the product is bitwise
 //            repeatable.
 #include <cuda_runtime.h>
 
@@ -260,70 +261,93 @@ __global__ void __launch_bounds__(kHT) hmv_project_kernel(const HBlock *__restri
     }
 }
 
-// y over the row segments (trans 0): dense terms one warp per row (row reads
-// coalesced), low-rank terms one thread per row; the two partial sums are
-// added at the end.
-__global__ void __launch_bounds__(kHT) hmv_apply_rows_kernel(const HBlock *__restrict__ desc, const int2 *__restrict__ seg,
-                                                             const int *__restrict__ ptr, const int *__restrict__ idx,
-                                                             const float2 *__restrict__ pool, const float2 *__restrict__ x,
-                                                             const float2 *__restrict__ t, float2 *y) {
-    __shared__ float2 acc_d[kHT];
-    const int2 sg = seg[blockIdx.x];
+// One output segment, split over P CTAs: warp w of CTA p takes the
+// segment's blocks e0 + p * 8 + w, then every 8 P-th one, and accumulates
+// its terms for every output entry of the segment (lanes over the entries,
+// loads independent across the inner loop) into its own shared slice; the
+// CTA adds the eight slices in warp order and writes its partial, and
+// hmv_combine_kernel adds the P partials in order.  The assignment and every
+// order are fixed, so the product is bitwise repeatable.
+// trans 0: entries are rows, y_I += D x_J (D row-major: each lane walks its
+// row) or U (V^T x_J) (U column-major: lanes read consecutive rows).
+// trans 1: entries are columns, y_J += D^H x_I (lanes read consecutive
+// columns of each row) or conj(V) (U^H x_I).
+constexpr int kSegChunk = 128;
+
+__global__ void __launch_bounds__(kHT) hmv_apply_kernel(const HBlock *__restrict__ desc, const int2 *__restrict__ seg,
+                                                        const int *__restrict__ ptr, const int *__restrict__ idx,
+                                                        const float2 *__restrict__ pool, const float2 *__restrict__ x,
+                                                        const float2 *__restrict__ t, float2 *part, int n_out, int P,
+                                                        int trans) {
+    __shared__ float2 acc[kHW][kSegChunk];
+    const int s = blockIdx.x / P, p = blockIdx.x - s * P;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int e0 = ptr[blockIdx.x], e1 = ptr[blockIdx.x + 1];
-    for (int ch = 0; ch < sg.y; ch += kHT) {
-        const int nrow = min(kHT, sg.y - ch);
-        acc_d[tid] = make_float2(0.f, 0.f);
-        __syncthreads();
-        float2 acc_l = make_float2(0.f, 0.f);
-        for (int e = e0; e < e1; e++) {
+    const int2 sg = seg[s];
+    const int e0 = ptr[s], e1 = ptr[s + 1];
+    for (int ch = 0; ch < sg.y; ch += kSegChunk) {
+        const int nout = min(kSegChunk, sg.y - ch);
+        for (int o = lane; o < kSegChunk; o += 32) acc[warp][o] = make_float2(0.f, 0.f);
+        __syncwarp();
+        for (int e = e0 + p * kHW + warp; e < e1; e += P * kHW) {
             const HBlock b = desc[idx[e]];
-            const int rbase = sg.x + ch - b.r0;   // row of the block at the chunk's first row
-            if (b.kind == 0) {
-                const float2 *xj = x + b.c0;
-                for (int rr = warp; rr < nrow; rr += kHW) {
-                    const float2 *drow = pool + b.off + (size_t)(rbase + rr) * b.cc;
-                    float2 s = make_float2(0.f, 0.f);
-                    for (int c = lane; c < b.cc; c += 32) s = cadd(s, cmul(drow[c], xj[c]));
-                    s = warp_sum2(s);
-                    if (lane == 0) acc_d[rr] = cadd(acc_d[rr], s);
+            const float2 *D = pool + b.off;
+            if (trans == 0) {
+                const int base = sg.x + ch - b.r0;   // block row of the chunk's first row
+                if (b.kind == 0) {
+                    const float2 *xj = x + b.c0;
+                    for (int o = lane; o < nout; o += 32) {
+                        const float2 *drow = D + (size_t)(base + o) * b.cc;
+                        float2 a = make_float2(0.f, 0.f);
+#pragma unroll 4
+                        for (int c = 0; c < b.cc; c++) a = cadd(a, cmul(drow[c], xj[c]));
+                        acc[warp][o] = cadd(acc[warp][o], a);
+                    }
+                } else {
+                    const float2 *tb = t + b.t_off;
+                    for (int o = lane; o < nout; o += 32) {
+                        float2 a = make_float2(0.f, 0.f);
+#pragma unroll 4
+                        for (int q = 0; q < b.k; q++) a = cadd(a, cmul(D[(size_t)q * b.rc + base + o], tb[q]));
+                        acc[warp][o] = cadd(acc[warp][o], a);
+                    }
                 }
-            } else if (tid < nrow) {
-                const float2 *U = pool + b.off;
-                const float2 *tb = t + b.t_off;
-                const int rl = rbase + tid;
-                for (int q = 0; q < b.k; q++) acc_l = cadd(acc_l, cmul(U[(size_t)q * b.rc + rl], tb[q]));
+            } else {
+                const int base = sg.x + ch - b.c0;   // block column of the chunk's first column
+                if (b.kind == 0) {
+                    const float2 *xi = x + b.r0;
+                    for (int o = lane; o < nout; o += 32) {
+                        float2 a = make_float2(0.f, 0.f);
+#pragma unroll 4
+                        for (int r = 0; r < b.rc; r++) a = cadd(a, cmulc(D[(size_t)r * b.cc + base + o], xi[r]));
+                        acc[warp][o] = cadd(acc[warp][o], a);
+                    }
+                } else {
+                    const float2 *V = D + (size_t)b.k * b.rc;
+                    const float2 *tb = t + b.t_off;
+                    for (int o = lane; o < nout; o += 32) {
+                        float2 a = make_float2(0.f, 0.f);
+#pragma unroll 4
+                        for (int q = 0; q < b.k; q++) a = cadd(a, cmulc(V[(size_t)q * b.cc + base + o], tb[q]));
+                        acc[warp][o] = cadd(acc[warp][o], a);
+                    }
+                }
             }
         }
         __syncthreads();
-        if (tid < nrow) y[sg.x + ch + tid] = cadd(acc_d[tid], acc_l);
+        for (int o = tid; o < nout; o += kHT) {
+            float2 a = acc[0][o];
+            for (int w = 1; w < kHW; w++) a = cadd(a, acc[w][o]);
+            part[(size_t)p * n_out + sg.x + ch + o] = a;
+        }
         __syncthreads();
     }
 }
 
-// y over the column segments (trans 1): one thread per column for both kinds
-// (dense rows read across consecutive columns).
-__global__ void __launch_bounds__(kHT) hmv_apply_cols_kernel(const HBlock *__restrict__ desc, const int2 *__restrict__ seg,
-                                                             const int *__restrict__ ptr, const int *__restrict__ idx,
-                                                             const float2 *__restrict__ pool, const float2 *__restrict__ x,
-                                                             const float2 *__restrict__ t, float2 *y) {
-    const int2 sg = seg[blockIdx.x];
-    const int e0 = ptr[blockIdx.x], e1 = ptr[blockIdx.x + 1];
-    for (int col = threadIdx.x; col < sg.y; col += kHT) {
-        float2 acc = make_float2(0.f, 0.f);
-        for (int e = e0; e < e1; e++) {
-            const HBlock b = desc[idx[e]];
-            const int cl = sg.x + col - b.c0;
-            if (b.kind == 0) {
-                const float2 *D = pool + b.off, *xi = x + b.r0;
-                for (int r = 0; r < b.rc; r++) acc = cadd(acc, cmulc(D[(size_t)r * b.cc + cl], xi[r]));
-            } else {
-                const float2 *V = pool + b.off + (size_t)b.k * b.rc;
-                const float2 *tb = t + b.t_off;
-                for (int q = 0; q < b.k; q++) acc = cadd(acc, cmulc(V[(size_t)q * b.cc + cl], tb[q]));
-            }
-        }
-        y[sg.x + col] = acc;
+__global__ void hmv_combine_kernel(const float2 *__restrict__ part, int n_out, int P, float2 *y) {
+    for (int o = blockIdx.x * blockDim.x + threadIdx.x; o < n_out; o += gridDim.x * blockDim.x) {
+        float2 a = part[o];
+        for (int p = 1; p < P; p++) a = cadd(a, part[(size_t)p * n_out + o]);
+        y[o] = a;
     }
 }
 
@@ -374,7 +398,9 @@ struct bem_hmat_s {
     int R = 0, N = 0;
     bem::DevMem pool, desc, lr, t;
     bem::DevMem rseg, rptr, ridx, cseg, cptr, cidx;
+    bem::DevMem part;                       // P partial outputs of the apply kernel
     int n_lr = 0, n_rseg = 0, n_cseg = 0;
+    int p_rows = 1, p_cols = 1;             // CTAs per output segment
     long long entries = 0;
     int max_rank = 0, n_lowrank = 0, n_dense = 0;
 };
@@ -511,6 +537,11 @@ extern "C" int bem_hmat_compress_c64(const void *A_dev, int R, int N, int lda, c
     upload(h->cseg, cseg, st);
     upload(h->cptr, cptr, st);
     upload(h->cidx, cidx, st);
+    // enough CTAs per segment to give every SM four
+    const int want = 4 * device_sm_count();
+    h->p_rows = std::min(8, std::max(1, (want + h->n_rseg - 1) / h->n_rseg));
+    h->p_cols = std::min(8, std::max(1, (want + h->n_cseg - 1) / h->n_cseg));
+    h->part.ensure(sizeof(float2) * (size_t)std::max(R * h->p_rows, N * h->p_cols));
     // the host vectors and the scratch are released on return
     CUDA_TRY(cudaStreamSynchronize(st));
     *out = h.release();
@@ -531,17 +562,22 @@ extern "C" int bem_hmat_matvec_c64(bem_hmat_t h, int trans, const void *x_dev, v
         count_launch();
         KERNEL_CHECK();
     }
-    BEM_PROF("hmat_apply", st);
-    if (trans == 0)
-        hmv_apply_rows_kernel<<<h->n_rseg, kHT, 0, st>>>(h->desc.as<HBlock>(), h->rseg.as<int2>(), h->rptr.as<int>(),
-                                                         h->ridx.as<int>(), h->pool.as<float2>(), x,
-                                                         h->t.as<float2>(), y);
-    else
-        hmv_apply_cols_kernel<<<h->n_cseg, kHT, 0, st>>>(h->desc.as<HBlock>(), h->cseg.as<int2>(), h->cptr.as<int>(),
-                                                         h->cidx.as<int>(), h->pool.as<float2>(), x,
-                                                         h->t.as<float2>(), y);
-    count_launch();
-    KERNEL_CHECK();
+    {
+        BEM_PROF("hmat_apply", st);
+        const int P = trans == 0 ? h->p_rows : h->p_cols;
+        const int nseg = trans == 0 ? h->n_rseg : h->n_cseg;
+        const int n_out = trans == 0 ? h->R : h->N;
+        const DevMem &sg = trans == 0 ? h->rseg : h->cseg, &pt = trans == 0 ? h->rptr : h->cptr,
+                     &ix = trans == 0 ? h->ridx : h->cidx;
+        hmv_apply_kernel<<<nseg * P, kHT, 0, st>>>(h->desc.as<HBlock>(), sg.as<int2>(), pt.as<int>(), ix.as<int>(),
+                                                   h->pool.as<float2>(), x, h->t.as<float2>(),
+                                                   h->part.as<float2>(), n_out, P, trans);
+        count_launch();
+        KERNEL_CHECK();
+        hmv_combine_kernel<<<(n_out + kHT - 1) / kHT, kHT, 0, st>>>(h->part.as<float2>(), n_out, P, y);
+        count_launch();
+        KERNEL_CHECK();
+    }
     BEM_API_END
 }
 
