@@ -141,6 +141,7 @@ SIGNATURES = {
     "bem_mesh_perturbed_ellipsoid": (_I, [_VP, _D, _D, _D, _I, _D, ctypes.c_ulonglong]),
     "bem_fibonacci_sphere": (_I, [_I, _D, _VP]),
     "bem_hmat_partition": (_I, [_VP, _I, _VP, _I, _I, _D, _VP, _VP, _VP, _I, ctypes.POINTER(_I)]),
+    "bem_hmat_partition_system": (_I, [_VP, _I, _VP, _I, _I, _D, _VP, _VP, _VP, _I, ctypes.POINTER(_I)]),
     "bem_hmat_compress_c64": (_I, [_VP, _I, _I, _I, _VP, _I, _D, _I, _VP, ctypes.POINTER(_VP)]),
     "bem_hmat_matvec_c64": (_I, [_VP, _I, _VP, _VP, _VP]),
     "bem_hmat_info": (_I, [_VP, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(_I), ctypes.POINTER(_I),
@@ -292,6 +293,26 @@ def hmat_partition(rows, cols, leaf: int = 128, eta: float = 1.0):
     _check(L.bem_hmat_partition(_ptr(rows), R, _ptr(cols), N, int(leaf), float(eta), _ptr(row_perm),
                                 _ptr(col_perm), _ptr(blocks), n.value, ctypes.byref(n)))
     return row_perm, col_perm, blocks[:n.value]
+
+
+def hmat_partition_system(pnts, chief, leaf: int = 128, eta: float = 1.0):
+    """Partition of a collocation system (bem_hmat_partition_system): rows
+    are the nodes in the column tree's order, then the CHIEF points.  Returns
+    (node_perm, chief_perm, blocks)."""
+    pnts = np.ascontiguousarray(pnts, dtype=np.float64).reshape(-1, 3)
+    chief = np.ascontiguousarray(chief if chief is not None else np.zeros((0, 3)), dtype=np.float64).reshape(-1, 3)
+    N, M = pnts.shape[0], chief.shape[0]
+    cptr = _ptr(chief) if M else None
+    n = _I(0)
+    L = lib()
+    _check(L.bem_hmat_partition_system(_ptr(pnts), N, cptr, M, int(leaf), float(eta), None, None, None, 0,
+                                       ctypes.byref(n)))
+    node_perm = np.zeros(N, dtype=np.int32)
+    chief_perm = np.zeros(M, dtype=np.int32)
+    blocks = np.zeros((max(n.value, 1), 5), dtype=np.int32)
+    _check(L.bem_hmat_partition_system(_ptr(pnts), N, cptr, M, int(leaf), float(eta), _ptr(node_perm),
+                                       _ptr(chief_perm) if M else None, _ptr(blocks), n.value, ctypes.byref(n)))
+    return node_perm, chief_perm, blocks[:n.value]
 
 
 class HMatrix:

@@ -120,6 +120,39 @@ void build_blocks(const ClusterTree &rt, int i, const ClusterTree &ct, int j, do
     }
 }
 
+// Row tree of a collocation system: a root over the nodes' tree (the column
+// tree itself, so row position p < N is column position p) and the CHIEF
+// points' tree, whose positions follow at N.
+void system_row_tree(const ClusterTree &nodes, const ClusterTree &chief, int N, ClusterTree &rt) {
+    rt.p = nullptr;
+    rt.perm = nodes.perm;
+    for (int i : chief.perm) rt.perm.push_back(N + i);
+    rt.nodes.clear();
+    Cluster root = nodes.nodes[0];
+    const Cluster &cr = chief.nodes[0];
+    for (int d = 0; d < 3; d++) {
+        root.lo[d] = std::min(root.lo[d], cr.lo[d]);
+        root.hi[d] = std::max(root.hi[d], cr.hi[d]);
+    }
+    const int off_n = 1, off_c = 1 + (int)nodes.nodes.size();
+    root.begin = 0;
+    root.count = N + cr.count;
+    root.child[0] = off_n;
+    root.child[1] = off_c;
+    rt.nodes.push_back(root);
+    for (Cluster c : nodes.nodes) {
+        for (int &ch : c.child)
+            if (ch >= 0) ch += off_n;
+        rt.nodes.push_back(c);
+    }
+    for (Cluster c : chief.nodes) {
+        c.begin += N;
+        for (int &ch : c.child)
+            if (ch >= 0) ch += off_c;
+        rt.nodes.push_back(c);
+    }
+}
+
 }  // namespace
 }  // namespace bem
 
@@ -141,6 +174,40 @@ extern "C" int bem_hmat_partition(const double *rows, int num_rows, const double
     *num_blocks = (int)out.size();
     if (row_perm) std::copy(rt.perm.begin(), rt.perm.end(), row_perm);
     if (col_perm) std::copy(ct.perm.begin(), ct.perm.end(), col_perm);
+    if (blocks) {
+        if (max_blocks < (int)out.size())
+            BEM_FAIL(BEM_ERR_TOO_LARGE, "block array holds fewer entries than the partition has blocks");
+        for (size_t q = 0; q < out.size(); q++)
+            std::copy(out[q].begin(), out[q].end(), blocks + 5 * q);
+    }
+    BEM_API_END
+}
+
+extern "C" int bem_hmat_partition_system(const double *pnts, int num_pnts, const double *chief, int num_chief,
+                                         int leaf, double eta, int *node_perm, int *chief_perm, int *blocks,
+                                         int max_blocks, int *num_blocks) {
+    BEM_API_BEGIN
+    BEM_CHECK_ARG(pnts && num_blocks && (chief || num_chief == 0), "null argument");
+    BEM_CHECK_ARG(num_pnts > 0 && num_chief >= 0, "empty point set");
+    BEM_CHECK_ARG(leaf >= 1, "leaf size must be at least 1");
+    BEM_CHECK_ARG(std::isfinite(eta) && eta > 0.0, "eta must be positive and finite");
+    for (long long q = 0; q < 3LL * num_pnts; q++) BEM_CHECK_ARG(std::isfinite(pnts[q]), "node not finite");
+    for (long long q = 0; q < 3LL * num_chief; q++) BEM_CHECK_ARG(std::isfinite(chief[q]), "CHIEF point not finite");
+    bem::ClusterTree ct, cht, rt;
+    bem::build_tree(ct, pnts, num_pnts, leaf);
+    std::vector<std::array<int, 5>> out;
+    if (num_chief > 0) {
+        bem::build_tree(cht, chief, num_chief, leaf);
+        bem::system_row_tree(ct, cht, num_pnts, rt);
+        // node rows against the node tree level by level, then the CHIEF rows
+        bem::build_blocks(rt, rt.nodes[0].child[0], ct, 0, eta, out);
+        bem::build_blocks(rt, rt.nodes[0].child[1], ct, 0, eta, out);
+    } else {
+        bem::build_blocks(ct, 0, ct, 0, eta, out);
+    }
+    *num_blocks = (int)out.size();
+    if (node_perm) std::copy(ct.perm.begin(), ct.perm.end(), node_perm);
+    if (chief_perm && num_chief > 0) std::copy(cht.perm.begin(), cht.perm.end(), chief_perm);
     if (blocks) {
         if (max_blocks < (int)out.size())
             BEM_FAIL(BEM_ERR_TOO_LARGE, "block array holds fewer entries than the partition has blocks");

@@ -149,6 +149,18 @@ int bem_fibonacci_sphere(int n, double radius, double *pts);
 int bem_hmat_partition(const double *rows, int num_rows, const double *cols, int num_cols, int leaf,
                        double eta, int *row_perm, int *col_perm, int *blocks, int max_blocks,
                        int *num_blocks);
+/* The same partition for a collocation system whose rows are the nodes and
+ * then the CHIEF points (no reference counterpart).  The node rows use the
+ * column tree itself: row position p < num_pnts and column position p are the
+ * same node, node_perm[p] (num_pnts entries); row position num_pnts + p is
+ * CHIEF point chief_perm[p] (num_chief entries, its own cluster tree).
+ * Renumbering the mesh nodes by node_perm and the CHIEF points by chief_perm
+ * before assembly therefore gives A directly in the clustered order.  No
+ * block mixes node rows and CHIEF rows.  Other arguments and results as for
+ * bem_hmat_partition. */
+int bem_hmat_partition_system(const double *pnts, int num_pnts, const double *chief, int num_chief, int leaf,
+                              double eta, int *node_perm, int *chief_perm, int *blocks, int max_blocks,
+                              int *num_blocks);
 /* Hierarchical form of a c64 matrix already on the device (no reference
  * counterpart).  A_dev: R x N, row-major with row stride lda, rows and
  * columns in the clustered order of the partition (A[row_perm][:, col_perm]);

@@ -128,3 +128,37 @@ def test_admissible_blocks_are_low_rank_in_oracle_matrix(bemlib, orc):
         assert (s > floor).sum() < 0.3 * min(rc, cc)
         checked += 1
     assert checked >= 100
+
+
+def test_system_partition_shares_the_node_tree(bemlib):
+    """Rows = nodes in the column tree's order, then the CHIEF points: the
+    blocks tile (N + M) x N once, no block mixes node and CHIEF rows, every
+    node-row range is a column cluster, and the admissible blocks meet the
+    criterion with the renumbered points."""
+    _, nodes, _ = _rows_cols(4)
+    chief = np.random.default_rng(1).uniform(-0.3, 0.3, (8, 3))
+    N, M = nodes.shape[0], chief.shape[0]
+    node_perm, chief_perm, b = bemlib.hmat_partition_system(nodes, chief, 64, 1.0)
+    assert np.array_equal(np.sort(node_perm), np.arange(N))
+    assert np.array_equal(np.sort(chief_perm), np.arange(M))
+    cover = np.zeros((N + M, N), dtype=np.int32)
+    for r0, rc, c0, cc, _ in b:
+        cover[r0:r0 + rc, c0:c0 + cc] += 1
+        assert r0 + rc <= N or r0 >= N
+    assert (cover == 1).all()
+    col_ranges = {(c0, cc) for _, _, c0, cc, _ in b}
+    assert {(r0, rc) for r0, rc, _, _, _ in b if r0 < N} <= col_ranges
+    # the node tree is the plain partition's column tree
+    _, cp, _ = bemlib.hmat_partition(np.vstack([nodes, chief]), nodes, 64, 1.0)
+    assert np.array_equal(node_perm, cp)
+    xr = np.vstack([nodes[node_perm], chief[chief_perm]])
+    xc = nodes[node_perm]
+    for r0, rc, c0, cc, adm in b:
+        if adm:
+            br, bc = _box(xr[r0:r0 + rc]), _box(xc[c0:c0 + cc])
+            d = _dist(br, bc)
+            assert d > 0.0 and min(_diam(*br), _diam(*bc)) <= d * (1 + 1e-12)
+    # without CHIEF points the rows are the nodes alone
+    p2, c2, b2 = bemlib.hmat_partition_system(nodes, None, 64, 1.0)
+    assert np.array_equal(p2, node_perm) and c2.size == 0
+    assert (b2[:, 0] + b2[:, 1]).max() == N
