@@ -348,7 +348,10 @@ class HMatrix:
             self._h = None
 
     def __del__(self):
-        self.close()
+        try:
+            self.close()
+        except Exception:   # interpreter shutdown: the library may already be gone
+            pass
 
 
 def set_medium(density: float, speed: float) -> None:
